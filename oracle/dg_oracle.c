@@ -1,0 +1,734 @@
+/*
+ * dg_oracle — CPU restatement of the reference (Dendro4) octree hot path.
+ * TEST INFRASTRUCTURE ONLY (see dg_oracle.h): the checker for the CUDA
+ * library, never part of it.
+ *
+ * Reference files cited are paths inside the Dendro4 source tree.
+ */
+#include "dg_oracle.h"
+
+#include <stdlib.h>
+#include <string.h>
+
+typedef unsigned __int128 u128;
+
+void dgo_free(void *p) { free(p); }
+
+/* ------------------------------------------------------------------------ */
+/* Morton order (include/TreeNode.tcc:211-236): interleave the anchor bits,  */
+/* z above y above x within every bit position; equal anchors: lower level   */
+/* (the ancestor) first (TreeNode.tcc:131-133).                              */
+/* ------------------------------------------------------------------------ */
+static u128 spread3(uint32_t v) {
+  u128 r = 0;
+  for (int b = 0; b < 32; b++)
+    if (v >> b & 1u) r |= (u128)1 << (3 * b);
+  return r;
+}
+
+static u128 morton(uint32_t x, uint32_t y, uint32_t z) {
+  return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
+}
+
+/* total order key: anchor Morton (96 bits) then level (5 bits) */
+static u128 okey(const dgo_oct *o) { return (morton(o->x, o->y, o->z) << 5) | (u128)(o->lev & 31u); }
+
+static int oct_lt(const dgo_oct *a, const dgo_oct *b) { return okey(a) < okey(b); }
+static int oct_eq(const dgo_oct *a, const dgo_oct *b) {
+  return a->x == b->x && a->y == b->y && a->z == b->z && a->lev == b->lev;
+}
+static int oct_le(const dgo_oct *a, const dgo_oct *b) { return okey(a) <= okey(b); }
+
+typedef struct {
+  u128 k;
+  dgo_oct o;
+} keyed_oct;
+
+static int cmp_keyed(const void *pa, const void *pb) {
+  const keyed_oct *a = (const keyed_oct *)pa, *b = (const keyed_oct *)pb;
+  return (a->k > b->k) - (a->k < b->k);
+}
+
+static int cmp_u128(const void *pa, const void *pb) {
+  u128 a = *(const u128 *)pa, b = *(const u128 *)pb;
+  return (a > b) - (a < b);
+}
+
+/* sort octants in Morton order (stable w.r.t. equal records is irrelevant:
+ * equal keys mean equal {x,y,z,lev}) */
+static int sort_octs(dgo_oct *a, size_t n) {
+  if (n < 2) return 0;
+  keyed_oct *t = (keyed_oct *)malloc(n * sizeof(keyed_oct));
+  if (!t) return DGO_ENOMEM;
+  for (size_t i = 0; i < n; i++) {
+    t[i].k = okey(&a[i]);
+    t[i].o = a[i];
+  }
+  qsort(t, n, sizeof(keyed_oct), cmp_keyed);
+  for (size_t i = 0; i < n; i++) a[i] = t[i].o;
+  free(t);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* TreeNode operations used by the walk (Morton build)                       */
+/* ------------------------------------------------------------------------ */
+static inline uint64_t oct_len(const dgo_oct *o, unsigned D) { return (uint64_t)1 << (D - o->lev); }
+
+/* isAncestor: strictly coarser and containing (TreeNode.tcc:590-609) */
+static int is_anc(const dgo_oct *a, const dgo_oct *b, unsigned D) {
+  if (!(a->lev < b->lev)) return 0;
+  uint64_t la = oct_len(a, D), lb = oct_len(b, D);
+  return b->x >= a->x && b->y >= a->y && b->z >= a->z && (uint64_t)b->x + lb <= (uint64_t)a->x + la &&
+         (uint64_t)b->y + lb <= (uint64_t)a->y + la && (uint64_t)b->z + lb <= (uint64_t)a->z + la;
+}
+
+/* getFirstChild, Morton: same anchor, one level finer (TreeNode.tcc:578-582) */
+static dgo_oct first_child(dgo_oct a) {
+  a.lev++;
+  return a;
+}
+
+/* getNext, Morton (TreeNode.tcc:533-549): the octant that follows a in SFC
+ * order, climbing while a is a last child. */
+static dgo_oct get_next(dgo_oct m, unsigned D) {
+  uint32_t mask = 1u << (D - m.lev);
+  int i;
+  for (i = (int)m.lev; i >= 0; --i) {
+    m.x ^= mask;
+    if (m.x & mask) break;
+    m.y ^= mask;
+    if (m.y & mask) break;
+    m.z ^= mask;
+    if (m.z & mask) break;
+    mask <<= 1;
+  }
+  m.lev = (uint32_t)i;
+  return m;
+}
+
+/* getDLD, Morton (TreeNode.tcc:453-455): deepest last descendant */
+static dgo_oct get_dld(const dgo_oct *a, unsigned D) {
+  uint32_t l = (uint32_t)oct_len(a, D);
+  dgo_oct r = {a->x + l - 1, a->y + l - 1, a->z + l - 1, D};
+  return r;
+}
+
+/* ------------------------------------------------------------------------ */
+/* points2Octree                                                             */
+/* ------------------------------------------------------------------------ */
+int dgo_quantize_sort(const double *xyz, size_t n, const double gLens[3], unsigned D, dgo_oct **out) {
+  if (D > 30 || (!xyz && n)) return DGO_EINVAL;
+  dgo_oct *p = (dgo_oct *)malloc((n ? n : 1) * sizeof(dgo_oct));
+  if (!p) return DGO_ENOMEM;
+  const double scale = (double)(1u << D);
+  for (size_t i = 0; i < n; i++) {
+    /* construct.cpp:935-941: (unsigned int)(pts * (double)(1u<<maxDepth) / gLens) */
+    p[i].x = (uint32_t)(xyz[3 * i] * scale / gLens[0]);
+    p[i].y = (uint32_t)(xyz[3 * i + 1] * scale / gLens[1]);
+    p[i].z = (uint32_t)(xyz[3 * i + 2] * scale / gLens[2]);
+    p[i].lev = D;
+  }
+  int rc = sort_octs(p, n);
+  if (rc) {
+    free(p);
+    return rc;
+  }
+  *out = p;
+  return 0;
+}
+
+typedef struct {
+  dgo_oct *a;
+  size_t n, cap;
+} oct_vec;
+
+static int ov_push(oct_vec *v, dgo_oct o) {
+  if (v->n == v->cap) {
+    size_t nc = v->cap ? 2 * v->cap : 1024;
+    dgo_oct *na = (dgo_oct *)realloc(v->a, nc * sizeof(dgo_oct));
+    if (!na) return DGO_ENOMEM;
+    v->a = na;
+    v->cap = nc;
+  }
+  v->a[v->n++] = o;
+  return 0;
+}
+
+/* std::lower_bound(first, last, value, std::less_equal<TreeNode>()):
+ * the first element e in [first,last) with !(e <= value). */
+static size_t lower_bound_le(const dgo_oct *a, size_t first, size_t last, const dgo_oct *value) {
+  size_t lo = first, hi = last;
+  while (lo < hi) {
+    size_t mid = lo + (hi - lo) / 2;
+    if (oct_le(&a[mid], value))
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+/* p2oLocal (src/construct.cpp:976-1076) from leaves = {root}.  The index
+ * arithmetic keeps the reference's unsigned 32-bit semantics for the point
+ * counters (next_pt, inc). */
+int dgo_p2o_local(const dgo_oct *pts, size_t n, unsigned D, unsigned m, dgo_oct **out, size_t *nout) {
+  if (m == 0 || D > 30 || n >= 0x7fffffffu) return DGO_EINVAL;
+  oct_vec lst = {0, 0, 0};
+  const uint32_t num_pts = (uint32_t)n;
+  dgo_oct root = {0, 0, 0, 0};
+  dgo_oct curr = root;
+  dgo_oct last = get_dld(&root, D);
+  dgo_oct next = get_next(curr, D);
+  uint32_t curr_pt = 0;
+  uint32_t next_pt = curr_pt + m;
+  int rc = 0;
+
+  while (next_pt < num_pts) { /* :1009 */
+    while (is_anc(&curr, &pts[next_pt - 1], D) & is_anc(&curr, &pts[next_pt], D) & (curr.lev < D)) {
+      curr = first_child(curr); /* :1013-1018 */
+      next = get_next(curr, D);
+    }
+    uint32_t inc = m; /* :1021-1031, curr can not be refined past maxDepth */
+    while (curr.lev == D - 1) {
+      inc = inc << 1;
+      next_pt += inc;
+      if (next_pt > num_pts) {
+        next_pt = num_pts - 1;
+        break;
+      }
+    }
+    /* :1037 found_pt = lower_bound(&nodes[curr_pt], &nodes[next_pt], next, less_equal) */
+    int found_pt = (int)(lower_bound_le(pts, curr_pt, next_pt, &next) - curr_pt);
+    next_pt = curr_pt + (uint32_t)found_pt;
+    if ((rc = ov_push(&lst, curr))) goto fail;
+    curr = next;
+    next = get_next(curr, D);
+    if (next_pt > curr_pt) curr_pt = next_pt;
+    next_pt = curr_pt + m;
+  }
+
+  while (oct_le(&curr, &last)) { /* :1051-1061 */
+    for (;;) {
+      dgo_oct dld = get_dld(&curr, D);
+      if (!(oct_lt(&last, &dld) && curr.lev < D)) break;
+      curr = first_child(curr);
+    }
+    if ((rc = ov_push(&lst, curr))) goto fail;
+    dgo_oct dld = get_dld(&curr, D);
+    if (oct_eq(&dld, &last)) break;
+    curr = get_next(curr, D);
+  }
+
+  /* :1063 std::list::unique (consecutive duplicates) */
+  size_t w = 0;
+  for (size_t i = 0; i < lst.n; i++)
+    if (w == 0 || !oct_eq(&lst.a[w - 1], &lst.a[i])) lst.a[w++] = lst.a[i];
+  *out = lst.a ? lst.a : (dgo_oct *)malloc(sizeof(dgo_oct));
+  *nout = w;
+  return 0;
+fail:
+  free(lst.a);
+  return rc;
+}
+
+int dgo_points_to_octree(const double *xyz, size_t n, const double gLens[3], unsigned D, unsigned m, dgo_oct **out,
+                         size_t *nout) {
+  if (m == 0 || D > 30) return DGO_EINVAL;
+  if (D == 0 || n <= m) { /* construct.cpp:916-920, 948-952 */
+    dgo_oct *r = (dgo_oct *)malloc(sizeof(dgo_oct));
+    if (!r) return DGO_ENOMEM;
+    r->x = r->y = r->z = r->lev = 0;
+    *out = r;
+    *nout = 1;
+    return 0;
+  }
+  dgo_oct *p = NULL;
+  int rc = dgo_quantize_sort(xyz, n, gLens, D, &p);
+  if (rc) return rc;
+  rc = dgo_p2o_local(p, n, D, m, out, nout);
+  free(p);
+  return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* balance: closure of the internal-node sets, finest level first.           */
+/*   I_l   = internal nodes at level l                                       */
+/*   I_l-1 = parents of the input leaves at level l, plus, for every q in    */
+/*           I_l, the level-(l-1) parents of q's 26 same-level neighbours    */
+/*           (these are the 8 parents of q's 3x3x3 block, inside the domain) */
+/*   leaves at level l = children(I_l-1) \ I_l                               */
+/* ------------------------------------------------------------------------ */
+static u128 lvl_index(uint32_t x, uint32_t y, uint32_t z, unsigned lev, unsigned D) {
+  unsigned s = D - lev;
+  return morton(x >> s, y >> s, z >> s);
+}
+
+static int cmp_u128_unique(u128 *a, size_t *n) {
+  if (*n > 1) qsort(a, *n, sizeof(u128), cmp_u128);
+  size_t w = 0;
+  for (size_t i = 0; i < *n; i++)
+    if (w == 0 || a[w - 1] != a[i]) a[w++] = a[i];
+  *n = w;
+  return 0;
+}
+
+static void level_index_decode(u128 k, uint32_t *x, uint32_t *y, uint32_t *z) {
+  uint32_t a = 0, b = 0, c = 0;
+  for (int bit = 0; bit < 32; bit++) {
+    a |= (uint32_t)((k >> (3 * bit)) & 1) << bit;
+    b |= (uint32_t)((k >> (3 * bit + 1)) & 1) << bit;
+    c |= (uint32_t)((k >> (3 * bit + 2)) & 1) << bit;
+  }
+  *x = a;
+  *y = b;
+  *z = c;
+}
+
+static int u128_contains(const u128 *a, size_t n, u128 v) {
+  size_t lo = 0, hi = n;
+  while (lo < hi) {
+    size_t mid = lo + (hi - lo) / 2;
+    if (a[mid] < v)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo < n && a[lo] == v;
+}
+
+int dgo_balance(const dgo_oct *in, size_t n, unsigned D, dgo_oct **out, size_t *nout) {
+  if (D > 30 || n == 0) return DGO_EINVAL;
+  if (n == 1) {
+    dgo_oct *r = (dgo_oct *)malloc(sizeof(dgo_oct));
+    if (!r) return DGO_ENOMEM;
+    *r = in[0];
+    *out = r;
+    *nout = 1;
+    return 0;
+  }
+  unsigned maxL = 0;
+  for (size_t i = 0; i < n; i++)
+    if (in[i].lev > maxL) maxL = in[i].lev;
+  /* I[l]: sorted unique level-l Morton indices of internal nodes */
+  u128 *I[32] = {0};
+  size_t nI[32] = {0};
+  int rc = 0;
+  const uint64_t dom = (uint64_t)1 << D;
+  for (int l = (int)maxL; l >= 1; l--) {
+    size_t cnt = 0;
+    for (size_t i = 0; i < n; i++) cnt += (in[i].lev == (unsigned)l);
+    size_t cap = cnt + 8 * nI[l] + 1;
+    u128 *cand = (u128 *)malloc(cap * sizeof(u128));
+    if (!cand) {
+      rc = DGO_ENOMEM;
+      goto done;
+    }
+    size_t nc = 0;
+    for (size_t i = 0; i < n; i++)
+      if (in[i].lev == (unsigned)l) cand[nc++] = lvl_index(in[i].x, in[i].y, in[i].z, l - 1, D);
+    const uint64_t s = (uint64_t)1 << (D - l); /* side at level l */
+    for (size_t i = 0; i < nI[l]; i++) {
+      uint32_t qx, qy, qz;
+      level_index_decode(I[l][i], &qx, &qy, &qz); /* level-l coordinates */
+      uint64_t q[3] = {(uint64_t)qx * s, (uint64_t)qy * s, (uint64_t)qz * s};
+      int64_t opt[3][2];
+      for (int a = 0; a < 3; a++) {
+        uint64_t par = q[a] & ~(2 * s - 1);
+        opt[a][0] = (int64_t)par;
+        opt[a][1] = (q[a] & s) ? (int64_t)(par + 2 * s) : (int64_t)par - (int64_t)(2 * s);
+      }
+      for (int c = 0; c < 8; c++) {
+        int64_t p0 = opt[0][c & 1], p1 = opt[1][(c >> 1) & 1], p2 = opt[2][(c >> 2) & 1];
+        if (p0 < 0 || p1 < 0 || p2 < 0 || p0 >= (int64_t)dom || p1 >= (int64_t)dom || p2 >= (int64_t)dom) continue;
+        cand[nc++] = lvl_index((uint32_t)p0, (uint32_t)p1, (uint32_t)p2, l - 1, D);
+      }
+    }
+    cmp_u128_unique(cand, &nc);
+    I[l - 1] = cand;
+    nI[l - 1] = nc;
+  }
+  {
+    size_t total = 0;
+    for (unsigned l = 0; l < maxL; l++) total += 8 * nI[l];
+    dgo_oct *res = (dgo_oct *)malloc((total ? total : 1) * sizeof(dgo_oct));
+    if (!res) {
+      rc = DGO_ENOMEM;
+      goto done;
+    }
+    size_t w = 0;
+    for (unsigned l = 1; l <= maxL; l++) {
+      const uint64_t s = (uint64_t)1 << (D - l);
+      for (size_t i = 0; i < nI[l - 1]; i++) {
+        for (int c = 0; c < 8; c++) {
+          u128 ch = (I[l - 1][i] << 3) | (u128)c;
+          if (u128_contains(I[l], nI[l], ch)) continue;
+          uint32_t cx, cy, cz;
+          level_index_decode(ch, &cx, &cy, &cz);
+          dgo_oct o = {(uint32_t)(cx * s), (uint32_t)(cy * s), (uint32_t)(cz * s), l};
+          res[w++] = o;
+        }
+      }
+    }
+    rc = sort_octs(res, w);
+    if (rc) {
+      free(res);
+      goto done;
+    }
+    *out = res;
+    *nout = w;
+  }
+done:
+  for (int l = 0; l < 32; l++) free(I[l]);
+  return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* checkers                                                                  */
+/* ------------------------------------------------------------------------ */
+int dgo_is_sorted_unique(const dgo_oct *a, size_t n, unsigned D) {
+  (void)D;
+  for (size_t i = 1; i < n; i++)
+    if (!(okey(&a[i - 1]) < okey(&a[i]))) return 0;
+  return 1;
+}
+
+int dgo_is_linear(const dgo_oct *a, size_t n, unsigned D) {
+  for (size_t i = 1; i < n; i++)
+    if (is_anc(&a[i - 1], &a[i], D)) return 0;
+  return 1;
+}
+
+/* complete + linear + sorted: consecutive leaves abut in Morton index space
+ * and the leaves tile the root */
+int dgo_is_complete(const dgo_oct *a, size_t n, unsigned D) {
+  if (n == 0) return 0;
+  u128 pos = 0;
+  for (size_t i = 0; i < n; i++) {
+    if (morton(a[i].x, a[i].y, a[i].z) != pos) return 0;
+    pos += (u128)1 << (3 * (D - a[i].lev));
+  }
+  return pos == ((u128)1 << (3 * D));
+}
+
+/* index of the leaf containing the level-D cell at (x,y,z); n if none */
+static size_t find_leaf(const u128 *keys, size_t n, uint32_t x, uint32_t y, uint32_t z) {
+  u128 k = morton(x, y, z);
+  size_t lo = 0, hi = n;
+  while (lo < hi) { /* first key > k */
+    size_t mid = lo + (hi - lo) / 2;
+    if (keys[mid] <= k)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo == 0 ? n : lo - 1;
+}
+
+int dgo_is_balanced(const dgo_oct *a, size_t n, unsigned D) {
+  u128 *keys = (u128 *)malloc((n ? n : 1) * sizeof(u128));
+  if (!keys) return 0;
+  for (size_t i = 0; i < n; i++) keys[i] = morton(a[i].x, a[i].y, a[i].z);
+  const int64_t dom = (int64_t)1 << D;
+  int ok = 1;
+  for (size_t i = 0; i < n && ok; i++) {
+    int64_t s = (int64_t)1 << (D - a[i].lev);
+    for (int dz = -1; dz <= 1 && ok; dz++)
+      for (int dy = -1; dy <= 1 && ok; dy++)
+        for (int dx = -1; dx <= 1 && ok; dx++) {
+          if (!dx && !dy && !dz) continue;
+          int64_t nx = a[i].x + dx * s, ny = a[i].y + dy * s, nz = a[i].z + dz * s;
+          if (nx < 0 || ny < 0 || nz < 0 || nx >= dom || ny >= dom || nz >= dom) continue;
+          size_t j = find_leaf(keys, n, (uint32_t)nx, (uint32_t)ny, (uint32_t)nz);
+          if (j == n || a[j].lev + 1 < a[i].lev) ok = 0;
+        }
+  }
+  free(keys);
+  return ok;
+}
+
+uint64_t dgo_fnv1a(const dgo_oct *a, size_t n) {
+  uint64_t h = 1469598103934665603ull;
+  const unsigned char *p = (const unsigned char *)a;
+  for (size_t i = 0; i < n * sizeof(dgo_oct); i++) {
+    h ^= p[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+/* ------------------------------------------------------------------------ */
+/* element types and stencils                                                */
+/* ------------------------------------------------------------------------ */
+/* The 18 hanging configurations of a child, as sets of vertices relative to
+ * the child's own corner (vertex c XOR r), in the reference's type order
+ * (include/oda/odaUtils.tcc:14-120, names of include/oda/cnumEtypes.h):
+ * r = 1,2,4 are the three edge midpoints, 3,5,6 the three face centres. */
+static const uint8_t k_canon_rel[18] = {
+    0x00,                        /* N */
+    1u << 2, 1u << 1,            /* Y, X */
+    (1u << 1) | (1u << 2),       /* XY */
+    1u << 4,                     /* Z */
+    (1u << 2) | (1u << 4),       /* ZY */
+    (1u << 1) | (1u << 4),       /* ZX */
+    (1u << 1) | (1u << 2) | (1u << 4),                       /* ZXY */
+    (1u << 1) | (1u << 2) | (1u << 3),                       /* XY_XY */
+    (1u << 1) | (1u << 2) | (1u << 3) | (1u << 4),           /* XY_ZXY */
+    (1u << 2) | (1u << 4) | (1u << 6),                       /* YZ_ZY */
+    (1u << 1) | (1u << 2) | (1u << 4) | (1u << 6),           /* YZ_ZXY */
+    (1u << 1) | (1u << 2) | (1u << 3) | (1u << 4) | (1u << 6), /* YZ_XY_ZXY */
+    (1u << 1) | (1u << 4) | (1u << 5),                       /* ZX_ZX */
+    (1u << 1) | (1u << 2) | (1u << 4) | (1u << 5),           /* ZX_ZXY */
+    (1u << 1) | (1u << 2) | (1u << 3) | (1u << 4) | (1u << 5), /* ZX_XY_ZXY */
+    (1u << 1) | (1u << 2) | (1u << 4) | (1u << 5) | (1u << 6), /* ZX_YZ_ZXY */
+    0x7e                                                     /* ZX_YZ_XY_ZXY */
+};
+/* Per child number, the axis bit that the canonical X, Y and Z axes of the
+ * configuration names map to (each child's table is the canonical one with
+ * its axes permuted). */
+static const uint8_t k_axis_perm[8][3] = {{1, 2, 4}, {2, 1, 4}, {2, 1, 4}, {1, 2, 4},
+                                          {1, 4, 2}, {2, 4, 1}, {2, 4, 1}, {1, 4, 2}};
+
+void dgo_etype_masks(uint8_t masks[8 * 18]) {
+  for (int c = 0; c < 8; c++)
+    for (int t = 0; t < 18; t++) {
+      uint8_t m = 0;
+      for (int r = 0; r < 8; r++) {
+        if (!(k_canon_rel[t] >> r & 1)) continue;
+        int pr = ((r & 1) ? k_axis_perm[c][0] : 0) | ((r & 2) ? k_axis_perm[c][1] : 0) |
+                 ((r & 4) ? k_axis_perm[c][2] : 0);
+        m |= (uint8_t)(1u << (pr ^ c));
+      }
+      masks[c * 18 + t] = m;
+    }
+}
+
+/* trilinear element matrices on [-1,1]^3, vertex k = (k&1, k>>1&1, k>>2&1) */
+static void element_matrices(double K[8][8], double Ms[8][8]) {
+  const double m1[2][2] = {{2.0 / 3.0, 1.0 / 3.0}, {1.0 / 3.0, 2.0 / 3.0}};
+  const double a1[2][2] = {{0.5, -0.5}, {-0.5, 0.5}};
+  for (int i = 0; i < 8; i++)
+    for (int j = 0; j < 8; j++) {
+      int ix = i & 1, iy = i >> 1 & 1, iz = i >> 2 & 1;
+      int jx = j & 1, jy = j >> 1 & 1, jz = j >> 2 & 1;
+      K[i][j] = a1[ix][jx] * m1[iy][jy] * m1[iz][jz] + m1[ix][jx] * a1[iy][jy] * m1[iz][jz] +
+                m1[ix][jx] * m1[iy][jy] * a1[iz][jz];
+      Ms[i][j] = m1[ix][jx] * m1[iy][jy] * m1[iz][jz];
+    }
+}
+
+/* interpolation: child vertex values from the 8 referenced values */
+static void hanging_interp(int c, uint8_t mask, double P[8][8]) {
+  memset(P, 0, 64 * sizeof(double));
+  for (int k = 0; k < 8; k++) {
+    if (!(mask >> k & 1)) {
+      P[k][k] = 1.0;
+      continue;
+    }
+    int d = k ^ c, cnt = 0;
+    for (int s = 0; s < 8; s++)
+      if ((s & d) == s) cnt++;
+    for (int s = 0; s < 8; s++)
+      if ((s & d) == s) P[k][c ^ s] += 1.0 / cnt;
+  }
+}
+
+void dgo_stencils(double *lap, double *mass) {
+  double K[8][8], Ms[8][8], P[8][8];
+  uint8_t masks[8 * 18];
+  element_matrices(K, Ms);
+  dgo_etype_masks(masks);
+  for (int c = 0; c < 8; c++)
+    for (int t = 0; t < 18; t++) {
+      hanging_interp(c, masks[c * 18 + t], P);
+      for (int i = 0; i < 8; i++)
+        for (int j = 0; j < 8; j++) {
+          double sl = 0.0, sm = 0.0;
+          for (int a = 0; a < 8; a++)
+            for (int b = 0; b < 8; b++) {
+              double w = P[a][i] * P[b][j];
+              if (w != 0.0) {
+                sl += w * K[a][b];
+                sm += w * Ms[a][b];
+              }
+            }
+          size_t o = (((size_t)c * 18 + t) * 8 + i) * 8 + j;
+          if (lap) lap[o] = sl;
+          if (mass) mass[o] = sm;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* DA                                                                        */
+/* ------------------------------------------------------------------------ */
+void dgo_da_free(dgo_da *da) {
+  free(da->child);
+  free(da->hmask);
+  free(da->etype);
+  free(da->level);
+  free(da->nodes);
+  free(da->node_xyz);
+  memset(da, 0, sizeof(*da));
+}
+
+/* is the octant (x,y,z,lev) a leaf of the sorted linear octree? */
+static int is_leaf_at(const dgo_oct *a, const u128 *keys, size_t n, int64_t x, int64_t y, int64_t z, unsigned lev,
+                      unsigned D) {
+  const int64_t dom = (int64_t)1 << D;
+  if (x < 0 || y < 0 || z < 0 || x >= dom || y >= dom || z >= dom) return 0;
+  size_t j = find_leaf(keys, n, (uint32_t)x, (uint32_t)y, (uint32_t)z);
+  return j < n && a[j].lev == lev && a[j].x == (uint32_t)x && a[j].y == (uint32_t)y && a[j].z == (uint32_t)z;
+}
+
+static size_t find_node(const u128 *nk, size_t nn, u128 k) {
+  size_t lo = 0, hi = nn;
+  while (lo < hi) {
+    size_t mid = lo + (hi - lo) / 2;
+    if (nk[mid] < k)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return (lo < nn && nk[lo] == k) ? lo : (size_t)-1;
+}
+
+int dgo_da_build(const dgo_oct *a, size_t n, unsigned D, dgo_da *da) {
+  memset(da, 0, sizeof(*da));
+  if (n == 0 || D > 30) return DGO_EINVAL;
+  int rc = 0;
+  uint8_t emask[8 * 18], tmap[8][256];
+  dgo_etype_masks(emask);
+  memset(tmap, 0xff, sizeof(tmap));
+  for (int c = 0; c < 8; c++)
+    for (int t = 0; t < 18; t++) tmap[c][emask[c * 18 + t]] = (uint8_t)t;
+
+  u128 *keys = (u128 *)malloc(n * sizeof(u128));
+  da->child = (uint8_t *)malloc(n);
+  da->hmask = (uint8_t *)malloc(n);
+  da->etype = (uint8_t *)malloc(n);
+  da->level = (uint8_t *)malloc(n);
+  da->nodes = (uint32_t *)malloc(8 * n * sizeof(uint32_t));
+  u128 *nk = (u128 *)malloc(8 * n * sizeof(u128));
+  if (!keys || !da->child || !da->hmask || !da->etype || !da->level || !da->nodes || !nk) {
+    rc = DGO_ENOMEM;
+    goto fail;
+  }
+  for (size_t i = 0; i < n; i++) keys[i] = morton(a[i].x, a[i].y, a[i].z);
+  const int64_t dom = (int64_t)1 << D;
+  size_t nn = 0;
+  for (size_t e = 0; e < n; e++) {
+    const unsigned l = a[e].lev;
+    const int64_t h = (int64_t)1 << (D - l);
+    const int64_t x = a[e].x, y = a[e].y, z = a[e].z;
+    /* Morton child number (include/oda/oda.tcc:1273-1302) */
+    int c = 0;
+    if (l > 0) c = (int)(((x / h) & 1) | (((y / h) & 1) << 1) | (((z / h) & 1) << 2));
+    uint8_t hm = 0;
+    if (l > 1) {
+      const int64_t H = 2 * h; /* parent side */
+      const int64_t P[3] = {x - ((c & 1) ? h : 0), y - ((c & 2) ? h : 0), z - ((c & 4) ? h : 0)};
+      /* shift of the parent towards the child's exterior along each axis */
+      const int64_t d[3] = {(c & 1) ? H : -H, (c & 2) ? H : -H, (c & 4) ? H : -H};
+      for (int r = 1; r < 7; r++) {
+        if (r == 7) continue;
+        /* vertex c^r: midpoint along the axes in r; on the parent's boundary
+         * (side c) along the others.  It hangs when one of the parent's
+         * neighbours sharing that face/edge is an unrefined leaf. */
+        int others = 7 & ~r, hang = 0;
+        for (int s = 1; s < 8 && !hang; s++) {
+          if ((s & others) != s) continue;
+          int64_t q[3] = {P[0], P[1], P[2]};
+          for (int ax = 0; ax < 3; ax++)
+            if (s >> ax & 1) q[ax] += d[ax];
+          if (is_leaf_at(a, keys, n, q[0], q[1], q[2], l - 1, D)) hang = 1;
+        }
+        if (hang) hm |= (uint8_t)(1u << (c ^ r));
+      }
+    }
+    da->child[e] = (uint8_t)c;
+    da->hmask[e] = hm;
+    da->level[e] = (uint8_t)l;
+    if (tmap[c][hm] == 0xff) {
+      rc = DGO_EINTERNAL; /* not a 2:1 balanced configuration */
+      goto fail;
+    }
+    da->etype[e] = tmap[c][hm];
+    /* nodes owned by this element: anchor, and vertices on the positive
+     * domain boundary that no other element anchors */
+    int bdy = ((x + h == dom) ? 1 : 0) | ((y + h == dom) ? 2 : 0) | ((z + h == dom) ? 4 : 0);
+    for (int k = 0; k < 8; k++) {
+      if ((k & bdy) != k || (hm >> k & 1)) continue;
+      nk[nn++] = morton((uint32_t)(x + ((k & 1) ? h : 0)), (uint32_t)(y + ((k & 2) ? h : 0)),
+                        (uint32_t)(z + ((k & 4) ? h : 0)));
+    }
+  }
+  cmp_u128_unique(nk, &nn);
+  da->n_elem = n;
+  da->n_node = nn;
+  da->node_xyz = (uint32_t *)malloc((nn ? 3 * nn : 3) * sizeof(uint32_t));
+  if (!da->node_xyz) {
+    rc = DGO_ENOMEM;
+    goto fail;
+  }
+  for (size_t i = 0; i < nn; i++)
+    level_index_decode(nk[i], &da->node_xyz[3 * i], &da->node_xyz[3 * i + 1], &da->node_xyz[3 * i + 2]);
+  for (size_t e = 0; e < n; e++) {
+    const int64_t h = (int64_t)1 << (D - a[e].lev);
+    const int c = da->child[e];
+    const int64_t x = a[e].x, y = a[e].y, z = a[e].z;
+    const int64_t px = x - ((c & 1) ? h : 0), py = y - ((c & 2) ? h : 0), pz = z - ((c & 4) ? h : 0);
+    for (int k = 0; k < 8; k++) {
+      int64_t vx, vy, vz;
+      if (da->hmask[e] >> k & 1) {
+        vx = px + ((k & 1) ? 2 * h : 0);
+        vy = py + ((k & 2) ? 2 * h : 0);
+        vz = pz + ((k & 4) ? 2 * h : 0);
+      } else {
+        vx = x + ((k & 1) ? h : 0);
+        vy = y + ((k & 2) ? h : 0);
+        vz = z + ((k & 4) ? h : 0);
+      }
+      size_t id = find_node(nk, nn, morton((uint32_t)vx, (uint32_t)vy, (uint32_t)vz));
+      if (id == (size_t)-1) {
+        rc = DGO_EINTERNAL;
+        goto fail;
+      }
+      da->nodes[8 * e + k] = (uint32_t)id;
+    }
+  }
+  free(keys);
+  free(nk);
+  return 0;
+fail:
+  free(keys);
+  free(nk);
+  dgo_da_free(da);
+  return rc;
+}
+
+int dgo_matvec(const dgo_da *da, unsigned D, const double *in, double *out, double lapFac, double massFac) {
+  static double L[8 * 18 * 64], M[8 * 18 * 64];
+  static int have = 0;
+  if (!have) {
+    dgo_stencils(L, M);
+    have = 1;
+  }
+  memset(out, 0, da->n_node * sizeof(double));
+  for (size_t e = 0; e < da->n_elem; e++) {
+    /* odaJac.C:311-313 + :276-279: h = hFac * 2^(maxD - lev) with the DA's
+     * maxD = D + 1 and DA level = level + 1, i.e. h = 2^-level */
+    double h = 1.0 / (double)((uint64_t)1 << da->level[e]);
+    double f1 = lapFac * h / 2.0, f2 = massFac * h * h * h / 8.0;
+    const double *Ls = &L[((size_t)da->child[e] * 18 + da->etype[e]) * 64];
+    const double *Ms = &M[((size_t)da->child[e] * 18 + da->etype[e]) * 64];
+    const uint32_t *id = &da->nodes[8 * e];
+    for (int k = 0; k < 8; k++) {
+      double acc = 0.0;
+      for (int j = 0; j < 8; j++) acc += (f1 * Ls[8 * k + j] + f2 * Ms[8 * k + j]) * in[id[j]];
+      out[id[k]] += acc;
+    }
+  }
+  (void)D;
+  return 0;
+}

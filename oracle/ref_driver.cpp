@@ -1,0 +1,344 @@
+/*
+ * Oracle driver around the REFERENCE's own code (Dendro4), compiled from the
+ * reference sources by oracle/Makefile into oracle/_ref/ref_driver.  Test
+ * infrastructure only: it produces golden outputs for the parity tests and
+ * times the reference CPU path.  Nothing in the shipped library uses it.
+ *
+ * Modes (all files are little-endian raw binary):
+ *   p2o   PTS MAXDEPTH MAXPTS OUT.oct
+ *         ot::points2Octree (src/construct.cpp:759) at 1 rank.
+ *   bal   IN.oct MAXDEPTH INCCORNER PATCHED OUT.oct
+ *         ot::balanceOctree (src/balance.cpp:31).  PATCHED=1 calls the same
+ *         1-rank body (copy + ot::comboRipple, balance.cpp:54-63) with a
+ *         maxNum of 4e9 instead of the default _COMBO_RIPPLE_FACTOR_
+ *         (include/octUtils.h:477), which works around the empty-output
+ *         defect of comboRipple above 1e7 octants (balance.cpp:821-900).
+ *   check IN.oct MAXDEPTH
+ *         ot::test::isLinear / isComplete / isBalanced (src/test/testUtils.C).
+ *   da    BAL.oct MAXDEPTH STENCILDIR VEC_IN|- OUT_PREFIX
+ *         ot::DA (src/oda/oda.cpp:250) then one Laplacian+mass element loop
+ *         (examples/src/backend/odaJac.C:275-292, hFac as odaJac.C:311-313).
+ *         Writes OUT_PREFIX.elem (per element: x y z level child hmask etype
+ *         and the 8 node indices as node coordinates) and, when VEC_IN is
+ *         given, OUT_PREFIX.mv (node coordinates + output value).
+ *
+ * Formats
+ *   .pts : u64 n, then n*3 f64 (x,y,z interleaved)
+ *   .oct : u64 n, then n*(u32 x, u32 y, u32 z, u32 level)
+ *   vec  : u64 n, then n*(u32 x, u32 y, u32 z, u32 pad, f64 value), node
+ *          coordinates at the octree's maxDepth scale (vertices in [0,2^D]).
+ */
+#include <chrono>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "TreeNode.h"
+#include "handleStencils.h"
+#include "octUtils.h"
+#include "oda.h"
+#include "odaUtils.h"
+#include "parUtils.h"
+#include "testUtils.h"
+
+double ****LaplacianType2Stencil = nullptr;
+double ****MassType2Stencil = nullptr;
+namespace ot {
+double ****ShapeFnCoeffs = nullptr;
+}
+
+static double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+static FILE *xopen(const char *p, const char *m) {
+  FILE *f = std::fopen(p, m);
+  if (!f) {
+    std::fprintf(stderr, "cannot open %s\n", p);
+    std::exit(2);
+  }
+  return f;
+}
+
+static std::vector<ot::TreeNode> read_oct(const char *path, unsigned maxDepth) {
+  FILE *f = xopen(path, "rb");
+  uint64_t n = 0;
+  if (std::fread(&n, 8, 1, f) != 1) std::exit(3);
+  std::vector<uint32_t> buf(4 * n);
+  if (n && std::fread(buf.data(), 4, 4 * n, f) != 4 * n) std::exit(3);
+  std::fclose(f);
+  std::vector<ot::TreeNode> out;
+  out.reserve(n);
+  for (uint64_t i = 0; i < n; i++)
+    out.push_back(ot::TreeNode(buf[4 * i], buf[4 * i + 1], buf[4 * i + 2], buf[4 * i + 3], 3, maxDepth));
+  return out;
+}
+
+static void write_oct(const char *path, const std::vector<ot::TreeNode> &v) {
+  FILE *f = xopen(path, "wb");
+  uint64_t n = v.size();
+  std::fwrite(&n, 8, 1, f);
+  std::vector<uint32_t> buf(4 * n);
+  for (uint64_t i = 0; i < n; i++) {
+    buf[4 * i] = v[i].getX();
+    buf[4 * i + 1] = v[i].getY();
+    buf[4 * i + 2] = v[i].getZ();
+    buf[4 * i + 3] = v[i].getLevel();
+  }
+  if (n) std::fwrite(buf.data(), 4, 4 * n, f);
+  std::fclose(f);
+}
+
+static int mode_p2o(int argc, char **argv) {
+  if (argc < 6) return 1;
+  unsigned maxDepth = std::atoi(argv[3]), maxPts = std::atoi(argv[4]);
+  FILE *f = xopen(argv[2], "rb");
+  uint64_t n = 0;
+  if (std::fread(&n, 8, 1, f) != 1) return 3;
+  std::vector<double> pts(3 * n);
+  if (n && std::fread(pts.data(), 8, 3 * n, f) != 3 * n) return 3;
+  std::fclose(f);
+  double gLens[3] = {1.0, 1.0, 1.0};
+  std::vector<ot::TreeNode> nodes;
+  double t0 = now_s();
+  ot::points2Octree(pts, gLens, nodes, 3, maxDepth, maxPts, MPI_COMM_WORLD);
+  double t1 = now_s();
+  write_oct(argv[5], nodes);
+  std::printf("{\"op\":\"p2o\",\"n_pts\":%llu,\"n_oct\":%zu,\"seconds\":%.6f}\n", (unsigned long long)n,
+              nodes.size(), t1 - t0);
+  return 0;
+}
+
+static int mode_bal(int argc, char **argv) {
+  if (argc < 7) return 1;
+  unsigned maxDepth = std::atoi(argv[3]);
+  bool incCorner = std::atoi(argv[4]) != 0;
+  bool patched = std::atoi(argv[5]) != 0;
+  std::vector<ot::TreeNode> in = read_oct(argv[2], maxDepth), out;
+  size_t nin = in.size();
+  double t0 = now_s();
+  if (patched) {
+    out = in;
+    in.clear();
+    ot::comboRipple(out, incCorner, 4000000000u);
+  } else {
+    ot::balanceOctree(in, out, 3, maxDepth, incCorner, MPI_COMM_WORLD, NULL, NULL);
+  }
+  double t1 = now_s();
+  write_oct(argv[6], out);
+  std::printf("{\"op\":\"bal\",\"n_in\":%zu,\"n_out\":%zu,\"patched\":%d,\"seconds\":%.6f}\n", nin, out.size(),
+              (int)patched, t1 - t0);
+  return 0;
+}
+
+static int mode_check(int argc, char **argv) {
+  if (argc < 4) return 1;
+  unsigned maxDepth = std::atoi(argv[3]);
+  std::vector<ot::TreeNode> v = read_oct(argv[2], maxDepth);
+  bool s = seq::test::isUniqueAndSorted(v);
+  bool l = ot::test::isLinear(v);
+  bool c = ot::test::isComplete(v);
+  bool b = ot::test::isBalanced(3, maxDepth, (char *)"_ref_check_fail", v, true, 1);
+  std::printf("{\"op\":\"check\",\"sorted\":%d,\"linear\":%d,\"complete\":%d,\"balanced\":%d}\n", (int)s, (int)l,
+              (int)c, (int)b);
+  return 0;
+}
+
+/* node coordinate key (coordinates at the octree's maxDepth scale, < 2^31) */
+static inline unsigned __int128 ckey(uint32_t x, uint32_t y, uint32_t z) {
+  return ((unsigned __int128)x << 64) | ((unsigned __int128)y << 32) | (unsigned __int128)z;
+}
+struct CKeyHash {
+  size_t operator()(unsigned __int128 k) const noexcept {
+    uint64_t a = (uint64_t)k, b = (uint64_t)(k >> 64);
+    return (size_t)((a * 0x9E3779B97F4A7C15ull) ^ (b + 0x632BE59BD9B4E019ull + (a << 6) + (a >> 2)));
+  }
+};
+
+static int mode_da(int argc, char **argv) {
+  if (argc < 7) return 1;
+  unsigned maxDepth = std::atoi(argv[3]);
+  std::string stencilDir = argv[4];
+  const char *vecIn = argv[5];
+  std::string prefix = argv[6];
+  std::vector<ot::TreeNode> bal = read_oct(argv[2], maxDepth);
+  size_t nb = bal.size();
+  {
+    /* DA_Initialize and the stencil loaders read their tables from the CWD */
+    char oldcwd[4096];
+    if (!getcwd(oldcwd, sizeof(oldcwd))) return 4;
+    if (chdir(stencilDir.c_str()) != 0) return 4;
+    ot::DA_Initialize(MPI_COMM_WORLD);
+    createLmatType2(LaplacianType2Stencil);
+    createMmatType2(MassType2Stencil);
+    if (chdir(oldcwd) != 0) return 4;
+  }
+
+  double t0 = now_s();
+  ot::DA da(bal, MPI_COMM_WORLD, MPI_COMM_WORLD, 0.3, false);
+  double t1 = now_s();
+  const unsigned maxD = da.getMaxDepth(); /* DA maxDepth = maxDepth + 1 */
+
+  /* Element sweep: record element data and the geometric position of every
+   * node index (vertex k of the element, or vertex k of its parent when the
+   * vertex is hanging).  A conflict would mean the hanging-vertex rule
+   * assumed here is wrong, so it is reported. */
+  std::vector<uint32_t> rec;
+  std::vector<uint32_t> idxPos; /* 3 per buffer slot */
+  std::vector<unsigned char> idxSeen;
+  size_t bufSize = da.getLocalBufferSize();
+  idxPos.assign(3 * bufSize, 0);
+  idxSeen.assign(bufSize, 0);
+  long conflicts = 0;
+  size_t nel = 0;
+  for (da.init<ot::DA_FLAGS::ALL>(); da.curr() < da.end<ot::DA_FLAGS::ALL>(); da.next<ot::DA_FLAGS::ALL>()) {
+    Point pt = da.getCurrentOffset();
+    unsigned lev = da.getLevel(da.curr());
+    unsigned idx[8];
+    da.getNodeIndices(idx);
+    unsigned char cn = da.getChildNumber();
+    unsigned char hm = da.getHangingNodeIndex(da.curr());
+    unsigned char et = 0;
+    GET_ETYPE_BLOCK(et, hm, cn)
+    uint32_t x = pt.xint(), y = pt.yint(), z = pt.zint();
+    uint32_t h = 1u << (maxD - lev);
+    uint32_t px = x - ((cn & 1) ? h : 0), py = y - ((cn & 2) ? h : 0), pz = z - ((cn & 4) ? h : 0);
+    rec.push_back(x);
+    rec.push_back(y);
+    rec.push_back(z);
+    rec.push_back(lev | (cn << 8) | (hm << 16) | (et << 24));
+    for (int k = 0; k < 8; k++) {
+      uint32_t vx, vy, vz;
+      if (hm & (1u << k)) {
+        vx = px + ((k & 1) ? 2 * h : 0);
+        vy = py + ((k & 2) ? 2 * h : 0);
+        vz = pz + ((k & 4) ? 2 * h : 0);
+      } else {
+        vx = x + ((k & 1) ? h : 0);
+        vy = y + ((k & 2) ? h : 0);
+        vz = z + ((k & 4) ? h : 0);
+      }
+      rec.push_back(vx);
+      rec.push_back(vy);
+      rec.push_back(vz);
+      if (idxSeen[idx[k]]) {
+        if (idxPos[3 * idx[k]] != vx || idxPos[3 * idx[k] + 1] != vy || idxPos[3 * idx[k] + 2] != vz) conflicts++;
+      } else {
+        idxSeen[idx[k]] = 1;
+        idxPos[3 * idx[k]] = vx;
+        idxPos[3 * idx[k] + 1] = vy;
+        idxPos[3 * idx[k] + 2] = vz;
+      }
+    }
+    nel++;
+  }
+  {
+    std::string p = prefix + ".elem";
+    FILE *f = xopen(p.c_str(), "wb");
+    uint64_t n = nel;
+    std::fwrite(&n, 8, 1, f);
+    if (n) std::fwrite(rec.data(), 4, rec.size(), f);
+    std::fclose(f);
+  }
+  size_t nNodesUsed = 0;
+  for (size_t i = 0; i < bufSize; i++) nNodesUsed += idxSeen[i];
+
+  double tmv = -1.0;
+  if (std::strcmp(vecIn, "-") != 0) {
+    /* input vector by node coordinate (node coordinates at the DA scale are
+     * the octree coordinates: the DA keeps anchors and adds one level) */
+    FILE *f = xopen(vecIn, "rb");
+    uint64_t nv = 0;
+    if (std::fread(&nv, 8, 1, f) != 1) return 3;
+    std::unordered_map<unsigned __int128, double, CKeyHash> val;
+    val.reserve(2 * nv);
+    for (uint64_t i = 0; i < nv; i++) {
+      uint32_t c[4];
+      double v;
+      if (std::fread(c, 4, 4, f) != 4 || std::fread(&v, 8, 1, f) != 1) return 3;
+      val[ckey(c[0], c[1], c[2])] = v;
+    }
+    std::fclose(f);
+
+    std::vector<double> in, out;
+    da.createVector(in, false, false, 1);
+    da.createVector(out, false, false, 1);
+    for (size_t i = 0; i < in.size(); i++) in[i] = out[i] = 0.0;
+    double *inArr = NULL, *outArr = NULL;
+    da.vecGetBuffer<double>(in, inArr, false, false, true, 1);
+    da.vecGetBuffer<double>(out, outArr, false, false, false, 1);
+    /* the buffers are indexed like getNodeIndices: fill the input by node
+     * coordinate, zero the output */
+    long missing = 0;
+    for (size_t i = 0; i < bufSize; i++) {
+      outArr[i] = 0.0;
+      if (!idxSeen[i]) continue;
+      auto it = val.find(ckey(idxPos[3 * i], idxPos[3 * i + 1], idxPos[3 * i + 2]));
+      if (it == val.end())
+        missing++;
+      else
+        inArr[i] = it->second;
+    }
+    da.ReadFromGhostsBegin<double>(inArr, 1);
+    da.ReadFromGhostsEnd<double>(inArr);
+    double hFac = 1.0 / ((double)(1u << (maxD - 1)));
+    double t2 = now_s();
+    for (da.init<ot::DA_FLAGS::ALL>(); da.curr() < da.end<ot::DA_FLAGS::ALL>(); da.next<ot::DA_FLAGS::ALL>()) {
+      unsigned lev = da.getLevel(da.curr());
+      double h = hFac * (1u << (maxD - lev));
+      double fac1 = h / 2.0, fac2 = h * h * h / 8.0;
+      unsigned idx[8];
+      da.getNodeIndices(idx);
+      unsigned char cn = da.getChildNumber();
+      unsigned char hm = da.getHangingNodeIndex(da.curr());
+      unsigned char et = 0;
+      GET_ETYPE_BLOCK(et, hm, cn)
+      for (int k = 0; k < 8; k++)
+        for (int j = 0; j < 8; j++)
+          outArr[idx[k]] += (fac1 * LaplacianType2Stencil[cn][et][k][j] + fac2 * MassType2Stencil[cn][et][k][j]) *
+                            inArr[idx[j]];
+    }
+    double t3 = now_s();
+    tmv = t3 - t2;
+    std::vector<double> res(bufSize, 0.0);
+    for (size_t i = 0; i < bufSize; i++) res[i] = outArr[i];
+    da.vecRestoreBuffer<double>(in, inArr, false, false, true, 1);
+    da.vecRestoreBuffer<double>(out, outArr, false, false, false, 1);
+    std::string p = prefix + ".mv";
+    FILE *g = xopen(p.c_str(), "wb");
+    uint64_t n = nNodesUsed;
+    std::fwrite(&n, 8, 1, g);
+    for (size_t i = 0; i < bufSize; i++) {
+      if (!idxSeen[i]) continue;
+      uint32_t c[4] = {idxPos[3 * i], idxPos[3 * i + 1], idxPos[3 * i + 2], 0};
+      std::fwrite(c, 4, 4, g);
+      std::fwrite(&res[i], 8, 1, g);
+    }
+    std::fclose(g);
+    if (missing) std::fprintf(stderr, "warning: %ld node values missing from input vector\n", missing);
+  }
+  std::printf(
+      "{\"op\":\"da\",\"n_bal\":%zu,\"n_elem\":%zu,\"n_nodes_da\":%u,\"n_nodes_used\":%zu,\"conflicts\":%ld,"
+      "\"t_da\":%.6f,\"t_matvec\":%.6f}\n",
+      nb, nel, da.getNodeSize(), nNodesUsed, conflicts, t1 - t0, tmv);
+  return conflicts ? 5 : 0;
+}
+
+int main(int argc, char **argv) {
+  if (argc < 2) {
+    std::fprintf(stderr, "usage: ref_driver p2o|bal|check|da ...\n");
+    return 1;
+  }
+  _InitializeHcurve(3);
+  std::string m = argv[1];
+  int rc = 1;
+  if (m == "p2o") rc = mode_p2o(argc, argv);
+  if (m == "bal") rc = mode_bal(argc, argv);
+  if (m == "check") rc = mode_check(argc, argv);
+  if (m == "da") rc = mode_da(argc, argv);
+  return rc;
+}

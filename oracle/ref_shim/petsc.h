@@ -1,0 +1,156 @@
+/*
+ * Header-only stand-in for the handful of PETSc types, macros and Vec/Mat
+ * calls that the reference's octree/DA/element-loop sources reference.  Used
+ * only to compile the reference into the CPU oracle binary (oracle/_ref).
+ * Vec is a plain heap array; Mat is a context holder.  No solver exists here.
+ */
+#ifndef DG_ORACLE_PETSC_SHIM_H
+#define DG_ORACLE_PETSC_SHIM_H
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#include "mpi.h"
+
+typedef int PetscErrorCode;
+typedef double PetscScalar;
+typedef double PetscReal;
+typedef int PetscInt;
+typedef int PetscMPIInt;
+typedef long long PetscInt64;
+typedef int PetscClassId;
+typedef int PetscLogEvent;
+typedef int PetscLogStage;
+typedef enum { PETSC_FALSE = 0, PETSC_TRUE = 1 } PetscBool;
+typedef PetscBool PetscTruth;
+typedef const char *MatType;
+typedef const char *VecType;
+typedef const char *KSPType;
+typedef const char *PCType;
+typedef enum { NOT_SET_VALUES = 0, INSERT_VALUES = 1, ADD_VALUES = 2 } InsertMode;
+typedef enum { SCATTER_FORWARD = 0, SCATTER_REVERSE = 1 } ScatterMode;
+typedef enum { MAT_FLUSH_ASSEMBLY = 1, MAT_FINAL_ASSEMBLY = 0 } MatAssemblyType;
+typedef enum { SAME_NONZERO_PATTERN = 0, DIFFERENT_NONZERO_PATTERN = 1 } MatStructure;
+typedef enum { NORM_1 = 0, NORM_2 = 1, NORM_INFINITY = 3 } NormType;
+typedef enum {
+  MATOP_MULT,
+  MATOP_MULT_ADD,
+  MATOP_MULT_TRANSPOSE,
+  MATOP_MULT_TRANSPOSE_ADD,
+  MATOP_GET_DIAGONAL,
+  MATOP_DESTROY
+} MatOperation;
+
+struct dg_shim_vec {
+  size_t n;
+  PetscScalar *a;
+};
+typedef dg_shim_vec *Vec;
+struct dg_shim_mat {
+  void *ctx;
+};
+typedef dg_shim_mat *Mat;
+struct dg_shim_opaque {
+  int unused;
+};
+typedef dg_shim_opaque *KSP;
+typedef dg_shim_opaque *PC;
+typedef dg_shim_opaque *VecScatter;
+typedef dg_shim_opaque *IS;
+typedef dg_shim_opaque *PetscViewer;
+typedef dg_shim_opaque *PetscRandom;
+typedef dg_shim_opaque *MatNullSpace;
+typedef dg_shim_opaque *PetscObject;
+
+#define PETSC_COMM_WORLD MPI_COMM_WORLD
+#define PETSC_COMM_SELF MPI_COMM_SELF
+#define PETSC_NULL 0
+#define PETSC_DECIDE (-1)
+#define PETSC_DETERMINE (-1)
+#define PETSC_DEFAULT (-2)
+#define PETSC_ERR_ARG_NULL 85
+#define PETSC_ERR_SUP 56
+#define MATSHELL "shell"
+#define MATAIJ "aij"
+#define MATSEQAIJ "seqaij"
+#define MATMPIAIJ "mpiaij"
+#define MATDAAD "daad"
+#define MATMFFD "mffd"
+#define VECSEQ "seq"
+#define VECMPI "mpi"
+
+#define CHKERRQ(e)      \
+  do {                  \
+    if (e) return (e);  \
+  } while (0)
+#define SETERRQ(c, e, m) return (e)
+#define PetscFunctionBegin
+#define PetscFunctionReturn(x) return (x)
+#define PetscLogEventBegin(...)
+#define PetscLogEventEnd(...)
+#define PetscLogFlops(x) 0
+
+inline PetscErrorCode VecCreate(MPI_Comm, Vec *v) {
+  *v = new dg_shim_vec{0, nullptr};
+  return 0;
+}
+inline PetscErrorCode VecSetSizes(Vec v, PetscInt n, PetscInt) {
+  v->n = (size_t)(n > 0 ? n : 0);
+  v->a = (PetscScalar *)std::calloc(v->n ? v->n : 1, sizeof(PetscScalar));
+  return 0;
+}
+inline PetscErrorCode VecSetType(Vec, VecType) { return 0; }
+inline PetscErrorCode VecGetLocalSize(Vec v, PetscInt *n) {
+  *n = (PetscInt)v->n;
+  return 0;
+}
+inline PetscErrorCode VecGetArray(Vec v, PetscScalar **a) {
+  *a = v->a;
+  return 0;
+}
+inline PetscErrorCode VecRestoreArray(Vec, PetscScalar **) { return 0; }
+inline PetscErrorCode VecGetArrayRead(Vec v, const PetscScalar **a) {
+  *a = v->a;
+  return 0;
+}
+inline PetscErrorCode VecRestoreArrayRead(Vec, const PetscScalar **) { return 0; }
+inline PetscErrorCode VecDestroy(Vec *v) {
+  if (*v) {
+    std::free((*v)->a);
+    delete *v;
+    *v = nullptr;
+  }
+  return 0;
+}
+inline PetscErrorCode VecZeroEntries(Vec v) {
+  std::memset(v->a, 0, v->n * sizeof(PetscScalar));
+  return 0;
+}
+inline PetscErrorCode VecSet(Vec v, PetscScalar s) {
+  for (size_t i = 0; i < v->n; i++) v->a[i] = s;
+  return 0;
+}
+inline PetscErrorCode PetscStrcmp(const char *a, const char *b, PetscBool *f) {
+  *f = (PetscBool)(std::strcmp(a, b) == 0);
+  return 0;
+}
+inline PetscErrorCode MatCreate(MPI_Comm, Mat *m) {
+  *m = new dg_shim_mat{nullptr};
+  return 0;
+}
+inline PetscErrorCode MatSetSizes(Mat, PetscInt, PetscInt, PetscInt, PetscInt) { return 0; }
+inline PetscErrorCode MatSetType(Mat, MatType) { return 0; }
+inline PetscErrorCode MatSeqAIJSetPreallocation(Mat, PetscInt, const PetscInt *) { return 0; }
+inline PetscErrorCode MatMPIAIJSetPreallocation(Mat, PetscInt, const PetscInt *, PetscInt, const PetscInt *) {
+  return 0;
+}
+inline PetscErrorCode MatSetValues(Mat, PetscInt, const PetscInt *, PetscInt, const PetscInt *,
+                                   const PetscScalar *, InsertMode) {
+  return 0;
+}
+inline PetscErrorCode MatZeroRows(Mat, PetscInt, const PetscInt *, PetscScalar, Vec, Vec) { return 0; }
+inline PetscErrorCode MatAssemblyBegin(Mat, MatAssemblyType) { return 0; }
+inline PetscErrorCode MatAssemblyEnd(Mat, MatAssemblyType) { return 0; }
+
+#endif
