@@ -1,0 +1,9 @@
+"""dendro_gb300: GB300-native (sm_103a) octree hot path of Dendro4.
+
+Morton sort -> ot::points2Octree -> ot::balanceOctree(incCorner) -> ot::DA
+-> Laplacian + mass element matVec, as hand-written CUDA kernels behind the
+C ABI of include/dendro_gb300.h.
+"""
+from .api import DA, Context, DendroError, Octree, balanceOctree, default_context, points2Octree, sortUniquePoints
+
+__all__ = ["DA", "Context", "DendroError", "Octree", "balanceOctree", "default_context", "points2Octree", "sortUniquePoints"]

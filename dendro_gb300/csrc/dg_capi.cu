@@ -1,0 +1,420 @@
+// C ABI (include/dendro_gb300.h) over the device pipelines.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <exception>
+#include <iterator>
+#include <new>
+#include <string>
+
+#include "dendro_gb300.h"
+#include "dg_da.cuh"
+
+struct dg_ctx_s {
+  dg::Context c;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+};
+struct dg_octree_s {
+  dg::Octree o;
+};
+struct dg_da_s {
+  dg::Mesh m;
+};
+
+namespace {
+
+template <typename F>
+int guarded(dg_ctx ctx, F &&f) {
+  if (!ctx) return DG_ERR_INVALID_ARG;
+  struct CurrentCtx {
+    CurrentCtx(dg::Context *c) { dg::current_context() = c; }
+    ~CurrentCtx() { dg::current_context() = nullptr; }
+  } current(&ctx->c);
+  try {
+    DG_CUDA(cudaSetDevice(ctx->c.device));
+    DG_CUDA(cudaEventRecord(ctx->ev0, ctx->c.stream));
+    f();
+    DG_CUDA(cudaEventRecord(ctx->ev1, ctx->c.stream));
+    DG_CUDA(cudaEventSynchronize(ctx->ev1));
+    dg::prof_resolve(ctx->c);
+    float ms = 0.f;
+    DG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    ctx->last_ms = ms;
+    ctx->c.last_error.clear();
+    return DG_OK;
+  } catch (const dg::Error &e) {
+    ctx->c.last_error = e.msg;
+    cudaStreamSynchronize(ctx->c.stream);
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    ctx->c.last_error = "host allocation failed";
+    return DG_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception &e) {
+    ctx->c.last_error = e.what();
+    return DG_ERR_INTERNAL;
+  }
+}
+
+// device copy of a host (or device) input array
+template <typename T>
+const T *device_input(dg::Context &c, const T *p, size_t n, int on_device, dg::DBuf<T> &hold) {
+  if (on_device || n == 0) return p;
+  hold.alloc(n, c.stream);
+  DG_CUDA(cudaMemcpyAsync(hold.get(), p, n * sizeof(T), cudaMemcpyHostToDevice, c.stream));
+  return hold.get();
+}
+
+template <typename T>
+void copy_out(dg::Context &c, T *dst, const T *src, size_t n, int dst_on_device) {
+  if (!n) return;
+  DG_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), dst_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                          c.stream));
+}
+
+}  // namespace
+
+extern "C" {
+
+int dg_version(void) { return 1; }
+
+const char *dg_status_string(int s) {
+  switch (s) {
+    case DG_OK: return "ok";
+    case DG_ERR_INVALID_ARG: return "invalid argument";
+    case DG_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case DG_ERR_CUDA: return "CUDA error";
+    case DG_ERR_DOMAIN: return "point outside the domain";
+    case DG_ERR_NOT_BALANCED: return "octree is not complete and 2:1 balanced";
+    case DG_ERR_TIMEOUT: return "device wait timed out";
+    case DG_ERR_INTERNAL: return "internal error";
+    case DG_ERR_COMM_SIZE: return "communicator size must be 1";
+    case DG_ERR_UNSUPPORTED: return "unsupported option";
+    default: return "unknown status";
+  }
+}
+
+int dg_ctx_create(int device, dg_ctx *out) {
+  if (!out) return DG_ERR_INVALID_ARG;
+  *out = nullptr;
+  dg_ctx ctx = new (std::nothrow) dg_ctx_s();
+  if (!ctx) return DG_ERR_OUT_OF_MEMORY;
+  ctx->c.device = device;
+  try {
+    DG_CUDA(cudaSetDevice(device));
+    DG_CUDA(cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking));
+    ctx->c.own_stream = true;
+    DG_CUDA(cudaMalloc((void **)&ctx->c.d_flags, sizeof(uint32_t)));
+    DG_CUDA(cudaMemset(ctx->c.d_flags, 0, sizeof(uint32_t)));
+    DG_CUDA(cudaMalloc((void **)&ctx->c.d_scratch, 64 * sizeof(unsigned long long)));
+    DG_CUDA(cudaMallocHost((void **)&ctx->c.h_scratch, 64 * sizeof(unsigned long long)));
+    DG_CUDA(cudaDeviceGetAttribute(&ctx->c.num_sms, cudaDevAttrMultiProcessorCount, device));
+    DG_CUDA(cudaEventCreate(&ctx->ev0));
+    DG_CUDA(cudaEventCreate(&ctx->ev1));
+    // keep freed blocks in this process's pool between calls
+    cudaMemPool_t pool;
+    DG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t thr = ~0ull;
+    DG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+  } catch (const dg::Error &e) {
+    int code = e.code;
+    dg_ctx_destroy(ctx);
+    return code;
+  }
+  *out = ctx;
+  return DG_OK;
+}
+
+int dg_ctx_destroy(dg_ctx ctx) {
+  if (!ctx) return DG_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->c.device);
+  if (ctx->c.stream) cudaStreamSynchronize(ctx->c.stream);
+  if (ctx->c.d_flags) cudaFree(ctx->c.d_flags);
+  if (ctx->c.d_scratch) cudaFree(ctx->c.d_scratch);
+  if (ctx->c.h_scratch) cudaFreeHost(ctx->c.h_scratch);
+  if (ctx->c.d_sten64) cudaFree(ctx->c.d_sten64);
+  if (ctx->c.d_sten32) cudaFree(ctx->c.d_sten32);
+  if (ctx->c.d_etype_of) cudaFree(ctx->c.d_etype_of);
+  if (ctx->c.d_etype_mask) cudaFree(ctx->c.d_etype_mask);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->c.own_stream && ctx->c.stream) cudaStreamDestroy(ctx->c.stream);
+  delete ctx;
+  return DG_OK;
+}
+
+int dg_ctx_set_stream(dg_ctx ctx, void *stream) {
+  if (!ctx) return DG_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->c.device);
+  cudaStreamSynchronize(ctx->c.stream);
+  if (stream) {
+    if (ctx->c.own_stream) cudaStreamDestroy(ctx->c.stream);
+    ctx->c.own_stream = false;
+    ctx->c.stream = (cudaStream_t)stream;
+  } else if (!ctx->c.own_stream) {
+    if (cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess) return DG_ERR_CUDA;
+    ctx->c.own_stream = true;
+  }
+  return DG_OK;
+}
+
+const char *dg_ctx_last_error(dg_ctx ctx) { return ctx ? ctx->c.last_error.c_str() : "null context"; }
+
+int dg_ctx_last_device_ms(dg_ctx ctx, double *ms) {
+  if (!ctx || !ms) return DG_ERR_INVALID_ARG;
+  *ms = ctx->last_ms;
+  return DG_OK;
+}
+
+int dg_ctx_profile(dg_ctx ctx, int enable) {
+  if (!ctx) return DG_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->c.device);
+  cudaStreamSynchronize(ctx->c.stream);
+  dg::prof_resolve(ctx->c);
+  ctx->c.prof_stats.clear();
+  ctx->c.prof = enable != 0;
+  return DG_OK;
+}
+
+int dg_ctx_profile_count(dg_ctx ctx, int *count) {
+  if (!ctx || !count) return DG_ERR_INVALID_ARG;
+  *count = (int)ctx->c.prof_stats.size();
+  return DG_OK;
+}
+
+int dg_ctx_profile_entry(dg_ctx ctx, int index, char *name, size_t name_len, double *total_ms,
+                         unsigned long long *launches, double *bytes) {
+  if (!ctx || index < 0 || index >= (int)ctx->c.prof_stats.size()) return DG_ERR_INVALID_ARG;
+  auto it = ctx->c.prof_stats.begin();
+  std::advance(it, index);
+  if (name && name_len) {
+    std::snprintf(name, name_len, "%s", it->first.c_str());
+  }
+  if (total_ms) *total_ms = it->second.ms;
+  if (launches) *launches = it->second.launches;
+  if (bytes) *bytes = it->second.bytes;
+  return DG_OK;
+}
+
+int dg_points_to_octree(dg_ctx ctx, const double *xyz, size_t n, const double gLens[3], unsigned maxDepth,
+                        unsigned maxNumPts, int comm_size, int xyz_on_device, dg_octree *out) {
+  if (!out || (!xyz && n) || !gLens) return DG_ERR_INVALID_ARG;
+  if (comm_size != 1) return DG_ERR_COMM_SIZE;
+  *out = nullptr;
+  dg_octree h = new (std::nothrow) dg_octree_s();
+  if (!h) return DG_ERR_OUT_OF_MEMORY;
+  int rc = guarded(ctx, [&]() {
+    if (!(gLens[0] > 0 && gLens[1] > 0 && gLens[2] > 0)) dg::fail(DG_ERR_INVALID_ARG, "gLens must be positive");
+    dg::DBuf<double> hold;
+    const double *d = device_input(ctx->c, xyz, 3 * n, xyz_on_device, hold);
+    dg::points_to_octree(ctx->c, d, n, gLens, maxDepth, maxNumPts, h->o);
+  });
+  if (rc != DG_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return DG_OK;
+}
+
+int dg_sort_unique_points(dg_ctx ctx, const double *xyz, size_t n, const double gLens[3], unsigned maxDepth,
+                          int xyz_on_device, uint32_t *out_xyzl, int out_on_device, size_t *n_unique) {
+  if ((!xyz && n) || !gLens || !n_unique || (!out_xyzl && n)) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() {
+    if (maxDepth > 30) dg::fail(DG_ERR_INVALID_ARG, "maxDepth must be <= 30");
+    dg::DBuf<double> hold;
+    const double *d = device_input(ctx->c, xyz, 3 * n, xyz_on_device, hold);
+    dg::DBuf<dg::Key128> uk(n ? n : 1, ctx->c.stream);
+    bool dups = false;
+    size_t nu = dg::sort_points(ctx->c, d, n, gLens, maxDepth, uk.get(), &dups);
+    dg::Octree tmp;
+    tmp.max_depth = maxDepth;
+    tmp.n = nu;
+    tmp.keys = uk.get();
+    if (out_on_device) {
+      dg::octree_to_xyzl(ctx->c, tmp, out_xyzl);
+    } else {
+      dg::DBuf<uint32_t> dx(4 * (nu ? nu : 1), ctx->c.stream);
+      dg::octree_to_xyzl(ctx->c, tmp, dx.get());
+      copy_out(ctx->c, out_xyzl, dx.get(), 4 * nu, 0);
+      DG_CUDA(cudaStreamSynchronize(ctx->c.stream));
+    }
+    *n_unique = nu;
+  });
+}
+
+int dg_balance_octree(dg_ctx ctx, dg_octree in, int incCorner, int comm_size, dg_octree *out) {
+  if (!in || !out) return DG_ERR_INVALID_ARG;
+  if (comm_size != 1) return DG_ERR_COMM_SIZE;
+  if (!incCorner) {
+    if (ctx) ctx->c.last_error = "balanceOctree: only incCorner = true is implemented";
+    return DG_ERR_UNSUPPORTED;
+  }
+  *out = nullptr;
+  dg_octree h = new (std::nothrow) dg_octree_s();
+  if (!h) return DG_ERR_OUT_OF_MEMORY;
+  int rc = guarded(ctx, [&]() { dg::balance_octree(ctx->c, in->o, h->o); });
+  if (rc != DG_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return DG_OK;
+}
+
+int dg_octree_size(dg_octree o, size_t *n, unsigned *maxDepth) {
+  if (!o) return DG_ERR_INVALID_ARG;
+  if (n) *n = o->o.n;
+  if (maxDepth) *maxDepth = o->o.max_depth;
+  return DG_OK;
+}
+
+int dg_octree_download(dg_ctx ctx, dg_octree o, uint32_t *xyzl, int dst_on_device) {
+  if (!o || (!xyzl && o->o.n)) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() {
+    if (dst_on_device) {
+      dg::octree_to_xyzl(ctx->c, o->o, xyzl);
+    } else {
+      dg::DBuf<uint32_t> dx(4 * (o->o.n ? o->o.n : 1), ctx->c.stream);
+      dg::octree_to_xyzl(ctx->c, o->o, dx.get());
+      copy_out(ctx->c, xyzl, dx.get(), 4 * o->o.n, 0);
+    }
+  });
+}
+
+int dg_octree_upload(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDepth, int src_on_device, dg_octree *out) {
+  if (!out || (!xyzl && n) || maxDepth > 30) return DG_ERR_INVALID_ARG;
+  *out = nullptr;
+  dg_octree h = new (std::nothrow) dg_octree_s();
+  if (!h) return DG_ERR_OUT_OF_MEMORY;
+  int rc = guarded(ctx, [&]() {
+    dg::DBuf<uint32_t> hold;
+    const uint32_t *d = device_input(ctx->c, xyzl, 4 * n, src_on_device, hold);
+    dg::octree_from_xyzl(ctx->c, d, n, maxDepth, h->o);
+  });
+  if (rc != DG_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return DG_OK;
+}
+
+int dg_octree_free(dg_ctx ctx, dg_octree o) {
+  if (!ctx || !o) return DG_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->c.device);
+  dg::octree_free(ctx->c, o->o);
+  cudaStreamSynchronize(ctx->c.stream);
+  delete o;
+  return DG_OK;
+}
+
+int dg_da_build(dg_ctx ctx, dg_octree balanced, dg_da *out) {
+  if (!balanced || !out) return DG_ERR_INVALID_ARG;
+  *out = nullptr;
+  dg_da h = new (std::nothrow) dg_da_s();
+  if (!h) return DG_ERR_OUT_OF_MEMORY;
+  int rc = guarded(ctx, [&]() { dg::mesh_build(ctx->c, balanced->o, h->m); });
+  if (rc != DG_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return DG_OK;
+}
+
+int dg_da_sizes(dg_da da, size_t *n_elem, size_t *n_node) {
+  if (!da) return DG_ERR_INVALID_ARG;
+  if (n_elem) *n_elem = da->m.n_elem;
+  if (n_node) *n_node = da->m.n_node;
+  return DG_OK;
+}
+
+namespace {
+__global__ void k_transpose_conn(const uint32_t *__restrict__ conn, size_t E, uint32_t *__restrict__ out) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+#pragma unroll
+  for (int k = 0; k < 8; k++) out[8 * e + k] = conn[(size_t)k * E + e];
+}
+__global__ void k_interleave3(const uint32_t *__restrict__ soa, size_t n, uint32_t *__restrict__ out) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[3 * i] = soa[i];
+  out[3 * i + 1] = soa[n + i];
+  out[3 * i + 2] = soa[2 * n + i];
+}
+}  // namespace
+
+int dg_da_download(dg_ctx ctx, dg_da da, uint32_t *meta, uint32_t *nodes, uint32_t *node_xyz, int dst_on_device) {
+  if (!da) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() {
+    dg::Context &c = ctx->c;
+    const size_t E = da->m.n_elem, V = da->m.n_node;
+    if (meta) copy_out(c, meta, da->m.meta, E, dst_on_device);
+    if (nodes && E) {
+      dg::DBuf<uint32_t> t(8 * E, c.stream);
+      {
+        dg::ProfScope _prof("da_transpose", (double)E * 64);
+        k_transpose_conn<<<dg::grid_for(E, 256), 256, 0, c.stream>>>(da->m.conn, E, t.get());
+        DG_LAUNCH_CHECK();
+      }
+      copy_out(c, nodes, t.get(), 8 * E, dst_on_device);
+      DG_CUDA(cudaStreamSynchronize(c.stream));
+    }
+    if (node_xyz && V) {
+      dg::DBuf<uint32_t> t(3 * V, c.stream);
+      {
+        dg::ProfScope _prof("da_interleave", (double)V * 24);
+        k_interleave3<<<dg::grid_for(V, 256), 256, 0, c.stream>>>(da->m.node_xyz, V, t.get());
+        DG_LAUNCH_CHECK();
+      }
+      copy_out(c, node_xyz, t.get(), 3 * V, dst_on_device);
+      DG_CUDA(cudaStreamSynchronize(c.stream));
+    }
+  });
+}
+
+int dg_da_free(dg_ctx ctx, dg_da da) {
+  if (!ctx || !da) return DG_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->c.device);
+  dg::mesh_free(ctx->c, da->m);
+  cudaStreamSynchronize(ctx->c.stream);
+  delete da;
+  return DG_OK;
+}
+
+int dg_matvec(dg_ctx ctx, dg_da da, const void *in, void *out, int precision, double lapFac, double massFac,
+              int on_device) {
+  if (!da || !in || !out) return DG_ERR_INVALID_ARG;
+  if (precision != 32 && precision != 64) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() {
+    dg::Context &c = ctx->c;
+    const size_t V = da->m.n_node;
+    if (precision == 64) {
+      dg::DBuf<double> hin, hout;
+      const double *x = device_input(c, (const double *)in, V, on_device, hin);
+      double *y = (double *)out;
+      if (!on_device) {
+        hout.alloc(V, c.stream);
+        y = hout.get();
+      }
+      dg::mesh_matvec<double>(c, da->m, x, y, lapFac, massFac);
+      if (!on_device) copy_out(c, (double *)out, y, V, 0);
+      DG_CUDA(cudaStreamSynchronize(c.stream));
+    } else {
+      dg::DBuf<float> hin, hout;
+      const float *x = device_input(c, (const float *)in, V, on_device, hin);
+      float *y = (float *)out;
+      if (!on_device) {
+        hout.alloc(V, c.stream);
+        y = hout.get();
+      }
+      dg::mesh_matvec<float>(c, da->m, x, y, lapFac, massFac);
+      if (!on_device) copy_out(c, (float *)out, y, V, 0);
+      DG_CUDA(cudaStreamSynchronize(c.stream));
+    }
+  });
+}
+
+}  // extern "C"

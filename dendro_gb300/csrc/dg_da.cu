@@ -1,0 +1,404 @@
+// Octree mesh build (ot::DA at one rank: src/oda/oda.cpp:250 ->
+// DA_FactoryPart1..3, src/oda/private/odaFactory.cpp, odaBuildNlist.cpp)
+// and the Laplacian + mass element loop (examples/src/backend/odaJac.C).
+//
+// Hanging vertices.  Element e at level l is child c of parent P (level
+// l-1).  Only the vertices c^r with r in {1,2,4} (midpoints of P's edges
+// through corner c) and r in {3,5,6} (centres of P's faces through corner
+// c) can hang.  Such a vertex hangs when one of P's same-size neighbours
+// that share that face or edge is an unrefined leaf (2:1 balance bounds the
+// neighbour to level l-1).  A hanging vertex k refers to P's vertex k, which
+// is always a mesh node; the element type (one of 18 per child number,
+// include/oda/cnumEtypes.h) selects the stencil that folds the hanging
+// interpolation into the element matrix.
+//
+// Nodes.  Every node is the anchor of exactly one octant of the reference's
+// DA octant set (elements plus the positive-boundary pseudo-octants of
+// octFunctions.cpp:681-770).  Here element e owns its anchor (when it does
+// not hang) and its vertices on the positive domain boundary, so the node
+// set is numbered by one scan over elements; the owner of any vertex is the
+// leaf that contains it after clamping boundary coordinates inward.
+#include "dg_da.cuh"
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <type_traits>
+#include <vector>
+
+namespace dg {
+
+// ------------------------------------------------------------------------
+// element-type and stencil tables (host)
+// ------------------------------------------------------------------------
+// The 18 hanging configurations in the reference's type order
+// (include/oda/odaUtils.tcc:14-120), as vertex sets relative to the child's
+// own corner: relative vertex r = 1, 2, 4 are the edge midpoints, 3, 5, 6 the
+// face centres.  Bit r of each entry marks relative vertex r as hanging.
+static const uint8_t kCanonRel[18] = {0x00, 0x04, 0x02, 0x06, 0x10, 0x14, 0x12, 0x16, 0x0e,
+                                      0x1e, 0x54, 0x56, 0x5e, 0x32, 0x36, 0x3e, 0x76, 0x7e};
+// Each child number's table is the canonical one with its axes permuted:
+// the relative axis bit that canonical x, y, z map to.
+static const uint8_t kAxisPerm[8][3] = {{1, 2, 4}, {2, 1, 4}, {2, 1, 4}, {1, 2, 4},
+                                        {1, 4, 2}, {2, 4, 1}, {2, 4, 1}, {1, 4, 2}};
+
+void gen_etype_masks(uint8_t masks[8 * 18]) {
+  for (int c = 0; c < 8; c++)
+    for (int t = 0; t < 18; t++) {
+      uint8_t m = 0;
+      for (int r = 0; r < 8; r++) {
+        if (!(kCanonRel[t] >> r & 1)) continue;
+        int pr = ((r & 1) ? kAxisPerm[c][0] : 0) | ((r & 2) ? kAxisPerm[c][1] : 0) | ((r & 4) ? kAxisPerm[c][2] : 0);
+        m |= (uint8_t)(1u << (pr ^ c));
+      }
+      masks[c * 18 + t] = m;
+    }
+}
+
+// S[c][t] = P^T K P on the reference element [-1,1]^3 with trilinear shape
+// functions; K = stiffness (Laplacian) or mass; P maps the 8 referenced
+// values to the child's vertex values (a hanging vertex is the average of
+// the parent corners spanning its edge or face).
+void gen_stencils(double *lap, double *mass) {
+  const double m1[2][2] = {{2.0 / 3.0, 1.0 / 3.0}, {1.0 / 3.0, 2.0 / 3.0}};
+  const double a1[2][2] = {{0.5, -0.5}, {-0.5, 0.5}};
+  double K[8][8], M[8][8];
+  for (int i = 0; i < 8; i++)
+    for (int j = 0; j < 8; j++) {
+      int ix = i & 1, iy = i >> 1 & 1, iz = i >> 2 & 1, jx = j & 1, jy = j >> 1 & 1, jz = j >> 2 & 1;
+      K[i][j] = a1[ix][jx] * m1[iy][jy] * m1[iz][jz] + m1[ix][jx] * a1[iy][jy] * m1[iz][jz] +
+                m1[ix][jx] * m1[iy][jy] * a1[iz][jz];
+      M[i][j] = m1[ix][jx] * m1[iy][jy] * m1[iz][jz];
+    }
+  uint8_t masks[8 * 18];
+  gen_etype_masks(masks);
+  for (int c = 0; c < 8; c++)
+    for (int t = 0; t < 18; t++) {
+      double P[8][8];
+      std::memset(P, 0, sizeof(P));
+      uint8_t hm = masks[c * 18 + t];
+      for (int k = 0; k < 8; k++) {
+        if (!(hm >> k & 1)) {
+          P[k][k] = 1.0;
+          continue;
+        }
+        int d = k ^ c, cnt = 0;
+        for (int s = 0; s < 8; s++) cnt += ((s & d) == s);
+        for (int s = 0; s < 8; s++)
+          if ((s & d) == s) P[k][c ^ s] += 1.0 / cnt;
+      }
+      for (int i = 0; i < 8; i++)
+        for (int j = 0; j < 8; j++) {
+          double sl = 0.0, sm = 0.0;
+          for (int a = 0; a < 8; a++)
+            for (int b = 0; b < 8; b++) {
+              double w = P[a][i] * P[b][j];
+              if (w != 0.0) {
+                sl += w * K[a][b];
+                sm += w * M[a][b];
+              }
+            }
+          size_t o = (((size_t)c * 18 + t) * 8 + i) * 8 + j;
+          lap[o] = sl;
+          mass[o] = sm;
+        }
+    }
+}
+
+// device layout: for each (c, t) a 128-entry block: 64 Laplacian then 64 mass
+constexpr int STEN_ENTRIES = 8 * 18 * 128;
+
+void ensure_stencils(Context &ctx) {
+  if (ctx.d_sten64) return;
+  std::vector<double> lap(8 * 18 * 64), mass(8 * 18 * 64);
+  gen_stencils(lap.data(), mass.data());
+  std::vector<double> s64(STEN_ENTRIES);
+  std::vector<float> s32(STEN_ENTRIES);
+  for (int ct = 0; ct < 8 * 18; ct++)
+    for (int q = 0; q < 64; q++) {
+      s64[ct * 128 + q] = lap[ct * 64 + q];
+      s64[ct * 128 + 64 + q] = mass[ct * 64 + q];
+    }
+  for (int i = 0; i < STEN_ENTRIES; i++) s32[i] = (float)s64[i];
+  uint8_t masks[8 * 18], etype_of[8 * 256];
+  gen_etype_masks(masks);
+  std::memset(etype_of, 0xff, sizeof(etype_of));
+  for (int c = 0; c < 8; c++)
+    for (int t = 0; t < 18; t++) etype_of[c * 256 + masks[c * 18 + t]] = (uint8_t)t;
+  double *d64 = nullptr;
+  float *d32 = nullptr;
+  uint8_t *det = nullptr, *dem = nullptr;
+  DG_CUDA(cudaMalloc((void **)&d64, STEN_ENTRIES * sizeof(double)));
+  DG_CUDA(cudaMalloc((void **)&d32, STEN_ENTRIES * sizeof(float)));
+  DG_CUDA(cudaMalloc((void **)&det, sizeof(etype_of)));
+  DG_CUDA(cudaMalloc((void **)&dem, sizeof(masks)));
+  DG_CUDA(cudaMemcpy(d64, s64.data(), STEN_ENTRIES * sizeof(double), cudaMemcpyHostToDevice));
+  DG_CUDA(cudaMemcpy(d32, s32.data(), STEN_ENTRIES * sizeof(float), cudaMemcpyHostToDevice));
+  DG_CUDA(cudaMemcpy(det, etype_of, sizeof(etype_of), cudaMemcpyHostToDevice));
+  DG_CUDA(cudaMemcpy(dem, masks, sizeof(masks), cudaMemcpyHostToDevice));
+  ctx.d_sten64 = d64;
+  ctx.d_sten32 = d32;
+  ctx.d_etype_of = det;
+  ctx.d_etype_mask = dem;
+}
+
+// ------------------------------------------------------------------------
+// mesh build
+// ------------------------------------------------------------------------
+// index of the leaf whose anchor is the largest anchor <= pos
+__device__ __forceinline__ size_t find_leaf(const Key128 *__restrict__ keys, size_t n, Key128 pos) {
+  size_t lo = 0, hi = n;
+  while (lo < hi) {
+    size_t mid = lo + (hi - lo) / 2;
+    if (key_le(tag_anchor(keys[mid]), pos)) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo ? lo - 1 : 0;  // lo >= 1 for a complete octree; callers verify
+}
+
+__device__ __forceinline__ bool is_leaf_at(const Key128 *__restrict__ keys, size_t n, int64_t x, int64_t y, int64_t z,
+                                           unsigned lev, int64_t dom) {
+  if (x < 0 || y < 0 || z < 0 || x >= dom || y >= dom || z >= dom) return false;
+  Key128 pos = morton3((uint32_t)x, (uint32_t)y, (uint32_t)z);
+  size_t j = find_leaf(keys, n, pos);
+  Key128 kj = keys[j];
+  return tag_level(kj) == lev && key_eq(tag_anchor(kj), pos);
+}
+
+__global__ void k_mesh_elems(const Key128 *__restrict__ keys, size_t n, unsigned D, const uint8_t *__restrict__ etype_of,
+                             uint32_t *__restrict__ meta, uint32_t *__restrict__ cnt, uint32_t *flags) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const Key128 ke = keys[e];
+  const unsigned l = tag_level(ke);
+  uint32_t ux, uy, uz;
+  demorton3(tag_anchor(ke), ux, uy, uz);
+  const int64_t dom = (int64_t)1 << D, h = (int64_t)1 << (D - l);
+  const int64_t x = ux, y = uy, z = uz;
+  int c = 0;
+  if (l > 0) c = (int)(((x >> (D - l)) & 1) | (((y >> (D - l)) & 1) << 1) | (((z >> (D - l)) & 1) << 2));
+  unsigned hm = 0;
+  if (l > 1) {
+    const int64_t H = 2 * h;
+    const int64_t P[3] = {x - ((c & 1) ? h : 0), y - ((c & 2) ? h : 0), z - ((c & 4) ? h : 0)};
+    const int64_t d[3] = {(c & 1) ? H : -H, (c & 2) ? H : -H, (c & 4) ? H : -H};
+    // neighbours of P towards the child's exterior: leaf[s] for s in 1..7
+    bool leaf[8];
+    leaf[0] = false;
+#pragma unroll
+    for (int s = 1; s < 8; s++) {
+      if (s == 7) {
+        leaf[s] = false;  // the corner neighbour hangs no vertex of e
+        continue;
+      }
+      leaf[s] = is_leaf_at(keys, n, P[0] + ((s & 1) ? d[0] : 0), P[1] + ((s & 2) ? d[1] : 0),
+                           P[2] + ((s & 4) ? d[2] : 0), l - 1, dom);
+    }
+#pragma unroll
+    for (int r = 1; r < 7; r++) {
+      const int others = 7 & ~r;
+      bool hang = false;
+#pragma unroll
+      for (int s = 1; s < 7; s++)
+        if ((s & others) == s && leaf[s]) hang = true;
+      if (hang) hm |= 1u << (c ^ r);
+    }
+  }
+  unsigned et = etype_of[c * 256 + hm];
+  if (et == 0xffu) {
+    atomicOr(flags, DGF_NOT_BALANCED);
+    et = 0;
+  }
+  meta[e] = l | ((unsigned)c << 8) | (hm << 16) | (et << 24);
+  const unsigned bdy = ((x + h == dom) ? 1u : 0u) | ((y + h == dom) ? 2u : 0u) | ((z + h == dom) ? 4u : 0u);
+  unsigned owned = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++)
+    if ((k & bdy) == (unsigned)k && !(hm >> k & 1)) owned++;
+  cnt[e] = owned;
+}
+
+__global__ void k_mesh_conn(const Key128 *__restrict__ keys, size_t n, unsigned D, const uint32_t *__restrict__ meta,
+                            const uint64_t *__restrict__ base, uint32_t *__restrict__ conn, uint32_t *__restrict__ nx,
+                            uint32_t *__restrict__ ny, uint32_t *__restrict__ nz, size_t n_node, uint32_t *flags) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const Key128 ke = keys[e];
+  const uint32_t me = meta[e];
+  const unsigned l = me & 255u, c = (me >> 8) & 7u, hm = (me >> 16) & 255u;
+  uint32_t ux, uy, uz;
+  demorton3(tag_anchor(ke), ux, uy, uz);
+  const int64_t dom = (int64_t)1 << D, h = (int64_t)1 << (D - l);
+  const int64_t x = ux, y = uy, z = uz;
+  const int64_t px = x - ((c & 1) ? h : 0), py = y - ((c & 2) ? h : 0), pz = z - ((c & 4) ? h : 0);
+  // owned nodes: coordinates
+  {
+    const unsigned bdy = ((x + h == dom) ? 1u : 0u) | ((y + h == dom) ? 2u : 0u) | ((z + h == dom) ? 4u : 0u);
+    uint64_t id = base[e];
+    for (int k = 0; k < 8; k++) {
+      if ((k & bdy) != (unsigned)k || (hm >> k & 1)) continue;
+      if (id < n_node) {
+        nx[id] = (uint32_t)(x + ((k & 1) ? h : 0));
+        ny[id] = (uint32_t)(y + ((k & 2) ? h : 0));
+        nz[id] = (uint32_t)(z + ((k & 4) ? h : 0));
+      }
+      id++;
+    }
+  }
+#pragma unroll 1
+  for (int k = 0; k < 8; k++) {
+    int64_t v[3];
+    if (hm >> k & 1) {
+      v[0] = px + ((k & 1) ? 2 * h : 0);
+      v[1] = py + ((k & 2) ? 2 * h : 0);
+      v[2] = pz + ((k & 4) ? 2 * h : 0);
+    } else {
+      v[0] = x + ((k & 1) ? h : 0);
+      v[1] = y + ((k & 2) ? h : 0);
+      v[2] = z + ((k & 4) ? h : 0);
+    }
+    unsigned kb = 0;
+    int64_t cl[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      if (v[a] == dom) {
+        kb |= 1u << a;
+        cl[a] = dom - 1;
+      } else {
+        cl[a] = v[a];
+      }
+    }
+    size_t o = find_leaf(keys, n, morton3((uint32_t)cl[0], (uint32_t)cl[1], (uint32_t)cl[2]));
+    const Key128 ko = keys[o];
+    const unsigned lo_ = tag_level(ko);
+    uint32_t ox, oy, oz;
+    demorton3(tag_anchor(ko), ox, oy, oz);
+    const int64_t ho = (int64_t)1 << (D - lo_);
+    const int64_t oc[3] = {ox, oy, oz};
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < 3; a++) ok = ok && ((kb >> a & 1) ? (oc[a] + ho == dom) : (oc[a] == v[a]));
+    const unsigned bo = ((oc[0] + ho == dom) ? 1u : 0u) | ((oc[1] + ho == dom) ? 2u : 0u) | ((oc[2] + ho == dom) ? 4u : 0u);
+    const unsigned hmo = (meta[o] >> 16) & 255u;
+    ok = ok && ((kb & bo) == kb) && !(hmo >> kb & 1);
+    unsigned rank = 0;
+    for (unsigned q = 0; q < kb; q++)
+      if ((q & bo) == q && !(hmo >> q & 1)) rank++;
+    uint64_t id = base[o] + rank;
+    if (!ok || id >= n_node) {
+      atomicOr(flags, DGF_NOT_BALANCED);
+      id = 0;
+    }
+    conn[(size_t)k * n + e] = (uint32_t)id;
+  }
+}
+
+void mesh_build(Context &ctx, const Octree &bal, Mesh &m) {
+  cudaStream_t s = ctx.stream;
+  const size_t n = bal.n;
+  const unsigned D = bal.max_depth;
+  if (n == 0) fail(DG_ERR_INVALID_ARG, "DA: empty octree");
+  if (n >= 0xffffffffull / 8) fail(DG_ERR_INVALID_ARG, "DA: too many elements");
+  ensure_stencils(ctx);
+  m.max_depth = D;
+  m.n_elem = n;
+  DBuf<uint32_t> meta(n, s), cnt(n, s);
+  DG_CUDA(cudaMemsetAsync(ctx.d_flags, 0, sizeof(uint32_t), s));
+  {
+    ProfScope _prof(ctx, "da_elems", (double)n * 24);
+    k_mesh_elems<<<grid_for(n, 256), 256, 0, s>>>(bal.keys, n, D, ctx.d_etype_of, meta.get(), cnt.get(), ctx.d_flags);
+  DG_LAUNCH_CHECK();
+    }
+  DBuf<uint64_t> base(n, s);
+  uint64_t *d_total = reinterpret_cast<uint64_t *>(ctx.d_scratch);
+  exclusive_scan<uint32_t, uint64_t>(cnt.get(), base.get(), n, d_total, s);
+  size_t nn = (size_t)read_scalar(ctx, d_total);
+  check_device_flags(ctx, "DA");
+  if (nn >= 0xffffffffull) fail(DG_ERR_INVALID_ARG, "DA: too many nodes");
+  cnt.release();
+  DBuf<uint32_t> conn(8 * n, s), nxyz(3 * (nn ? nn : 1), s);
+  {
+    ProfScope _prof(ctx, "da_conn", (double)n * 56);
+    k_mesh_conn<<<grid_for(n, 256), 256, 0, s>>>(bal.keys, n, D, meta.get(), base.get(), conn.get(), nxyz.get(),
+                                               nxyz.get() + nn, nxyz.get() + 2 * nn, nn, ctx.d_flags);
+  DG_LAUNCH_CHECK();
+    }
+  check_device_flags(ctx, "DA");
+  m.n_node = nn;
+  m.meta = meta.release_ptr();
+  m.conn = conn.release_ptr();
+  m.node_xyz = nxyz.release_ptr();
+}
+
+void mesh_free(Context &ctx, Mesh &m) {
+  if (m.meta) cudaFreeAsync(m.meta, ctx.stream);
+  if (m.conn) cudaFreeAsync(m.conn, ctx.stream);
+  if (m.node_xyz) cudaFreeAsync(m.node_xyz, ctx.stream);
+  m = Mesh();
+}
+
+// ------------------------------------------------------------------------
+// element loop
+// ------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(512) k_matvec(const uint32_t *__restrict__ meta, const uint32_t *__restrict__ conn,
+                                                size_t E, const T *__restrict__ sten, const T *__restrict__ x,
+                                                T *__restrict__ y, T lapf, T massf) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *ss = reinterpret_cast<T *>(smem_raw);
+  for (int i = threadIdx.x; i < STEN_ENTRIES; i += blockDim.x) ss[i] = sten[i];
+  __syncthreads();
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t me = meta[e];
+    const unsigned l = me & 255u, c = (me >> 8) & 7u, t = me >> 24;
+    uint32_t id[8];
+    T xv[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) id[k] = conn[(size_t)k * E + e];
+#pragma unroll
+    for (int k = 0; k < 8; k++) xv[k] = x[id[k]];
+    // h = 2^-l (element side in the unit cube)
+    const T h = (T)1 / (T)(1ull << l);
+    const T f1 = lapf * h * (T)0.5, f2 = massf * h * h * h * (T)0.125;
+    const T *S = ss + (c * 18 + t) * 128;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      T aL = 0, aM = 0;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        aL += S[8 * k + j] * xv[j];
+        aM += S[64 + 8 * k + j] * xv[j];
+      }
+      atomicAdd(&y[id[k]], f1 * aL + f2 * aM);
+    }
+  }
+}
+
+template <typename T>
+void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, double mass_fac) {
+  ensure_stencils(ctx);
+  cudaStream_t s = ctx.stream;
+  DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
+  const size_t smem = STEN_ENTRIES * sizeof(T);
+  static std::once_flag once;
+  std::call_once(once, [&]() {
+    DG_CUDA(cudaFuncSetAttribute(k_matvec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  });
+  const int block = 512;
+  int per_sm = 1;
+  DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_matvec<T>, block, smem));
+  if (per_sm < 1) per_sm = 1;
+  unsigned grid = grid_for(m.n_elem, block, (unsigned)(per_sm * ctx.num_sms));
+  const T *sten = std::is_same<T, double>::value ? reinterpret_cast<const T *>(ctx.d_sten64)
+                                                 : reinterpret_cast<const T *>(ctx.d_sten32);
+  {
+    ProfScope _prof(ctx, "matvec", (double)m.n_elem * 36 + (double)m.n_node * 3 * sizeof(T));
+    k_matvec<T><<<grid, block, smem, s>>>(m.meta, m.conn, m.n_elem, sten, x, y, (T)lap_fac, (T)mass_fac);
+  DG_LAUNCH_CHECK();
+    }
+}
+
+template void mesh_matvec<float>(Context &, const Mesh &, const float *, float *, double, double);
+template void mesh_matvec<double>(Context &, const Mesh &, const double *, double *, double, double);
+
+}  // namespace dg

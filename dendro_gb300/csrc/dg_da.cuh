@@ -1,0 +1,41 @@
+// Octree mesh (the reference's ot::DA at one rank) and the element-loop
+// operators that run on it.
+#pragma once
+
+#include "dg_octree.cuh"
+
+namespace dg {
+
+// Element e of the mesh is octant e of the balanced octree.  Storage (SoA,
+// coalesced by element):
+//   meta[e]    = level | child << 8 | hanging mask << 16 | element type << 24
+//   conn[k][e] = node id of vertex k (k = x + 2y + 4z); a hanging vertex k
+//                refers to vertex k of the element's parent
+// Nodes are the mesh vertices that are not hanging, coordinates in
+// [0, 2^D]^3.  Node ids follow element order: the non-hanging anchor of
+// every element, then its vertices on the positive domain boundary.
+struct Mesh {
+  unsigned max_depth = 0;
+  size_t n_elem = 0;
+  size_t n_node = 0;
+  uint32_t *meta = nullptr;
+  uint32_t *conn = nullptr;      // 8 * n_elem, vertex-major
+  uint32_t *node_xyz = nullptr;  // 3 * n_node, coordinate-major
+};
+
+void mesh_build(Context &ctx, const Octree &bal, Mesh &m);
+void mesh_free(Context &ctx, Mesh &m);
+
+// y = (lapFac * Laplacian + massFac * mass) x over all elements
+// (examples/src/backend/odaJac.C:294-377, block :275-292)
+template <typename T>
+void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, double mass_fac);
+
+// stencil tables on the device, generated on first use
+void ensure_stencils(Context &ctx);
+
+// host-side generators (same mathematics as the reference's .inp tables)
+void gen_etype_masks(uint8_t masks[8 * 18]);
+void gen_stencils(double *lap, double *mass);
+
+}  // namespace dg

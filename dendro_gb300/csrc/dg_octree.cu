@@ -1,0 +1,679 @@
+// Octree construction (points2Octree) and 2:1 balance (balanceOctree) on
+// the GPU.  All data stays in HBM; the host only reads sizes.
+//
+// Construction (unique points, reference p2oLocal, src/construct.cpp:976):
+// the leaf that holds point i is the child of its deepest ancestor that
+// contains more than maxPts points.  With the points in Morton order that
+// ancestor's level is max_j NCA(p_j, p_{j+m}) over the windows j in
+// [i-m, i] (m = maxPts), so every point's leaf is computed independently;
+// the empty leaves between consecutive point leaves are the maximal aligned
+// Morton blocks of the gap.  Inputs with repeated points take the
+// reference's sequential walk verbatim (a single-thread kernel), because its
+// point bookkeeping then departs from the rule above.
+//
+// Balance (reference comboRipple, src/balance.cpp:801): the coarsest 2:1
+// balanced refinement is unique.  With I_l the internal nodes at level l,
+//   I_{l-1} = parent(input leaves at level l) U parents of the 3x3x3 blocks
+//             around every q in I_l (8 octants per q, clipped to the domain)
+// and the balanced leaves at level l are children(I_{l-1}) \ I_l.  Each
+// level is one generate + radix sort + unique; the leaves are then placed in
+// Morton order by a bottom-up leaf count and a top-down offset pass.
+#include "dg_octree.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace dg {
+
+__device__ __forceinline__ void set_flag(uint32_t *flags, uint32_t f) { atomicOr(flags, f); }
+
+// ------------------------------------------------------------------------
+// quantize + Morton key (construct.cpp:930-942)
+// ------------------------------------------------------------------------
+__global__ void k_quantize(const double *__restrict__ xyz, size_t n, double scale, double gx, double gy, double gz,
+                           unsigned D, Key128 *__restrict__ keys, uint32_t *flags) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+  // (unsigned int)(x * (double)(1u << D) / gLen): multiply, divide, truncate
+  double qx = __ddiv_rn(__dmul_rn(x, scale), gx);
+  double qy = __ddiv_rn(__dmul_rn(y, scale), gy);
+  double qz = __ddiv_rn(__dmul_rn(z, scale), gz);
+  // valid iff the truncated value lies in [0, 2^D): q in (-1, 2^D); NaN fails
+  bool ok = (qx > -1.0) && (qx < scale) && (qy > -1.0) && (qy < scale) && (qz > -1.0) && (qz < scale);
+  uint32_t ux = 0, uy = 0, uz = 0;
+  if (ok) {
+    ux = (uint32_t)__double2uint_rz(qx);
+    uy = (uint32_t)__double2uint_rz(qy);
+    uz = (uint32_t)__double2uint_rz(qz);
+  } else {
+    set_flag(flags, DGF_DOMAIN);
+  }
+  keys[i] = make_tagged(morton3(ux, uy, uz), D);
+}
+
+__device__ __forceinline__ int nca_level(Key128 a, Key128 b, unsigned D) {
+  Key128 x = key_xor(tag_anchor(a), tag_anchor(b));
+  if (!x.lo && !x.hi) return (int)D;
+  return key_clz(x, 3 * (int)D) / 3;
+}
+
+__global__ void k_flag_dups(const Key128 *__restrict__ p, size_t n, uint32_t *flags) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 1 && i < n && key_eq(p[i], p[i - 1])) set_flag(flags, 0x100u);
+}
+
+// leaf level of every point and the flag "first point of its leaf"
+__global__ void k_p2o_seeds(const Key128 *__restrict__ p, size_t n, unsigned m, unsigned D,
+                            Key128 *__restrict__ seeds, uint32_t *__restrict__ first) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  size_t lo = (i >= m) ? i - m : 0;
+  size_t hi = (i + m < n) ? i : n - 1 - m;
+  int best = 0;
+  for (size_t j = lo; j <= hi; j++) best = max(best, nca_level(p[j], p[j + m], D));
+  unsigned L = min((unsigned)best + 1u, D);
+  Key128 a = tag_anchor(p[i]);
+  a = key_shl(key_shr(a, 3 * (D - L)), 3 * (D - L));
+  Key128 s = make_tagged(a, L);
+  seeds[i] = s;
+  // same leaf as the previous point?  (recomputed, not read back)
+  bool f = true;
+  if (i > 0) {
+    size_t lo2 = (i - 1 >= m) ? i - 1 - m : 0;
+    size_t hi2 = (i - 1 + m < n) ? i - 1 : n - 1 - m;
+    int best2 = 0;
+    for (size_t j = lo2; j <= hi2; j++) best2 = max(best2, nca_level(p[j], p[j + m], D));
+    unsigned L2 = min((unsigned)best2 + 1u, D);
+    Key128 a2 = tag_anchor(p[i - 1]);
+    a2 = key_shl(key_shr(a2, 3 * (D - L2)), 3 * (D - L2));
+    f = !(L2 == L && key_eq(a2, a));
+  }
+  first[i] = f ? 1u : 0u;
+}
+
+__device__ __forceinline__ u128 kpos(Key128 k) { return to_u128(tag_anchor(k)); }
+
+__device__ __forceinline__ int ctz128(u128 v) {
+  uint64_t lo = (uint64_t)v;
+  if (lo) return __ffsll((long long)lo) - 1;
+  uint64_t hi = (uint64_t)(v >> 64);
+  return hi ? 64 + __ffsll((long long)hi) - 1 : 128;
+}
+__device__ __forceinline__ int log2_128(u128 v) {  // v > 0
+  uint64_t hi = (uint64_t)(v >> 64);
+  if (hi) return 127 - __clzll((long long)hi);
+  return 63 - __clzll((long long)(uint64_t)v);
+}
+
+// largest k with s % 8^k == 0 and s + 8^k <= e (s < e)
+__device__ __forceinline__ int block_exp(u128 s, u128 e, unsigned D) {
+  int k1 = (s == 0) ? (int)D : min((int)D, ctz128(s) / 3);
+  int k2 = log2_128(e - s) / 3;
+  return min(k1, k2);
+}
+
+__device__ unsigned gap_count(u128 s, u128 e, unsigned D) {
+  unsigned c = 0;
+  while (s < e) {
+    int k = block_exp(s, e, D);
+    s += (u128)1 << (3 * k);
+    c++;
+  }
+  return c;
+}
+
+__device__ size_t gap_emit(u128 s, u128 e, unsigned D, Key128 *out, size_t w) {
+  while (s < e) {
+    int k = block_exp(s, e, D);
+    out[w++] = make_tagged(from_u128(s), D - (unsigned)k);
+    s += (u128)1 << (3 * k);
+  }
+  return w;
+}
+
+__device__ __forceinline__ u128 seed_end(Key128 s, unsigned D) {
+  return kpos(s) + ((u128)1 << (3 * (D - tag_level(s))));
+}
+
+__global__ void k_fill_count(const Key128 *__restrict__ seeds, size_t ns, unsigned D, uint32_t *__restrict__ cnt) {
+  size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ns) return;
+  const u128 total = (u128)1 << (3 * D);
+  u128 e = (j + 1 < ns) ? kpos(seeds[j + 1]) : total;
+  unsigned c = 1 + gap_count(seed_end(seeds[j], D), e, D);
+  if (j == 0) c += gap_count(0, kpos(seeds[0]), D);
+  cnt[j] = c;
+}
+
+__global__ void k_fill_emit(const Key128 *__restrict__ seeds, size_t ns, unsigned D, const uint64_t *__restrict__ off,
+                            Key128 *__restrict__ out) {
+  size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ns) return;
+  const u128 total = (u128)1 << (3 * D);
+  size_t w = off[j];
+  if (j == 0) w = gap_emit(0, kpos(seeds[0]), D, out, w);
+  out[w++] = seeds[j];
+  u128 e = (j + 1 < ns) ? kpos(seeds[j + 1]) : total;
+  gap_emit(seed_end(seeds[j], D), e, D, out, w);
+}
+
+// ------------------------------------------------------------------------
+// the reference walk, verbatim, for inputs with repeated points
+// (construct.cpp:976-1076); one thread; count pass then emit pass
+// ------------------------------------------------------------------------
+struct WOct {
+  uint32_t x, y, z, lev;
+};
+__device__ __forceinline__ WOct wo_from_key(Key128 k) {
+  WOct o;
+  demorton3(tag_anchor(k), o.x, o.y, o.z);
+  o.lev = tag_level(k);
+  return o;
+}
+__device__ __forceinline__ u128 wo_key(const WOct &o) {
+  return (to_u128(morton3(o.x, o.y, o.z)) << 5) | (u128)(o.lev & 31u);
+}
+__device__ __forceinline__ bool wo_is_anc(const WOct &a, const WOct &b, unsigned D) {
+  if (!(a.lev < b.lev)) return false;
+  uint64_t la = 1ull << (D - a.lev), lb = 1ull << (D - b.lev);
+  return b.x >= a.x && b.y >= a.y && b.z >= a.z && (uint64_t)b.x + lb <= (uint64_t)a.x + la &&
+         (uint64_t)b.y + lb <= (uint64_t)a.y + la && (uint64_t)b.z + lb <= (uint64_t)a.z + la;
+}
+__device__ __forceinline__ WOct wo_next(WOct m, unsigned D) {
+  uint32_t mask = 1u << (D - m.lev);
+  int i;
+  for (i = (int)m.lev; i >= 0; --i) {
+    m.x ^= mask;
+    if (m.x & mask) break;
+    m.y ^= mask;
+    if (m.y & mask) break;
+    m.z ^= mask;
+    if (m.z & mask) break;
+    mask <<= 1;
+  }
+  m.lev = (uint32_t)i;
+  return m;
+}
+__device__ __forceinline__ WOct wo_dld(const WOct &a, unsigned D) {
+  uint32_t l = 1u << (D - a.lev);
+  return WOct{a.x + l - 1, a.y + l - 1, a.z + l - 1, D};
+}
+
+__global__ void k_p2o_walk_serial(const Key128 *__restrict__ pk, size_t n, unsigned m, unsigned D,
+                                  Key128 *__restrict__ out, unsigned long long *count) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const uint32_t num_pts = (uint32_t)n;
+  WOct curr{0, 0, 0, 0};
+  WOct last = wo_dld(curr, D);
+  WOct next = wo_next(curr, D);
+  uint32_t curr_pt = 0, next_pt = curr_pt + m;
+  size_t w = 0;
+  u128 prev_key = ~(u128)0;
+  auto push = [&](const WOct &o) {
+    u128 k = wo_key(o);
+    if (k == prev_key) return;  // std::list::unique
+    prev_key = k;
+    if (out) out[w] = make_tagged(morton3(o.x, o.y, o.z), o.lev);
+    w++;
+  };
+  while (next_pt < num_pts) {
+    for (;;) {
+      WOct a = wo_from_key(pk[next_pt - 1]), b = wo_from_key(pk[next_pt]);
+      if (!(wo_is_anc(curr, a, D) && wo_is_anc(curr, b, D) && curr.lev < D)) break;
+      curr.lev++;
+      next = wo_next(curr, D);
+    }
+    uint32_t inc = m;
+    while (curr.lev == D - 1) {
+      inc <<= 1;
+      next_pt += inc;
+      if (next_pt > num_pts) {
+        next_pt = num_pts - 1;
+        break;
+      }
+    }
+    // lower_bound(pts[curr_pt..next_pt), next, less_equal)
+    u128 nk = wo_key(next);
+    uint32_t lo = curr_pt, hi = next_pt;
+    while (lo < hi) {
+      uint32_t mid = lo + (hi - lo) / 2;
+      if (wo_key(wo_from_key(pk[mid])) <= nk) lo = mid + 1;
+      else hi = mid;
+    }
+    int found_pt = (int)(lo - curr_pt);
+    next_pt = curr_pt + (uint32_t)found_pt;
+    push(curr);
+    curr = next;
+    next = wo_next(curr, D);
+    if (next_pt > curr_pt) curr_pt = next_pt;
+    next_pt = curr_pt + m;
+  }
+  u128 lastk = wo_key(last);
+  while (wo_key(curr) <= lastk) {
+    while (wo_key(wo_dld(curr, D)) > lastk && curr.lev < D) curr.lev++;
+    push(curr);
+    if (wo_key(wo_dld(curr, D)) == lastk) break;
+    curr = wo_next(curr, D);
+  }
+  *count = w;
+}
+
+// ------------------------------------------------------------------------
+// host: point sort and construction
+// ------------------------------------------------------------------------
+void check_device_flags(Context &ctx, const char *where) {
+  uint32_t f = read_scalar(ctx, ctx.d_flags);
+  if (f) {
+    DG_CUDA(cudaMemsetAsync(ctx.d_flags, 0, sizeof(uint32_t), ctx.stream));
+    if (f & DGF_DOMAIN) fail(DG_ERR_DOMAIN, std::string(where) + ": a point lies outside [0, gLen)^3");
+    if (f & DGF_NOT_BALANCED) fail(DG_ERR_NOT_BALANCED, std::string(where) + ": input is not a complete 2:1 balanced octree");
+    if (f & DGF_TIMEOUT) fail(DG_ERR_TIMEOUT, std::string(where) + ": a device wait timed out");
+    if (f & DGF_INTERNAL) fail(DG_ERR_INTERNAL, std::string(where) + ": internal consistency check failed");
+  }
+}
+
+static void quantize_sorted(Context &ctx, const double *d_xyz, size_t n, const double g[3], unsigned D,
+                            DBuf<Key128> &keys, DBuf<Key128> &tmp, Key128 **sorted) {
+  keys.alloc(n, ctx.stream);
+  tmp.alloc(n, ctx.stream);
+  {
+    ProfScope _prof(ctx, "quantize", (double)n * 40);
+    k_quantize<<<grid_for(n, 256), 256, 0, ctx.stream>>>(d_xyz, n, (double)(1u << D), g[0], g[1], g[2], D, keys.get(),
+                                                       ctx.d_flags);
+  DG_LAUNCH_CHECK();
+    }
+  check_device_flags(ctx, "points2Octree");
+  *sorted = radix_sort<Key128>(ctx, keys.get(), tmp.get(), n, 3 * (int)D);
+}
+
+size_t sort_points(Context &ctx, const double *d_xyz, size_t n, const double g[3], unsigned D, Key128 *d_out,
+                   bool *has_dups) {
+  if (n == 0) return 0;
+  DBuf<Key128> keys, tmp;
+  Key128 *sorted;
+  quantize_sorted(ctx, d_xyz, n, g, D, keys, tmp, &sorted);
+  DBuf<uint32_t> flags(n, ctx.stream);
+  k_flag_unique<Key128><<<grid_for(n, 256), 256, 0, ctx.stream>>>(sorted, n, flags.get());
+  DG_LAUNCH_CHECK();
+  size_t nu = compact<Key128>(ctx, sorted, flags.get(), n, d_out);
+  if (has_dups) *has_dups = nu != n;
+  return nu;
+}
+
+void points_to_octree(Context &ctx, const double *d_xyz, size_t n, const double g[3], unsigned D, unsigned m,
+                      Octree &out) {
+  if (m == 0 || D > 30) fail(DG_ERR_INVALID_ARG, "points2Octree: maxNumPts must be >= 1 and maxDepth <= 30");
+  if (n >= 0x7fffffffull) fail(DG_ERR_INVALID_ARG, "points2Octree: too many points");
+  out.max_depth = D;
+  cudaStream_t s = ctx.stream;
+  if (D == 0 || n <= m) {  // construct.cpp:916-920, 948-952: the root alone
+    if (n && D) {
+      // still validate the domain like the quantize loop would see it
+      DBuf<Key128> keys(n, s);
+      {
+        ProfScope _prof("quantize", (double)n * 40);
+        k_quantize<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, (double)(1u << D), g[0], g[1], g[2], D, keys.get(),
+                                                    ctx.d_flags);
+        DG_LAUNCH_CHECK();
+      }
+      check_device_flags(ctx, "points2Octree");
+    }
+    out.n = 1;
+    DG_CUDA(cudaMallocAsync((void **)&out.keys, sizeof(Key128), s));
+    Key128 root = make_tagged(Key128{0, 0}, 0);
+    DG_CUDA(cudaMemcpyAsync(out.keys, &root, sizeof(Key128), cudaMemcpyHostToDevice, s));
+    DG_CUDA(cudaStreamSynchronize(s));
+    return;
+  }
+  DBuf<Key128> keys, tmp;
+  Key128 *p;
+  quantize_sorted(ctx, d_xyz, n, g, D, keys, tmp, &p);
+  Key128 *other = (p == keys.get()) ? tmp.get() : keys.get();
+
+  DG_CUDA(cudaMemsetAsync(ctx.d_flags, 0, sizeof(uint32_t), s));
+  {
+    ProfScope _prof("flag_dups", (double)n * 16);
+    k_flag_dups<<<grid_for(n, 256), 256, 0, s>>>(p, n, ctx.d_flags);
+    DG_LAUNCH_CHECK();
+  }
+  uint32_t dupflag = read_scalar(ctx, ctx.d_flags);
+  DG_CUDA(cudaMemsetAsync(ctx.d_flags, 0, sizeof(uint32_t), s));
+
+  if (dupflag) {
+    unsigned long long *d_cnt = ctx.d_scratch + 8;
+    {
+      ProfScope _prof("p2o_walk_serial", (double)n * 16);
+      k_p2o_walk_serial<<<1, 1, 0, s>>>(p, n, m, D, nullptr, d_cnt);
+      DG_LAUNCH_CHECK();
+    }
+    size_t cnt = (size_t)read_scalar(ctx, d_cnt);
+    DBuf<Key128> res(cnt, s);
+    {
+      ProfScope _prof("p2o_walk_serial", (double)n * 16 + (double)cnt * 16);
+      k_p2o_walk_serial<<<1, 1, 0, s>>>(p, n, m, D, res.get(), d_cnt);
+      DG_LAUNCH_CHECK();
+    }
+    DG_CUDA(cudaStreamSynchronize(s));
+    out.n = cnt;
+    out.keys = res.release_ptr();
+    return;
+  }
+
+  DBuf<uint32_t> first(n, s);
+  {
+    ProfScope _prof(ctx, "p2o_seeds", (double)n * 36);
+    k_p2o_seeds<<<grid_for(n, 256), 256, 0, s>>>(p, n, m, D, other, first.get());
+  DG_LAUNCH_CHECK();
+    }
+  // compact seeds into p (the sorted points are no longer needed)
+  size_t ns = compact<Key128>(ctx, other, first.get(), n, p);
+  DBuf<uint32_t> cnt(ns, s);
+  {
+    ProfScope _prof(ctx, "fill_count", (double)ns * 20);
+    k_fill_count<<<grid_for(ns, 256), 256, 0, s>>>(p, ns, D, cnt.get());
+  DG_LAUNCH_CHECK();
+    }
+  DBuf<uint64_t> off(ns, s);
+  uint64_t *d_total = reinterpret_cast<uint64_t *>(ctx.d_scratch);
+  exclusive_scan<uint32_t, uint64_t>(cnt.get(), off.get(), ns, d_total, s);
+  size_t total = (size_t)read_scalar(ctx, d_total);
+  DBuf<Key128> res(total, s);
+  {
+    ProfScope _prof(ctx, "fill_emit", (double)ns * 24);
+    k_fill_emit<<<grid_for(ns, 256), 256, 0, s>>>(p, ns, D, off.get(), res.get());
+  DG_LAUNCH_CHECK();
+    }
+  out.n = total;
+  out.keys = res.release_ptr();
+}
+
+// ------------------------------------------------------------------------
+// balance
+// ------------------------------------------------------------------------
+__global__ void k_level_hist(const Key128 *__restrict__ k, size_t n, unsigned long long *hist) {
+  __shared__ unsigned int h[32];
+  if (threadIdx.x < 32) h[threadIdx.x] = 0;
+  __syncthreads();
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    atomicAdd(&h[tag_level(k[i]) & 31u], 1u);
+  __syncthreads();
+  if (threadIdx.x < 32 && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], (unsigned long long)h[threadIdx.x]);
+}
+
+// level-(l-1) Morton index of the parent of every input leaf at level l
+__global__ void k_leaf_parents(const Key128 *__restrict__ k, size_t n, unsigned D, unsigned l, Key128 *__restrict__ out) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = key_shr(tag_anchor(k[i]), 3 * (D - l + 1));
+}
+
+// for q at level l: the 8 level-(l-1) parents of q's 3x3x3 block; parents
+// outside the domain are replaced by q's own parent (removed by the unique)
+__global__ void k_block_parents(const Key128 *__restrict__ q, size_t nq, unsigned l, Key128 *__restrict__ out) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  uint32_t c[3];
+  demorton3(q[i], c[0], c[1], c[2]);  // level-l integer coordinates
+  const int64_t side = (int64_t)1 << (l - 1);  // parents per axis
+  int64_t opt[3][2];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    int64_t par = c[a] >> 1;
+    opt[a][0] = par;
+    opt[a][1] = (c[a] & 1) ? par + 1 : par - 1;
+  }
+#pragma unroll
+  for (int t = 0; t < 8; t++) {
+    int64_t p0 = opt[0][t & 1], p1 = opt[1][(t >> 1) & 1], p2 = opt[2][(t >> 2) & 1];
+    if (p0 < 0 || p1 < 0 || p2 < 0 || p0 >= side || p1 >= side || p2 >= side) {
+      p0 = opt[0][0];
+      p1 = opt[1][0];
+      p2 = opt[2][0];
+    }
+    out[8 * i + t] = morton3((uint32_t)p0, (uint32_t)p1, (uint32_t)p2);
+  }
+}
+
+__device__ __forceinline__ size_t lower_bound_key(const Key128 *a, size_t n, Key128 v) {
+  size_t lo = 0, hi = n;
+  while (lo < hi) {
+    size_t mid = lo + (hi - lo) / 2;
+    if (key_lt(a[mid], v)) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// rank map: R[8*parent_index + child] = index of the internal child in I_l
+__global__ void k_mark_internal(const Key128 *__restrict__ Il, size_t nl, const Key128 *__restrict__ Ip, size_t np,
+                                uint32_t *__restrict__ R, uint32_t *flags) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nl) return;
+  Key128 par = key_shr(Il[i], 3);
+  size_t p = lower_bound_key(Ip, np, par);
+  if (p >= np || !key_eq(Ip[p], par)) {
+    atomicOr(flags, DGF_INTERNAL);
+    return;
+  }
+  R[8 * p + (Il[i].lo & 7u)] = (uint32_t)i;
+}
+
+__global__ void k_subtree_count(const uint32_t *__restrict__ R, size_t np, const uint64_t *__restrict__ sub_child,
+                                uint64_t *__restrict__ sub) {
+  size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= np) return;
+  uint64_t c = 0;
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    uint32_t x = R ? R[8 * r + q] : 0xffffffffu;
+    c += (x == 0xffffffffu) ? 1ull : sub_child[x];
+  }
+  sub[r] = c;
+}
+
+__global__ void k_place(const Key128 *__restrict__ Ip, size_t np, unsigned l, unsigned D, const uint32_t *__restrict__ R,
+                        const uint64_t *__restrict__ sub_child, const uint64_t *__restrict__ off,
+                        uint64_t *__restrict__ off_child, Key128 *__restrict__ out) {
+  size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= np) return;
+  uint64_t run = off[r];
+  Key128 base = key_shl(Ip[r], 3);
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    uint32_t x = R ? R[8 * r + q] : 0xffffffffu;
+    if (x == 0xffffffffu) {
+      Key128 ch = base;
+      ch.lo |= (uint64_t)q;
+      out[run] = make_tagged(key_shl(ch, 3 * (D - l - 1)), l + 1);
+      run += 1;
+    } else {
+      off_child[x] = run;
+      run += sub_child[x];
+    }
+  }
+}
+
+void balance_octree(Context &ctx, const Octree &in, Octree &out) {
+  cudaStream_t s = ctx.stream;
+  const unsigned D = in.max_depth;
+  out.max_depth = D;
+  const size_t n = in.n;
+  if (n == 0) fail(DG_ERR_INVALID_ARG, "balanceOctree: empty input");
+  if (n == 1) {
+    out.n = 1;
+    DG_CUDA(cudaMallocAsync((void **)&out.keys, sizeof(Key128), s));
+    DG_CUDA(cudaMemcpyAsync(out.keys, in.keys, sizeof(Key128), cudaMemcpyDeviceToDevice, s));
+    DG_CUDA(cudaStreamSynchronize(s));
+    return;
+  }
+  // level histogram
+  unsigned long long *d_hist = ctx.d_scratch + 16;
+  DG_CUDA(cudaMemsetAsync(d_hist, 0, 32 * sizeof(unsigned long long), s));
+  {
+    ProfScope _prof("bal_level_hist", (double)n * 16);
+    k_level_hist<<<grid_for(n, 256, ctx.num_sms * 4), 256, 0, s>>>(in.keys, n, d_hist);
+    DG_LAUNCH_CHECK();
+  }
+  unsigned long long hcnt[32];
+  DG_CUDA(cudaMemcpyAsync(ctx.h_scratch + 16, d_hist, sizeof(hcnt), cudaMemcpyDeviceToHost, s));
+  DG_CUDA(cudaStreamSynchronize(s));
+  std::memcpy(hcnt, ctx.h_scratch + 16, sizeof(hcnt));
+  unsigned maxL = 0;
+  for (unsigned l = 0; l < 32; l++)
+    if (hcnt[l]) maxL = l;
+  if (maxL > D) fail(DG_ERR_INVALID_ARG, "balanceOctree: octant level exceeds maxDepth");
+
+  // bucket the leaves by level (one stable radix pass on the level byte);
+  // every bucket stays in Morton order
+  DBuf<Key128> bucketed(n, s);
+  {
+    size_t ntiles = (n + RS_TILE - 1) / RS_TILE;
+    DBuf<uint32_t> hist(256 * ntiles, s);
+    {
+      ProfScope _prof("rs_hist", (double)n * 16);
+      k_rs_hist<Key128><<<(unsigned)ntiles, RS_BLOCK, 0, s>>>(in.keys, n, 120, hist.get(), ntiles);
+      DG_LAUNCH_CHECK();
+    }
+    exclusive_scan<uint32_t, uint32_t>(hist.get(), hist.get(), 256 * ntiles, (uint32_t *)nullptr, s);
+    {
+      ProfScope _prof("rs_scatter", (double)n * 32);
+      k_rs_scatter<Key128><<<(unsigned)ntiles, RS_BLOCK, 0, s>>>(in.keys, bucketed.get(), n, 120, hist.get(), ntiles);
+      DG_LAUNCH_CHECK();
+    }
+  }
+  std::vector<size_t> boff(33, 0);
+  for (unsigned l = 0; l < 32; l++) boff[l + 1] = boff[l] + hcnt[l];
+
+  std::vector<DBuf<Key128>> I(maxL + 1);
+  std::vector<size_t> nI(maxL + 1, 0);
+  for (int l = (int)maxL; l >= 1; l--) {
+    size_t nt = hcnt[l], nq = nI[l];
+    size_t nc = nt + 8 * nq;
+    if (nc == 0) continue;
+    DBuf<Key128> cand(nc, s), ctmp(nc, s);
+    if (nt) {
+      {
+    ProfScope _prof(ctx, "bal_leaf_parents", (double)nt * 32);
+    k_leaf_parents<<<grid_for(nt, 256), 256, 0, s>>>(bucketed.get() + boff[l], nt, D, (unsigned)l, cand.get());
+      DG_LAUNCH_CHECK();
+    }
+    }
+    if (nq) {
+      {
+    ProfScope _prof(ctx, "bal_block_parents", (double)nq * 144);
+    k_block_parents<<<grid_for(nq, 256), 256, 0, s>>>(I[l].get(), nq, (unsigned)l, cand.get() + nt);
+      DG_LAUNCH_CHECK();
+    }
+    }
+    Key128 *res;
+    size_t nu = sort_unique<Key128>(ctx, cand.get(), ctmp.get(), nc, 3 * (l - 1), &res);
+    DBuf<Key128> Il(nu, s);
+    DG_CUDA(cudaMemcpyAsync(Il.get(), res, nu * sizeof(Key128), cudaMemcpyDeviceToDevice, s));
+    I[l - 1] = std::move(Il);
+    nI[l - 1] = nu;
+  }
+  if (nI[0] != 1) fail(DG_ERR_INTERNAL, "balanceOctree: root is not internal");
+
+  // rank maps R_l (l = 0..maxL-1): children of I_l that are internal
+  std::vector<DBuf<uint32_t>> R(maxL + 1);
+  DG_CUDA(cudaMemsetAsync(ctx.d_flags, 0, sizeof(uint32_t), s));
+  for (unsigned l = 0; l + 1 <= maxL; l++) {
+    if (!nI[l] || !nI[l + 1]) continue;
+    R[l].alloc(8 * nI[l], s);
+    DG_CUDA(cudaMemsetAsync(R[l].get(), 0xff, 8 * nI[l] * sizeof(uint32_t), s));
+    {
+    ProfScope _prof(ctx, "bal_mark_internal", (double)nI[l + 1] * 20);
+    k_mark_internal<<<grid_for(nI[l + 1], 256), 256, 0, s>>>(I[l + 1].get(), nI[l + 1], I[l].get(), nI[l], R[l].get(),
+                                                             ctx.d_flags);
+    DG_LAUNCH_CHECK();
+    }
+  }
+  check_device_flags(ctx, "balanceOctree");
+  // bottom-up leaf counts
+  std::vector<DBuf<uint64_t>> sub(maxL + 1);
+  for (int l = (int)maxL - 1; l >= 0; l--) {
+    if (!nI[l]) continue;
+    sub[l].alloc(nI[l], s);
+    {
+    ProfScope _prof(ctx, "bal_subtree_count", (double)nI[l] * 72);
+    k_subtree_count<<<grid_for(nI[l], 256), 256, 0, s>>>(R[l].get(), nI[l], sub[l + 1].get(), sub[l].get());
+    DG_LAUNCH_CHECK();
+    }
+  }
+  size_t total = (size_t)read_scalar(ctx, sub[0].get());
+  DBuf<Key128> res(total, s);
+  // top-down placement
+  DBuf<uint64_t> off_cur(1, s);
+  DG_CUDA(cudaMemsetAsync(off_cur.get(), 0, sizeof(uint64_t), s));
+  for (unsigned l = 0; l < maxL; l++) {
+    if (!nI[l]) break;
+    DBuf<uint64_t> off_next(nI[l + 1] ? nI[l + 1] : 1, s);
+    {
+    ProfScope _prof(ctx, "bal_place", (double)nI[l] * 24);
+    k_place<<<grid_for(nI[l], 256), 256, 0, s>>>(I[l].get(), nI[l], l, D, R[l].get(), sub[l + 1].get(), off_cur.get(),
+                                                 off_next.get(), res.get());
+    DG_LAUNCH_CHECK();
+    }
+    off_cur = std::move(off_next);
+  }
+  DG_CUDA(cudaStreamSynchronize(s));
+  out.n = total;
+  out.keys = res.release_ptr();
+}
+
+// ------------------------------------------------------------------------
+// conversions
+// ------------------------------------------------------------------------
+__global__ void k_to_xyzl(const Key128 *__restrict__ k, size_t n, uint4 *__restrict__ out) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t x, y, z;
+  demorton3(tag_anchor(k[i]), x, y, z);
+  out[i] = make_uint4(x, y, z, tag_level(k[i]));
+}
+
+__global__ void k_from_xyzl(const uint4 *__restrict__ in, size_t n, unsigned D, Key128 *__restrict__ out,
+                            uint32_t *flags) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint4 v = in[i];
+  unsigned lev = v.w & 31u;
+  uint64_t len = 1ull << (D - min(lev, D));
+  uint64_t dom = 1ull << D;
+  bool ok = lev <= D && v.x % len == 0 && v.y % len == 0 && v.z % len == 0 && v.x < dom && v.y < dom && v.z < dom;
+  if (!ok) atomicOr(flags, DGF_DOMAIN);
+  out[i] = make_tagged(morton3(v.x, v.y, v.z), lev);
+}
+
+void octree_to_xyzl(Context &ctx, const Octree &o, uint32_t *d_xyzl) {
+  if (!o.n) return;
+  {
+    ProfScope _prof("to_xyzl", (double)o.n * 32);
+    k_to_xyzl<<<grid_for(o.n, 256), 256, 0, ctx.stream>>>(o.keys, o.n, reinterpret_cast<uint4 *>(d_xyzl));
+    DG_LAUNCH_CHECK();
+  }
+}
+
+void octree_from_xyzl(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned D, Octree &out) {
+  out.max_depth = D;
+  out.n = n;
+  DBuf<Key128> k(n, ctx.stream);
+  if (n) {
+    {
+      ProfScope _prof("from_xyzl", (double)n * 32);
+      k_from_xyzl<<<grid_for(n, 256), 256, 0, ctx.stream>>>(reinterpret_cast<const uint4 *>(d_xyzl), n, D, k.get(),
+                                                            ctx.d_flags);
+      DG_LAUNCH_CHECK();
+    }
+    check_device_flags(ctx, "octree upload");
+  }
+  out.keys = k.release_ptr();
+}
+
+void octree_free(Context &ctx, Octree &o) {
+  if (o.keys) cudaFreeAsync(o.keys, ctx.stream);
+  o.keys = nullptr;
+  o.n = 0;
+}
+
+}  // namespace dg

@@ -1,0 +1,45 @@
+// Device-resident linear octrees and the construction / balance pipelines.
+#pragma once
+
+#include "dg_prims.cuh"
+
+namespace dg {
+
+// An octant is one 16-byte tagged key: the Morton index of its anchor at the
+// finest level D in bits [0, 3D) and its level in the top byte (bits
+// 120..127).  A linear octree is a sorted array of tagged keys; ordering
+// compares the anchor bits only.
+constexpr uint64_t TAG_MASK = 0x00ffffffffffffffull;
+
+__host__ __device__ __forceinline__ unsigned tag_level(Key128 k) { return (unsigned)(k.hi >> 56); }
+__host__ __device__ __forceinline__ Key128 tag_anchor(Key128 k) { return Key128{k.lo, k.hi & TAG_MASK}; }
+__host__ __device__ __forceinline__ Key128 make_tagged(Key128 anchor, unsigned lev) {
+  return Key128{anchor.lo, (anchor.hi & TAG_MASK) | ((uint64_t)lev << 56)};
+}
+
+struct Octree {
+  unsigned max_depth = 0;
+  size_t n = 0;
+  Key128 *keys = nullptr;  // tagged, sorted
+};
+
+void octree_free(Context &ctx, Octree &o);
+
+// ot::points2Octree (src/construct.cpp:759) on device-resident FP64 xyz.
+void points_to_octree(Context &ctx, const double *d_xyz, size_t n, const double glens[3], unsigned max_depth,
+                      unsigned max_pts, Octree &out);
+
+// Morton sort of level-D point anchors (par::sampleSort / removeDuplicates
+// step); returns sorted tagged keys in d_out and the number of distinct
+// points.
+size_t sort_points(Context &ctx, const double *d_xyz, size_t n, const double glens[3], unsigned max_depth,
+                   Key128 *d_out, bool *has_duplicates);
+
+// ot::balanceOctree(incCorner = 1) (src/balance.cpp:31).
+void balance_octree(Context &ctx, const Octree &in, Octree &out);
+
+// conversions between tagged keys and {x, y, z, level} u32 records
+void octree_to_xyzl(Context &ctx, const Octree &o, uint32_t *d_xyzl);
+void octree_from_xyzl(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned max_depth, Octree &out);
+
+}  // namespace dg

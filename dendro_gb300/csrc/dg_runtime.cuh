@@ -1,0 +1,199 @@
+// Runtime plumbing for the GB300 octree library: the per-handle context
+// (stream, device error word, scratch counters), stream-ordered device
+// buffers and error propagation.  Every C-ABI entry point runs on the
+// context's stream; a context is used by one host thread at a time.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "dg_common.cuh"
+
+namespace dg {
+
+// per-kernel timing (enabled by dg_ctx_profile): CUDA events around the
+// launches on the context's stream, resolved when an API call completes
+struct ProfStat {
+  double ms = 0.0;
+  uint64_t launches = 0;
+  double bytes = 0.0;  // algorithmic bytes moved by those launches
+};
+struct ProfPending {
+  std::string name;
+  cudaEvent_t a, b;
+  double bytes;
+};
+
+struct Context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  uint32_t *d_flags = nullptr;     // device error bitmask (DGF_*)
+  unsigned long long *d_scratch = nullptr;  // small device counters
+  unsigned long long *h_scratch = nullptr;  // pinned mirror of d_scratch
+  int num_sms = 0;
+  std::string last_error;
+  // stencil tables (FP64 and FP32) on the device, created on first use
+  double *d_sten64 = nullptr;
+  float *d_sten32 = nullptr;
+  uint8_t *d_etype_of = nullptr;   // [8][256] -> element type or 255
+  uint8_t *d_etype_mask = nullptr; // [8][18] -> hanging mask
+  bool prof = false;
+  std::map<std::string, ProfStat> prof_stats;
+  std::vector<ProfPending> prof_pending;
+  std::vector<cudaEvent_t> prof_pool;
+};
+
+// thrown inside the library, converted to a status code at the C ABI
+struct Error {
+  int code;
+  std::string msg;
+};
+
+[[noreturn]] inline void fail(int code, const std::string &msg) { throw Error{code, msg}; }
+
+inline void check_cuda(cudaError_t e, const char *what, const char *file, int line) {
+  if (e != cudaSuccess) {
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    fail(e == cudaErrorMemoryAllocation ? DG_ERR_OUT_OF_MEMORY : DG_ERR_CUDA, buf);
+  }
+}
+#define DG_CUDA(call) ::dg::check_cuda((call), #call, __FILE__, __LINE__)
+#define DG_LAUNCH_CHECK() ::dg::check_cuda(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
+
+// Stream-ordered device buffer (cudaMallocAsync from the device's default
+// pool; the pool keeps freed blocks for reuse by later calls).
+template <typename T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaStream_t s = nullptr;
+  DBuf() = default;
+  DBuf(size_t count, cudaStream_t stream) { alloc(count, stream); }
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  DBuf(DBuf &&o) noexcept : p(o.p), n(o.n), s(o.s) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  DBuf &operator=(DBuf &&o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      n = o.n;
+      s = o.s;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
+  void alloc(size_t count, cudaStream_t stream) {
+    release();
+    s = stream;
+    n = count;
+    if (count) DG_CUDA(cudaMallocAsync((void **)&p, count * sizeof(T), stream));
+  }
+  void release() {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+    n = 0;
+  }
+  ~DBuf() { release(); }
+  T *get() const { return p; }
+  T *release_ptr() {
+    T *q = p;
+    p = nullptr;
+    n = 0;
+    return q;
+  }
+};
+
+inline unsigned grid_for(size_t n, unsigned block, unsigned max_blocks = 1u << 30) {
+  size_t g = (n + block - 1) / block;
+  if (g == 0) g = 1;
+  if (g > max_blocks) g = max_blocks;
+  return (unsigned)g;
+}
+
+// synchronously read one small device value through the pinned mirror
+template <typename T>
+inline T read_scalar(Context &ctx, const T *dptr) {
+  DG_CUDA(cudaMemcpyAsync(ctx.h_scratch, dptr, sizeof(T), cudaMemcpyDeviceToHost, ctx.stream));
+  DG_CUDA(cudaStreamSynchronize(ctx.stream));
+  T v;
+  std::memcpy(&v, ctx.h_scratch, sizeof(T));
+  return v;
+}
+
+inline cudaEvent_t prof_event(Context &c) {
+  if (!c.prof_pool.empty()) {
+    cudaEvent_t e = c.prof_pool.back();
+    c.prof_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  DG_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+// the context of the C-ABI call running on this thread (for primitives
+// that only receive a stream)
+inline Context *&current_context() {
+  static thread_local Context *c = nullptr;
+  return c;
+}
+
+// RAII timing scope around one kernel launch (no-op unless profiling)
+struct ProfScope {
+  Context *c = nullptr;
+  cudaEvent_t a = nullptr;
+  const char *name;
+  double bytes;
+  ProfScope(Context &ctx, const char *nm, double b) : name(nm), bytes(b) { start(&ctx); }
+  ProfScope(const char *nm, double b) : name(nm), bytes(b) { start(current_context()); }
+  void start(Context *ctx) {
+    if (!ctx || !ctx->prof) return;
+    c = ctx;
+    a = prof_event(*ctx);
+    cudaEventRecord(a, ctx->stream);
+  }
+  ~ProfScope() {
+    if (!c) return;
+    cudaEvent_t b = nullptr;
+    try {
+      b = prof_event(*c);
+    } catch (...) {
+      return;
+    }
+    cudaEventRecord(b, c->stream);
+    c->prof_pending.push_back(ProfPending{name, a, b, bytes});
+  }
+};
+
+// fold completed timing events into the statistics (stream must be idle)
+inline void prof_resolve(Context &c) {
+  for (auto &p : c.prof_pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      ProfStat &st = c.prof_stats[p.name];
+      st.ms += ms;
+      st.launches += 1;
+      st.bytes += p.bytes;
+    }
+    c.prof_pool.push_back(p.a);
+    c.prof_pool.push_back(p.b);
+  }
+  c.prof_pending.clear();
+}
+
+// read and clear the device error word; throw on any flag
+void check_device_flags(Context &ctx, const char *where);
+
+}  // namespace dg

@@ -1,0 +1,144 @@
+/*
+ * dendro_gb300 — C ABI of the GB300 octree hot path.
+ *
+ * One library, one GPU, no inter-GPU communication.  Each entry point
+ * replaces one function of the reference (Dendro4) C++ API at one MPI rank;
+ * the reference function is cited beside it (paths inside the Dendro4
+ * source tree).  Plain pointers and sizes only.
+ *
+ * Conventions
+ *   - Every function returns int: DG_OK (0) on success, a DG_ERR_* code
+ *     otherwise; dg_ctx_last_error() returns the message of the last failure
+ *     on that context.  (The reference returns 1 from ot::/par:: functions
+ *     and asserts on errors; the C++ mirror in include/dendro_gb300.hpp maps
+ *     back to that convention.)
+ *   - Pointer arguments flagged `*_on_device` are CUDA device pointers when
+ *     the flag is nonzero, host pointers otherwise.  Host pointers may be
+ *     pageable or pinned; pinned memory gives the full link bandwidth.
+ *   - Octants are exchanged as 4 x uint32 records {x, y, z, level} (the
+ *     anchor and level fields of ot::TreeNode, include/TreeNode.h:42) in the
+ *     reference's Morton order.
+ *   - A context owns a CUDA stream; calls on one context are serialised on
+ *     it and return once their results are complete.  Handles (octrees,
+ *     meshes) keep their data resident in device memory until freed.
+ *   - The reference's MPI_Comm parameters are represented by `comm_size`
+ *     where an entry point takes one: only 1 is accepted (DG_ERR_COMM_SIZE
+ *     otherwise).
+ */
+#ifndef DENDRO_GB300_H
+#define DENDRO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DG_OK 0
+#define DG_ERR_INVALID_ARG 1
+#define DG_ERR_OUT_OF_MEMORY 2
+#define DG_ERR_CUDA 3
+#define DG_ERR_DOMAIN 4       /* a point outside [0, gLen)^3, or NaN */
+#define DG_ERR_NOT_BALANCED 5 /* mesh input is not a complete 2:1 balanced octree */
+#define DG_ERR_TIMEOUT 6
+#define DG_ERR_INTERNAL 7
+#define DG_ERR_COMM_SIZE 8
+#define DG_ERR_UNSUPPORTED 9
+
+typedef struct dg_ctx_s *dg_ctx;
+typedef struct dg_octree_s *dg_octree;
+typedef struct dg_da_s *dg_da;
+
+/* ---- context ------------------------------------------------------------
+ * Replaces the per-rank global state the reference sets up in
+ * _InitializeHcurve (src/hcurvedata.cpp:23) and ot::DA_Initialize
+ * (src/oda/odaUtils.cpp:3352): here the SFC is always Morton and the
+ * stencil tables are generated on the device on first use. */
+int dg_ctx_create(int device, dg_ctx *out);
+int dg_ctx_destroy(dg_ctx ctx);
+/* Run subsequent calls on an external cudaStream_t (NULL: the context's own). */
+int dg_ctx_set_stream(dg_ctx ctx, void *cuda_stream);
+const char *dg_ctx_last_error(dg_ctx ctx);
+const char *dg_status_string(int status);
+int dg_version(void);
+
+/* ---- ot::points2Octree ---------------------------------------------------
+ * include/octUtils.h:633 / src/construct.cpp:759 (1-rank branch :767-770 ->
+ * points2OctreeSeq :911).  xyz holds n points, x y z interleaved (FP64).
+ * Unlike the reference, xyz is not cleared.  A point whose quantised
+ * coordinate falls outside [0, 2^maxDepth) is rejected (DG_ERR_DOMAIN); the
+ * reference would produce an octant outside the domain. */
+int dg_points_to_octree(dg_ctx ctx, const double *xyz, size_t n, const double gLens[3], unsigned maxDepth,
+                        unsigned maxNumPtsPerOctant, int comm_size, int xyz_on_device, dg_octree *out);
+
+/* ---- par::sampleSort + par::removeDuplicates of point octants -------------
+ * include/parUtils.h:424,437 (1-rank branch parUtils.tcc:1868-1875): the
+ * points quantised to level maxDepth, sorted in Morton order, duplicates
+ * removed.  Writes up to n records {x, y, z, maxDepth} to out_xyzl and the
+ * count to *n_unique. */
+int dg_sort_unique_points(dg_ctx ctx, const double *xyz, size_t n, const double gLens[3], unsigned maxDepth,
+                          int xyz_on_device, uint32_t *out_xyzl, int out_on_device, size_t *n_unique);
+
+/* ---- ot::balanceOctree(incCorner = true) ----------------------------------
+ * include/octUtils.h:692 / src/balance.cpp:31 (1-rank branch :54-63).  The
+ * input must be sorted, linear and complete (the reference's assumption).
+ * incCorner = 0 is not supported (DG_ERR_UNSUPPORTED).  The input handle is
+ * left intact (the reference clears `in`). */
+int dg_balance_octree(dg_ctx ctx, dg_octree in, int incCorner, int comm_size, dg_octree *out);
+
+/* ---- octree handles --------------------------------------------------------
+ * Materialise / import the std::vector<ot::TreeNode> of the reference as
+ * {x, y, z, level} records. */
+int dg_octree_size(dg_octree o, size_t *n, unsigned *maxDepth);
+int dg_octree_download(dg_ctx ctx, dg_octree o, uint32_t *xyzl, int dst_on_device);
+int dg_octree_upload(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDepth, int src_on_device, dg_octree *out);
+int dg_octree_free(dg_ctx ctx, dg_octree o);
+
+/* ---- ot::DA ----------------------------------------------------------------
+ * include/oda/oda.h:622 / src/oda/oda.cpp:250 at one rank: element -> node
+ * map with hanging vertices resolved to the parent's vertex
+ * (getNodeIndices, include/oda/oda.tcc:1304), child numbers
+ * (getChildNumber, oda.tcc:1273), hanging masks (getHangingNodeIndex,
+ * src/oda/oda.cpp:1038) and element types (GET_ETYPE_BLOCK,
+ * include/oda/odaUtils.h:379).  Node numbering differs from the
+ * reference's buffer layout; nodes are identified by coordinates
+ * (dg_da_download node_xyz). */
+int dg_da_build(dg_ctx ctx, dg_octree balanced, dg_da *out);
+int dg_da_sizes(dg_da da, size_t *n_elem, size_t *n_node);
+/* Any output pointer may be NULL.  meta[e] = level | child<<8 | hmask<<16 |
+ * etype<<24; nodes is 8*n_elem, element-major (nodes[8e+k]); node_xyz is
+ * 3*n_node, point-major (x y z per node), coordinates at the octree's
+ * maxDepth scale, vertices in [0, 2^maxDepth]. */
+int dg_da_download(dg_ctx ctx, dg_da da, uint32_t *meta, uint32_t *nodes, uint32_t *node_xyz, int dst_on_device);
+int dg_da_free(dg_ctx ctx, dg_da da);
+
+/* ---- Jacobian1MatMult ------------------------------------------------------
+ * examples/src/backend/odaJac.C:294-377 (element block :275-292, the
+ * PETSc MatShell MATOP_MULT callback of examples/include/odaJac.h:35):
+ * out = (lapFac * Laplacian + massFac * mass) in, nodal vectors of n_node
+ * entries in dg_da node order.  precision 64: FP64 in/out (double*);
+ * precision 32: FP32 in/out (float*).  lapFac and massFac play the role of
+ * the -lapMatPropFac / -massMatPropFac options (odaJac.C:302-306). */
+int dg_matvec(dg_ctx ctx, dg_da da, const void *in, void *out, int precision, double lapFac, double massFac,
+              int on_device);
+
+/* ---- timing ---------------------------------------------------------------
+ * Milliseconds of device time spent by the last completed call on ctx
+ * (CUDA events on the context's stream). */
+int dg_ctx_last_device_ms(dg_ctx ctx, double *ms);
+
+/* Per-kernel timing: while enabled, every kernel launch of the library is
+ * bracketed by CUDA events on the context's stream and accumulated by kernel
+ * name (total device ms, launch count, algorithmic bytes moved).  Enabling
+ * or disabling clears the statistics.  No counterpart in the reference (it
+ * logs PETSc events, src/sys.cpp:19). */
+int dg_ctx_profile(dg_ctx ctx, int enable);
+int dg_ctx_profile_count(dg_ctx ctx, int *count);
+int dg_ctx_profile_entry(dg_ctx ctx, int index, char *name, size_t name_len, double *total_ms,
+                         unsigned long long *launches, double *bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

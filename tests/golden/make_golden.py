@@ -1,0 +1,172 @@
+"""Generate the golden fixtures of tests/golden from the REFERENCE itself.
+
+Runs the reference's own code (oracle/_ref/ref_driver, built from the
+reference sources by oracle/Makefile) on seeded inputs and stores its
+outputs next to the inputs:
+
+  ref_cases.npz   points2Octree and balanceOctree outputs for small inputs
+  ref_da.npz      ot::DA element data and one Laplacian+mass matVec
+  ref_tables.npz  element-type masks (include/oda/cnumEtypes.h) and
+                  statistics of the type-2 stencil tables (Stencils/*.inp)
+  ref_hashes.json counts and FNV-1a hashes of larger octrees
+
+Usage:  python tests/golden/make_golden.py [/path/to/reference]
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from dendro_gb300 import datagen  # noqa: E402
+from tests.golden import cases  # noqa: E402
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+
+
+def run(*args):
+    r = subprocess.run([DRIVER, *map(str, args)], capture_output=True, text=True, check=True)
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def write_pts(path, p):
+    with open(path, "wb") as f:
+        f.write(np.uint64(len(p)).tobytes())
+        f.write(np.ascontiguousarray(p, np.float64).tobytes())
+
+
+def read_oct(path):
+    b = open(path, "rb").read()
+    n = int(np.frombuffer(b[:8], np.uint64)[0])
+    return np.frombuffer(b[8:], np.uint32).reshape(n, 4).copy()
+
+
+def write_oct(path, o):
+    with open(path, "wb") as f:
+        f.write(np.uint64(len(o)).tobytes())
+        f.write(np.ascontiguousarray(o, np.uint32).tobytes())
+
+
+def fnv1a(o):
+    h = 1469598103934665603
+    for byte in np.ascontiguousarray(o, np.uint32).tobytes():
+        h ^= byte
+        h = (h * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    return h
+
+
+def ref_p2o_bal(tmp, name, pts, depth, maxpts):
+    """Reference points2Octree then balanceOctree; the balanced octree is
+    None when the reference aborts (it asserts on octants outside the domain,
+    which its construction emits for some inputs with repeated points)."""
+    pf, of, bf = (os.path.join(tmp, f"{name}.{e}") for e in ("pts", "oct", "bal"))
+    write_pts(pf, pts)
+    run("p2o", pf, depth, maxpts, of)
+    lin = read_oct(of)
+    try:
+        run("bal", of, depth, 1, 1, bf)
+    except subprocess.CalledProcessError:
+        return lin, None
+    return lin, read_oct(bf)
+
+
+def main():
+    if not os.path.exists(DRIVER):
+        subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), f"REF={REF}"])
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, (fn, depth, maxpts) in cases.SMALL.items():
+            pts = fn()
+            lin, bal = ref_p2o_bal(tmp, name, pts, depth, maxpts)
+            out[f"{name}/pts"] = pts
+            out[f"{name}/lin"] = lin
+            out[f"{name}/bal_aborted"] = np.bool_(bal is None)
+            if bal is None:
+                bal = np.zeros((0, 4), np.uint32)
+            # large balanced outputs are kept as count + FNV-1a only
+            out[f"{name}/bal_n"] = np.int64(len(bal))
+            out[f"{name}/bal_fnv"] = np.uint64(fnv1a(bal))
+            out[f"{name}/bal"] = bal if len(bal) <= 50000 else np.zeros((0, 4), np.uint32)
+            out[f"{name}/params"] = np.array([depth, maxpts], np.int64)
+        np.savez_compressed(os.path.join(HERE, "ref_cases.npz"), **out)
+
+        # DA + matVec on a small balanced octree
+        pts = cases.da_points()
+        _, bal = ref_p2o_bal(tmp, "da", pts, 30, 1)
+        bf = os.path.join(tmp, "da.bal")
+        write_oct(bf, bal)
+        # nodes of the DA are only known after the DA is built: first pass
+        # without a vector gives the element dump (node coordinates)
+        prefix = os.path.join(tmp, "da")
+        run("da", bf, 30, os.path.join(REF, "Stencils"), "-", prefix)
+        e = open(prefix + ".elem", "rb").read()
+        ne = int(np.frombuffer(e[:8], np.uint64)[0])
+        E = np.frombuffer(e[8:], np.uint32).reshape(ne, 28)
+        node_xyz = np.unique(E[:, 4:].reshape(-1, 3), axis=0)
+        vals = cases.nodal_function(node_xyz)
+        rec = np.zeros(len(node_xyz), dtype=[("x", "<u4"), ("y", "<u4"), ("z", "<u4"), ("p", "<u4"), ("v", "<f8")])
+        rec["x"], rec["y"], rec["z"] = node_xyz.T
+        rec["v"] = vals
+        vf = os.path.join(tmp, "vec.bin")
+        with open(vf, "wb") as f:
+            f.write(np.uint64(len(rec)).tobytes())
+            f.write(rec.tobytes())
+        info = run("da", bf, 30, os.path.join(REF, "Stencils"), vf, prefix)
+        m = open(prefix + ".mv", "rb").read()
+        R = np.frombuffer(m[8:], dtype=rec.dtype)
+        meta = E[:, 3]
+        np.savez_compressed(
+            os.path.join(HERE, "ref_da.npz"),
+            bal=bal,
+            level=(meta & 255).astype(np.uint8),
+            child=((meta >> 8) & 255).astype(np.uint8),
+            hmask=((meta >> 16) & 255).astype(np.uint8),
+            etype=(meta >> 24).astype(np.uint8),
+            elem_node_xyz=E[:, 4:].reshape(ne, 8, 3),
+            mv_xyz=np.stack([R["x"], R["y"], R["z"]], 1),
+            mv_val=R["v"].copy(),
+            n_nodes=np.int64(info["n_nodes_da"]),
+        )
+
+        # larger cases: hashes only
+        hashes = {}
+        for name, (fn, depth, maxpts) in cases.LARGE.items():
+            lin, bal = ref_p2o_bal(tmp, name, fn(), depth, maxpts)
+            hashes[name] = {"n_lin": len(lin), "fnv_lin": f"{fnv1a(lin):016x}", "n_bal": len(bal),
+                            "fnv_bal": f"{fnv1a(bal):016x}"}
+        with open(os.path.join(HERE, "ref_hashes.json"), "w") as f:
+            json.dump(hashes, f, indent=1, sort_keys=True)
+
+    # tables
+    src = open(os.path.join(REF, "include", "oda", "cnumEtypes.h")).read()
+    blocks = re.split(r"class cNumEtype<(\d)>", src)[1:]
+    order = ["ET_N", "ET_Y", "ET_X", "ET_XY", "ET_Z", "ET_ZY", "ET_ZX", "ET_ZXY", "ET_XY_XY", "ET_XY_ZXY", "ET_YZ_ZY",
+             "ET_YZ_ZXY", "ET_YZ_XY_ZXY", "ET_ZX_ZX", "ET_ZX_ZXY", "ET_ZX_XY_ZXY", "ET_ZX_YZ_ZXY", "ET_ZX_YZ_XY_ZXY"]
+    masks = np.zeros((8, 18), np.uint8)
+    for i in range(0, len(blocks), 2):
+        c = int(blocks[i])
+        d = dict(re.findall(r"(ET_\w+)\s*=\s*(\d+)", blocks[i + 1]))
+        masks[c] = [int(d[k]) for k in order]
+
+    def stats(fname):
+        a = np.array(open(os.path.join(REF, "Stencils", fname)).read().split(), np.float64).reshape(8, 18, 8, 8)
+        w = np.arange(1, 65, dtype=np.float64).reshape(8, 8)
+        return np.stack([a.sum((2, 3)), (a * a).sum((2, 3)), (a * w).sum((2, 3)), a[:, :, 0, :].sum(2)], -1)
+
+    np.savez_compressed(os.path.join(HERE, "ref_tables.npz"), etype_masks=masks, lap_stats=stats("LapType2Stencils.inp"),
+                        mass_stats=stats("MassType2Stencils.inp"))
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,75 @@
+"""The C ABI library builds, loads and exports every declared symbol (CPU only;
+no compute call is made without a GPU)."""
+import ctypes
+import os
+import subprocess
+
+import pytest
+
+from dendro_gb300 import _lib
+from dendro_gb300 import build as cuda_build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_builds_for_sm103a():
+    path = cuda_build.build()
+    assert os.path.exists(path)
+    assert "arch=compute_103a,code=sm_103a" in " ".join(cuda_build.NVCC_FLAGS)
+
+
+def test_exports_every_header_symbol():
+    L = _lib.load()
+    names = _lib.header_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_exported_symbols_are_c_linkage():
+    out = subprocess.run(["nm", "-D", "--defined-only", cuda_build.LIB], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    for n in _lib.header_functions():
+        assert n in exported, n
+
+
+def test_status_strings_without_gpu():
+    L = _lib.load()
+    assert L.dg_version() >= 1
+    assert L.dg_status_string(0) == b"ok"
+    assert L.dg_status_string(8) == b"communicator size must be 1"
+
+
+def test_invalid_arguments_rejected_before_any_gpu_work():
+    L = _lib.load()
+    # null context / null outputs return DG_ERR_INVALID_ARG without touching a device
+    assert L.dg_ctx_destroy(None) == 1
+    out = ctypes.c_void_p()
+    assert L.dg_points_to_octree(None, None, 0, None, 30, 1, 1, 0, ctypes.byref(out)) == 1
+    assert L.dg_points_to_octree(None, None, 0, (ctypes.c_double * 3)(1, 1, 1), 30, 1, 2, 0, ctypes.byref(out)) == 8
+    assert L.dg_matvec(None, None, None, None, 64, 1.0, 1.0, 0) == 1
+
+
+def test_product_fails_loudly_without_gpu():
+    import dendro_gb300
+
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    with pytest.raises(dendro_gb300.DendroError):
+        dendro_gb300.Context(0)
+
+
+def test_no_oracle_in_product_sources():
+    pkg = os.path.join(ROOT, "dendro_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        if "_build" in dirpath:
+            continue
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
+                text = open(os.path.join(dirpath, f)).read()
+                assert "oracle" not in text.replace("the oracle", ""), f

@@ -1,0 +1,167 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle.
+
+Octrees must be bit-exact; the FP64 matVec within 1e-12 relative (L2) of
+the oracle's FP64 element loop, the FP32 matVec within 1e-6 relative of it.
+"""
+import numpy as np
+import pytest
+
+from dendro_gb300 import DA, DendroError, Octree, balanceOctree, datagen, points2Octree, sortUniquePoints
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-12
+FP32_RTOL = 1e-6
+
+
+def clustered(n, seed):
+    """Points packed into a few tiny boxes: leaves down to maxDepth."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    c = rng.uniform(0.2, 0.8, size=(4, 3))
+    p = c[rng.integers(0, 4, n)] + rng.uniform(0, 2.0 ** -27, size=(n, 3))
+    return p
+
+
+def boundary(n, seed):
+    """Points on and next to the faces, edges and corners of the unit cube."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    p = rng.uniform(0, 1, size=(n, 3))
+    hi = np.nextafter(1.0, 0.0)
+    for a in range(3):
+        sel = rng.random(n) < 0.3
+        p[sel, a] = rng.choice([0.0, hi, 0.5, 2.0 ** -30, 1 - 2.0 ** -30], size=sel.sum())
+    return p
+
+
+CASES = {
+    "gauss": lambda: datagen.gaussian(20000, 0.5, 0.1, seed=5),
+    "lognormal": lambda: datagen.lognormal(20000, seed=6),
+    "mixture": lambda: datagen.mixture(15000, np.random.Generator(np.random.PCG64(7))),
+    "clustered": lambda: clustered(3000, 8),
+    "boundary": lambda: boundary(4000, 9),
+    "one": lambda: np.array([[0.3, 0.6, 0.9]]),
+    "two": lambda: np.array([[0.1, 0.1, 0.1], [0.1 + 2.0 ** -30, 0.1, 0.1]]),
+}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+@pytest.mark.parametrize("max_pts", [1, 3])
+def test_points2octree_bit_exact(ctx, oracle, case, max_pts):
+    pts = CASES[case]()
+    ref = oracle.points_to_octree(pts, 30, max_pts)
+    got = points2Octree(pts, maxDepth=30, maxNumPtsPerOctant=max_pts, ctx=ctx).to_numpy()
+    assert got.shape == ref.shape
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("max_depth", [30, 12, 4])
+def test_points2octree_depths(ctx, oracle, max_depth):
+    pts = datagen.gaussian(5000, 0.5, 0.2, seed=11)
+    ref = oracle.points_to_octree(pts, max_depth, 1)
+    got = points2Octree(pts, maxDepth=max_depth, maxNumPtsPerOctant=1, ctx=ctx).to_numpy()
+    assert np.array_equal(got, ref)
+
+
+def test_points2octree_duplicates_follow_reference_walk(ctx, oracle):
+    # repeated points make the reference walk skip refinements; the CUDA
+    # path detects them and runs the walk verbatim
+    base = datagen.gaussian(3000, 0.5, 0.1, seed=12)
+    pts = np.concatenate([base, base[::7], base[::13]])
+    ref = oracle.points_to_octree(pts, 30, 1)
+    got = points2Octree(pts, maxDepth=30, maxNumPtsPerOctant=1, ctx=ctx).to_numpy()
+    assert np.array_equal(got, ref)
+
+
+def test_sort_unique_points(ctx, oracle):
+    base = datagen.lognormal(30000, seed=13)
+    pts = np.concatenate([base, base[:500]])
+    ref = oracle.quantize_sort(pts, 30)
+    keep = np.ones(len(ref), bool)
+    keep[1:] = np.any(ref[1:] != ref[:-1], axis=1)
+    got = sortUniquePoints(pts, maxDepth=30, ctx=ctx)
+    assert np.array_equal(got, ref[keep])
+
+
+def test_domain_error(ctx):
+    with pytest.raises(DendroError) as e:
+        points2Octree(np.array([[0.5, 0.5, 1.0], [0.1, 0.2, 0.3]]), ctx=ctx)
+    assert e.value.status == 4
+    with pytest.raises(DendroError):
+        points2Octree(np.array([[np.nan, 0.5, 0.5], [0.1, 0.2, 0.3]]), ctx=ctx)
+
+
+@pytest.mark.parametrize("case", ["gauss", "lognormal", "mixture", "clustered", "boundary", "one", "two"])
+def test_balance_bit_exact(ctx, oracle, case):
+    pts = CASES[case]()
+    lin = oracle.points_to_octree(pts, 30, 1)
+    ref = oracle.balance(lin, 30)
+    got = balanceOctree(Octree.from_numpy(lin, 30, ctx=ctx)).to_numpy()
+    assert np.array_equal(got, ref)
+    assert all(oracle.checks(got, 30).values())
+
+
+def test_pipeline_resident(ctx, oracle):
+    pts = datagen.gaussian(50000, 0.5, 0.1, seed=14)
+    lin = points2Octree(pts, ctx=ctx)
+    bal = balanceOctree(lin)
+    ref = oracle.balance(oracle.points_to_octree(pts, 30, 1), 30)
+    assert np.array_equal(bal.to_numpy(), ref)
+
+
+def _da_parity(ctx, oracle, bal):
+    oda = oracle.DA(bal, 30)
+    da = DA(Octree.from_numpy(bal, 30, ctx=ctx))
+    assert da.n_elem == oda.n_elem
+    assert da.n_node == oda.n_node
+    d = da.download()
+    assert np.array_equal(d["level"], oda.level)
+    assert np.array_equal(d["child"], oda.child)
+    assert np.array_equal(d["hmask"], oda.hmask)
+    assert np.array_equal(d["etype"], oda.etype)
+    # element -> node maps agree by node coordinates
+    assert np.array_equal(d["node_xyz"][d["nodes"]], oda.node_xyz[oda.nodes])
+    return da, oda, d
+
+
+def _to_oracle_order(d, oda):
+    """permutation p with gpu_node[p[i]] == oracle node i (by coordinates)"""
+    def key(x):
+        x = x.astype(np.uint64)
+        return (x[:, 0] << np.uint64(42)) | (x[:, 1] << np.uint64(21)) | x[:, 2]
+    kg, ko = key(d["node_xyz"]), key(oda.node_xyz)
+    og = np.argsort(kg)
+    pos = np.searchsorted(kg[og], ko)
+    p = og[pos]
+    assert np.array_equal(kg[p], ko)
+    return p
+
+
+@pytest.mark.parametrize("case", ["gauss", "lognormal", "clustered", "boundary", "one"])
+def test_da_and_matvec(ctx, oracle, case):
+    pts = CASES[case]()
+    bal = oracle.balance(oracle.points_to_octree(pts, 30, 1), 30)
+    da, oda, d = _da_parity(ctx, oracle, bal)
+    p = _to_oracle_order(d, oda)
+    rng = np.random.Generator(np.random.PCG64(1))
+    x_o = rng.uniform(-1.0, 1.0, oda.n_node)
+    y_o = oda.matvec(x_o, 1.0, 1.0)
+    x_g = np.empty(da.n_node)
+    x_g[p] = x_o
+    y64 = da.matvec(x_g, precision=64)[p]
+    assert np.linalg.norm(y64 - y_o) <= FP64_RTOL * np.linalg.norm(y_o)
+    y32 = da.matvec(x_g.astype(np.float32), precision=32)[p].astype(np.float64)
+    assert np.linalg.norm(y32 - y_o) <= FP32_RTOL * np.linalg.norm(y_o)
+    # material factors (-lapMatPropFac / -massMatPropFac)
+    y_f = oda.matvec(x_o, 2.5, 0.25)
+    yg_f = da.matvec(x_g, precision=64, lapFac=2.5, massFac=0.25)[p]
+    assert np.linalg.norm(yg_f - y_f) <= FP64_RTOL * np.linalg.norm(y_f)
+
+
+def test_da_rejects_unbalanced(ctx, oracle):
+    pts = datagen.gaussian(2000, 0.5, 0.1, seed=15)
+    lin = oracle.points_to_octree(pts, 30, 1)
+    if oracle.checks(lin, 30)["balanced"]:
+        pytest.skip("input happens to be balanced")
+    with pytest.raises(DendroError) as e:
+        DA(Octree.from_numpy(lin, 30, ctx=ctx))
+    assert e.value.status == 5
