@@ -19,6 +19,7 @@
 // level is one generate + radix sort + unique; the leaves are then placed in
 // Morton order by a bottom-up leaf count and a top-down offset pass.
 #include "dg_octree.cuh"
+#include "dg_walk.cuh"
 
 #include <algorithm>
 #include <vector>
@@ -159,104 +160,12 @@ __global__ void k_fill_emit(const Key128 *__restrict__ seeds, size_t ns, unsigne
 }
 
 // ------------------------------------------------------------------------
-// the reference walk, verbatim, for inputs with repeated points
-// (construct.cpp:976-1076); one thread; count pass then emit pass
+// the reference walk for inputs with repeated points (dg_walk.cuh)
 // ------------------------------------------------------------------------
-struct WOct {
-  uint32_t x, y, z, lev;
-};
-__device__ __forceinline__ WOct wo_from_key(Key128 k) {
-  WOct o;
-  demorton3(tag_anchor(k), o.x, o.y, o.z);
-  o.lev = tag_level(k);
-  return o;
-}
-__device__ __forceinline__ u128 wo_key(const WOct &o) {
-  return (to_u128(morton3(o.x, o.y, o.z)) << 5) | (u128)(o.lev & 31u);
-}
-__device__ __forceinline__ bool wo_is_anc(const WOct &a, const WOct &b, unsigned D) {
-  if (!(a.lev < b.lev)) return false;
-  uint64_t la = 1ull << (D - a.lev), lb = 1ull << (D - b.lev);
-  return b.x >= a.x && b.y >= a.y && b.z >= a.z && (uint64_t)b.x + lb <= (uint64_t)a.x + la &&
-         (uint64_t)b.y + lb <= (uint64_t)a.y + la && (uint64_t)b.z + lb <= (uint64_t)a.z + la;
-}
-__device__ __forceinline__ WOct wo_next(WOct m, unsigned D) {
-  uint32_t mask = 1u << (D - m.lev);
-  int i;
-  for (i = (int)m.lev; i >= 0; --i) {
-    m.x ^= mask;
-    if (m.x & mask) break;
-    m.y ^= mask;
-    if (m.y & mask) break;
-    m.z ^= mask;
-    if (m.z & mask) break;
-    mask <<= 1;
-  }
-  m.lev = (uint32_t)i;
-  return m;
-}
-__device__ __forceinline__ WOct wo_dld(const WOct &a, unsigned D) {
-  uint32_t l = 1u << (D - a.lev);
-  return WOct{a.x + l - 1, a.y + l - 1, a.z + l - 1, D};
-}
-
 __global__ void k_p2o_walk_serial(const Key128 *__restrict__ pk, size_t n, unsigned m, unsigned D,
                                   Key128 *__restrict__ out, unsigned long long *count) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const uint32_t num_pts = (uint32_t)n;
-  WOct curr{0, 0, 0, 0};
-  WOct last = wo_dld(curr, D);
-  WOct next = wo_next(curr, D);
-  uint32_t curr_pt = 0, next_pt = curr_pt + m;
-  size_t w = 0;
-  u128 prev_key = ~(u128)0;
-  auto push = [&](const WOct &o) {
-    u128 k = wo_key(o);
-    if (k == prev_key) return;  // std::list::unique
-    prev_key = k;
-    if (out) out[w] = make_tagged(morton3(o.x, o.y, o.z), o.lev);
-    w++;
-  };
-  while (next_pt < num_pts) {
-    for (;;) {
-      WOct a = wo_from_key(pk[next_pt - 1]), b = wo_from_key(pk[next_pt]);
-      if (!(wo_is_anc(curr, a, D) && wo_is_anc(curr, b, D) && curr.lev < D)) break;
-      curr.lev++;
-      next = wo_next(curr, D);
-    }
-    uint32_t inc = m;
-    while (curr.lev == D - 1) {
-      inc <<= 1;
-      next_pt += inc;
-      if (next_pt > num_pts) {
-        next_pt = num_pts - 1;
-        break;
-      }
-    }
-    // lower_bound(pts[curr_pt..next_pt), next, less_equal)
-    u128 nk = wo_key(next);
-    uint32_t lo = curr_pt, hi = next_pt;
-    while (lo < hi) {
-      uint32_t mid = lo + (hi - lo) / 2;
-      if (wo_key(wo_from_key(pk[mid])) <= nk) lo = mid + 1;
-      else hi = mid;
-    }
-    int found_pt = (int)(lo - curr_pt);
-    next_pt = curr_pt + (uint32_t)found_pt;
-    push(curr);
-    curr = next;
-    next = wo_next(curr, D);
-    if (next_pt > curr_pt) curr_pt = next_pt;
-    next_pt = curr_pt + m;
-  }
-  u128 lastk = wo_key(last);
-  while (wo_key(curr) <= lastk) {
-    while (wo_key(wo_dld(curr, D)) > lastk && curr.lev < D) curr.lev++;
-    push(curr);
-    if (wo_key(wo_dld(curr, D)) == lastk) break;
-    curr = wo_next(curr, D);
-  }
-  *count = w;
+  *count = p2o_walk(pk, n, m, D, out);
 }
 
 // ------------------------------------------------------------------------
@@ -266,7 +175,7 @@ void check_device_flags(Context &ctx, const char *where) {
   uint32_t f = read_scalar(ctx, ctx.d_flags);
   if (f) {
     DG_CUDA(cudaMemsetAsync(ctx.d_flags, 0, sizeof(uint32_t), ctx.stream));
-    if (f & DGF_DOMAIN) fail(DG_ERR_DOMAIN, std::string(where) + ": a point lies outside [0, gLen)^3");
+    if (f & DGF_DOMAIN) fail(DG_ERR_DOMAIN, std::string(where) + ": input outside the domain");
     if (f & DGF_NOT_BALANCED) fail(DG_ERR_NOT_BALANCED, std::string(where) + ": input is not a complete 2:1 balanced octree");
     if (f & DGF_TIMEOUT) fail(DG_ERR_TIMEOUT, std::string(where) + ": a device wait timed out");
     if (f & DGF_INTERNAL) fail(DG_ERR_INTERNAL, std::string(where) + ": internal consistency check failed");
@@ -348,6 +257,9 @@ void points_to_octree(Context &ctx, const double *d_xyz, size_t n, const double 
       DG_LAUNCH_CHECK();
     }
     size_t cnt = (size_t)read_scalar(ctx, d_cnt);
+    if (cnt == P2O_WALK_NO_END)
+      fail(DG_ERR_INVALID_ARG,
+           "points2Octree: with these repeated points the reference construction walk never terminates");
     DBuf<Key128> res(cnt, s);
     {
       ProfScope _prof("p2o_walk_serial", (double)n * 16 + (double)cnt * 16);
@@ -391,12 +303,22 @@ void points_to_octree(Context &ctx, const double *d_xyz, size_t n, const double 
 // ------------------------------------------------------------------------
 // balance
 // ------------------------------------------------------------------------
-__global__ void k_level_hist(const Key128 *__restrict__ k, size_t n, unsigned long long *hist) {
+// level histogram; flags octants that are not aligned octants of the
+// domain (the reference asserts on those, octFunctions.cpp:310)
+__global__ void k_level_hist(const Key128 *__restrict__ k, size_t n, unsigned D, unsigned long long *hist,
+                             uint32_t *flags) {
   __shared__ unsigned int h[32];
   if (threadIdx.x < 32) h[threadIdx.x] = 0;
   __syncthreads();
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    atomicAdd(&h[tag_level(k[i]) & 31u], 1u);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    Key128 ki = k[i];
+    unsigned l = tag_level(ki);
+    Key128 a = tag_anchor(ki);
+    bool ok = l <= D && key_shr(a, 3 * D).lo == 0 && key_shr(a, 3 * D).hi == 0;
+    if (ok && l < D) ok = key_eq(key_shl(key_shr(a, 3 * (D - l)), 3 * (D - l)), a);
+    if (!ok) atomicOr(flags, DGF_DOMAIN);
+    atomicAdd(&h[l & 31u], 1u);
+  }
   __syncthreads();
   if (threadIdx.x < 32 && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], (unsigned long long)h[threadIdx.x]);
 }
@@ -511,9 +433,10 @@ void balance_octree(Context &ctx, const Octree &in, Octree &out) {
   DG_CUDA(cudaMemsetAsync(d_hist, 0, 32 * sizeof(unsigned long long), s));
   {
     ProfScope _prof("bal_level_hist", (double)n * 16);
-    k_level_hist<<<grid_for(n, 256, ctx.num_sms * 4), 256, 0, s>>>(in.keys, n, d_hist);
+    k_level_hist<<<grid_for(n, 256, ctx.num_sms * 4), 256, 0, s>>>(in.keys, n, D, d_hist, ctx.d_flags);
     DG_LAUNCH_CHECK();
   }
+  check_device_flags(ctx, "balanceOctree (octant outside the domain or misaligned)");
   unsigned long long hcnt[32];
   DG_CUDA(cudaMemcpyAsync(ctx.h_scratch + 16, d_hist, sizeof(hcnt), cudaMemcpyDeviceToHost, s));
   DG_CUDA(cudaStreamSynchronize(s));

@@ -184,7 +184,16 @@ int dgo_p2o_local(const dgo_oct *pts, size_t n, unsigned D, unsigned m, dgo_oct 
   uint32_t next_pt = curr_pt + m;
   int rc = 0;
 
+  /* The walk's getNext climbs above the root after the last octant; at
+   * level "-1" it no longer moves and the reference loops forever.  Report
+   * that state (and a step bound) instead of looping. */
+  const uint64_t max_steps = 64ull * ((uint64_t)n + 1) * (D + 2);
+  uint64_t steps = 0;
   while (next_pt < num_pts) { /* :1009 */
+    if (curr.lev > D || ++steps > max_steps) {
+      rc = DGO_ENOTERM;
+      goto fail;
+    }
     while (is_anc(&curr, &pts[next_pt - 1], D) & is_anc(&curr, &pts[next_pt], D) & (curr.lev < D)) {
       curr = first_child(curr); /* :1013-1018 */
       next = get_next(curr, D);
@@ -209,6 +218,10 @@ int dgo_p2o_local(const dgo_oct *pts, size_t n, unsigned D, unsigned m, dgo_oct 
   }
 
   while (oct_le(&curr, &last)) { /* :1051-1061 */
+    if (curr.lev > D || ++steps > max_steps) {
+      rc = DGO_ENOTERM;
+      goto fail;
+    }
     for (;;) {
       dgo_oct dld = get_dld(&curr, D);
       if (!(oct_lt(&last, &dld) && curr.lev < D)) break;
@@ -308,8 +321,15 @@ int dgo_balance(const dgo_oct *in, size_t n, unsigned D, dgo_oct **out, size_t *
     return 0;
   }
   unsigned maxL = 0;
-  for (size_t i = 0; i < n; i++)
+  for (size_t i = 0; i < n; i++) {
+    /* octants must lie in the domain and be aligned (the reference asserts
+     * otherwise, src/octFunctions.cpp:310) */
+    if (in[i].lev > D) return DGO_EINVAL;
+    uint64_t len = (uint64_t)1 << (D - in[i].lev), dom = (uint64_t)1 << D;
+    if (in[i].x >= dom || in[i].y >= dom || in[i].z >= dom || in[i].x % len || in[i].y % len || in[i].z % len)
+      return DGO_EINVAL;
     if (in[i].lev > maxL) maxL = in[i].lev;
+  }
   /* I[l]: sorted unique level-l Morton indices of internal nodes */
   u128 *I[32] = {0};
   size_t nI[32] = {0};

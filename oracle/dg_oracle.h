@@ -28,6 +28,7 @@ extern "C" {
 #define DGO_EINVAL (-1)
 #define DGO_ENOMEM (-2)
 #define DGO_EINTERNAL (-3)
+#define DGO_ENOTERM (-4) /* the reference's walk would never terminate */
 
 typedef struct {
   uint32_t x, y, z, lev;

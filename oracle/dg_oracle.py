@@ -86,7 +86,13 @@ def _take_octs(p: ctypes.c_void_p, n: int) -> np.ndarray:
     return out
 
 
+class NoTermination(RuntimeError):
+    """The reference's construction walk would loop forever on this input."""
+
+
 def _check(rc: int, what: str):
+    if rc == -4:
+        raise NoTermination(f"oracle {what}: the reference walk does not terminate on this input")
     if rc != 0:
         raise RuntimeError(f"oracle {what} failed with code {rc}")
 

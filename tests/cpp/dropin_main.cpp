@@ -1,0 +1,63 @@
+// C++ caller of the drop-in mirror (include/dendro_gb300.hpp) with its own
+// octant type shaped like the reference's ot::TreeNode constructor.
+// Reads FP64 points (u64 n, then 3n doubles), runs points2Octree ->
+// balanceOctree -> DA -> matVec, writes the balanced octree as {x,y,z,level}
+// records and prints sizes.  Driven by tests/test_gpu_cpp_dropin.py.
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "dendro_gb300.hpp"
+
+struct MyNode {
+  unsigned x, y, z, lev;
+  MyNode(unsigned x_, unsigned y_, unsigned z_, unsigned l_, unsigned /*dim*/, unsigned /*maxDepth*/)
+      : x(x_), y(y_), z(z_), lev(l_) {}
+  unsigned getX() const { return x; }
+  unsigned getY() const { return y; }
+  unsigned getZ() const { return z; }
+  unsigned getLevel() const { return lev; }
+};
+
+int main(int argc, char **argv) {
+  if (argc < 3) return 2;
+  FILE *f = std::fopen(argv[1], "rb");
+  if (!f) return 2;
+  uint64_t n = 0;
+  if (std::fread(&n, 8, 1, f) != 1) return 2;
+  std::vector<double> pts(3 * n);
+  if (std::fread(pts.data(), 8, 3 * n, f) != 3 * n) return 2;
+  std::fclose(f);
+  double gLens[3] = {1.0, 1.0, 1.0};
+  std::vector<MyNode> lin, bal;
+  dg::ot::points2Octree(pts, gLens, lin, 3, 30, 1);
+  size_t nlin = lin.size();
+  dg::ot::balanceOctree(lin, bal, 3, 30, true);
+  dg::ot::DA da(bal, 30);
+  std::vector<double> x(da.getNodeSize(), 1.0), y;
+  da.matVec(x, y);  // A * 1: the Laplacian part vanishes, mass rows remain
+  double s = 0;
+  for (double v : y) s += v;
+  FILE *g = std::fopen(argv[2], "wb");
+  uint64_t nb = bal.size();
+  std::fwrite(&nb, 8, 1, g);
+  for (auto &o : bal) {
+    uint32_t r[4] = {o.x, o.y, o.z, o.lev};
+    std::fwrite(r, 4, 4, g);
+  }
+  std::fclose(g);
+  // sum of the mass matrix applied to ones = volume of the unit cube
+  std::printf("{\"n_lin\": %zu, \"n_bal\": %zu, \"n_elem\": %u, \"n_node\": %u, \"sum_A1\": %.15f}\n", nlin, bal.size(),
+              da.getElementSize(), da.getNodeSize(), s);
+  // error path: a communicator of size 2 is refused
+  try {
+    std::vector<double> p2 = {0.5, 0.5, 0.5, 0.25, 0.25, 0.25};
+    std::vector<MyNode> o2;
+    dg::ot::points2Octree(p2, gLens, o2, 3, 30, 1, 2);
+    return 3;
+  } catch (const dg::cxx::Error &e) {
+    if (e.status != DG_ERR_COMM_SIZE) return 4;
+  }
+  return 0;
+}

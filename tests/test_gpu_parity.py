@@ -48,18 +48,36 @@ CASES = {
 @pytest.mark.parametrize("max_pts", [1, 3])
 def test_points2octree_bit_exact(ctx, oracle, case, max_pts):
     pts = CASES[case]()
-    ref = oracle.points_to_octree(pts, 30, max_pts)
+    try:
+        ref = oracle.points_to_octree(pts, 30, max_pts)
+    except oracle.NoTermination:
+        # heavily repeated points: the reference walk never ends; refused
+        with pytest.raises(DendroError) as e:
+            points2Octree(pts, maxDepth=30, maxNumPtsPerOctant=max_pts, ctx=ctx)
+        assert e.value.status == 1
+        return
     got = points2Octree(pts, maxDepth=30, maxNumPtsPerOctant=max_pts, ctx=ctx).to_numpy()
     assert got.shape == ref.shape
     assert np.array_equal(got, ref)
 
 
-@pytest.mark.parametrize("max_depth", [30, 12, 4])
+@pytest.mark.parametrize("max_depth", [30, 12, 6])
 def test_points2octree_depths(ctx, oracle, max_depth):
     pts = datagen.gaussian(5000, 0.5, 0.2, seed=11)
     ref = oracle.points_to_octree(pts, max_depth, 1)
     got = points2Octree(pts, maxDepth=max_depth, maxNumPtsPerOctant=1, ctx=ctx).to_numpy()
     assert np.array_equal(got, ref)
+
+
+def test_points2octree_nonterminating_reference_walk(ctx, oracle):
+    # 5000 points on a 16^3 grid repeat heavily; the reference walk then
+    # climbs above the root and never terminates (it runs out of memory)
+    pts = datagen.gaussian(5000, 0.5, 0.2, seed=11)
+    with pytest.raises(oracle.NoTermination):
+        oracle.points_to_octree(pts, 4, 1)
+    with pytest.raises(DendroError) as e:
+        points2Octree(pts, maxDepth=4, maxNumPtsPerOctant=1, ctx=ctx)
+    assert e.value.status == 1
 
 
 def test_points2octree_duplicates_follow_reference_walk(ctx, oracle):
@@ -93,7 +111,16 @@ def test_domain_error(ctx):
 @pytest.mark.parametrize("case", ["gauss", "lognormal", "mixture", "clustered", "boundary", "one", "two"])
 def test_balance_bit_exact(ctx, oracle, case):
     pts = CASES[case]()
+    if case == "clustered":
+        pts = np.unique(oracle.quantize_sort(pts, 30)[:, :3], axis=0).astype(np.float64) / (1 << 30)
     lin = oracle.points_to_octree(pts, 30, 1)
+    if (lin[:, :3] >= (1 << 30)).any():
+        # repeated points drove the construction walk outside the domain;
+        # the reference asserts on such an octree, the CUDA path rejects it
+        with pytest.raises(DendroError) as e:
+            balanceOctree(Octree.from_numpy(lin, 30, ctx=ctx))
+        assert e.value.status == 4
+        return
     ref = oracle.balance(lin, 30)
     got = balanceOctree(Octree.from_numpy(lin, 30, ctx=ctx)).to_numpy()
     assert np.array_equal(got, ref)
@@ -139,7 +166,11 @@ def _to_oracle_order(d, oda):
 @pytest.mark.parametrize("case", ["gauss", "lognormal", "clustered", "boundary", "one"])
 def test_da_and_matvec(ctx, oracle, case):
     pts = CASES[case]()
-    bal = oracle.balance(oracle.points_to_octree(pts, 30, 1), 30)
+    if case in ("boundary", "clustered"):
+        pts = np.unique(oracle.quantize_sort(pts, 30)[:, :3], axis=0).astype(np.float64) / (1 << 30)
+    lin = oracle.points_to_octree(pts, 30, 1)
+    assert not (lin[:, :3] >= (1 << 30)).any()
+    bal = oracle.balance(lin, 30)
     da, oda, d = _da_parity(ctx, oracle, bal)
     p = _to_oracle_order(d, oda)
     rng = np.random.Generator(np.random.PCG64(1))
@@ -165,3 +196,67 @@ def test_da_rejects_unbalanced(ctx, oracle):
     with pytest.raises(DendroError) as e:
         DA(Octree.from_numpy(lin, 30, ctx=ctx))
     assert e.value.status == 5
+
+
+# ---- against the reference's own outputs (tests/golden) -------------------
+import json  # noqa: E402
+import os  # noqa: E402
+
+from tests.golden import cases as gcases  # noqa: E402
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _fnv1a(o):
+    h = 1469598103934665603
+    for byte in np.ascontiguousarray(o, np.uint32).tobytes():
+        h ^= byte
+        h = (h * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    return h
+
+
+@pytest.mark.parametrize("name", sorted(gcases.SMALL))
+def test_golden_reference_cases(ctx, name):
+    g = np.load(os.path.join(GOLDEN, "ref_cases.npz"))
+    depth, maxpts = (int(v) for v in g[f"{name}/params"])
+    lin = points2Octree(g[f"{name}/pts"], maxDepth=depth, maxNumPtsPerOctant=maxpts, ctx=ctx)
+    assert np.array_equal(lin.to_numpy(), g[f"{name}/lin"])
+    if bool(g[f"{name}/bal_aborted"]):
+        # the reference asserts on its own construction output here
+        with pytest.raises(DendroError) as e:
+            balanceOctree(lin)
+        assert e.value.status == 4
+        return
+    bal = balanceOctree(lin).to_numpy()
+    assert len(bal) == int(g[f"{name}/bal_n"])
+    assert _fnv1a(bal) == int(g[f"{name}/bal_fnv"])
+
+
+@pytest.mark.parametrize("name", sorted(gcases.LARGE))
+def test_golden_reference_hashes(ctx, name):
+    exp = json.load(open(os.path.join(GOLDEN, "ref_hashes.json")))[name]
+    fn, depth, maxpts = gcases.LARGE[name]
+    lin = points2Octree(fn(), maxDepth=depth, maxNumPtsPerOctant=maxpts, ctx=ctx)
+    bal = balanceOctree(lin)
+    a, b = lin.to_numpy(), bal.to_numpy()
+    assert (len(a), f"{_fnv1a(a):016x}") == (exp["n_lin"], exp["fnv_lin"])
+    assert (len(b), f"{_fnv1a(b):016x}") == (exp["n_bal"], exp["fnv_bal"])
+
+
+def test_golden_reference_da_and_matvec(ctx):
+    g = np.load(os.path.join(GOLDEN, "ref_da.npz"))
+    da = DA(Octree.from_numpy(g["bal"], 30, ctx=ctx))
+    assert (da.n_elem, da.n_node) == (len(g["bal"]), int(g["n_nodes"]))
+    d = da.download()
+    assert np.array_equal(d["level"] + 1, g["level"])
+    assert np.array_equal(d["child"], g["child"])
+    assert np.array_equal(d["hmask"], g["hmask"])
+    assert np.array_equal(d["etype"], g["etype"])
+    assert np.array_equal(d["node_xyz"][d["nodes"]], g["elem_node_xyz"])
+    ref = dict(zip(map(tuple, g["mv_xyz"]), g["mv_val"]))
+    r = np.array([ref[tuple(v)] for v in d["node_xyz"]])
+    x = gcases.nodal_function(d["node_xyz"])
+    y64 = da.matvec(x, precision=64)
+    assert np.linalg.norm(y64 - r) <= FP64_RTOL * np.linalg.norm(r)
+    y32 = da.matvec(x.astype(np.float32), precision=32).astype(np.float64)
+    assert np.linalg.norm(y32 - r) <= FP32_RTOL * np.linalg.norm(r)
