@@ -152,14 +152,12 @@ def _da_parity(ctx, oracle, bal):
 
 def _to_oracle_order(d, oda):
     """permutation p with gpu_node[p[i]] == oracle node i (by coordinates)"""
-    def key(x):
-        x = x.astype(np.uint64)
-        return (x[:, 0] << np.uint64(42)) | (x[:, 1] << np.uint64(21)) | x[:, 2]
-    kg, ko = key(d["node_xyz"]), key(oda.node_xyz)
-    og = np.argsort(kg)
-    pos = np.searchsorted(kg[og], ko)
-    p = og[pos]
-    assert np.array_equal(kg[p], ko)
+    og = np.lexsort(d["node_xyz"].T[::-1])
+    oo = np.lexsort(oda.node_xyz.T[::-1])
+    assert np.array_equal(d["node_xyz"][og], oda.node_xyz[oo])
+    p = np.empty(len(oo), np.int64)
+    p[oo] = og
+    assert np.array_equal(d["node_xyz"][p], oda.node_xyz)
     return p
 
 
