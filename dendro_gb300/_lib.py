@@ -64,6 +64,8 @@ def _declare(L):
         "dg_ctx_profile_entry": ([P, I, ctypes.c_char_p, SZ, ctypes.POINTER(D), ctypes.POINTER(ctypes.c_ulonglong),
                                   ctypes.POINTER(D)], I),
         "dg_points_to_octree": ([P, P, SZ, P, U, U, I, I, PP], I),
+        "dg_points_to_octree_batch": ([P, P, SZ, P, SZ, P, U, U, I, PP], I),
+        "dg_octree_segments": ([P, P, ctypes.POINTER(SZ), P], I),
         "dg_sort_unique_points": ([P, P, SZ, P, U, I, P, I, ctypes.POINTER(SZ)], I),
         "dg_balance_octree": ([P, P, I, I, PP], I),
         "dg_octree_size": ([P, ctypes.POINTER(SZ), ctypes.POINTER(U)], I),

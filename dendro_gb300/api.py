@@ -23,6 +23,7 @@ __all__ = [
     "points2Octree",
     "balanceOctree",
     "sortUniquePoints",
+    "points2OctreeBatch",
     "default_context",
 ]
 
@@ -110,6 +111,22 @@ class Octree:
     def __len__(self):
         return self.size
 
+    def segments(self) -> np.ndarray:
+        """Start offsets of each cloud's octants (nseg + 1 entries)."""
+        ns = ctypes.c_size_t()
+        check(self.ctx.handle, self.ctx._L.dg_octree_segments(self.ctx.handle, self.handle, ctypes.byref(ns), None),
+              "dg_octree_segments")
+        off = np.empty(ns.value + 1, np.uint64)
+        check(self.ctx.handle, self.ctx._L.dg_octree_segments(self.ctx.handle, self.handle, ctypes.byref(ns), _ptr(off)),
+              "dg_octree_segments")
+        return off
+
+    def split(self) -> list:
+        """The octree of every cloud, as (n_s, 4) uint32 arrays."""
+        a = self.to_numpy()
+        off = self.segments()
+        return [a[off[i]:off[i + 1]] for i in range(len(off) - 1)]
+
     def to_numpy(self) -> np.ndarray:
         out = np.empty((self.size, 4), np.uint32)
         check(self.ctx.handle, self.ctx._L.dg_octree_download(self.ctx.handle, self.handle, _ptr(out), 0), "dg_octree_download")
@@ -169,6 +186,31 @@ def points2Octree(pts, gLens=(1.0, 1.0, 1.0), dim: int = 3, maxDepth: int = 30, 
                                    ctypes.byref(h)),
         "points2Octree",
     )
+    return Octree(ctx, h)
+
+
+def points2OctreeBatch(clouds, gLens=(1.0, 1.0, 1.0), maxDepth: int = 30, maxNumPtsPerOctant: int = 1,
+                       ctx: Context | None = None, seg_start=None) -> Octree:
+    """points2Octree over a batch of clouds in one pass.
+
+    ``clouds`` is a list of (n_s, 3) arrays, or one concatenated array / CUDA
+    tensor together with ``seg_start`` (nseg + 1 offsets).
+    """
+    ctx = ctx or default_context()
+    if seg_start is None:
+        sizes = [len(c) for c in clouds]
+        seg_start = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+        pts = np.concatenate([np.asarray(c, np.float64).reshape(-1, 3) for c in clouds]) if sizes else np.zeros((0, 3))
+    else:
+        pts = clouds
+        seg_start = np.ascontiguousarray(seg_start, dtype=np.uint64)
+    a, n, on_dev = _points_arg(pts)
+    g = np.asarray(gLens, np.float64)
+    h = ctypes.c_void_p()
+    check(ctx.handle,
+          ctx._L.dg_points_to_octree_batch(ctx.handle, _ptr(a), n, _ptr(seg_start), len(seg_start) - 1, _ptr(g), maxDepth,
+                                           maxNumPtsPerOctant, on_dev, ctypes.byref(h)),
+          "points2OctreeBatch")
     return Octree(ctx, h)
 
 

@@ -217,6 +217,34 @@ int dg_points_to_octree(dg_ctx ctx, const double *xyz, size_t n, const double gL
   return DG_OK;
 }
 
+int dg_points_to_octree_batch(dg_ctx ctx, const double *xyz, size_t n, const uint64_t *seg_start, size_t nseg,
+                              const double gLens[3], unsigned maxDepth, unsigned maxNumPts, int xyz_on_device,
+                              dg_octree *out) {
+  if (!out || (!xyz && n) || !gLens || !seg_start || nseg == 0) return DG_ERR_INVALID_ARG;
+  *out = nullptr;
+  dg_octree h = new (std::nothrow) dg_octree_s();
+  if (!h) return DG_ERR_OUT_OF_MEMORY;
+  int rc = guarded(ctx, [&]() {
+    if (!(gLens[0] > 0 && gLens[1] > 0 && gLens[2] > 0)) dg::fail(DG_ERR_INVALID_ARG, "gLens must be positive");
+    dg::DBuf<double> hold;
+    const double *d = device_input(ctx->c, xyz, 3 * n, xyz_on_device, hold);
+    dg::points_to_octree(ctx->c, d, n, gLens, maxDepth, maxNumPts, h->o, seg_start, nseg);
+  });
+  if (rc != DG_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return DG_OK;
+}
+
+int dg_octree_segments(dg_ctx ctx, dg_octree o, size_t *nseg, uint64_t *offsets) {
+  if (!o) return DG_ERR_INVALID_ARG;
+  if (nseg) *nseg = o->o.nseg;
+  if (!offsets) return DG_OK;
+  return guarded(ctx, [&]() { dg::octree_segment_offsets(ctx->c, o->o, offsets); });
+}
+
 int dg_sort_unique_points(dg_ctx ctx, const double *xyz, size_t n, const double gLens[3], unsigned maxDepth,
                           int xyz_on_device, uint32_t *out_xyzl, int out_on_device, size_t *n_unique) {
   if ((!xyz && n) || !gLens || !n_unique || (!out_xyzl && n)) return DG_ERR_INVALID_ARG;
@@ -314,7 +342,10 @@ int dg_da_build(dg_ctx ctx, dg_octree balanced, dg_da *out) {
   *out = nullptr;
   dg_da h = new (std::nothrow) dg_da_s();
   if (!h) return DG_ERR_OUT_OF_MEMORY;
-  int rc = guarded(ctx, [&]() { dg::mesh_build(ctx->c, balanced->o, h->m); });
+  int rc = guarded(ctx, [&]() {
+    if (balanced->o.nseg != 1) dg::fail(DG_ERR_UNSUPPORTED, "DA: one cloud per mesh");
+    dg::mesh_build(ctx->c, balanced->o, h->m);
+  });
   if (rc != DG_OK) {
     delete h;
     return rc;

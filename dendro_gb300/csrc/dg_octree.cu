@@ -1,6 +1,10 @@
 // Octree construction (points2Octree) and 2:1 balance (balanceOctree) on
 // the GPU.  All data stays in HBM; the host only reads sizes.
 //
+// Batches: several clouds ("segments") are processed by the same launches;
+// segment s lives in key bits [3D, 3D + seg_bits) (dg_octree.cuh), so every
+// sort, NCA and gap computation below stays inside its own cloud.
+//
 // Construction (unique points, reference p2oLocal, src/construct.cpp:976):
 // the leaf that holds point i is the child of its deepest ancestor that
 // contains more than maxPts points.  With the points in Morton order that
@@ -28,11 +32,30 @@ namespace dg {
 
 __device__ __forceinline__ void set_flag(uint32_t *flags, uint32_t f) { atomicOr(flags, f); }
 
+// key with only the Morton bits of one cloud (bits [0, 3D))
+__host__ __device__ __forceinline__ Key128 morton_part(Key128 k, unsigned D) {
+  Key128 a = tag_anchor(k);
+  if (3 * D < 64) {
+    a.lo &= (3 * D) ? ((1ull << (3 * D)) - 1) : 0ull;
+    a.hi = 0;
+  } else {
+    a.hi &= (1ull << (3 * D - 64)) - 1;
+  }
+  return a;
+}
+__host__ __device__ __forceinline__ uint64_t seg_of(Key128 k, unsigned D) {
+  return to_u128(tag_anchor(k)) >> (3 * D) & 0xffffffffffull;
+}
+__host__ __device__ __forceinline__ Key128 seg_key(uint64_t seg, unsigned D) {
+  return from_u128((u128)seg << (3 * D));
+}
+
 // ------------------------------------------------------------------------
 // quantize + Morton key (construct.cpp:930-942)
 // ------------------------------------------------------------------------
 __global__ void k_quantize(const double *__restrict__ xyz, size_t n, double scale, double gx, double gy, double gz,
-                           unsigned D, Key128 *__restrict__ keys, uint32_t *flags) {
+                           unsigned D, const uint64_t *__restrict__ seg_start, size_t nseg, Key128 *__restrict__ keys,
+                           uint32_t *flags) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
@@ -50,44 +73,58 @@ __global__ void k_quantize(const double *__restrict__ xyz, size_t n, double scal
   } else {
     set_flag(flags, DGF_DOMAIN);
   }
-  keys[i] = make_tagged(morton3(ux, uy, uz), D);
+  Key128 k = morton3(ux, uy, uz);
+  if (seg_start) {  // segment of point i: last s with seg_start[s] <= i
+    size_t lo = 0, hi = nseg;
+    while (hi - lo > 1) {
+      size_t mid = (lo + hi) / 2;
+      if (seg_start[mid] <= i) lo = mid;
+      else hi = mid;
+    }
+    k = key_or(k, seg_key(lo, D));
+  }
+  keys[i] = make_tagged(k, D);
 }
 
+// NCA level of two points of the same cloud; -1 across clouds
 __device__ __forceinline__ int nca_level(Key128 a, Key128 b, unsigned D) {
   Key128 x = key_xor(tag_anchor(a), tag_anchor(b));
   if (!x.lo && !x.hi) return (int)D;
-  return key_clz(x, 3 * (int)D) / 3;
+  int lz = key_clz(x, 3 * (int)D);
+  return lz < 0 ? -1 : lz / 3;
 }
 
-__global__ void k_flag_dups(const Key128 *__restrict__ p, size_t n, uint32_t *flags) {
+// dupseg[s] = 1 when cloud s holds a repeated point
+__global__ void k_flag_dups(const Key128 *__restrict__ p, size_t n, unsigned D, uint32_t *dupseg, uint32_t *flags) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= 1 && i < n && key_eq(p[i], p[i - 1])) set_flag(flags, 0x100u);
+  if (i >= 1 && i < n && key_eq(p[i], p[i - 1])) {
+    dupseg[seg_of(p[i], D)] = 1u;
+    set_flag(flags, 0x100u);
+  }
 }
 
-// leaf level of every point and the flag "first point of its leaf"
+__device__ __forceinline__ unsigned leaf_level(const Key128 *__restrict__ p, size_t n, size_t i, unsigned m,
+                                               unsigned D) {
+  size_t lo = (i >= m) ? i - m : 0;
+  size_t hi = (i + m < n) ? i : (n > m ? n - 1 - m : 0);
+  int best = -1;
+  if (n > m)
+    for (size_t j = lo; j <= hi; j++) best = max(best, nca_level(p[j], p[j + m], D));
+  return (unsigned)min(best + 1, (int)D);
+}
+
+// leaf of every point and the flag "first point of its leaf"
 __global__ void k_p2o_seeds(const Key128 *__restrict__ p, size_t n, unsigned m, unsigned D,
                             Key128 *__restrict__ seeds, uint32_t *__restrict__ first) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  size_t lo = (i >= m) ? i - m : 0;
-  size_t hi = (i + m < n) ? i : n - 1 - m;
-  int best = 0;
-  for (size_t j = lo; j <= hi; j++) best = max(best, nca_level(p[j], p[j + m], D));
-  unsigned L = min((unsigned)best + 1u, D);
-  Key128 a = tag_anchor(p[i]);
-  a = key_shl(key_shr(a, 3 * (D - L)), 3 * (D - L));
-  Key128 s = make_tagged(a, L);
-  seeds[i] = s;
-  // same leaf as the previous point?  (recomputed, not read back)
+  unsigned L = leaf_level(p, n, i, m, D);
+  Key128 a = key_shl(key_shr(tag_anchor(p[i]), 3 * (D - L)), 3 * (D - L));
+  seeds[i] = make_tagged(a, L);
   bool f = true;
   if (i > 0) {
-    size_t lo2 = (i - 1 >= m) ? i - 1 - m : 0;
-    size_t hi2 = (i - 1 + m < n) ? i - 1 : n - 1 - m;
-    int best2 = 0;
-    for (size_t j = lo2; j <= hi2; j++) best2 = max(best2, nca_level(p[j], p[j + m], D));
-    unsigned L2 = min((unsigned)best2 + 1u, D);
-    Key128 a2 = tag_anchor(p[i - 1]);
-    a2 = key_shl(key_shr(a2, 3 * (D - L2)), 3 * (D - L2));
+    unsigned L2 = leaf_level(p, n, i - 1, m, D);
+    Key128 a2 = key_shl(key_shr(tag_anchor(p[i - 1]), 3 * (D - L2)), 3 * (D - L2));
     f = !(L2 == L && key_eq(a2, a));
   }
   first[i] = f ? 1u : 0u;
@@ -107,7 +144,8 @@ __device__ __forceinline__ int log2_128(u128 v) {  // v > 0
   return 63 - __clzll((long long)(uint64_t)v);
 }
 
-// largest k with s % 8^k == 0 and s + 8^k <= e (s < e)
+// largest k <= D with s % 8^k == 0 and s + 8^k <= e (s < e); blocks never
+// cross a cloud boundary because clouds are aligned 8^D ranges
 __device__ __forceinline__ int block_exp(u128 s, u128 e, unsigned D) {
   int k1 = (s == 0) ? (int)D : min((int)D, ctz128(s) / 3);
   int k2 = log2_128(e - s) / 3;
@@ -137,21 +175,20 @@ __device__ __forceinline__ u128 seed_end(Key128 s, unsigned D) {
   return kpos(s) + ((u128)1 << (3 * (D - tag_level(s))));
 }
 
-__global__ void k_fill_count(const Key128 *__restrict__ seeds, size_t ns, unsigned D, uint32_t *__restrict__ cnt) {
+__global__ void k_fill_count(const Key128 *__restrict__ seeds, size_t ns, unsigned D, u128 total,
+                             uint32_t *__restrict__ cnt) {
   size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= ns) return;
-  const u128 total = (u128)1 << (3 * D);
   u128 e = (j + 1 < ns) ? kpos(seeds[j + 1]) : total;
   unsigned c = 1 + gap_count(seed_end(seeds[j], D), e, D);
   if (j == 0) c += gap_count(0, kpos(seeds[0]), D);
   cnt[j] = c;
 }
 
-__global__ void k_fill_emit(const Key128 *__restrict__ seeds, size_t ns, unsigned D, const uint64_t *__restrict__ off,
-                            Key128 *__restrict__ out) {
+__global__ void k_fill_emit(const Key128 *__restrict__ seeds, size_t ns, unsigned D, u128 total,
+                            const uint64_t *__restrict__ off, Key128 *__restrict__ out) {
   size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= ns) return;
-  const u128 total = (u128)1 << (3 * D);
   size_t w = off[j];
   if (j == 0) w = gap_emit(0, kpos(seeds[0]), D, out, w);
   out[w++] = seeds[j];
@@ -160,12 +197,54 @@ __global__ void k_fill_emit(const Key128 *__restrict__ seeds, size_t ns, unsigne
 }
 
 // ------------------------------------------------------------------------
-// the reference walk for inputs with repeated points (dg_walk.cuh)
+// the reference walk for clouds with repeated points (dg_walk.cuh): one
+// block per such cloud, thread 0 walks it; count pass then emit pass
 // ------------------------------------------------------------------------
-__global__ void k_p2o_walk_serial(const Key128 *__restrict__ pk, size_t n, unsigned m, unsigned D,
-                                  Key128 *__restrict__ out, unsigned long long *count) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  *count = p2o_walk(pk, n, m, D, out);
+__global__ void k_p2o_walk_segments(const Key128 *__restrict__ pk, const uint64_t *__restrict__ pt_start,
+                                    const uint32_t *__restrict__ dup_list, unsigned m, unsigned D,
+                                    const uint64_t *__restrict__ out_off, Key128 *__restrict__ out,
+                                    unsigned long long *counts) {
+  if (threadIdx.x != 0) return;
+  const uint32_t s = dup_list[blockIdx.x];
+  const size_t b = pt_start[s], e = pt_start[s + 1];
+  size_t c = p2o_walk(pk + b, e - b, m, D, out ? out + out_off[blockIdx.x] : nullptr, seg_key(s, D));
+  counts[blockIdx.x] = c;
+}
+
+// first index of each cloud in a sorted key array (lower bound of s << 3D)
+__global__ void k_seg_bounds(const Key128 *__restrict__ keys, size_t n, unsigned D, size_t nseg,
+                             uint64_t *__restrict__ off) {
+  size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s > nseg) return;
+  Key128 v = seg_key(s, D);
+  size_t lo = 0, hi = n;
+  while (lo < hi) {
+    size_t mid = lo + (hi - lo) / 2;
+    if (key_lt(tag_anchor(keys[mid]), v)) lo = mid + 1;
+    else hi = mid;
+  }
+  off[s] = lo;
+}
+
+// place each cloud's octants at their final offsets: clouds with repeated
+// points take the walk's output, the others the parallel construction's
+__global__ void k_assemble(const Key128 *__restrict__ par, size_t npar, const uint64_t *__restrict__ par_off,
+                           const Key128 *__restrict__ walk, const uint64_t *__restrict__ walk_off,
+                           const uint32_t *__restrict__ walk_slot, const uint32_t *__restrict__ dupseg,
+                           const uint64_t *__restrict__ final_off, unsigned D, Key128 *__restrict__ out,
+                           size_t nwalk_total) {
+  size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < npar) {
+    uint64_t s = seg_of(par[j], D);
+    if (!dupseg[s]) out[final_off[s] + (j - par_off[s])] = par[j];
+  }
+  if (j < nwalk_total) {
+    // walk outputs are stored cloud after cloud in dup-list order
+    Key128 k = walk[j];
+    uint64_t s = seg_of(k, D);
+    uint32_t slot = walk_slot[s];
+    out[final_off[s] + (j - walk_off[slot])] = k;
+  }
 }
 
 // ------------------------------------------------------------------------
@@ -183,17 +262,18 @@ void check_device_flags(Context &ctx, const char *where) {
 }
 
 static void quantize_sorted(Context &ctx, const double *d_xyz, size_t n, const double g[3], unsigned D,
-                            DBuf<Key128> &keys, DBuf<Key128> &tmp, Key128 **sorted) {
+                            const uint64_t *d_seg_start, size_t nseg, unsigned seg_bits, DBuf<Key128> &keys,
+                            DBuf<Key128> &tmp, Key128 **sorted) {
   keys.alloc(n, ctx.stream);
   tmp.alloc(n, ctx.stream);
   {
     ProfScope _prof(ctx, "quantize", (double)n * 40);
-    k_quantize<<<grid_for(n, 256), 256, 0, ctx.stream>>>(d_xyz, n, (double)(1u << D), g[0], g[1], g[2], D, keys.get(),
-                                                       ctx.d_flags);
-  DG_LAUNCH_CHECK();
-    }
+    k_quantize<<<grid_for(n, 256), 256, 0, ctx.stream>>>(d_xyz, n, (double)(1u << D), g[0], g[1], g[2], D,
+                                                         d_seg_start, nseg, keys.get(), ctx.d_flags);
+    DG_LAUNCH_CHECK();
+  }
   check_device_flags(ctx, "points2Octree");
-  *sorted = radix_sort<Key128>(ctx, keys.get(), tmp.get(), n, 3 * (int)D);
+  *sorted = radix_sort<Key128>(ctx, keys.get(), tmp.get(), n, 3 * (int)D + (int)seg_bits);
 }
 
 size_t sort_points(Context &ctx, const double *d_xyz, size_t n, const double g[3], unsigned D, Key128 *d_out,
@@ -201,120 +281,241 @@ size_t sort_points(Context &ctx, const double *d_xyz, size_t n, const double g[3
   if (n == 0) return 0;
   DBuf<Key128> keys, tmp;
   Key128 *sorted;
-  quantize_sorted(ctx, d_xyz, n, g, D, keys, tmp, &sorted);
+  quantize_sorted(ctx, d_xyz, n, g, D, nullptr, 1, 0, keys, tmp, &sorted);
   DBuf<uint32_t> flags(n, ctx.stream);
-  k_flag_unique<Key128><<<grid_for(n, 256), 256, 0, ctx.stream>>>(sorted, n, flags.get());
-  DG_LAUNCH_CHECK();
+  {
+    ProfScope _prof(ctx, "flag_unique", (double)n * 20);
+    k_flag_unique<Key128><<<grid_for(n, 256), 256, 0, ctx.stream>>>(sorted, n, flags.get());
+    DG_LAUNCH_CHECK();
+  }
   size_t nu = compact<Key128>(ctx, sorted, flags.get(), n, d_out);
   if (has_dups) *has_dups = nu != n;
   return nu;
 }
 
 void points_to_octree(Context &ctx, const double *d_xyz, size_t n, const double g[3], unsigned D, unsigned m,
-                      Octree &out) {
+                      Octree &out, const uint64_t *h_seg_start, size_t nseg) {
   if (m == 0 || D > 30) fail(DG_ERR_INVALID_ARG, "points2Octree: maxNumPts must be >= 1 and maxDepth <= 30");
   if (n >= 0x7fffffffull) fail(DG_ERR_INVALID_ARG, "points2Octree: too many points");
+  if (nseg == 0) fail(DG_ERR_INVALID_ARG, "points2Octree: no clouds");
+  const unsigned SB = bits_for(nseg);
+  if (3 * D + SB > 120) fail(DG_ERR_INVALID_ARG, "points2Octree: too many clouds for maxDepth");
+  if (h_seg_start) {
+    if (h_seg_start[0] != 0 || h_seg_start[nseg] != n)
+      fail(DG_ERR_INVALID_ARG, "points2Octree: cloud offsets must run from 0 to n");
+    for (size_t s = 0; s < nseg; s++)
+      if (h_seg_start[s + 1] < h_seg_start[s]) fail(DG_ERR_INVALID_ARG, "points2Octree: cloud offsets decrease");
+  }
   out.max_depth = D;
+  out.nseg = nseg;
+  out.seg_bits = SB;
   cudaStream_t s = ctx.stream;
-  if (D == 0 || n <= m) {  // construct.cpp:916-920, 948-952: the root alone
+  const u128 total = (u128)nseg << (3 * D);
+  DBuf<uint64_t> d_seg_start;
+  if (nseg > 1) {
+    d_seg_start.alloc(nseg + 1, s);
+    DG_CUDA(cudaMemcpyAsync(d_seg_start.get(), h_seg_start, (nseg + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+  }
+  if (D == 0 || n == 0 || (nseg == 1 && n <= m)) {
+    // construct.cpp:916-920, 948-952: a cloud with at most maxPts points is
+    // the root alone (still validate the points like the quantize loop)
     if (n && D) {
-      // still validate the domain like the quantize loop would see it
       DBuf<Key128> keys(n, s);
       {
-        ProfScope _prof("quantize", (double)n * 40);
-        k_quantize<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, (double)(1u << D), g[0], g[1], g[2], D, keys.get(),
-                                                    ctx.d_flags);
+        ProfScope _prof(ctx, "quantize", (double)n * 40);
+        k_quantize<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, (double)(1u << D), g[0], g[1], g[2], D, nullptr, 1,
+                                                    keys.get(), ctx.d_flags);
         DG_LAUNCH_CHECK();
       }
       check_device_flags(ctx, "points2Octree");
     }
-    out.n = 1;
-    DG_CUDA(cudaMallocAsync((void **)&out.keys, sizeof(Key128), s));
-    Key128 root = make_tagged(Key128{0, 0}, 0);
-    DG_CUDA(cudaMemcpyAsync(out.keys, &root, sizeof(Key128), cudaMemcpyHostToDevice, s));
+    std::vector<Key128> roots(nseg);
+    for (size_t i = 0; i < nseg; i++) roots[i] = make_tagged(seg_key(i, D), 0);
+    out.n = nseg;
+    DG_CUDA(cudaMallocAsync((void **)&out.keys, nseg * sizeof(Key128), s));
+    DG_CUDA(cudaMemcpyAsync(out.keys, roots.data(), nseg * sizeof(Key128), cudaMemcpyHostToDevice, s));
+    if (nseg > 1) {
+      std::vector<uint64_t> off(nseg + 1);
+      for (size_t i = 0; i <= nseg; i++) off[i] = i;
+      DG_CUDA(cudaMallocAsync((void **)&out.seg_off, (nseg + 1) * sizeof(uint64_t), s));
+      DG_CUDA(cudaMemcpyAsync(out.seg_off, off.data(), (nseg + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    }
     DG_CUDA(cudaStreamSynchronize(s));
     return;
   }
   DBuf<Key128> keys, tmp;
   Key128 *p;
-  quantize_sorted(ctx, d_xyz, n, g, D, keys, tmp, &p);
+  quantize_sorted(ctx, d_xyz, n, g, D, d_seg_start.get(), nseg, SB, keys, tmp, &p);
   Key128 *other = (p == keys.get()) ? tmp.get() : keys.get();
 
+  // clouds with repeated points
+  DBuf<uint32_t> dupseg(nseg, s);
+  DG_CUDA(cudaMemsetAsync(dupseg.get(), 0, nseg * sizeof(uint32_t), s));
   DG_CUDA(cudaMemsetAsync(ctx.d_flags, 0, sizeof(uint32_t), s));
   {
-    ProfScope _prof("flag_dups", (double)n * 16);
-    k_flag_dups<<<grid_for(n, 256), 256, 0, s>>>(p, n, ctx.d_flags);
+    ProfScope _prof(ctx, "flag_dups", (double)n * 16);
+    k_flag_dups<<<grid_for(n, 256), 256, 0, s>>>(p, n, D, dupseg.get(), ctx.d_flags);
     DG_LAUNCH_CHECK();
   }
   uint32_t dupflag = read_scalar(ctx, ctx.d_flags);
   DG_CUDA(cudaMemsetAsync(ctx.d_flags, 0, sizeof(uint32_t), s));
 
-  if (dupflag) {
-    unsigned long long *d_cnt = ctx.d_scratch + 8;
-    {
-      ProfScope _prof("p2o_walk_serial", (double)n * 16);
-      k_p2o_walk_serial<<<1, 1, 0, s>>>(p, n, m, D, nullptr, d_cnt);
-      DG_LAUNCH_CHECK();
-    }
-    size_t cnt = (size_t)read_scalar(ctx, d_cnt);
-    if (cnt == P2O_WALK_NO_END)
-      fail(DG_ERR_INVALID_ARG,
-           "points2Octree: with these repeated points the reference construction walk never terminates");
-    DBuf<Key128> res(cnt, s);
-    {
-      ProfScope _prof("p2o_walk_serial", (double)n * 16 + (double)cnt * 16);
-      k_p2o_walk_serial<<<1, 1, 0, s>>>(p, n, m, D, res.get(), d_cnt);
-      DG_LAUNCH_CHECK();
-    }
-    DG_CUDA(cudaStreamSynchronize(s));
-    out.n = cnt;
-    out.keys = res.release_ptr();
-    return;
-  }
-
+  // parallel construction over all points (clouds with repeated points are
+  // replaced below)
   DBuf<uint32_t> first(n, s);
   {
     ProfScope _prof(ctx, "p2o_seeds", (double)n * 36);
     k_p2o_seeds<<<grid_for(n, 256), 256, 0, s>>>(p, n, m, D, other, first.get());
-  DG_LAUNCH_CHECK();
-    }
-  // compact seeds into p (the sorted points are no longer needed)
-  size_t ns = compact<Key128>(ctx, other, first.get(), n, p);
+    DG_LAUNCH_CHECK();
+  }
+  DBuf<Key128> walk_keys;  // keeps p alive for the walk when needed
+  Key128 *seeds = other;
+  if (dupflag) {
+    // the walk needs the sorted points: compact the seeds into a new buffer
+    walk_keys.alloc(n, s);
+    seeds = walk_keys.get();
+  }
+  size_t ns = compact<Key128>(ctx, other, first.get(), n, dupflag ? seeds : p);
+  if (!dupflag) seeds = p;
+  first.release();
   DBuf<uint32_t> cnt(ns, s);
   {
     ProfScope _prof(ctx, "fill_count", (double)ns * 20);
-    k_fill_count<<<grid_for(ns, 256), 256, 0, s>>>(p, ns, D, cnt.get());
-  DG_LAUNCH_CHECK();
-    }
+    k_fill_count<<<grid_for(ns, 256), 256, 0, s>>>(seeds, ns, D, total, cnt.get());
+    DG_LAUNCH_CHECK();
+  }
   DBuf<uint64_t> off(ns, s);
   uint64_t *d_total = reinterpret_cast<uint64_t *>(ctx.d_scratch);
   exclusive_scan<uint32_t, uint64_t>(cnt.get(), off.get(), ns, d_total, s);
-  size_t total = (size_t)read_scalar(ctx, d_total);
-  DBuf<Key128> res(total, s);
+  size_t npar = (size_t)read_scalar(ctx, d_total);
+  DBuf<Key128> res(npar, s);
   {
     ProfScope _prof(ctx, "fill_emit", (double)ns * 24);
-    k_fill_emit<<<grid_for(ns, 256), 256, 0, s>>>(p, ns, D, off.get(), res.get());
-  DG_LAUNCH_CHECK();
+    k_fill_emit<<<grid_for(ns, 256), 256, 0, s>>>(seeds, ns, D, total, off.get(), res.get());
+    DG_LAUNCH_CHECK();
+  }
+  cnt.release();
+  off.release();
+
+  DBuf<uint64_t> seg_off;
+  if (nseg > 1 || dupflag) {
+    seg_off.alloc(nseg + 1, s);
+    {
+      ProfScope _prof(ctx, "seg_bounds", (double)(nseg + 1) * 16);
+      k_seg_bounds<<<grid_for(nseg + 1, 256), 256, 0, s>>>(res.get(), npar, D, nseg, seg_off.get());
+      DG_LAUNCH_CHECK();
     }
-  out.n = total;
-  out.keys = res.release_ptr();
+  }
+  if (!dupflag) {
+    out.n = npar;
+    out.keys = res.release_ptr();
+    out.seg_off = nseg > 1 ? seg_off.release_ptr() : nullptr;
+    DG_CUDA(cudaStreamSynchronize(s));
+    return;
+  }
+
+  // walk every cloud with repeated points
+  std::vector<uint32_t> h_dup(nseg);
+  DG_CUDA(cudaMemcpyAsync(h_dup.data(), dupseg.get(), nseg * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  std::vector<uint64_t> h_par_off(nseg + 1);
+  DG_CUDA(cudaMemcpyAsync(h_par_off.data(), seg_off.get(), (nseg + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  DG_CUDA(cudaStreamSynchronize(s));
+  std::vector<uint32_t> dup_list, walk_slot(nseg, 0xffffffffu);
+  for (size_t i = 0; i < nseg; i++)
+    if (h_dup[i]) {
+      walk_slot[i] = (uint32_t)dup_list.size();
+      dup_list.push_back((uint32_t)i);
+    }
+  const size_t nd = dup_list.size();
+  std::vector<uint64_t> h_pt_start(nseg + 1);
+  if (h_seg_start) {
+    for (size_t i = 0; i <= nseg; i++) h_pt_start[i] = h_seg_start[i];
+  } else {
+    h_pt_start[0] = 0;
+    h_pt_start[1] = n;
+  }
+  DBuf<uint64_t> d_pt_start(nseg + 1, s), d_walk_off(nd + 1, s);
+  DBuf<uint32_t> d_dup_list(nd, s), d_walk_slot(nseg, s);
+  DBuf<unsigned long long> d_counts(nd, s);
+  DG_CUDA(cudaMemcpyAsync(d_pt_start.get(), h_pt_start.data(), (nseg + 1) * 8, cudaMemcpyHostToDevice, s));
+  DG_CUDA(cudaMemcpyAsync(d_dup_list.get(), dup_list.data(), nd * 4, cudaMemcpyHostToDevice, s));
+  DG_CUDA(cudaMemcpyAsync(d_walk_slot.get(), walk_slot.data(), nseg * 4, cudaMemcpyHostToDevice, s));
+  {
+    ProfScope _prof(ctx, "p2o_walk_serial", (double)n * 16);
+    k_p2o_walk_segments<<<(unsigned)nd, 32, 0, s>>>(p, d_pt_start.get(), d_dup_list.get(), m, D, nullptr, nullptr,
+                                                    d_counts.get());
+    DG_LAUNCH_CHECK();
+  }
+  std::vector<unsigned long long> h_counts(nd);
+  DG_CUDA(cudaMemcpyAsync(h_counts.data(), d_counts.get(), nd * 8, cudaMemcpyDeviceToHost, s));
+  DG_CUDA(cudaStreamSynchronize(s));
+  std::vector<uint64_t> h_walk_off(nd + 1, 0);
+  for (size_t i = 0; i < nd; i++) {
+    if (h_counts[i] == (unsigned long long)P2O_WALK_NO_END)
+      fail(DG_ERR_INVALID_ARG,
+           "points2Octree: with these repeated points the reference construction walk never terminates");
+    h_walk_off[i + 1] = h_walk_off[i] + h_counts[i];
+  }
+  const size_t nwalk = h_walk_off[nd];
+  DG_CUDA(cudaMemcpyAsync(d_walk_off.get(), h_walk_off.data(), (nd + 1) * 8, cudaMemcpyHostToDevice, s));
+  DBuf<Key128> walk_out(nwalk ? nwalk : 1, s);
+  {
+    ProfScope _prof(ctx, "p2o_walk_serial", (double)n * 16 + (double)nwalk * 16);
+    k_p2o_walk_segments<<<(unsigned)nd, 32, 0, s>>>(p, d_pt_start.get(), d_dup_list.get(), m, D, d_walk_off.get(),
+                                                    walk_out.get(), d_counts.get());
+    DG_LAUNCH_CHECK();
+  }
+  // final offsets
+  std::vector<uint64_t> h_final(nseg + 1, 0);
+  for (size_t i = 0; i < nseg; i++) {
+    uint64_t c = h_dup[i] ? h_counts[walk_slot[i]] : (h_par_off[i + 1] - h_par_off[i]);
+    h_final[i + 1] = h_final[i] + c;
+  }
+  const size_t nfinal = h_final[nseg];
+  DBuf<uint64_t> d_final(nseg + 1, s);
+  DG_CUDA(cudaMemcpyAsync(d_final.get(), h_final.data(), (nseg + 1) * 8, cudaMemcpyHostToDevice, s));
+  DBuf<Key128> fin(nfinal ? nfinal : 1, s);
+  {
+    ProfScope _prof(ctx, "p2o_assemble", (double)(npar + nwalk) * 32);
+    k_assemble<<<grid_for(std::max(npar, nwalk), 256), 256, 0, s>>>(res.get(), npar, seg_off.get(), walk_out.get(),
+                                                                    d_walk_off.get(), d_walk_slot.get(), dupseg.get(),
+                                                                    d_final.get(), D, fin.get(), nwalk);
+    DG_LAUNCH_CHECK();
+  }
+  out.n = nfinal;
+  out.keys = fin.release_ptr();
+  if (nseg > 1) {
+    out.seg_off = d_final.release_ptr();
+  }
+  DG_CUDA(cudaStreamSynchronize(s));
+}
+
+void octree_segment_offsets(Context &ctx, const Octree &o, uint64_t *h_off) {
+  if (o.nseg == 1 || !o.seg_off) {
+    h_off[0] = 0;
+    h_off[1] = o.n;
+    return;
+  }
+  DG_CUDA(cudaMemcpyAsync(h_off, o.seg_off, (o.nseg + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
+  DG_CUDA(cudaStreamSynchronize(ctx.stream));
 }
 
 // ------------------------------------------------------------------------
 // balance
 // ------------------------------------------------------------------------
 // level histogram; flags octants that are not aligned octants of the
-// domain (the reference asserts on those, octFunctions.cpp:310)
-__global__ void k_level_hist(const Key128 *__restrict__ k, size_t n, unsigned D, unsigned long long *hist,
-                             uint32_t *flags) {
+// domain of their cloud (the reference asserts on those,
+// octFunctions.cpp:310)
+__global__ void k_level_hist(const Key128 *__restrict__ k, size_t n, unsigned D, uint64_t nseg,
+                             unsigned long long *hist, uint32_t *flags) {
   __shared__ unsigned int h[32];
   if (threadIdx.x < 32) h[threadIdx.x] = 0;
   __syncthreads();
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     Key128 ki = k[i];
     unsigned l = tag_level(ki);
-    Key128 a = tag_anchor(ki);
-    bool ok = l <= D && key_shr(a, 3 * D).lo == 0 && key_shr(a, 3 * D).hi == 0;
+    Key128 a = morton_part(ki, D);
+    bool ok = l <= D && seg_of(ki, D) < nseg;
     if (ok && l < D) ok = key_eq(key_shl(key_shr(a, 3 * (D - l)), 3 * (D - l)), a);
     if (!ok) atomicOr(flags, DGF_DOMAIN);
     atomicAdd(&h[l & 31u], 1u);
@@ -323,7 +524,8 @@ __global__ void k_level_hist(const Key128 *__restrict__ k, size_t n, unsigned D,
   if (threadIdx.x < 32 && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], (unsigned long long)h[threadIdx.x]);
 }
 
-// level-(l-1) Morton index of the parent of every input leaf at level l
+// level-(l-1) index (cloud bits included) of the parent of every input leaf
+// at level l
 __global__ void k_leaf_parents(const Key128 *__restrict__ k, size_t n, unsigned D, unsigned l, Key128 *__restrict__ out) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = key_shr(tag_anchor(k[i]), 3 * (D - l + 1));
@@ -334,8 +536,17 @@ __global__ void k_leaf_parents(const Key128 *__restrict__ k, size_t n, unsigned 
 __global__ void k_block_parents(const Key128 *__restrict__ q, size_t nq, unsigned l, Key128 *__restrict__ out) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nq) return;
+  const Key128 qi = q[i];
+  const Key128 segk = key_shl(key_shr(qi, 3 * l), 3 * (l - 1));  // cloud bits at level l-1
+  Key128 idx = qi;
+  if (3 * l < 64) {
+    idx.lo &= (1ull << (3 * l)) - 1;
+    idx.hi = 0;
+  } else {
+    idx.hi &= (1ull << (3 * l - 64)) - 1;
+  }
   uint32_t c[3];
-  demorton3(q[i], c[0], c[1], c[2]);  // level-l integer coordinates
+  demorton3(idx, c[0], c[1], c[2]);  // level-l integer coordinates
   const int64_t side = (int64_t)1 << (l - 1);  // parents per axis
   int64_t opt[3][2];
 #pragma unroll
@@ -352,7 +563,7 @@ __global__ void k_block_parents(const Key128 *__restrict__ q, size_t nq, unsigne
       p1 = opt[1][0];
       p2 = opt[2][0];
     }
-    out[8 * i + t] = morton3((uint32_t)p0, (uint32_t)p1, (uint32_t)p2);
+    out[8 * i + t] = key_or(morton3((uint32_t)p0, (uint32_t)p1, (uint32_t)p2), segk);
   }
 }
 
@@ -380,6 +591,19 @@ __global__ void k_mark_internal(const Key128 *__restrict__ Il, size_t nl, const 
   R[8 * p + (Il[i].lo & 7u)] = (uint32_t)i;
 }
 
+// clouds whose root is internal: Rtop[cloud] = index of its root in I_0
+__global__ void k_mark_roots(const Key128 *__restrict__ I0, size_t n0, size_t nseg, uint32_t *__restrict__ Rtop,
+                             uint32_t *flags) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n0) return;
+  uint64_t sg = I0[i].lo;
+  if (I0[i].hi || sg >= nseg) {
+    atomicOr(flags, DGF_INTERNAL);
+    return;
+  }
+  Rtop[sg] = (uint32_t)i;
+}
+
 __global__ void k_subtree_count(const uint32_t *__restrict__ R, size_t np, const uint64_t *__restrict__ sub_child,
                                 uint64_t *__restrict__ sub) {
   size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -391,6 +615,26 @@ __global__ void k_subtree_count(const uint32_t *__restrict__ R, size_t np, const
     c += (x == 0xffffffffu) ? 1ull : sub_child[x];
   }
   sub[r] = c;
+}
+
+// leaf count of every cloud (1 when its root is a leaf)
+__global__ void k_cloud_count(const uint32_t *__restrict__ Rtop, size_t nseg, const uint64_t *__restrict__ sub0,
+                              uint64_t *__restrict__ cnt) {
+  size_t sg = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (sg >= nseg) return;
+  uint32_t x = Rtop[sg];
+  cnt[sg] = (x == 0xffffffffu) ? 1ull : sub0[x];
+}
+
+// place cloud roots: a leaf root is written out, an internal one passes its
+// offset to level 0
+__global__ void k_place_roots(const uint32_t *__restrict__ Rtop, size_t nseg, const uint64_t *__restrict__ cloud_off,
+                              unsigned D, uint64_t *__restrict__ off0, Key128 *__restrict__ out) {
+  size_t sg = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (sg >= nseg) return;
+  uint32_t x = Rtop[sg];
+  if (x == 0xffffffffu) out[cloud_off[sg]] = make_tagged(from_u128((u128)sg << (3 * D)), 0);
+  else off0[x] = cloud_off[sg];
 }
 
 __global__ void k_place(const Key128 *__restrict__ Ip, size_t np, unsigned l, unsigned D, const uint32_t *__restrict__ R,
@@ -418,22 +662,20 @@ __global__ void k_place(const Key128 *__restrict__ Ip, size_t np, unsigned l, un
 void balance_octree(Context &ctx, const Octree &in, Octree &out) {
   cudaStream_t s = ctx.stream;
   const unsigned D = in.max_depth;
+  const size_t nseg = in.nseg;
+  const unsigned SB = in.seg_bits;
   out.max_depth = D;
+  out.nseg = nseg;
+  out.seg_bits = SB;
   const size_t n = in.n;
   if (n == 0) fail(DG_ERR_INVALID_ARG, "balanceOctree: empty input");
-  if (n == 1) {
-    out.n = 1;
-    DG_CUDA(cudaMallocAsync((void **)&out.keys, sizeof(Key128), s));
-    DG_CUDA(cudaMemcpyAsync(out.keys, in.keys, sizeof(Key128), cudaMemcpyDeviceToDevice, s));
-    DG_CUDA(cudaStreamSynchronize(s));
-    return;
-  }
-  // level histogram
+  // level histogram + domain validation
   unsigned long long *d_hist = ctx.d_scratch + 16;
   DG_CUDA(cudaMemsetAsync(d_hist, 0, 32 * sizeof(unsigned long long), s));
+  DG_CUDA(cudaMemsetAsync(ctx.d_flags, 0, sizeof(uint32_t), s));
   {
-    ProfScope _prof("bal_level_hist", (double)n * 16);
-    k_level_hist<<<grid_for(n, 256, ctx.num_sms * 4), 256, 0, s>>>(in.keys, n, D, d_hist, ctx.d_flags);
+    ProfScope _prof(ctx, "bal_level_hist", (double)n * 16);
+    k_level_hist<<<grid_for(n, 256, ctx.num_sms * 4), 256, 0, s>>>(in.keys, n, D, nseg, d_hist, ctx.d_flags);
     DG_LAUNCH_CHECK();
   }
   check_device_flags(ctx, "balanceOctree (octant outside the domain or misaligned)");
@@ -444,22 +686,21 @@ void balance_octree(Context &ctx, const Octree &in, Octree &out) {
   unsigned maxL = 0;
   for (unsigned l = 0; l < 32; l++)
     if (hcnt[l]) maxL = l;
-  if (maxL > D) fail(DG_ERR_INVALID_ARG, "balanceOctree: octant level exceeds maxDepth");
 
   // bucket the leaves by level (one stable radix pass on the level byte);
-  // every bucket stays in Morton order
+  // every bucket stays in (cloud, Morton) order
   DBuf<Key128> bucketed(n, s);
   {
     size_t ntiles = (n + RS_TILE - 1) / RS_TILE;
     DBuf<uint32_t> hist(256 * ntiles, s);
     {
-      ProfScope _prof("rs_hist", (double)n * 16);
+      ProfScope _prof(ctx, "rs_hist", (double)n * 16);
       k_rs_hist<Key128><<<(unsigned)ntiles, RS_BLOCK, 0, s>>>(in.keys, n, 120, hist.get(), ntiles);
       DG_LAUNCH_CHECK();
     }
     exclusive_scan<uint32_t, uint32_t>(hist.get(), hist.get(), 256 * ntiles, (uint32_t *)nullptr, s);
     {
-      ProfScope _prof("rs_scatter", (double)n * 32);
+      ProfScope _prof(ctx, "rs_scatter", (double)n * 32);
       k_rs_scatter<Key128><<<(unsigned)ntiles, RS_BLOCK, 0, s>>>(in.keys, bucketed.get(), n, 120, hist.get(), ntiles);
       DG_LAUNCH_CHECK();
     }
@@ -475,41 +716,42 @@ void balance_octree(Context &ctx, const Octree &in, Octree &out) {
     if (nc == 0) continue;
     DBuf<Key128> cand(nc, s), ctmp(nc, s);
     if (nt) {
-      {
-    ProfScope _prof(ctx, "bal_leaf_parents", (double)nt * 32);
-    k_leaf_parents<<<grid_for(nt, 256), 256, 0, s>>>(bucketed.get() + boff[l], nt, D, (unsigned)l, cand.get());
+      ProfScope _prof(ctx, "bal_leaf_parents", (double)nt * 32);
+      k_leaf_parents<<<grid_for(nt, 256), 256, 0, s>>>(bucketed.get() + boff[l], nt, D, (unsigned)l, cand.get());
       DG_LAUNCH_CHECK();
-    }
     }
     if (nq) {
-      {
-    ProfScope _prof(ctx, "bal_block_parents", (double)nq * 144);
-    k_block_parents<<<grid_for(nq, 256), 256, 0, s>>>(I[l].get(), nq, (unsigned)l, cand.get() + nt);
+      ProfScope _prof(ctx, "bal_block_parents", (double)nq * 144);
+      k_block_parents<<<grid_for(nq, 256), 256, 0, s>>>(I[l].get(), nq, (unsigned)l, cand.get() + nt);
       DG_LAUNCH_CHECK();
     }
-    }
     Key128 *res;
-    size_t nu = sort_unique<Key128>(ctx, cand.get(), ctmp.get(), nc, 3 * (l - 1), &res);
+    size_t nu = sort_unique<Key128>(ctx, cand.get(), ctmp.get(), nc, 3 * (l - 1) + (int)SB, &res);
     DBuf<Key128> Il(nu, s);
     DG_CUDA(cudaMemcpyAsync(Il.get(), res, nu * sizeof(Key128), cudaMemcpyDeviceToDevice, s));
     I[l - 1] = std::move(Il);
     nI[l - 1] = nu;
   }
-  if (nI[0] != 1) fail(DG_ERR_INTERNAL, "balanceOctree: root is not internal");
+  bucketed.release();
 
   // rank maps R_l (l = 0..maxL-1): children of I_l that are internal
   std::vector<DBuf<uint32_t>> R(maxL + 1);
-  DG_CUDA(cudaMemsetAsync(ctx.d_flags, 0, sizeof(uint32_t), s));
   for (unsigned l = 0; l + 1 <= maxL; l++) {
     if (!nI[l] || !nI[l + 1]) continue;
     R[l].alloc(8 * nI[l], s);
     DG_CUDA(cudaMemsetAsync(R[l].get(), 0xff, 8 * nI[l] * sizeof(uint32_t), s));
     {
-    ProfScope _prof(ctx, "bal_mark_internal", (double)nI[l + 1] * 20);
-    k_mark_internal<<<grid_for(nI[l + 1], 256), 256, 0, s>>>(I[l + 1].get(), nI[l + 1], I[l].get(), nI[l], R[l].get(),
-                                                             ctx.d_flags);
-    DG_LAUNCH_CHECK();
+      ProfScope _prof(ctx, "bal_mark_internal", (double)nI[l + 1] * 20);
+      k_mark_internal<<<grid_for(nI[l + 1], 256), 256, 0, s>>>(I[l + 1].get(), nI[l + 1], I[l].get(), nI[l],
+                                                               R[l].get(), ctx.d_flags);
+      DG_LAUNCH_CHECK();
     }
+  }
+  DBuf<uint32_t> Rtop(nseg, s);
+  DG_CUDA(cudaMemsetAsync(Rtop.get(), 0xff, nseg * sizeof(uint32_t), s));
+  if (maxL > 0 && nI[0]) {
+    k_mark_roots<<<grid_for(nI[0], 256), 256, 0, s>>>(I[0].get(), nI[0], nseg, Rtop.get(), ctx.d_flags);
+    DG_LAUNCH_CHECK();
   }
   check_device_flags(ctx, "balanceOctree");
   // bottom-up leaf counts
@@ -518,40 +760,48 @@ void balance_octree(Context &ctx, const Octree &in, Octree &out) {
     if (!nI[l]) continue;
     sub[l].alloc(nI[l], s);
     {
-    ProfScope _prof(ctx, "bal_subtree_count", (double)nI[l] * 72);
-    k_subtree_count<<<grid_for(nI[l], 256), 256, 0, s>>>(R[l].get(), nI[l], sub[l + 1].get(), sub[l].get());
-    DG_LAUNCH_CHECK();
+      ProfScope _prof(ctx, "bal_subtree_count", (double)nI[l] * 72);
+      k_subtree_count<<<grid_for(nI[l], 256), 256, 0, s>>>(R[l].get(), nI[l], sub[l + 1].get(), sub[l].get());
+      DG_LAUNCH_CHECK();
     }
   }
-  size_t total = (size_t)read_scalar(ctx, sub[0].get());
+  DBuf<uint64_t> ccnt(nseg, s), coff(nseg + 1, s);
+  k_cloud_count<<<grid_for(nseg, 256), 256, 0, s>>>(Rtop.get(), nseg, sub[0].get(), ccnt.get());
+  DG_LAUNCH_CHECK();
+  uint64_t *d_total = reinterpret_cast<uint64_t *>(ctx.d_scratch);
+  exclusive_scan<uint64_t, uint64_t>(ccnt.get(), coff.get(), nseg, d_total, s);
+  size_t total = (size_t)read_scalar(ctx, d_total);
+  DG_CUDA(cudaMemcpyAsync(coff.get() + nseg, d_total, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
   DBuf<Key128> res(total, s);
   // top-down placement
-  DBuf<uint64_t> off_cur(1, s);
-  DG_CUDA(cudaMemsetAsync(off_cur.get(), 0, sizeof(uint64_t), s));
+  DBuf<uint64_t> off_cur(nI[0] ? nI[0] : 1, s);
+  k_place_roots<<<grid_for(nseg, 256), 256, 0, s>>>(Rtop.get(), nseg, coff.get(), D, off_cur.get(), res.get());
+  DG_LAUNCH_CHECK();
   for (unsigned l = 0; l < maxL; l++) {
     if (!nI[l]) break;
     DBuf<uint64_t> off_next(nI[l + 1] ? nI[l + 1] : 1, s);
     {
-    ProfScope _prof(ctx, "bal_place", (double)nI[l] * 24);
-    k_place<<<grid_for(nI[l], 256), 256, 0, s>>>(I[l].get(), nI[l], l, D, R[l].get(), sub[l + 1].get(), off_cur.get(),
-                                                 off_next.get(), res.get());
-    DG_LAUNCH_CHECK();
+      ProfScope _prof(ctx, "bal_place", (double)nI[l] * 24);
+      k_place<<<grid_for(nI[l], 256), 256, 0, s>>>(I[l].get(), nI[l], l, D, R[l].get(), sub[l + 1].get(),
+                                                   off_cur.get(), off_next.get(), res.get());
+      DG_LAUNCH_CHECK();
     }
     off_cur = std::move(off_next);
   }
   DG_CUDA(cudaStreamSynchronize(s));
   out.n = total;
   out.keys = res.release_ptr();
+  out.seg_off = nseg > 1 ? coff.release_ptr() : nullptr;
 }
 
 // ------------------------------------------------------------------------
 // conversions
 // ------------------------------------------------------------------------
-__global__ void k_to_xyzl(const Key128 *__restrict__ k, size_t n, uint4 *__restrict__ out) {
+__global__ void k_to_xyzl(const Key128 *__restrict__ k, size_t n, unsigned D, uint4 *__restrict__ out) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint32_t x, y, z;
-  demorton3(tag_anchor(k[i]), x, y, z);
+  demorton3(morton_part(k[i], D), x, y, z);
   out[i] = make_uint4(x, y, z, tag_level(k[i]));
 }
 
@@ -572,7 +822,7 @@ void octree_to_xyzl(Context &ctx, const Octree &o, uint32_t *d_xyzl) {
   if (!o.n) return;
   {
     ProfScope _prof("to_xyzl", (double)o.n * 32);
-    k_to_xyzl<<<grid_for(o.n, 256), 256, 0, ctx.stream>>>(o.keys, o.n, reinterpret_cast<uint4 *>(d_xyzl));
+    k_to_xyzl<<<grid_for(o.n, 256), 256, 0, ctx.stream>>>(o.keys, o.n, o.max_depth, reinterpret_cast<uint4 *>(d_xyzl));
     DG_LAUNCH_CHECK();
   }
 }
@@ -595,8 +845,8 @@ void octree_from_xyzl(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned D
 
 void octree_free(Context &ctx, Octree &o) {
   if (o.keys) cudaFreeAsync(o.keys, ctx.stream);
-  o.keys = nullptr;
-  o.n = 0;
+  if (o.seg_off) cudaFreeAsync(o.seg_off, ctx.stream);
+  o = Octree();
 }
 
 }  // namespace dg

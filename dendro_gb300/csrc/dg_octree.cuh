@@ -17,17 +17,36 @@ __host__ __device__ __forceinline__ Key128 make_tagged(Key128 anchor, unsigned l
   return Key128{anchor.lo, (anchor.hi & TAG_MASK) | ((uint64_t)lev << 56)};
 }
 
+// A batch of independent octrees ("segments", one per point cloud) shares
+// one key array: segment s occupies keys [seg_off[s], seg_off[s+1]) and its
+// keys carry s in bits [3D, 3D + seg_bits), so one sort orders the whole
+// batch by cloud, then by Morton order within each cloud.
 struct Octree {
   unsigned max_depth = 0;
   size_t n = 0;
-  Key128 *keys = nullptr;  // tagged, sorted
+  Key128 *keys = nullptr;      // tagged, sorted
+  size_t nseg = 1;
+  unsigned seg_bits = 0;
+  uint64_t *seg_off = nullptr;  // device, nseg + 1 (null for one segment)
 };
+
+inline unsigned bits_for(size_t nseg) {
+  unsigned b = 0;
+  while (b < 40 && ((size_t)1 << b) < nseg) b++;
+  return b;
+}
 
 void octree_free(Context &ctx, Octree &o);
 
-// ot::points2Octree (src/construct.cpp:759) on device-resident FP64 xyz.
+// ot::points2Octree (src/construct.cpp:759) on device-resident FP64 xyz, for
+// a batch of clouds: cloud s holds points [h_seg_start[s], h_seg_start[s+1])
+// (host array of nseg + 1 entries; null for a single cloud).  Each cloud's
+// octree is the one the reference builds for that cloud alone.
 void points_to_octree(Context &ctx, const double *d_xyz, size_t n, const double glens[3], unsigned max_depth,
-                      unsigned max_pts, Octree &out);
+                      unsigned max_pts, Octree &out, const uint64_t *h_seg_start = nullptr, size_t nseg = 1);
+
+// per-segment output offsets of a batched octree, on the host
+void octree_segment_offsets(Context &ctx, const Octree &o, uint64_t *h_off);
 
 // Morton sort of level-D point anchors (par::sampleSort / removeDuplicates
 // step); returns sorted tagged keys in d_out and the number of distinct

@@ -13,9 +13,17 @@ namespace dg {
 struct WOct {
   uint32_t x, y, z, lev;
 };
-__host__ __device__ __forceinline__ WOct wo_from_key(Key128 k) {
+// the point's anchor within its cloud (segment bits above 3D dropped)
+__host__ __device__ __forceinline__ WOct wo_from_key(Key128 k, unsigned D) {
   WOct o;
-  demorton3(tag_anchor(k), o.x, o.y, o.z);
+  Key128 a = tag_anchor(k);
+  if (3 * D < 64) {
+    a.lo &= (1ull << (3 * D)) - 1;
+    a.hi = 0;
+  } else {
+    a.hi &= (1ull << (3 * D - 64)) - 1;
+  }
+  demorton3(a, o.x, o.y, o.z);
   o.lev = tag_level(k);
   return o;
 }
@@ -54,9 +62,11 @@ __host__ __device__ __forceinline__ WOct wo_dld(const WOct &a, unsigned D) {
 // below stops there, and also after a step bound no terminating walk reaches.
 constexpr size_t P2O_WALK_NO_END = ~(size_t)0;
 
-// Runs the walk over n sorted level-D point keys; writes the octants to out
-// (when not null) and returns their count, or P2O_WALK_NO_END.
-__host__ __device__ inline size_t p2o_walk(const Key128 *pk, size_t n, unsigned m, unsigned D, Key128 *out) {
+// Runs the walk over the n sorted level-D point keys of one cloud; writes the
+// octants (with the cloud's segment key `seg` or-ed in) to out when not null
+// and returns their count, or P2O_WALK_NO_END.
+__host__ __device__ inline size_t p2o_walk(const Key128 *pk, size_t n, unsigned m, unsigned D, Key128 *out,
+                                           Key128 seg = Key128{0, 0}) {
   const uint32_t num_pts = (uint32_t)n;
   WOct curr{0, 0, 0, 0};
   WOct last = wo_dld(curr, D);
@@ -68,7 +78,7 @@ __host__ __device__ inline size_t p2o_walk(const Key128 *pk, size_t n, unsigned 
     u128 k = wo_key(o);
     if (k == prev_key) return;  // std::list::unique
     prev_key = k;
-    if (out) out[w] = make_tagged(morton3(o.x, o.y, o.z), o.lev);
+    if (out) out[w] = make_tagged(key_or(morton3(o.x, o.y, o.z), seg), o.lev);
     w++;
   };
   const uint64_t max_steps = 64ull * ((uint64_t)n + 1) * (D + 2);
@@ -76,7 +86,7 @@ __host__ __device__ inline size_t p2o_walk(const Key128 *pk, size_t n, unsigned 
   while (next_pt < num_pts) {
     if (curr.lev > D || ++steps > max_steps) return P2O_WALK_NO_END;
     for (;;) {
-      WOct a = wo_from_key(pk[next_pt - 1]), b = wo_from_key(pk[next_pt]);
+      WOct a = wo_from_key(pk[next_pt - 1], D), b = wo_from_key(pk[next_pt], D);
       if (!(wo_is_anc(curr, a, D) && wo_is_anc(curr, b, D) && curr.lev < D)) break;
       curr.lev++;
       next = wo_next(curr, D);
@@ -95,7 +105,7 @@ __host__ __device__ inline size_t p2o_walk(const Key128 *pk, size_t n, unsigned 
     uint32_t lo = curr_pt, hi = next_pt;
     while (lo < hi) {
       uint32_t mid = lo + (hi - lo) / 2;
-      if (wo_key(wo_from_key(pk[mid])) <= nk) lo = mid + 1;
+      if (wo_key(wo_from_key(pk[mid], D)) <= nk) lo = mid + 1;
       else hi = mid;
     }
     int found_pt = (int)(lo - curr_pt);

@@ -72,6 +72,21 @@ int dg_version(void);
 int dg_points_to_octree(dg_ctx ctx, const double *xyz, size_t n, const double gLens[3], unsigned maxDepth,
                         unsigned maxNumPtsPerOctant, int comm_size, int xyz_on_device, dg_octree *out);
 
+/* ---- batches of clouds ------------------------------------------------------
+ * points2Octree for nseg independent clouds in one pass: cloud s holds the
+ * points [seg_start[s], seg_start[s+1]) of xyz (seg_start: host array of
+ * nseg + 1 offsets, seg_start[0] = 0, seg_start[nseg] = n).  The resulting
+ * handle holds the nseg octrees back to back, each identical to what
+ * dg_points_to_octree returns for that cloud alone; dg_balance_octree on it
+ * balances every cloud independently.  dg_octree_segments reports where each
+ * cloud's octants start.  No counterpart in the reference (one cloud per
+ * call, construct.cpp:759). */
+int dg_points_to_octree_batch(dg_ctx ctx, const double *xyz, size_t n, const uint64_t *seg_start, size_t nseg,
+                              const double gLens[3], unsigned maxDepth, unsigned maxNumPtsPerOctant,
+                              int xyz_on_device, dg_octree *out);
+/* offsets: host array of nseg + 1 entries (may be NULL to query nseg) */
+int dg_octree_segments(dg_ctx ctx, dg_octree o, size_t *nseg, uint64_t *offsets);
+
 /* ---- par::sampleSort + par::removeDuplicates of point octants -------------
  * include/parUtils.h:424,437 (1-rank branch parUtils.tcc:1868-1875): the
  * points quantised to level maxDepth, sorted in Morton order, duplicates
@@ -91,6 +106,7 @@ int dg_balance_octree(dg_ctx ctx, dg_octree in, int incCorner, int comm_size, dg
  * Materialise / import the std::vector<ot::TreeNode> of the reference as
  * {x, y, z, level} records. */
 int dg_octree_size(dg_octree o, size_t *n, unsigned *maxDepth);
+/* DA handles accept single-cloud octrees only (DG_ERR_UNSUPPORTED otherwise). */
 int dg_octree_download(dg_ctx ctx, dg_octree o, uint32_t *xyzl, int dst_on_device);
 int dg_octree_upload(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDepth, int src_on_device, dg_octree *out);
 int dg_octree_free(dg_ctx ctx, dg_octree o);
