@@ -203,12 +203,14 @@ __global__ void k_fill_emit(const Key128 *__restrict__ seeds, size_t ns, unsigne
 __global__ void k_p2o_walk_segments(const Key128 *__restrict__ pk, const uint64_t *__restrict__ pt_start,
                                     const uint32_t *__restrict__ dup_list, unsigned m, unsigned D,
                                     const uint64_t *__restrict__ out_off, Key128 *__restrict__ out,
-                                    unsigned long long *counts) {
+                                    unsigned long long *counts, bool batched) {
   if (threadIdx.x != 0) return;
   const uint32_t s = dup_list[blockIdx.x];
   const size_t b = pt_start[s], e = pt_start[s + 1];
-  size_t c = p2o_walk(pk + b, e - b, m, D, out ? out + out_off[blockIdx.x] : nullptr, seg_key(s, D));
+  bool outside = false;
+  size_t c = p2o_walk(pk + b, e - b, m, D, out ? out + out_off[blockIdx.x] : nullptr, seg_key(s, D), &outside);
   counts[blockIdx.x] = c;
+  if (outside && batched) counts[blockIdx.x] = (unsigned long long)P2O_WALK_OUTSIDE;
 }
 
 // first index of each cloud in a sorted key array (lower bound of s << 3D)
@@ -227,23 +229,29 @@ __global__ void k_seg_bounds(const Key128 *__restrict__ keys, size_t n, unsigned
 }
 
 // place each cloud's octants at their final offsets: clouds with repeated
-// points take the walk's output, the others the parallel construction's
+// points take the walk's output, the others the parallel construction's.
+// The walk outputs are stored cloud after cloud in dup-list order; a walk
+// octant's cloud is found from its position (its key may lie outside the
+// cloud's domain, see dg_walk.cuh).
 __global__ void k_assemble(const Key128 *__restrict__ par, size_t npar, const uint64_t *__restrict__ par_off,
-                           const Key128 *__restrict__ walk, const uint64_t *__restrict__ walk_off,
-                           const uint32_t *__restrict__ walk_slot, const uint32_t *__restrict__ dupseg,
+                           const Key128 *__restrict__ walk, const uint64_t *__restrict__ walk_off, size_t nd,
+                           const uint32_t *__restrict__ dup_list, const uint32_t *__restrict__ dupseg, size_t nseg,
                            const uint64_t *__restrict__ final_off, unsigned D, Key128 *__restrict__ out,
                            size_t nwalk_total) {
   size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j < npar) {
     uint64_t s = seg_of(par[j], D);
-    if (!dupseg[s]) out[final_off[s] + (j - par_off[s])] = par[j];
+    if (s < nseg && !dupseg[s]) out[final_off[s] + (j - par_off[s])] = par[j];
   }
   if (j < nwalk_total) {
-    // walk outputs are stored cloud after cloud in dup-list order
-    Key128 k = walk[j];
-    uint64_t s = seg_of(k, D);
-    uint32_t slot = walk_slot[s];
-    out[final_off[s] + (j - walk_off[slot])] = k;
+    size_t lo = 0, hi = nd;  // last slot with walk_off[slot] <= j
+    while (hi - lo > 1) {
+      size_t mid = (lo + hi) / 2;
+      if (walk_off[mid] <= j) lo = mid;
+      else hi = mid;
+    }
+    uint32_t s = dup_list[lo];
+    out[final_off[s] + (j - walk_off[lo])] = walk[j];
   }
 }
 
@@ -435,15 +443,14 @@ void points_to_octree(Context &ctx, const double *d_xyz, size_t n, const double 
     h_pt_start[1] = n;
   }
   DBuf<uint64_t> d_pt_start(nseg + 1, s), d_walk_off(nd + 1, s);
-  DBuf<uint32_t> d_dup_list(nd, s), d_walk_slot(nseg, s);
+  DBuf<uint32_t> d_dup_list(nd, s);
   DBuf<unsigned long long> d_counts(nd, s);
   DG_CUDA(cudaMemcpyAsync(d_pt_start.get(), h_pt_start.data(), (nseg + 1) * 8, cudaMemcpyHostToDevice, s));
   DG_CUDA(cudaMemcpyAsync(d_dup_list.get(), dup_list.data(), nd * 4, cudaMemcpyHostToDevice, s));
-  DG_CUDA(cudaMemcpyAsync(d_walk_slot.get(), walk_slot.data(), nseg * 4, cudaMemcpyHostToDevice, s));
   {
     ProfScope _prof(ctx, "p2o_walk_serial", (double)n * 16);
     k_p2o_walk_segments<<<(unsigned)nd, 32, 0, s>>>(p, d_pt_start.get(), d_dup_list.get(), m, D, nullptr, nullptr,
-                                                    d_counts.get());
+                                                    d_counts.get(), nseg > 1);
     DG_LAUNCH_CHECK();
   }
   std::vector<unsigned long long> h_counts(nd);
@@ -454,6 +461,10 @@ void points_to_octree(Context &ctx, const double *d_xyz, size_t n, const double 
     if (h_counts[i] == (unsigned long long)P2O_WALK_NO_END)
       fail(DG_ERR_INVALID_ARG,
            "points2Octree: with these repeated points the reference construction walk never terminates");
+    if (h_counts[i] == (unsigned long long)P2O_WALK_OUTSIDE)
+      fail(DG_ERR_DOMAIN,
+           "points2Octree: with these repeated points the reference construction emits octants outside the domain, "
+           "which a batch can not hold (build this cloud alone)");
     h_walk_off[i + 1] = h_walk_off[i] + h_counts[i];
   }
   const size_t nwalk = h_walk_off[nd];
@@ -462,7 +473,7 @@ void points_to_octree(Context &ctx, const double *d_xyz, size_t n, const double 
   {
     ProfScope _prof(ctx, "p2o_walk_serial", (double)n * 16 + (double)nwalk * 16);
     k_p2o_walk_segments<<<(unsigned)nd, 32, 0, s>>>(p, d_pt_start.get(), d_dup_list.get(), m, D, d_walk_off.get(),
-                                                    walk_out.get(), d_counts.get());
+                                                    walk_out.get(), d_counts.get(), nseg > 1);
     DG_LAUNCH_CHECK();
   }
   // final offsets
@@ -478,8 +489,9 @@ void points_to_octree(Context &ctx, const double *d_xyz, size_t n, const double 
   {
     ProfScope _prof(ctx, "p2o_assemble", (double)(npar + nwalk) * 32);
     k_assemble<<<grid_for(std::max(npar, nwalk), 256), 256, 0, s>>>(res.get(), npar, seg_off.get(), walk_out.get(),
-                                                                    d_walk_off.get(), d_walk_slot.get(), dupseg.get(),
-                                                                    d_final.get(), D, fin.get(), nwalk);
+                                                                    d_walk_off.get(), nd, d_dup_list.get(),
+                                                                    dupseg.get(), nseg, d_final.get(), D, fin.get(),
+                                                                    nwalk);
     DG_LAUNCH_CHECK();
   }
   out.n = nfinal;
@@ -526,14 +538,19 @@ __global__ void k_level_hist(const Key128 *__restrict__ k, size_t n, unsigned D,
 
 // level-(l-1) index (cloud bits included) of the parent of every input leaf
 // at level l
-__global__ void k_leaf_parents(const Key128 *__restrict__ k, size_t n, unsigned D, unsigned l, Key128 *__restrict__ out) {
+__device__ __forceinline__ void put_key(Key128 *out, size_t i, Key128 v) { out[i] = v; }
+__device__ __forceinline__ void put_key(uint64_t *out, size_t i, Key128 v) { out[i] = v.lo; }
+
+template <typename K>
+__global__ void k_leaf_parents(const Key128 *__restrict__ k, size_t n, unsigned D, unsigned l, K *__restrict__ out) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = key_shr(tag_anchor(k[i]), 3 * (D - l + 1));
+  if (i < n) put_key(out, i, key_shr(tag_anchor(k[i]), 3 * (D - l + 1)));
 }
 
 // for q at level l: the 8 level-(l-1) parents of q's 3x3x3 block; parents
 // outside the domain are replaced by q's own parent (removed by the unique)
-__global__ void k_block_parents(const Key128 *__restrict__ q, size_t nq, unsigned l, Key128 *__restrict__ out) {
+template <typename K>
+__global__ void k_block_parents(const Key128 *__restrict__ q, size_t nq, unsigned l, K *__restrict__ out) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nq) return;
   const Key128 qi = q[i];
@@ -563,8 +580,13 @@ __global__ void k_block_parents(const Key128 *__restrict__ q, size_t nq, unsigne
       p1 = opt[1][0];
       p2 = opt[2][0];
     }
-    out[8 * i + t] = key_or(morton3((uint32_t)p0, (uint32_t)p1, (uint32_t)p2), segk);
+    put_key(out, 8 * i + t, key_or(morton3((uint32_t)p0, (uint32_t)p1, (uint32_t)p2), segk));
   }
+}
+
+__global__ void k_widen(const uint64_t *__restrict__ in, size_t n, Key128 *__restrict__ out) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = Key128{in[i], 0};
 }
 
 __device__ __forceinline__ size_t lower_bound_key(const Key128 *a, size_t n, Key128 v) {
@@ -714,23 +736,51 @@ void balance_octree(Context &ctx, const Octree &in, Octree &out) {
     size_t nt = hcnt[l], nq = nI[l];
     size_t nc = nt + 8 * nq;
     if (nc == 0) continue;
-    DBuf<Key128> cand(nc, s), ctmp(nc, s);
-    if (nt) {
-      ProfScope _prof(ctx, "bal_leaf_parents", (double)nt * 32);
-      k_leaf_parents<<<grid_for(nt, 256), 256, 0, s>>>(bucketed.get() + boff[l], nt, D, (unsigned)l, cand.get());
-      DG_LAUNCH_CHECK();
+    const int kbits = 3 * (l - 1) + (int)SB;
+    if (kbits <= 64) {
+      // level-(l-1) indices fit one word: sort 8-byte keys
+      DBuf<uint64_t> cand(nc, s), ctmp(nc, s);
+      if (nt) {
+        ProfScope _prof(ctx, "bal_leaf_parents", (double)nt * 24);
+        k_leaf_parents<uint64_t><<<grid_for(nt, 256), 256, 0, s>>>(bucketed.get() + boff[l], nt, D, (unsigned)l,
+                                                                   cand.get());
+        DG_LAUNCH_CHECK();
+      }
+      if (nq) {
+        ProfScope _prof(ctx, "bal_block_parents", (double)nq * 80);
+        k_block_parents<uint64_t><<<grid_for(nq, 256), 256, 0, s>>>(I[l].get(), nq, (unsigned)l, cand.get() + nt);
+        DG_LAUNCH_CHECK();
+      }
+      uint64_t *res;
+      size_t nu = sort_unique<uint64_t>(ctx, cand.get(), ctmp.get(), nc, kbits, &res);
+      DBuf<Key128> Il(nu, s);
+      {
+        ProfScope _prof(ctx, "bal_widen", (double)nu * 24);
+        k_widen<<<grid_for(nu, 256), 256, 0, s>>>(res, nu, Il.get());
+        DG_LAUNCH_CHECK();
+      }
+      I[l - 1] = std::move(Il);
+      nI[l - 1] = nu;
+    } else {
+      DBuf<Key128> cand(nc, s), ctmp(nc, s);
+      if (nt) {
+        ProfScope _prof(ctx, "bal_leaf_parents", (double)nt * 32);
+        k_leaf_parents<Key128><<<grid_for(nt, 256), 256, 0, s>>>(bucketed.get() + boff[l], nt, D, (unsigned)l,
+                                                                 cand.get());
+        DG_LAUNCH_CHECK();
+      }
+      if (nq) {
+        ProfScope _prof(ctx, "bal_block_parents", (double)nq * 144);
+        k_block_parents<Key128><<<grid_for(nq, 256), 256, 0, s>>>(I[l].get(), nq, (unsigned)l, cand.get() + nt);
+        DG_LAUNCH_CHECK();
+      }
+      Key128 *res;
+      size_t nu = sort_unique<Key128>(ctx, cand.get(), ctmp.get(), nc, kbits, &res);
+      DBuf<Key128> Il(nu, s);
+      DG_CUDA(cudaMemcpyAsync(Il.get(), res, nu * sizeof(Key128), cudaMemcpyDeviceToDevice, s));
+      I[l - 1] = std::move(Il);
+      nI[l - 1] = nu;
     }
-    if (nq) {
-      ProfScope _prof(ctx, "bal_block_parents", (double)nq * 144);
-      k_block_parents<<<grid_for(nq, 256), 256, 0, s>>>(I[l].get(), nq, (unsigned)l, cand.get() + nt);
-      DG_LAUNCH_CHECK();
-    }
-    Key128 *res;
-    size_t nu = sort_unique<Key128>(ctx, cand.get(), ctmp.get(), nc, 3 * (l - 1) + (int)SB, &res);
-    DBuf<Key128> Il(nu, s);
-    DG_CUDA(cudaMemcpyAsync(Il.get(), res, nu * sizeof(Key128), cudaMemcpyDeviceToDevice, s));
-    I[l - 1] = std::move(Il);
-    nI[l - 1] = nu;
   }
   bucketed.release();
 
@@ -797,11 +847,14 @@ void balance_octree(Context &ctx, const Octree &in, Octree &out) {
 // ------------------------------------------------------------------------
 // conversions
 // ------------------------------------------------------------------------
-__global__ void k_to_xyzl(const Key128 *__restrict__ k, size_t n, unsigned D, uint4 *__restrict__ out) {
+// (a single cloud may hold octants just outside its domain: the reference's
+// construction emits them for some inputs with repeated points; their
+// anchor bits then run past 3D and are decoded as is)
+__global__ void k_to_xyzl(const Key128 *__restrict__ k, size_t n, unsigned D, bool batched, uint4 *__restrict__ out) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint32_t x, y, z;
-  demorton3(morton_part(k[i], D), x, y, z);
+  demorton3(batched ? morton_part(k[i], D) : tag_anchor(k[i]), x, y, z);
   out[i] = make_uint4(x, y, z, tag_level(k[i]));
 }
 
@@ -822,7 +875,8 @@ void octree_to_xyzl(Context &ctx, const Octree &o, uint32_t *d_xyzl) {
   if (!o.n) return;
   {
     ProfScope _prof("to_xyzl", (double)o.n * 32);
-    k_to_xyzl<<<grid_for(o.n, 256), 256, 0, ctx.stream>>>(o.keys, o.n, o.max_depth, reinterpret_cast<uint4 *>(d_xyzl));
+    k_to_xyzl<<<grid_for(o.n, 256), 256, 0, ctx.stream>>>(o.keys, o.n, o.max_depth, o.nseg > 1,
+                                                          reinterpret_cast<uint4 *>(d_xyzl));
     DG_LAUNCH_CHECK();
   }
 }

@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "dg_common.cuh"
 #include "dg_runtime.cuh"
 
@@ -308,52 +310,228 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_scatter(const K *__restrict__ i
   }
 }
 
-// Sort n keys (stable).  Only digits of bits [0, end_bit) on which the keys
-// differ are processed.  Returns the buffer that holds the result (keys or
-// tmp).  n must be < 2^32.
+// ------------------------------------------------------------------------
+// single-pass-per-digit ("onesweep") radix sort
+//   1. one read of all keys builds the 256-bin histogram of every digit
+//      position that is sorted; digits with a single occupied bin are
+//      skipped; the digit offsets come from these histograms
+//   2. per digit, one kernel: a block takes the next tile (ticket order),
+//      counts its digits, publishes the counts, looks back over the
+//      preceding tiles' published counts (decoupled look-back) for its
+//      global offsets, and scatters its keys stably
+// Look-back waits are bounded: a wait that exceeds the bound sets
+// DGF_TIMEOUT and the host reports DG_ERR_TIMEOUT.
+// ------------------------------------------------------------------------
+constexpr int OS_MAX_PASSES = 16;
+constexpr uint64_t OS_FLAG_AGG = 1ull << 62;
+constexpr uint64_t OS_FLAG_INCL = 2ull << 62;
+constexpr uint64_t OS_VALUE = (1ull << 62) - 1;
+constexpr unsigned OS_SPIN_LIMIT = 1u << 22;
+
+template <typename K>
+struct OsCfg {
+  static constexpr int ITEMS = sizeof(K) == 16 ? 8 : 16;
+  static constexpr int TILE = RS_BLOCK * ITEMS;
+  static constexpr int WARP_KEYS = TILE / RS_WARPS;
+};
+
+__device__ __forceinline__ uint64_t ld_relaxed(const uint64_t *p) {
+  uint64_t v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(uint64_t *p, uint64_t v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Histograms of every sorted digit position in one read of the keys.  Two
+// shared copies (even / odd lanes) halve the same-address contention that
+// skewed high digits cause.
+template <typename K>
+__global__ void __launch_bounds__(RS_BLOCK) k_rs_digit_hists(const K *__restrict__ keys, size_t n, int npass,
+                                                              const int *__restrict__ shifts,
+                                                              unsigned long long *__restrict__ ghist) {
+  __shared__ uint32_t h[2][OS_MAX_PASSES * 256];
+  __shared__ int sh[OS_MAX_PASSES];
+  for (int i = threadIdx.x; i < 2 * OS_MAX_PASSES * 256; i += blockDim.x) (&h[0][0])[i] = 0;
+  if (threadIdx.x < npass) sh[threadIdx.x] = shifts[threadIdx.x];
+  __syncthreads();
+  uint32_t *mine = h[threadIdx.x & 1];
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    K k = keys[i];
+    for (int p = 0; p < npass; p++) atomicAdd(&mine[p * 256 + KeyOps<K>::digit(k, sh[p])], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < npass * 256; i += blockDim.x) {
+    uint32_t v = h[0][i] + h[1][i];
+    if (v) atomicAdd(&ghist[i], (unsigned long long)v);
+  }
+}
+
+// One digit pass.  Keys are ranked in registers (warp-striped tile layout:
+// match_any gives the rank among equal digits of a warp round, per-warp
+// running counters order the rounds), placed in shared memory in digit
+// order, then written out so that consecutive threads write consecutive
+// addresses of each digit's run.
+template <typename K>
+__global__ void __launch_bounds__(RS_BLOCK) k_rs_onesweep(const K *__restrict__ in, K *__restrict__ out, size_t n,
+                                                          int shift, const uint64_t *__restrict__ digit_off,
+                                                          uint64_t *__restrict__ status, unsigned *tile_counter,
+                                                          uint32_t *flags) {
+  constexpr int ITEMS = OsCfg<K>::ITEMS, TILE = OsCfg<K>::TILE, WK = OsCfg<K>::WARP_KEYS;
+  __shared__ K tk[TILE];
+  __shared__ uint32_t wh[RS_WARPS][256];
+  __shared__ uint32_t s_local[256];
+  __shared__ uint64_t s_glob[256];
+  __shared__ unsigned s_tile;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
+#pragma unroll
+  for (int i = 0; i < 256 / 32; i++) wh[wid][i * 32 + lane] = 0;
+  __syncthreads();
+  const unsigned tile = s_tile;
+  const size_t base = (size_t)tile * TILE;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  K k[ITEMS];
+  unsigned d[ITEMS];
+  uint32_t rank[ITEMS];
+#pragma unroll
+  for (int r = 0; r < ITEMS; r++) {
+    size_t idx = base + (size_t)(wid * WK + r * 32 + lane);
+    if (idx < n) {
+      k[r] = in[idx];
+      d[r] = KeyOps<K>::digit(k[r], shift);
+    } else {
+      d[r] = 256u + lane;
+    }
+  }
+  // rank within the warp's part of the tile, in key order
+#pragma unroll
+  for (int r = 0; r < ITEMS; r++) {
+    const bool valid = d[r] < 256u;
+    unsigned peers = __match_any_sync(0xffffffffu, d[r]);
+    uint32_t cur = valid ? wh[wid][d[r]] : 0u;
+    __syncwarp();
+    if (valid && (peers & lt_mask) == 0) wh[wid][d[r]] = cur + __popc(peers);
+    __syncwarp();
+    rank[r] = cur + __popc(peers & lt_mask);
+  }
+  __syncthreads();
+  {
+    const unsigned dg = threadIdx.x;
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; w++) {
+      uint32_t c = wh[w][dg];
+      wh[w][dg] = run;
+      run += c;
+    }
+    uint32_t total_unused;
+    const uint32_t local = block_excl_scan<uint32_t, RS_BLOCK>(run, total_unused);
+    s_local[dg] = local;
+    uint64_t *my = status + (size_t)tile * 256 + dg;
+    uint64_t excl = 0;
+    if (tile == 0) {
+      st_relaxed(my, OS_FLAG_INCL | (uint64_t)run);
+    } else {
+      st_relaxed(my, OS_FLAG_AGG | (uint64_t)run);
+      long t = (long)tile - 1;
+      unsigned spins = 0;
+      while (t >= 0) {
+        uint64_t v = ld_relaxed(status + (size_t)t * 256 + dg);
+        if ((v & ~OS_VALUE) == 0) {
+          if (++spins > OS_SPIN_LIMIT) {
+            atomicOr(flags, DGF_TIMEOUT);
+            break;
+          }
+          __nanosleep(32);
+          continue;
+        }
+        excl += v & OS_VALUE;
+        if (v & OS_FLAG_INCL) break;
+        t--;
+      }
+      st_relaxed(my, OS_FLAG_INCL | (excl + run));
+    }
+    s_glob[dg] = digit_off[dg] + excl - (uint64_t)local;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < ITEMS; r++)
+    if (d[r] < 256u) tk[s_local[d[r]] + wh[wid][d[r]] + rank[r]] = k[r];
+  __syncthreads();
+  const size_t tile_n = (n - base < (size_t)TILE) ? n - base : (size_t)TILE;
+#pragma unroll
+  for (int i = 0; i < ITEMS; i++) {
+    const int p = i * RS_BLOCK + threadIdx.x;
+    if ((size_t)p < tile_n) {
+      K key = tk[p];
+      out[s_glob[KeyOps<K>::digit(key, shift)] + (uint64_t)p] = key;
+    }
+  }
+}
+
+// Sort n keys (stable) on the digits of bits [0, end_bit) (8-bit digits;
+// end_bit must not cut into bits that vary above it).  Digits on which all
+// keys agree are skipped.  Returns the buffer that holds the result (keys or
+// tmp).
 template <typename K>
 K *radix_sort(Context &ctx, K *keys, K *tmp, size_t n, int end_bit) {
-  if (n < 2) return keys;
+  if (n < 2 || end_bit <= 0) return keys;
   cudaStream_t s = ctx.stream;
-  unsigned long long init[4] = {0ull, 0ull, ~0ull, ~0ull};
-  unsigned long long *d_oa = ctx.d_scratch + 4;
-  DG_CUDA(cudaMemcpyAsync(d_oa, init, sizeof(init), cudaMemcpyHostToDevice, s));
-  unsigned g = grid_for(n, 256, (unsigned)(ctx.num_sms * 8));
+  int shifts[OS_MAX_PASSES];
+  int npass = 0;
+  for (int sh = 0; sh < end_bit && sh < KeyOps<K>::BITS && npass < OS_MAX_PASSES; sh += 8) shifts[npass++] = sh;
+  // histograms of every digit position, one read of the keys
+  DBuf<unsigned long long> ghist(npass * 256, s);
+  DBuf<int> dshifts(npass, s);
+  DG_CUDA(cudaMemcpyAsync(dshifts.get(), shifts, npass * sizeof(int), cudaMemcpyHostToDevice, s));
+  DG_CUDA(cudaMemsetAsync(ghist.get(), 0, npass * 256 * sizeof(unsigned long long), s));
   {
-    ProfScope _prof(ctx, "key_or_and", (double)n * sizeof(K));
-    k_key_or_and<K><<<g, 256, 0, s>>>(keys, n, d_oa);
+    ProfScope _prof(ctx, "rs_digit_hists", (double)n * sizeof(K));
+    unsigned g = grid_for(n, RS_BLOCK, (unsigned)(ctx.num_sms * 4));
+    k_rs_digit_hists<K><<<g, RS_BLOCK, 0, s>>>(keys, n, npass, dshifts.get(), ghist.get());
     DG_LAUNCH_CHECK();
   }
-  DG_CUDA(cudaMemcpyAsync(ctx.h_scratch + 4, d_oa, sizeof(init), cudaMemcpyDeviceToHost, s));
+  std::vector<unsigned long long> h(npass * 256);
+  DG_CUDA(cudaMemcpyAsync(h.data(), ghist.get(), h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
   DG_CUDA(cudaStreamSynchronize(s));
-  uint64_t vary_lo = ctx.h_scratch[4] ^ ctx.h_scratch[6];
-  uint64_t vary_hi = ctx.h_scratch[5] ^ ctx.h_scratch[7];
-
-  size_t ntiles = (n + RS_TILE - 1) / RS_TILE;
-  DBuf<uint32_t> hist(256 * ntiles, s);
+  std::vector<int> active;
+  std::vector<uint64_t> offs;
+  for (int p = 0; p < npass; p++) {
+    int occupied = 0;
+    for (int d = 0; d < 256; d++) occupied += h[p * 256 + d] != 0;
+    if (occupied <= 1) continue;  // every key has the same digit here
+    active.push_back(p);
+    uint64_t run = 0;
+    for (int d = 0; d < 256; d++) {
+      offs.push_back(run);
+      run += h[p * 256 + d];
+    }
+  }
+  if (active.empty()) return keys;
+  DBuf<uint64_t> doffs(offs.size(), s);
+  DG_CUDA(cudaMemcpyAsync(doffs.get(), offs.data(), offs.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+  const size_t ntiles = (n + OsCfg<K>::TILE - 1) / OsCfg<K>::TILE;
+  if (ntiles >= 0xffffffffull) fail(DG_ERR_INVALID_ARG, "radix sort: too many keys");
+  DBuf<uint64_t> status(ntiles * 256, s);
+  unsigned *d_counter = reinterpret_cast<unsigned *>(ctx.d_scratch + 12);
   K *src = keys, *dst = tmp;
-  for (int shift = 0; shift < end_bit && shift < KeyOps<K>::BITS; shift += 8) {
-    uint64_t mlo = 0, mhi = 0;
-    for (int b = shift; b < shift + 8 && b < end_bit; b++) {
-      if (b < 64) mlo |= 1ull << b;
-      else mhi |= 1ull << (b - 64);
-    }
-    if (!((vary_lo & mlo) | (vary_hi & mhi))) continue;
+  for (size_t a = 0; a < active.size(); a++) {
+    DG_CUDA(cudaMemsetAsync(status.get(), 0, ntiles * 256 * sizeof(uint64_t), s));
+    DG_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s));
     {
-    ProfScope _prof(ctx, "rs_hist", (double)n * sizeof(K));
-    k_rs_hist<K><<<(unsigned)ntiles, RS_BLOCK, 0, s>>>(src, n, shift, hist.get(), ntiles);
-    DG_LAUNCH_CHECK();
-    }
-    exclusive_scan<uint32_t, uint32_t>(hist.get(), hist.get(), 256 * ntiles, (uint32_t *)nullptr, s);
-    {
-    ProfScope _prof(ctx, "rs_scatter", (double)n * sizeof(K) * 2);
-    k_rs_scatter<K><<<(unsigned)ntiles, RS_BLOCK, 0, s>>>(src, dst, n, shift, hist.get(), ntiles);
-    DG_LAUNCH_CHECK();
+      ProfScope _prof(ctx, "rs_onesweep", (double)n * sizeof(K) * 2);
+      k_rs_onesweep<K><<<(unsigned)ntiles, RS_BLOCK, 0, s>>>(src, dst, n, shifts[active[a]], doffs.get() + 256 * a,
+                                                             status.get(), d_counter, ctx.d_flags);
+      DG_LAUNCH_CHECK();
     }
     K *t = src;
     src = dst;
     dst = t;
   }
+  check_device_flags(ctx, "radix sort");
   return src;
 }
 

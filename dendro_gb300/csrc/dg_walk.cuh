@@ -61,12 +61,14 @@ __host__ __device__ __forceinline__ WOct wo_dld(const WOct &a, unsigned D) {
 // forever (repeated points at a coarse maxDepth reach that state).  The walk
 // below stops there, and also after a step bound no terminating walk reaches.
 constexpr size_t P2O_WALK_NO_END = ~(size_t)0;
+// count reported for a batched cloud whose walk leaves the cloud's domain
+constexpr size_t P2O_WALK_OUTSIDE = ~(size_t)0 - 1;
 
 // Runs the walk over the n sorted level-D point keys of one cloud; writes the
 // octants (with the cloud's segment key `seg` or-ed in) to out when not null
 // and returns their count, or P2O_WALK_NO_END.
 __host__ __device__ inline size_t p2o_walk(const Key128 *pk, size_t n, unsigned m, unsigned D, Key128 *out,
-                                           Key128 seg = Key128{0, 0}) {
+                                           Key128 seg = Key128{0, 0}, bool *outside = nullptr) {
   const uint32_t num_pts = (uint32_t)n;
   WOct curr{0, 0, 0, 0};
   WOct last = wo_dld(curr, D);
@@ -78,6 +80,7 @@ __host__ __device__ inline size_t p2o_walk(const Key128 *pk, size_t n, unsigned 
     u128 k = wo_key(o);
     if (k == prev_key) return;  // std::list::unique
     prev_key = k;
+    if (outside && (o.x >> D || o.y >> D || o.z >> D)) *outside = true;
     if (out) out[w] = make_tagged(key_or(morton3(o.x, o.y, o.z), seg), o.lev);
     w++;
   };

@@ -404,6 +404,48 @@ done:
 }
 
 /* ------------------------------------------------------------------------ */
+/* coarsenOctree (src/coarsen.cpp:53-103): between consecutive first        */
+/* children (Morton child number 0), when at least 8 octants separate them,  */
+/* the first 8 are replaced by their parent and the rest are kept.           */
+/* ------------------------------------------------------------------------ */
+static unsigned child_number(const dgo_oct *o, unsigned D) {
+  if (o->lev == 0) return 0;
+  unsigned sh = D - o->lev;
+  return ((o->x >> sh) & 1u) | (((o->y >> sh) & 1u) << 1) | (((o->z >> sh) & 1u) << 2);
+}
+
+int dgo_coarsen(const dgo_oct *in, size_t n, unsigned D, dgo_oct **out, size_t *nout) {
+  dgo_oct *r = (dgo_oct *)malloc((n ? n : 1) * sizeof(dgo_oct));
+  if (!r) return DGO_ENOMEM;
+  size_t w = 0;
+  if (n < 8) { /* coarsen.cpp:66-70 */
+    for (size_t i = 0; i < n; i++) r[w++] = in[i];
+  } else {
+    size_t prev = 0;
+    while (prev < n) {
+      size_t curr = prev + 1;
+      while (curr < n && child_number(&in[curr], D) != 0) curr++;
+      if (curr >= prev + 8) {
+        dgo_oct p = in[prev];
+        unsigned pl = p.lev ? p.lev - 1 : 0, sh = D - pl;
+        p.x = (p.x >> sh) << sh;
+        p.y = (p.y >> sh) << sh;
+        p.z = (p.z >> sh) << sh;
+        p.lev = pl;
+        r[w++] = p;
+        for (size_t i = prev + 8; i < curr; i++) r[w++] = in[i];
+      } else {
+        for (size_t i = prev; i < curr; i++) r[w++] = in[i];
+      }
+      prev = curr;
+    }
+  }
+  *out = r;
+  *nout = w;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* checkers                                                                  */
 /* ------------------------------------------------------------------------ */
 int dgo_is_sorted_unique(const dgo_oct *a, size_t n, unsigned D) {

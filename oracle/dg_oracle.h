@@ -58,6 +58,11 @@ int dgo_p2o_local(const dgo_oct *pts, size_t n, unsigned maxDepth, unsigned maxP
  * (balance.cpp:801-1338, TreeNode.cpp:884-1342). */
 int dgo_balance(const dgo_oct *in, size_t n, unsigned maxDepth, dgo_oct **out, size_t *nout);
 
+/* ot::coarsenOctree, sequential form (src/coarsen.cpp:53): every complete
+ * family of 8 sibling leaves of a sorted, linear, complete octree is
+ * replaced by its parent. */
+int dgo_coarsen(const dgo_oct *in, size_t n, unsigned maxDepth, dgo_oct **out, size_t *nout);
+
 /* Checkers mirroring src/test/testUtils.C:18 (isLinear), :28 (isComplete)
  * and :82 (isBalanced with corners, maxLevDiff 1).  Return 1 / 0. */
 int dgo_is_sorted_unique(const dgo_oct *a, size_t n, unsigned maxDepth);

@@ -58,6 +58,7 @@ def lib():
         L.dgo_points_to_octree.argtypes = [P, SZ, P, U, U, ctypes.POINTER(P), ctypes.POINTER(SZ)]
         L.dgo_p2o_local.argtypes = [P, SZ, U, U, ctypes.POINTER(P), ctypes.POINTER(SZ)]
         L.dgo_balance.argtypes = [P, SZ, U, ctypes.POINTER(P), ctypes.POINTER(SZ)]
+        L.dgo_coarsen.argtypes = [P, SZ, U, ctypes.POINTER(P), ctypes.POINTER(SZ)]
         for f in ("dgo_is_sorted_unique", "dgo_is_linear", "dgo_is_complete", "dgo_is_balanced"):
             getattr(L, f).argtypes = [P, SZ, U]
         L.dgo_etype_masks.argtypes = [P]
@@ -127,6 +128,13 @@ def balance(octs: np.ndarray, max_depth: int = 30) -> np.ndarray:
     octs = np.ascontiguousarray(octs, dtype=np.uint32).reshape(-1, 4)
     p, n = ctypes.c_void_p(), ctypes.c_size_t()
     _check(lib().dgo_balance(_ptr(octs), octs.shape[0], max_depth, ctypes.byref(p), ctypes.byref(n)), "balance")
+    return _take_octs(p, n.value)
+
+
+def coarsen(octs: np.ndarray, max_depth: int = 30) -> np.ndarray:
+    octs = np.ascontiguousarray(octs, dtype=np.uint32).reshape(-1, 4)
+    p, n = ctypes.c_void_p(), ctypes.c_size_t()
+    _check(lib().dgo_coarsen(_ptr(octs), octs.shape[0], max_depth, ctypes.byref(p), ctypes.byref(n)), "coarsen")
     return _take_octs(p, n.value)
 
 

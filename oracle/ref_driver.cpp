@@ -13,6 +13,8 @@
  *         maxNum of 4e9 instead of the default _COMBO_RIPPLE_FACTOR_
  *         (include/octUtils.h:477), which works around the empty-output
  *         defect of comboRipple above 1e7 octants (balance.cpp:821-900).
+ *   coarsen IN.oct MAXDEPTH OUT.oct
+ *         ot::coarsenOctree, sequential form (src/coarsen.cpp:53).
  *   check IN.oct MAXDEPTH
  *         ot::test::isLinear / isComplete / isBalanced (src/test/testUtils.C).
  *   da    BAL.oct MAXDEPTH STENCILDIR VEC_IN|- OUT_PREFIX
@@ -132,6 +134,18 @@ static int mode_bal(int argc, char **argv) {
   write_oct(argv[6], out);
   std::printf("{\"op\":\"bal\",\"n_in\":%zu,\"n_out\":%zu,\"patched\":%d,\"seconds\":%.6f}\n", nin, out.size(),
               (int)patched, t1 - t0);
+  return 0;
+}
+
+static int mode_coarsen(int argc, char **argv) {
+  if (argc < 5) return 1;
+  unsigned maxDepth = std::atoi(argv[3]);
+  std::vector<ot::TreeNode> in = read_oct(argv[2], maxDepth), out;
+  double t0 = now_s();
+  ot::coarsenOctree(in, out);
+  double t1 = now_s();
+  write_oct(argv[4], out);
+  std::printf("{\"op\":\"coarsen\",\"n_in\":%zu,\"n_out\":%zu,\"seconds\":%.6f}\n", in.size(), out.size(), t1 - t0);
   return 0;
 }
 
@@ -339,6 +353,7 @@ int main(int argc, char **argv) {
   if (m == "p2o") rc = mode_p2o(argc, argv);
   if (m == "bal") rc = mode_bal(argc, argv);
   if (m == "check") rc = mode_check(argc, argv);
+  if (m == "coarsen") rc = mode_coarsen(argc, argv);
   if (m == "da") rc = mode_da(argc, argv);
   return rc;
 }
