@@ -24,6 +24,7 @@ __all__ = [
     "balanceOctree",
     "sortUniquePoints",
     "points2OctreeBatch",
+    "coarsenOctree",
     "default_context",
 ]
 
@@ -237,6 +238,14 @@ def balanceOctree(octree: Octree, dim: int = 3, maxDepth: int | None = None, inc
     h = ctypes.c_void_p()
     check(ctx.handle, ctx._L.dg_balance_octree(ctx.handle, octree.handle, 1 if incCorner else 0, comm_size, ctypes.byref(h)),
           "balanceOctree")
+    return Octree(ctx, h)
+
+
+def coarsenOctree(octree: Octree) -> Octree:
+    """ot::coarsenOctree (src/coarsen.cpp:53): merge every complete family of 8 leaves."""
+    ctx = octree.ctx
+    h = ctypes.c_void_p()
+    check(ctx.handle, ctx._L.dg_coarsen_octree(ctx.handle, octree.handle, ctypes.byref(h)), "coarsenOctree")
     return Octree(ctx, h)
 
 

@@ -290,6 +290,20 @@ int dg_balance_octree(dg_ctx ctx, dg_octree in, int incCorner, int comm_size, dg
   return DG_OK;
 }
 
+int dg_coarsen_octree(dg_ctx ctx, dg_octree in, dg_octree *out) {
+  if (!in || !out) return DG_ERR_INVALID_ARG;
+  *out = nullptr;
+  dg_octree h = new (std::nothrow) dg_octree_s();
+  if (!h) return DG_ERR_OUT_OF_MEMORY;
+  int rc = guarded(ctx, [&]() { dg::coarsen_octree(ctx->c, in->o, h->o); });
+  if (rc != DG_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return DG_OK;
+}
+
 int dg_octree_size(dg_octree o, size_t *n, unsigned *maxDepth) {
   if (!o) return DG_ERR_INVALID_ARG;
   if (n) *n = o->o.n;

@@ -105,8 +105,6 @@ void gen_stencils(double *lap, double *mass) {
     }
 }
 
-// device layout: for each (c, t) a 128-entry block: 64 Laplacian then 64 mass
-constexpr int STEN_ENTRIES = 8 * 18 * 128;
 
 void ensure_stencils(Context &ctx) {
   if (ctx.d_sten64) return;
@@ -145,17 +143,6 @@ void ensure_stencils(Context &ctx) {
 // ------------------------------------------------------------------------
 // mesh build
 // ------------------------------------------------------------------------
-// index of the leaf whose anchor is the largest anchor <= pos
-__device__ __forceinline__ size_t find_leaf(const Key128 *__restrict__ keys, size_t n, Key128 pos) {
-  size_t lo = 0, hi = n;
-  while (lo < hi) {
-    size_t mid = lo + (hi - lo) / 2;
-    if (key_le(tag_anchor(keys[mid]), pos)) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo ? lo - 1 : 0;  // lo >= 1 for a complete octree; callers verify
-}
-
 __device__ __forceinline__ bool is_leaf_at(const Key128 *__restrict__ keys, size_t n, int64_t x, int64_t y, int64_t z,
                                            unsigned lev, int64_t dom) {
   if (x < 0 || y < 0 || z < 0 || x >= dom || y >= dom || z >= dom) return false;

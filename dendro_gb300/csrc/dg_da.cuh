@@ -31,6 +31,22 @@ void mesh_free(Context &ctx, Mesh &m);
 template <typename T>
 void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, double mass_fac);
 
+// index of the leaf whose anchor is the largest anchor <= pos in a sorted
+// tagged-key array (0 when pos precedes every leaf; callers verify)
+__device__ __forceinline__ size_t find_leaf(const Key128 *__restrict__ keys, size_t n, Key128 pos) {
+  size_t lo = 0, hi = n;
+  while (lo < hi) {
+    size_t mid = lo + (hi - lo) / 2;
+    if (key_le(tag_anchor(keys[mid]), pos)) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo ? lo - 1 : 0;
+}
+
+// device stencil layout: for each (child, type) a 128-entry block, 64
+// Laplacian then 64 mass entries, row-major 8x8
+constexpr int STEN_ENTRIES = 8 * 18 * 128;
+
 // stencil tables on the device, generated on first use
 void ensure_stencils(Context &ctx);
 

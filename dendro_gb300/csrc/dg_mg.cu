@@ -1,0 +1,653 @@
+// Geometric multigrid on the octree meshes (reference: src/omg/blockDiag.cpp
+// DAMG set-up, examples/src/backend/omgJac.C Dirichlet operators,
+// src/omg/restrictMatVec.cpp and prolongMatVec.cpp transfers; the PETSc
+// KSP CG + PCMG V-cycle with Richardson/Jacobi smoothing configured in
+// bin/options:48-206 is restated here as plain CUDA + host control).
+//
+// Transfers.  A coarse element is either a fine element or the parent of 8
+// fine elements (coarsen merges one level; balance never refines past the
+// fine octree), so every fine node sits at local coordinates in
+// {0, 1/2, 1}^3 of the coarse element that contains it.  Its prolongation
+// weights are the coarse element's trilinear shape functions there, folded
+// through the coarse element's hanging-vertex interpolation; the weights are
+// dyadic and exact in FP32.  They reproduce the reference's restriction
+// stencils RmatType1 / RmatType2 exactly.  Restriction is the transpose.
+// Pairs with a fine or a coarse boundary node carry no weight, as with the
+// reference's suppressed Dirichlet DOFs.
+#include "dg_mg.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <type_traits>
+
+namespace dg {
+
+void coarsen_octree(Context &ctx, const Octree &in, Octree &out);
+
+namespace {
+
+template <typename T>
+const T *sten_ptr(const Context &c) {
+  return std::is_same<T, double>::value ? reinterpret_cast<const T *>(c.d_sten64)
+                                        : reinterpret_cast<const T *>(c.d_sten32);
+}
+
+__global__ void k_node_bdy(const uint32_t *__restrict__ xyz, size_t V, unsigned D, uint8_t *__restrict__ bdy) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V) return;
+  const uint32_t dom = 1u << D;
+  uint32_t x = xyz[i], y = xyz[V + i], z = xyz[2 * V + i];
+  bdy[i] = (x == 0 || y == 0 || z == 0 || x == dom || y == dom || z == dom) ? 1 : 0;
+}
+
+// DirichletJacobianMatMult (omgJac.C:958-1057): boundary rows are the
+// identity, boundary columns are skipped
+template <typename T>
+__global__ void __launch_bounds__(512) k_dirichlet_matvec(const uint32_t *__restrict__ meta,
+                                                          const uint32_t *__restrict__ conn, size_t E,
+                                                          const T *__restrict__ sten, const uint8_t *__restrict__ bdy,
+                                                          const T *__restrict__ x, T *__restrict__ y) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *ss = reinterpret_cast<T *>(smem_raw);
+  for (int i = threadIdx.x; i < STEN_ENTRIES; i += blockDim.x) ss[i] = sten[i];
+  __syncthreads();
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t me = meta[e];
+    const unsigned l = me & 255u, c = (me >> 8) & 7u, t = me >> 24;
+    uint32_t id[8];
+    T xv[8];
+    unsigned bm = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) id[k] = conn[(size_t)k * E + e];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      bm |= (unsigned)bdy[id[k]] << k;
+      xv[k] = x[id[k]];
+    }
+    const T h = (T)1 / (T)(1ull << l);
+    const T f1 = h * (T)0.5, f2 = h * h * h * (T)0.125;
+    const T *S = ss + (c * 18 + t) * 128;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      if (bm >> k & 1) {
+        y[id[k]] = xv[k];
+        continue;
+      }
+      T aL = 0, aM = 0;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const T xj = (bm >> j & 1) ? (T)0 : xv[j];
+        aL += S[8 * k + j] * xj;
+        aM += S[64 + 8 * k + j] * xj;
+      }
+      atomicAdd(&y[id[k]], f1 * aL + f2 * aM);
+    }
+  }
+}
+
+// DirichletJacobianMatGetDiagonal: interior diagonal, 1 on the boundary
+__global__ void k_dirichlet_diag(const uint32_t *__restrict__ meta, const uint32_t *__restrict__ conn, size_t E,
+                                 const double *__restrict__ sten, const uint8_t *__restrict__ bdy,
+                                 double *__restrict__ diag) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const uint32_t me = meta[e];
+  const unsigned l = me & 255u, c = (me >> 8) & 7u, t = me >> 24;
+  const double h = 1.0 / (double)(1ull << l);
+  const double f1 = h * 0.5, f2 = h * h * h * 0.125;
+  const double *S = sten + (c * 18 + t) * 128;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    uint32_t id = conn[(size_t)k * E + e];
+    if (bdy[id]) diag[id] = 1.0;
+    else atomicAdd(&diag[id], f1 * S[9 * k] + f2 * S[64 + 9 * k]);
+  }
+}
+
+__global__ void k_invert(const double *__restrict__ d, size_t n, double *__restrict__ inv64, float *__restrict__ inv32) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double v = 1.0 / d[i];
+  inv64[i] = v;
+  inv32[i] = (float)v;
+}
+
+// prolongation weights of every fine node (see the file comment)
+__global__ void k_prolong_map(const uint32_t *__restrict__ fxyz, size_t Vf, const uint8_t *__restrict__ fbdy,
+                              const Key128 *__restrict__ ckeys, size_t Ec, const uint32_t *__restrict__ cmeta,
+                              const uint32_t *__restrict__ cconn, const uint8_t *__restrict__ cbdy, unsigned D,
+                              uint32_t *__restrict__ pid, float *__restrict__ pw, uint32_t *flags) {
+  size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= Vf) return;
+  const uint32_t dom = 1u << D;
+  uint32_t p[3] = {fxyz[v], fxyz[Vf + v], fxyz[2 * Vf + v]};
+  uint32_t q[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) q[a] = p[a] == dom ? dom - 1 : p[a];
+  size_t e = find_leaf(ckeys, Ec, morton3(q[0], q[1], q[2]));
+  const Key128 ke = ckeys[e];
+  const unsigned lc = tag_level(ke);
+  uint32_t an[3];
+  demorton3(tag_anchor(ke), an[0], an[1], an[2]);
+  const uint64_t h = 1ull << (D - lc);
+  const uint32_t me = cmeta[e];
+  const unsigned c = (me >> 8) & 7u, hm = (me >> 16) & 255u;
+  int xi2[3];
+  bool ok = true;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    uint64_t dlt = (uint64_t)p[a] - an[a];
+    if (dlt == 0) xi2[a] = 0;
+    else if (2 * dlt == h) xi2[a] = 1;
+    else if (dlt == h) xi2[a] = 2;
+    else {
+      ok = false;
+      xi2[a] = 0;
+    }
+  }
+  float N[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    float w = 1.f;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      float t = 0.5f * (float)xi2[a];
+      w *= ((k >> a) & 1) ? t : 1.f - t;
+    }
+    N[k] = w;
+  }
+  float wj[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) wj[j] = (hm >> j & 1) ? 0.f : N[j];
+  // hanging vertex k: the mean of the parent corners c^s, s a subset of k^c
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    if (!(hm >> k & 1) || N[k] == 0.f) continue;
+    const unsigned dd = (unsigned)(k ^ (int)c);
+    const float share = N[k] / (float)(1u << __popc(dd));
+    for (unsigned s = 0; s < 8; s++)
+      if ((s & dd) == s) wj[c ^ s] += share;
+  }
+  const bool fb = fbdy[v] != 0;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    uint32_t id = cconn[(size_t)j * Ec + e];
+    float w = (fb || cbdy[id]) ? 0.f : wj[j];
+    pid[(size_t)j * Vf + v] = id;
+    pw[(size_t)j * Vf + v] = w;
+  }
+  if (!ok) atomicOr(flags, DGF_INTERNAL);
+}
+
+template <typename T>
+__global__ void k_prolong(const uint32_t *__restrict__ pid, const float *__restrict__ pw, size_t Vf,
+                          const T *__restrict__ xc, T *__restrict__ xf, bool add) {
+  size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= Vf) return;
+  T acc = 0;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    float w = pw[(size_t)j * Vf + v];
+    if (w != 0.f) acc += (T)w * xc[pid[(size_t)j * Vf + v]];
+  }
+  xf[v] = add ? xf[v] + acc : acc;
+}
+
+template <typename T>
+__global__ void k_restrict(const uint32_t *__restrict__ pid, const float *__restrict__ pw, size_t Vf,
+                           const T *__restrict__ rf, T *__restrict__ bc) {
+  size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= Vf) return;
+  const T r = rf[v];
+  if (r == (T)0) return;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    float w = pw[(size_t)j * Vf + v];
+    if (w != 0.f) atomicAdd(&bc[pid[(size_t)j * Vf + v]], (T)w * r);
+  }
+}
+
+// damped Jacobi: x = w D^-1 b (first sweep from zero) or x += w D^-1 (b - Ax)
+template <typename T>
+__global__ void k_jacobi(T *__restrict__ x, const T *__restrict__ b, const T *__restrict__ ax,
+                         const T *__restrict__ dinv, T omega, size_t n, bool from_zero) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  x[i] = from_zero ? omega * dinv[i] * b[i] : x[i] + omega * dinv[i] * (b[i] - ax[i]);
+}
+
+template <typename T>
+__global__ void k_residual(const T *__restrict__ b, const T *__restrict__ ax, T *__restrict__ r, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) r[i] = b[i] - ax[i];
+}
+
+// x = A^-1 b with the dense inverse of the coarsest level, one warp per row
+template <typename T>
+__global__ void k_gemv(const T *__restrict__ A, size_t n, const T *__restrict__ b, T *__restrict__ x) {
+  size_t row = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const T *a = A + row * n;
+  T acc = 0;
+  for (size_t j = lane; j < n; j += 32) acc += a[j] * b[j];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) x[row] = acc;
+}
+
+__global__ void k_assemble_dense(const uint32_t *__restrict__ meta, const uint32_t *__restrict__ conn, size_t E,
+                                 const double *__restrict__ sten, const uint8_t *__restrict__ bdy, size_t n,
+                                 double *__restrict__ A) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const uint32_t me = meta[e];
+  const unsigned l = me & 255u, c = (me >> 8) & 7u, t = me >> 24;
+  const double h = 1.0 / (double)(1ull << l);
+  const double f1 = h * 0.5, f2 = h * h * h * 0.125;
+  const double *S = sten + (c * 18 + t) * 128;
+  uint32_t id[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) id[k] = conn[(size_t)k * E + e];
+  for (int k = 0; k < 8; k++) {
+    if (bdy[id[k]]) continue;
+    for (int j = 0; j < 8; j++) {
+      if (bdy[id[j]]) continue;
+      atomicAdd(&A[(size_t)id[k] * n + id[j]], f1 * S[8 * k + j] + f2 * S[64 + 8 * k + j]);
+    }
+  }
+}
+
+__global__ void k_set_bdy_identity(const uint8_t *__restrict__ bdy, size_t n, double *__restrict__ A) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && bdy[i]) A[i * n + i] = 1.0;
+}
+
+// in-place Gauss-Jordan inversion (no pivoting: the operator is SPD)
+__global__ void k_gj_col(const double *__restrict__ A, size_t n, size_t p, double *__restrict__ col) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) col[i] = A[i * n + p];
+}
+__global__ void k_gj_row(double *__restrict__ A, size_t n, size_t p, const double *__restrict__ col) {
+  size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double inv = 1.0 / col[p];
+  double v = (j == p) ? 1.0 : A[p * n + j];
+  A[p * n + j] = v * inv;
+}
+__global__ void k_gj_update(double *__restrict__ A, size_t n, size_t p, const double *__restrict__ col) {
+  size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * n) return;
+  size_t i = idx / n, j = idx % n;
+  if (i == p) return;
+  const double f = col[i];
+  double a = (j == p) ? 0.0 : A[i * n + j];
+  A[i * n + j] = a - f * A[p * n + j];
+}
+
+__global__ void k_to_float(const double *__restrict__ a, size_t n, float *__restrict__ b) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+__global__ void k_to_double(const float *__restrict__ a, size_t n, double *__restrict__ b) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (double)a[i];
+}
+
+// block partial sums of a.b (and of a.a when b is null)
+__global__ void k_dot_partial(const double *__restrict__ a, const double *__restrict__ b, size_t n,
+                              double *__restrict__ part) {
+  double acc = 0.0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    acc += a[i] * (b ? b[i] : a[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double ws[32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = (threadIdx.x < (blockDim.x >> 5)) ? ws[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) part[blockIdx.x] = v;
+  }
+}
+__global__ void k_sum(const double *__restrict__ part, int np, double *__restrict__ out) {
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) acc += part[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double ws[32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = (threadIdx.x < (blockDim.x >> 5)) ? ws[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) *out = v;
+  }
+}
+
+__global__ void k_cg_xr(double *__restrict__ x, double *__restrict__ r, const double *__restrict__ p,
+                        const double *__restrict__ q, const double *__restrict__ alpha_num,
+                        const double *__restrict__ alpha_den, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double alpha = *alpha_num / *alpha_den;
+  x[i] += alpha * p[i];
+  r[i] -= alpha * q[i];
+}
+__global__ void k_cg_p(double *__restrict__ p, const double *__restrict__ z, const double *__restrict__ rz_new,
+                       const double *__restrict__ rz_old, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  p[i] = z[i] + (*rz_new / *rz_old) * p[i];
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------
+template <typename T>
+void dirichlet_matvec(Context &ctx, const MGLevel &L, const T *x, T *y) {
+  ensure_stencils(ctx);
+  cudaStream_t s = ctx.stream;
+  const Mesh &m = L.mesh;
+  DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
+  const size_t smem = STEN_ENTRIES * sizeof(T);
+  static std::once_flag once;
+  std::call_once(once, [&]() {
+    DG_CUDA(cudaFuncSetAttribute(k_dirichlet_matvec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  });
+  int per_sm = 1;
+  DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dirichlet_matvec<T>, 512, smem));
+  unsigned grid = grid_for(m.n_elem, 512, (unsigned)(std::max(per_sm, 1) * ctx.num_sms));
+  ProfScope _prof(ctx, "dirichlet_matvec", (double)m.n_elem * 36 + (double)m.n_node * (3 * sizeof(T) + 1));
+  k_dirichlet_matvec<T><<<grid, 512, smem, s>>>(m.meta, m.conn, m.n_elem, sten_ptr<T>(ctx), L.bdy, x, y);
+  DG_LAUNCH_CHECK();
+}
+
+template <typename T>
+void mg_restrict(Context &ctx, const MG &mg, int f, const T *rf, T *bc) {
+  const MGLevel &F = mg.lv[f];
+  const MGLevel &C = mg.lv[f + 1];
+  cudaStream_t s = ctx.stream;
+  DG_CUDA(cudaMemsetAsync(bc, 0, C.mesh.n_node * sizeof(T), s));
+  ProfScope _prof(ctx, "mg_restrict", (double)F.mesh.n_node * (8 * 8 + sizeof(T)));
+  k_restrict<T><<<grid_for(F.mesh.n_node, 256), 256, 0, s>>>(F.pid, F.pw, F.mesh.n_node, rf, bc);
+  DG_LAUNCH_CHECK();
+}
+
+template <typename T>
+void mg_prolong(Context &ctx, const MG &mg, int f, const T *xc, T *xf) {
+  const MGLevel &F = mg.lv[f];
+  ProfScope _prof(ctx, "mg_prolong", (double)F.mesh.n_node * (8 * 8 + sizeof(T)));
+  k_prolong<T><<<grid_for(F.mesh.n_node, 256), 256, 0, ctx.stream>>>(F.pid, F.pw, F.mesh.n_node, xc, xf, false);
+  DG_LAUNCH_CHECK();
+}
+
+namespace {
+
+template <typename T>
+struct VWork {
+  std::vector<DBuf<T>> b, x, ax;
+};
+
+template <typename T>
+const T *dinv_of(const MGLevel &L) {
+  return std::is_same<T, double>::value ? reinterpret_cast<const T *>(L.dinv64) : reinterpret_cast<const T *>(L.dinv32);
+}
+
+template <typename T>
+void vcycle_level(Context &ctx, const MG &mg, VWork<T> &w, int l, const T *b, T *x) {
+  cudaStream_t s = ctx.stream;
+  const MGLevel &L = mg.lv[l];
+  const size_t n = L.mesh.n_node;
+  if (l + 1 == (int)mg.lv.size()) {
+    const T *Ainv = std::is_same<T, double>::value ? reinterpret_cast<const T *>(mg.cinv64)
+                                                   : reinterpret_cast<const T *>(mg.cinv32);
+    ProfScope _prof(ctx, "mg_coarse_solve", (double)n * n * sizeof(T));
+    k_gemv<T><<<grid_for(n * 32, 256), 256, 0, s>>>(Ainv, n, b, x);
+    DG_LAUNCH_CHECK();
+    return;
+  }
+  const T om = (T)mg.omega;
+  T *ax = w.ax[l].get();
+  const unsigned g = grid_for(n, 256);
+  for (int it = 0; it < mg.nu_pre; it++) {
+    if (it > 0) dirichlet_matvec<T>(ctx, L, x, ax);
+    ProfScope _prof(ctx, "mg_jacobi", (double)n * 4 * sizeof(T));
+    k_jacobi<T><<<g, 256, 0, s>>>(x, b, ax, dinv_of<T>(L), om, n, it == 0);
+    DG_LAUNCH_CHECK();
+  }
+  if (mg.nu_pre == 0) DG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(T), s));
+  dirichlet_matvec<T>(ctx, L, x, ax);
+  {
+    ProfScope _prof(ctx, "mg_residual", (double)n * 3 * sizeof(T));
+    k_residual<T><<<g, 256, 0, s>>>(b, ax, ax, n);  // ax now holds the residual
+    DG_LAUNCH_CHECK();
+  }
+  T *bc = w.b[l + 1].get(), *xc = w.x[l + 1].get();
+  mg_restrict<T>(ctx, mg, l, ax, bc);
+  vcycle_level<T>(ctx, mg, w, l + 1, bc, xc);
+  {
+    ProfScope _prof(ctx, "mg_prolong", (double)n * (8 * 8 + 2 * sizeof(T)));
+    k_prolong<T><<<g, 256, 0, s>>>(L.pid, L.pw, n, xc, x, true);
+    DG_LAUNCH_CHECK();
+  }
+  for (int it = 0; it < mg.nu_post; it++) {
+    dirichlet_matvec<T>(ctx, L, x, ax);
+    ProfScope _prof(ctx, "mg_jacobi", (double)n * 4 * sizeof(T));
+    k_jacobi<T><<<g, 256, 0, s>>>(x, b, ax, dinv_of<T>(L), om, n, false);
+    DG_LAUNCH_CHECK();
+  }
+}
+
+template <typename T>
+VWork<T> make_work(Context &ctx, const MG &mg) {
+  VWork<T> w;
+  for (auto &L : mg.lv) {
+    size_t n = L.mesh.n_node;
+    w.b.emplace_back(n, ctx.stream);
+    w.x.emplace_back(n, ctx.stream);
+    w.ax.emplace_back(n, ctx.stream);
+  }
+  return w;
+}
+
+}  // namespace
+
+template <typename T>
+void mg_vcycle(Context &ctx, const MG &mg, const T *b, T *x) {
+  VWork<T> w = make_work<T>(ctx, mg);
+  vcycle_level<T>(ctx, mg, w, 0, b, x);
+}
+
+// ------------------------------------------------------------------------
+void mg_free(Context &ctx, MG &mg) {
+  for (auto &L : mg.lv) {
+    octree_free(ctx, L.oct);
+    mesh_free(ctx, L.mesh);
+    if (L.bdy) cudaFreeAsync(L.bdy, ctx.stream);
+    if (L.dinv64) cudaFreeAsync(L.dinv64, ctx.stream);
+    if (L.dinv32) cudaFreeAsync(L.dinv32, ctx.stream);
+    if (L.pid) cudaFreeAsync(L.pid, ctx.stream);
+    if (L.pw) cudaFreeAsync(L.pw, ctx.stream);
+  }
+  if (mg.cinv64) cudaFreeAsync(mg.cinv64, ctx.stream);
+  if (mg.cinv32) cudaFreeAsync(mg.cinv32, ctx.stream);
+  cudaStreamSynchronize(ctx.stream);
+  mg = MG();
+}
+
+static void copy_octree(Context &ctx, const Octree &in, Octree &out) {
+  out = Octree();
+  out.max_depth = in.max_depth;
+  out.n = in.n;
+  DG_CUDA(cudaMallocAsync((void **)&out.keys, in.n * sizeof(Key128), ctx.stream));
+  DG_CUDA(cudaMemcpyAsync(out.keys, in.keys, in.n * sizeof(Key128), cudaMemcpyDeviceToDevice, ctx.stream));
+}
+
+void mg_setup(Context &ctx, const Octree &fine, size_t max_coarse_elem, MG &mg) {
+  if (fine.nseg != 1) fail(DG_ERR_UNSUPPORTED, "multigrid: one cloud per hierarchy");
+  if (max_coarse_elem < 1) fail(DG_ERR_INVALID_ARG, "multigrid: max_coarse_elem must be >= 1");
+  ensure_stencils(ctx);
+  cudaStream_t s = ctx.stream;
+  mg = MG();
+  try {
+    mg.lv.emplace_back();
+    copy_octree(ctx, fine, mg.lv[0].oct);
+    mesh_build(ctx, mg.lv[0].oct, mg.lv[0].mesh);
+    while (mg.lv.back().mesh.n_elem > max_coarse_elem) {
+      Octree c, b;
+      coarsen_octree(ctx, mg.lv.back().oct, c);
+      if (c.n == mg.lv.back().oct.n) {
+        octree_free(ctx, c);
+        break;  // nothing left to coarsen
+      }
+      balance_octree(ctx, c, b);
+      octree_free(ctx, c);
+      mg.lv.emplace_back();
+      mg.lv.back().oct = b;
+      mesh_build(ctx, mg.lv.back().oct, mg.lv.back().mesh);
+    }
+    const unsigned D = fine.max_depth;
+    for (auto &L : mg.lv) {
+      const size_t V = L.mesh.n_node, E = L.mesh.n_elem;
+      DG_CUDA(cudaMallocAsync((void **)&L.bdy, V, s));
+      k_node_bdy<<<grid_for(V, 256), 256, 0, s>>>(L.mesh.node_xyz, V, D, L.bdy);
+      DG_LAUNCH_CHECK();
+      DBuf<double> diag(V, s);
+      DG_CUDA(cudaMemsetAsync(diag.get(), 0, V * sizeof(double), s));
+      k_dirichlet_diag<<<grid_for(E, 256), 256, 0, s>>>(L.mesh.meta, L.mesh.conn, E, ctx.d_sten64, L.bdy, diag.get());
+      DG_LAUNCH_CHECK();
+      DG_CUDA(cudaMallocAsync((void **)&L.dinv64, V * sizeof(double), s));
+      DG_CUDA(cudaMallocAsync((void **)&L.dinv32, V * sizeof(float), s));
+      k_invert<<<grid_for(V, 256), 256, 0, s>>>(diag.get(), V, L.dinv64, L.dinv32);
+      DG_LAUNCH_CHECK();
+    }
+    DG_CUDA(cudaMemsetAsync(ctx.d_flags, 0, sizeof(uint32_t), s));
+    for (size_t l = 0; l + 1 < mg.lv.size(); l++) {
+      MGLevel &F = mg.lv[l];
+      const MGLevel &C = mg.lv[l + 1];
+      const size_t Vf = F.mesh.n_node;
+      DG_CUDA(cudaMallocAsync((void **)&F.pid, 8 * Vf * sizeof(uint32_t), s));
+      DG_CUDA(cudaMallocAsync((void **)&F.pw, 8 * Vf * sizeof(float), s));
+      k_prolong_map<<<grid_for(Vf, 256), 256, 0, s>>>(F.mesh.node_xyz, Vf, F.bdy, C.oct.keys, C.oct.n, C.mesh.meta,
+                                                      C.mesh.conn, C.bdy, D, F.pid, F.pw, ctx.d_flags);
+      DG_LAUNCH_CHECK();
+    }
+    check_device_flags(ctx, "multigrid transfers");
+    // dense inverse of the coarsest operator
+    const MGLevel &C = mg.lv.back();
+    const size_t n = C.mesh.n_node;
+    if (n > 20000) fail(DG_ERR_INVALID_ARG, "multigrid: coarsest level too large for the dense solve");
+    mg.nc = n;
+    DG_CUDA(cudaMallocAsync((void **)&mg.cinv64, n * n * sizeof(double), s));
+    DG_CUDA(cudaMallocAsync((void **)&mg.cinv32, n * n * sizeof(float), s));
+    DG_CUDA(cudaMemsetAsync(mg.cinv64, 0, n * n * sizeof(double), s));
+    k_assemble_dense<<<grid_for(C.mesh.n_elem, 128), 128, 0, s>>>(C.mesh.meta, C.mesh.conn, C.mesh.n_elem,
+                                                                   ctx.d_sten64, C.bdy, n, mg.cinv64);
+    DG_LAUNCH_CHECK();
+    k_set_bdy_identity<<<grid_for(n, 256), 256, 0, s>>>(C.bdy, n, mg.cinv64);
+    DG_LAUNCH_CHECK();
+    DBuf<double> col(n, s);
+    for (size_t p = 0; p < n; p++) {
+      k_gj_col<<<grid_for(n, 256), 256, 0, s>>>(mg.cinv64, n, p, col.get());
+      k_gj_row<<<grid_for(n, 256), 256, 0, s>>>(mg.cinv64, n, p, col.get());
+      k_gj_update<<<grid_for(n * n, 256), 256, 0, s>>>(mg.cinv64, n, p, col.get());
+    }
+    DG_LAUNCH_CHECK();
+    k_to_float<<<grid_for(n * n, 256), 256, 0, s>>>(mg.cinv64, n * n, mg.cinv32);
+    DG_LAUNCH_CHECK();
+    DG_CUDA(cudaStreamSynchronize(s));
+  } catch (...) {
+    mg_free(ctx, mg);
+    throw;
+  }
+}
+
+// ------------------------------------------------------------------------
+void mg_solve(Context &ctx, MG &mg, const double *b, double *x, int precision, double rtol, int maxit,
+              MGResult &res) {
+  if (precision != 32 && precision != 64) fail(DG_ERR_INVALID_ARG, "multigrid: precision must be 32 or 64");
+  cudaStream_t s = ctx.stream;
+  const MGLevel &L0 = mg.lv[0];
+  const size_t n = L0.mesh.n_node;
+  const unsigned g = grid_for(n, 256);
+  DBuf<double> r(n, s), z(n, s), p(n, s), q(n, s);
+  const int nparts = (int)std::min<size_t>(grid_for(n, 256), (size_t)(ctx.num_sms * 4));
+  DBuf<double> part(nparts, s), sc(8, s);  // sc: rz, pq, rr, rz_new, bb
+  VWork<float> w32;
+  VWork<double> w64;
+  DBuf<float> r32, z32;
+  if (precision == 32) {
+    w32 = make_work<float>(ctx, mg);
+    r32.alloc(n, s);
+    z32.alloc(n, s);
+  } else {
+    w64 = make_work<double>(ctx, mg);
+  }
+  auto dot = [&](const double *a, const double *bb, double *out) {
+    ProfScope _prof(ctx, "cg_dot", (double)n * (bb ? 16 : 8));
+    k_dot_partial<<<nparts, 256, 0, s>>>(a, bb, n, part.get());
+    k_sum<<<1, 256, 0, s>>>(part.get(), nparts, out);
+    DG_LAUNCH_CHECK();
+  };
+  auto precond = [&](const double *rin, double *zout) {
+    if (precision == 32) {
+      k_to_float<<<g, 256, 0, s>>>(rin, n, r32.get());
+      vcycle_level<float>(ctx, mg, w32, 0, r32.get(), z32.get());
+      k_to_double<<<g, 256, 0, s>>>(z32.get(), n, zout);
+      DG_LAUNCH_CHECK();
+    } else {
+      vcycle_level<double>(ctx, mg, w64, 0, rin, zout);
+    }
+  };
+  double *d_rz = sc.get(), *d_pq = sc.get() + 1, *d_rr = sc.get() + 2, *d_rzn = sc.get() + 3, *d_bb = sc.get() + 4;
+  DG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+  DG_CUDA(cudaMemcpyAsync(r.get(), b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  dot(b, nullptr, d_bb);
+  double bb = read_scalar(ctx, d_bb);
+  res = MGResult();
+  if (bb == 0.0) return;
+  const double bnorm = std::sqrt(bb);
+  precond(r.get(), z.get());
+  DG_CUDA(cudaMemcpyAsync(p.get(), z.get(), n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  dot(r.get(), z.get(), d_rz);
+  int it = 0;
+  double relres = 1.0;
+  for (it = 1; it <= maxit; it++) {
+    dirichlet_matvec<double>(ctx, L0, p.get(), q.get());
+    dot(p.get(), q.get(), d_pq);
+    k_cg_xr<<<g, 256, 0, s>>>(x, r.get(), p.get(), q.get(), d_rz, d_pq, n);
+    DG_LAUNCH_CHECK();
+    dot(r.get(), nullptr, d_rr);
+    relres = std::sqrt(read_scalar(ctx, d_rr)) / bnorm;
+    if (relres <= rtol) break;
+    precond(r.get(), z.get());
+    dot(r.get(), z.get(), d_rzn);
+    k_cg_p<<<g, 256, 0, s>>>(p.get(), z.get(), d_rzn, d_rz, n);
+    DG_LAUNCH_CHECK();
+    DG_CUDA(cudaMemcpyAsync(d_rz, d_rzn, sizeof(double), cudaMemcpyDeviceToDevice, s));
+  }
+  // the true residual, recomputed in FP64
+  dirichlet_matvec<double>(ctx, L0, x, q.get());
+  k_residual<double><<<g, 256, 0, s>>>(b, q.get(), r.get(), n);
+  DG_LAUNCH_CHECK();
+  dot(r.get(), nullptr, d_rr);
+  res.iterations = std::min(it, maxit);
+  res.relres = std::sqrt(read_scalar(ctx, d_rr)) / bnorm;
+}
+
+template void dirichlet_matvec<float>(Context &, const MGLevel &, const float *, float *);
+template void dirichlet_matvec<double>(Context &, const MGLevel &, const double *, double *);
+template void mg_restrict<float>(Context &, const MG &, int, const float *, float *);
+template void mg_restrict<double>(Context &, const MG &, int, const double *, double *);
+template void mg_prolong<float>(Context &, const MG &, int, const float *, float *);
+template void mg_prolong<double>(Context &, const MG &, int, const double *, double *);
+template void mg_vcycle<float>(Context &, const MG &, const float *, float *);
+template void mg_vcycle<double>(Context &, const MG &, const double *, double *);
+
+}  // namespace dg

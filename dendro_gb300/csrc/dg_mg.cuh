@@ -1,0 +1,60 @@
+// Geometric multigrid on octree meshes (the reference's omg module at one
+// rank) for -lap(u) + u = f with u = 0 on the boundary of the unit cube:
+// level hierarchy by coarsen + balance, Dirichlet element operators, the
+// inter-grid transfers, a damped-Jacobi V-cycle and an FP64 preconditioned
+// CG whose V-cycle runs in FP32 or FP64.
+#pragma once
+
+#include <vector>
+
+#include "dg_da.cuh"
+
+namespace dg {
+
+struct MGLevel {
+  Octree oct;  // balanced octree of this level (owned)
+  Mesh mesh;
+  uint8_t *bdy = nullptr;  // 1 for nodes on the domain boundary
+  double *dinv64 = nullptr;  // inverse diagonal of the Dirichlet operator
+  float *dinv32 = nullptr;
+  // prolongation from the next coarser level onto this level's nodes:
+  // slot j of node v refers to coarse node pid[j*V + v] with weight pw[j*V + v]
+  uint32_t *pid = nullptr;
+  float *pw = nullptr;
+};
+
+struct MG {
+  std::vector<MGLevel> lv;  // 0 = finest
+  size_t nc = 0;            // nodes of the coarsest level
+  double *cinv64 = nullptr;  // dense inverse of the coarsest operator
+  float *cinv32 = nullptr;
+  double omega = 0.667;  // Jacobi damping (bin/options:190)
+  int nu_pre = 2, nu_post = 2;
+};
+
+struct MGResult {
+  int iterations = 0;
+  double relres = 0.0;  // final ||b - A x|| / ||b|| in FP64
+};
+
+// levels from a balanced octree: coarsen (src/coarsen.cpp:53) + balance
+// until a level has at most max_coarse_elem elements
+// (examples/src/omg/blockDiag.cpp:1384-1425 coarsens to < 500 octants)
+void mg_setup(Context &ctx, const Octree &fine, size_t max_coarse_elem, MG &mg);
+void mg_free(Context &ctx, MG &mg);
+
+// PCG to ||r|| / ||b|| <= rtol; residual, dot products and updates in FP64,
+// the V-cycle preconditioner in FP32 (precision 32) or FP64 (precision 64)
+void mg_solve(Context &ctx, MG &mg, const double *b, double *x, int precision, double rtol, int maxit, MGResult &res);
+
+// building blocks (level operators), exposed for tests and callers
+template <typename T>
+void dirichlet_matvec(Context &ctx, const MGLevel &L, const T *x, T *y);  // DirichletJacobianMatMult
+template <typename T>
+void mg_restrict(Context &ctx, const MG &mg, int fine_level, const T *rf, T *bc);  // restrictMatVecType1
+template <typename T>
+void mg_prolong(Context &ctx, const MG &mg, int fine_level, const T *xc, T *xf);  // prolongMatVecType1 (xf = P xc)
+template <typename T>
+void mg_vcycle(Context &ctx, const MG &mg, const T *b, T *x);  // one V(nu_pre, nu_post) from x = 0
+
+}  // namespace dg

@@ -845,6 +845,83 @@ void balance_octree(Context &ctx, const Octree &in, Octree &out) {
 }
 
 // ------------------------------------------------------------------------
+// coarsenOctree (src/coarsen.cpp:53): every complete family of 8 sibling
+// leaves is replaced by its parent.  On a sorted, linear, complete octree
+// the reference's rule (a first child followed by 7 octants that are not
+// first children) is exactly "the 8 octants from a first child are the 8
+// children of one parent"; a batch never merges across clouds because the
+// parent test includes the cloud bits.
+// ------------------------------------------------------------------------
+__device__ __forceinline__ unsigned key_child(Key128 k, unsigned D) {
+  unsigned l = tag_level(k);
+  if (l == 0) return 0;
+  return (unsigned)(key_shr(tag_anchor(k), 3 * (D - l)).lo & 7u);
+}
+__device__ __forceinline__ Key128 key_parent(Key128 k, unsigned D) {
+  unsigned l = tag_level(k);
+  unsigned sh = 3 * (D - l + 1);
+  return make_tagged(key_shl(key_shr(tag_anchor(k), sh), sh), l - 1);
+}
+
+__global__ void k_coarsen_mark(const Key128 *__restrict__ k, size_t n, unsigned D, uint32_t *__restrict__ fam) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Key128 ki = k[i];
+  const unsigned l = tag_level(ki);
+  bool start = l >= 1 && key_child(ki, D) == 0 && i + 7 < n;
+  if (start) {
+    const Key128 par = key_parent(ki, D);
+    for (int j = 1; j < 8 && start; j++) {
+      Key128 kj = k[i + j];
+      start = tag_level(kj) == l && key_eq(key_parent(kj, D), par);
+    }
+  }
+  fam[i] = start ? 1u : 0u;
+}
+
+__global__ void k_coarsen_apply(const Key128 *__restrict__ k, size_t n, unsigned D, const uint32_t *__restrict__ fam,
+                                Key128 *__restrict__ val, uint32_t *__restrict__ keep) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Key128 ki = k[i];
+  const unsigned c = key_child(ki, D);
+  const bool member = c >= 1 && i >= c && fam[i - c];
+  keep[i] = member ? 0u : 1u;
+  val[i] = fam[i] ? key_parent(ki, D) : ki;
+}
+
+void coarsen_octree(Context &ctx, const Octree &in, Octree &out) {
+  cudaStream_t s = ctx.stream;
+  const size_t n = in.n;
+  out.max_depth = in.max_depth;
+  out.nseg = in.nseg;
+  out.seg_bits = in.seg_bits;
+  if (in.nseg != 1) fail(DG_ERR_UNSUPPORTED, "coarsenOctree: one cloud per call");
+  DBuf<Key128> res(n ? n : 1, s);
+  if (n < 8) {  // coarsen.cpp:66-70
+    if (n) DG_CUDA(cudaMemcpyAsync(res.get(), in.keys, n * sizeof(Key128), cudaMemcpyDeviceToDevice, s));
+    DG_CUDA(cudaStreamSynchronize(s));
+    out.n = n;
+    out.keys = res.release_ptr();
+    return;
+  }
+  DBuf<uint32_t> fam(n, s), keep(n, s);
+  DBuf<Key128> val(n, s);
+  {
+    ProfScope _prof(ctx, "coarsen_mark", (double)n * 20);
+    k_coarsen_mark<<<grid_for(n, 256), 256, 0, s>>>(in.keys, n, in.max_depth, fam.get());
+    DG_LAUNCH_CHECK();
+  }
+  {
+    ProfScope _prof(ctx, "coarsen_apply", (double)n * 40);
+    k_coarsen_apply<<<grid_for(n, 256), 256, 0, s>>>(in.keys, n, in.max_depth, fam.get(), val.get(), keep.get());
+    DG_LAUNCH_CHECK();
+  }
+  out.n = compact<Key128>(ctx, val.get(), keep.get(), n, res.get());
+  out.keys = res.release_ptr();
+}
+
+// ------------------------------------------------------------------------
 // conversions
 // ------------------------------------------------------------------------
 // (a single cloud may hold octants just outside its domain: the reference's

@@ -57,6 +57,9 @@ size_t sort_points(Context &ctx, const double *d_xyz, size_t n, const double gle
 // ot::balanceOctree(incCorner = 1) (src/balance.cpp:31).
 void balance_octree(Context &ctx, const Octree &in, Octree &out);
 
+// ot::coarsenOctree (src/coarsen.cpp:53), one cloud.
+void coarsen_octree(Context &ctx, const Octree &in, Octree &out);
+
 // conversions between tagged keys and {x, y, z, level} u32 records
 void octree_to_xyzl(Context &ctx, const Octree &o, uint32_t *d_xyzl);
 void octree_from_xyzl(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned max_depth, Octree &out);

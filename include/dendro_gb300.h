@@ -102,6 +102,12 @@ int dg_sort_unique_points(dg_ctx ctx, const double *xyz, size_t n, const double 
  * left intact (the reference clears `in`). */
 int dg_balance_octree(dg_ctx ctx, dg_octree in, int incCorner, int comm_size, dg_octree *out);
 
+/* ---- ot::coarsenOctree -----------------------------------------------------
+ * include/octUtils.h:825 / src/coarsen.cpp:53 (sequential form): every
+ * complete family of 8 sibling leaves of a sorted, linear, complete octree is
+ * replaced by its parent.  One cloud per call. */
+int dg_coarsen_octree(dg_ctx ctx, dg_octree in, dg_octree *out);
+
 /* ---- octree handles --------------------------------------------------------
  * Materialise / import the std::vector<ot::TreeNode> of the reference as
  * {x, y, z, level} records. */
