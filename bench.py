@@ -178,6 +178,48 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_poisson(dg, datagen, ctx, local, args):
+    """-lap(u) + u = f, u = 0 on the cube boundary, on the balanced octree of
+    16e6 N(0.5, 0.15^2) points (seed 3), f = 4 Gaussian bumps (seed 3), load
+    vector = mass matrix times nodal f; levels by coarsen + balance down to
+    <= 4096 elements; CG to 1e-8 relative residual with one V(2,2) damped-
+    Jacobi (omega 0.667) cycle per iteration, FP32 or FP64 cycle, FP64 CG."""
+    import torch
+
+    npts = args.poisson_npts
+    pts = torch.from_numpy(datagen.gaussian(npts, 0.5, 0.15, seed=3)).to(f"cuda:{local}")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lin = dg.points2Octree(pts, maxDepth=30, maxNumPtsPerOctant=1, ctx=ctx)
+    bal = dg.balanceOctree(lin)
+    lin.free()
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    mg = dg.MultiGrid(bal, max_coarse_elems=4096)
+    t_setup = time.perf_counter() - t0
+    bal.free()
+    f = torch.from_numpy(datagen.bumps(mg.level_nodes(0))).to(f"cuda:{local}")
+    b = mg.rhs(f)
+    out = {"points": npts, "levels": mg.n_levels, "level_elements": [e for e, _ in mg.sizes],
+           "fine_nodes": mg.sizes[0][1], "build_balance_ms": 1e3 * t_build, "mg_setup_ms": 1e3 * t_setup}
+    for prec in (32, 64):
+        mg.solve(b, precision=prec, rtol=1e-8, maxit=200)  # warm-up
+        times, its, rrs = [], [], []
+        for _ in range(args.poisson_reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            x, it, rr = mg.solve(b, precision=prec, rtol=1e-8, maxit=200)
+            torch.cuda.synchronize()
+            times.append(1e3 * (time.perf_counter() - t0))
+            its.append(it)
+            rrs.append(rr)
+        out[f"fp{prec}_vcycle"] = {"solve_ms": min(times), "iterations": its[0], "relres_fp64": max(rrs)}
+    out["speedup_fp32_vs_fp64"] = out["fp64_vcycle"]["solve_ms"] / out["fp32_vcycle"]["solve_ms"]
+    mg.free()
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -305,6 +347,10 @@ def run_ours(args):
         da.free()
         extra = {"da_build_ms": da_ms, "n_elem": E, "n_node": V, "matvec": mv}
 
+    # ---- precision workload: FP32-MG vs FP64 solve to 1e-8 ----------------
+    if not args.skip_mg:
+        extra["poisson"] = run_poisson(dg, datagen, ctx, local, args)
+
     # ---- roofline of the dominant kernel of the timed step ----------------
     peak, peak_kind = _peaks()
     launches = sum(v[1] for v in stats.values())
@@ -376,6 +422,9 @@ def main():
     ap.add_argument("--npts", type=int, default=0, help="override the workload's point count")
     ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE_PTS)
     ap.add_argument("--skip-da", action="store_true")
+    ap.add_argument("--skip-mg", action="store_true")
+    ap.add_argument("--poisson-npts", type=int, default=16_000_000)
+    ap.add_argument("--poisson-reps", type=int, default=3)
     ap.add_argument("--skip-cpu", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -4,10 +4,10 @@ Morton sort -> ot::points2Octree -> ot::balanceOctree(incCorner) -> ot::DA
 -> Laplacian + mass element matVec, as hand-written CUDA kernels behind the
 C ABI of include/dendro_gb300.h.
 """
-from .api import (DA, Context, DendroError, Octree, balanceOctree, coarsenOctree, default_context, points2Octree,
-                  points2OctreeBatch, sortUniquePoints)
+from .api import (DA, Context, DendroError, MultiGrid, Octree, balanceOctree, coarsenOctree, default_context,
+                  points2Octree, points2OctreeBatch, sortUniquePoints)
 
 __all__ = [
-    "DA", "Context", "DendroError", "Octree", "balanceOctree", "coarsenOctree", "default_context", "points2Octree", "points2OctreeBatch",
+    "DA", "Context", "DendroError", "MultiGrid", "Octree", "balanceOctree", "coarsenOctree", "default_context", "points2Octree", "points2OctreeBatch",
     "sortUniquePoints",
 ]

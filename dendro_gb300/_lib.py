@@ -78,6 +78,18 @@ def _declare(L):
         "dg_da_download": ([P, P, P, P, P, I], I),
         "dg_da_free": ([P, P], I),
         "dg_matvec": ([P, P, P, P, I, D, D, I], I),
+        "dg_mg_setup": ([P, P, SZ, PP], I),
+        "dg_mg_levels": ([P, ctypes.POINTER(SZ)], I),
+        "dg_mg_level_sizes": ([P, SZ, ctypes.POINTER(SZ), ctypes.POINTER(SZ)], I),
+        "dg_mg_level_nodes": ([P, P, SZ, P, I], I),
+        "dg_mg_level_octree": ([P, P, SZ, P, I], I),
+        "dg_mg_matvec": ([P, P, SZ, P, P, I, I], I),
+        "dg_mg_restrict": ([P, P, SZ, P, P, I, I], I),
+        "dg_mg_prolong": ([P, P, SZ, P, P, I, I], I),
+        "dg_mg_set_smoother": ([P, D, I, I], I),
+        "dg_mg_rhs": ([P, P, P, P, I], I),
+        "dg_mg_solve": ([P, P, P, P, I, D, I, I, ctypes.POINTER(I), ctypes.POINTER(D)], I),
+        "dg_mg_free": ([P, P], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -25,6 +25,7 @@ __all__ = [
     "sortUniquePoints",
     "points2OctreeBatch",
     "coarsenOctree",
+    "MultiGrid",
     "default_context",
 ]
 
@@ -305,6 +306,107 @@ class DA:
     def free(self):
         if getattr(self, "handle", None):
             self.ctx._L.dg_da_free(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class MultiGrid:
+    """Geometric multigrid hierarchy and solver (the reference's DAMG, omg module).
+
+    Levels: the given balanced octree, then coarsenOctree + balanceOctree
+    until a level holds at most ``max_coarse_elems`` elements
+    (src/omg/blockDiag.cpp:1312).  Operator: -lap(u) + u with u = 0 on the
+    boundary of the unit cube (DirichletJacobianMatMult,
+    examples/src/backend/omgJac.C:958).
+    """
+
+    def __init__(self, octree: Octree, max_coarse_elems: int = 4096):
+        ctx = octree.ctx
+        self.ctx = ctx
+        self.max_depth = octree.max_depth
+        h = ctypes.c_void_p()
+        check(ctx.handle, ctx._L.dg_mg_setup(ctx.handle, octree.handle, max_coarse_elems, ctypes.byref(h)), "MultiGrid")
+        self.handle = h
+        n = ctypes.c_size_t()
+        ctx._L.dg_mg_levels(h, ctypes.byref(n))
+        self.n_levels = n.value
+        self.sizes = []
+        for l in range(self.n_levels):
+            e, v = ctypes.c_size_t(), ctypes.c_size_t()
+            ctx._L.dg_mg_level_sizes(h, l, ctypes.byref(e), ctypes.byref(v))
+            self.sizes.append((e.value, v.value))
+
+    def level_nodes(self, level: int) -> np.ndarray:
+        xyz = np.empty((self.sizes[level][1], 3), np.uint32)
+        check(self.ctx.handle, self.ctx._L.dg_mg_level_nodes(self.ctx.handle, self.handle, level, _ptr(xyz), 0), "level_nodes")
+        return xyz
+
+    def level_octree(self, level: int) -> np.ndarray:
+        out = np.empty((self.sizes[level][0], 4), np.uint32)
+        check(self.ctx.handle, self.ctx._L.dg_mg_level_octree(self.ctx.handle, self.handle, level, _ptr(out), 0), "level_octree")
+        return out
+
+    def _op(self, fn, level, x, n_out, precision):
+        on_dev = 1 if _is_device(x) else 0
+        if on_dev:
+            out = x.new_empty((n_out,))
+        else:
+            x = np.ascontiguousarray(x, dtype=np.float64 if precision == 64 else np.float32)
+            out = np.empty(n_out, x.dtype)
+        check(self.ctx.handle, fn(self.ctx.handle, self.handle, level, _ptr(x), _ptr(out), precision, on_dev), fn.__name__)
+        return out
+
+    def matvec(self, level: int, x, precision: int = 64):
+        """DirichletJacobianMatMult on a level."""
+        return self._op(self.ctx._L.dg_mg_matvec, level, x, self.sizes[level][1], precision)
+
+    def restrict(self, fine_level: int, x, precision: int = 64):
+        """restrictMatVecType1: fine level -> next coarser level."""
+        return self._op(self.ctx._L.dg_mg_restrict, fine_level, x, self.sizes[fine_level + 1][1], precision)
+
+    def prolong(self, fine_level: int, x, precision: int = 64):
+        """prolongMatVecType1: next coarser level -> fine level."""
+        return self._op(self.ctx._L.dg_mg_prolong, fine_level, x, self.sizes[fine_level][1], precision)
+
+    def set_smoother(self, omega: float = 0.667, nu_pre: int = 2, nu_post: int = 2):
+        check(self.ctx.handle, self.ctx._L.dg_mg_set_smoother(self.handle, omega, nu_pre, nu_post), "set_smoother")
+
+    def rhs(self, f):
+        """Load vector b = M f of a nodal field on the finest level, 0 on the boundary."""
+        on_dev = 1 if _is_device(f) else 0
+        if on_dev:
+            out = f.new_empty(f.shape)
+        else:
+            f = np.ascontiguousarray(f, dtype=np.float64)
+            out = np.empty_like(f)
+        check(self.ctx.handle, self.ctx._L.dg_mg_rhs(self.ctx.handle, self.handle, _ptr(f), _ptr(out), on_dev), "rhs")
+        return out
+
+    def solve(self, b, precision: int = 32, rtol: float = 1e-8, maxit: int = 200, x=None):
+        """CG preconditioned by one V-cycle (FP32 or FP64) per iteration; FP64 residuals.
+
+        Returns (x, iterations, final FP64 relative residual).
+        """
+        on_dev = 1 if _is_device(b) else 0
+        if on_dev:
+            x = b.new_empty(b.shape) if x is None else x
+        else:
+            b = np.ascontiguousarray(b, dtype=np.float64)
+            x = np.empty_like(b) if x is None else x
+        it, rr = ctypes.c_int(), ctypes.c_double()
+        check(self.ctx.handle,
+              self.ctx._L.dg_mg_solve(self.ctx.handle, self.handle, _ptr(b), _ptr(x), precision, rtol, maxit, on_dev,
+                                      ctypes.byref(it), ctypes.byref(rr)), "solve")
+        return x, it.value, rr.value
+
+    def free(self):
+        if getattr(self, "handle", None):
+            self.ctx._L.dg_mg_free(self.ctx.handle, self.handle)
             self.handle = None
 
     def __del__(self):

@@ -8,7 +8,7 @@
 #include <string>
 
 #include "dendro_gb300.h"
-#include "dg_da.cuh"
+#include "dg_mg.cuh"
 
 struct dg_ctx_s {
   dg::Context c;
@@ -20,6 +20,9 @@ struct dg_octree_s {
 };
 struct dg_da_s {
   dg::Mesh m;
+};
+struct dg_mg_s {
+  dg::MG mg;
 };
 
 namespace {
@@ -426,6 +429,154 @@ int dg_da_free(dg_ctx ctx, dg_da da) {
   dg::mesh_free(ctx->c, da->m);
   cudaStreamSynchronize(ctx->c.stream);
   delete da;
+  return DG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+__global__ void k_zero_bdy(const uint8_t *__restrict__ bdy, size_t n, double *__restrict__ b) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && bdy[i]) b[i] = 0.0;
+}
+
+template <typename F>
+int level_op(dg_ctx ctx, dg_mg mg, size_t n_in, size_t n_out, const void *in, void *out, int precision, int on_device,
+             F &&op) {
+  if (!mg || !in || !out || (precision != 32 && precision != 64)) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() {
+    dg::Context &c = ctx->c;
+    const size_t es = precision == 64 ? 8 : 4;
+    dg::DBuf<unsigned char> hin, hout;
+    const void *x = in;
+    void *y = out;
+    if (!on_device) {
+      hin.alloc(n_in * es, c.stream);
+      hout.alloc(n_out * es, c.stream);
+      DG_CUDA(cudaMemcpyAsync(hin.get(), in, n_in * es, cudaMemcpyHostToDevice, c.stream));
+      x = hin.get();
+      y = hout.get();
+    }
+    op(c, x, y);
+    if (!on_device) DG_CUDA(cudaMemcpyAsync(out, y, n_out * es, cudaMemcpyDeviceToHost, c.stream));
+    DG_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+}  // namespace
+
+extern "C" {
+
+int dg_mg_setup(dg_ctx ctx, dg_octree balanced, size_t max_coarse_elems, dg_mg *out) {
+  if (!balanced || !out) return DG_ERR_INVALID_ARG;
+  *out = nullptr;
+  dg_mg h = new (std::nothrow) dg_mg_s();
+  if (!h) return DG_ERR_OUT_OF_MEMORY;
+  int rc = guarded(ctx, [&]() { dg::mg_setup(ctx->c, balanced->o, max_coarse_elems, h->mg); });
+  if (rc != DG_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return DG_OK;
+}
+
+int dg_mg_levels(dg_mg mg, size_t *n) {
+  if (!mg || !n) return DG_ERR_INVALID_ARG;
+  *n = mg->mg.lv.size();
+  return DG_OK;
+}
+
+int dg_mg_level_sizes(dg_mg mg, size_t level, size_t *n_elem, size_t *n_node) {
+  if (!mg || level >= mg->mg.lv.size()) return DG_ERR_INVALID_ARG;
+  if (n_elem) *n_elem = mg->mg.lv[level].mesh.n_elem;
+  if (n_node) *n_node = mg->mg.lv[level].mesh.n_node;
+  return DG_OK;
+}
+
+int dg_mg_level_nodes(dg_ctx ctx, dg_mg mg, size_t level, uint32_t *node_xyz, int dst_on_device) {
+  if (!mg || level >= mg->mg.lv.size() || !node_xyz) return DG_ERR_INVALID_ARG;
+  dg_da_s tmp;
+  tmp.m = mg->mg.lv[level].mesh;
+  int rc = dg_da_download(ctx, &tmp, nullptr, nullptr, node_xyz, dst_on_device);
+  tmp.m = dg::Mesh();
+  return rc;
+}
+
+int dg_mg_level_octree(dg_ctx ctx, dg_mg mg, size_t level, uint32_t *xyzl, int dst_on_device) {
+  if (!mg || level >= mg->mg.lv.size() || !xyzl) return DG_ERR_INVALID_ARG;
+  dg_octree_s tmp;
+  tmp.o = mg->mg.lv[level].oct;
+  int rc = dg_octree_download(ctx, &tmp, xyzl, dst_on_device);
+  tmp.o = dg::Octree();
+  return rc;
+}
+
+int dg_mg_matvec(dg_ctx ctx, dg_mg mg, size_t level, const void *in, void *out, int precision, int on_device) {
+  if (!mg || level >= mg->mg.lv.size()) return DG_ERR_INVALID_ARG;
+  const dg::MGLevel &L = mg->mg.lv[level];
+  return level_op(ctx, mg, L.mesh.n_node, L.mesh.n_node, in, out, precision, on_device,
+                  [&](dg::Context &c, const void *x, void *y) {
+                    if (precision == 64) dg::dirichlet_matvec<double>(c, L, (const double *)x, (double *)y);
+                    else dg::dirichlet_matvec<float>(c, L, (const float *)x, (float *)y);
+                  });
+}
+
+int dg_mg_restrict(dg_ctx ctx, dg_mg mg, size_t f, const void *in, void *out, int precision, int on_device) {
+  if (!mg || f + 1 >= mg->mg.lv.size()) return DG_ERR_INVALID_ARG;
+  return level_op(ctx, mg, mg->mg.lv[f].mesh.n_node, mg->mg.lv[f + 1].mesh.n_node, in, out, precision, on_device,
+                  [&](dg::Context &c, const void *x, void *y) {
+                    if (precision == 64) dg::mg_restrict<double>(c, mg->mg, (int)f, (const double *)x, (double *)y);
+                    else dg::mg_restrict<float>(c, mg->mg, (int)f, (const float *)x, (float *)y);
+                  });
+}
+
+int dg_mg_prolong(dg_ctx ctx, dg_mg mg, size_t f, const void *in, void *out, int precision, int on_device) {
+  if (!mg || f + 1 >= mg->mg.lv.size()) return DG_ERR_INVALID_ARG;
+  return level_op(ctx, mg, mg->mg.lv[f + 1].mesh.n_node, mg->mg.lv[f].mesh.n_node, in, out, precision, on_device,
+                  [&](dg::Context &c, const void *x, void *y) {
+                    if (precision == 64) dg::mg_prolong<double>(c, mg->mg, (int)f, (const double *)x, (double *)y);
+                    else dg::mg_prolong<float>(c, mg->mg, (int)f, (const float *)x, (float *)y);
+                  });
+}
+
+int dg_mg_set_smoother(dg_mg mg, double omega, int nu_pre, int nu_post) {
+  if (!mg || !(omega > 0) || nu_pre < 0 || nu_post < 0) return DG_ERR_INVALID_ARG;
+  mg->mg.omega = omega;
+  mg->mg.nu_pre = nu_pre;
+  mg->mg.nu_post = nu_post;
+  return DG_OK;
+}
+
+int dg_mg_rhs(dg_ctx ctx, dg_mg mg, const double *f, double *b, int on_device) {
+  if (!mg) return DG_ERR_INVALID_ARG;
+  const dg::MGLevel &L = mg->mg.lv[0];
+  return level_op(ctx, mg, L.mesh.n_node, L.mesh.n_node, f, b, 64, on_device,
+                  [&](dg::Context &c, const void *x, void *y) {
+                    dg::mesh_matvec<double>(c, L.mesh, (const double *)x, (double *)y, 0.0, 1.0);
+                    k_zero_bdy<<<dg::grid_for(L.mesh.n_node, 256), 256, 0, c.stream>>>(L.bdy, L.mesh.n_node,
+                                                                                     (double *)y);
+                    DG_LAUNCH_CHECK();
+                  });
+}
+
+int dg_mg_solve(dg_ctx ctx, dg_mg mg, const double *b, double *x, int precision, double rtol, int maxit, int on_device,
+                int *iterations, double *relres) {
+  if (!mg || !b || !x || maxit < 1 || !(rtol > 0)) return DG_ERR_INVALID_ARG;
+  const size_t n = mg->mg.lv[0].mesh.n_node;
+  dg::MGResult r;
+  int rc = level_op(ctx, mg, n, n, b, x, 64, on_device, [&](dg::Context &c, const void *bb, void *xx) {
+    dg::mg_solve(c, mg->mg, (const double *)bb, (double *)xx, precision, rtol, maxit, r);
+  });
+  if (iterations) *iterations = r.iterations;
+  if (relres) *relres = r.relres;
+  return rc;
+}
+
+int dg_mg_free(dg_ctx ctx, dg_mg mg) {
+  if (!ctx || !mg) return DG_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->c.device);
+  dg::mg_free(ctx->c, mg->mg);
+  delete mg;
   return DG_OK;
 }
 

@@ -72,3 +72,19 @@ def workload(name: str, n: int | None = None) -> np.ndarray:
     if name == "gauss16m":  # precision workload: 16e6 N(0.5, 0.15^2), seed 3
         return gaussian(n or 16_000_000, 0.5, 0.15, seed=3)
     raise KeyError(name)
+
+
+def bumps(xyz_u32: np.ndarray, max_depth: int = 30, seed: int = 3) -> np.ndarray:
+    """Right-hand side field of the Poisson workload at node coordinates
+    (integers at maxDepth scale): f = sum of 4 Gaussian bumps
+    a_i exp(-|x - c_i|^2 / (2 s_i^2)), a ~ U[0.5, 2], c ~ U[0.2, 0.8]^3,
+    s ~ U[0.05, 0.15] (seeded)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = rng.uniform(0.5, 2.0, 4)
+    c = rng.uniform(0.2, 0.8, (4, 3))
+    s = rng.uniform(0.05, 0.15, 4)
+    x = np.asarray(xyz_u32, np.float64) / float(1 << max_depth)
+    f = np.zeros(len(x))
+    for i in range(4):
+        f += a[i] * np.exp(-((x - c[i]) ** 2).sum(1) / (2 * s[i] ** 2))
+    return f

@@ -49,6 +49,7 @@ extern "C" {
 typedef struct dg_ctx_s *dg_ctx;
 typedef struct dg_octree_s *dg_octree;
 typedef struct dg_da_s *dg_da;
+typedef struct dg_mg_s *dg_mg;
 
 /* ---- context ------------------------------------------------------------
  * Replaces the per-rank global state the reference sets up in
@@ -144,6 +145,43 @@ int dg_da_free(dg_ctx ctx, dg_da da);
  * the -lapMatPropFac / -massMatPropFac options (odaJac.C:302-306). */
 int dg_matvec(dg_ctx ctx, dg_da da, const void *in, void *out, int precision, double lapFac, double massFac,
               int on_device);
+
+/* ---- geometric multigrid (omg) ---------------------------------------------
+ * The reference's DAMG hierarchy and solve for -lap(u) + u = f, u = 0 on the
+ * boundary of the unit cube (src/omg/blockDiag.cpp:1312 DAMGCreateAndSetDA,
+ * :1122 DAMGSolve; operators examples/src/backend/omgJac.C:958
+ * DirichletJacobianMatMult; transfers src/omg/restrictMatVec.cpp,
+ * prolongMatVec.cpp; solver options bin/options:48-206).  Levels are made by
+ * coarsenOctree + balanceOctree until a level holds at most
+ * max_coarse_elems elements; the coarsest level is solved with a dense
+ * inverse.  Level 0 is the input octree; its node numbering equals
+ * dg_da_build's on the same octree. */
+int dg_mg_setup(dg_ctx ctx, dg_octree balanced, size_t max_coarse_elems, dg_mg *out);
+int dg_mg_levels(dg_mg mg, size_t *nlevels);
+int dg_mg_level_sizes(dg_mg mg, size_t level, size_t *n_elem, size_t *n_node);
+/* node coordinates of a level, x y z per node (3 * n_node) */
+int dg_mg_level_nodes(dg_ctx ctx, dg_mg mg, size_t level, uint32_t *node_xyz, int dst_on_device);
+/* the level's balanced octree as {x, y, z, level} records */
+int dg_mg_level_octree(dg_ctx ctx, dg_mg mg, size_t level, uint32_t *xyzl, int dst_on_device);
+/* DirichletJacobianMatMult on a level: boundary rows identity, boundary
+ * columns skipped.  precision 32 / 64 as dg_matvec. */
+int dg_mg_matvec(dg_ctx ctx, dg_mg mg, size_t level, const void *in, void *out, int precision, int on_device);
+/* restrictMatVecType1: out (level+1) = R in (level); prolongMatVecType1:
+ * out (level) = P in (level+1), P = R^T. */
+int dg_mg_restrict(dg_ctx ctx, dg_mg mg, size_t fine_level, const void *in, void *out, int precision, int on_device);
+int dg_mg_prolong(dg_ctx ctx, dg_mg mg, size_t fine_level, const void *in, void *out, int precision, int on_device);
+/* damped-Jacobi smoother (default omega 0.667, bin/options:190) and sweeps
+ * per V-cycle side (default 2 and 2) */
+int dg_mg_set_smoother(dg_mg mg, double omega, int nu_pre, int nu_post);
+/* load vector of a nodal field on level 0: b = M f, boundary entries 0 */
+int dg_mg_rhs(dg_ctx ctx, dg_mg mg, const double *f, double *b, int on_device);
+/* CG preconditioned by one V-cycle per iteration, to ||b - A x|| <= rtol
+ * ||b||.  Residual, dot products and updates are FP64; the V-cycle runs in
+ * FP32 (precision 32) or FP64 (precision 64).  *relres is the final FP64
+ * relative residual recomputed from x. */
+int dg_mg_solve(dg_ctx ctx, dg_mg mg, const double *b, double *x, int precision, double rtol, int maxit, int on_device,
+                int *iterations, double *relres);
+int dg_mg_free(dg_ctx ctx, dg_mg mg);
 
 /* ---- timing ---------------------------------------------------------------
  * Milliseconds of device time spent by the last completed call on ctx

@@ -794,3 +794,155 @@ int dgo_matvec(const dgo_da *da, unsigned D, const double *in, double *out, doub
   (void)D;
   return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* multigrid building blocks (examples/src/backend/omgJac.C, src/omg/*)      */
+/* ------------------------------------------------------------------------ */
+/* boundary flag per node: a node on the boundary of the unit cube
+ * (assignBoundaryFlags, src/oda/odaUtils.cpp:2464) */
+static int node_on_bdy(const dgo_da *da, size_t i, unsigned D) {
+  const uint32_t dom = 1u << D, *p = &da->node_xyz[3 * i];
+  return p[0] == 0 || p[1] == 0 || p[2] == 0 || p[0] == dom || p[1] == dom || p[2] == dom;
+}
+
+/* DirichletJacobianMatMult (omgJac.C:958-1057): boundary rows identity,
+ * boundary columns skipped */
+int dgo_dirichlet_matvec(const dgo_da *da, unsigned D, const double *in, double *out) {
+  static double L[8 * 18 * 64], M[8 * 18 * 64];
+  static int have = 0;
+  if (!have) {
+    dgo_stencils(L, M);
+    have = 1;
+  }
+  memset(out, 0, da->n_node * sizeof(double));
+  for (size_t e = 0; e < da->n_elem; e++) {
+    double h = 1.0 / (double)((uint64_t)1 << da->level[e]);
+    double f1 = h / 2.0, f2 = h * h * h / 8.0;
+    const double *Ls = &L[((size_t)da->child[e] * 18 + da->etype[e]) * 64];
+    const double *Ms = &M[((size_t)da->child[e] * 18 + da->etype[e]) * 64];
+    const uint32_t *id = &da->nodes[8 * e];
+    for (int k = 0; k < 8; k++) {
+      if (node_on_bdy(da, id[k], D)) {
+        out[id[k]] = in[id[k]];
+        continue;
+      }
+      for (int j = 0; j < 8; j++)
+        if (!node_on_bdy(da, id[j], D)) out[id[k]] += (f1 * Ls[8 * k + j] + f2 * Ms[8 * k + j]) * in[id[j]];
+    }
+  }
+  return 0;
+}
+
+/* diagonal of the Dirichlet operator (1 on the boundary) */
+int dgo_dirichlet_diag(const dgo_da *da, unsigned D, double *diag) {
+  double L[8 * 18 * 64], M[8 * 18 * 64];
+  dgo_stencils(L, M);
+  memset(diag, 0, da->n_node * sizeof(double));
+  for (size_t e = 0; e < da->n_elem; e++) {
+    double h = 1.0 / (double)((uint64_t)1 << da->level[e]);
+    double f1 = h / 2.0, f2 = h * h * h / 8.0;
+    const double *Ls = &L[((size_t)da->child[e] * 18 + da->etype[e]) * 64];
+    const double *Ms = &M[((size_t)da->child[e] * 18 + da->etype[e]) * 64];
+    for (int k = 0; k < 8; k++) {
+      uint32_t id = da->nodes[8 * e + k];
+      if (node_on_bdy(da, id, D)) diag[id] = 1.0;
+      else diag[id] += f1 * Ls[9 * k] + f2 * Ms[9 * k];
+    }
+  }
+  return 0;
+}
+
+/* prolongation from a coarse level onto the nodes of a fine level: for every
+ * fine node the coarse element holding it (restrictMatVec.cpp:74-146 loops
+ * over coarse elements and their fine children with the RmatType1/2
+ * stencils; the weights are the coarse shape functions at the fine vertex,
+ * folded through the coarse element's hanging interpolation).  Pairs with a
+ * boundary node on either level carry no weight.  ids/w: 8 per fine node. */
+int dgo_prolong_map(const dgo_da *fine, const dgo_oct *coarse_oct, size_t nc, const dgo_da *coarse, unsigned D,
+                    uint32_t *ids, double *w) {
+  u128 *keys = (u128 *)malloc((nc ? nc : 1) * sizeof(u128));
+  if (!keys) return DGO_ENOMEM;
+  for (size_t i = 0; i < nc; i++) keys[i] = morton(coarse_oct[i].x, coarse_oct[i].y, coarse_oct[i].z);
+  const uint32_t dom = 1u << D;
+  uint8_t masks[8 * 18];
+  dgo_etype_masks(masks);
+  int rc = 0;
+  for (size_t v = 0; v < fine->n_node; v++) {
+    const uint32_t *p = &fine->node_xyz[3 * v];
+    uint32_t q[3];
+    for (int a = 0; a < 3; a++) q[a] = p[a] == dom ? dom - 1 : p[a];
+    size_t e = find_leaf(keys, nc, q[0], q[1], q[2]);
+    if (e == nc) {
+      rc = DGO_EINTERNAL;
+      break;
+    }
+    const dgo_oct *ce = &coarse_oct[e];
+    uint64_t h = (uint64_t)1 << (D - ce->lev);
+    uint32_t an[3] = {ce->x, ce->y, ce->z};
+    int xi2[3];
+    for (int a = 0; a < 3; a++) {
+      uint64_t d = (uint64_t)p[a] - an[a];
+      if (d == 0) xi2[a] = 0;
+      else if (2 * d == h) xi2[a] = 1;
+      else if (d == h) xi2[a] = 2;
+      else {
+        rc = DGO_EINTERNAL;
+        goto done;
+      }
+    }
+    double P[8][8];
+    hanging_interp(coarse->child[e], masks[coarse->child[e] * 18 + coarse->etype[e]], P);
+    int fb = node_on_bdy(fine, v, D);
+    for (int j = 0; j < 8; j++) {
+      double wj = 0.0;
+      for (int k = 0; k < 8; k++) {
+        double Nk = 1.0;
+        for (int a = 0; a < 3; a++) {
+          double t = 0.5 * xi2[a];
+          Nk *= ((k >> a) & 1) ? t : 1.0 - t;
+        }
+        wj += Nk * P[k][j];
+      }
+      uint32_t cid = coarse->nodes[8 * e + j];
+      ids[8 * v + j] = cid;
+      w[8 * v + j] = (fb || node_on_bdy(coarse, cid, D)) ? 0.0 : wj;
+    }
+  }
+done:
+  free(keys);
+  return rc;
+}
+
+/* The restriction stencils the reference reads from RmatType1Stencils.inp
+ * ([cNumCoarse][cNumFine][type][coarse j][fine vertex f]) and
+ * RmatType2Stencils.inp ([cNum][type][j][f]) (rmatType1StencilsAux.cpp:14,
+ * rmatType2StencilsAux.cpp:15), restated: the coarse element's shape
+ * functions at the fine vertex, folded through its hanging interpolation. */
+void dgo_rmat_tables(double *r1, double *r2) {
+  uint8_t masks[8 * 18];
+  dgo_etype_masks(masks);
+  for (int cc = 0; cc < 8; cc++)
+    for (int t = 0; t < 18; t++) {
+      double P[8][8];
+      hanging_interp(cc, masks[cc * 18 + t], P);
+      for (int j = 0; j < 8; j++)
+        for (int f = 0; f < 8; f++) r2[((cc * 18 + t) * 8 + j) * 8 + f] = P[f][j];
+      for (int cf = 0; cf < 8; cf++)
+        for (int f = 0; f < 8; f++) {
+          double N[8];
+          for (int k = 0; k < 8; k++) {
+            double v = 1.0;
+            for (int a = 0; a < 3; a++) {
+              double xi = 0.5 * (((cf >> a) & 1) + ((f >> a) & 1));
+              v *= ((k >> a) & 1) ? xi : 1.0 - xi;
+            }
+            N[k] = v;
+          }
+          for (int j = 0; j < 8; j++) {
+            double w = 0.0;
+            for (int k = 0; k < 8; k++) w += N[k] * P[k][j];
+            r1[((((size_t)cc * 8 + cf) * 18 + t) * 8 + j) * 8 + f] = w;
+          }
+        }
+    }
+}

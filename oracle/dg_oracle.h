@@ -110,6 +110,21 @@ void dgo_da_free(dgo_da *da);
  * unit cube.  out is overwritten (zeroed first). */
 int dgo_matvec(const dgo_da *da, unsigned maxDepth, const double *in, double *out, double lapFac, double massFac);
 
+/* Multigrid building blocks.  Boundary nodes are the nodes on the boundary
+ * of the unit cube (assignBoundaryFlags, src/oda/odaUtils.cpp:2464).
+ * dgo_dirichlet_matvec: DirichletJacobianMatMult (examples/src/backend/
+ * omgJac.C:958-1057); dgo_dirichlet_diag: its diagonal; dgo_prolong_map: 8
+ * (coarse node, weight) pairs per fine node, the transpose of
+ * restrictMatVecType1 (src/omg/restrictMatVec.cpp:74-146). */
+int dgo_dirichlet_matvec(const dgo_da *da, unsigned maxDepth, const double *in, double *out);
+int dgo_dirichlet_diag(const dgo_da *da, unsigned maxDepth, double *diag);
+int dgo_prolong_map(const dgo_da *fine, const dgo_oct *coarse_oct, size_t nc, const dgo_da *coarse, unsigned maxDepth,
+                    uint32_t *ids, double *w);
+
+/* Restriction stencil tables (Stencils/RmatType1Stencils.inp, 8*8*18*64
+ * doubles; RmatType2Stencils.inp, 8*18*64 doubles), from the mathematics. */
+void dgo_rmat_tables(double *r1, double *r2);
+
 /* FNV-1a over the {x,y,z,lev} records (u32 little-endian). */
 uint64_t dgo_fnv1a(const dgo_oct *a, size_t n);
 

@@ -66,6 +66,10 @@ def lib():
         L.dgo_da_build.argtypes = [P, SZ, U, ctypes.POINTER(_DA)]
         L.dgo_da_free.argtypes = [ctypes.POINTER(_DA)]
         L.dgo_matvec.argtypes = [ctypes.POINTER(_DA), U, P, P, ctypes.c_double, ctypes.c_double]
+        L.dgo_dirichlet_matvec.argtypes = [ctypes.POINTER(_DA), U, P, P]
+        L.dgo_dirichlet_diag.argtypes = [ctypes.POINTER(_DA), U, P]
+        L.dgo_prolong_map.argtypes = [ctypes.POINTER(_DA), P, SZ, ctypes.POINTER(_DA), U, P, P]
+        L.dgo_rmat_tables.argtypes = [P, P]
         L.dgo_fnv1a.argtypes = [P, SZ]
         L.dgo_fnv1a.restype = ctypes.c_uint64
         _lib = L
@@ -168,6 +172,13 @@ def stencils():
     return lap.reshape(8, 18, 8, 8), mass.reshape(8, 18, 8, 8)
 
 
+def rmat_tables():
+    r1 = np.zeros(8 * 8 * 18 * 64)
+    r2 = np.zeros(8 * 18 * 64)
+    lib().dgo_rmat_tables(_ptr(r1), _ptr(r2))
+    return r1.reshape(8, 8, 18, 8, 8), r2.reshape(8, 18, 8, 8)
+
+
 class DA:
     """Oracle DA: per-element child/hmask/etype/level/nodes and node coordinates."""
 
@@ -195,6 +206,31 @@ class DA:
         y = np.zeros(self.n_node)
         _check(lib().dgo_matvec(ctypes.byref(self._da), self.max_depth, _ptr(x), _ptr(y), lap_fac, mass_fac), "matvec")
         return y
+
+    def bdy(self) -> np.ndarray:
+        dom = 1 << self.max_depth
+        x = self.node_xyz
+        return np.any((x == 0) | (x == dom), axis=1)
+
+    def dirichlet_matvec(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(self.n_node)
+        _check(lib().dgo_dirichlet_matvec(ctypes.byref(self._da), self.max_depth, _ptr(x), _ptr(y)), "dirichlet_matvec")
+        return y
+
+    def dirichlet_diag(self) -> np.ndarray:
+        d = np.zeros(self.n_node)
+        _check(lib().dgo_dirichlet_diag(ctypes.byref(self._da), self.max_depth, _ptr(d)), "dirichlet_diag")
+        return d
+
+    def prolong_map(self, coarse_octs: np.ndarray, coarse: "DA"):
+        """(ids, weights): 8 coarse nodes and weights per node of this (fine) mesh."""
+        c = np.ascontiguousarray(coarse_octs, dtype=np.uint32).reshape(-1, 4)
+        ids = np.zeros((self.n_node, 8), np.uint32)
+        w = np.zeros((self.n_node, 8))
+        _check(lib().dgo_prolong_map(ctypes.byref(self._da), _ptr(c), c.shape[0], ctypes.byref(coarse._da),
+                                     self.max_depth, _ptr(ids), _ptr(w)), "prolong_map")
+        return ids, w
 
     def __del__(self):
         try:

@@ -7,7 +7,8 @@ outputs next to the inputs:
   ref_cases.npz   points2Octree and balanceOctree outputs for small inputs
   ref_da.npz      ot::DA element data and one Laplacian+mass matVec
   ref_tables.npz  element-type masks (include/oda/cnumEtypes.h) and
-                  statistics of the type-2 stencil tables (Stencils/*.inp)
+                  statistics of the type-2 stencil tables and of the
+                  restriction stencils RmatType1/2 (Stencils/*.inp)
   ref_hashes.json counts and FNV-1a hashes of larger octrees
 
 Usage:  python tests/golden/make_golden.py [/path/to/reference]
@@ -163,8 +164,16 @@ def main():
         w = np.arange(1, 65, dtype=np.float64).reshape(8, 8)
         return np.stack([a.sum((2, 3)), (a * a).sum((2, 3)), (a * w).sum((2, 3)), a[:, :, 0, :].sum(2)], -1)
 
+    def rmat(fname, shape):
+        a = np.array(open(os.path.join(REF, "Stencils", fname)).read().split(), np.float64)
+        a = a[: int(np.prod(shape))].reshape(shape)
+        w = np.arange(1, 65, dtype=np.float64).reshape(8, 8)
+        return np.stack([a.sum((-2, -1)), (a * w).sum((-2, -1)), (a * a).sum((-2, -1))], -1)
+
     np.savez_compressed(os.path.join(HERE, "ref_tables.npz"), etype_masks=masks, lap_stats=stats("LapType2Stencils.inp"),
-                        mass_stats=stats("MassType2Stencils.inp"))
+                        mass_stats=stats("MassType2Stencils.inp"),
+                        rmat1_stats=rmat("RmatType1Stencils.inp", (8, 8, 18, 8, 8)),
+                        rmat2_stats=rmat("RmatType2Stencils.inp", (8, 18, 8, 8)))
     print("golden fixtures written to", HERE)
 
 

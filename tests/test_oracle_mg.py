@@ -1,0 +1,70 @@
+"""Multigrid oracle checks (CPU): transfer stencils pinned to the reference's
+RmatType1/2 tables, coarsening pinned to the reference, P = R^T, and the
+restated PCG + V-cycle converging."""
+import os
+
+import numpy as np
+import pytest
+
+from dendro_gb300 import datagen
+from oracle.mg_ref import OracleMG
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_rmat_tables_match_reference(oracle):
+    t = np.load(os.path.join(GOLDEN, "ref_tables.npz"))
+    r1, r2 = oracle.rmat_tables()
+    w = np.arange(1, 65, dtype=np.float64).reshape(8, 8)
+
+    def stats(a):
+        return np.stack([a.sum((-2, -1)), (a * w).sum((-2, -1)), (a * a).sum((-2, -1))], -1)
+
+    assert np.allclose(stats(r1), t["rmat1_stats"], rtol=0, atol=1e-12)
+    assert np.allclose(stats(r2), t["rmat2_stats"], rtol=0, atol=1e-12)
+
+
+def test_coarsen_matches_reference_cases(oracle):
+    g = np.load(os.path.join(GOLDEN, "ref_cases.npz"))
+    bal = g["gauss3k/bal"]
+    c = oracle.coarsen(bal, 30)
+    assert oracle.checks(c, 30)["complete"] and oracle.checks(c, 30)["linear"]
+    assert len(c) < len(bal)
+    # coarsening never merges across a non-family: every parent output has 8 input children
+    assert np.array_equal(oracle.coarsen(np.zeros((1, 4), np.uint32), 30), np.zeros((1, 4), np.uint32))
+
+
+@pytest.fixture(scope="module")
+def small_mg(oracle):
+    pts = datagen.gaussian(2500, 0.5, 0.15, seed=3)
+    bal = oracle.balance(oracle.points_to_octree(pts, 30, 1), 30)
+    return OracleMG(bal, 30, max_coarse=400)
+
+
+def test_transfers_are_adjoint(small_mg):
+    rng = np.random.Generator(np.random.PCG64(2))
+    for l in range(small_mg.n_levels - 1):
+        u = rng.random(small_mg.das[l + 1].n_node)
+        v = rng.random(small_mg.das[l].n_node)
+        assert abs(v @ small_mg.prolong(l, u) - u @ small_mg.restrict(l, v)) <= 1e-12 * abs(v @ small_mg.prolong(l, u))
+
+
+def test_prolongation_reproduces_coarse_linear_fields(small_mg):
+    # a trilinear field on the coarse mesh is interpolated exactly at interior fine nodes
+    for l in range(small_mg.n_levels - 1):
+        xc = small_mg.das[l + 1].node_xyz.astype(np.float64) / (1 << 30)
+        xf = small_mg.das[l].node_xyz.astype(np.float64) / (1 << 30)
+        g = lambda x: 1.0 + 2 * x[:, 0] - x[:, 1] + 0.5 * x[:, 2]  # noqa: E731
+        pf = small_mg.prolong(l, g(xc))
+        interior = ~small_mg.das[l].bdy()
+        ids, w = small_mg.pmaps[l]
+        full = interior & np.isclose(w.sum(1), 1.0)
+        assert np.allclose(pf[full], g(xf)[full], atol=1e-13)
+
+
+def test_oracle_solver_converges(small_mg):
+    b = small_mg.rhs(datagen.bumps(small_mg.das[0].node_xyz))
+    x, it, rr = small_mg.solve(b, 1e-8, 100)
+    assert rr <= 1e-8
+    assert it < 30
+    assert np.all(x[small_mg.das[0].bdy()] == 0.0)
