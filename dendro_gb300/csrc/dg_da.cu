@@ -19,6 +19,7 @@
 // set is numbered by one scan over elements; the owner of any vertex is the
 // leaf that contains it after clamping boundary coordinates inward.
 #include "dg_da.cuh"
+#include "dg_elem.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -134,6 +135,23 @@ void ensure_stencils(Context &ctx) {
   DG_CUDA(cudaMemcpy(d32, s32.data(), STEN_ENTRIES * sizeof(float), cudaMemcpyHostToDevice));
   DG_CUDA(cudaMemcpy(det, etype_of, sizeof(etype_of), cudaMemcpyHostToDevice));
   DG_CUDA(cudaMemcpy(dem, masks, sizeof(masks), cudaMemcpyHostToDevice));
+  std::vector<double> p64(PSTEN_ENTRIES);
+  std::vector<float> p32(PSTEN_ENTRIES);
+  for (int ct = 0; ct < 8 * 18; ct++)
+    for (int k = 0; k < 8; k++)
+      for (int j = 0; j <= k; j++) {
+        p64[ct * PSTEN_PER_TYPE + tri_index(k, j)] = lap[ct * 64 + 8 * k + j];
+        p64[ct * PSTEN_PER_TYPE + 36 + tri_index(k, j)] = mass[ct * 64 + 8 * k + j];
+      }
+  for (int i = 0; i < PSTEN_ENTRIES; i++) p32[i] = (float)p64[i];
+  double *dp64 = nullptr;
+  float *dp32 = nullptr;
+  DG_CUDA(cudaMalloc((void **)&dp64, PSTEN_ENTRIES * sizeof(double)));
+  DG_CUDA(cudaMalloc((void **)&dp32, PSTEN_ENTRIES * sizeof(float)));
+  DG_CUDA(cudaMemcpy(dp64, p64.data(), PSTEN_ENTRIES * sizeof(double), cudaMemcpyHostToDevice));
+  DG_CUDA(cudaMemcpy(dp32, p32.data(), PSTEN_ENTRIES * sizeof(float), cudaMemcpyHostToDevice));
+  ctx.d_psten64 = dp64;
+  ctx.d_psten32 = dp32;
   ctx.d_sten64 = d64;
   ctx.d_sten32 = d32;
   ctx.d_etype_of = det;
@@ -329,35 +347,36 @@ void mesh_free(Context &ctx, Mesh &m) {
 // ------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(512) k_matvec(const uint32_t *__restrict__ meta, const uint32_t *__restrict__ conn,
-                                                size_t E, const T *__restrict__ sten, const T *__restrict__ x,
+                                                size_t E, const T *__restrict__ psten, const T *__restrict__ x,
                                                 T *__restrict__ y, T lapf, T massf) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *ss = reinterpret_cast<T *>(smem_raw);
-  for (int i = threadIdx.x; i < STEN_ENTRIES; i += blockDim.x) ss[i] = sten[i];
-  __syncthreads();
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
-    const uint32_t me = meta[e];
-    const unsigned l = me & 255u, c = (me >> 8) & 7u, t = me >> 24;
-    uint32_t id[8];
-    T xv[8];
+  T *ps = reinterpret_cast<T *>(smem_raw);
+  T *aval = ps + PSTEN_ENTRIES;
+  uint32_t *akey = reinterpret_cast<uint32_t *>(aval + ACC_SLOTS);
+  for (int i = threadIdx.x; i < PSTEN_ENTRIES; i += blockDim.x) ps[i] = psten[i];
+  BlockAccum<T> acc{akey, aval};
+  for (size_t base = (size_t)blockIdx.x * blockDim.x; base < E; base += (size_t)gridDim.x * blockDim.x) {
+    acc.clear();
+    __syncthreads();
+    const size_t e = base + threadIdx.x;
+    if (e < E) {
+      const uint32_t me = meta[e];
+      const unsigned l = me & 255u, c = (me >> 8) & 7u, t = me >> 24;
+      uint32_t id[8];
+      T xv[8], yv[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) id[k] = conn[(size_t)k * E + e];
+      for (int k = 0; k < 8; k++) id[k] = conn[(size_t)k * E + e];
 #pragma unroll
-    for (int k = 0; k < 8; k++) xv[k] = x[id[k]];
-    // h = 2^-l (element side in the unit cube)
-    const T h = (T)1 / (T)(1ull << l);
-    const T f1 = lapf * h * (T)0.5, f2 = massf * h * h * h * (T)0.125;
-    const T *S = ss + (c * 18 + t) * 128;
+      for (int k = 0; k < 8; k++) xv[k] = x[id[k]];
+      // h = 2^-l (element side in the unit cube)
+      const T h = (T)1 / (T)(1ull << l);
+      apply_packed<T>(ps + (c * 18 + t) * PSTEN_PER_TYPE, lapf * h * (T)0.5, massf * h * h * h * (T)0.125, xv, yv);
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-      T aL = 0, aM = 0;
-#pragma unroll
-      for (int j = 0; j < 8; j++) {
-        aL += S[8 * k + j] * xv[j];
-        aM += S[64 + 8 * k + j] * xv[j];
-      }
-      atomicAdd(&y[id[k]], f1 * aL + f2 * aM);
+      for (int k = 0; k < 8; k++) acc.add(id[k], yv[k], y);
     }
+    __syncthreads();
+    acc.flush(y);
+    __syncthreads();
   }
 }
 
@@ -366,7 +385,7 @@ void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, 
   ensure_stencils(ctx);
   cudaStream_t s = ctx.stream;
   DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
-  const size_t smem = STEN_ENTRIES * sizeof(T);
+  const size_t smem = PSTEN_ENTRIES * sizeof(T) + ACC_SLOTS * (sizeof(T) + sizeof(uint32_t));
   static std::once_flag once;
   std::call_once(once, [&]() {
     DG_CUDA(cudaFuncSetAttribute(k_matvec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -376,13 +395,13 @@ void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, 
   DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_matvec<T>, block, smem));
   if (per_sm < 1) per_sm = 1;
   unsigned grid = grid_for(m.n_elem, block, (unsigned)(per_sm * ctx.num_sms));
-  const T *sten = std::is_same<T, double>::value ? reinterpret_cast<const T *>(ctx.d_sten64)
-                                                 : reinterpret_cast<const T *>(ctx.d_sten32);
+  const T *psten = std::is_same<T, double>::value ? reinterpret_cast<const T *>(ctx.d_psten64)
+                                                  : reinterpret_cast<const T *>(ctx.d_psten32);
   {
     ProfScope _prof(ctx, "matvec", (double)m.n_elem * 36 + (double)m.n_node * 3 * sizeof(T));
-    k_matvec<T><<<grid, block, smem, s>>>(m.meta, m.conn, m.n_elem, sten, x, y, (T)lap_fac, (T)mass_fac);
-  DG_LAUNCH_CHECK();
-    }
+    k_matvec<T><<<grid, block, smem, s>>>(m.meta, m.conn, m.n_elem, psten, x, y, (T)lap_fac, (T)mass_fac);
+    DG_LAUNCH_CHECK();
+  }
 }
 
 template void mesh_matvec<float>(Context &, const Mesh &, const float *, float *, double, double);

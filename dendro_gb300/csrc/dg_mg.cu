@@ -15,6 +15,7 @@
 // Pairs with a fine or a coarse boundary node carry no weight, as with the
 // reference's suppressed Dirichlet DOFs.
 #include "dg_mg.cuh"
+#include "dg_elem.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -29,9 +30,9 @@ void coarsen_octree(Context &ctx, const Octree &in, Octree &out);
 namespace {
 
 template <typename T>
-const T *sten_ptr(const Context &c) {
-  return std::is_same<T, double>::value ? reinterpret_cast<const T *>(c.d_sten64)
-                                        : reinterpret_cast<const T *>(c.d_sten32);
+const T *psten_ptr(const Context &c) {
+  return std::is_same<T, double>::value ? reinterpret_cast<const T *>(c.d_psten64)
+                                        : reinterpret_cast<const T *>(c.d_psten32);
 }
 
 __global__ void k_node_bdy(const uint32_t *__restrict__ xyz, size_t V, unsigned D, uint8_t *__restrict__ bdy) {
@@ -47,43 +48,44 @@ __global__ void k_node_bdy(const uint32_t *__restrict__ xyz, size_t V, unsigned 
 template <typename T>
 __global__ void __launch_bounds__(512) k_dirichlet_matvec(const uint32_t *__restrict__ meta,
                                                           const uint32_t *__restrict__ conn, size_t E,
-                                                          const T *__restrict__ sten, const uint8_t *__restrict__ bdy,
-                                                          const T *__restrict__ x, T *__restrict__ y) {
+                                                          const T *__restrict__ psten,
+                                                          const uint8_t *__restrict__ bdy, const T *__restrict__ x,
+                                                          T *__restrict__ y) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *ss = reinterpret_cast<T *>(smem_raw);
-  for (int i = threadIdx.x; i < STEN_ENTRIES; i += blockDim.x) ss[i] = sten[i];
-  __syncthreads();
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
-    const uint32_t me = meta[e];
-    const unsigned l = me & 255u, c = (me >> 8) & 7u, t = me >> 24;
-    uint32_t id[8];
-    T xv[8];
-    unsigned bm = 0;
+  T *ps = reinterpret_cast<T *>(smem_raw);
+  T *aval = ps + PSTEN_ENTRIES;
+  uint32_t *akey = reinterpret_cast<uint32_t *>(aval + ACC_SLOTS);
+  for (int i = threadIdx.x; i < PSTEN_ENTRIES; i += blockDim.x) ps[i] = psten[i];
+  BlockAccum<T> acc{akey, aval};
+  for (size_t base = (size_t)blockIdx.x * blockDim.x; base < E; base += (size_t)gridDim.x * blockDim.x) {
+    acc.clear();
+    __syncthreads();
+    const size_t e = base + threadIdx.x;
+    if (e < E) {
+      const uint32_t me = meta[e];
+      const unsigned l = me & 255u, c = (me >> 8) & 7u, t = me >> 24;
+      uint32_t id[8];
+      T xv[8], xin[8], yv[8];
+      unsigned bm = 0;
 #pragma unroll
-    for (int k = 0; k < 8; k++) id[k] = conn[(size_t)k * E + e];
+      for (int k = 0; k < 8; k++) id[k] = conn[(size_t)k * E + e];
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-      bm |= (unsigned)bdy[id[k]] << k;
-      xv[k] = x[id[k]];
-    }
-    const T h = (T)1 / (T)(1ull << l);
-    const T f1 = h * (T)0.5, f2 = h * h * h * (T)0.125;
-    const T *S = ss + (c * 18 + t) * 128;
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-      if (bm >> k & 1) {
-        y[id[k]] = xv[k];
-        continue;
+      for (int k = 0; k < 8; k++) {
+        bm |= (unsigned)bdy[id[k]] << k;
+        xin[k] = x[id[k]];
+        xv[k] = (bm >> k & 1) ? (T)0 : xin[k];
       }
-      T aL = 0, aM = 0;
+      const T h = (T)1 / (T)(1ull << l);
+      apply_packed<T>(ps + (c * 18 + t) * PSTEN_PER_TYPE, h * (T)0.5, h * h * h * (T)0.125, xv, yv);
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
-        const T xj = (bm >> j & 1) ? (T)0 : xv[j];
-        aL += S[8 * k + j] * xj;
-        aM += S[64 + 8 * k + j] * xj;
+      for (int k = 0; k < 8; k++) {
+        if (bm >> k & 1) y[id[k]] = xin[k];
+        else acc.add(id[k], yv[k], y);
       }
-      atomicAdd(&y[id[k]], f1 * aL + f2 * aM);
     }
+    __syncthreads();
+    acc.flush(y);
+    __syncthreads();
   }
 }
 
@@ -355,7 +357,7 @@ void dirichlet_matvec(Context &ctx, const MGLevel &L, const T *x, T *y) {
   cudaStream_t s = ctx.stream;
   const Mesh &m = L.mesh;
   DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
-  const size_t smem = STEN_ENTRIES * sizeof(T);
+  const size_t smem = PSTEN_ENTRIES * sizeof(T) + ACC_SLOTS * (sizeof(T) + sizeof(uint32_t));
   static std::once_flag once;
   std::call_once(once, [&]() {
     DG_CUDA(cudaFuncSetAttribute(k_dirichlet_matvec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -364,7 +366,7 @@ void dirichlet_matvec(Context &ctx, const MGLevel &L, const T *x, T *y) {
   DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dirichlet_matvec<T>, 512, smem));
   unsigned grid = grid_for(m.n_elem, 512, (unsigned)(std::max(per_sm, 1) * ctx.num_sms));
   ProfScope _prof(ctx, "dirichlet_matvec", (double)m.n_elem * 36 + (double)m.n_node * (3 * sizeof(T) + 1));
-  k_dirichlet_matvec<T><<<grid, 512, smem, s>>>(m.meta, m.conn, m.n_elem, sten_ptr<T>(ctx), L.bdy, x, y);
+  k_dirichlet_matvec<T><<<grid, 512, smem, s>>>(m.meta, m.conn, m.n_elem, psten_ptr<T>(ctx), L.bdy, x, y);
   DG_LAUNCH_CHECK();
 }
 

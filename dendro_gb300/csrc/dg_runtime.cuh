@@ -44,6 +44,8 @@ struct Context {
   float *d_sten32 = nullptr;
   uint8_t *d_etype_of = nullptr;   // [8][256] -> element type or 255
   uint8_t *d_etype_mask = nullptr; // [8][18] -> hanging mask
+  double *d_psten64 = nullptr;     // packed symmetric stencils (dg_elem.cuh)
+  float *d_psten32 = nullptr;
   bool prof = false;
   std::map<std::string, ProfStat> prof_stats;
   std::vector<ProfPending> prof_pending;
