@@ -66,6 +66,7 @@ def _declare(L):
         "dg_points_to_octree": ([P, P, SZ, P, U, U, I, I, PP], I),
         "dg_points_to_octree_batch": ([P, P, SZ, P, SZ, P, U, U, I, PP], I),
         "dg_octree_segments": ([P, P, ctypes.POINTER(SZ), P], I),
+        "dg_octree_extract": ([P, P, SZ, PP], I),
         "dg_sort_unique_points": ([P, P, SZ, P, U, I, P, I, ctypes.POINTER(SZ)], I),
         "dg_balance_octree": ([P, P, I, I, PP], I),
         "dg_coarsen_octree": ([P, P, PP], I),

@@ -123,6 +123,12 @@ class Octree:
               "dg_octree_segments")
         return off
 
+    def extract(self, seg: int) -> "Octree":
+        """Cloud ``seg`` of a batch as its own device-resident octree."""
+        h = ctypes.c_void_p()
+        check(self.ctx.handle, self.ctx._L.dg_octree_extract(self.ctx.handle, self.handle, seg, ctypes.byref(h)), "extract")
+        return Octree(self.ctx, h)
+
     def split(self) -> list:
         """The octree of every cloud, as (n_s, 4) uint32 arrays."""
         a = self.to_numpy()
@@ -150,9 +156,11 @@ class Octree:
         check(ctx.handle, ctx._L.dg_octree_upload(ctx.handle, _ptr(a), a.shape[0], maxDepth, 0, ctypes.byref(h)), "dg_octree_upload")
         return cls(ctx, h)
 
-    def free(self):
+    def free(self, ctx: "Context | None" = None):
+        """Release the device memory (on ``ctx``'s stream when given)."""
         if self.handle:
-            self.ctx._L.dg_octree_free(self.ctx.handle, self.handle)
+            c = ctx or self.ctx
+            c._L.dg_octree_free(c.handle, self.handle)
             self.handle = None
 
     def __del__(self):
@@ -325,8 +333,8 @@ class MultiGrid:
     examples/src/backend/omgJac.C:958).
     """
 
-    def __init__(self, octree: Octree, max_coarse_elems: int = 4096):
-        ctx = octree.ctx
+    def __init__(self, octree: Octree, max_coarse_elems: int = 4096, ctx: Context | None = None):
+        ctx = ctx or octree.ctx
         self.ctx = ctx
         self.max_depth = octree.max_depth
         h = ctypes.c_void_p()

@@ -250,6 +250,20 @@ int dg_octree_segments(dg_ctx ctx, dg_octree o, size_t *nseg, uint64_t *offsets)
   return guarded(ctx, [&]() { dg::octree_segment_offsets(ctx->c, o->o, offsets); });
 }
 
+int dg_octree_extract(dg_ctx ctx, dg_octree o, size_t seg, dg_octree *out) {
+  if (!o || !out) return DG_ERR_INVALID_ARG;
+  *out = nullptr;
+  dg_octree h = new (std::nothrow) dg_octree_s();
+  if (!h) return DG_ERR_OUT_OF_MEMORY;
+  int rc = guarded(ctx, [&]() { dg::octree_extract(ctx->c, o->o, seg, h->o); });
+  if (rc != DG_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return DG_OK;
+}
+
 int dg_sort_unique_points(dg_ctx ctx, const double *xyz, size_t n, const double gLens[3], unsigned maxDepth,
                           int xyz_on_device, uint32_t *out_xyzl, int out_on_device, size_t *n_unique) {
   if ((!xyz && n) || !gLens || !n_unique || (!out_xyzl && n)) return DG_ERR_INVALID_ARG;

@@ -346,36 +346,41 @@ void mesh_free(Context &ctx, Mesh &m) {
 // element loop
 // ------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(512) k_matvec(const uint32_t *__restrict__ meta, const uint32_t *__restrict__ conn,
+__global__ void __launch_bounds__(512, 2) k_matvec(const uint32_t *__restrict__ meta, const uint32_t *__restrict__ conn,
                                                 size_t E, const T *__restrict__ psten, const T *__restrict__ x,
-                                                T *__restrict__ y, T lapf, T massf) {
+                                                T *__restrict__ y, size_t n_node, T lapf, T massf) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *ps = reinterpret_cast<T *>(smem_raw);
   T *aval = ps + PSTEN_ENTRIES;
-  uint32_t *akey = reinterpret_cast<uint32_t *>(aval + ACC_SLOTS);
+  __shared__ uint32_t lo_s;
   for (int i = threadIdx.x; i < PSTEN_ENTRIES; i += blockDim.x) ps[i] = psten[i];
-  BlockAccum<T> acc{akey, aval};
+  WindowAccum<T, acc_window<T>()> acc{aval, &lo_s};
+  acc.init();
   for (size_t base = (size_t)blockIdx.x * blockDim.x; base < E; base += (size_t)gridDim.x * blockDim.x) {
-    acc.clear();
-    __syncthreads();
     const size_t e = base + threadIdx.x;
+    uint32_t id[8];
+    uint32_t my_min = 0xffffffffu;
+    if (e < E) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        id[k] = conn[(size_t)k * E + e];
+        my_min = min(my_min, id[k]);
+      }
+    }
+    acc.set_lo(my_min);
     if (e < E) {
       const uint32_t me = meta[e];
       const unsigned l = me & 255u, c = (me >> 8) & 7u, t = me >> 24;
-      uint32_t id[8];
-      T xv[8], yv[8];
-#pragma unroll
-      for (int k = 0; k < 8; k++) id[k] = conn[(size_t)k * E + e];
+      T xv[8];
 #pragma unroll
       for (int k = 0; k < 8; k++) xv[k] = x[id[k]];
       // h = 2^-l (element side in the unit cube)
       const T h = (T)1 / (T)(1ull << l);
-      apply_packed<T>(ps + (c * 18 + t) * PSTEN_PER_TYPE, lapf * h * (T)0.5, massf * h * h * h * (T)0.125, xv, yv);
-#pragma unroll
-      for (int k = 0; k < 8; k++) acc.add(id[k], yv[k], y);
+      apply_packed_emit<T>(ps + (c * 18 + t) * PSTEN_PER_TYPE, lapf * h * (T)0.5, massf * h * h * h * (T)0.125, xv,
+                           [&](int k, T yk) { acc.add(id[k], yk, y); });
     }
     __syncthreads();
-    acc.flush(y);
+    acc.flush(y, n_node);
     __syncthreads();
   }
 }
@@ -385,7 +390,7 @@ void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, 
   ensure_stencils(ctx);
   cudaStream_t s = ctx.stream;
   DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
-  const size_t smem = PSTEN_ENTRIES * sizeof(T) + ACC_SLOTS * (sizeof(T) + sizeof(uint32_t));
+  const size_t smem = PSTEN_ENTRIES * sizeof(T) + acc_window<T>() * sizeof(T);
   static std::once_flag once;
   std::call_once(once, [&]() {
     DG_CUDA(cudaFuncSetAttribute(k_matvec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -399,7 +404,8 @@ void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, 
                                                   : reinterpret_cast<const T *>(ctx.d_psten32);
   {
     ProfScope _prof(ctx, "matvec", (double)m.n_elem * 36 + (double)m.n_node * 3 * sizeof(T));
-    k_matvec<T><<<grid, block, smem, s>>>(m.meta, m.conn, m.n_elem, psten, x, y, (T)lap_fac, (T)mass_fac);
+    k_matvec<T><<<grid, block, smem, s>>>(m.meta, m.conn, m.n_elem, psten, x, y, m.n_node, (T)lap_fac,
+                                          (T)mass_fac);
     DG_LAUNCH_CHECK();
   }
 }

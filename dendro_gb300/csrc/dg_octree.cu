@@ -922,6 +922,33 @@ void coarsen_octree(Context &ctx, const Octree &in, Octree &out) {
 }
 
 // ------------------------------------------------------------------------
+// one cloud of a batch as its own octree (cloud bits cleared)
+// ------------------------------------------------------------------------
+__global__ void k_strip_cloud(const Key128 *__restrict__ in, size_t n, unsigned D, Key128 *__restrict__ out) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = make_tagged(morton_part(in[i], D), tag_level(in[i]));
+}
+
+void octree_extract(Context &ctx, const Octree &in, size_t seg, Octree &out) {
+  if (seg >= in.nseg) fail(DG_ERR_INVALID_ARG, "octree: cloud index out of range");
+  uint64_t off[2] = {0, in.n};
+  if (in.nseg > 1)
+    DG_CUDA(cudaMemcpyAsync(off, in.seg_off + seg, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
+  DG_CUDA(cudaStreamSynchronize(ctx.stream));
+  const size_t n = off[1] - off[0];
+  out = Octree();
+  out.max_depth = in.max_depth;
+  out.n = n;
+  DBuf<Key128> k(n ? n : 1, ctx.stream);
+  if (n) {
+    ProfScope _prof(ctx, "strip_cloud", (double)n * 32);
+    k_strip_cloud<<<grid_for(n, 256), 256, 0, ctx.stream>>>(in.keys + off[0], n, in.max_depth, k.get());
+    DG_LAUNCH_CHECK();
+  }
+  out.keys = k.release_ptr();
+}
+
+// ------------------------------------------------------------------------
 // conversions
 // ------------------------------------------------------------------------
 // (a single cloud may hold octants just outside its domain: the reference's

@@ -57,6 +57,9 @@ size_t sort_points(Context &ctx, const double *d_xyz, size_t n, const double gle
 // ot::balanceOctree(incCorner = 1) (src/balance.cpp:31).
 void balance_octree(Context &ctx, const Octree &in, Octree &out);
 
+// cloud `seg` of a batched octree as a single-cloud octree
+void octree_extract(Context &ctx, const Octree &in, size_t seg, Octree &out);
+
 // ot::coarsenOctree (src/coarsen.cpp:53), one cloud.
 void coarsen_octree(Context &ctx, const Octree &in, Octree &out);
 

@@ -87,6 +87,8 @@ int dg_points_to_octree_batch(dg_ctx ctx, const double *xyz, size_t n, const uin
                               int xyz_on_device, dg_octree *out);
 /* offsets: host array of nseg + 1 entries (may be NULL to query nseg) */
 int dg_octree_segments(dg_ctx ctx, dg_octree o, size_t *nseg, uint64_t *offsets);
+/* cloud `seg` of a batch as its own octree handle (device copy) */
+int dg_octree_extract(dg_ctx ctx, dg_octree o, size_t seg, dg_octree *out);
 
 /* ---- par::sampleSort + par::removeDuplicates of point octants -------------
  * include/parUtils.h:424,437 (1-rank branch parUtils.tcc:1868-1875): the
