@@ -68,6 +68,7 @@ def _declare(L):
         "dg_octree_segments": ([P, P, ctypes.POINTER(SZ), P], I),
         "dg_octree_extract": ([P, P, SZ, PP], I),
         "dg_sort_unique_points": ([P, P, SZ, P, U, I, P, I, ctypes.POINTER(SZ)], I),
+        "dg_sort_unique_points_noalloc": ([P, SZ, P, U, P, ctypes.POINTER(SZ), P], I),
         "dg_balance_octree": ([P, P, I, I, PP], I),
         "dg_coarsen_octree": ([P, P, PP], I),
         "dg_octree_size": ([P, ctypes.POINTER(SZ), ctypes.POINTER(U)], I),

@@ -93,6 +93,7 @@ const char *dg_status_string(int s) {
     case DG_ERR_INTERNAL: return "internal error";
     case DG_ERR_COMM_SIZE: return "communicator size must be 1";
     case DG_ERR_UNSUPPORTED: return "unsupported option";
+    case DG_ERR_CAPACITY: return "input larger than the fixed capacity of a no-allocation entry point";
     default: return "unknown status";
   }
 }

@@ -45,6 +45,7 @@ extern "C" {
 #define DG_ERR_INTERNAL 7
 #define DG_ERR_COMM_SIZE 8
 #define DG_ERR_UNSUPPORTED 9
+#define DG_ERR_CAPACITY 10 /* input larger than a fixed-capacity entry point accepts */
 
 typedef struct dg_ctx_s *dg_ctx;
 typedef struct dg_octree_s *dg_octree;
@@ -97,6 +98,31 @@ int dg_octree_extract(dg_ctx ctx, dg_octree o, size_t seg, dg_octree *out);
  * count to *n_unique. */
 int dg_sort_unique_points(dg_ctx ctx, const double *xyz, size_t n, const double gLens[3], unsigned maxDepth,
                           int xyz_on_device, uint32_t *out_xyzl, int out_on_device, size_t *n_unique);
+
+/* ---- sort + unique of points, allocating nothing --------------------------
+ * No counterpart in the reference.  dg_sort_unique_points for callers that
+ * must not allocate device memory during the call: a process whose device
+ * memory is wholly reserved by another allocator (a framework's caching
+ * allocator, or a fixed pool sized at start-up), and steady-state loops that
+ * may not call cudaMalloc / cudaFree because those can synchronise the whole
+ * device.  Same inputs, same results bit for bit.  Differences:
+ *   - xyz and out_xyzl are device (or managed) memory of the current device,
+ *     xyz 8-byte and out_xyzl 16-byte aligned (DG_ERR_INVALID_ARG otherwise,
+ *     checked before any work);
+ *   - n <= DG_NOALLOC_MAX_POINTS, else DG_ERR_CAPACITY before any work;
+ *   - all scratch (about 41 MB) is one static device array of the library,
+ *     set up on the first call on each device (cudaGetSymbolAddress with
+ *     that device current): make that first call before any stream capture
+ *     begins;
+ *   - the work runs on cuda_stream (a cudaStream_t of the current device;
+ *     NULL: the legacy default stream), which the call synchronises before
+ *     it returns;
+ *   - the scratch is shared by every call on one device: calls that overlap
+ *     in time there (two host threads, or two streams) race, and the caller
+ *     must serialise them. */
+#define DG_NOALLOC_MAX_POINTS ((size_t)1 << 20)
+int dg_sort_unique_points_noalloc(const double *xyz, size_t n, const double gLens[3], unsigned maxDepth,
+                                  uint32_t *out_xyzl, size_t *n_unique, void *cuda_stream);
 
 /* ---- ot::balanceOctree(incCorner = true) ----------------------------------
  * include/octUtils.h:692 / src/balance.cpp:31 (1-rank branch :54-63).  The
