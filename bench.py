@@ -178,6 +178,12 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _top_kernels(stats: dict, k: int = 10) -> dict:
+    """{kernel: [total ms, launches]} of the k kernels with the most time."""
+    top = sorted(stats.items(), key=lambda kv: -kv[1][0])[:k]
+    return {name: [round(v[0], 3), int(v[1])] for name, v in top}
+
+
 def run_poisson(dg, datagen, ctx, local, args):
     """-lap(u) + u = f, u = 0 on the cube boundary, on the balanced octree of
     16e6 N(0.5, 0.15^2) points (seed 3), f = 4 Gaussian bumps (seed 3), load
@@ -215,6 +221,10 @@ def run_poisson(dg, datagen, ctx, local, args):
             its.append(it)
             rrs.append(rr)
         out[f"fp{prec}_vcycle"] = {"solve_ms": min(times), "iterations": its[0], "relres_fp64": max(rrs)}
+        ctx.profile(True)  # one more solve, timed per kernel
+        mg.solve(b, precision=prec, rtol=1e-8, maxit=200)
+        out[f"fp{prec}_vcycle"]["kernels_ms"] = _top_kernels(ctx.profile_stats())
+        ctx.profile(False)
     out["speedup_fp32_vs_fp64"] = out["fp64_vcycle"]["solve_ms"] / out["fp32_vcycle"]["solve_ms"]
     mg.free()
     return out
@@ -326,6 +336,10 @@ def run_ours(args):
         t0 = time.perf_counter()
         da = dg.DA(bal)
         da_ms = 1e3 * (time.perf_counter() - t0)
+        ctx.profile(True)  # a second build, timed per kernel
+        dg.DA(bal).free()
+        da_kernels = _top_kernels(ctx.profile_stats())
+        ctx.profile(False)
         bal.free()
         V, E = da.n_node, da.n_elem
         ctx.profile(True)
@@ -345,7 +359,7 @@ def run_ours(args):
             mv[f"fp{prec}"] = {"ms": kms, "GB/s": nbytes / (kms * 1e-3) / 1e9, "algorithmic_bytes": nbytes}
         ctx.profile(False)
         da.free()
-        extra = {"da_build_ms": da_ms, "n_elem": E, "n_node": V, "matvec": mv}
+        extra = {"da_build_ms": da_ms, "da_kernels_ms": da_kernels, "n_elem": E, "n_node": V, "matvec": mv}
 
     # ---- precision workload: FP32-MG vs FP64 solve to 1e-8 ----------------
     if not args.skip_mg:

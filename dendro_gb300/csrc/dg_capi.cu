@@ -138,8 +138,9 @@ int dg_ctx_destroy(dg_ctx ctx) {
   if (ctx->c.h_scratch) cudaFreeHost(ctx->c.h_scratch);
   if (ctx->c.d_sten64) cudaFree(ctx->c.d_sten64);
   if (ctx->c.d_sten32) cudaFree(ctx->c.d_sten32);
-  if (ctx->c.d_psten64) cudaFree(ctx->c.d_psten64);
-  if (ctx->c.d_psten32) cudaFree(ctx->c.d_psten32);
+  if (ctx->c.d_csten64) cudaFree(ctx->c.d_csten64);
+  if (ctx->c.d_csten32) cudaFree(ctx->c.d_csten32);
+  if (ctx->c.d_cperm) cudaFree(ctx->c.d_cperm);
   if (ctx->c.d_etype_of) cudaFree(ctx->c.d_etype_of);
   if (ctx->c.d_etype_mask) cudaFree(ctx->c.d_etype_mask);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);

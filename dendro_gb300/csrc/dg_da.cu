@@ -21,6 +21,7 @@
 #include "dg_da.cuh"
 #include "dg_elem.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -135,27 +136,62 @@ void ensure_stencils(Context &ctx) {
   DG_CUDA(cudaMemcpy(d32, s32.data(), STEN_ENTRIES * sizeof(float), cudaMemcpyHostToDevice));
   DG_CUDA(cudaMemcpy(det, etype_of, sizeof(etype_of), cudaMemcpyHostToDevice));
   DG_CUDA(cudaMemcpy(dem, masks, sizeof(masks), cudaMemcpyHostToDevice));
-  std::vector<double> p64(PSTEN_ENTRIES);
-  std::vector<float> p32(PSTEN_ENTRIES);
-  for (int ct = 0; ct < 8 * 18; ct++)
-    for (int k = 0; k < 8; k++)
-      for (int j = 0; j <= k; j++) {
-        p64[ct * PSTEN_PER_TYPE + tri_index(k, j)] = lap[ct * 64 + 8 * k + j];
-        p64[ct * PSTEN_PER_TYPE + 36 + tri_index(k, j)] = mass[ct * 64 + 8 * k + j];
-      }
-  for (int i = 0; i < PSTEN_ENTRIES; i++) p32[i] = (float)p64[i];
-  double *dp64 = nullptr;
-  float *dp32 = nullptr;
-  DG_CUDA(cudaMalloc((void **)&dp64, PSTEN_ENTRIES * sizeof(double)));
-  DG_CUDA(cudaMalloc((void **)&dp32, PSTEN_ENTRIES * sizeof(float)));
-  DG_CUDA(cudaMemcpy(dp64, p64.data(), PSTEN_ENTRIES * sizeof(double), cudaMemcpyHostToDevice));
-  DG_CUDA(cudaMemcpy(dp32, p32.data(), PSTEN_ENTRIES * sizeof(float), cudaMemcpyHostToDevice));
-  ctx.d_psten64 = dp64;
-  ctx.d_psten32 = dp32;
   ctx.d_sten64 = d64;
   ctx.d_sten32 = d32;
   ctx.d_etype_of = det;
   ctx.d_etype_mask = dem;
+  // canonical stencils: S(c,t) = S(0,t) relabelled by a cube symmetry
+  std::vector<double> c64(fsten_entries<double>(), 0.0);
+  std::vector<float> c32(fsten_entries<float>(), 0.0f);
+  std::vector<uint32_t> cperm(8 * 18);
+  for (int t = 0; t < 18; t++)
+    for (int q = 0; q < 64; q++) {
+      c64[t * fsten_stride<double>() + q] = lap[t * 64 + q];
+      c64[t * fsten_stride<double>() + 64 + q] = mass[t * 64 + q];
+      c32[t * fsten_stride<float>() + q] = (float)lap[t * 64 + q];
+      c32[t * fsten_stride<float>() + 64 + q] = (float)mass[t * 64 + q];
+    }
+  static const int axes[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  for (int c = 0; c < 8; c++)
+    for (int t = 0; t < 18; t++) {
+      double best = 1e300;
+      uint32_t best_sig = 0;
+      for (int a = 0; a < 6; a++)
+        for (int fl = 0; fl < 8; fl++) {
+          int pk[8];
+          for (int k = 0; k < 8; k++) {
+            int nb = 0;
+            for (int i = 0; i < 3; i++) nb |= (((k >> axes[a][i]) & 1) ^ ((fl >> i) & 1)) << i;
+            pk[k] = nb;
+          }
+          double err = 0;
+          const int ct = c * 18 + t;
+          for (int k = 0; k < 8; k++)
+            for (int j = 0; j < 8; j++) {
+              err = std::max(err, std::fabs(lap[t * 64 + 8 * pk[k] + pk[j]] - lap[ct * 64 + 8 * k + j]));
+              err = std::max(err, std::fabs(mass[t * 64 + 8 * pk[k] + pk[j]] - mass[ct * 64 + 8 * k + j]));
+            }
+          if (err < best) {
+            best = err;
+            best_sig = 0;
+            for (int k = 0; k < 8; k++) best_sig |= (uint32_t)k << (3 * pk[k]);  // slot of relabelled vertex pk[k]
+          }
+        }
+      if (!(best <= 1e-12)) fail(DG_ERR_INTERNAL, "stencil tables: a (child, type) stencil has no canonical form");
+      cperm[c * 18 + t] = best_sig;
+    }
+  double *dc64 = nullptr;
+  float *dc32 = nullptr;
+  uint32_t *dcp = nullptr;
+  DG_CUDA(cudaMalloc((void **)&dc64, c64.size() * sizeof(double)));
+  DG_CUDA(cudaMalloc((void **)&dc32, c32.size() * sizeof(float)));
+  DG_CUDA(cudaMalloc((void **)&dcp, cperm.size() * sizeof(uint32_t)));
+  DG_CUDA(cudaMemcpy(dc64, c64.data(), c64.size() * sizeof(double), cudaMemcpyHostToDevice));
+  DG_CUDA(cudaMemcpy(dc32, c32.data(), c32.size() * sizeof(float), cudaMemcpyHostToDevice));
+  DG_CUDA(cudaMemcpy(dcp, cperm.data(), cperm.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  ctx.d_csten64 = dc64;
+  ctx.d_csten32 = dc32;
+  ctx.d_cperm = dcp;
 }
 
 // ------------------------------------------------------------------------
@@ -298,6 +334,160 @@ __global__ void k_mesh_conn(const Key128 *__restrict__ keys, size_t n, unsigned 
   }
 }
 
+// ------------------------------------------------------------------------
+// element loop tables: per patch, the (element, vertex) pairs sorted by node
+// ------------------------------------------------------------------------
+__global__ void k_node_incidence(const uint32_t *__restrict__ conn, size_t n8, uint32_t *__restrict__ cnt) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += stride) atomicAdd(&cnt[conn[i]], 1u);
+}
+
+// one block per patch: the patch's elements ordered by (type, level, index),
+// then a bitonic sort of its (node << 12 | slot) keys in shared memory, run
+// starts, run lengths against the node's mesh-wide pair count, and the
+// packed entries
+template <typename K>
+__device__ __forceinline__ void block_bitonic(K *a, int n) {
+  for (int size = 2; size <= n; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < n / 2; i += blockDim.x) {
+        const int lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
+        const bool asc = (lo & size) == 0;
+        const K x = a[lo], y = a[hi];
+        if ((x > y) == asc) {
+          a[lo] = y;
+          a[hi] = x;
+        }
+      }
+      __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict__ conn,
+                                                      const uint32_t *__restrict__ meta, size_t E,
+                                                      const uint32_t *__restrict__ node_pairs,
+                                                      uint16_t *__restrict__ pinc, uint16_t *__restrict__ pexc,
+                                                      uint32_t *__restrict__ pmeta, uint32_t *__restrict__ run_node,
+                                                      uint32_t *__restrict__ n_run) {
+  __shared__ uint64_t sk[PATCH_ENT];
+  __shared__ uint16_t runpos[PATCH_ENT + 1];
+  __shared__ uint32_t ek[PATCH];
+  __shared__ uint16_t rank[PATCH];
+  const int tid = threadIdx.x;
+  const size_t p = blockIdx.x;
+  const size_t e0 = p * PATCH;
+  const int ne = (int)((E - e0) < (size_t)PATCH ? (E - e0) : (size_t)PATCH);
+  // element order: (type, level, index); missing elements last
+  uint32_t me = 0;
+  if (tid < ne) {
+    me = meta[e0 + tid];
+    ek[tid] = ((me >> 24) << 5 | (me & 31u)) << 9 | (uint32_t)tid;
+  } else {
+    ek[tid] = 0xffffffffu;
+  }
+  __syncthreads();
+  block_bitonic<uint32_t>(ek, PATCH);
+  if (tid < ne) {
+    const uint32_t eo = ek[tid] & (PATCH - 1);
+    rank[eo] = (uint16_t)tid;
+    pmeta[p * PATCH + tid] = meta[e0 + eo];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const int i = k * PATCH + (tid < ne ? rank[tid] : tid);
+    sk[k * PATCH + tid] = tid < ne ? ((uint64_t)conn[(size_t)k * E + e0 + tid] << 12 | (uint64_t)i) : ~0ull;
+  }
+  __syncthreads();
+  block_bitonic<uint64_t>(sk, PATCH_ENT);
+  const int nent = 8 * ne;
+  uint32_t id[8];
+  bool st[8];
+  int nst = 0;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const int i = 8 * tid + j;
+    id[j] = (uint32_t)(sk[i] >> 12);
+    st[j] = i < nent && (i == 0 || (uint32_t)(sk[i - 1] >> 12) != id[j]);
+    nst += st[j];
+  }
+  int total;
+  const int ex = block_excl_scan<int, PATCH>(nst, total);
+  pexc[p * PATCH + tid] = (uint16_t)ex;
+  int u = ex - 1;
+#pragma unroll
+  for (int j = 0; j < 8; j++)
+    if (st[j]) {
+      u++;
+      runpos[u] = (uint16_t)(8 * tid + j);
+      run_node[p * PATCH_ENT + u] = id[j];
+    }
+  if (tid == 0) {
+    runpos[total] = (uint16_t)nent;
+    n_run[p] = (uint32_t)total;
+  }
+  __syncthreads();
+  u = ex - 1;
+  uint32_t e[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const int i = 8 * tid + j;
+    e[j] = 0;
+    if (i < nent) {
+      if (st[j]) u++;
+      const uint32_t len = (uint32_t)runpos[u + 1] - (uint32_t)runpos[u];
+      e[j] = (uint32_t)(sk[i] & ENT_SLOT) | (st[j] ? ENT_START : 0u) | (len == node_pairs[id[j]] ? ENT_COMPLETE : 0u);
+    }
+  }
+  reinterpret_cast<uint4 *>(pinc + p * PATCH_ENT)[tid] =
+      make_uint4(e[0] | e[1] << 16, e[2] | e[3] << 16, e[4] | e[5] << 16, e[6] | e[7] << 16);
+}
+
+__global__ void k_patch_nodes(const uint32_t *__restrict__ run_node, const uint32_t *__restrict__ n_run,
+                              const uint64_t *__restrict__ poff, uint32_t *__restrict__ pnode) {
+  const size_t p = blockIdx.x;
+  const uint32_t nr = n_run[p];
+  for (uint32_t i = threadIdx.x; i < nr; i += blockDim.x) pnode[poff[p] + i] = run_node[p * PATCH_ENT + i];
+}
+
+static void mesh_patches(Context &ctx, Mesh &m) {
+  cudaStream_t s = ctx.stream;
+  const size_t n = m.n_elem, np = (n + PATCH - 1) / PATCH;
+  if (m.n_node >= (size_t)RUN_BDY) fail(DG_ERR_INVALID_ARG, "DA: too many nodes for the element loop tables");
+  DBuf<uint32_t> pairs(m.n_node, s), run_node(np * PATCH_ENT, s), n_run(np, s);
+  DBuf<uint16_t> pinc(np * PATCH_ENT, s), pexc(np * PATCH, s);
+  DBuf<uint32_t> pmeta(np * PATCH, s);
+  DBuf<uint64_t> poff(np + 1, s);
+  DG_CUDA(cudaMemsetAsync(pairs.get(), 0, m.n_node * sizeof(uint32_t), s));
+  {
+    ProfScope _prof(ctx, "da_node_pairs", (double)n * 8 * 8);
+    k_node_incidence<<<grid_for(8 * n, 256, (unsigned)ctx.num_sms * 16), 256, 0, s>>>(m.conn, 8 * n, pairs.get());
+    DG_LAUNCH_CHECK();
+  }
+  {
+    ProfScope _prof(ctx, "da_patch_sort", (double)n * 8 * 14);
+    k_patch_sort<<<(unsigned)np, PATCH, 0, s>>>(m.conn, m.meta, n, pairs.get(), pinc.get(), pexc.get(),
+                                                pmeta.get(), run_node.get(), n_run.get());
+    DG_LAUNCH_CHECK();
+  }
+  exclusive_scan<uint32_t, uint64_t>(n_run.get(), poff.get(), np, poff.get() + np, s);
+  uint64_t nruns = 0;
+  DG_CUDA(cudaMemcpyAsync(&nruns, poff.get() + np, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  DG_CUDA(cudaStreamSynchronize(s));
+  DBuf<uint32_t> pnode(nruns ? nruns : 1, s);
+  {
+    ProfScope _prof(ctx, "da_patch_nodes", (double)nruns * 8);
+    k_patch_nodes<<<(unsigned)np, 256, 0, s>>>(run_node.get(), n_run.get(), poff.get(), pnode.get());
+    DG_LAUNCH_CHECK();
+  }
+  m.n_patch = np;
+  m.pinc = pinc.release_ptr();
+  m.pexc = pexc.release_ptr();
+  m.pmeta = pmeta.release_ptr();
+  m.pnode = pnode.release_ptr();
+  m.poff = poff.release_ptr();
+}
+
 void mesh_build(Context &ctx, const Octree &bal, Mesh &m) {
   cudaStream_t s = ctx.stream;
   const size_t n = bal.n;
@@ -333,12 +523,18 @@ void mesh_build(Context &ctx, const Octree &bal, Mesh &m) {
   m.meta = meta.release_ptr();
   m.conn = conn.release_ptr();
   m.node_xyz = nxyz.release_ptr();
+  mesh_patches(ctx, m);
 }
 
 void mesh_free(Context &ctx, Mesh &m) {
   if (m.meta) cudaFreeAsync(m.meta, ctx.stream);
   if (m.conn) cudaFreeAsync(m.conn, ctx.stream);
   if (m.node_xyz) cudaFreeAsync(m.node_xyz, ctx.stream);
+  if (m.pinc) cudaFreeAsync(m.pinc, ctx.stream);
+  if (m.pexc) cudaFreeAsync(m.pexc, ctx.stream);
+  if (m.pmeta) cudaFreeAsync(m.pmeta, ctx.stream);
+  if (m.pnode) cudaFreeAsync(m.pnode, ctx.stream);
+  if (m.poff) cudaFreeAsync(m.poff, ctx.stream);
   m = Mesh();
 }
 
@@ -346,66 +542,26 @@ void mesh_free(Context &ctx, Mesh &m) {
 // element loop
 // ------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(512, 2) k_matvec(const uint32_t *__restrict__ meta, const uint32_t *__restrict__ conn,
-                                                size_t E, const T *__restrict__ psten, const T *__restrict__ x,
-                                                T *__restrict__ y, size_t n_node, T lapf, T massf) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *ps = reinterpret_cast<T *>(smem_raw);
-  T *aval = ps + PSTEN_ENTRIES;
-  __shared__ uint32_t lo_s;
-  for (int i = threadIdx.x; i < PSTEN_ENTRIES; i += blockDim.x) ps[i] = psten[i];
-  WindowAccum<T, acc_window<T>()> acc{aval, &lo_s};
-  acc.init();
-  for (size_t base = (size_t)blockIdx.x * blockDim.x; base < E; base += (size_t)gridDim.x * blockDim.x) {
-    const size_t e = base + threadIdx.x;
-    uint32_t id[8];
-    uint32_t my_min = 0xffffffffu;
-    if (e < E) {
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        id[k] = conn[(size_t)k * E + e];
-        my_min = min(my_min, id[k]);
-      }
-    }
-    acc.set_lo(my_min);
-    if (e < E) {
-      const uint32_t me = meta[e];
-      const unsigned l = me & 255u, c = (me >> 8) & 7u, t = me >> 24;
-      T xv[8];
-#pragma unroll
-      for (int k = 0; k < 8; k++) xv[k] = x[id[k]];
-      // h = 2^-l (element side in the unit cube)
-      const T h = (T)1 / (T)(1ull << l);
-      apply_packed_emit<T>(ps + (c * 18 + t) * PSTEN_PER_TYPE, lapf * h * (T)0.5, massf * h * h * h * (T)0.125, xv,
-                           [&](int k, T yk) { acc.add(id[k], yk, y); });
-    }
-    __syncthreads();
-    acc.flush(y, n_node);
-    __syncthreads();
-  }
-}
-
-template <typename T>
 void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, double mass_fac) {
   ensure_stencils(ctx);
   cudaStream_t s = ctx.stream;
   DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
-  const size_t smem = PSTEN_ENTRIES * sizeof(T) + acc_window<T>() * sizeof(T);
+  const size_t smem = patch_smem<T>();
   static std::once_flag once;
   std::call_once(once, [&]() {
-    DG_CUDA(cudaFuncSetAttribute(k_matvec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    DG_CUDA(cudaFuncSetAttribute(k_patch_matvec<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   });
-  const int block = 512;
   int per_sm = 1;
-  DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_matvec<T>, block, smem));
+  DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_patch_matvec<T, false>, PATCH, smem));
   if (per_sm < 1) per_sm = 1;
-  unsigned grid = grid_for(m.n_elem, block, (unsigned)(per_sm * ctx.num_sms));
-  const T *psten = std::is_same<T, double>::value ? reinterpret_cast<const T *>(ctx.d_psten64)
-                                                  : reinterpret_cast<const T *>(ctx.d_psten32);
+  const unsigned grid = (unsigned)std::min<size_t>(m.n_patch, (size_t)per_sm * ctx.num_sms);
+  const T *cs = std::is_same<T, double>::value ? reinterpret_cast<const T *>(ctx.d_csten64)
+                                               : reinterpret_cast<const T *>(ctx.d_csten32);
   {
     ProfScope _prof(ctx, "matvec", (double)m.n_elem * 36 + (double)m.n_node * 3 * sizeof(T));
-    k_matvec<T><<<grid, block, smem, s>>>(m.meta, m.conn, m.n_elem, psten, x, y, m.n_node, (T)lap_fac,
-                                          (T)mass_fac);
+    k_patch_matvec<T, false><<<grid, PATCH, smem, s>>>(m.pmeta, m.pinc, m.pexc, m.pnode, m.poff, m.n_elem,
+                                                       m.n_patch, cs, ctx.d_cperm, nullptr, x, y, (T)lap_fac,
+                                                       (T)mass_fac);
     DG_LAUNCH_CHECK();
   }
 }

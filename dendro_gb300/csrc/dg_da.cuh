@@ -21,6 +21,13 @@ struct Mesh {
   uint32_t *meta = nullptr;
   uint32_t *conn = nullptr;      // 8 * n_elem, vertex-major
   uint32_t *node_xyz = nullptr;  // 3 * n_node, coordinate-major
+  // element loop tables (dg_elem.cuh): n_patch patches of PATCH elements
+  size_t n_patch = 0;
+  uint16_t *pinc = nullptr;   // PATCH_ENT per patch, node-sorted pairs
+  uint16_t *pexc = nullptr;   // PATCH per patch: runs starting before pair 8t
+  uint32_t *pmeta = nullptr;  // PATCH per patch: meta in the patch's element order
+  uint32_t *pnode = nullptr;  // node of each run, patch after patch
+  uint64_t *poff = nullptr;   // n_patch + 1 run offsets into pnode
 };
 
 void mesh_build(Context &ctx, const Octree &bal, Mesh &m);

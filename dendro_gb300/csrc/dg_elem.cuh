@@ -1,98 +1,288 @@
 // Element-loop building blocks shared by the matVec kernels.
 //
-// Packed stencils: every type-2 stencil is symmetric, so a (child, type)
-// pair keeps 36 Laplacian + 36 mass entries (lower triangle, row-major:
-// entry (k, j), k >= j, at k(k+1)/2 + j).  All 144 pairs fit in shared
-// memory in FP64 (83 KB) and FP32 (41 KB).
+// Canonical stencils: every (child, type) stencil is a relabelling of the
+// child-0 stencil of the same type by one of the 48 symmetries of the cube,
+// S(c,t)[k][j] = S(0,t)[p[k]][p[j]] (equal to rounding), so 18 full 8x8
+// Laplacian + mass stencils (18 KB in FP64, 9 KB in FP32) and one 8-entry
+// relabelling per (child, type) stand for all 144.  Full rows load as
+// 16-byte vectors; the elements of a patch are ordered by (type, level), so
+// the threads of a warp mostly read the same stencil (a broadcast).
 //
-// Block accumulation: the elements of a block are consecutive in Morton
-// order, and node ids follow the element order of their owners, so the
-// nodes a block touches sit mostly in a short id window starting at the
-// smallest id the block touches.  Contributions inside the window are summed
-// with shared-memory atomics, the window is flushed with one global atomic
-// per touched node, and the few contributions outside it go to global
-// memory directly.
+// Patches: PATCH consecutive elements form a patch.  Its incidence table
+// lists the 8 x PATCH (element, vertex) pairs sorted by node id, 16 bits
+// each:
+//   bits 0..11  slot = vertex * PATCH + element within the patch
+//   bit 12      first pair of a node's run
+//   bit 13      the run holds every pair of its node in the whole mesh, so
+//               the node's sum is complete in this patch (stored, not added)
+// pnode[poff[p] + u] is the node of run u of patch p, pexc[p][t] the number
+// of runs that start before pair 8t, and pmeta[p][t] the meta word of the
+// patch's element t in (type, level) order (the order slots use).  An element loop over a patch
+// gathers x once per node into the slots, applies the element stencils
+// slot-to-slot in shared memory, and sums each run with a segmented scan:
+// no shared-memory atomics, and global atomics only for nodes that other
+// patches also touch.
 #pragma once
 
-#include "dg_common.cuh"
+#include "dg_prims.cuh"
 
 namespace dg {
 
-constexpr int PSTEN_PER_TYPE = 72;                   // 36 + 36
-constexpr int PSTEN_ENTRIES = 8 * 18 * PSTEN_PER_TYPE;
-
-__host__ __device__ constexpr int tri_index(int k, int j) { return k >= j ? k * (k + 1) / 2 + j : j * (j + 1) / 2 + k; }
-
-// node ids summed in shared memory per chunk: 16 KB of accumulators
+// per type: 8x8 Laplacian rows, then 8x8 mass rows, then 16 bytes of padding
+// so that the same row of two neighbouring types sits in different banks
 template <typename T>
-constexpr int acc_window() {
-  return 16384 / (int)sizeof(T);
+constexpr int fsten_stride() {
+  return 128 + 16 / (int)sizeof(T);
+}
+template <typename T>
+constexpr int fsten_entries() {
+  return 18 * fsten_stride<T>();
+}
+constexpr int PATCH = 512;
+constexpr int PATCH_ENT = 8 * PATCH;
+constexpr uint32_t ENT_SLOT = 0xfffu, ENT_START = 1u << 12, ENT_COMPLETE = 1u << 13;
+constexpr uint32_t RUN_BDY = 1u << 31;  // run node flag in shared memory (Dirichlet)
+
+// 2^-l exactly, from the exponent bits (0 <= l <= 30)
+__device__ __forceinline__ float exp2_neg(float, unsigned l) { return __int_as_float((int)(127u - l) << 23); }
+__device__ __forceinline__ double exp2_neg(double, unsigned l) {
+  return __longlong_as_double((long long)(1023u - l) << 52);
 }
 
-// window accumulator: W consecutive node ids from lo
-template <typename T, int W>
-struct WindowAccum {
-  T *val;          // W entries, zero between chunks
-  uint32_t *lo_s;  // shared word
-  __device__ __forceinline__ void init() {
-    for (int i = threadIdx.x; i < W; i += blockDim.x) val[i] = (T)0;
-  }
-  // block-wide: lo = smallest id of the chunk (call with UINT_MAX for idle threads)
-  __device__ __forceinline__ void set_lo(uint32_t my_min) {
-    if (threadIdx.x == 0) *lo_s = 0xffffffffu;
-    __syncthreads();
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) my_min = min(my_min, __shfl_xor_sync(0xffffffffu, my_min, o));
-    if ((threadIdx.x & 31) == 0) atomicMin(lo_s, my_min);
-    __syncthreads();
-  }
-  __device__ __forceinline__ void add(uint32_t id, T v, T *__restrict__ gy) {
-    const uint32_t off = id - *lo_s;
-    if (off < (uint32_t)W) atomicAdd(&val[off], v);
-    else atomicAdd(&gy[id], v);
-  }
-  // flush touched entries and zero them for the next chunk (after a barrier)
-  __device__ __forceinline__ void flush(T *__restrict__ gy, size_t n) {
-    const uint32_t lo = *lo_s;
-    for (int i = threadIdx.x; i < W; i += blockDim.x) {
-      T v = val[i];
-      if (v != (T)0) {
-        if ((size_t)lo + i < n) atomicAdd(&gy[lo + i], v);
-        val[i] = (T)0;
-      }
-    }
-  }
-};
+// two FP32 fused multiply-adds in one instruction (Blackwell f32x2)
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
 
-// y_k = sum_j (f1 L[k][j] + f2 M[k][j]) x_j for k = 0..7 from a packed stencil
-template <typename T>
-__device__ __forceinline__ void apply_packed(const T *__restrict__ P, T f1, T f2, const T (&xv)[8], T (&yv)[8]) {
+// y_k = f1 sum_j L[k][j] x_j + f2 sum_j M[k][j] x_j (full-row stencil S),
+// handing each y_k to emit(k, y_k)
+template <typename Emit>
+__device__ __forceinline__ void apply_full(const float *__restrict__ S, float f1, float f2, const float (&xv)[8],
+                                           Emit &&emit) {
+  const float2 x0 = make_float2(xv[0], xv[1]), x1 = make_float2(xv[2], xv[3]);
+  const float2 x2 = make_float2(xv[4], xv[5]), x3 = make_float2(xv[6], xv[7]);
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    T aL = 0, aM = 0;
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      aL += P[tri_index(k, j)] * xv[j];
-      aM += P[36 + tri_index(k, j)] * xv[j];
-    }
-    yv[k] = f1 * aL + f2 * aM;
+    const float4 l0 = reinterpret_cast<const float4 *>(S + 8 * k)[0];
+    const float4 l1 = reinterpret_cast<const float4 *>(S + 8 * k)[1];
+    const float4 m0 = reinterpret_cast<const float4 *>(S + 64 + 8 * k)[0];
+    const float4 m1 = reinterpret_cast<const float4 *>(S + 64 + 8 * k)[1];
+    float2 aL = ffma2(make_float2(l0.x, l0.y), x0, make_float2(0.f, 0.f));
+    aL = ffma2(make_float2(l0.z, l0.w), x1, aL);
+    aL = ffma2(make_float2(l1.x, l1.y), x2, aL);
+    aL = ffma2(make_float2(l1.z, l1.w), x3, aL);
+    float2 aM = ffma2(make_float2(m0.x, m0.y), x0, make_float2(0.f, 0.f));
+    aM = ffma2(make_float2(m0.z, m0.w), x1, aM);
+    aM = ffma2(make_float2(m1.x, m1.y), x2, aM);
+    aM = ffma2(make_float2(m1.z, m1.w), x3, aM);
+    emit(k, f1 * (aL.x + aL.y) + f2 * (aM.x + aM.y));
   }
 }
 
-// same, handing each y_k to emit(k, y_k) as soon as it is formed (keeps
-// fewer values live than a y array)
-template <typename T, typename Emit>
-__device__ __forceinline__ void apply_packed_emit(const T *__restrict__ P, T f1, T f2, const T (&xv)[8], Emit &&emit) {
+template <typename Emit>
+__device__ __forceinline__ void apply_full(const double *__restrict__ S, double f1, double f2, const double (&xv)[8],
+                                           Emit &&emit) {
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    T aL = 0, aM = 0;
+    double aL = 0, aM = 0;
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-      aL += P[tri_index(k, j)] * xv[j];
-      aM += P[36 + tri_index(k, j)] * xv[j];
+    for (int j = 0; j < 8; j += 2) {
+      const double2 l = reinterpret_cast<const double2 *>(S + 8 * k + j)[0];
+      const double2 m = reinterpret_cast<const double2 *>(S + 64 + 8 * k + j)[0];
+      aL = fma(l.x, xv[j], aL);
+      aL = fma(l.y, xv[j + 1], aL);
+      aM = fma(m.x, xv[j], aM);
+      aM = fma(m.y, xv[j + 1], aM);
     }
     emit(k, f1 * aL + f2 * aM);
   }
+}
+
+// y = (lapf K + massf M) x over the elements of every patch; with DIR the
+// Dirichlet form: boundary rows are the identity (y = x), boundary columns
+// are dropped.  One block of PATCH threads per patch, grid-strided; thread t
+// holds pairs 8t..8t+7 of the patch's table and is element t of the patch.
+// The slot buffer and the run-node array are double-buffered by patch
+// parity and the next patch's table words are loaded one patch ahead, so a
+// patch costs three barriers.
+template <typename T, bool DIR>
+__global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
+    k_patch_matvec(const uint32_t *__restrict__ pmeta, const uint16_t *__restrict__ pinc,
+                   const uint16_t *__restrict__ pexc, const uint32_t *__restrict__ pnode,
+                   const uint64_t *__restrict__ poff, size_t E, size_t n_patch, const T *__restrict__ fsten,
+                   const uint32_t *__restrict__ cperm, const uint8_t *__restrict__ bdy, const T *__restrict__ x,
+                   T *__restrict__ y, T lapf, T massf) {
+  constexpr int NW = PATCH / 32;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *cs = reinterpret_cast<T *>(smem_raw);
+  T *bufs = cs + fsten_entries<T>();
+  uint32_t *gns = reinterpret_cast<uint32_t *>(bufs + 2 * PATCH_ENT);
+  uint32_t *cp = gns + 2 * PATCH_ENT;
+  __shared__ T ws_v[2][NW];
+  __shared__ int ws_f[2][NW];
+  __shared__ int ws_first[2][NW + 1];
+  for (int i = threadIdx.x; i < fsten_entries<T>(); i += PATCH) cs[i] = fsten[i];
+  for (int i = threadIdx.x; i < 8 * 18; i += PATCH) cp[i] = cperm[i];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+
+  auto patch_ne = [&](size_t q) { return (int)((E - q * PATCH) < (size_t)PATCH ? (E - q * PATCH) : (size_t)PATCH); };
+  size_t p = blockIdx.x;
+  uint4 w = make_uint4(0, 0, 0, 0);
+  uint32_t ex = 0, me = 0;
+  uint64_t ub = 0;
+  if (p < n_patch) {
+    ub = poff[p];
+    if (tid < patch_ne(p)) {
+      w = reinterpret_cast<const uint4 *>(pinc + p * PATCH_ENT)[tid];
+      ex = pexc[p * PATCH + tid];
+      me = pmeta[p * PATCH + tid];
+    }
+  }
+  int par = 0;
+  for (; p < n_patch; p += gridDim.x, par ^= 1) {
+    const int ne = patch_ne(p);
+    const bool have = tid < ne;
+    const uint4 cw = w;
+    const uint32_t cex = ex, cme = me;
+    const uint64_t cub = ub;
+    // the next patch's table words, one patch ahead
+    const size_t pn = p + gridDim.x;
+    if (pn < n_patch) {
+      ub = poff[pn];
+      if (tid < patch_ne(pn)) {
+        w = reinterpret_cast<const uint4 *>(pinc + pn * PATCH_ENT)[tid];
+        ex = pexc[pn * PATCH + tid];
+        me = pmeta[pn * PATCH + tid];
+      }
+    }
+    auto ent = [&](int j) -> uint32_t {
+      const uint32_t word = j < 2 ? cw.x : j < 4 ? cw.y : j < 6 ? cw.z : cw.w;
+      return (j & 1) ? word >> 16 : word & 0xffffu;
+    };
+    T *buf = bufs + par * PATCH_ENT;
+    uint32_t *gn = gns + par * PATCH_ENT;
+    // 1. x of each run's node into its slots; the run's node into gn
+    if (have) {
+      int u = (int)cex - 1;
+      T xv = (T)0;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const uint32_t e = ent(j);
+        if (e & ENT_START) {
+          u++;
+          const uint32_t g = pnode[cub + u];
+          xv = x[g];
+          uint32_t tag = g;
+          if (DIR && bdy[g]) {
+            xv = (T)0;
+            tag |= RUN_BDY;
+          }
+          gn[u] = tag;
+        } else if (j == 0) {
+          xv = x[pnode[cub + u]];  // the run began in an earlier thread
+          if (DIR && bdy[pnode[cub + u]]) xv = (T)0;
+        }
+        buf[e & ENT_SLOT] = xv;
+      }
+    }
+    if (lane == 0) ws_first[par][wid] = (ent(0) & ENT_START) ? 1 : 0;
+    if (tid == 0) ws_first[par][NW] = 1;
+    __syncthreads();
+    // 2. element stencils, slot to slot (canonical stencil, relabelled slots)
+    if (have) {
+      const unsigned l = cme & 255u, c = (cme >> 8) & 7u, t = cme >> 24;
+      const uint32_t sig = cp[c * 18 + t];
+      T xv[8];
+#pragma unroll
+      for (int m = 0; m < 8; m++) xv[m] = buf[((sig >> (3 * m)) & 7u) * PATCH + tid];
+      const T h = exp2_neg((T)0, l);
+      apply_full(cs + t * fsten_stride<T>(), lapf * h * (T)0.5, massf * h * h * h * (T)0.125, xv,
+                 [&](int m, T ym) { buf[((sig >> (3 * m)) & 7u) * PATCH + tid] = ym; });
+    }
+    __syncthreads();
+    // 3. run sums: segmented scan of the threads' trailing partial sums
+    T v[8];
+    T tail = (T)0;
+    int head = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const uint32_t e = ent(j);
+      v[j] = have ? buf[e & ENT_SLOT] : (T)0;
+      if (e & ENT_START) {
+        head = 1;
+        tail = (T)0;
+      }
+      tail += v[j];
+    }
+    T s = tail;
+    int f = head;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T s2 = __shfl_up_sync(0xffffffffu, s, o);
+      const int f2 = __shfl_up_sync(0xffffffffu, f, o);
+      if (lane >= o) {
+        if (!f) s += s2;
+        f |= f2;
+      }
+    }
+    if (lane == 31) {
+      ws_v[par][wid] = s;
+      ws_f[par][wid] = f;
+    }
+    __syncthreads();
+    T wv = lane < NW ? ws_v[par][lane] : (T)0;
+    int wf = lane < NW ? ws_f[par][lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T s2 = __shfl_up_sync(0xffffffffu, wv, o);
+      const int f2 = __shfl_up_sync(0xffffffffu, wf, o);
+      if (lane >= o) {
+        if (!wf) wv += s2;
+        wf |= f2;
+      }
+    }
+    const T wpre = __shfl_sync(0xffffffffu, wv, wid > 0 ? wid - 1 : 0);
+    const T wprefix = wid > 0 ? wpre : (T)0;
+    const T ex_s = __shfl_up_sync(0xffffffffu, s, 1);
+    const int ex_f = __shfl_up_sync(0xffffffffu, f, 1);
+    const T carry = (lane == 0) ? wprefix : (ex_f ? ex_s : wprefix + ex_s);
+    const int nxt = __shfl_down_sync(0xffffffffu, (ent(0) & ENT_START) ? 1 : 0, 1);
+    if (have) {
+      const bool last_run_ends = tid + 1 >= ne || (lane < 31 ? nxt : ws_first[par][wid + 1]);
+      auto emit = [&](int u, T acc, uint32_t e) {
+        const uint32_t tag = gn[u];
+        const uint32_t g = tag & ~RUN_BDY;
+        if (DIR && (tag & RUN_BDY)) y[g] = x[g];
+        else if (e & ENT_COMPLETE) y[g] = acc;
+        else atomicAdd(&y[g], acc);
+      };
+      int u = (int)cex - 1;
+      T acc = carry;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const uint32_t e = ent(j);
+        if (e & ENT_START) {
+          if (j > 0) emit(u, acc, ent(j - 1));
+          u++;
+          acc = (T)0;
+        }
+        acc += v[j];
+      }
+      if (last_run_ends) emit(u, acc, ent(7));
+    }
+  }
+}
+
+template <typename T>
+constexpr size_t patch_smem() {
+  return fsten_entries<T>() * sizeof(T) + 2 * PATCH_ENT * sizeof(T) + 2 * PATCH_ENT * sizeof(uint32_t) +
+         8 * 18 * sizeof(uint32_t);
 }
 
 }  // namespace dg

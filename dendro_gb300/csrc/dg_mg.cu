@@ -29,74 +29,12 @@ void coarsen_octree(Context &ctx, const Octree &in, Octree &out);
 
 namespace {
 
-template <typename T>
-const T *psten_ptr(const Context &c) {
-  return std::is_same<T, double>::value ? reinterpret_cast<const T *>(c.d_psten64)
-                                        : reinterpret_cast<const T *>(c.d_psten32);
-}
-
 __global__ void k_node_bdy(const uint32_t *__restrict__ xyz, size_t V, unsigned D, uint8_t *__restrict__ bdy) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V) return;
   const uint32_t dom = 1u << D;
   uint32_t x = xyz[i], y = xyz[V + i], z = xyz[2 * V + i];
   bdy[i] = (x == 0 || y == 0 || z == 0 || x == dom || y == dom || z == dom) ? 1 : 0;
-}
-
-// DirichletJacobianMatMult (omgJac.C:958-1057): boundary rows are the
-// identity, boundary columns are skipped
-template <typename T>
-__global__ void __launch_bounds__(512, 2) k_dirichlet_matvec(const uint32_t *__restrict__ meta,
-                                                          const uint32_t *__restrict__ conn, size_t E,
-                                                          const T *__restrict__ psten,
-                                                          const uint8_t *__restrict__ bdy, const T *__restrict__ x,
-                                                          T *__restrict__ y, size_t n_node) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *ps = reinterpret_cast<T *>(smem_raw);
-  T *aval = ps + PSTEN_ENTRIES;
-  __shared__ uint32_t lo_s;
-  for (int i = threadIdx.x; i < PSTEN_ENTRIES; i += blockDim.x) ps[i] = psten[i];
-  WindowAccum<T, acc_window<T>()> acc{aval, &lo_s};
-  acc.init();
-  for (size_t base = (size_t)blockIdx.x * blockDim.x; base < E; base += (size_t)gridDim.x * blockDim.x) {
-    const size_t e = base + threadIdx.x;
-    uint32_t id[8];
-    uint32_t my_min = 0xffffffffu;
-    if (e < E) {
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        id[k] = conn[(size_t)k * E + e];
-        my_min = min(my_min, id[k]);
-      }
-    }
-    acc.set_lo(my_min);
-    if (e < E) {
-      const uint32_t me = meta[e];
-      const unsigned l = me & 255u, c = (me >> 8) & 7u, t = me >> 24;
-      T xv[8];
-      unsigned bm = 0;
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        bm |= (unsigned)bdy[id[k]] << k;
-        xv[k] = x[id[k]];
-      }
-      // boundary rows: the identity (store the input value)
-#pragma unroll
-      for (int k = 0; k < 8; k++)
-        if (bm >> k & 1) {
-          y[id[k]] = xv[k];
-          xv[k] = (T)0;  // boundary columns are skipped
-        }
-      const T h = (T)1 / (T)(1ull << l);
-      apply_packed_emit<T>(ps + (c * 18 + t) * PSTEN_PER_TYPE, h * (T)0.5, h * h * h * (T)0.125, xv,
-                           [&](int k, T yk) {
-                             if (!(bm >> k & 1)) acc.add(id[k], yk, y);
-                           });
-    }
-    __syncthreads();
-    acc.flush(y, n_node);
-    __syncthreads();
-  }
 }
 
 // DirichletJacobianMatGetDiagonal: interior diagonal, 1 on the boundary
@@ -361,23 +299,27 @@ __global__ void k_cg_p(double *__restrict__ p, const double *__restrict__ z, con
 }  // namespace
 
 // ------------------------------------------------------------------------
+// DirichletJacobianMatMult (omgJac.C:958-1057): boundary rows are the
+// identity, boundary columns are skipped (the patch element loop with DIR)
 template <typename T>
 void dirichlet_matvec(Context &ctx, const MGLevel &L, const T *x, T *y) {
   ensure_stencils(ctx);
   cudaStream_t s = ctx.stream;
   const Mesh &m = L.mesh;
   DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
-  const size_t smem = PSTEN_ENTRIES * sizeof(T) + acc_window<T>() * sizeof(T);
+  const size_t smem = patch_smem<T>();
   static std::once_flag once;
   std::call_once(once, [&]() {
-    DG_CUDA(cudaFuncSetAttribute(k_dirichlet_matvec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    DG_CUDA(cudaFuncSetAttribute(k_patch_matvec<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   });
   int per_sm = 1;
-  DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dirichlet_matvec<T>, 512, smem));
-  unsigned grid = grid_for(m.n_elem, 512, (unsigned)(std::max(per_sm, 1) * ctx.num_sms));
+  DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_patch_matvec<T, true>, PATCH, smem));
+  const unsigned grid = (unsigned)std::min<size_t>(m.n_patch, (size_t)std::max(per_sm, 1) * ctx.num_sms);
+  const T *cs = std::is_same<T, double>::value ? reinterpret_cast<const T *>(ctx.d_csten64)
+                                               : reinterpret_cast<const T *>(ctx.d_csten32);
   ProfScope _prof(ctx, "dirichlet_matvec", (double)m.n_elem * 36 + (double)m.n_node * (3 * sizeof(T) + 1));
-  k_dirichlet_matvec<T><<<grid, 512, smem, s>>>(m.meta, m.conn, m.n_elem, psten_ptr<T>(ctx), L.bdy, x, y,
-                                                  m.n_node);
+  k_patch_matvec<T, true><<<grid, PATCH, smem, s>>>(m.pmeta, m.pinc, m.pexc, m.pnode, m.poff, m.n_elem, m.n_patch,
+                                                    cs, ctx.d_cperm, L.bdy, x, y, (T)1, (T)1);
   DG_LAUNCH_CHECK();
 }
 

@@ -44,8 +44,9 @@ struct Context {
   float *d_sten32 = nullptr;
   uint8_t *d_etype_of = nullptr;   // [8][256] -> element type or 255
   uint8_t *d_etype_mask = nullptr; // [8][18] -> hanging mask
-  double *d_psten64 = nullptr;     // packed symmetric stencils (dg_elem.cuh)
-  float *d_psten32 = nullptr;
+  double *d_csten64 = nullptr;     // canonical full stencils, 18 types (dg_elem.cuh)
+  float *d_csten32 = nullptr;
+  uint32_t *d_cperm = nullptr;     // [8][18] vertex relabelling, 3 bits each
   bool prof = false;
   std::map<std::string, ProfStat> prof_stats;
   std::vector<ProfPending> prof_pending;
