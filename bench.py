@@ -1,25 +1,41 @@
-"""Benchmark of the octree hot path: points2Octree + balanceOctree(incCorner).
+"""Benchmark of the octree hot path on one GB300, on the metric
+"served vs plain Mpts/s + p99 ms; FP32-MG vs FP64 solve time @1e-8 rel res".
 
-Workload (default): 64e6 points, per axis u = exp(N(0,1)) mapped by u/(1+u)
-into (0,1), FP64 coordinates, seed 0 (numpy PCG64), maxDepth 30,
-maxNumPtsPerOctant 1 — the scale configuration.  One step = one
-points2Octree followed by one balanceOctree of that cloud.
+Headline workload (serving): a stream of SERVE_REQUESTS requests with
+Poisson arrivals (mean 200 req/s, seed 4), cloud sizes log-uniform in
+[1e4, 8e6], alternately Gaussian-mixture and log-normal clouds, FP64
+coordinates.  Each request is points2Octree -> balanceOctree(incCorner) ->
+mesh (ot::DA) -> multigrid set-up -> CG with an FP32 V-cycle (FP64
+residuals) to 1e-8 relative residual, at most 50 iterations.  One step = the
+whole stream served once by the continuous-batching server
+(dendro_gb300.serving.BatchingServer).
 
-  value : Mpts/s with the points already resident in HBM (device-timed)
-  e2e   : the same through the C ABI with host buffers: the step's points
-          copied in from pinned host memory and the balanced octree copied
-          back to pinned host memory, inside the timed region
-Also reported: the mesh (ot::DA) build time and the Laplacian+mass matVec
-(FP32 and FP64) on the balanced octree of the workload, per-kernel roofline
-figures, nvidia-smi clocks sampled during the timed region, and the CPU
-oracle timed on a bounded sample of the same workload.
+  value : served Mpts/s with every cloud already resident in HBM
+  e2e   : the same stream served from host (pinned) clouds through the C ABI,
+          each request's points copied in and its result read back inside
+          the timed region
+  plain : the same stream through the per-call drop-in (PlainServer: one
+          request at a time, one call per reference function)
+  p50 / p99 request latency (arrival -> result) for both servers.
 
---impl reference times the CPU restatement of the reference path (oracle/,
-C) on the host cores: one process per core, each building and balancing its
-own bounded sample of the workload per step.
+Also reported, each as its own block:
+  precision : the Poisson workload (16e6 N(0.5, 0.15^2) points, seed 3):
+              FP32-V-cycle vs all-FP64 solve time to 1e-8, per-kernel times
+  batching  : 256 Gaussian-mixture clouds (sizes log-uniform in [1e4, 4e6],
+              seed 2) built and balanced in one segmented pass vs one call
+              per cloud
+  scale     : 64e6 log-normal points (seed 0): build+balance Mpts/s with
+              the per-kernel roofline, the mesh build and the Laplacian+mass
+              matVec (FP32 / FP64) on the balanced octree
+nvidia-smi clocks are sampled during the timed region.
 
-Multi-GPU: replicas only (the path has no exchange step); each rank builds
-its own copy of the workload, value sums the ranks' points over the slowest
+--impl reference serves a bounded sample of the same stream on the host
+cores with the CPU restatement of the reference path (oracle/: C for the
+octree and mesh, numpy for the FP64 multigrid solve), one request per
+process.
+
+Multi-GPU: replicas only (the path has no exchange step): each rank serves
+its own copy of the stream; value sums the ranks' points over the slowest
 rank's time.
 """
 from __future__ import annotations
@@ -36,12 +52,13 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOADS = {
-    # name: (npts, generator description)
-    "lognormal64m": 64_000_000,
-    "gauss1m": 1_000_000,
-}
-CPU_SAMPLE_PTS = 1_000_000
+METRIC = "served vs plain Mpts/s + p99 ms; FP32-MG vs FP64 solve time @1e-8 rel res"
+SERVE_REQUESTS = 32
+SERVE_RATE = 200.0
+SERVE_SIZES = (1e4, 8e6)
+SERVE_SEED = 4
+SOLVE_MAXIT = 50
+REF_MAX_POINTS = 40_000  # reference arm: requests of the stream up to this size
 
 
 def _peaks():
@@ -118,22 +135,54 @@ def _dist():
     return ws, rank, local
 
 
-def cpu_sample_run(args):
-    """One bounded CPU sample: oracle points2Octree + balance (runs in a worker process)."""
-    npts, seed = args
+def _top_kernels(stats: dict, k: int = 10) -> dict:
+    """{kernel: [total ms, launches]} of the k kernels with the most time."""
+    top = sorted(stats.items(), key=lambda kv: -kv[1][0])[:k]
+    return {name: [round(v[0], 3), int(v[1])] for name, v in top}
+
+
+def _merge_stats(parts) -> dict:
+    out = {}
+    for st in parts:
+        for k, (ms, cnt, b) in st.items():
+            o = out.get(k, (0.0, 0, 0.0))
+            out[k] = (o[0] + ms, o[1] + cnt, o[2] + b)
+    return out
+
+
+def _stream():
+    from dendro_gb300 import serving
+
+    return serving.poisson_stream(SERVE_REQUESTS, rate=SERVE_RATE, lo=SERVE_SIZES[0], hi=SERVE_SIZES[1],
+                                  seed=SERVE_SEED)
+
+
+# ---------------------------------------------------------------------------
+# reference arm (CPU)
+# ---------------------------------------------------------------------------
+def cpu_request_run(args):
+    """One request of the stream on the CPU restatement (worker process):
+    points2Octree + balanceOctree + DA (oracle C), then the FP64 multigrid
+    CG (oracle numpy) on the same right-hand side as the GPU path."""
+    rid, pts, maxit = args
     sys.path.insert(0, ROOT)
     from dendro_gb300 import datagen
     from oracle import dg_oracle
+    from oracle.mg_ref import OracleMG
 
-    pts = datagen.lognormal(npts, seed=seed)
     t0 = time.perf_counter()
     lin = dg_oracle.points_to_octree(pts, 30, 1)
     bal = dg_oracle.balance(lin, 30)
-    return time.perf_counter() - t0, len(lin), len(bal)
+    mg = OracleMG(bal, 30, max_coarse=4096)
+    f = datagen.bumps(mg.das[0].node_xyz)
+    b = mg.rhs(f)
+    _, it, rr = mg.solve(b, rtol=1e-8, maxit=maxit)
+    return rid, time.perf_counter() - t0, len(pts), it, rr
 
 
 def run_reference(args):
-    """CPU arm: the oracle's restatement of the reference path on every host core."""
+    """CPU arm: the requests of the stream with at most REF_MAX_POINTS points,
+    each served by the oracle on its own host core, all at once per step."""
     ws, rank, _ = _dist()
     if rank != 0:
         return
@@ -142,22 +191,28 @@ def run_reference(args):
     from oracle import dg_oracle
 
     dg_oracle.build()
-    cores = os.cpu_count() or 1
-    npts = args.cpu_sample
+    reqs = [r for r in _stream() if len(r.points) <= REF_MAX_POINTS]
+    cores = min(os.cpu_count() or 1, max(len(reqs), 1))
+    npts = sum(len(r.points) for r in reqs)
     ctxmp = mp.get_context("spawn")
-    times = []
+    times, lat = [], []
     with ctxmp.Pool(cores) as pool:
         for step in range(args.warmup + args.steps):
             t0 = time.perf_counter()
-            pool.map(cpu_sample_run, [(npts, 1000 + i) for i in range(cores)])
+            res = pool.map(cpu_request_run, [(r.rid, r.points, SOLVE_MAXIT) for r in reqs])
             dt = time.perf_counter() - t0
             if step >= args.warmup:
                 times.append(dt)
+                lat.extend(1e3 * r[1] for r in res)
     ms = 1e3 * sum(times) / len(times)
-    value = cores * npts / (ms * 1e-3) / 1e6
+    value = npts / (ms * 1e-3) / 1e6
+    lat.sort()
+    sample = (f"{len(reqs)} requests of the serving stream with <= {REF_MAX_POINTS} points ({npts} points), "
+              f"one per process on {cores} host cores: oracle C points2Octree + balanceOctree + DA per level, "
+              f"numpy FP64 multigrid CG to 1e-8 (<= {SOLVE_MAXIT} iterations)")
     line = {
         "impl": "reference",
-        "metric": "build+balance throughput, Mpts/s (points2Octree + balanceOctree incCorner)",
+        "metric": METRIC,
         "value": value,
         "unit": "Mpts/s",
         "n_gpus": ws,
@@ -167,30 +222,298 @@ def run_reference(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "u32/int64 keys, FP64 coords",
+        "dtype": "int keys, FP64 coords and solve",
         "data": "synthetic",
-        "config": {"workload": args.workload, "max_depth": 30, "max_pts_per_octant": 1,
-                   "sample": f"{cores} processes x {npts} log-normal pts per step (seeds 1000+)"},
-        "cpu_baseline": {"value": value, "unit": "Mpts/s", "cores": cores, "kind": "port",
-                         "sample": f"{cores} x {npts} pts per step, oracle C restatement, 1 thread per process"},
+        "config": {"workload": "serving stream (bounded CPU sample)", "requests": len(reqs), "points": npts,
+                   "max_depth": 30, "max_pts_per_octant": 1, "rate_req_s": SERVE_RATE, "seed": SERVE_SEED},
+        "p50_ms": lat[len(lat) // 2] if lat else None,
+        "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None,
+        "cpu_baseline": {"value": value, "unit": "Mpts/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def _top_kernels(stats: dict, k: int = 10) -> dict:
-    """{kernel: [total ms, launches]} of the k kernels with the most time."""
-    top = sorted(stats.items(), key=lambda kv: -kv[1][0])[:k]
-    return {name: [round(v[0], 3), int(v[1])] for name, v in top}
+def cpu_baseline_sample(cores: int) -> dict:
+    """The reference arm's measurement, short (1 warm-up + 1 timed pass), for
+    the cpu_baseline key of the GPU line."""
+    import multiprocessing as mp
+
+    from oracle import dg_oracle
+
+    dg_oracle.build()
+    reqs = [r for r in _stream() if len(r.points) <= REF_MAX_POINTS]
+    cores = min(cores, max(len(reqs), 1))
+    npts = sum(len(r.points) for r in reqs)
+    with mp.get_context("spawn").Pool(cores) as pool:
+        pool.map(cpu_request_run, [(r.rid, r.points, SOLVE_MAXIT) for r in reqs])
+        t0 = time.perf_counter()
+        pool.map(cpu_request_run, [(r.rid, r.points, SOLVE_MAXIT) for r in reqs])
+        dt = time.perf_counter() - t0
+    return {"value": npts / dt / 1e6, "unit": "Mpts/s", "cores": cores, "kind": "port",
+            "sample": f"{len(reqs)} requests of the serving stream with <= {REF_MAX_POINTS} points ({npts} points), "
+                      f"one per process: oracle C octree + DA, numpy FP64 multigrid CG to 1e-8; {dt:.2f} s"}
 
 
-def run_poisson(dg, datagen, ctx, local, args):
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def _latency(out) -> dict:
+    lat = sorted(1e3 * r.latency for r in out)
+    return {"p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))]}
+
+
+def run_serving(args, local, barrier):
+    """The headline: the stream served by BatchingServer (device-resident and
+    host clouds) and by PlainServer."""
+    import numpy as np
+    import torch
+
+    from dendro_gb300 import serving
+
+    host = _stream()
+    npts = sum(len(r.points) for r in host)
+    dev = f"cuda:{local}"
+    on_dev = [torch.from_numpy(r.points).to(dev) for r in host]
+    pinned = [torch.from_numpy(r.points).pin_memory() for r in host]
+    torch.cuda.synchronize()
+
+    def replay(srv, clouds):
+        reqs = [serving.Request(r.rid, r.arrival, c) for r, c in zip(host, clouds)]
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = srv.run(reqs)
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    srv = serving.BatchingServer(device=local, workers=3, solve_maxit=SOLVE_MAXIT)
+    for _ in range(args.warmup):
+        replay(srv, on_dev)
+    ctxs = [srv.ctx] + srv.worker_ctx
+    for c in ctxs:
+        c.profile(True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    walls, outs = [], []
+    for _ in range(args.steps):
+        out, wall = replay(srv, on_dev)
+        walls.append(wall)
+        outs.extend(out)
+    clocks = sampler.stop()
+    stats = _merge_stats(c.profile_stats() for c in ctxs)
+    for c in ctxs:
+        c.profile(False)
+    batches = list(srv.batches)
+    # the same stream from pinned host memory (copies in, results out)
+    e2e_walls = []
+    replay(srv, pinned)
+    for _ in range(args.steps):
+        _, wall = replay(srv, pinned)
+        e2e_walls.append(wall)
+    srv.close()
+    # the per-call drop-in on the same stream
+    plain = serving.PlainServer(device=local, solve_maxit=SOLVE_MAXIT)
+    replay(plain, on_dev)
+    p_walls, p_outs = [], []
+    for _ in range(2):
+        out, wall = replay(plain, on_dev)
+        p_walls.append(wall)
+        p_outs.extend(out)
+    plain.close()
+    errors = sum(1 for r in outs + p_outs if r.error)
+    ms = 1e3 * sum(walls) / len(walls)
+    res = {
+        "ms_per_step": ms,
+        "points": npts,
+        "requests": len(host),
+        "value": npts / (ms * 1e-3) / 1e6,
+        "e2e_ms": 1e3 * sum(e2e_walls) / len(e2e_walls),
+        "served": {"Mpts_per_s": npts / (ms * 1e-3) / 1e6, **_latency(outs),
+                   "mean_batch": float(np.mean(batches)) if batches else None},
+        "plain": {"Mpts_per_s": npts / (1e-3 * 1e3 * sum(p_walls) / len(p_walls)) / 1e6, **_latency(p_outs)},
+        "iterations_max": max(r.iterations for r in outs),
+        "relres_max": max(r.relres for r in outs),
+        "errors": errors,
+        "stats": stats,
+        "clocks": clocks,
+    }
+    res["served_over_plain"] = res["served"]["Mpts_per_s"] / res["plain"]["Mpts_per_s"]
+    return res
+
+
+def run_scale(args, dg, ctx, local):
+    """64e6 log-normal points: build+balance Mpts/s (device and host
+    buffers), per-kernel figures, mesh build, FP32 / FP64 matVec."""
+    import torch
+
+    from dendro_gb300 import datagen
+
+    npts = args.scale_npts
+    host = datagen.lognormal(npts, seed=0)
+    pinned = torch.from_numpy(host).pin_memory()
+    dev = pinned.to(f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    def step():
+        lin = dg.points2Octree(dev, maxDepth=30, maxNumPtsPerOctant=1, ctx=ctx)
+        bal = dg.balanceOctree(lin)
+        n_lin, n_bal = lin.size, bal.size
+        lin.free()
+        return bal, n_lin, n_bal
+
+    for _ in range(3):
+        bal, n_lin, n_bal = step()
+        bal.free()
+    ctx.profile(True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    e0.record()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        bal, n_lin, n_bal = step()
+        bal.free()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = max(e0.elapsed_time(e1), 1e3 * (time.perf_counter() - t0)) / reps
+    stats = ctx.profile_stats()
+    ctx.profile(False)
+    out_host = torch.empty((n_bal, 4), dtype=torch.int32).pin_memory()
+    e2e = []
+    for i in range(reps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lin = dg.points2Octree(pinned.numpy(), maxDepth=30, maxNumPtsPerOctant=1, ctx=ctx)
+        bal = dg.balanceOctree(lin)
+        lin.free()
+        bal.download_to(out_host.numpy())
+        bal.free()
+        if i > 0:
+            e2e.append(time.perf_counter() - t0)
+    peak, _ = _peaks()
+    kernels = {k: {"ms_per_step": v[0] / reps, "launches_per_step": v[1] / reps,
+                   "GB/s": (v[2] / (v[0] * 1e-3) / 1e9) if v[0] > 0 else None}
+               for k, v in sorted(stats.items(), key=lambda kv: -kv[1][0])[:12]}
+    top, (tms, tcnt, tbytes) = max(stats.items(), key=lambda kv: kv[1][0])
+    res = {"workload": "lognormal64m", "points": npts, "octants_p2o": n_lin, "octants_balanced": n_bal,
+           "build_balance_Mpts_per_s": npts / (ms * 1e-3) / 1e6, "ms_per_step": ms,
+           "e2e_Mpts_per_s": npts / (sum(e2e) / len(e2e)) / 1e6,
+           "top_kernel": {"name": top, "ms_per_launch": tms / tcnt, "GB/s": tbytes / (tms * 1e-3) / 1e9,
+                          "frac_of_measured_peak": tbytes / (tms * 1e-3) / 1e9 / peak},
+           "kernels": kernels}
+    if not args.skip_da:
+        lin = dg.points2Octree(dev, maxDepth=30, maxNumPtsPerOctant=1, ctx=ctx)
+        bal = dg.balanceOctree(lin)
+        lin.free()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        da = dg.DA(bal)
+        res["da_build_ms"] = 1e3 * (time.perf_counter() - t0)
+        ctx.profile(True)  # a second build, timed per kernel
+        dg.DA(bal).free()
+        res["da_kernels_ms"] = _top_kernels(ctx.profile_stats())
+        ctx.profile(False)
+        bal.free()
+        V, E = da.n_node, da.n_elem
+        res["n_elem"], res["n_node"] = E, V
+        mv = {}
+        for prec, dt in ((32, torch.float32), (64, torch.float64)):
+            x = torch.rand(V, dtype=dt, device=f"cuda:{local}") * 2 - 1
+            y = torch.empty_like(x)
+            for _ in range(3):
+                da.matvec(x, y, precision=prec)
+            ctx.profile(True)
+            for _ in range(10):
+                da.matvec(x, y, precision=prec)
+            st = ctx.profile_stats()["matvec"]
+            ctx.profile(False)
+            kms = st[0] / st[1]
+            nbytes = 36 * E + 3 * (prec // 8) * V
+            mv[f"fp{prec}"] = {"ms": kms, "GB/s": nbytes / (kms * 1e-3) / 1e9,
+                               "frac_of_measured_peak": nbytes / (kms * 1e-3) / 1e9 / peak,
+                               "algorithmic_bytes": nbytes}
+        # FP32 against FP64 on the same input: relative L2 difference
+        x64 = torch.rand(V, dtype=torch.float64, device=f"cuda:{local}") * 2 - 1
+        y64, y32 = torch.empty_like(x64), torch.empty(V, dtype=torch.float32, device=f"cuda:{local}")
+        da.matvec(x64, y64, precision=64)
+        da.matvec(x64.float(), y32, precision=32)
+        mv["fp32_vs_fp64_rel_l2"] = float(torch.linalg.vector_norm(y32.double() - y64) / torch.linalg.vector_norm(y64))
+        res["matvec"] = mv
+        da.free()
+    del dev, pinned
+    torch.cuda.empty_cache()
+    return res
+
+
+def run_batching(args, dg, ctx, local):
+    """256 Gaussian-mixture clouds: one segmented points2Octree +
+    balanceOctree over all of them vs one call pair per cloud."""
+    import numpy as np
+    import torch
+
+    from dendro_gb300 import datagen
+
+    sizes = datagen.cloud_sizes(args.batch_clouds, 1e4, 4e6, seed=2)
+    rng = np.random.Generator(np.random.PCG64(2))
+    clouds = [datagen.mixture(int(n), rng) for n in sizes]
+    seg = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    dev = torch.from_numpy(np.concatenate(clouds)).to(f"cuda:{local}")
+    del clouds
+    npts = int(seg[-1])
+    torch.cuda.synchronize()
+
+    def batched():
+        lin = dg.points2OctreeBatch(dev, seg_start=seg, ctx=ctx)
+        bal = dg.balanceOctree(lin)
+        lin.free()
+        off = bal.segments()
+        bal.free()
+        return off
+
+    def per_call():
+        counts = []
+        for s in range(len(sizes)):
+            lin = dg.points2Octree(dev[int(seg[s]):int(seg[s + 1])], maxDepth=30, maxNumPtsPerOctant=1, ctx=ctx)
+            bal = dg.balanceOctree(lin)
+            lin.free()
+            counts.append(bal.size)
+            bal.free()
+        return counts
+
+    for _ in range(2):
+        off = batched()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        off = batched()
+    torch.cuda.synchronize()
+    t_b = (time.perf_counter() - t0) / reps
+    counts = per_call()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    counts = per_call()
+    torch.cuda.synchronize()
+    t_p = time.perf_counter() - t0
+    same = bool(np.array_equal(np.diff(np.asarray(off, np.int64)), np.asarray(counts, np.int64)))
+    del dev
+    torch.cuda.empty_cache()
+    return {"clouds": len(sizes), "points": npts, "balanced_octants": int(off[-1]),
+            "batched_Mpts_per_s": npts / t_b / 1e6, "per_call_Mpts_per_s": npts / t_p / 1e6,
+            "batched_over_per_call": t_p / t_b, "batched_ms": 1e3 * t_b, "per_call_ms": 1e3 * t_p,
+            "per_cloud_sizes_equal": same}
+
+
+def run_poisson(args, dg, ctx, local):
     """-lap(u) + u = f, u = 0 on the cube boundary, on the balanced octree of
     16e6 N(0.5, 0.15^2) points (seed 3), f = 4 Gaussian bumps (seed 3), load
     vector = mass matrix times nodal f; levels by coarsen + balance down to
     <= 4096 elements; CG to 1e-8 relative residual with one V(2,2) damped-
     Jacobi (omega 0.667) cycle per iteration, FP32 or FP64 cycle, FP64 CG."""
     import torch
+
+    from dendro_gb300 import datagen
 
     npts = args.poisson_npts
     pts = torch.from_numpy(datagen.gaussian(npts, 0.5, 0.15, seed=3)).to(f"cuda:{local}")
@@ -202,13 +525,15 @@ def run_poisson(dg, datagen, ctx, local, args):
     torch.cuda.synchronize()
     t_build = time.perf_counter() - t0
     t0 = time.perf_counter()
-    mg = dg.MultiGrid(bal, max_coarse_elems=4096)
+    mg = dg.MultiGrid(bal, max_coarse_elems=4096, ctx=ctx)
     t_setup = time.perf_counter() - t0
     bal.free()
-    f = torch.from_numpy(datagen.bumps(mg.level_nodes(0))).to(f"cuda:{local}")
+    f = datagen.bumps(mg.level_nodes(0, device=True))
+    torch.cuda.synchronize()
     b = mg.rhs(f)
     out = {"points": npts, "levels": mg.n_levels, "level_elements": [e for e, _ in mg.sizes],
            "fine_nodes": mg.sizes[0][1], "build_balance_ms": 1e3 * t_build, "mg_setup_ms": 1e3 * t_setup}
+    xs = {}
     for prec in (32, 64):
         mg.solve(b, precision=prec, rtol=1e-8, maxit=200)  # warm-up
         times, its, rrs = [], [], []
@@ -220,18 +545,20 @@ def run_poisson(dg, datagen, ctx, local, args):
             times.append(1e3 * (time.perf_counter() - t0))
             its.append(it)
             rrs.append(rr)
+        xs[prec] = x
         out[f"fp{prec}_vcycle"] = {"solve_ms": min(times), "iterations": its[0], "relres_fp64": max(rrs)}
         ctx.profile(True)  # one more solve, timed per kernel
         mg.solve(b, precision=prec, rtol=1e-8, maxit=200)
         out[f"fp{prec}_vcycle"]["kernels_ms"] = _top_kernels(ctx.profile_stats())
         ctx.profile(False)
+    out["fp32_vs_fp64_solution_rel_l2"] = float(torch.linalg.vector_norm(xs[32] - xs[64]) /
+                                                torch.linalg.vector_norm(xs[64]))
     out["speedup_fp32_vs_fp64"] = out["fp64_vcycle"]["solve_ms"] / out["fp32_vcycle"]["solve_ms"]
     mg.free()
     return out
 
 
 def run_ours(args):
-    import numpy as np
     import torch
 
     ws, rank, local = _dist()
@@ -239,7 +566,6 @@ def run_ours(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    torch.cuda.set_device(local)
 
     def barrier():
         if ws > 1:
@@ -247,154 +573,52 @@ def run_ours(args):
 
             dist.barrier()
 
+    # the CPU baseline first: its worker processes start before this process
+    # touches the GPU
+    cpu = None
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        try:
+            cpu = cpu_baseline_sample(os.cpu_count() or 1)
+        except Exception as exc:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "Mpts/s", "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {exc}"}
+
+    torch.cuda.set_device(local)
     import dendro_gb300 as dg
-    from dendro_gb300 import datagen
 
-    npts = args.npts or WORKLOADS[args.workload]
-    if args.workload.startswith("lognormal"):
-        host = datagen.lognormal(npts, seed=0)
-    else:
-        host = datagen.gaussian(npts, 0.5, 0.1, seed=0)
-    pinned = torch.from_numpy(host).pin_memory()
-    dev = pinned.to(f"cuda:{local}")
     ctx = dg.Context(local)
-    torch.cuda.synchronize()
-
-    def step_device():
-        lin = dg.points2Octree(dev, maxDepth=30, maxNumPtsPerOctant=1, ctx=ctx)
-        bal = dg.balanceOctree(lin)
-        n_lin, n_bal = lin.size, bal.size
-        lin.free()
-        return bal, n_lin, n_bal
-
-    for _ in range(args.warmup):
-        bal, n_lin, n_bal = step_device()
-        bal.free()
-    torch.cuda.synchronize()
-
-    # ---- device-resident timed region --------------------------------------
-    ctx.profile(True)
-    sampler = ClockSampler(local)
-    sampler.start()
-    barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        bal, n_lin, n_bal = step_device()
-        bal.free()
-    e1.record()
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
-    barrier()
-    clocks = sampler.stop()
-    stats = ctx.profile_stats()
-    ctx.profile(False)
-    ms = e0.elapsed_time(e1) / args.steps
-    ms = max(ms, 1e3 * wall / args.steps)  # host waits inside the calls count too
+    serve = run_serving(args, local, barrier)
+    ms = serve["ms_per_step"]
+    e2e_ms = serve["e2e_ms"]
     if ws > 1:
         import torch.distributed as dist
 
-        t = torch.tensor([ms], device=f"cuda:{local}")
+        t = torch.tensor([ms, e2e_ms], device=f"cuda:{local}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * npts / (ms * 1e-3) / 1e6
-
-    # ---- end-to-end through the C ABI with host buffers --------------------
-    out_host = torch.empty((n_bal, 4), dtype=torch.int32).pin_memory()
-    e2e_ms = []
-    for i in range(args.steps + 1):
-        barrier()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        lin = dg.points2Octree(pinned.numpy(), maxDepth=30, maxNumPtsPerOctant=1, ctx=ctx)
-        bal = dg.balanceOctree(lin)
-        lin.free()
-        bal.download_to(out_host.numpy())
-        bal.free()
-        dt = time.perf_counter() - t0
-        if i > 0:
-            e2e_ms.append(1e3 * dt)
-    e2e_step = sum(e2e_ms) / len(e2e_ms)
-    if ws > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([e2e_step], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_step = float(t.item())
-    e2e = {"value": ws * npts / (e2e_step * 1e-3) / 1e6, "unit": "Mpts/s", "h2d_bytes_per_step": 24 * npts,
-           "d2h_bytes_per_step": 16 * n_bal}
-
-    # ---- mesh + matVec on the balanced octree ------------------------------
+        ms, e2e_ms = float(t[0]), float(t[1])
+    value = ws * serve["points"] / (ms * 1e-3) / 1e6
     extra = {}
-    if not args.skip_da:
-        lin = dg.points2Octree(dev, maxDepth=30, maxNumPtsPerOctant=1, ctx=ctx)
-        bal = dg.balanceOctree(lin)
-        lin.free()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        da = dg.DA(bal)
-        da_ms = 1e3 * (time.perf_counter() - t0)
-        ctx.profile(True)  # a second build, timed per kernel
-        dg.DA(bal).free()
-        da_kernels = _top_kernels(ctx.profile_stats())
-        ctx.profile(False)
-        bal.free()
-        V, E = da.n_node, da.n_elem
-        ctx.profile(True)
-        mv = {}
-        for prec, dt in ((32, torch.float32), (64, torch.float64)):
-            x = torch.rand(V, dtype=dt, device=f"cuda:{local}") * 2 - 1
-            y = torch.empty_like(x)
-            for _ in range(3):
-                da.matvec(x, y, precision=prec)
-            ctx.profile(True)
-            reps = 10
-            for _ in range(reps):
-                da.matvec(x, y, precision=prec)
-            st = ctx.profile_stats()["matvec"]
-            kms = st[0] / st[1]
-            nbytes = 36 * E + 3 * (prec // 8) * V
-            mv[f"fp{prec}"] = {"ms": kms, "GB/s": nbytes / (kms * 1e-3) / 1e9, "algorithmic_bytes": nbytes}
-        ctx.profile(False)
-        da.free()
-        extra = {"da_build_ms": da_ms, "da_kernels_ms": da_kernels, "n_elem": E, "n_node": V, "matvec": mv}
-
-    # ---- precision workload: FP32-MG vs FP64 solve to 1e-8 ----------------
+    if not args.skip_scale:
+        extra["scale"] = run_scale(args, dg, ctx, local)
+    if not args.skip_batch:
+        extra["batching"] = run_batching(args, dg, ctx, local)
     if not args.skip_mg:
-        extra["poisson"] = run_poisson(dg, datagen, ctx, local, args)
+        extra["precision"] = run_poisson(args, dg, ctx, local)
 
-    # ---- roofline of the dominant kernel of the timed step ----------------
+    # roofline of the dominant kernel of the served step
+    stats = serve["stats"]
     peak, peak_kind = _peaks()
     launches = sum(v[1] for v in stats.values())
-    top = max(stats.items(), key=lambda kv: kv[1][0])
-    tname, (tms, tcnt, tbytes) = top
-    per_launch_ms = tms / tcnt
-    per_launch_bytes = tbytes / tcnt
+    tname, (tms, tcnt, tbytes) = max(stats.items(), key=lambda kv: kv[1][0])
+    per_launch_ms, per_launch_bytes = tms / tcnt, tbytes / tcnt
     achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9
-    step_ms_total = sum(v[0] for v in stats.values())
+    step_total = sum(v[0] for v in stats.values())
     kernels = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps,
                    "GB/s": (v[2] / (v[0] * 1e-3) / 1e9) if v[0] > 0 else None,
-                   "share": v[0] / step_ms_total if step_ms_total else None}
-               for k, v in sorted(stats.items(), key=lambda kv: -kv[1][0])}
-
-    cpu = None
-    if rank == 0 and not args.skip_cpu:
-        try:
-            from oracle import dg_oracle
-
-            dg_oracle.build()
-            dt, _, _ = cpu_sample_run((args.cpu_sample, 1000))
-            cpu = {"value": args.cpu_sample / dt / 1e6, "unit": "Mpts/s", "cores": 1, "kind": "port",
-                   "sample": f"{args.cpu_sample} log-normal pts (seed 1000), oracle C restatement of "
-                             f"points2Octree + balanceOctree, 1 thread, {dt:.2f} s"}
-        except Exception as exc:  # the baseline is reported, never required
-            cpu = {"value": None, "unit": "Mpts/s", "cores": 1, "kind": "port", "sample": f"failed: {exc}"}
-
+                   "share": v[0] / step_total if step_total else None}
+               for k, v in sorted(stats.items(), key=lambda kv: -kv[1][0])[:15]}
     if rank == 0:
         line = {
-            "metric": "build+balance throughput, Mpts/s (points2Octree + balanceOctree incCorner)",
+            "metric": METRIC,
             "value": value,
             "unit": "Mpts/s",
             "n_gpus": ws,
@@ -404,17 +628,26 @@ def run_ours(args):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "u64x2 Morton keys (int), FP64 coords",
+            "dtype": "int keys (octree, mesh); FP32 V-cycle, FP64 CG (solve)",
             "data": "synthetic",
-            "config": {"workload": args.workload, "points": npts, "max_depth": 30, "max_pts_per_octant": 1,
-                       "octants_p2o": n_lin, "octants_balanced": n_bal,
-                       "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2 (1.5 GB of points per step)"},
-            "e2e": e2e,
-            "gpu_launches": int(launches // max(args.steps, 1)) * args.steps,
+            "config": {"workload": "serving stream", "requests": serve["requests"], "points": serve["points"],
+                       "rate_req_s": SERVE_RATE, "sizes": list(SERVE_SIZES), "seed": SERVE_SEED,
+                       "max_depth": 30, "max_pts_per_octant": 1, "solve": f"FP32 V(2,2) CG to 1e-8, <= {SOLVE_MAXIT} it",
+                       "parallelism": f"replicas x{ws}",
+                       "l2": f"inputs larger than L2 ({24 * serve['points'] / 1e9:.2f} GB of points per step)"},
+            "served": serve["served"],
+            "plain": serve["plain"],
+            "served_over_plain": serve["served_over_plain"],
+            "solve_iterations_max": serve["iterations_max"],
+            "solve_relres_max": serve["relres_max"],
+            "request_errors": serve["errors"],
+            "e2e": {"value": ws * serve["points"] / (e2e_ms * 1e-3) / 1e6, "unit": "Mpts/s",
+                    "h2d_bytes_per_step": 24 * serve["points"], "d2h_bytes_per_step": 24 * serve["requests"]},
+            "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": tname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
                          "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms},
-            "clocks": clocks,
+            "clocks": serve["clocks"],
             "cpu_baseline": cpu,
             "kernels": kernels,
             **extra,
@@ -432,15 +665,18 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="lognormal64m", choices=sorted(WORKLOADS))
-    ap.add_argument("--npts", type=int, default=0, help="override the workload's point count")
-    ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE_PTS)
-    ap.add_argument("--skip-da", action="store_true")
-    ap.add_argument("--skip-mg", action="store_true")
+    ap.add_argument("--scale-npts", type=int, default=64_000_000)
+    ap.add_argument("--batch-clouds", type=int, default=256)
     ap.add_argument("--poisson-npts", type=int, default=16_000_000)
     ap.add_argument("--poisson-reps", type=int, default=3)
+    ap.add_argument("--skip-scale", action="store_true")
+    ap.add_argument("--skip-da", action="store_true")
+    ap.add_argument("--skip-batch", action="store_true")
+    ap.add_argument("--skip-mg", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("note: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
         run_reference(args)
     else:

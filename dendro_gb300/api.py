@@ -35,7 +35,14 @@ def _is_device(a) -> bool:
 
 
 def _ptr(a):
+    """Address of an argument.  A CUDA tensor may still be being written by
+    torch on torch's current stream, while the library works on its own
+    stream: wait for torch's stream first, so the library reads finished data
+    (every library call itself returns with its results complete)."""
     if _is_device(a):
+        import torch
+
+        torch.cuda.current_stream(a.device).synchronize()
         return ctypes.c_void_p(a.data_ptr())
     return a.ctypes.data_as(ctypes.c_void_p)
 
@@ -210,7 +217,12 @@ def points2OctreeBatch(clouds, gLens=(1.0, 1.0, 1.0), maxDepth: int = 30, maxNum
     if seg_start is None:
         sizes = [len(c) for c in clouds]
         seg_start = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
-        pts = np.concatenate([np.asarray(c, np.float64).reshape(-1, 3) for c in clouds]) if sizes else np.zeros((0, 3))
+        if sizes and all(_is_device(c) for c in clouds):
+            import torch
+
+            pts = torch.cat([c.reshape(-1, 3) for c in clouds]).contiguous()
+        else:
+            pts = np.concatenate([np.asarray(c, np.float64).reshape(-1, 3) for c in clouds]) if sizes else np.zeros((0, 3))
     else:
         pts = clouds
         seg_start = np.ascontiguousarray(seg_start, dtype=np.uint64)
@@ -349,9 +361,18 @@ class MultiGrid:
             ctx._L.dg_mg_level_sizes(h, l, ctypes.byref(e), ctypes.byref(v))
             self.sizes.append((e.value, v.value))
 
-    def level_nodes(self, level: int) -> np.ndarray:
-        xyz = np.empty((self.sizes[level][1], 3), np.uint32)
-        check(self.ctx.handle, self.ctx._L.dg_mg_level_nodes(self.ctx.handle, self.handle, level, _ptr(xyz), 0), "level_nodes")
+    def level_nodes(self, level: int, device: bool = False):
+        """Node coordinates (n_node, 3) of a level: numpy uint32, or with
+        ``device`` an int32 CUDA tensor holding the same bits."""
+        if device:
+            import torch
+
+            xyz = torch.empty((self.sizes[level][1], 3), dtype=torch.int32, device=f"cuda:{self.ctx.device}")
+        else:
+            xyz = np.empty((self.sizes[level][1], 3), np.uint32)
+        check(self.ctx.handle,
+              self.ctx._L.dg_mg_level_nodes(self.ctx.handle, self.handle, level, _ptr(xyz), 1 if device else 0),
+              "level_nodes")
         return xyz
 
     def level_octree(self, level: int) -> np.ndarray:

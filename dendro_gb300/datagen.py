@@ -83,6 +83,15 @@ def bumps(xyz_u32: np.ndarray, max_depth: int = 30, seed: int = 3) -> np.ndarray
     a = rng.uniform(0.5, 2.0, 4)
     c = rng.uniform(0.2, 0.8, (4, 3))
     s = rng.uniform(0.05, 0.15, 4)
+    if hasattr(xyz_u32, "is_cuda"):  # node coordinates on the device: FP64 field there
+        import torch
+
+        x = (xyz_u32.to(torch.int64) & 0xFFFFFFFF).to(torch.float64) / float(1 << max_depth)
+        f = torch.zeros(x.shape[0], dtype=torch.float64, device=x.device)
+        for i in range(4):
+            ci = torch.tensor(c[i], dtype=torch.float64, device=x.device)
+            f += float(a[i]) * torch.exp(-((x - ci) ** 2).sum(1) / (2 * float(s[i]) ** 2))
+        return f
     x = np.asarray(xyz_u32, np.float64) / float(1 << max_depth)
     f = np.zeros(len(x))
     for i in range(4):

@@ -46,6 +46,7 @@ class Request:
     iterations: int = 0
     relres: float = 0.0
     solution_norm: float = 0.0
+    t_setup: float = 0.0        # multigrid set-up seconds (mesh hierarchy)
     error: str = ""
 
     @property
@@ -79,17 +80,36 @@ def poisson_stream(count: int, rate: float = 200.0, lo: float = 1e4, hi: float =
     return reqs
 
 
-def _solve(ctx: Context, bal, req: Request, maxit: int, max_coarse: int):
-    """Mesh + multigrid + FP32-V-cycle CG for one balanced octree (device)."""
+def _solve(ctx: Context, bal, req: Request, maxit: int, max_coarse: int, stream=None):
+    """Mesh + multigrid + FP32-V-cycle CG for one balanced octree, all on the
+    device: the right-hand side field is evaluated at the device-resident
+    node coordinates, and only the iteration count, the residual and the
+    solution norm come back to the host.  ``stream``: the torch stream for
+    the field evaluation (synchronised before the library reads it)."""
+    import torch
+
+    t0 = time.perf_counter()
     mg = MultiGrid(bal, max_coarse_elems=max_coarse, ctx=ctx)
     try:
-        f = datagen.bumps(mg.level_nodes(0))
+        req.t_setup = time.perf_counter() - t0
+        with torch.cuda.stream(stream or torch.cuda.current_stream(ctx.device)):
+            f = datagen.bumps(mg.level_nodes(0, device=True))
+            torch.cuda.current_stream(ctx.device).synchronize()
         b = mg.rhs(f)
         x, it, rr = mg.solve(b, precision=32, rtol=1e-8, maxit=maxit)
         req.iterations, req.relres = it, rr
-        req.solution_norm = float(np.linalg.norm(x))
+        with torch.cuda.stream(stream or torch.cuda.current_stream(ctx.device)):
+            req.solution_norm = float(torch.linalg.vector_norm(x))
     finally:
         mg.free()
+
+
+def _host_or_device(points):
+    """Points as the API takes them: a numpy array (host, pinned or not) or a
+    CUDA tensor; a CPU tensor is passed as its numpy view (same memory)."""
+    if hasattr(points, "is_cuda") and not points.is_cuda:
+        return points.numpy()
+    return points
 
 
 class PlainServer:
@@ -106,7 +126,7 @@ class PlainServer:
             if now < r.arrival:
                 time.sleep(r.arrival - now)
             r.t_admit = time.perf_counter() - t0
-            lin = points2Octree(r.points, ctx=self.ctx)
+            lin = points2Octree(_host_or_device(r.points), ctx=self.ctx)
             bal = balanceOctree(lin)
             r.n_octants, r.n_balanced = lin.size, bal.size
             lin.free()
@@ -143,13 +163,16 @@ class BatchingServer:
             self.cv.notify_all()
 
     def _worker(self, ctx: Context, work: queue.Queue, t0: float):
+        import torch
+
+        stream = torch.cuda.Stream(device=ctx.device)
         while True:
             item = work.get()
             if item is None:
                 return
             req, bal, nbytes = item
             try:
-                _solve(ctx, bal, req, self.maxit, self.max_coarse)
+                _solve(ctx, bal, req, self.maxit, self.max_coarse, stream)
             except Exception as e:  # reported per request
                 req.error = str(e)
             finally:
@@ -209,8 +232,17 @@ class BatchingServer:
                 if not batch:
                     self.cv.wait(timeout=0.05)
                     continue
-            # one segmented construction + balance for the whole batch
-            lin = points2OctreeBatch([r.points for r, _ in batch], ctx=self.ctx)
+            # one segmented construction + balance for the whole batch; host
+            # clouds are copied in one by one (from pinned memory when they
+            # live there) and joined on the device
+            clouds = [r.points for r, _ in batch]
+            if not all(getattr(c, "is_cuda", False) for c in clouds):
+                import torch
+
+                dev = f"cuda:{self.ctx.device}"
+                clouds = [torch.as_tensor(c).to(dev, non_blocking=True) for c in clouds]
+                torch.cuda.current_stream(self.ctx.device).synchronize()
+            lin = points2OctreeBatch(clouds, ctx=self.ctx)
             bal = balanceOctree(lin)
             off_lin, off_bal = lin.segments(), bal.segments()
             lin.free()

@@ -59,3 +59,20 @@ def test_batch_rejects_bad_offsets(ctx):
     pts = datagen.gaussian(100, seed=1)
     with pytest.raises(DendroError):
         points2OctreeBatch(pts, seg_start=np.array([0, 50, 40, 100], np.uint64), ctx=ctx)
+
+
+def test_batch_of_device_tensors_equals_host_batch(ctx):
+    """Clouds handed over as CUDA tensors (joined on the device by torch) give
+    the same octrees as the same clouds from host memory, call after call:
+    the library waits for torch's stream before it reads."""
+    torch = pytest.importorskip("torch")
+    clouds = [c for i, c in enumerate(make_batch(54, count=16)) if i != 7]
+    want = [p.copy() for p in balanceOctree(points2OctreeBatch(clouds, ctx=ctx)).split()]
+    dev = [torch.from_numpy(np.ascontiguousarray(c)).cuda() for c in clouds]
+    for _ in range(3):
+        # scribble over freed torch memory so a read before the join completes shows
+        junk = torch.full((sum(len(c) for c in clouds), 3), 0.25, dtype=torch.float64, device="cuda")
+        del junk
+        got = balanceOctree(points2OctreeBatch(dev, ctx=ctx)).split()
+        for a, b in zip(want, got):
+            assert np.array_equal(a, b)
