@@ -367,7 +367,8 @@ __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict
                                                       const uint32_t *__restrict__ meta, size_t E,
                                                       const uint32_t *__restrict__ node_pairs,
                                                       uint16_t *__restrict__ pinc, uint16_t *__restrict__ pexc,
-                                                      uint32_t *__restrict__ pmeta, uint32_t *__restrict__ run_node,
+                                                      uint32_t *__restrict__ pmeta, uint16_t *__restrict__ pkeys,
+                                                      uint16_t *__restrict__ pkcount, uint32_t *__restrict__ run_node,
                                                       uint32_t *__restrict__ n_run) {
   __shared__ uint64_t sk[PATCH_ENT];
   __shared__ uint16_t runpos[PATCH_ENT + 1];
@@ -387,11 +388,19 @@ __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict
   }
   __syncthreads();
   block_bitonic<uint32_t>(ek, PATCH);
+  // (type, level) groups of the ordered elements: the patch's stencil keys
+  const uint32_t grp = ek[tid] >> 9;
+  const int gstart = tid < ne && (tid == 0 || (ek[tid - 1] >> 9) != grp) ? 1 : 0;
+  int nkeys;
+  const int kidx = block_excl_scan<int, PATCH>(gstart, nkeys) + gstart - 1;
   if (tid < ne) {
     const uint32_t eo = ek[tid] & (PATCH - 1);
     rank[eo] = (uint16_t)tid;
-    pmeta[p * PATCH + tid] = meta[e0 + eo];
+    const uint32_t mo = meta[e0 + eo];
+    pmeta[p * PATCH + tid] = (mo & 0xff00ffffu) | (uint32_t)(kidx < PKEY_MAX ? kidx : 0) << 16;
+    if (gstart && kidx < PKEY_MAX) pkeys[p * PKEY_MAX + kidx] = (uint16_t)grp;
   }
+  if (tid == 0) pkcount[p] = (uint16_t)nkeys;
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < 8; k++) {
@@ -457,6 +466,7 @@ static void mesh_patches(Context &ctx, Mesh &m) {
   DBuf<uint32_t> pairs(m.n_node, s), run_node(np * PATCH_ENT, s), n_run(np, s);
   DBuf<uint16_t> pinc(np * PATCH_ENT, s), pexc(np * PATCH, s);
   DBuf<uint32_t> pmeta(np * PATCH, s);
+  DBuf<uint16_t> pkeys(np * PKEY_MAX, s), pkcount(np, s);
   DBuf<uint64_t> poff(np + 1, s);
   DG_CUDA(cudaMemsetAsync(pairs.get(), 0, m.n_node * sizeof(uint32_t), s));
   {
@@ -467,7 +477,7 @@ static void mesh_patches(Context &ctx, Mesh &m) {
   {
     ProfScope _prof(ctx, "da_patch_sort", (double)n * 8 * 14);
     k_patch_sort<<<(unsigned)np, PATCH, 0, s>>>(m.conn, m.meta, n, pairs.get(), pinc.get(), pexc.get(),
-                                                pmeta.get(), run_node.get(), n_run.get());
+                                                pmeta.get(), pkeys.get(), pkcount.get(), run_node.get(), n_run.get());
     DG_LAUNCH_CHECK();
   }
   exclusive_scan<uint32_t, uint64_t>(n_run.get(), poff.get(), np, poff.get() + np, s);
@@ -484,6 +494,8 @@ static void mesh_patches(Context &ctx, Mesh &m) {
   m.pinc = pinc.release_ptr();
   m.pexc = pexc.release_ptr();
   m.pmeta = pmeta.release_ptr();
+  m.pkeys = pkeys.release_ptr();
+  m.pkcount = pkcount.release_ptr();
   m.pnode = pnode.release_ptr();
   m.poff = poff.release_ptr();
 }
@@ -533,6 +545,8 @@ void mesh_free(Context &ctx, Mesh &m) {
   if (m.pinc) cudaFreeAsync(m.pinc, ctx.stream);
   if (m.pexc) cudaFreeAsync(m.pexc, ctx.stream);
   if (m.pmeta) cudaFreeAsync(m.pmeta, ctx.stream);
+  if (m.pkeys) cudaFreeAsync(m.pkeys, ctx.stream);
+  if (m.pkcount) cudaFreeAsync(m.pkcount, ctx.stream);
   if (m.pnode) cudaFreeAsync(m.pnode, ctx.stream);
   if (m.poff) cudaFreeAsync(m.poff, ctx.stream);
   m = Mesh();
@@ -559,9 +573,9 @@ void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, 
                                                : reinterpret_cast<const T *>(ctx.d_csten32);
   {
     ProfScope _prof(ctx, "matvec", (double)m.n_elem * 36 + (double)m.n_node * 3 * sizeof(T));
-    k_patch_matvec<T, false><<<grid, PATCH, smem, s>>>(m.pmeta, m.pinc, m.pexc, m.pnode, m.poff, m.n_elem,
-                                                       m.n_patch, cs, ctx.d_cperm, nullptr, x, y, (T)lap_fac,
-                                                       (T)mass_fac);
+    k_patch_matvec<T, false><<<grid, PATCH, smem, s>>>(m.pmeta, m.pinc, m.pexc, m.pnode, m.poff, m.pkeys,
+                                                       m.pkcount, m.n_elem, m.n_patch, cs, ctx.d_cperm, nullptr, x,
+                                                       y, (T)lap_fac, (T)mass_fac);
     DG_LAUNCH_CHECK();
   }
 }

@@ -25,7 +25,10 @@ struct Mesh {
   size_t n_patch = 0;
   uint16_t *pinc = nullptr;   // PATCH_ENT per patch, node-sorted pairs
   uint16_t *pexc = nullptr;   // PATCH per patch: runs starting before pair 8t
-  uint32_t *pmeta = nullptr;  // PATCH per patch: meta in the patch's element order
+  uint32_t *pmeta = nullptr;  // PATCH per patch: meta in the patch's element order,
+                              // bits 16..23 = the element's stencil key index
+  uint16_t *pkeys = nullptr;  // PKEY_MAX per patch: (type << 5 | level) of each key
+  uint16_t *pkcount = nullptr;  // keys per patch (> PKEY_MAX: per-element L, M path)
   uint32_t *pnode = nullptr;  // node of each run, patch after patch
   uint64_t *poff = nullptr;   // n_patch + 1 run offsets into pnode
 };

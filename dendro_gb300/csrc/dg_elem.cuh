@@ -40,6 +40,14 @@ constexpr int fsten_entries() {
 }
 constexpr int PATCH = 512;
 constexpr int PATCH_ENT = 8 * PATCH;
+// per-patch combined stencils: one 8x8 S = f1(l) L_t + f2(l) M_t per
+// (type, level) present in the patch, up to PKEY_MAX of them; rows padded by
+// 16 bytes so neighbouring keys sit in different banks
+constexpr int PKEY_MAX = 64;
+template <typename T>
+constexpr int sstride() {
+  return 64 + 16 / (int)sizeof(T);
+}
 constexpr uint32_t ENT_SLOT = 0xfffu, ENT_START = 1u << 12, ENT_COMPLETE = 1u << 13;
 constexpr uint32_t RUN_BDY = 1u << 31;  // run node flag in shared memory (Dirichlet)
 
@@ -104,6 +112,38 @@ __device__ __forceinline__ void apply_full(const double *__restrict__ S, double 
   }
 }
 
+// y'_k = sum_j S[k][j] x_j with a combined, already scaled stencil S
+template <typename Emit>
+__device__ __forceinline__ void apply_comb(const float *__restrict__ S, const float (&xv)[8], Emit &&emit) {
+  const float2 x0 = make_float2(xv[0], xv[1]), x1 = make_float2(xv[2], xv[3]);
+  const float2 x2 = make_float2(xv[4], xv[5]), x3 = make_float2(xv[6], xv[7]);
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const float4 s0 = reinterpret_cast<const float4 *>(S + 8 * k)[0];
+    const float4 s1 = reinterpret_cast<const float4 *>(S + 8 * k)[1];
+    float2 a = ffma2(make_float2(s0.x, s0.y), x0, make_float2(0.f, 0.f));
+    a = ffma2(make_float2(s0.z, s0.w), x1, a);
+    a = ffma2(make_float2(s1.x, s1.y), x2, a);
+    a = ffma2(make_float2(s1.z, s1.w), x3, a);
+    emit(k, a.x + a.y);
+  }
+}
+
+template <typename Emit>
+__device__ __forceinline__ void apply_comb(const double *__restrict__ S, const double (&xv)[8], Emit &&emit) {
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    double a = 0, b = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j += 2) {
+      const double2 sv = reinterpret_cast<const double2 *>(S + 8 * k + j)[0];
+      a = fma(sv.x, xv[j], a);
+      b = fma(sv.y, xv[j + 1], b);
+    }
+    emit(k, a + b);
+  }
+}
+
 // y = (lapf K + massf M) x over the elements of every patch; with DIR the
 // Dirichlet form: boundary rows are the identity (y = x), boundary columns
 // are dropped.  One block of PATCH threads per patch, grid-strided; thread t
@@ -115,7 +155,8 @@ template <typename T, bool DIR>
 __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
     k_patch_matvec(const uint32_t *__restrict__ pmeta, const uint16_t *__restrict__ pinc,
                    const uint16_t *__restrict__ pexc, const uint32_t *__restrict__ pnode,
-                   const uint64_t *__restrict__ poff, size_t E, size_t n_patch, const T *__restrict__ fsten,
+                   const uint64_t *__restrict__ poff, const uint16_t *__restrict__ pkeys,
+                   const uint16_t *__restrict__ pkcount, size_t E, size_t n_patch, const T *__restrict__ fsten,
                    const uint32_t *__restrict__ cperm, const uint8_t *__restrict__ bdy, const T *__restrict__ x,
                    T *__restrict__ y, T lapf, T massf) {
   constexpr int NW = PATCH / 32;
@@ -124,20 +165,23 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
   T *bufs = cs + fsten_entries<T>();
   uint32_t *gns = reinterpret_cast<uint32_t *>(bufs + 2 * PATCH_ENT);
   uint32_t *cp = gns + 2 * PATCH_ENT;
+  T *sc = reinterpret_cast<T *>(cp + 8 * 18 + 4);  // PKEY_MAX combined stencils (16-byte aligned)
   __shared__ T ws_v[2][NW];
   __shared__ int ws_f[2][NW];
   __shared__ int ws_first[2][NW + 1];
   for (int i = threadIdx.x; i < fsten_entries<T>(); i += PATCH) cs[i] = fsten[i];
   for (int i = threadIdx.x; i < 8 * 18; i += PATCH) cp[i] = cperm[i];
+  __syncthreads();  // step 1 of the first patch already reads cs
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
 
   auto patch_ne = [&](size_t q) { return (int)((E - q * PATCH) < (size_t)PATCH ? (E - q * PATCH) : (size_t)PATCH); };
   size_t p = blockIdx.x;
   uint4 w = make_uint4(0, 0, 0, 0);
-  uint32_t ex = 0, me = 0;
+  uint32_t ex = 0, me = 0, kc = 0;
   uint64_t ub = 0;
   if (p < n_patch) {
     ub = poff[p];
+    kc = pkcount[p];
     if (tid < patch_ne(p)) {
       w = reinterpret_cast<const uint4 *>(pinc + p * PATCH_ENT)[tid];
       ex = pexc[p * PATCH + tid];
@@ -149,12 +193,13 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
     const int ne = patch_ne(p);
     const bool have = tid < ne;
     const uint4 cw = w;
-    const uint32_t cex = ex, cme = me;
+    const uint32_t cex = ex, cme = me, ckc = kc;
     const uint64_t cub = ub;
     // the next patch's table words, one patch ahead
     const size_t pn = p + gridDim.x;
     if (pn < n_patch) {
       ub = poff[pn];
+      kc = pkcount[pn];
       if (tid < patch_ne(pn)) {
         w = reinterpret_cast<const uint4 *>(pinc + pn * PATCH_ENT)[tid];
         ex = pexc[pn * PATCH + tid];
@@ -191,6 +236,19 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
         buf[e & ENT_SLOT] = xv;
       }
     }
+    // the patch's combined stencils (read only in step 2 of this patch, and
+    // rewritten only after every thread has passed that step's barrier)
+    const bool comb = ckc <= (uint32_t)PKEY_MAX;
+    if (comb) {
+      for (int i = tid; i < (int)ckc * 64; i += PATCH) {
+        const uint32_t key = pkeys[p * PKEY_MAX + (i >> 6)];
+        const unsigned t = key >> 5, l = key & 31u;
+        const T h = exp2_neg((T)0, l);
+        const T *st = cs + t * fsten_stride<T>();
+        sc[(i >> 6) * sstride<T>() + (i & 63)] =
+            lapf * h * (T)0.5 * st[i & 63] + massf * h * h * h * (T)0.125 * st[64 + (i & 63)];
+      }
+    }
     if (lane == 0) ws_first[par][wid] = (ent(0) & ENT_START) ? 1 : 0;
     if (tid == 0) ws_first[par][NW] = 1;
     __syncthreads();
@@ -201,9 +259,13 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
       T xv[8];
 #pragma unroll
       for (int m = 0; m < 8; m++) xv[m] = buf[((sig >> (3 * m)) & 7u) * PATCH + tid];
-      const T h = exp2_neg((T)0, l);
-      apply_full(cs + t * fsten_stride<T>(), lapf * h * (T)0.5, massf * h * h * h * (T)0.125, xv,
-                 [&](int m, T ym) { buf[((sig >> (3 * m)) & 7u) * PATCH + tid] = ym; });
+      auto put = [&](int m, T ym) { buf[((sig >> (3 * m)) & 7u) * PATCH + tid] = ym; };
+      if (comb) {
+        apply_comb(sc + ((cme >> 16) & 255u) * sstride<T>(), xv, put);
+      } else {
+        const T h = exp2_neg((T)0, l);
+        apply_full(cs + t * fsten_stride<T>(), lapf * h * (T)0.5, massf * h * h * h * (T)0.125, xv, put);
+      }
     }
     __syncthreads();
     // 3. run sums: segmented scan of the threads' trailing partial sums
@@ -282,7 +344,7 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
 template <typename T>
 constexpr size_t patch_smem() {
   return fsten_entries<T>() * sizeof(T) + 2 * PATCH_ENT * sizeof(T) + 2 * PATCH_ENT * sizeof(uint32_t) +
-         8 * 18 * sizeof(uint32_t);
+         (8 * 18 + 4) * sizeof(uint32_t) + PKEY_MAX * sstride<T>() * sizeof(T);
 }
 
 }  // namespace dg

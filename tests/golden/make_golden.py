@@ -19,6 +19,7 @@ import json
 import os
 import re
 import subprocess
+import tempfile
 import sys
 import tempfile
 
@@ -35,8 +36,15 @@ REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 
 
+SCRATCH = tempfile.mkdtemp(prefix="dendro_golden_")
+
+
 def run(*args):
-    r = subprocess.run([DRIVER, *map(str, args)], capture_output=True, text=True, check=True)
+    # the reference's property checks write their failure dumps (.ot, .vtk)
+    # into the working directory: run it in a scratch directory, with
+    # absolute paths for every file argument
+    args = [os.path.abspath(a) if isinstance(a, str) and os.sep in a else a for a in args]
+    r = subprocess.run([DRIVER, *map(str, args)], capture_output=True, text=True, check=True, cwd=SCRATCH)
     return json.loads(r.stdout.strip().splitlines()[-1])
 
 
