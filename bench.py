@@ -150,10 +150,10 @@ def _merge_stats(parts) -> dict:
     return out
 
 
-def _stream():
+def _stream(count: int = SERVE_REQUESTS):
     from dendro_gb300 import serving
 
-    return serving.poisson_stream(SERVE_REQUESTS, rate=SERVE_RATE, lo=SERVE_SIZES[0], hi=SERVE_SIZES[1],
+    return serving.poisson_stream(count, rate=SERVE_RATE, lo=SERVE_SIZES[0], hi=SERVE_SIZES[1],
                                   seed=SERVE_SEED)
 
 
@@ -271,7 +271,7 @@ def run_serving(args, local, barrier):
 
     from dendro_gb300 import serving
 
-    host = _stream()
+    host = _stream(args.serve_requests)
     npts = sum(len(r.points) for r in host)
     dev = f"cuda:{local}"
     on_dev = [torch.from_numpy(r.points).to(dev) for r in host]
@@ -307,20 +307,22 @@ def run_serving(args, local, barrier):
     batches = list(srv.batches)
     # the same stream from pinned host memory (copies in, results out)
     e2e_walls = []
-    replay(srv, pinned)
-    for _ in range(args.steps):
-        _, wall = replay(srv, pinned)
-        e2e_walls.append(wall)
+    if not args.skip_e2e:
+        replay(srv, pinned)
+        for _ in range(args.steps):
+            _, wall = replay(srv, pinned)
+            e2e_walls.append(wall)
     srv.close()
     # the per-call drop-in on the same stream
-    plain = serving.PlainServer(device=local, solve_maxit=SOLVE_MAXIT)
-    replay(plain, on_dev)
     p_walls, p_outs = [], []
-    for _ in range(2):
-        out, wall = replay(plain, on_dev)
-        p_walls.append(wall)
-        p_outs.extend(out)
-    plain.close()
+    if not args.skip_plain:
+        plain = serving.PlainServer(device=local, solve_maxit=SOLVE_MAXIT)
+        replay(plain, on_dev)
+        for _ in range(2):
+            out, wall = replay(plain, on_dev)
+            p_walls.append(wall)
+            p_outs.extend(out)
+        plain.close()
     errors = sum(1 for r in outs + p_outs if r.error)
     ms = 1e3 * sum(walls) / len(walls)
     res = {
@@ -328,17 +330,18 @@ def run_serving(args, local, barrier):
         "points": npts,
         "requests": len(host),
         "value": npts / (ms * 1e-3) / 1e6,
-        "e2e_ms": 1e3 * sum(e2e_walls) / len(e2e_walls),
+        "e2e_ms": 1e3 * sum(e2e_walls) / len(e2e_walls) if e2e_walls else float("nan"),
         "served": {"Mpts_per_s": npts / (ms * 1e-3) / 1e6, **_latency(outs),
                    "mean_batch": float(np.mean(batches)) if batches else None},
-        "plain": {"Mpts_per_s": npts / (1e-3 * 1e3 * sum(p_walls) / len(p_walls)) / 1e6, **_latency(p_outs)},
+        "plain": ({"Mpts_per_s": npts / (sum(p_walls) / len(p_walls)) / 1e6, **_latency(p_outs)} if p_walls
+                  else None),
         "iterations_max": max(r.iterations for r in outs),
         "relres_max": max(r.relres for r in outs),
         "errors": errors,
         "stats": stats,
         "clocks": clocks,
     }
-    res["served_over_plain"] = res["served"]["Mpts_per_s"] / res["plain"]["Mpts_per_s"]
+    res["served_over_plain"] = (res["served"]["Mpts_per_s"] / res["plain"]["Mpts_per_s"]) if p_walls else None
     return res
 
 
@@ -426,7 +429,7 @@ def run_scale(args, dg, ctx, local):
             ctx.profile(True)
             for _ in range(10):
                 da.matvec(x, y, precision=prec)
-            st = ctx.profile_stats()["matvec"]
+            st = ctx.profile_stats()[f"matvec_fp{prec}"]
             ctx.profile(False)
             kms = st[0] / st[1]
             nbytes = 36 * E + 3 * (prec // 8) * V
@@ -591,6 +594,17 @@ def run_ours(args):
     import dendro_gb300 as dg
 
     ctx = dg.Context(local)
+    if args.skip_serve:  # profiling runs of the other blocks only
+        extra = {}
+        if not args.skip_scale:
+            extra["scale"] = run_scale(args, dg, ctx, local)
+        if not args.skip_batch:
+            extra["batching"] = run_batching(args, dg, ctx, local)
+        if not args.skip_mg:
+            extra["precision"] = run_poisson(args, dg, ctx, local)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": None, "note": "serving skipped", **extra}), flush=True)
+        return
     serve = run_serving(args, local, barrier)
     ms = serve["ms_per_step"]
     e2e_ms = serve["e2e_ms"]
@@ -670,6 +684,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--serve-requests", type=int, default=SERVE_REQUESTS)
+    ap.add_argument("--skip-serve", action="store_true")
+    ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--scale-npts", type=int, default=64_000_000)
     ap.add_argument("--batch-clouds", type=int, default=256)
     ap.add_argument("--poisson-npts", type=int, default=16_000_000)

@@ -572,7 +572,8 @@ void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, 
   const T *cs = std::is_same<T, double>::value ? reinterpret_cast<const T *>(ctx.d_csten64)
                                                : reinterpret_cast<const T *>(ctx.d_csten32);
   {
-    ProfScope _prof(ctx, "matvec", (double)m.n_elem * 36 + (double)m.n_node * 3 * sizeof(T));
+    ProfScope _prof(ctx, sizeof(T) == 4 ? "matvec_fp32" : "matvec_fp64",
+                    (double)m.n_elem * 36 + (double)m.n_node * 3 * sizeof(T));
     k_patch_matvec<T, false><<<grid, PATCH, smem, s>>>(m.pmeta, m.pinc, m.pexc, m.pnode, m.poff, m.pkeys,
                                                        m.pkcount, m.n_elem, m.n_patch, cs, ctx.d_cperm, nullptr, x,
                                                        y, (T)lap_fac, (T)mass_fac);
