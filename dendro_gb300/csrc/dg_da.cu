@@ -198,10 +198,10 @@ void ensure_stencils(Context &ctx) {
 // mesh build
 // ------------------------------------------------------------------------
 __device__ __forceinline__ bool is_leaf_at(const Key128 *__restrict__ keys, size_t n, int64_t x, int64_t y, int64_t z,
-                                           unsigned lev, int64_t dom) {
+                                           unsigned lev, int64_t dom, size_t hint) {
   if (x < 0 || y < 0 || z < 0 || x >= dom || y >= dom || z >= dom) return false;
   Key128 pos = morton3((uint32_t)x, (uint32_t)y, (uint32_t)z);
-  size_t j = find_leaf(keys, n, pos);
+  size_t j = find_leaf_from(keys, n, pos, hint);
   Key128 kj = keys[j];
   return tag_level(kj) == lev && key_eq(tag_anchor(kj), pos);
 }
@@ -233,7 +233,7 @@ __global__ void k_mesh_elems(const Key128 *__restrict__ keys, size_t n, unsigned
         continue;
       }
       leaf[s] = is_leaf_at(keys, n, P[0] + ((s & 1) ? d[0] : 0), P[1] + ((s & 2) ? d[1] : 0),
-                           P[2] + ((s & 4) ? d[2] : 0), l - 1, dom);
+                           P[2] + ((s & 4) ? d[2] : 0), l - 1, dom, e);
     }
 #pragma unroll
     for (int r = 1; r < 7; r++) {
@@ -309,7 +309,7 @@ __global__ void k_mesh_conn(const Key128 *__restrict__ keys, size_t n, unsigned 
         cl[a] = v[a];
       }
     }
-    size_t o = find_leaf(keys, n, morton3((uint32_t)cl[0], (uint32_t)cl[1], (uint32_t)cl[2]));
+    size_t o = find_leaf_from(keys, n, morton3((uint32_t)cl[0], (uint32_t)cl[1], (uint32_t)cl[2]), e);
     const Key128 ko = keys[o];
     const unsigned lo_ = tag_level(ko);
     uint32_t ox, oy, oz;
@@ -346,21 +346,56 @@ __global__ void k_node_incidence(const uint32_t *__restrict__ conn, size_t n8, u
 // then a bitonic sort of its (node << 12 | slot) keys in shared memory, run
 // starts, run lengths against the node's mesh-wide pair count, and the
 // packed entries
+// Bitonic sort of BLOCK * I keys held I per thread (key I*t + j in v[j] of
+// thread t), ascending.  Compare-exchanges with partners in the same thread
+// run in registers, those within a warp by shuffles, and only the strides
+// that cross warps go through shared memory (`stage`, BLOCK * I keys).
 template <typename K>
-__device__ __forceinline__ void block_bitonic(K *a, int n) {
-  for (int size = 2; size <= n; size <<= 1)
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      for (int i = threadIdx.x; i < n / 2; i += blockDim.x) {
-        const int lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
-        const bool asc = (lo & size) == 0;
-        const K x = a[lo], y = a[hi];
-        if ((x > y) == asc) {
-          a[lo] = y;
-          a[hi] = x;
-        }
+__device__ __forceinline__ K keep_of(K mine, K other, bool keep_min) {
+  return keep_min ? (other < mine ? other : mine) : (other > mine ? other : mine);
+}
+
+template <typename K, int I, int BLOCK>
+__device__ void block_sort_regs(K (&v)[I], K *stage) {
+  constexpr int N = BLOCK * I;
+  const int t = threadIdx.x;
+  for (int s = 2; s <= N; s <<= 1) {
+    int d = s >> 1;
+    for (; d >= 32 * I; d >>= 1) {  // across warps
+#pragma unroll
+      for (int j = 0; j < I; j++) stage[I * t + j] = v[j];
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < I; j++) {
+        const int i = I * t + j;
+        v[j] = keep_of(v[j], stage[i ^ d], ((i & d) == 0) == ((i & s) == 0));
       }
       __syncthreads();
     }
+    for (; d >= I; d >>= 1) {  // within a warp
+#pragma unroll
+      for (int j = 0; j < I; j++) {
+        const int i = I * t + j;
+        const K o = __shfl_xor_sync(0xffffffffu, v[j], d / I);
+        v[j] = keep_of(v[j], o, ((i & d) == 0) == ((i & s) == 0));
+      }
+    }
+#pragma unroll
+    for (int dd = I / 2; dd > 0; dd >>= 1) {  // within the thread
+      if (dd < s) {
+#pragma unroll
+        for (int j = 0; j < I; j++) {
+          if (j & dd) continue;
+          const bool up = (((I * t + j) & s) == 0);
+          const K a = v[j], b = v[j | dd];
+          if ((a > b) == up) {
+            v[j] = b;
+            v[j | dd] = a;
+          }
+        }
+      }
+    }
+  }
 }
 
 __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict__ conn,
@@ -379,15 +414,19 @@ __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict
   const size_t e0 = p * PATCH;
   const int ne = (int)((E - e0) < (size_t)PATCH ? (E - e0) : (size_t)PATCH);
   // element order: (type, level, index); missing elements last
-  uint32_t me = 0;
-  if (tid < ne) {
-    me = meta[e0 + tid];
-    ek[tid] = ((me >> 24) << 5 | (me & 31u)) << 9 | (uint32_t)tid;
-  } else {
-    ek[tid] = 0xffffffffu;
+  {
+    uint32_t k1[1];
+    if (tid < ne) {
+      const uint32_t me = meta[e0 + tid];
+      k1[0] = ((me >> 24) << 5 | (me & 31u)) << 9 | (uint32_t)tid;
+    } else {
+      k1[0] = 0xffffffffu;
+    }
+    block_sort_regs<uint32_t, 1, PATCH>(k1, ek);
+    __syncthreads();
+    ek[tid] = k1[0];
+    __syncthreads();
   }
-  __syncthreads();
-  block_bitonic<uint32_t>(ek, PATCH);
   // (type, level) groups of the ordered elements: the patch's stencil keys
   const uint32_t grp = ek[tid] >> 9;
   const int gstart = tid < ne && (tid == 0 || (ek[tid - 1] >> 9) != grp) ? 1 : 0;
@@ -402,13 +441,19 @@ __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict
   }
   if (tid == 0) pkcount[p] = (uint16_t)nkeys;
   __syncthreads();
+  {
+    uint64_t k8[8];
 #pragma unroll
-  for (int k = 0; k < 8; k++) {
-    const int i = k * PATCH + (tid < ne ? rank[tid] : tid);
-    sk[k * PATCH + tid] = tid < ne ? ((uint64_t)conn[(size_t)k * E + e0 + tid] << 12 | (uint64_t)i) : ~0ull;
+    for (int k = 0; k < 8; k++) {
+      const int i = k * PATCH + (tid < ne ? rank[tid] : tid);
+      k8[k] = tid < ne ? ((uint64_t)conn[(size_t)k * E + e0 + tid] << 12 | (uint64_t)i) : ~0ull;
+    }
+    block_sort_regs<uint64_t, 8, PATCH>(k8, sk);
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 8; j++) sk[8 * tid + j] = k8[j];
+    __syncthreads();
   }
-  __syncthreads();
-  block_bitonic<uint64_t>(sk, PATCH_ENT);
   const int nent = 8 * ne;
   uint32_t id[8];
   bool st[8];

@@ -53,6 +53,45 @@ __device__ __forceinline__ size_t find_leaf(const Key128 *__restrict__ keys, siz
   return lo ? lo - 1 : 0;
 }
 
+// the same index as find_leaf, searched outward from `hint` (doubling steps,
+// then bisection): a leaf near the hint in Morton order costs a few nearby
+// probes instead of a bisection of the whole array
+__device__ __forceinline__ size_t find_leaf_from(const Key128 *__restrict__ keys, size_t n, Key128 pos, size_t hint) {
+  size_t lo, hi;  // keys[lo] <= pos < keys[hi] (hi == n: past the end)
+  if (key_le(tag_anchor(keys[hint]), pos)) {
+    lo = hint;
+    hi = n;
+    for (size_t step = 1; hint + step < n; step <<= 1) {
+      if (key_le(tag_anchor(keys[hint + step]), pos)) {
+        lo = hint + step;
+      } else {
+        hi = hint + step;
+        break;
+      }
+    }
+  } else {
+    hi = hint;
+    lo = n;  // none found yet
+    for (size_t step = 1; step <= hint; step <<= 1) {
+      if (key_le(tag_anchor(keys[hint - step]), pos)) {
+        lo = hint - step;
+        break;
+      }
+      hi = hint - step;
+    }
+    if (lo == n) {
+      if (!key_le(tag_anchor(keys[0]), pos)) return 0;  // pos precedes every leaf
+      lo = 0;
+    }
+  }
+  while (hi - lo > 1) {
+    const size_t mid = lo + (hi - lo) / 2;
+    if (key_le(tag_anchor(keys[mid]), pos)) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
 // device stencil layout: for each (child, type) a 128-entry block, 64
 // Laplacian then 64 mass entries, row-major 8x8
 constexpr int STEN_ENTRIES = 8 * 18 * 128;

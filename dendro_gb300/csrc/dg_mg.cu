@@ -174,20 +174,6 @@ __global__ void k_residual(const T *__restrict__ b, const T *__restrict__ ax, T 
   if (i < n) r[i] = b[i] - ax[i];
 }
 
-// x = A^-1 b with the dense inverse of the coarsest level, one warp per row
-template <typename T>
-__global__ void k_gemv(const T *__restrict__ A, size_t n, const T *__restrict__ b, T *__restrict__ x) {
-  size_t row = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (row >= n) return;
-  const T *a = A + row * n;
-  T acc = 0;
-  for (size_t j = lane; j < n; j += 32) acc += a[j] * b[j];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) x[row] = acc;
-}
-
 __global__ void k_assemble_dense(const uint32_t *__restrict__ meta, const uint32_t *__restrict__ conn, size_t E,
                                  const double *__restrict__ sten, const uint8_t *__restrict__ bdy, size_t n,
                                  double *__restrict__ A) {
@@ -215,26 +201,171 @@ __global__ void k_set_bdy_identity(const uint8_t *__restrict__ bdy, size_t n, do
   if (i < n && bdy[i]) A[i * n + i] = 1.0;
 }
 
-// in-place Gauss-Jordan inversion (no pivoting: the operator is SPD)
-__global__ void k_gj_col(const double *__restrict__ A, size_t n, size_t p, double *__restrict__ col) {
-  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) col[i] = A[i * n + p];
+// ---- coarsest level: FP32 inverse by block Gauss-Jordan, FP64 refinement
+// In-place block Gauss-Jordan (no pivoting: the operator is SPD).  For each
+// block K of GJB pivots, with R the other indices and P = inv(X_KK):
+//   X_RR -= (X_RK P) X_KR,  X_KR = P X_KR,  X_RK = -(X_RK P),  X_KK = P;
+// after the last block X holds the inverse.  The X_RR update is a tiled
+// rank-GJB product, so the inverse costs n^3 FP32 multiply-adds in n / GJB
+// steps of five launches.
+constexpr int GJB = 64;
+
+__global__ void __launch_bounds__(256) k_bgj_diag(const float *__restrict__ X, size_t n, size_t k0, int b,
+                                                  float *__restrict__ P) {
+  __shared__ float S[GJB][GJB + 1];
+  for (int q = threadIdx.x; q < b * b; q += 256) S[q / b][q % b] = X[(k0 + q / b) * n + k0 + q % b];
+  __syncthreads();
+  for (int p = 0; p < b; p++) {
+    const float inv = 1.0f / S[p][p];
+    float nv[GJB * GJB / 256];
+#pragma unroll
+    for (int it = 0; it < GJB * GJB / 256; it++) {
+      const int q = threadIdx.x + 256 * it;
+      if (q < b * b) {
+        const int r = q / b, c = q % b;
+        float v;
+        if (r == p && c == p) v = inv;
+        else if (r == p) v = S[p][c] * inv;
+        else if (c == p) v = -S[r][p] * inv;
+        else v = S[r][c] - S[r][p] * S[p][c] * inv;
+        nv[it] = v;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < GJB * GJB / 256; it++) {
+      const int q = threadIdx.x + 256 * it;
+      if (q < b * b) S[q / b][q % b] = nv[it];
+    }
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < b * b; q += 256) P[q] = S[q / b][q % b];
 }
-__global__ void k_gj_row(double *__restrict__ A, size_t n, size_t p, const double *__restrict__ col) {
-  size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
-  const double inv = 1.0 / col[p];
-  double v = (j == p) ? 1.0 : A[p * n + j];
-  A[p * n + j] = v * inv;
+
+// U[i][:] = X[i][K] P for rows i outside K (one block of GJB threads per row)
+__global__ void k_bgj_u(const float *__restrict__ X, size_t n, size_t k0, int b, const float *__restrict__ P,
+                        float *__restrict__ U) {
+  const size_t i = blockIdx.x;
+  if (i >= k0 && i < k0 + (size_t)b) return;
+  __shared__ float xs[GJB];
+  const int j = threadIdx.x;
+  if (j < b) xs[j] = X[i * n + k0 + j];
+  __syncthreads();
+  if (j < b) {
+    float acc = 0.f;
+    for (int m = 0; m < b; m++) acc += xs[m] * P[m * b + j];
+    U[i * GJB + j] = acc;
+  }
 }
-__global__ void k_gj_update(double *__restrict__ A, size_t n, size_t p, const double *__restrict__ col) {
-  size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= n * n) return;
-  size_t i = idx / n, j = idx % n;
-  if (i == p) return;
-  const double f = col[i];
-  double a = (j == p) ? 0.0 : A[i * n + j];
-  A[i * n + j] = a - f * A[p * n + j];
+
+// X[i][j] -= sum_m U[i][m] X[K_m][j] for i, j outside K: 64 x 64 tiles, 4 x 4 per thread
+__global__ void __launch_bounds__(256) k_bgj_update(float *__restrict__ X, size_t n, size_t k0, int b,
+                                                    const float *__restrict__ U) {
+  __shared__ __align__(16) float Ut[GJB][64 + 4];
+  __shared__ __align__(16) float Bs[GJB][64 + 4];
+  const size_t i0 = (size_t)blockIdx.y * 64, j0 = (size_t)blockIdx.x * 64;
+  const int tid = threadIdx.x;
+  for (int q = tid; q < 64 * GJB; q += 256) {
+    const int r = q / GJB, m = q % GJB;
+    Ut[m][r] = (m < b && i0 + r < n) ? U[(i0 + r) * GJB + m] : 0.f;
+  }
+  for (int q = tid; q < GJB * 64; q += 256) {
+    const int m = q / 64, c = q % 64;
+    Bs[m][c] = (m < b && j0 + c < n) ? X[(k0 + m) * n + j0 + c] : 0.f;
+  }
+  __syncthreads();
+  const int ty = tid / 16, tx = tid % 16;
+  float acc[4][4] = {};
+  for (int m = 0; m < b; m++) {
+    const float4 a = *reinterpret_cast<const float4 *>(&Ut[m][ty * 4]);
+    const float4 c4 = *reinterpret_cast<const float4 *>(&Bs[m][tx * 4]);
+    const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) acc[r][c] = fmaf(av[r], bv[c], acc[r][c]);
+  }
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    const size_t i = i0 + ty * 4 + r;
+    if (i >= n || (i >= k0 && i < k0 + (size_t)b)) continue;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const size_t j = j0 + tx * 4 + c;
+      if (j < n && !(j >= k0 && j < k0 + (size_t)b)) X[i * n + j] -= acc[r][c];
+    }
+  }
+}
+
+// X[K_r][j] = sum_m P[r][m] X[K_m][j] for columns j outside K (64 columns per block)
+__global__ void __launch_bounds__(256) k_bgj_row(float *__restrict__ X, size_t n, size_t k0, int b,
+                                                 const float *__restrict__ P) {
+  __shared__ float Ps[GJB][GJB + 1];
+  __shared__ float Bs[GJB][64 + 1];
+  const size_t j0 = (size_t)blockIdx.x * 64;
+  for (int q = threadIdx.x; q < b * b; q += 256) Ps[q / b][q % b] = P[q];
+  for (int q = threadIdx.x; q < b * 64; q += 256) {
+    const int m = q / 64, c = q % 64;
+    Bs[m][c] = (j0 + c < n) ? X[(k0 + m) * n + j0 + c] : 0.f;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < b * 64; q += 256) {
+    const int r = q / 64, c = q % 64;
+    const size_t j = j0 + c;
+    if (j >= n || (j >= k0 && j < k0 + (size_t)b)) continue;
+    float acc = 0.f;
+    for (int m = 0; m < b; m++) acc = fmaf(Ps[r][m], Bs[m][c], acc);
+    X[(k0 + r) * n + j] = acc;
+  }
+}
+
+// X[i][K] = -U[i][:] for rows outside K, X[K][K] = P
+__global__ void k_bgj_col(float *__restrict__ X, size_t n, size_t k0, int b, const float *__restrict__ P,
+                          const float *__restrict__ U) {
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n * (size_t)b) return;
+  const size_t i = q / b;
+  const int j = (int)(q % b);
+  X[i * n + k0 + j] = (i >= k0 && i < k0 + (size_t)b) ? P[(i - k0) * b + j] : -U[i * GJB + j];
+}
+
+// coarse solve x = A^-1 b to FP64 accuracy: x = X b, then CS_REFINE rounds of
+// r = b - A x (FP64), x += X r, with X the FP32 inverse and A the assembled
+// FP64 operator; one warp per row
+constexpr int CS_REFINE = 4;
+
+template <typename T>
+__global__ void k_cs_apply(const float *__restrict__ Xi, size_t n, const T *__restrict__ v, double *__restrict__ x,
+                           bool accumulate) {
+  const size_t row = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const float *a = Xi + row * n;
+  double acc = 0.0;
+  for (size_t j = lane; j < n; j += 32) acc = fma((double)a[j], (double)v[j], acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) x[row] = accumulate ? x[row] + acc : acc;
+}
+
+template <typename T>
+__global__ void k_cs_resid(const double *__restrict__ A, size_t n, const T *__restrict__ b,
+                           const double *__restrict__ x, double *__restrict__ r) {
+  const size_t row = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const double *a = A + row * n;
+  double acc = 0.0;
+  for (size_t j = lane; j < n; j += 32) acc = fma(a[j], x[j], acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) r[row] = (double)b[row] - acc;
+}
+
+template <typename T>
+__global__ void k_cs_out(const double *__restrict__ x, size_t n, T *__restrict__ out) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (T)x[i];
 }
 
 __global__ void k_to_float(const double *__restrict__ a, size_t n, float *__restrict__ b) {
@@ -348,6 +479,7 @@ namespace {
 template <typename T>
 struct VWork {
   std::vector<DBuf<T>> b, x, ax;
+  DBuf<double> cx, cr;  // coarse solve iterate and residual (FP64)
 };
 
 template <typename T>
@@ -361,10 +493,14 @@ void vcycle_level(Context &ctx, const MG &mg, VWork<T> &w, int l, const T *b, T 
   const MGLevel &L = mg.lv[l];
   const size_t n = L.mesh.n_node;
   if (l + 1 == (int)mg.lv.size()) {
-    const T *Ainv = std::is_same<T, double>::value ? reinterpret_cast<const T *>(mg.cinv64)
-                                                   : reinterpret_cast<const T *>(mg.cinv32);
-    ProfScope _prof(ctx, "mg_coarse_solve", (double)n * n * sizeof(T));
-    k_gemv<T><<<grid_for(n * 32, 256), 256, 0, s>>>(Ainv, n, b, x);
+    ProfScope _prof(ctx, "mg_coarse_solve", (double)n * n * (4 + CS_REFINE * 12));
+    const unsigned gw = grid_for(n * 32, 256);
+    k_cs_apply<T><<<gw, 256, 0, s>>>(mg.cinv32, n, b, w.cx.get(), false);
+    for (int it = 0; it < CS_REFINE; it++) {
+      k_cs_resid<T><<<gw, 256, 0, s>>>(mg.ca64, n, b, w.cx.get(), w.cr.get());
+      k_cs_apply<double><<<gw, 256, 0, s>>>(mg.cinv32, n, w.cr.get(), w.cx.get(), true);
+    }
+    k_cs_out<T><<<grid_for(n, 256), 256, 0, s>>>(w.cx.get(), n, x);
     DG_LAUNCH_CHECK();
     return;
   }
@@ -409,6 +545,8 @@ VWork<T> make_work(Context &ctx, const MG &mg) {
     w.x.emplace_back(n, ctx.stream);
     w.ax.emplace_back(n, ctx.stream);
   }
+  w.cx.alloc(mg.nc ? mg.nc : 1, ctx.stream);
+  w.cr.alloc(mg.nc ? mg.nc : 1, ctx.stream);
   return w;
 }
 
@@ -431,7 +569,7 @@ void mg_free(Context &ctx, MG &mg) {
     if (L.pid) cudaFreeAsync(L.pid, ctx.stream);
     if (L.pw) cudaFreeAsync(L.pw, ctx.stream);
   }
-  if (mg.cinv64) cudaFreeAsync(mg.cinv64, ctx.stream);
+  if (mg.ca64) cudaFreeAsync(mg.ca64, ctx.stream);
   if (mg.cinv32) cudaFreeAsync(mg.cinv32, ctx.stream);
   cudaStreamSynchronize(ctx.stream);
   mg = MG();
@@ -500,23 +638,30 @@ void mg_setup(Context &ctx, const Octree &fine, size_t max_coarse_elem, MG &mg) 
     const size_t n = C.mesh.n_node;
     if (n > 20000) fail(DG_ERR_INVALID_ARG, "multigrid: coarsest level too large for the dense solve");
     mg.nc = n;
-    DG_CUDA(cudaMallocAsync((void **)&mg.cinv64, n * n * sizeof(double), s));
+    DG_CUDA(cudaMallocAsync((void **)&mg.ca64, n * n * sizeof(double), s));
     DG_CUDA(cudaMallocAsync((void **)&mg.cinv32, n * n * sizeof(float), s));
-    DG_CUDA(cudaMemsetAsync(mg.cinv64, 0, n * n * sizeof(double), s));
+    DG_CUDA(cudaMemsetAsync(mg.ca64, 0, n * n * sizeof(double), s));
     k_assemble_dense<<<grid_for(C.mesh.n_elem, 128), 128, 0, s>>>(C.mesh.meta, C.mesh.conn, C.mesh.n_elem,
-                                                                   ctx.d_sten64, C.bdy, n, mg.cinv64);
+                                                                   ctx.d_sten64, C.bdy, n, mg.ca64);
     DG_LAUNCH_CHECK();
-    k_set_bdy_identity<<<grid_for(n, 256), 256, 0, s>>>(C.bdy, n, mg.cinv64);
+    k_set_bdy_identity<<<grid_for(n, 256), 256, 0, s>>>(C.bdy, n, mg.ca64);
     DG_LAUNCH_CHECK();
-    DBuf<double> col(n, s);
-    for (size_t p = 0; p < n; p++) {
-      k_gj_col<<<grid_for(n, 256), 256, 0, s>>>(mg.cinv64, n, p, col.get());
-      k_gj_row<<<grid_for(n, 256), 256, 0, s>>>(mg.cinv64, n, p, col.get());
-      k_gj_update<<<grid_for(n * n, 256), 256, 0, s>>>(mg.cinv64, n, p, col.get());
+    k_to_float<<<grid_for(n * n, 256), 256, 0, s>>>(mg.ca64, n * n, mg.cinv32);
+    DG_LAUNCH_CHECK();
+    {
+      ProfScope _prof_inv(ctx, "mg_coarse_inverse", (double)n * n * 4 * 2 * ((n + GJB - 1) / GJB));
+      DBuf<float> P(GJB * GJB, s), U(n * GJB, s);
+      const unsigned nt = (unsigned)((n + 63) / 64);
+      for (size_t k0 = 0; k0 < n; k0 += GJB) {
+        const int b = (int)std::min<size_t>(GJB, n - k0);
+        k_bgj_diag<<<1, 256, 0, s>>>(mg.cinv32, n, k0, b, P.get());
+        k_bgj_u<<<(unsigned)n, GJB, 0, s>>>(mg.cinv32, n, k0, b, P.get(), U.get());
+        k_bgj_update<<<dim3(nt, nt), 256, 0, s>>>(mg.cinv32, n, k0, b, U.get());
+        k_bgj_row<<<nt, 256, 0, s>>>(mg.cinv32, n, k0, b, P.get());
+        k_bgj_col<<<grid_for(n * b, 256), 256, 0, s>>>(mg.cinv32, n, k0, b, P.get(), U.get());
+      }
+      DG_LAUNCH_CHECK();
     }
-    DG_LAUNCH_CHECK();
-    k_to_float<<<grid_for(n * n, 256), 256, 0, s>>>(mg.cinv64, n * n, mg.cinv32);
-    DG_LAUNCH_CHECK();
     DG_CUDA(cudaStreamSynchronize(s));
   } catch (...) {
     mg_free(ctx, mg);

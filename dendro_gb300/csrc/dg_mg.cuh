@@ -26,8 +26,8 @@ struct MGLevel {
 struct MG {
   std::vector<MGLevel> lv;  // 0 = finest
   size_t nc = 0;            // nodes of the coarsest level
-  double *cinv64 = nullptr;  // dense inverse of the coarsest operator
-  float *cinv32 = nullptr;
+  double *ca64 = nullptr;    // the coarsest level's assembled operator (dense, FP64)
+  float *cinv32 = nullptr;   // its inverse in FP32 (refined in FP64 when applied)
   double omega = 0.667;  // Jacobi damping (bin/options:190)
   int nu_pre = 2, nu_post = 2;
 };
