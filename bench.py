@@ -532,7 +532,7 @@ def run_poisson(args, dg, ctx, local):
     t_setup = time.perf_counter() - t0
     ctx.profile(True)  # a second set-up, timed per kernel
     dg.MultiGrid(bal, max_coarse_elems=4096, ctx=ctx).free()
-    setup_kernels = _top_kernels(ctx.profile_stats(), 14)
+    setup_kernels = _top_kernels(ctx.profile_stats(), 20)
     ctx.profile(False)
     bal.free()
     f = datagen.bumps(mg.level_nodes(0, device=True))

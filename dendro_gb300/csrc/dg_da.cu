@@ -198,10 +198,10 @@ void ensure_stencils(Context &ctx) {
 // mesh build
 // ------------------------------------------------------------------------
 __device__ __forceinline__ bool is_leaf_at(const Key128 *__restrict__ keys, size_t n, int64_t x, int64_t y, int64_t z,
-                                           unsigned lev, int64_t dom, size_t hint) {
+                                           unsigned lev, int64_t dom) {
   if (x < 0 || y < 0 || z < 0 || x >= dom || y >= dom || z >= dom) return false;
   Key128 pos = morton3((uint32_t)x, (uint32_t)y, (uint32_t)z);
-  size_t j = find_leaf_from(keys, n, pos, hint);
+  size_t j = find_leaf(keys, n, pos);
   Key128 kj = keys[j];
   return tag_level(kj) == lev && key_eq(tag_anchor(kj), pos);
 }
@@ -233,7 +233,7 @@ __global__ void k_mesh_elems(const Key128 *__restrict__ keys, size_t n, unsigned
         continue;
       }
       leaf[s] = is_leaf_at(keys, n, P[0] + ((s & 1) ? d[0] : 0), P[1] + ((s & 2) ? d[1] : 0),
-                           P[2] + ((s & 4) ? d[2] : 0), l - 1, dom, e);
+                           P[2] + ((s & 4) ? d[2] : 0), l - 1, dom);
     }
 #pragma unroll
     for (int r = 1; r < 7; r++) {

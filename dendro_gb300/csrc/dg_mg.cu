@@ -210,36 +210,45 @@ __global__ void k_set_bdy_identity(const uint8_t *__restrict__ bdy, size_t n, do
 // steps of five launches.
 constexpr int GJB = 64;
 
+// P = inv(X_KK) for one diagonal block (one CTA of 256 threads): thread t
+// holds 16 entries of row t / 4 in registers; per pivot the pivot row goes
+// through shared memory (double-buffered, one barrier) and each row's pivot
+// column entry comes by a shuffle within the row's four threads.  A partial
+// last block is padded with the identity.
 __global__ void __launch_bounds__(256) k_bgj_diag(const float *__restrict__ X, size_t n, size_t k0, int b,
                                                   float *__restrict__ P) {
-  __shared__ float S[GJB][GJB + 1];
-  for (int q = threadIdx.x; q < b * b; q += 256) S[q / b][q % b] = X[(k0 + q / b) * n + k0 + q % b];
-  __syncthreads();
-  for (int p = 0; p < b; p++) {
-    const float inv = 1.0f / S[p][p];
-    float nv[GJB * GJB / 256];
+  static_assert(GJB == 64, "one CTA of 256 threads covers a 64 x 64 block");
+  __shared__ float prow[2][GJB];
+  const int t = threadIdx.x, r = t >> 2, c0 = (t & 3) * 16;
+  const int lane = t & 31, base = lane & ~3;
+  float v[16];
 #pragma unroll
-    for (int it = 0; it < GJB * GJB / 256; it++) {
-      const int q = threadIdx.x + 256 * it;
-      if (q < b * b) {
-        const int r = q / b, c = q % b;
-        float v;
-        if (r == p && c == p) v = inv;
-        else if (r == p) v = S[p][c] * inv;
-        else if (c == p) v = -S[r][p] * inv;
-        else v = S[r][c] - S[r][p] * S[p][c] * inv;
-        nv[it] = v;
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int it = 0; it < GJB * GJB / 256; it++) {
-      const int q = threadIdx.x + 256 * it;
-      if (q < b * b) S[q / b][q % b] = nv[it];
-    }
-    __syncthreads();
+  for (int i = 0; i < 16; i++) {
+    const int c = c0 + i;
+    v[i] = (r < b && c < b) ? X[(k0 + r) * n + k0 + c] : (r == c ? 1.f : 0.f);
   }
-  for (int q = threadIdx.x; q < b * b; q += 256) P[q] = S[q / b][q % b];
+#pragma unroll
+  for (int p = 0; p < GJB; p++) {
+    float *pr = prow[p & 1];
+    if (r == p) {
+#pragma unroll
+      for (int i = 0; i < 16; i++) pr[c0 + i] = v[i];
+    }
+    __syncthreads();
+    const float inv = 1.0f / pr[p];
+    const float f = __shfl_sync(0xffffffffu, v[p & 15], base | (p >> 4));  // this row's entry in column p
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      const int c = c0 + i;
+      if (r == p) v[i] = (c == p) ? inv : v[i] * inv;
+      else v[i] = (c == p) ? -f * inv : v[i] - f * pr[c] * inv;
+    }
+  }
+  if (r < b) {
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+      if (c0 + i < b) P[r * b + c0 + i] = v[i];
+  }
 }
 
 // U[i][:] = X[i][K] P for rows i outside K (one block of GJB threads per row)
@@ -654,11 +663,26 @@ void mg_setup(Context &ctx, const Octree &fine, size_t max_coarse_elem, MG &mg) 
       const unsigned nt = (unsigned)((n + 63) / 64);
       for (size_t k0 = 0; k0 < n; k0 += GJB) {
         const int b = (int)std::min<size_t>(GJB, n - k0);
-        k_bgj_diag<<<1, 256, 0, s>>>(mg.cinv32, n, k0, b, P.get());
-        k_bgj_u<<<(unsigned)n, GJB, 0, s>>>(mg.cinv32, n, k0, b, P.get(), U.get());
-        k_bgj_update<<<dim3(nt, nt), 256, 0, s>>>(mg.cinv32, n, k0, b, U.get());
-        k_bgj_row<<<nt, 256, 0, s>>>(mg.cinv32, n, k0, b, P.get());
-        k_bgj_col<<<grid_for(n * b, 256), 256, 0, s>>>(mg.cinv32, n, k0, b, P.get(), U.get());
+        {
+          ProfScope _p(ctx, "bgj_diag", (double)b * b * 8);
+          k_bgj_diag<<<1, 256, 0, s>>>(mg.cinv32, n, k0, b, P.get());
+        }
+        {
+          ProfScope _p(ctx, "bgj_u", (double)n * b * 8);
+          k_bgj_u<<<(unsigned)n, GJB, 0, s>>>(mg.cinv32, n, k0, b, P.get(), U.get());
+        }
+        {
+          ProfScope _p(ctx, "bgj_update", (double)n * n * 8);
+          k_bgj_update<<<dim3(nt, nt), 256, 0, s>>>(mg.cinv32, n, k0, b, U.get());
+        }
+        {
+          ProfScope _p(ctx, "bgj_row", (double)n * b * 8);
+          k_bgj_row<<<nt, 256, 0, s>>>(mg.cinv32, n, k0, b, P.get());
+        }
+        {
+          ProfScope _p(ctx, "bgj_col", (double)n * b * 8);
+          k_bgj_col<<<grid_for(n * b, 256), 256, 0, s>>>(mg.cinv32, n, k0, b, P.get(), U.get());
+        }
       }
       DG_LAUNCH_CHECK();
     }
