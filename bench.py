@@ -287,7 +287,7 @@ def run_serving(args, local, barrier):
         torch.cuda.synchronize()
         return out, time.perf_counter() - t0
 
-    srv = serving.BatchingServer(device=local, workers=3, solve_maxit=SOLVE_MAXIT)
+    srv = serving.BatchingServer(device=local, workers=args.serve_workers, solve_maxit=SOLVE_MAXIT)
     for _ in range(args.warmup):
         replay(srv, on_dev)
     ctxs = [srv.ctx] + srv.worker_ctx
@@ -685,6 +685,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--serve-requests", type=int, default=SERVE_REQUESTS)
+    ap.add_argument("--serve-workers", type=int, default=3, help="solver streams of the batching server")
     ap.add_argument("--skip-serve", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")

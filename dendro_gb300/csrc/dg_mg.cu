@@ -341,7 +341,7 @@ __global__ void k_bgj_col(float *__restrict__ X, size_t n, size_t k0, int b, con
 // coarse solve x = A^-1 b to FP64 accuracy: x = X b, then CS_REFINE rounds of
 // r = b - A x (FP64), x += X r, with X the FP32 inverse and A the assembled
 // FP64 operator; one warp per row
-constexpr int CS_REFINE = 4;
+constexpr int CS_REFINE = 3;
 
 template <typename T>
 __global__ void k_cs_apply(const float *__restrict__ Xi, size_t n, const T *__restrict__ v, double *__restrict__ x,
