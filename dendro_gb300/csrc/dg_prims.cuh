@@ -375,7 +375,7 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_digit_hists(const K *__restrict
 // order, then written out so that consecutive threads write consecutive
 // addresses of each digit's run.
 template <typename K>
-__global__ void __launch_bounds__(RS_BLOCK) k_rs_onesweep(const K *__restrict__ in, K *__restrict__ out, size_t n,
+__global__ void __launch_bounds__(RS_BLOCK, 4) k_rs_onesweep(const K *__restrict__ in, K *__restrict__ out, size_t n,
                                                           int shift, const uint64_t *__restrict__ digit_off,
                                                           uint64_t *__restrict__ status, unsigned *tile_counter,
                                                           uint32_t *flags) {
