@@ -59,6 +59,13 @@ SERVE_SIZES = (1e4, 8e6)
 SERVE_SEED = 4
 SOLVE_MAXIT = 50
 REF_MAX_POINTS = 40_000  # reference arm: requests of the stream up to this size
+# DRAM bytes per algorithmic byte, from one ncu capture of each kernel
+# (profiles/ncu_patch_matvec_fp32_and_onesweep.md): 774.6 MB for a
+# 2.20e7-element / 1.48e7-node Dirichlet FP32 launch (36 E + 12 V = 969.0 MB
+# algorithmic), 485.2 MB for a 1.6e7-key onesweep pass (512 MB); the traffic
+# grows with the elements / keys a launch processes, so the ratio scales it
+# to the bench's average launch
+TRAFFIC_PER_ALG_BYTE = {"dirichlet_matvec_fp32": 774.6 / 969.0, "rs_onesweep": 485.2 / 512.0}
 
 
 def _peaks():
@@ -403,7 +410,9 @@ def run_scale(args, dg, ctx, local):
            "build_balance_Mpts_per_s": npts / (ms * 1e-3) / 1e6, "ms_per_step": ms,
            "e2e_Mpts_per_s": npts / (sum(e2e) / len(e2e)) / 1e6,
            "top_kernel": {"name": top, "ms_per_launch": tms / tcnt, "GB/s": tbytes / (tms * 1e-3) / 1e9,
-                          "frac_of_measured_peak": tbytes / (tms * 1e-3) / 1e9 / peak},
+                          "frac_of_measured_peak": tbytes / (tms * 1e-3) / 1e9 / peak,
+                          "traffic_per_launch": (TRAFFIC_PER_ALG_BYTE[top] * tbytes / tcnt
+                                                 if top in TRAFFIC_PER_ALG_BYTE else None)},
            "kernels": kernels}
     if not args.skip_da:
         lin = dg.points2Octree(dev, maxDepth=30, maxNumPtsPerOctant=1, ctx=ctx)
@@ -664,7 +673,11 @@ def run_ours(args):
                     "h2d_bytes_per_step": 24 * serve["points"], "d2h_bytes_per_step": 24 * serve["requests"]},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": tname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": (TRAFFIC_PER_ALG_BYTE[tname] * per_launch_bytes
+                                     if tname in TRAFFIC_PER_ALG_BYTE else None),
+                         "traffic_source": ("ncu capture of a smaller launch, scaled by algorithmic bytes"
+                                            if tname in TRAFFIC_PER_ALG_BYTE else None),
                          "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms},
             "clocks": serve["clocks"],
             "cpu_baseline": cpu,
@@ -685,7 +698,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--serve-requests", type=int, default=SERVE_REQUESTS)
-    ap.add_argument("--serve-workers", type=int, default=3, help="solver streams of the batching server")
+    ap.add_argument("--serve-workers", type=int, default=6, help="solver streams of the batching server")
     ap.add_argument("--skip-serve", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
