@@ -5,9 +5,11 @@ Morton sort -> ot::points2Octree -> ot::balanceOctree(incCorner) -> ot::DA
 C ABI of include/dendro_gb300.h.
 """
 from .api import (DA, Context, DendroError, MultiGrid, Octree, balanceOctree, coarsenOctree, default_context,
-                  points2Octree, points2OctreeBatch, sortUniquePoints)
+                  points2Octree, points2OctreeBatch, readNodesFromFile, readNodesFromFile_binary, readPtsFromFile,
+                  sortUniquePoints, writeNodesToFile, writeNodesToFile_binary, writePtsToFile)
 
 __all__ = [
     "DA", "Context", "DendroError", "MultiGrid", "Octree", "balanceOctree", "coarsenOctree", "default_context", "points2Octree", "points2OctreeBatch",
-    "sortUniquePoints",
+    "sortUniquePoints", "readPtsFromFile", "writePtsToFile", "readNodesFromFile", "writeNodesToFile",
+    "readNodesFromFile_binary", "writeNodesToFile_binary",
 ]

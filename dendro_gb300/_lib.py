@@ -75,6 +75,13 @@ def _declare(L):
         "dg_octree_download": ([P, P, P, I], I),
         "dg_octree_upload": ([P, P, SZ, U, I, PP], I),
         "dg_octree_free": ([P, P], I),
+        "dg_pts_file_count": ([ctypes.c_char_p, ctypes.POINTER(SZ)], I),
+        "dg_pts_file_read": ([P, ctypes.c_char_p, P, SZ, I, ctypes.POINTER(SZ)], I),
+        "dg_pts_file_write": ([P, ctypes.c_char_p, P, SZ, I], I),
+        "dg_octree_write_text": ([P, P, ctypes.c_char_p], I),
+        "dg_octree_read_text": ([P, ctypes.c_char_p, PP], I),
+        "dg_octree_write_binary": ([P, P, ctypes.c_char_p], I),
+        "dg_octree_read_binary": ([P, ctypes.c_char_p, PP], I),
         "dg_da_build": ([P, P, PP], I),
         "dg_da_sizes": ([P, ctypes.POINTER(SZ), ctypes.POINTER(SZ)], I),
         "dg_da_download": ([P, P, P, P, P, I], I),

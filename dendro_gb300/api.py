@@ -27,6 +27,12 @@ __all__ = [
     "coarsenOctree",
     "MultiGrid",
     "default_context",
+    "readPtsFromFile",
+    "writePtsToFile",
+    "readNodesFromFile",
+    "writeNodesToFile",
+    "readNodesFromFile_binary",
+    "writeNodesToFile_binary",
 ]
 
 
@@ -246,6 +252,71 @@ def sortUniquePoints(pts, gLens=(1.0, 1.0, 1.0), maxDepth: int = 30, ctx: Contex
     check(ctx.handle, ctx._L.dg_sort_unique_points(ctx.handle, _ptr(a), n, _ptr(g), maxDepth, on_dev, _ptr(out), 0, ctypes.byref(nu)),
           "sortUniquePoints")
     return out[: nu.value].copy()
+
+
+def _path(p) -> bytes:
+    import os
+
+    return os.fsencode(p)
+
+
+def readPtsFromFile(path, device: bool = False, ctx: Context | None = None):
+    """ot::readPtsFromFile (src/octFunctions.cpp:319): the points of a .pts
+    file, (n, 3) FP64 -- numpy, or with ``device`` a CUDA tensor filled
+    through pinned staging buffers."""
+    ctx = ctx or default_context()
+    n = ctypes.c_size_t()
+    check(None, ctx._L.dg_pts_file_count(_path(path), ctypes.byref(n)), "readPtsFromFile")
+    if device:
+        import torch
+
+        out = torch.empty((n.value, 3), dtype=torch.float64, device=f"cuda:{ctx.device}")
+    else:
+        out = np.empty((n.value, 3), np.float64)
+    got = ctypes.c_size_t()
+    check(ctx.handle, ctx._L.dg_pts_file_read(ctx.handle, _path(path), _ptr(out), n.value, 1 if device else 0,
+                                              ctypes.byref(got)), "readPtsFromFile")
+    return out[: got.value]
+
+
+def writePtsToFile(path, pts, ctx: Context | None = None):
+    """ot::writePtsToFile (src/octFunctions.cpp:380); pts is (n, 3) FP64,
+    numpy or a CUDA tensor."""
+    ctx = ctx or default_context()
+    a, n, on_dev = _points_arg(pts)
+    check(ctx.handle, ctx._L.dg_pts_file_write(ctx.handle, _path(path), _ptr(a), n, on_dev), "writePtsToFile")
+
+
+def writeNodesToFile(path, octree: Octree):
+    """ot::writeNodesToFile (src/octFunctions.cpp:496): text, byte for byte
+    as the reference writes it; the lines are formatted on the GPU."""
+    check(octree.ctx.handle, octree.ctx._L.dg_octree_write_text(octree.ctx.handle, octree.handle, _path(path)),
+          "writeNodesToFile")
+
+
+def writeNodesToFile_binary(path, octree: Octree):
+    """ot::writeNodesToFile_binary (src/octFunctions.cpp:482): 28-byte records."""
+    check(octree.ctx.handle, octree.ctx._L.dg_octree_write_binary(octree.ctx.handle, octree.handle, _path(path)),
+          "writeNodesToFile_binary")
+
+
+def readNodesFromFile(path, ctx: Context | None = None) -> Octree:
+    """ot::readNodesFromFile (src/octFunctions.cpp:452): the octants of a text
+    file, in the file's order, parsed on the GPU."""
+    ctx = ctx or default_context()
+    h = ctypes.c_void_p()
+    check(ctx.handle, ctx._L.dg_octree_read_text(ctx.handle, _path(path), ctypes.byref(h)), "readNodesFromFile")
+    return Octree(ctx, h)
+
+
+def readNodesFromFile_binary(path, ctx: Context | None = None) -> Octree:
+    """ot::readNodesFromFile_binary (src/octFunctions.cpp:435): the file's
+    records (the reference's reader repeats the last one)."""
+    ctx = ctx or default_context()
+    h = ctypes.c_void_p()
+    check(ctx.handle, ctx._L.dg_octree_read_binary(ctx.handle, _path(path), ctypes.byref(h)),
+          "readNodesFromFile_binary")
+    return Octree(ctx, h)
 
 
 def balanceOctree(octree: Octree, dim: int = 3, maxDepth: int | None = None, incCorner: bool = True,

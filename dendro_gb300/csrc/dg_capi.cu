@@ -8,6 +8,7 @@
 #include <string>
 
 #include "dendro_gb300.h"
+#include "dg_io.cuh"
 #include "dg_mg.cuh"
 
 struct dg_ctx_s {
@@ -57,6 +58,21 @@ int guarded(dg_ctx ctx, F &&f) {
     ctx->c.last_error = e.what();
     return DG_ERR_INTERNAL;
   }
+}
+
+template <typename F>
+int read_octree_file(dg_ctx ctx, dg_octree *out, F &&reader) {
+  if (!out) return DG_ERR_INVALID_ARG;
+  *out = nullptr;
+  dg_octree h = new (std::nothrow) dg_octree_s();
+  if (!h) return DG_ERR_OUT_OF_MEMORY;
+  int rc = guarded(ctx, [&]() { reader(h->o); });
+  if (rc != DG_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return DG_OK;
 }
 
 // device copy of a host (or device) input array
@@ -361,6 +377,46 @@ int dg_octree_upload(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDep
   }
   *out = h;
   return DG_OK;
+}
+
+int dg_pts_file_count(const char *path, size_t *n) {
+  if (!path || !n) return DG_ERR_INVALID_ARG;
+  try {
+    *n = dg::pts_file_count(path);
+  } catch (const dg::Error &e) {
+    return e.code;
+  }
+  return DG_OK;
+}
+
+int dg_pts_file_read(dg_ctx ctx, const char *path, double *xyz, size_t capacity, int dst_on_device, size_t *n) {
+  if (!path || !n || (!xyz && capacity)) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() { *n = dg::pts_file_read(ctx->c, path, xyz, capacity, dst_on_device != 0); });
+}
+
+int dg_pts_file_write(dg_ctx ctx, const char *path, const double *xyz, size_t n, int src_on_device) {
+  if (!path || (!xyz && n)) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() { dg::pts_file_write(ctx->c, path, xyz, n, src_on_device != 0); });
+}
+
+int dg_octree_write_text(dg_ctx ctx, dg_octree o, const char *path) {
+  if (!o || !path) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() { dg::octree_write_text(ctx->c, o->o, path); });
+}
+
+int dg_octree_write_binary(dg_ctx ctx, dg_octree o, const char *path) {
+  if (!o || !path) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() { dg::octree_write_binary(ctx->c, o->o, path); });
+}
+
+int dg_octree_read_text(dg_ctx ctx, const char *path, dg_octree *out) {
+  if (!path) return DG_ERR_INVALID_ARG;
+  return read_octree_file(ctx, out, [&](dg::Octree &o) { dg::octree_read_text(ctx->c, path, o); });
+}
+
+int dg_octree_read_binary(dg_ctx ctx, const char *path, dg_octree *out) {
+  if (!path) return DG_ERR_INVALID_ARG;
+  return read_octree_file(ctx, out, [&](dg::Octree &o) { dg::octree_read_binary(ctx->c, path, o); });
 }
 
 int dg_octree_free(dg_ctx ctx, dg_octree o) {

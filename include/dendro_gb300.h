@@ -146,6 +146,28 @@ int dg_octree_download(dg_ctx ctx, dg_octree o, uint32_t *xyzl, int dst_on_devic
 int dg_octree_upload(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDepth, int src_on_device, dg_octree *out);
 int dg_octree_free(dg_ctx ctx, dg_octree o);
 
+/* ---- point and octree files ------------------------------------------------
+ * The reference's formats (src/octFunctions.cpp).  Point files
+ * (readPtsFromFile :319, writePtsToFile :380): a uint32 count, then x y z per
+ * point in FP64; no points -> an empty file.  Octree text files
+ * (readNodesFromFile :452, writeNodesToFile :496): "3 maxDepth", the count,
+ * then "x y z level" per octant, one per line, byte for byte as the reference
+ * writes them.  Binary octree files (readNodesFromFile_binary :435,
+ * writeNodesToFile_binary :482): 28-byte records x y z level weight dim
+ * maxDepth.  Differences: the binary reader returns the file's records (the
+ * reference's repeats the last one), malformed files get DG_ERR_INVALID_ARG
+ * instead of undefined values, and writers take one cloud per octree.  Device
+ * buffers and octree handles are filled through pinned staging buffers;
+ * octree text is formatted and parsed on the GPU.  The order of the file's
+ * octants is kept. */
+int dg_pts_file_count(const char *path, size_t *n);
+int dg_pts_file_read(dg_ctx ctx, const char *path, double *xyz, size_t capacity, int dst_on_device, size_t *n);
+int dg_pts_file_write(dg_ctx ctx, const char *path, const double *xyz, size_t n, int src_on_device);
+int dg_octree_write_text(dg_ctx ctx, dg_octree o, const char *path);
+int dg_octree_read_text(dg_ctx ctx, const char *path, dg_octree *out);
+int dg_octree_write_binary(dg_ctx ctx, dg_octree o, const char *path);
+int dg_octree_read_binary(dg_ctx ctx, const char *path, dg_octree *out);
+
 /* ---- ot::DA ----------------------------------------------------------------
  * include/oda/oda.h:622 / src/oda/oda.cpp:250 at one rank: element -> node
  * map with hanging vertices resolved to the parent's vertex

@@ -342,6 +342,46 @@ static int mode_da(int argc, char **argv) {
   return conflicts ? 5 : 0;
 }
 
+// io PTS D OUTPREFIX: the reference's own file writers on one cloud --
+// writePtsToFile (OUTPREFIX.pts), and for its balanced octree writeNodesToFile
+// (OUTPREFIX.ot, text) and writeNodesToFile_binary (OUTPREFIX.otb); then its
+// readers on those files, reporting what they return
+static int mode_io(int argc, char **argv) {
+  if (argc < 5) return 1;
+  unsigned maxDepth = std::atoi(argv[3]);
+  FILE *f = xopen(argv[2], "rb");
+  uint64_t n = 0;
+  if (std::fread(&n, 8, 1, f) != 1) return 3;
+  std::vector<double> pts(3 * n);
+  if (n && std::fread(pts.data(), 8, 3 * n, f) != 3 * n) return 3;
+  std::fclose(f);
+  std::string pre = argv[4];
+  std::string fp = pre + ".pts", ft = pre + ".ot", fb = pre + ".otb";
+  ot::writePtsToFile(&fp[0], pts);
+  std::vector<double> back;
+  ot::readPtsFromFile(&fp[0], back);
+  const bool pts_same = back == pts;
+  double gLens[3] = {1.0, 1.0, 1.0};
+  std::vector<ot::TreeNode> lin, bal;
+  ot::points2Octree(pts, gLens, lin, 3, maxDepth, 1, MPI_COMM_WORLD);
+  ot::balanceOctree(lin, bal, 3, maxDepth, true, MPI_COMM_WORLD, NULL, NULL);
+  ot::writeNodesToFile(&ft[0], bal);
+  ot::writeNodesToFile_binary(&fb[0], bal);
+  std::vector<ot::TreeNode> rt, rb;
+  ot::readNodesFromFile(&ft[0], rt);
+  ot::readNodesFromFile_binary(&fb[0], rb);
+  bool text_same = rt.size() == bal.size();
+  for (size_t i = 0; text_same && i < rt.size(); i++) text_same = rt[i] == bal[i] && rt[i].getLevel() == bal[i].getLevel();
+  bool bin_prefix_same = rb.size() >= bal.size();
+  for (size_t i = 0; bin_prefix_same && i < bal.size(); i++)
+    bin_prefix_same = rb[i] == bal[i] && rb[i].getLevel() == bal[i].getLevel();
+  std::printf("{\"op\":\"io\",\"n_pts\":%llu,\"n_bal\":%zu,\"pts_roundtrip\":%d,\"text_read\":%zu,"
+              "\"text_same\":%d,\"binary_read\":%zu,\"binary_prefix_same\":%d,\"treenode_bytes\":%zu}\n",
+              (unsigned long long)n, bal.size(), (int)pts_same, rt.size(), (int)text_same, rb.size(),
+              (int)bin_prefix_same, sizeof(ot::TreeNode));
+  return 0;
+}
+
 int main(int argc, char **argv) {
   if (argc < 2) {
     std::fprintf(stderr, "usage: ref_driver p2o|bal|check|da ...\n");
@@ -355,5 +395,6 @@ int main(int argc, char **argv) {
   if (m == "check") rc = mode_check(argc, argv);
   if (m == "coarsen") rc = mode_coarsen(argc, argv);
   if (m == "da") rc = mode_da(argc, argv);
+  if (m == "io") rc = mode_io(argc, argv);
   return rc;
 }

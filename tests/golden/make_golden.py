@@ -32,7 +32,7 @@ sys.path.insert(0, ROOT)
 from dendro_gb300 import datagen  # noqa: E402
 from tests.golden import cases  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = next((a for a in sys.argv[1:] if not a.startswith("--")), "/root/reference")
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 
 
@@ -89,7 +89,28 @@ def ref_p2o_bal(tmp, name, pts, depth, maxpts):
     return lin, read_oct(bf)
 
 
+def make_io():
+    """The reference's own writers (writePtsToFile, writeNodesToFile,
+    writeNodesToFile_binary) on the balanced octree of a 200-point cloud, and
+    what its readers return for those files: tests/golden/io/."""
+    outdir = os.path.join(HERE, "io")
+    os.makedirs(outdir, exist_ok=True)
+    pts = datagen.gaussian(200, 0.5, 0.1, seed=11)
+    with tempfile.TemporaryDirectory() as tmp:
+        pf = os.path.join(tmp, "in.bin")
+        write_pts(pf, pts)
+        info = run("io", pf, 30, os.path.join(outdir, "gauss200"))
+    np.save(os.path.join(outdir, "gauss200_points.npy"), pts)
+    with open(os.path.join(outdir, "gauss200.json"), "w") as f:
+        json.dump(info, f, indent=1, sort_keys=True)
+
+
 def main():
+    if "--io-only" in sys.argv:
+        if not os.path.exists(DRIVER):
+            subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), f"REF={REF}"])
+        make_io()
+        return
     if not os.path.exists(DRIVER):
         subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), f"REF={REF}"])
     out = {}
@@ -183,6 +204,7 @@ def main():
                         rmat1_stats=rmat("RmatType1Stencils.inp", (8, 8, 18, 8, 8)),
                         rmat2_stats=rmat("RmatType2Stencils.inp", (8, 18, 8, 8)))
     print("golden fixtures written to", HERE)
+    make_io()
 
 
 if __name__ == "__main__":
