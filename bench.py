@@ -319,6 +319,7 @@ def run_serving(args, local, barrier):
         for _ in range(args.steps):
             _, wall = replay(srv, pinned)
             e2e_walls.append(wall)
+    tune = sorted({ln for c in [srv.ctx] + srv.worker_ctx for ln in c.autotune_log().splitlines()})
     srv.close()
     # the per-call drop-in on the same stream
     p_walls, p_outs = [], []
@@ -347,6 +348,7 @@ def run_serving(args, local, barrier):
         "errors": errors,
         "stats": stats,
         "clocks": clocks,
+        "autotune": tune,
     }
     res["served_over_plain"] = (res["served"]["Mpts_per_s"] / res["plain"]["Mpts_per_s"]) if p_walls else None
     return res
@@ -413,7 +415,7 @@ def run_scale(args, dg, ctx, local):
                           "frac_of_measured_peak": tbytes / (tms * 1e-3) / 1e9 / peak,
                           "traffic_per_launch": (TRAFFIC_PER_ALG_BYTE[top] * tbytes / tcnt
                                                  if top in TRAFFIC_PER_ALG_BYTE else None)},
-           "kernels": kernels}
+           "kernels": kernels, "autotune": ctx.autotune_log().splitlines()}
     if not args.skip_da:
         lin = dg.points2Octree(dev, maxDepth=30, maxNumPtsPerOctant=1, ctx=ctx)
         bal = dg.balanceOctree(lin)
@@ -663,6 +665,7 @@ def run_ours(args):
                        "max_depth": 30, "max_pts_per_octant": 1, "solve": f"FP32 V(2,2) CG to 1e-8, <= {SOLVE_MAXIT} it",
                        "parallelism": f"replicas x{ws}",
                        "l2": f"inputs larger than L2 ({24 * serve['points'] / 1e9:.2f} GB of points per step)"},
+            "autotune": serve["autotune"],
             "served": serve["served"],
             "plain": serve["plain"],
             "served_over_plain": serve["served_over_plain"],

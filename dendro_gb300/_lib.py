@@ -58,6 +58,7 @@ def _declare(L):
         "dg_ctx_destroy": ([P], I),
         "dg_ctx_set_stream": ([P, P], I),
         "dg_ctx_last_error": ([P], ctypes.c_char_p),
+        "dg_ctx_autotune_log": ([P], ctypes.c_char_p),
         "dg_ctx_last_device_ms": ([P, ctypes.POINTER(D)], I),
         "dg_ctx_profile": ([P, I], I),
         "dg_ctx_profile_count": ([P, ctypes.POINTER(I)], I),

@@ -77,6 +77,10 @@ class Context:
         """Start (or stop) per-kernel timing; clears the statistics."""
         check(self.handle, self._L.dg_ctx_profile(self.handle, 1 if enable else 0), "dg_ctx_profile")
 
+    def autotune_log(self) -> str:
+        """The autotuner's decisions on this context, one line each."""
+        return self._L.dg_ctx_autotune_log(self.handle).decode()
+
     def profile_stats(self) -> dict:
         """{kernel: (total_ms, launches, algorithmic_bytes)} since profile()."""
         n = ctypes.c_int()

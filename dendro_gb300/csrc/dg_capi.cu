@@ -379,6 +379,8 @@ int dg_octree_upload(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDep
   return DG_OK;
 }
 
+const char *dg_ctx_autotune_log(dg_ctx ctx) { return ctx ? ctx->c.tune_log.c_str() : ""; }
+
 int dg_pts_file_count(const char *path, size_t *n) {
   if (!path || !n) return DG_ERR_INVALID_ARG;
   try {

@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cstdio>
+#include <utility>
 #include <vector>
 
 #include "dg_common.cuh"
@@ -328,12 +330,19 @@ constexpr uint64_t OS_FLAG_INCL = 2ull << 62;
 constexpr uint64_t OS_VALUE = (1ull << 62) - 1;
 constexpr unsigned OS_SPIN_LIMIT = 1u << 22;
 
+// tile of one onesweep block: ITEMS keys per thread (the default; the
+// autotuner also tries OsAlt<K>::ITEMS)
 template <typename K>
 struct OsCfg {
   static constexpr int ITEMS = sizeof(K) == 16 ? 8 : 16;
   static constexpr int TILE = RS_BLOCK * ITEMS;
   static constexpr int WARP_KEYS = TILE / RS_WARPS;
 };
+template <typename K>
+struct OsAlt {
+  static constexpr int ITEMS = OsCfg<K>::ITEMS / 2;
+};
+constexpr size_t OS_TUNE_MIN = size_t(1) << 16;  // smaller sorts use the default tile
 
 __device__ __forceinline__ uint64_t ld_relaxed(const uint64_t *p) {
   uint64_t v;
@@ -374,12 +383,12 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_digit_hists(const K *__restrict
 // running counters order the rounds), placed in shared memory in digit
 // order, then written out so that consecutive threads write consecutive
 // addresses of each digit's run.
-template <typename K>
+template <typename K, int ITEMS = OsCfg<K>::ITEMS>
 __global__ void __launch_bounds__(RS_BLOCK, 4) k_rs_onesweep(const K *__restrict__ in, K *__restrict__ out, size_t n,
                                                           int shift, const uint64_t *__restrict__ digit_off,
                                                           uint64_t *__restrict__ status, unsigned *tile_counter,
                                                           uint32_t *flags) {
-  constexpr int ITEMS = OsCfg<K>::ITEMS, TILE = OsCfg<K>::TILE, WK = OsCfg<K>::WARP_KEYS;
+  constexpr int TILE = RS_BLOCK * ITEMS, WK = TILE / RS_WARPS;
   __shared__ K tk[TILE];
   __shared__ uint32_t wh[RS_WARPS][256];
   __shared__ uint32_t s_local[256];
@@ -513,20 +522,59 @@ K *radix_sort(Context &ctx, K *keys, K *tmp, size_t n, int end_bit) {
   if (active.empty()) return keys;
   DBuf<uint64_t> doffs(offs.size(), s);
   DG_CUDA(cudaMemcpyAsync(doffs.get(), offs.data(), offs.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
-  const size_t ntiles = (n + OsCfg<K>::TILE - 1) / OsCfg<K>::TILE;
-  if (ntiles >= 0xffffffffull) fail(DG_ERR_INVALID_ARG, "radix sort: too many keys");
-  DBuf<uint64_t> status(ntiles * 256, s);
+  const size_t max_tiles = (n + RS_BLOCK * OsAlt<K>::ITEMS - 1) / (RS_BLOCK * OsAlt<K>::ITEMS);
+  if (max_tiles >= 0xffffffffull) fail(DG_ERR_INVALID_ARG, "radix sort: too many keys");
+  DBuf<uint64_t> status(max_tiles * 256, s);
   unsigned *d_counter = reinterpret_cast<unsigned *>(ctx.d_scratch + 12);
-  K *src = keys, *dst = tmp;
-  for (size_t a = 0; a < active.size(); a++) {
+  // one digit pass with `items` keys per thread
+  auto pass = [&](int items, const K *src, K *dst, size_t a) {
+    const size_t tile = (size_t)RS_BLOCK * items, ntiles = (n + tile - 1) / tile;
     DG_CUDA(cudaMemsetAsync(status.get(), 0, ntiles * 256 * sizeof(uint64_t), s));
     DG_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s));
-    {
-      ProfScope _prof(ctx, "rs_onesweep", (double)n * sizeof(K) * 2);
-      k_rs_onesweep<K><<<(unsigned)ntiles, RS_BLOCK, 0, s>>>(src, dst, n, shifts[active[a]], doffs.get() + 256 * a,
-                                                             status.get(), d_counter, ctx.d_flags);
-      DG_LAUNCH_CHECK();
+    ProfScope _prof(ctx, "rs_onesweep", (double)n * sizeof(K) * 2);
+    if (items == OsCfg<K>::ITEMS)
+      k_rs_onesweep<K, OsCfg<K>::ITEMS><<<(unsigned)ntiles, RS_BLOCK, 0, s>>>(
+          src, dst, n, shifts[active[a]], doffs.get() + 256 * a, status.get(), d_counter, ctx.d_flags);
+    else
+      k_rs_onesweep<K, OsAlt<K>::ITEMS><<<(unsigned)ntiles, RS_BLOCK, 0, s>>>(
+          src, dst, n, shifts[active[a]], doffs.get() + 256 * a, status.get(), d_counter, ctx.d_flags);
+    DG_LAUNCH_CHECK();
+  };
+  // autotuner: the first sort of each size (log2 of the key count) times both
+  // tiles on its first digit pass (the pass is stable, so both write the same
+  // output) and keeps the faster for every later pass and sort of that size
+  const int width = sizeof(K) == 16 ? 1 : 0;
+  int bucket = 0;
+  while (bucket < 63 && ((size_t)2 << bucket) <= n) bucket++;
+  int &items = ctx.tune_items[width][bucket];
+  K *src = keys, *dst = tmp;
+  size_t a0 = 0;
+  if (items == 0 && n >= OS_TUNE_MIN) {
+    const int cand[2] = {OsCfg<K>::ITEMS, OsAlt<K>::ITEMS};
+    float ms[2] = {0.f, 0.f};
+    cudaEvent_t e0, e1;
+    DG_CUDA(cudaEventCreate(&e0));
+    DG_CUDA(cudaEventCreate(&e1));
+    for (int c = 0; c < 2; c++) {
+      DG_CUDA(cudaEventRecord(e0, s));
+      pass(cand[c], src, dst, 0);
+      DG_CUDA(cudaEventRecord(e1, s));
+      DG_CUDA(cudaEventSynchronize(e1));
+      DG_CUDA(cudaEventElapsedTime(&ms[c], e0, e1));
     }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    items = ms[1] < ms[0] ? cand[1] : cand[0];
+    char line[160];
+    std::snprintf(line, sizeof(line), "onesweep %d-byte keys, 2^%d: %d keys/thread (%.3f ms) vs %d (%.3f ms) -> %d\n",
+                  (int)sizeof(K), bucket, cand[0], ms[0], cand[1], ms[1], items);
+    ctx.tune_log += line;
+    std::swap(src, dst);
+    a0 = 1;
+  }
+  const int use = items ? items : OsCfg<K>::ITEMS;
+  for (size_t a = a0; a < active.size(); a++) {
+    pass(use, src, dst, a);
     K *t = src;
     src = dst;
     dst = t;

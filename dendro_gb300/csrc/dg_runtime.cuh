@@ -51,6 +51,10 @@ struct Context {
   std::map<std::string, ProfStat> prof_stats;
   std::vector<ProfPending> prof_pending;
   std::vector<cudaEvent_t> prof_pool;
+  // autotuner: onesweep tile per (key width: 0 = 8 bytes, 1 = 16 bytes,
+  // log2 of the key count); 0 = not tuned yet, else the items per thread
+  int tune_items[2][64] = {};
+  std::string tune_log;  // one line per decision
 };
 
 // thrown inside the library, converted to a status code at the C ABI

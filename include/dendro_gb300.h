@@ -62,6 +62,10 @@ int dg_ctx_destroy(dg_ctx ctx);
 /* Run subsequent calls on an external cudaStream_t (NULL: the context's own). */
 int dg_ctx_set_stream(dg_ctx ctx, void *cuda_stream);
 const char *dg_ctx_last_error(dg_ctx ctx);
+/* Choices the context's autotuner made so far, one line each (the radix
+ * sort's tile: each size class's first sort times both tiles on its first
+ * digit pass and keeps the faster).  No counterpart in the reference. */
+const char *dg_ctx_autotune_log(dg_ctx ctx);
 const char *dg_status_string(int status);
 int dg_version(void);
 
