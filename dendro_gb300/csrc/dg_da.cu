@@ -409,6 +409,7 @@ __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict
   __shared__ uint16_t runpos[PATCH_ENT + 1];
   __shared__ uint32_t ek[PATCH];
   __shared__ uint16_t rank[PATCH];
+  __shared__ uint8_t runc[PATCH_ENT];  // run u holds every pair of its node
   const int tid = threadIdx.x;
   const size_t p = blockIdx.x;
   const size_t e0 = p * PATCH;
@@ -481,6 +482,17 @@ __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict
     n_run[p] = (uint32_t)total;
   }
   __syncthreads();
+  // one look-up of the node's mesh-wide pair count per run, by the thread
+  // holding the run's first pair
+  u = ex - 1;
+#pragma unroll
+  for (int j = 0; j < 8; j++)
+    if (st[j]) {
+      u++;
+      const uint32_t len = (uint32_t)runpos[u + 1] - (uint32_t)runpos[u];
+      runc[u] = len == node_pairs[id[j]] ? 1 : 0;
+    }
+  __syncthreads();
   u = ex - 1;
   uint32_t e[8];
 #pragma unroll
@@ -489,8 +501,7 @@ __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict
     e[j] = 0;
     if (i < nent) {
       if (st[j]) u++;
-      const uint32_t len = (uint32_t)runpos[u + 1] - (uint32_t)runpos[u];
-      e[j] = (uint32_t)(sk[i] & ENT_SLOT) | (st[j] ? ENT_START : 0u) | (len == node_pairs[id[j]] ? ENT_COMPLETE : 0u);
+      e[j] = (uint32_t)(sk[i] & ENT_SLOT) | (st[j] ? ENT_START : 0u) | (runc[u] ? ENT_COMPLETE : 0u);
     }
   }
   reinterpret_cast<uint4 *>(pinc + p * PATCH_ENT)[tid] =
