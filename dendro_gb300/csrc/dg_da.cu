@@ -398,6 +398,27 @@ __device__ void block_sort_regs(K (&v)[I], K *stage) {
   }
 }
 
+// one block per patch: the patch's elements ordered by (type, level, index);
+// then its (element, vertex) pairs grouped by node with a shared-memory hash
+// table (one run per distinct node; the pairs of a run ordered by slot, so
+// sums over a run are reproducible), run starts, and whether each run holds
+// every pair of its node in the mesh.  The element loop needs the pairs of a
+// node together, not the runs in any order.
+constexpr int PS_HT = PATCH_ENT;  // hash slots (>= distinct nodes of a patch)
+constexpr uint32_t PS_EMPTY = 0xffffffffu;
+
+struct PatchSortSmem {
+  uint32_t hkey[PS_HT];        // node of each hash slot
+  uint16_t hrun[PS_HT];        // run of each hash slot
+  uint16_t hcnt[PS_HT];        // pairs per hash slot, then placement cursor per run
+  uint16_t roff[PATCH_ENT + 1];  // run offsets
+  uint32_t rnode[PATCH_ENT];   // node of each run
+  uint16_t ent[PATCH_ENT];     // slots grouped by run
+  uint8_t rflag[PATCH_ENT];    // bit 0: a run starts here; bit 1 (per run): complete
+  uint32_t ek[PATCH];
+  uint16_t rank[PATCH];
+};
+
 __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict__ conn,
                                                       const uint32_t *__restrict__ meta, size_t E,
                                                       const uint32_t *__restrict__ node_pairs,
@@ -405,15 +426,17 @@ __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict
                                                       uint32_t *__restrict__ pmeta, uint16_t *__restrict__ pkeys,
                                                       uint16_t *__restrict__ pkcount, uint32_t *__restrict__ run_node,
                                                       uint32_t *__restrict__ n_run) {
-  __shared__ uint64_t sk[PATCH_ENT];
-  __shared__ uint16_t runpos[PATCH_ENT + 1];
-  __shared__ uint32_t ek[PATCH];
-  __shared__ uint16_t rank[PATCH];
-  __shared__ uint8_t runc[PATCH_ENT];  // run u holds every pair of its node
+  extern __shared__ __align__(16) unsigned char ps_raw[];
+  PatchSortSmem &S = *reinterpret_cast<PatchSortSmem *>(ps_raw);
   const int tid = threadIdx.x;
   const size_t p = blockIdx.x;
   const size_t e0 = p * PATCH;
   const int ne = (int)((E - e0) < (size_t)PATCH ? (E - e0) : (size_t)PATCH);
+  for (int i = tid; i < PS_HT; i += PATCH) {
+    S.hkey[i] = PS_EMPTY;
+    S.hcnt[i] = 0;
+  }
+  for (int i = tid; i < PATCH_ENT; i += PATCH) S.rflag[i] = 0;
   // element order: (type, level, index); missing elements last
   {
     uint32_t k1[1];
@@ -423,85 +446,128 @@ __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict
     } else {
       k1[0] = 0xffffffffu;
     }
-    block_sort_regs<uint32_t, 1, PATCH>(k1, ek);
+    block_sort_regs<uint32_t, 1, PATCH>(k1, S.ek);
     __syncthreads();
-    ek[tid] = k1[0];
+    S.ek[tid] = k1[0];
     __syncthreads();
   }
   // (type, level) groups of the ordered elements: the patch's stencil keys
-  const uint32_t grp = ek[tid] >> 9;
-  const int gstart = tid < ne && (tid == 0 || (ek[tid - 1] >> 9) != grp) ? 1 : 0;
+  const uint32_t grp = S.ek[tid] >> 9;
+  const int gstart = tid < ne && (tid == 0 || (S.ek[tid - 1] >> 9) != grp) ? 1 : 0;
   int nkeys;
   const int kidx = block_excl_scan<int, PATCH>(gstart, nkeys) + gstart - 1;
   if (tid < ne) {
-    const uint32_t eo = ek[tid] & (PATCH - 1);
-    rank[eo] = (uint16_t)tid;
+    const uint32_t eo = S.ek[tid] & (PATCH - 1);
+    S.rank[eo] = (uint16_t)tid;
     const uint32_t mo = meta[e0 + eo];
     pmeta[p * PATCH + tid] = (mo & 0xff00ffffu) | (uint32_t)(kidx < PKEY_MAX ? kidx : 0) << 16;
     if (gstart && kidx < PKEY_MAX) pkeys[p * PKEY_MAX + kidx] = (uint16_t)grp;
   }
   if (tid == 0) pkcount[p] = (uint16_t)nkeys;
   __syncthreads();
-  {
-    uint64_t k8[8];
+  // 1. one hash slot per distinct node; pairs counted per slot
+  uint16_t hpos[8];
+  uint16_t slot[8];
+  const bool have = tid < ne;
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-      const int i = k * PATCH + (tid < ne ? rank[tid] : tid);
-      k8[k] = tid < ne ? ((uint64_t)conn[(size_t)k * E + e0 + tid] << 12 | (uint64_t)i) : ~0ull;
+  for (int k = 0; k < 8; k++) {
+    hpos[k] = 0;
+    slot[k] = (uint16_t)(k * PATCH + (have ? S.rank[tid] : 0));
+    if (have) {
+      const uint32_t g = conn[(size_t)k * E + e0 + tid];
+      uint32_t h = (g * 2654435761u) >> (32 - 12);  // PS_HT = 2^12
+      for (int probe = 0; probe < PS_HT; probe++) {
+        const uint32_t cur = atomicCAS(&S.hkey[h], PS_EMPTY, g);
+        if (cur == PS_EMPTY || cur == g) break;
+        h = (h + 1) & (PS_HT - 1);
+      }
+      hpos[k] = (uint16_t)h;
+      atomicAdd(reinterpret_cast<unsigned int *>(&S.hcnt[h & ~1u]), (h & 1u) ? 0x10000u : 1u);
     }
-    block_sort_regs<uint64_t, 8, PATCH>(k8, sk);
-    __syncthreads();
+  }
+  __syncthreads();
+  // 2. runs in hash-slot order: run index and offset of each occupied slot
+  {
+    constexpr int PER = PS_HT / PATCH;  // slots per thread
+    int nr = 0, np = 0;
 #pragma unroll
-    for (int j = 0; j < 8; j++) sk[8 * tid + j] = k8[j];
+    for (int q = 0; q < PER; q++) {
+      const int h = tid * PER + q;
+      nr += S.hkey[h] != PS_EMPTY ? 1 : 0;
+      np += S.hcnt[h];
+    }
+    int tot_runs, tot_pairs;
+    int ur = block_excl_scan<int, PATCH>(nr, tot_runs);
+    int up = block_excl_scan<int, PATCH>(np, tot_pairs);
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+      const int h = tid * PER + q;
+      if (S.hkey[h] != PS_EMPTY) {
+        S.hrun[h] = (uint16_t)ur;
+        S.roff[ur] = (uint16_t)up;
+        S.rnode[ur] = S.hkey[h];
+        S.rflag[up] = 1;
+        up += S.hcnt[h];
+        ur++;
+      }
+    }
+    if (tid == 0) {
+      S.roff[tot_runs] = (uint16_t)tot_pairs;
+      n_run[p] = (uint32_t)tot_runs;
+    }
+    __syncthreads();
+    for (int i = tid; i < PS_HT; i += PATCH) S.hcnt[i] = 0;  // becomes the placement cursor per run
+    __syncthreads();
+    // 3. place the pairs (any order), then order each run by slot
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      if (have) {
+        const int u = S.hrun[hpos[k]];
+        const unsigned old = atomicAdd(reinterpret_cast<unsigned int *>(&S.hcnt[u & ~1]), (u & 1) ? 0x10000u : 1u);
+        const int at = (int)S.roff[u] + (int)((old >> ((u & 1) ? 16 : 0)) & 0xffffu);
+        S.ent[at] = slot[k];
+      }
+    __syncthreads();
+    for (int u = tid; u < tot_runs; u += PATCH) {
+      const int b = S.roff[u], e = S.roff[u + 1];
+      for (int i = b + 1; i < e; i++) {  // insertion sort: runs are short
+        const uint16_t v = S.ent[i];
+        int j = i - 1;
+        while (j >= b && S.ent[j] > v) {
+          S.ent[j + 1] = S.ent[j];
+          j--;
+        }
+        S.ent[j + 1] = v;
+      }
+      const uint32_t g = S.rnode[u];
+      run_node[p * PATCH_ENT + u] = g;
+      if ((uint32_t)(e - b) == node_pairs[g]) S.rflag[b] |= 2;
+    }
     __syncthreads();
   }
+  // 4. the packed entries, 8 per thread, and runs starting before each thread
   const int nent = 8 * ne;
-  uint32_t id[8];
-  bool st[8];
   int nst = 0;
 #pragma unroll
-  for (int j = 0; j < 8; j++) {
-    const int i = 8 * tid + j;
-    id[j] = (uint32_t)(sk[i] >> 12);
-    st[j] = i < nent && (i == 0 || (uint32_t)(sk[i - 1] >> 12) != id[j]);
-    nst += st[j];
-  }
+  for (int j = 0; j < 8; j++) nst += (8 * tid + j < nent && (S.rflag[8 * tid + j] & 1)) ? 1 : 0;
   int total;
   const int ex = block_excl_scan<int, PATCH>(nst, total);
   pexc[p * PATCH + tid] = (uint16_t)ex;
-  int u = ex - 1;
-#pragma unroll
-  for (int j = 0; j < 8; j++)
-    if (st[j]) {
-      u++;
-      runpos[u] = (uint16_t)(8 * tid + j);
-      run_node[p * PATCH_ENT + u] = id[j];
-    }
-  if (tid == 0) {
-    runpos[total] = (uint16_t)nent;
-    n_run[p] = (uint32_t)total;
-  }
-  __syncthreads();
-  // one look-up of the node's mesh-wide pair count per run, by the thread
-  // holding the run's first pair
-  u = ex - 1;
-#pragma unroll
-  for (int j = 0; j < 8; j++)
-    if (st[j]) {
-      u++;
-      const uint32_t len = (uint32_t)runpos[u + 1] - (uint32_t)runpos[u];
-      runc[u] = len == node_pairs[id[j]] ? 1 : 0;
-    }
-  __syncthreads();
-  u = ex - 1;
   uint32_t e[8];
+  uint8_t comp = 0;
+  if (ex > 0) {  // the run in progress at this thread's first pair started earlier
+    int i = 8 * tid;
+    while (i > 0 && !(S.rflag[i] & 1)) i--;
+    comp = S.rflag[i] & 2;
+  }
 #pragma unroll
   for (int j = 0; j < 8; j++) {
     const int i = 8 * tid + j;
     e[j] = 0;
     if (i < nent) {
-      if (st[j]) u++;
-      e[j] = (uint32_t)(sk[i] & ENT_SLOT) | (st[j] ? ENT_START : 0u) | (runc[u] ? ENT_COMPLETE : 0u);
+      const uint8_t f = S.rflag[i];
+      if (f & 1) comp = f & 2;
+      e[j] = (uint32_t)S.ent[i] | ((f & 1) ? ENT_START : 0u) | (comp ? ENT_COMPLETE : 0u);
     }
   }
   reinterpret_cast<uint4 *>(pinc + p * PATCH_ENT)[tid] =
@@ -532,8 +598,14 @@ static void mesh_patches(Context &ctx, Mesh &m) {
   }
   {
     ProfScope _prof(ctx, "da_patch_sort", (double)n * 8 * 14);
-    k_patch_sort<<<(unsigned)np, PATCH, 0, s>>>(m.conn, m.meta, n, pairs.get(), pinc.get(), pexc.get(),
-                                                pmeta.get(), pkeys.get(), pkcount.get(), run_node.get(), n_run.get());
+    static std::once_flag once;
+    std::call_once(once, []() {
+      DG_CUDA(cudaFuncSetAttribute(k_patch_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)sizeof(PatchSortSmem)));
+    });
+    k_patch_sort<<<(unsigned)np, PATCH, sizeof(PatchSortSmem), s>>>(m.conn, m.meta, n, pairs.get(), pinc.get(),
+                                                                    pexc.get(), pmeta.get(), pkeys.get(),
+                                                                    pkcount.get(), run_node.get(), n_run.get());
     DG_LAUNCH_CHECK();
   }
   exclusive_scan<uint32_t, uint64_t>(n_run.get(), poff.get(), np, poff.get() + np, s);
