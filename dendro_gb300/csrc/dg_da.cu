@@ -197,16 +197,52 @@ void ensure_stencils(Context &ctx) {
 // ------------------------------------------------------------------------
 // mesh build
 // ------------------------------------------------------------------------
-__device__ __forceinline__ bool is_leaf_at(const Key128 *__restrict__ keys, size_t n, int64_t x, int64_t y, int64_t z,
-                                           unsigned lev, int64_t dom) {
-  if (x < 0 || y < 0 || z < 0 || x >= dom || y >= dom || z >= dom) return false;
-  Key128 pos = morton3((uint32_t)x, (uint32_t)y, (uint32_t)z);
-  size_t j = find_leaf(keys, n, pos);
-  Key128 kj = keys[j];
-  return tag_level(kj) == lev && key_eq(tag_anchor(kj), pos);
+// Anchor -> element map: no two octants of a linear octree share an anchor,
+// so "the element anchored at p" is one look-up.  Open addressing with
+// linear probing over a power-of-two table of element indices (at most half
+// full); a slot's anchor is read back from the keys.
+constexpr uint32_t AH_EMPTY = 0xffffffffu;
+
+__device__ __forceinline__ uint64_t anchor_hash(Key128 a) {
+  uint64_t x = a.lo ^ (a.hi * 0x9e3779b97f4a7c15ull);
+  x ^= x >> 31;
+  x *= 0xbf58476d1ce4e5b9ull;
+  x ^= x >> 29;
+  return x;
 }
 
-__global__ void k_mesh_elems(const Key128 *__restrict__ keys, size_t n, unsigned D, const uint8_t *__restrict__ etype_of,
+__global__ void k_anchor_insert(const Key128 *__restrict__ keys, size_t n, uint32_t *__restrict__ tab, uint64_t mask) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  uint64_t h = anchor_hash(tag_anchor(keys[e])) & mask;
+  for (uint64_t probe = 0; probe <= mask; probe++) {
+    if (atomicCAS(&tab[h], AH_EMPTY, (uint32_t)e) == AH_EMPTY) return;
+    h = (h + 1) & mask;
+  }
+}
+
+// element anchored at `pos` (a bare anchor), or AH_EMPTY
+__device__ __forceinline__ uint32_t anchor_find(const Key128 *__restrict__ keys, const uint32_t *__restrict__ tab,
+                                                uint64_t mask, Key128 pos) {
+  uint64_t h = anchor_hash(pos) & mask;
+  for (uint64_t probe = 0; probe <= mask; probe++) {
+    const uint32_t e = tab[h];
+    if (e == AH_EMPTY) return AH_EMPTY;
+    if (key_eq(tag_anchor(keys[e]), pos)) return e;
+    h = (h + 1) & mask;
+  }
+  return AH_EMPTY;
+}
+
+__device__ __forceinline__ bool is_leaf_at(const Key128 *__restrict__ keys, const uint32_t *__restrict__ tab,
+                                           uint64_t mask, int64_t x, int64_t y, int64_t z, unsigned lev, int64_t dom) {
+  if (x < 0 || y < 0 || z < 0 || x >= dom || y >= dom || z >= dom) return false;
+  const uint32_t j = anchor_find(keys, tab, mask, morton3((uint32_t)x, (uint32_t)y, (uint32_t)z));
+  return j != AH_EMPTY && tag_level(keys[j]) == lev;
+}
+
+__global__ void k_mesh_elems(const Key128 *__restrict__ keys, size_t n, const uint32_t *__restrict__ tab,
+                             uint64_t mask, unsigned D, const uint8_t *__restrict__ etype_of,
                              uint32_t *__restrict__ meta, uint32_t *__restrict__ cnt, uint32_t *flags) {
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
@@ -232,7 +268,7 @@ __global__ void k_mesh_elems(const Key128 *__restrict__ keys, size_t n, unsigned
         leaf[s] = false;  // the corner neighbour hangs no vertex of e
         continue;
       }
-      leaf[s] = is_leaf_at(keys, n, P[0] + ((s & 1) ? d[0] : 0), P[1] + ((s & 2) ? d[1] : 0),
+      leaf[s] = is_leaf_at(keys, tab, mask, P[0] + ((s & 1) ? d[0] : 0), P[1] + ((s & 2) ? d[1] : 0),
                            P[2] + ((s & 4) ? d[2] : 0), l - 1, dom);
     }
 #pragma unroll
@@ -259,7 +295,8 @@ __global__ void k_mesh_elems(const Key128 *__restrict__ keys, size_t n, unsigned
   cnt[e] = owned;
 }
 
-__global__ void k_mesh_conn(const Key128 *__restrict__ keys, size_t n, unsigned D, const uint32_t *__restrict__ meta,
+__global__ void k_mesh_conn(const Key128 *__restrict__ keys, size_t n, const uint32_t *__restrict__ tab,
+                            uint64_t mask, unsigned D, const uint32_t *__restrict__ meta,
                             const uint64_t *__restrict__ base, uint32_t *__restrict__ conn, uint32_t *__restrict__ nx,
                             uint32_t *__restrict__ ny, uint32_t *__restrict__ nz, size_t n_node, uint32_t *flags) {
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -309,7 +346,15 @@ __global__ void k_mesh_conn(const Key128 *__restrict__ keys, size_t n, unsigned 
         cl[a] = v[a];
       }
     }
-    size_t o = find_leaf_from(keys, n, morton3((uint32_t)cl[0], (uint32_t)cl[1], (uint32_t)cl[2]), e);
+    // the owner is the element anchored at the vertex; on the positive domain
+    // boundary, the leaf containing the vertex clamped inward (a search)
+    size_t o;
+    if (kb == 0) {
+      const uint32_t f = anchor_find(keys, tab, mask, morton3((uint32_t)cl[0], (uint32_t)cl[1], (uint32_t)cl[2]));
+      o = f == AH_EMPTY ? 0 : f;
+    } else {
+      o = find_leaf_from(keys, n, morton3((uint32_t)cl[0], (uint32_t)cl[1], (uint32_t)cl[2]), e);
+    }
     const Key128 ko = keys[o];
     const unsigned lo_ = tag_level(ko);
     uint32_t ox, oy, oz;
@@ -638,10 +683,22 @@ void mesh_build(Context &ctx, const Octree &bal, Mesh &m) {
   m.max_depth = D;
   m.n_elem = n;
   DBuf<uint32_t> meta(n, s), cnt(n, s);
+  // anchor -> element map, at most half full
+  size_t cap = 1;
+  while (cap < 2 * n) cap <<= 1;
+  DBuf<uint32_t> atab(cap, s);
+  const uint64_t amask = cap - 1;
+  DG_CUDA(cudaMemsetAsync(atab.get(), 0xff, cap * sizeof(uint32_t), s));
+  {
+    ProfScope _prof(ctx, "da_anchor_map", (double)n * 16 + (double)cap * 4);
+    k_anchor_insert<<<grid_for(n, 256), 256, 0, s>>>(bal.keys, n, atab.get(), amask);
+    DG_LAUNCH_CHECK();
+  }
   DG_CUDA(cudaMemsetAsync(ctx.d_flags, 0, sizeof(uint32_t), s));
   {
     ProfScope _prof(ctx, "da_elems", (double)n * 24);
-    k_mesh_elems<<<grid_for(n, 256), 256, 0, s>>>(bal.keys, n, D, ctx.d_etype_of, meta.get(), cnt.get(), ctx.d_flags);
+    k_mesh_elems<<<grid_for(n, 256), 256, 0, s>>>(bal.keys, n, atab.get(), amask, D, ctx.d_etype_of, meta.get(),
+                                                 cnt.get(), ctx.d_flags);
   DG_LAUNCH_CHECK();
     }
   DBuf<uint64_t> base(n, s);
@@ -654,7 +711,8 @@ void mesh_build(Context &ctx, const Octree &bal, Mesh &m) {
   DBuf<uint32_t> conn(8 * n, s), nxyz(3 * (nn ? nn : 1), s);
   {
     ProfScope _prof(ctx, "da_conn", (double)n * 56);
-    k_mesh_conn<<<grid_for(n, 256), 256, 0, s>>>(bal.keys, n, D, meta.get(), base.get(), conn.get(), nxyz.get(),
+    k_mesh_conn<<<grid_for(n, 256), 256, 0, s>>>(bal.keys, n, atab.get(), amask, D, meta.get(), base.get(), conn.get(),
+                                                nxyz.get(),
                                                nxyz.get() + nn, nxyz.get() + 2 * nn, nn, ctx.d_flags);
   DG_LAUNCH_CHECK();
     }
