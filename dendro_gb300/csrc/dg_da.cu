@@ -349,7 +349,9 @@ __global__ void k_mesh_conn(const Key128 *__restrict__ keys, size_t n, const uin
     // the owner is the element anchored at the vertex; on the positive domain
     // boundary, the leaf containing the vertex clamped inward (a search)
     size_t o;
-    if (kb == 0) {
+    if (k == 0 && !(hm & 1u)) {
+      o = e;  // a vertex 0 that does not hang is the element's own anchor
+    } else if (kb == 0) {
       const uint32_t f = anchor_find(keys, tab, mask, morton3((uint32_t)cl[0], (uint32_t)cl[1], (uint32_t)cl[2]));
       o = f == AH_EMPTY ? 0 : f;
     } else {
