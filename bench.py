@@ -303,10 +303,12 @@ def run_serving(args, local, barrier):
     sampler = ClockSampler(local)
     sampler.start()
     walls, outs = [], []
+    srv.build_s.clear()
     for _ in range(args.steps):
         out, wall = replay(srv, on_dev)
         walls.append(wall)
         outs.extend(out)
+    served_build_s = sum(srv.build_s) / args.steps
     clocks = sampler.stop()
     stats = _merge_stats(c.profile_stats() for c in ctxs)
     for c in ctxs:
@@ -323,6 +325,7 @@ def run_serving(args, local, barrier):
     srv.close()
     # the per-call drop-in on the same stream
     p_walls, p_outs = [], []
+    plain_build_s = None
     if not args.skip_plain:
         plain = serving.PlainServer(device=local, solve_maxit=SOLVE_MAXIT)
         replay(plain, on_dev)
@@ -331,6 +334,7 @@ def run_serving(args, local, barrier):
             p_walls.append(wall)
             p_outs.extend(out)
         plain.close()
+        plain_build_s = sum(r.t_built - r.t_admit for r in p_outs) / 2
     errors = sum(1 for r in outs + p_outs if r.error)
     ms = 1e3 * sum(walls) / len(walls)
     res = {
@@ -351,6 +355,12 @@ def run_serving(args, local, barrier):
         "autotune": tune,
     }
     res["served_over_plain"] = (res["served"]["Mpts_per_s"] / res["plain"]["Mpts_per_s"]) if p_walls else None
+    # the construction + balance phase alone: the batches' build time (while
+    # other requests' solves share the GPU) against the per-call builds
+    res["build_balance"] = {"served_Mpts_per_s": npts / served_build_s / 1e6 if served_build_s else None,
+                            "plain_Mpts_per_s": npts / plain_build_s / 1e6 if plain_build_s else None}
+    if served_build_s and plain_build_s:
+        res["build_balance"]["served_over_plain"] = plain_build_s / served_build_s
     return res
 
 
@@ -669,6 +679,7 @@ def run_ours(args):
             "served": serve["served"],
             "plain": serve["plain"],
             "served_over_plain": serve["served_over_plain"],
+            "build_balance_served_vs_plain": serve["build_balance"],
             "solve_iterations_max": serve["iterations_max"],
             "solve_relres_max": serve["relres_max"],
             "request_errors": serve["errors"],

@@ -156,6 +156,7 @@ class BatchingServer:
         self.in_flight = 0
         self.cv = threading.Condition()
         self.batches = []  # sizes of the batches that were built
+        self.build_s = []  # seconds of each batch's construction + balance
 
     def _release(self, nbytes: int):
         with self.cv:
@@ -235,6 +236,7 @@ class BatchingServer:
             # one segmented construction + balance for the whole batch; host
             # clouds are copied in one by one (from pinned memory when they
             # live there) and joined on the device
+            tb0 = time.perf_counter() - t0
             clouds = [r.points for r, _ in batch]
             if not all(getattr(c, "is_cuda", False) for c in clouds):
                 import torch
@@ -248,6 +250,7 @@ class BatchingServer:
             lin.free()
             self.batches.append(len(batch))
             tb = time.perf_counter() - t0
+            self.build_s.append(tb - tb0)
             for s, (r, need) in enumerate(batch):
                 r.n_octants = int(off_lin[s + 1] - off_lin[s])
                 r.n_balanced = int(off_bal[s + 1] - off_bal[s])
