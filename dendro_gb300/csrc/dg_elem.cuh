@@ -188,31 +188,13 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
       me = pmeta[p * PATCH + tid];
     }
   }
-  // the node of each run of a patch (tagged RUN_BDY on the Dirichlet
-  // boundary) into gn: for the next patch while the current one finishes, so
-  // step 1 waits for x alone
-  auto fill_runs = [&](const uint4 &ww, uint32_t exx, uint64_t ubb, bool hv, uint32_t *gout) {
-    if (!hv) return;
-    int u = (int)exx - 1;
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      const uint32_t word = j < 2 ? ww.x : j < 4 ? ww.y : j < 6 ? ww.z : ww.w;
-      const uint32_t e = (j & 1) ? word >> 16 : word & 0xffffu;
-      if (e & ENT_START) {
-        u++;
-        const uint32_t g = pnode[ubb + u];
-        gout[u] = (DIR && bdy[g]) ? (g | RUN_BDY) : g;
-      }
-    }
-  };
-  if (p < n_patch) fill_runs(w, ex, ub, tid < patch_ne(p), gns);
-  __syncthreads();
   int par = 0;
   for (; p < n_patch; p += gridDim.x, par ^= 1) {
     const int ne = patch_ne(p);
     const bool have = tid < ne;
     const uint4 cw = w;
     const uint32_t cex = ex, cme = me, ckc = kc;
+    const uint64_t cub = ub;
     // the next patch's table words, one patch ahead
     const size_t pn = p + gridDim.x;
     if (pn < n_patch) {
@@ -230,17 +212,26 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
     };
     T *buf = bufs + par * PATCH_ENT;
     uint32_t *gn = gns + par * PATCH_ENT;
-    // 1. x of each run's node (gn, filled one patch ahead) into its slots
+    // 1. x of each run's node into its slots; the run's node into gn
     if (have) {
       int u = (int)cex - 1;
       T xv = (T)0;
 #pragma unroll
       for (int j = 0; j < 8; j++) {
         const uint32_t e = ent(j);
-        if (e & ENT_START) u++;
-        if (j == 0 || (e & ENT_START)) {  // j == 0: the run may have begun in an earlier thread
-          const uint32_t tag = gn[u];
-          xv = (DIR && (tag & RUN_BDY)) ? (T)0 : x[tag & ~RUN_BDY];
+        if (e & ENT_START) {
+          u++;
+          const uint32_t g = pnode[cub + u];
+          xv = x[g];
+          uint32_t tag = g;
+          if (DIR && bdy[g]) {
+            xv = (T)0;
+            tag |= RUN_BDY;
+          }
+          gn[u] = tag;
+        } else if (j == 0) {
+          xv = x[pnode[cub + u]];  // the run began in an earlier thread
+          if (DIR && bdy[pnode[cub + u]]) xv = (T)0;
         }
         buf[e & ENT_SLOT] = xv;
       }
@@ -306,7 +297,6 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
       ws_v[par][wid] = s;
       ws_f[par][wid] = f;
     }
-    if (pn < n_patch) fill_runs(w, ex, ub, tid < patch_ne(pn), gns + (par ^ 1) * PATCH_ENT);
     __syncthreads();
     T wv = lane < NW ? ws_v[par][lane] : (T)0;
     int wf = lane < NW ? ws_f[par][lane] : 0;
