@@ -469,7 +469,7 @@ struct PatchSortSmem {
 __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict__ conn,
                                                       const uint32_t *__restrict__ meta, size_t E,
                                                       const uint32_t *__restrict__ node_pairs,
-                                                      uint16_t *__restrict__ pinc, uint16_t *__restrict__ run_end,
+                                                      uint16_t *__restrict__ pinc, uint16_t *__restrict__ pexc,
                                                       uint32_t *__restrict__ pmeta, uint16_t *__restrict__ pkeys,
                                                       uint16_t *__restrict__ pkcount, uint32_t *__restrict__ run_node,
                                                       uint32_t *__restrict__ n_run) {
@@ -588,29 +588,44 @@ __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict
       }
       const uint32_t g = S.rnode[u];
       run_node[p * PATCH_ENT + u] = g;
-      const bool complete = (uint32_t)(e - b) == node_pairs[g];
-      run_end[p * PATCH_ENT + u] = (uint16_t)(e | (complete ? RUN_COMPLETE : 0u));
+      if ((uint32_t)(e - b) == node_pairs[g]) S.rflag[b] |= 2;
     }
     __syncthreads();
   }
-  // 4. the pairs' slots in run order, 8 per thread
+  // 4. the packed entries, 8 per thread, and runs starting before each thread
   const int nent = 8 * ne;
-  uint32_t e[8];
+  int nst = 0;
 #pragma unroll
-  for (int j = 0; j < 8; j++) e[j] = (8 * tid + j < nent) ? (uint32_t)S.ent[8 * tid + j] : 0u;
+  for (int j = 0; j < 8; j++) nst += (8 * tid + j < nent && (S.rflag[8 * tid + j] & 1)) ? 1 : 0;
+  int total;
+  const int ex = block_excl_scan<int, PATCH>(nst, total);
+  pexc[p * PATCH + tid] = (uint16_t)ex;
+  uint32_t e[8];
+  uint8_t comp = 0;
+  if (ex > 0) {  // the run in progress at this thread's first pair started earlier
+    int i = 8 * tid;
+    while (i > 0 && !(S.rflag[i] & 1)) i--;
+    comp = S.rflag[i] & 2;
+  }
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const int i = 8 * tid + j;
+    e[j] = 0;
+    if (i < nent) {
+      const uint8_t f = S.rflag[i];
+      if (f & 1) comp = f & 2;
+      e[j] = (uint32_t)S.ent[i] | ((f & 1) ? ENT_START : 0u) | (comp ? ENT_COMPLETE : 0u);
+    }
+  }
   reinterpret_cast<uint4 *>(pinc + p * PATCH_ENT)[tid] =
       make_uint4(e[0] | e[1] << 16, e[2] | e[3] << 16, e[4] | e[5] << 16, e[6] | e[7] << 16);
 }
 
-__global__ void k_patch_nodes(const uint32_t *__restrict__ run_node, const uint16_t *__restrict__ run_end,
-                              const uint32_t *__restrict__ n_run, const uint64_t *__restrict__ poff,
-                              uint32_t *__restrict__ pnode, uint16_t *__restrict__ prend) {
+__global__ void k_patch_nodes(const uint32_t *__restrict__ run_node, const uint32_t *__restrict__ n_run,
+                              const uint64_t *__restrict__ poff, uint32_t *__restrict__ pnode) {
   const size_t p = blockIdx.x;
   const uint32_t nr = n_run[p];
-  for (uint32_t i = threadIdx.x; i < nr; i += blockDim.x) {
-    pnode[poff[p] + i] = run_node[p * PATCH_ENT + i];
-    prend[poff[p] + i] = run_end[p * PATCH_ENT + i];
-  }
+  for (uint32_t i = threadIdx.x; i < nr; i += blockDim.x) pnode[poff[p] + i] = run_node[p * PATCH_ENT + i];
 }
 
 static void mesh_patches(Context &ctx, Mesh &m) {
@@ -618,7 +633,7 @@ static void mesh_patches(Context &ctx, Mesh &m) {
   const size_t n = m.n_elem, np = (n + PATCH - 1) / PATCH;
   if (m.n_node >= (size_t)RUN_BDY) fail(DG_ERR_INVALID_ARG, "DA: too many nodes for the element loop tables");
   DBuf<uint32_t> pairs(m.n_node, s), run_node(np * PATCH_ENT, s), n_run(np, s);
-  DBuf<uint16_t> pinc(np * PATCH_ENT, s), run_end(np * PATCH_ENT, s);
+  DBuf<uint16_t> pinc(np * PATCH_ENT, s), pexc(np * PATCH, s);
   DBuf<uint32_t> pmeta(np * PATCH, s);
   DBuf<uint16_t> pkeys(np * PKEY_MAX, s), pkcount(np, s);
   DBuf<uint64_t> poff(np + 1, s);
@@ -636,7 +651,7 @@ static void mesh_patches(Context &ctx, Mesh &m) {
                                    (int)sizeof(PatchSortSmem)));
     });
     k_patch_sort<<<(unsigned)np, PATCH, sizeof(PatchSortSmem), s>>>(m.conn, m.meta, n, pairs.get(), pinc.get(),
-                                                                    run_end.get(), pmeta.get(), pkeys.get(),
+                                                                    pexc.get(), pmeta.get(), pkeys.get(),
                                                                     pkcount.get(), run_node.get(), n_run.get());
     DG_LAUNCH_CHECK();
   }
@@ -645,16 +660,14 @@ static void mesh_patches(Context &ctx, Mesh &m) {
   DG_CUDA(cudaMemcpyAsync(&nruns, poff.get() + np, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
   DG_CUDA(cudaStreamSynchronize(s));
   DBuf<uint32_t> pnode(nruns ? nruns : 1, s);
-  DBuf<uint16_t> prend(nruns ? nruns : 1, s);
   {
-    ProfScope _prof(ctx, "da_patch_nodes", (double)nruns * 12);
-    k_patch_nodes<<<(unsigned)np, 256, 0, s>>>(run_node.get(), run_end.get(), n_run.get(), poff.get(), pnode.get(),
-                                               prend.get());
+    ProfScope _prof(ctx, "da_patch_nodes", (double)nruns * 8);
+    k_patch_nodes<<<(unsigned)np, 256, 0, s>>>(run_node.get(), n_run.get(), poff.get(), pnode.get());
     DG_LAUNCH_CHECK();
   }
   m.n_patch = np;
   m.pinc = pinc.release_ptr();
-  m.prend = prend.release_ptr();
+  m.pexc = pexc.release_ptr();
   m.pmeta = pmeta.release_ptr();
   m.pkeys = pkeys.release_ptr();
   m.pkcount = pkcount.release_ptr();
@@ -718,7 +731,7 @@ void mesh_free(Context &ctx, Mesh &m) {
   if (m.conn) cudaFreeAsync(m.conn, ctx.stream);
   if (m.node_xyz) cudaFreeAsync(m.node_xyz, ctx.stream);
   if (m.pinc) cudaFreeAsync(m.pinc, ctx.stream);
-  if (m.prend) cudaFreeAsync(m.prend, ctx.stream);
+  if (m.pexc) cudaFreeAsync(m.pexc, ctx.stream);
   if (m.pmeta) cudaFreeAsync(m.pmeta, ctx.stream);
   if (m.pkeys) cudaFreeAsync(m.pkeys, ctx.stream);
   if (m.pkcount) cudaFreeAsync(m.pkcount, ctx.stream);
@@ -749,7 +762,7 @@ void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, 
   {
     ProfScope _prof(ctx, sizeof(T) == 4 ? "matvec_fp32" : "matvec_fp64",
                     (double)m.n_elem * 36 + (double)m.n_node * 3 * sizeof(T));
-    k_patch_matvec<T, false><<<grid, PATCH, smem, s>>>(m.pmeta, m.pinc, m.prend, m.pnode, m.poff, m.pkeys,
+    k_patch_matvec<T, false><<<grid, PATCH, smem, s>>>(m.pmeta, m.pinc, m.pexc, m.pnode, m.poff, m.pkeys,
                                                        m.pkcount, m.n_elem, m.n_patch, cs, ctx.d_cperm, nullptr, x,
                                                        y, (T)lap_fac, (T)mass_fac);
     DG_LAUNCH_CHECK();

@@ -24,7 +24,7 @@ struct Mesh {
   // element loop tables (dg_elem.cuh): n_patch patches of PATCH elements
   size_t n_patch = 0;
   uint16_t *pinc = nullptr;   // PATCH_ENT per patch, node-sorted pairs
-  uint16_t *prend = nullptr;  // per run (beside pnode): end of the run's pairs | RUN_COMPLETE
+  uint16_t *pexc = nullptr;   // PATCH per patch: runs starting before pair 8t
   uint32_t *pmeta = nullptr;  // PATCH per patch: meta in the patch's element order,
                               // bits 16..23 = the element's stencil key index
   uint16_t *pkeys = nullptr;  // PKEY_MAX per patch: (type << 5 | level) of each key

@@ -8,20 +8,19 @@
 // 16-byte vectors; the elements of a patch are ordered by (type, level), so
 // the threads of a warp mostly read the same stencil (a broadcast).
 //
-// Patches: PATCH consecutive elements form a patch.  Its tables:
-//   pinc   the 8 x PATCH (element, vertex) pairs as slots (vertex * PATCH +
-//          element within the patch, 12 bits), grouped into runs, one run per
-//          node (runs in any order, the pairs of a run by slot);
-//   pnode  the node of each run (pnode[poff[p] + u]);
-//   prend  the end of each run's pairs, with RUN_COMPLETE when the run holds
-//          every pair of its node in the whole mesh (its sum is then stored,
-//          not added);
-//   pmeta  the meta words of the patch's elements in (type, level) order (the
-//          order slots use), bits 16..23 the element's stencil key;
-//   pkeys  the patch's distinct (type, level) pairs.
-// The element loop gathers x once per node into the slots, applies the
-// element stencils slot to slot in shared memory and sums each run: no
-// shared-memory atomics, and global atomics only for nodes that other
+// Patches: PATCH consecutive elements form a patch.  Its incidence table
+// lists the 8 x PATCH (element, vertex) pairs sorted by node id, 16 bits
+// each:
+//   bits 0..11  slot = vertex * PATCH + element within the patch
+//   bit 12      first pair of a node's run
+//   bit 13      the run holds every pair of its node in the whole mesh, so
+//               the node's sum is complete in this patch (stored, not added)
+// pnode[poff[p] + u] is the node of run u of patch p, pexc[p][t] the number
+// of runs that start before pair 8t, and pmeta[p][t] the meta word of the
+// patch's element t in (type, level) order (the order slots use).  An element loop over a patch
+// gathers x once per node into the slots, applies the element stencils
+// slot-to-slot in shared memory, and sums each run with a segmented scan:
+// no shared-memory atomics, and global atomics only for nodes that other
 // patches also touch.
 #pragma once
 
@@ -49,8 +48,7 @@ template <typename T>
 constexpr int sstride() {
   return 64 + 16 / (int)sizeof(T);
 }
-constexpr uint32_t ENT_SLOT = 0xfffu;
-constexpr uint32_t RUN_END = 0x7fffu, RUN_COMPLETE = 0x8000u;  // run-end words
+constexpr uint32_t ENT_SLOT = 0xfffu, ENT_START = 1u << 12, ENT_COMPLETE = 1u << 13;
 constexpr uint32_t RUN_BDY = 1u << 31;  // run node flag in shared memory (Dirichlet)
 
 // 2^-l exactly, from the exponent bits (0 <= l <= 30)
@@ -148,52 +146,101 @@ __device__ __forceinline__ void apply_comb(const double *__restrict__ S, const d
 
 // y = (lapf K + massf M) x over the elements of every patch; with DIR the
 // Dirichlet form: boundary rows are the identity (y = x), boundary columns
-// are dropped.  One block of PATCH threads per patch, grid-strided:
-//   stage  the patch's pair slots (in run order), each run's node and end,
-//          its meta words and its combined stencils into shared memory;
-//   1.     thread per run: x of the run's node into every slot of the run;
-//   2.     thread per element: the element stencil, slot to slot;
-//   3.     thread per run: the sum over the run's slots, stored (the run holds
-//          every pair of its node) or added atomically (other patches share
-//          the node).
+// are dropped.  One block of PATCH threads per patch, grid-strided; thread t
+// holds pairs 8t..8t+7 of the patch's table and is element t of the patch.
+// The slot buffer and the run-node array are double-buffered by patch
+// parity and the next patch's table words are loaded one patch ahead, so a
+// patch costs three barriers.
 template <typename T, bool DIR>
 __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
     k_patch_matvec(const uint32_t *__restrict__ pmeta, const uint16_t *__restrict__ pinc,
-                   const uint16_t *__restrict__ prend, const uint32_t *__restrict__ pnode,
+                   const uint16_t *__restrict__ pexc, const uint32_t *__restrict__ pnode,
                    const uint64_t *__restrict__ poff, const uint16_t *__restrict__ pkeys,
                    const uint16_t *__restrict__ pkcount, size_t E, size_t n_patch, const T *__restrict__ fsten,
                    const uint32_t *__restrict__ cperm, const uint8_t *__restrict__ bdy, const T *__restrict__ x,
                    T *__restrict__ y, T lapf, T massf) {
+  constexpr int NW = PATCH / 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *cs = reinterpret_cast<T *>(smem_raw);
-  T *buf = cs + fsten_entries<T>();
-  T *sc = buf + PATCH_ENT;  // PKEY_MAX combined stencils
-  uint32_t *rn = reinterpret_cast<uint32_t *>(sc + PKEY_MAX * sstride<T>());
-  uint16_t *ents = reinterpret_cast<uint16_t *>(rn + PATCH_ENT);
-  uint16_t *re = ents + PATCH_ENT;
-  uint32_t *cp = reinterpret_cast<uint32_t *>(re + PATCH_ENT);
+  T *bufs = cs + fsten_entries<T>();
+  uint32_t *gns = reinterpret_cast<uint32_t *>(bufs + 2 * PATCH_ENT);
+  uint32_t *cp = gns + 2 * PATCH_ENT;
+  T *sc = reinterpret_cast<T *>(cp + 8 * 18 + 4);  // PKEY_MAX combined stencils (16-byte aligned)
+  __shared__ T ws_v[2][NW];
+  __shared__ int ws_f[2][NW];
+  __shared__ int ws_first[2][NW + 1];
   for (int i = threadIdx.x; i < fsten_entries<T>(); i += PATCH) cs[i] = fsten[i];
   for (int i = threadIdx.x; i < 8 * 18; i += PATCH) cp[i] = cperm[i];
-  __syncthreads();
-  const int tid = threadIdx.x;
-  for (size_t p = blockIdx.x; p < n_patch; p += gridDim.x) {
-    const size_t e0 = p * PATCH;
-    const int ne = (int)((E - e0) < (size_t)PATCH ? (E - e0) : (size_t)PATCH);
-    const bool have = tid < ne;
-    const uint64_t ub = poff[p];
-    const int nr = (int)(poff[p + 1] - ub);
-    const uint32_t kc = pkcount[p];
-    // stage
-    if (have) reinterpret_cast<uint4 *>(ents)[tid] = reinterpret_cast<const uint4 *>(pinc + p * PATCH_ENT)[tid];
-    const uint32_t me = have ? pmeta[e0 + tid] : 0u;
-    for (int u = tid; u < nr; u += PATCH) {
-      const uint32_t g = pnode[ub + u];
-      rn[u] = (DIR && bdy[g]) ? (g | RUN_BDY) : g;
-      re[u] = prend[ub + u];
+  __syncthreads();  // step 1 of the first patch already reads cs
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+
+  auto patch_ne = [&](size_t q) { return (int)((E - q * PATCH) < (size_t)PATCH ? (E - q * PATCH) : (size_t)PATCH); };
+  size_t p = blockIdx.x;
+  uint4 w = make_uint4(0, 0, 0, 0);
+  uint32_t ex = 0, me = 0, kc = 0;
+  uint64_t ub = 0;
+  if (p < n_patch) {
+    ub = poff[p];
+    kc = pkcount[p];
+    if (tid < patch_ne(p)) {
+      w = reinterpret_cast<const uint4 *>(pinc + p * PATCH_ENT)[tid];
+      ex = pexc[p * PATCH + tid];
+      me = pmeta[p * PATCH + tid];
     }
-    const bool comb = kc <= (uint32_t)PKEY_MAX;
+  }
+  int par = 0;
+  for (; p < n_patch; p += gridDim.x, par ^= 1) {
+    const int ne = patch_ne(p);
+    const bool have = tid < ne;
+    const uint4 cw = w;
+    const uint32_t cex = ex, cme = me, ckc = kc;
+    const uint64_t cub = ub;
+    // the next patch's table words, one patch ahead
+    const size_t pn = p + gridDim.x;
+    if (pn < n_patch) {
+      ub = poff[pn];
+      kc = pkcount[pn];
+      if (tid < patch_ne(pn)) {
+        w = reinterpret_cast<const uint4 *>(pinc + pn * PATCH_ENT)[tid];
+        ex = pexc[pn * PATCH + tid];
+        me = pmeta[pn * PATCH + tid];
+      }
+    }
+    auto ent = [&](int j) -> uint32_t {
+      const uint32_t word = j < 2 ? cw.x : j < 4 ? cw.y : j < 6 ? cw.z : cw.w;
+      return (j & 1) ? word >> 16 : word & 0xffffu;
+    };
+    T *buf = bufs + par * PATCH_ENT;
+    uint32_t *gn = gns + par * PATCH_ENT;
+    // 1. x of each run's node into its slots; the run's node into gn
+    if (have) {
+      int u = (int)cex - 1;
+      T xv = (T)0;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const uint32_t e = ent(j);
+        if (e & ENT_START) {
+          u++;
+          const uint32_t g = pnode[cub + u];
+          xv = x[g];
+          uint32_t tag = g;
+          if (DIR && bdy[g]) {
+            xv = (T)0;
+            tag |= RUN_BDY;
+          }
+          gn[u] = tag;
+        } else if (j == 0) {
+          xv = x[pnode[cub + u]];  // the run began in an earlier thread
+          if (DIR && bdy[pnode[cub + u]]) xv = (T)0;
+        }
+        buf[e & ENT_SLOT] = xv;
+      }
+    }
+    // the patch's combined stencils (read only in step 2 of this patch, and
+    // rewritten only after every thread has passed that step's barrier)
+    const bool comb = ckc <= (uint32_t)PKEY_MAX;
     if (comb) {
-      for (int i = tid; i < (int)kc * 64; i += PATCH) {
+      for (int i = tid; i < (int)ckc * 64; i += PATCH) {
         const uint32_t key = pkeys[p * PKEY_MAX + (i >> 6)];
         const unsigned t = key >> 5, l = key & 31u;
         const T h = exp2_neg((T)0, l);
@@ -202,50 +249,102 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
             lapf * h * (T)0.5 * st[i & 63] + massf * h * h * h * (T)0.125 * st[64 + (i & 63)];
       }
     }
-    __syncthreads();
-    // 1. x of each run's node into the run's slots
-    for (int u = tid; u < nr; u += PATCH) {
-      const int b = u ? (int)(re[u - 1] & RUN_END) : 0, e = (int)(re[u] & RUN_END);
-      const uint32_t tag = rn[u];
-      const T xv = (DIR && (tag & RUN_BDY)) ? (T)0 : x[tag & ~RUN_BDY];
-      for (int i = b; i < e; i++) buf[ents[i] & ENT_SLOT] = xv;
-    }
+    if (lane == 0) ws_first[par][wid] = (ent(0) & ENT_START) ? 1 : 0;
+    if (tid == 0) ws_first[par][NW] = 1;
     __syncthreads();
     // 2. element stencils, slot to slot (canonical stencil, relabelled slots)
     if (have) {
-      const unsigned l = me & 255u, c = (me >> 8) & 7u, t = me >> 24;
+      const unsigned l = cme & 255u, c = (cme >> 8) & 7u, t = cme >> 24;
       const uint32_t sig = cp[c * 18 + t];
       T xv[8];
 #pragma unroll
       for (int m = 0; m < 8; m++) xv[m] = buf[((sig >> (3 * m)) & 7u) * PATCH + tid];
       auto put = [&](int m, T ym) { buf[((sig >> (3 * m)) & 7u) * PATCH + tid] = ym; };
       if (comb) {
-        apply_comb(sc + ((me >> 16) & 255u) * sstride<T>(), xv, put);
+        apply_comb(sc + ((cme >> 16) & 255u) * sstride<T>(), xv, put);
       } else {
         const T h = exp2_neg((T)0, l);
         apply_full(cs + t * fsten_stride<T>(), lapf * h * (T)0.5, massf * h * h * h * (T)0.125, xv, put);
       }
     }
     __syncthreads();
-    // 3. each run's sum to its node
-    for (int u = tid; u < nr; u += PATCH) {
-      const int b = u ? (int)(re[u - 1] & RUN_END) : 0, e = (int)(re[u] & RUN_END);
-      T acc = (T)0;
-      for (int i = b; i < e; i++) acc += buf[ents[i] & ENT_SLOT];
-      const uint32_t tag = rn[u];
-      const uint32_t g = tag & ~RUN_BDY;
-      if (DIR && (tag & RUN_BDY)) y[g] = x[g];
-      else if (re[u] & RUN_COMPLETE) y[g] = acc;
-      else atomicAdd(&y[g], acc);
+    // 3. run sums: segmented scan of the threads' trailing partial sums
+    T v[8];
+    T tail = (T)0;
+    int head = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const uint32_t e = ent(j);
+      v[j] = have ? buf[e & ENT_SLOT] : (T)0;
+      if (e & ENT_START) {
+        head = 1;
+        tail = (T)0;
+      }
+      tail += v[j];
+    }
+    T s = tail;
+    int f = head;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T s2 = __shfl_up_sync(0xffffffffu, s, o);
+      const int f2 = __shfl_up_sync(0xffffffffu, f, o);
+      if (lane >= o) {
+        if (!f) s += s2;
+        f |= f2;
+      }
+    }
+    if (lane == 31) {
+      ws_v[par][wid] = s;
+      ws_f[par][wid] = f;
     }
     __syncthreads();
+    T wv = lane < NW ? ws_v[par][lane] : (T)0;
+    int wf = lane < NW ? ws_f[par][lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T s2 = __shfl_up_sync(0xffffffffu, wv, o);
+      const int f2 = __shfl_up_sync(0xffffffffu, wf, o);
+      if (lane >= o) {
+        if (!wf) wv += s2;
+        wf |= f2;
+      }
+    }
+    const T wpre = __shfl_sync(0xffffffffu, wv, wid > 0 ? wid - 1 : 0);
+    const T wprefix = wid > 0 ? wpre : (T)0;
+    const T ex_s = __shfl_up_sync(0xffffffffu, s, 1);
+    const int ex_f = __shfl_up_sync(0xffffffffu, f, 1);
+    const T carry = (lane == 0) ? wprefix : (ex_f ? ex_s : wprefix + ex_s);
+    const int nxt = __shfl_down_sync(0xffffffffu, (ent(0) & ENT_START) ? 1 : 0, 1);
+    if (have) {
+      const bool last_run_ends = tid + 1 >= ne || (lane < 31 ? nxt : ws_first[par][wid + 1]);
+      auto emit = [&](int u, T acc, uint32_t e) {
+        const uint32_t tag = gn[u];
+        const uint32_t g = tag & ~RUN_BDY;
+        if (DIR && (tag & RUN_BDY)) y[g] = x[g];
+        else if (e & ENT_COMPLETE) y[g] = acc;
+        else atomicAdd(&y[g], acc);
+      };
+      int u = (int)cex - 1;
+      T acc = carry;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const uint32_t e = ent(j);
+        if (e & ENT_START) {
+          if (j > 0) emit(u, acc, ent(j - 1));
+          u++;
+          acc = (T)0;
+        }
+        acc += v[j];
+      }
+      if (last_run_ends) emit(u, acc, ent(7));
+    }
   }
 }
 
 template <typename T>
 constexpr size_t patch_smem() {
-  return fsten_entries<T>() * sizeof(T) + PATCH_ENT * sizeof(T) + PKEY_MAX * sstride<T>() * sizeof(T) +
-         PATCH_ENT * sizeof(uint32_t) + 2 * PATCH_ENT * sizeof(uint16_t) + 8 * 18 * sizeof(uint32_t);
+  return fsten_entries<T>() * sizeof(T) + 2 * PATCH_ENT * sizeof(T) + 2 * PATCH_ENT * sizeof(uint32_t) +
+         (8 * 18 + 4) * sizeof(uint32_t) + PKEY_MAX * sstride<T>() * sizeof(T);
 }
 
 }  // namespace dg
