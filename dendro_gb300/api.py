@@ -345,6 +345,22 @@ def coarsenOctree(octree: Octree) -> Octree:
     return Octree(ctx, h)
 
 
+def completeOctree(octants, maxDepth: int = 30, isUnique: bool = False, isSorted: bool = False,
+                   ctx: Context | None = None) -> Octree:
+    """ot::completeOctree (src/construct.cpp:518) at one rank.  ``octants``:
+    n x 4 uint32 records {x, y, z, level} (numpy array or CUDA tensor).  Not
+    declared unique: sorted, duplicates and octants with a descendant in the
+    input dropped; gaps filled with the coarsest octants."""
+    ctx = ctx or default_context()
+    dev = _is_device(octants)
+    a = octants if dev else np.ascontiguousarray(octants, dtype=np.uint32).reshape(-1, 4)
+    n = a.shape[0] if a.ndim > 1 else a.shape[0] // 4
+    h = ctypes.c_void_p()
+    check(ctx.handle, ctx._L.dg_complete_octree(ctx.handle, _ptr(a), n, maxDepth, int(isUnique), int(isSorted),
+                                                1 if dev else 0, ctypes.byref(h)), "completeOctree")
+    return Octree(ctx, h)
+
+
 class DA:
     """ot::DA (src/oda/oda.cpp:250) at one rank, device resident."""
 

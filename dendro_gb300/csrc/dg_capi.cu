@@ -379,6 +379,25 @@ int dg_octree_upload(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDep
   return DG_OK;
 }
 
+int dg_complete_octree(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDepth, int isUnique, int isSorted,
+                       int src_on_device, dg_octree *out) {
+  if (!out || (!xyzl && n) || maxDepth > 30) return DG_ERR_INVALID_ARG;
+  *out = nullptr;
+  dg_octree h = new (std::nothrow) dg_octree_s();
+  if (!h) return DG_ERR_OUT_OF_MEMORY;
+  int rc = guarded(ctx, [&]() {
+    dg::DBuf<uint32_t> hold;
+    const uint32_t *d = device_input(ctx->c, xyzl, 4 * n, src_on_device, hold);
+    dg::complete_octree(ctx->c, d, n, maxDepth, isUnique != 0, isSorted != 0, h->o);
+  });
+  if (rc != DG_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return DG_OK;
+}
+
 const char *dg_ctx_autotune_log(dg_ctx ctx) { return ctx ? ctx->c.tune_log.c_str() : ""; }
 
 int dg_pts_file_count(const char *path, size_t *n) {

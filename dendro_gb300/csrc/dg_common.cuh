@@ -107,6 +107,7 @@ enum {
   DGF_NOT_BALANCED = 2u,   // DA input not 2:1 balanced / not complete
   DGF_TIMEOUT = 4u,        // a bounded spin gave up
   DGF_INTERNAL = 8u,       // internal consistency check failed
+  DGF_ORDER = 16u,         // input not sorted / unique as the caller declared
 };
 
 }  // namespace dg

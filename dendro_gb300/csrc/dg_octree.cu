@@ -266,6 +266,7 @@ void check_device_flags(Context &ctx, const char *where) {
     if (f & DGF_NOT_BALANCED) fail(DG_ERR_NOT_BALANCED, std::string(where) + ": input is not a complete 2:1 balanced octree");
     if (f & DGF_TIMEOUT) fail(DG_ERR_TIMEOUT, std::string(where) + ": a device wait timed out");
     if (f & DGF_INTERNAL) fail(DG_ERR_INTERNAL, std::string(where) + ": internal consistency check failed");
+    if (f & DGF_ORDER) fail(DG_ERR_INVALID_ARG, std::string(where) + ": input is not sorted / unique as declared");
   }
 }
 
@@ -922,6 +923,46 @@ void coarsen_octree(Context &ctx, const Octree &in, Octree &out) {
 }
 
 // ------------------------------------------------------------------------
+// completeOctree (src/construct.cpp:518).  At one rank the reference runs its
+// general path (:534-700): the tree sort's sort + duplicate + ancestor
+// removal when the input is not declared unique (include/sfcSort.h:532-575),
+// a plain sort when it is unique but not declared sorted, then
+// appendCompleteRegion (:1077) between consecutive octants, an octant that is
+// followed by its own descendant being left out.  The filled gaps are the
+// maximal aligned Morton blocks between consecutive leaves (the same blocks
+// appendCompleteRegion emits), so the construction's gap kernels apply.
+// ------------------------------------------------------------------------
+// sort form: the Morton anchor above the 5 level bits, so that a radix sort
+// over the low 3D + 5 bits gives the reference's order (on equal anchors the
+// coarser octant first)
+__global__ void k_to_sortform(const Key128 *__restrict__ in, size_t n, Key128 *__restrict__ out) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = key_or(key_shl(tag_anchor(in[i]), 5), Key128{(uint64_t)tag_level(in[i]), 0});
+}
+
+// octant i is kept unless its successor is its descendant; an order that
+// breaks the caller's declaration raises DGF_ORDER
+__global__ void k_complete_leaves(const Key128 *__restrict__ s, size_t n, unsigned D, bool strict,
+                                  Key128 *__restrict__ val, uint32_t *__restrict__ keep, uint32_t *flags) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Key128 a = s[i];
+  const unsigned la = (unsigned)(a.lo & 31u);
+  bool k = true;
+  if (i + 1 < n) {
+    const Key128 b = s[i + 1];
+    if (key_lt(b, a) || (strict && key_eq(a, b))) atomicOr(flags, DGF_ORDER);
+    const unsigned lb = (unsigned)(b.lo & 31u);
+    if (la < lb) {
+      const unsigned sh = 5 + 3 * (D - la);
+      k = !key_eq(key_shr(a, sh), key_shr(b, sh));
+    }
+  }
+  val[i] = make_tagged(key_shr(a, 5), la);
+  keep[i] = k ? 1u : 0u;
+}
+
+// ------------------------------------------------------------------------
 // one cloud of a batch as its own octree (cloud bits cleared)
 // ------------------------------------------------------------------------
 __global__ void k_strip_cloud(const Key128 *__restrict__ in, size_t n, unsigned D, Key128 *__restrict__ out) {
@@ -1005,6 +1046,58 @@ void octree_free(Context &ctx, Octree &o) {
   if (o.keys) cudaFreeAsync(o.keys, ctx.stream);
   if (o.seg_off) cudaFreeAsync(o.seg_off, ctx.stream);
   o = Octree();
+}
+
+void complete_octree(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned D, bool is_unique, bool is_sorted,
+                     Octree &out) {
+  cudaStream_t s = ctx.stream;
+  out = Octree();
+  out.max_depth = D;
+  if (n == 0) return;  // construct.cpp:587: nothing to complete
+  DBuf<Key128> a(n, s), b(n, s);
+  {
+    ProfScope _prof(ctx, "complete_sortform", (double)n * 48);
+    k_from_xyzl<<<grid_for(n, 256), 256, 0, s>>>(reinterpret_cast<const uint4 *>(d_xyzl), n, D, b.get(),
+                                                 ctx.d_flags);
+    DG_LAUNCH_CHECK();
+    k_to_sortform<<<grid_for(n, 256), 256, 0, s>>>(b.get(), n, a.get());
+    DG_LAUNCH_CHECK();
+  }
+  check_device_flags(ctx, "completeOctree");  // domain and alignment of the records
+  const int bits = 3 * (int)D + 5;
+  Key128 *sorted = a.get();
+  size_t m = n;
+  if (!is_unique) m = sort_unique<Key128>(ctx, a.get(), b.get(), n, bits, &sorted);
+  else if (!is_sorted) sorted = radix_sort<Key128>(ctx, a.get(), b.get(), n, bits);
+  Key128 *other = (sorted == a.get()) ? b.get() : a.get();
+  DBuf<uint32_t> keep(m, s);
+  {
+    ProfScope _prof(ctx, "complete_leaves", (double)m * 36);
+    k_complete_leaves<<<grid_for(m, 256), 256, 0, s>>>(sorted, m, D, is_unique, other, keep.get(), ctx.d_flags);
+    DG_LAUNCH_CHECK();
+  }
+  check_device_flags(ctx, "completeOctree");
+  const size_t ns = compact<Key128>(ctx, other, keep.get(), m, sorted);
+  keep.release();
+  const u128 total = (u128)1 << (3 * D);
+  DBuf<uint32_t> cnt(ns, s);
+  {
+    ProfScope _prof(ctx, "fill_count", (double)ns * 20);
+    k_fill_count<<<grid_for(ns, 256), 256, 0, s>>>(sorted, ns, D, total, cnt.get());
+    DG_LAUNCH_CHECK();
+  }
+  DBuf<uint64_t> off(ns, s);
+  uint64_t *d_total = reinterpret_cast<uint64_t *>(ctx.d_scratch);
+  exclusive_scan<uint32_t, uint64_t>(cnt.get(), off.get(), ns, d_total, s);
+  const size_t nout = (size_t)read_scalar(ctx, d_total);
+  DBuf<Key128> res(nout, s);
+  {
+    ProfScope _prof(ctx, "fill_emit", (double)ns * 24);
+    k_fill_emit<<<grid_for(ns, 256), 256, 0, s>>>(sorted, ns, D, total, off.get(), res.get());
+    DG_LAUNCH_CHECK();
+  }
+  out.n = nout;
+  out.keys = res.release_ptr();
 }
 
 }  // namespace dg

@@ -63,6 +63,12 @@ void octree_extract(Context &ctx, const Octree &in, size_t seg, Octree &out);
 // ot::coarsenOctree (src/coarsen.cpp:53), one cloud.
 void coarsen_octree(Context &ctx, const Octree &in, Octree &out);
 
+// ot::completeOctree (src/construct.cpp:518), one cloud: the octants of
+// d_xyzl (n records x y z level at max_depth), sorted and made unique and
+// linear unless declared so, completed with the coarsest octants.
+void complete_octree(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned max_depth, bool is_unique,
+                     bool is_sorted, Octree &out);
+
 // conversions between tagged keys and {x, y, z, level} u32 records
 void octree_to_xyzl(Context &ctx, const Octree &o, uint32_t *d_xyzl);
 void octree_from_xyzl(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned max_depth, Octree &out);

@@ -141,6 +141,21 @@ int dg_balance_octree(dg_ctx ctx, dg_octree in, int incCorner, int comm_size, dg
  * replaced by its parent.  One cloud per call. */
 int dg_coarsen_octree(dg_ctx ctx, dg_octree in, dg_octree *out);
 
+/* ---- ot::completeOctree ----------------------------------------------------
+ * include/octUtils.h:813 / src/construct.cpp:518 at one rank: the n octants
+ * xyzl ({x, y, z, level} records at maxDepth, host or device memory) are
+ * sorted and made unique when isUnique is 0 (duplicates and every octant
+ * that has a descendant in the input are dropped, include/sfcSort.h:532-575),
+ * sorted when isUnique is 1 and isSorted is 0, and the gaps are filled with
+ * the coarsest octants (appendCompleteRegion, construct.cpp:1077), giving a
+ * sorted, linear, complete octree.  n = 0 gives an empty octree.  Records
+ * outside the domain or not aligned to their level: DG_ERR_DOMAIN.  Input
+ * that breaks its declared order (isSorted = 1 but not sorted, isUnique = 1
+ * with repeated octants): DG_ERR_INVALID_ARG, where the reference returns an
+ * unspecified list. */
+int dg_complete_octree(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDepth, int isUnique, int isSorted,
+                       int src_on_device, dg_octree *out);
+
 /* ---- octree handles --------------------------------------------------------
  * Materialise / import the std::vector<ot::TreeNode> of the reference as
  * {x, y, z, level} records. */

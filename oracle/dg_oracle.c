@@ -446,6 +446,159 @@ int dgo_coarsen(const dgo_oct *in, size_t n, unsigned D, dgo_oct **out, size_t *
 }
 
 /* ------------------------------------------------------------------------ */
+/* completeOctree (src/construct.cpp:518).  At one rank the reference runs   */
+/* completeSubtree and then, with its result overwritten, the general path    */
+/* (:534-700) with one rank; that path is restated here.                      */
+/* ------------------------------------------------------------------------ */
+/* getNCA: the deepest octant that contains both */
+static dgo_oct nca_of(const dgo_oct *a, const dgo_oct *b, unsigned D) {
+  uint32_t d = (a->x ^ b->x) | (a->y ^ b->y) | (a->z ^ b->z);
+  unsigned l = D;
+  if (d) {
+    unsigned h = 31u - (unsigned)__builtin_clz(d); /* highest differing bit */
+    l = D - (h + 1);
+  }
+  if (a->lev < l) l = a->lev;
+  if (b->lev < l) l = b->lev;
+  uint32_t mask = ~((1u << (D - l)) - 1u);
+  dgo_oct r = {a->x & mask, a->y & mask, a->z & mask, l};
+  return r;
+}
+
+static dgo_oct parent_of(const dgo_oct *a, unsigned D) {
+  unsigned l = a->lev ? a->lev - 1 : 0;
+  uint32_t mask = ~((1u << (D - l)) - 1u);
+  dgo_oct r = {a->x & mask, a->y & mask, a->z & mask, l};
+  return r;
+}
+
+/* addChildren, Morton order: child c at x + (c&1)h, y + (c>>1&1)h, z + (c>>2)h */
+static void children_of(const dgo_oct *p, unsigned D, dgo_oct kids[8]) {
+  uint32_t h = (uint32_t)(oct_len(p, D) >> 1);
+  for (unsigned c = 0; c < 8; c++) {
+    dgo_oct k = {p->x + (c & 1u) * h, p->y + ((c >> 1) & 1u) * h, p->z + ((c >> 2) & 1u) * h, p->lev + 1};
+    kids[c] = k;
+  }
+}
+
+/* the top-down part of appendCompleteRegion (:1113-1142, :1172-1204): the
+ * children of t before max, descending into the child that holds max */
+static int region_top_down(dgo_oct t, const dgo_oct *max, unsigned D, oct_vec *v) {
+  int rc, again;
+  do {
+    again = 0;
+    dgo_oct kids[8];
+    children_of(&t, D, kids);
+    for (unsigned j = 0; j < 8; j++) {
+      if (oct_lt(&kids[j], max) && !is_anc(&kids[j], max, D)) {
+        if ((rc = ov_push(v, kids[j]))) return rc;
+      } else if (is_anc(&kids[j], max, D)) {
+        t = kids[j];
+        again = 1;
+        break;
+      } else {
+        break;
+      }
+    }
+  } while (again);
+  return 0;
+}
+
+/* appendCompleteRegion (:1077-1218) */
+static int append_complete_region(dgo_oct first, dgo_oct second, oct_vec *v, int inc_min, int inc_max, unsigned D) {
+  int rc;
+  dgo_oct min = oct_lt(&first, &second) ? first : second;
+  if (inc_min && (rc = ov_push(v, min))) return rc;
+  if (oct_eq(&first, &second)) return 0;
+  dgo_oct max = oct_lt(&second, &first) ? first : second;
+  dgo_oct nca = nca_of(&min, &max, D);
+  if (oct_eq(&min, &nca)) {
+    if ((rc = region_top_down(min, &max, D, v))) return rc;
+  } else {
+    dgo_oct cur = min;
+    while (oct_lt(&nca, &cur)) {
+      dgo_oct par = parent_of(&cur, D), bros[8];
+      children_of(&par, D, bros);
+      for (unsigned i = 0; i < 8; i++) {
+        if (oct_lt(&min, &bros[i]) && oct_lt(&bros[i], &max) && !is_anc(&bros[i], &max, D)) {
+          if ((rc = ov_push(v, bros[i]))) return rc;
+        } else if (is_anc(&bros[i], &max, D)) {
+          if ((rc = region_top_down(bros[i], &max, D, v))) return rc;
+          break;
+        }
+      }
+      cur = par;
+    }
+  }
+  if (inc_max && (rc = ov_push(v, max))) return rc;
+  return 0;
+}
+
+int dgo_complete(const dgo_oct *in, size_t n, unsigned D, int is_unique, int is_sorted, dgo_oct **out, size_t *nout) {
+  if (D > 30) return DGO_EINVAL;
+  dgo_oct *a = (dgo_oct *)malloc((n ? n : 1) * sizeof(dgo_oct));
+  if (!a) return DGO_ENOMEM;
+  if (n) memcpy(a, in, n * sizeof(dgo_oct));
+  int rc;
+  if (!is_unique) {
+    /* tree sort with TS_REMOVE_DUPLICATES (include/sfcSort.h:532-575): sort,
+     * drop repeats, then replace every octant by its following descendant */
+    if ((rc = sort_octs(a, n))) goto fail;
+    size_t w = 0;
+    for (size_t i = 0; i < n; i++)
+      if (w == 0 || !oct_eq(&a[w - 1], &a[i])) a[w++] = a[i];
+    size_t m = w;
+    w = 0;
+    for (size_t i = 0; i < m; i++) {
+      if (w > 0 && is_anc(&a[w - 1], &a[i], D))
+        a[w - 1] = a[i];
+      else
+        a[w++] = a[i];
+    }
+    n = w;
+  } else if (!is_sorted) {
+    if ((rc = sort_octs(a, n))) goto fail;
+  }
+  oct_vec v = {0, 0, 0};
+  if (n) {
+    oct_vec lst = {0, 0, 0};
+    dgo_oct min_corner = {0, 0, 0, D}, root = {0, 0, 0, 0};
+    dgo_oct max_corner = get_dld(&root, D);
+    if (!oct_eq(&a[0], &min_corner) && !is_anc(&a[0], &min_corner, D)) { /* :598-607 */
+      dgo_oct nc = nca_of(&a[0], &min_corner, D), kids[8];
+      children_of(&nc, D, kids);
+      if ((rc = ov_push(&lst, kids[0]))) goto fail_v;
+    }
+    for (size_t i = 0; i < n; i++)
+      if ((rc = ov_push(&lst, a[i]))) goto fail_v;
+    if (!oct_eq(&a[n - 1], &max_corner) && !is_anc(&a[n - 1], &max_corner, D)) { /* :610-622 */
+      dgo_oct nc = nca_of(&a[n - 1], &max_corner, D), kids[8];
+      children_of(&nc, D, kids);
+      if ((rc = ov_push(&lst, kids[7]))) goto fail_v;
+    }
+    for (size_t i = 0; i + 1 < lst.n; i++) { /* :625-640 */
+      int anc = is_anc(&lst.a[i], &lst.a[i + 1], D);
+      if ((rc = append_complete_region(lst.a[i], lst.a[i + 1], &v, !anc, 0, D))) {
+        free(lst.a);
+        goto fail_v;
+      }
+    }
+    rc = ov_push(&v, lst.a[lst.n - 1]); /* :645 */
+    free(lst.a);
+    if (rc) goto fail_v;
+  }
+  free(a);
+  *out = v.a ? v.a : (dgo_oct *)malloc(sizeof(dgo_oct));
+  *nout = v.n;
+  return 0;
+fail_v:
+  free(v.a);
+fail:
+  free(a);
+  return rc;
+}
+
+/* ------------------------------------------------------------------------ */
 /* checkers                                                                  */
 /* ------------------------------------------------------------------------ */
 int dgo_is_sorted_unique(const dgo_oct *a, size_t n, unsigned D) {

@@ -65,6 +65,11 @@ int dgo_coarsen(const dgo_oct *in, size_t n, unsigned maxDepth, dgo_oct **out, s
 
 /* Checkers mirroring src/test/testUtils.C:18 (isLinear), :28 (isComplete)
  * and :82 (isBalanced with corners, maxLevDiff 1).  Return 1 / 0. */
+/* completeOctree (src/construct.cpp:518) at one rank, input in any order
+ * unless declared sorted / unique. */
+int dgo_complete(const dgo_oct *in, size_t n, unsigned maxDepth, int isUnique, int isSorted, dgo_oct **out,
+                 size_t *nout);
+
 int dgo_is_sorted_unique(const dgo_oct *a, size_t n, unsigned maxDepth);
 int dgo_is_linear(const dgo_oct *a, size_t n, unsigned maxDepth);
 int dgo_is_complete(const dgo_oct *a, size_t n, unsigned maxDepth);

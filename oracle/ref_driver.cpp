@@ -15,6 +15,9 @@
  *         defect of comboRipple above 1e7 octants (balance.cpp:821-900).
  *   coarsen IN.oct MAXDEPTH OUT.oct
  *         ot::coarsenOctree, sequential form (src/coarsen.cpp:53).
+ *   complete IN.oct MAXDEPTH ISUNIQUE ISSORTED OUT.oct
+ *         ot::completeOctree (src/construct.cpp:518) at 1 rank, with the
+ *         input octants in file order.
  *   check IN.oct MAXDEPTH
  *         ot::test::isLinear / isComplete / isBalanced (src/test/testUtils.C).
  *   da    BAL.oct MAXDEPTH STENCILDIR VEC_IN|- OUT_PREFIX
@@ -146,6 +149,20 @@ static int mode_coarsen(int argc, char **argv) {
   double t1 = now_s();
   write_oct(argv[4], out);
   std::printf("{\"op\":\"coarsen\",\"n_in\":%zu,\"n_out\":%zu,\"seconds\":%.6f}\n", in.size(), out.size(), t1 - t0);
+  return 0;
+}
+
+static int mode_complete(int argc, char **argv) {
+  if (argc < 7) return 1;
+  unsigned maxDepth = std::atoi(argv[3]);
+  bool isUnique = std::atoi(argv[4]) != 0, isSorted = std::atoi(argv[5]) != 0;
+  std::vector<ot::TreeNode> in = read_oct(argv[2], maxDepth), out;
+  double t0 = now_s();
+  ot::completeOctree(in, out, 3, maxDepth, isUnique, isSorted, false, MPI_COMM_WORLD);
+  double t1 = now_s();
+  write_oct(argv[6], out);
+  std::printf("{\"op\":\"complete\",\"n_in\":%zu,\"n_out\":%zu,\"seconds\":%.6f}\n", in.size(), out.size(),
+              t1 - t0);
   return 0;
 }
 
@@ -394,6 +411,7 @@ int main(int argc, char **argv) {
   if (m == "bal") rc = mode_bal(argc, argv);
   if (m == "check") rc = mode_check(argc, argv);
   if (m == "coarsen") rc = mode_coarsen(argc, argv);
+  if (m == "complete") rc = mode_complete(argc, argv);
   if (m == "da") rc = mode_da(argc, argv);
   if (m == "io") rc = mode_io(argc, argv);
   return rc;

@@ -55,3 +55,74 @@ def nodal_function(xyz_u32: np.ndarray) -> np.ndarray:
     """Smooth nodal field used for the matVec fixture (coordinates at maxDepth 30)."""
     c = np.asarray(xyz_u32, np.float64) / float(1 << 30)
     return np.sin(3.0 * c[:, 0]) * np.cos(2.0 * c[:, 1]) + c[:, 2] ** 2 - 0.5
+
+
+def sparse_octants(rng, D: int, lmax: int, keep: float = 0.3, p_split: float = 0.6, n_anc: int = 0,
+                   n_dup: int = 0) -> np.ndarray:
+    """Octants {x, y, z, level} at maxDepth D for completeOctree: the leaves
+    of a random refinement of the root (levels <= lmax), a random subset of
+    them (so the set has gaps), plus n_anc ancestors of chosen leaves and
+    n_dup repeated octants, shuffled."""
+    leaves, stack = [], [(0, 0, 0, 0)]
+    while stack:
+        x, y, z, lev = stack.pop()
+        if lev < lmax and (lev == 0 or rng.random() < p_split):
+            h = 1 << (D - lev - 1)
+            for c in range(8):
+                stack.append((x + (c & 1) * h, y + ((c >> 1) & 1) * h, z + ((c >> 2) & 1) * h, lev + 1))
+        else:
+            leaves.append((x, y, z, lev))
+    octs = np.array(leaves, np.uint32).reshape(-1, 4)
+    octs = octs[rng.random(len(octs)) < keep]
+    if len(octs) == 0:
+        octs = np.array(leaves[:1], np.uint32)
+    extra = []
+    for _ in range(n_anc):
+        x, y, z, lev = octs[rng.integers(len(octs))].tolist()
+        if lev >= 2:
+            la = int(rng.integers(1, lev))
+            m = ~((1 << (D - la)) - 1) & 0xFFFFFFFF
+            extra.append((x & m, y & m, z & m, la))
+    if extra:
+        octs = np.concatenate([octs, np.array(extra, np.uint32)])
+    if n_dup:
+        octs = np.concatenate([octs, octs[rng.integers(0, len(octs), n_dup)]])
+    rng.shuffle(octs)
+    return np.ascontiguousarray(octs, np.uint32)
+
+
+def morton_sort(octs: np.ndarray, D: int) -> np.ndarray:
+    """Unique octants in the reference's Morton order (ancestor first)."""
+    def key(o):
+        x, y, z, lev = (int(v) for v in o)
+        m = 0
+        for b in range(D):
+            m |= (((x >> b) & 1) << (3 * b)) | (((y >> b) & 1) << (3 * b + 1)) | (((z >> b) & 1) << (3 * b + 2))
+        return (m << 5) | lev
+    uniq = {tuple(int(v) for v in o): o for o in octs}
+    return np.array(sorted(uniq.keys(), key=key), np.uint32).reshape(-1, 4)
+
+
+def complete_inputs():
+    """(name, octants, maxDepth, isUnique, isSorted) cases for completeOctree;
+    the declared flags are always true of the input."""
+    rng = np.random.Generator(np.random.PCG64(2024))
+    out = [
+        ("empty", np.zeros((0, 4), np.uint32), 8, 0, 0),
+        ("root", np.array([[0, 0, 0, 0]], np.uint32), 8, 0, 0),
+        ("one_D4", np.array([[4, 8, 0, 2]], np.uint32), 4, 0, 0),
+        ("min_corner_D5", np.array([[0, 0, 0, 5]], np.uint32), 5, 1, 1),
+        ("max_corner_D5", np.array([[31, 31, 31, 5]], np.uint32), 5, 1, 1),
+        ("both_corners_D30", np.array([[0, 0, 0, 30], [2 ** 30 - 1] * 3 + [30]], np.uint32), 30, 1, 1),
+    ]
+    for i in range(24):
+        D = int(rng.choice([3, 6, 10, 20, 30]))
+        octs = sparse_octants(rng, D, min(D, int(rng.integers(2, 6))), keep=float(rng.uniform(0.05, 0.8)),
+                              n_anc=int(rng.integers(0, 3)), n_dup=int(rng.integers(0, 20)))
+        srt = morton_sort(octs, D)
+        shuf = srt.copy()
+        rng.shuffle(shuf)
+        out.append((f"sparse{i}_any", octs, D, 0, 0))
+        out.append((f"sparse{i}_sorted", srt, D, 1, 1))
+        out.append((f"sparse{i}_unique", shuf, D, 1, 0))
+    return out

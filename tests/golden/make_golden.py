@@ -10,6 +10,11 @@ outputs next to the inputs:
                   statistics of the type-2 stencil tables and of the
                   restriction stencils RmatType1/2 (Stencils/*.inp)
   ref_hashes.json counts and FNV-1a hashes of larger octrees
+  ref_complete.npz completeOctree outputs (cases.complete_inputs), or the
+                  reference's abort on inputs that hold an octant and a
+                  descendant in its first child (getNCA's assertion,
+                  src/octFunctions.cpp:310)
+  io/             the reference's point and octree files
 
 Usage:  python tests/golden/make_golden.py [/path/to/reference]
 """
@@ -105,7 +110,32 @@ def make_io():
         json.dump(info, f, indent=1, sort_keys=True)
 
 
+def make_complete():
+    """ot::completeOctree on cases.complete_inputs(): ref_complete.npz."""
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        fi, fo = os.path.join(tmp, "in.oct"), os.path.join(tmp, "out.oct")
+        for name, octs, D, uniq, srt in cases.complete_inputs():
+            write_oct(fi, octs)
+            try:
+                run("complete", fi, D, uniq, srt, fo)
+                res, aborted = read_oct(fo), False
+            except subprocess.CalledProcessError as e:
+                assert "getNCA" in e.stderr, e.stderr
+                res, aborted = np.zeros((0, 4), np.uint32), True
+            out[f"{name}/in"] = octs
+            out[f"{name}/params"] = np.array([D, uniq, srt], np.int64)
+            out[f"{name}/out"] = res
+            out[f"{name}/aborted"] = np.bool_(aborted)
+    np.savez_compressed(os.path.join(HERE, "ref_complete.npz"), **out)
+
+
 def main():
+    if "--complete-only" in sys.argv:
+        if not os.path.exists(DRIVER):
+            subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), f"REF={REF}"])
+        make_complete()
+        return
     if "--io-only" in sys.argv:
         if not os.path.exists(DRIVER):
             subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), f"REF={REF}"])
@@ -205,6 +235,7 @@ def main():
                         rmat2_stats=rmat("RmatType2Stencils.inp", (8, 18, 8, 8)))
     print("golden fixtures written to", HERE)
     make_io()
+    make_complete()
 
 
 if __name__ == "__main__":
