@@ -113,6 +113,42 @@ int balanceOctree(std::vector<TN> &in, std::vector<TN> &out, unsigned int dim, u
   return 1;
 }
 
+// ot::completeOctree (include/octUtils.h:813, src/construct.cpp:518) at one
+// rank.  A declared order the input breaks throws DG_ERR_INVALID_ARG.
+template <class TN>
+int completeOctree(const std::vector<TN> &in, std::vector<TN> &out, unsigned int dim, unsigned int maxDepth,
+                   bool isUnique, bool isSorted, bool /*assertNoEmptyProcs*/ = false, int /*comm_size*/ = 1) {
+  if (dim != 3) throw cxx::Error(DG_ERR_UNSUPPORTED, "completeOctree: only dim = 3");
+  dg_ctx c = cxx::context();
+  std::vector<uint32_t> r = cxx::nodes_to_records(in);
+  dg_octree o = nullptr;
+  cxx::check(c, dg_complete_octree(c, r.data(), in.size(), maxDepth, isUnique ? 1 : 0, isSorted ? 1 : 0, 0, &o),
+             "completeOctree");
+  r = cxx::download(c, o);
+  dg_octree_free(c, o);
+  cxx::records_to_nodes(r, maxDepth, out);
+  return 1;
+}
+
+// ot::coarsenOctree (include/octUtils.h:825, sequential form src/coarsen.cpp:53):
+// every complete family of 8 sibling leaves replaced by its parent.
+template <class TN>
+int coarsenOctree(const std::vector<TN> &in, std::vector<TN> &out, unsigned int dim, unsigned int maxDepth,
+                  int /*comm_size*/ = 1) {
+  if (dim != 3) throw cxx::Error(DG_ERR_UNSUPPORTED, "coarsenOctree: only dim = 3");
+  dg_ctx c = cxx::context();
+  std::vector<uint32_t> r = cxx::nodes_to_records(in);
+  dg_octree a = nullptr, b = nullptr;
+  cxx::check(c, dg_octree_upload(c, r.data(), in.size(), maxDepth, 0, &a), "coarsenOctree (upload)");
+  int st = dg_coarsen_octree(c, a, &b);
+  dg_octree_free(c, a);
+  cxx::check(c, st, "coarsenOctree");
+  r = cxx::download(c, b);
+  dg_octree_free(c, b);
+  cxx::records_to_nodes(r, maxDepth, out);
+  return 1;
+}
+
 // par::removeDuplicates of point octants at level maxDepth
 // (include/parUtils.h:437), from FP64 points.
 template <class TN>

@@ -2,7 +2,8 @@
 // octant type shaped like the reference's ot::TreeNode constructor.
 // Reads FP64 points (u64 n, then 3n doubles), runs points2Octree ->
 // balanceOctree -> DA -> matVec, writes the balanced octree as {x,y,z,level}
-// records and prints sizes.  Driven by tests/test_gpu_cpp_dropin.py.
+// records and prints sizes; then coarsenOctree of the balanced octree and
+// completeOctree of every 5th balanced octant in reverse order.  Driven by tests/test_gpu_cpp_dropin.py.
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -47,9 +48,18 @@ int main(int argc, char **argv) {
     std::fwrite(r, 4, 4, g);
   }
   std::fclose(g);
+  std::vector<MyNode> coarse, sub, comp, same;
+  dg::ot::coarsenOctree(bal, coarse, 3, 30);
+  for (size_t i = 0; i < bal.size(); i += 5) sub.push_back(bal[bal.size() - 1 - i]);
+  dg::ot::completeOctree(sub, comp, 3, 30, false, false);
+  dg::ot::completeOctree(bal, same, 3, 30, true, true);
+  bool same_ok = same.size() == bal.size();
+  for (size_t i = 0; same_ok && i < bal.size(); i++)
+    same_ok = same[i].x == bal[i].x && same[i].y == bal[i].y && same[i].z == bal[i].z && same[i].lev == bal[i].lev;
   // sum of the mass matrix applied to ones = volume of the unit cube
-  std::printf("{\"n_lin\": %zu, \"n_bal\": %zu, \"n_elem\": %u, \"n_node\": %u, \"sum_A1\": %.15f}\n", nlin, bal.size(),
-              da.getElementSize(), da.getNodeSize(), s);
+  std::printf("{\"n_lin\": %zu, \"n_bal\": %zu, \"n_elem\": %u, \"n_node\": %u, \"sum_A1\": %.15f, "
+              "\"n_coarse\": %zu, \"n_complete_sub\": %zu, \"complete_bal_same\": %d}\n",
+              nlin, bal.size(), da.getElementSize(), da.getNodeSize(), s, coarse.size(), comp.size(), same_ok ? 1 : 0);
   // error path: a communicator of size 2 is refused
   try {
     std::vector<double> p2 = {0.5, 0.5, 0.5, 0.25, 0.25, 0.25};

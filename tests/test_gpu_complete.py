@@ -60,7 +60,7 @@ def test_edge_and_error_cases(ctx):
     assert completeOctree(np.zeros((0, 4), np.uint32), 30, ctx=ctx).size == 0
     assert completeOctree(np.array([[0, 0, 0, 0]], np.uint32), 30, ctx=ctx).to_numpy().tolist() == [[0, 0, 0, 0]]
     with pytest.raises(DendroError) as e:  # anchor not aligned to its level
-        completeOctree(np.array([[4, 0, 0, 2]], np.uint32), 4, ctx=ctx)
+        completeOctree(np.array([[2, 0, 0, 2]], np.uint32), 4, ctx=ctx)
     assert e.value.status == DG_ERR_DOMAIN
     with pytest.raises(DendroError) as e:  # level above maxDepth
         completeOctree(np.array([[0, 0, 0, 5]], np.uint32), 4, ctx=ctx)

@@ -36,3 +36,7 @@ def test_cpp_dropin(oracle, tmp_path):
     assert info["n_node"] == oracle.DA(ref, 30).n_node
     # mass matrix applied to ones sums to the domain volume
     assert abs(info["sum_A1"] - 1.0) < 1e-12
+    assert info["n_coarse"] == len(oracle.coarsen(ref, 30))
+    sub = ref[::-1][::5]
+    assert info["n_complete_sub"] == len(oracle.complete(sub, 30, 0, 0))
+    assert info["complete_bal_same"] == 1
