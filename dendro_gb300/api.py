@@ -77,6 +77,18 @@ class Context:
         """Start (or stop) per-kernel timing; clears the statistics."""
         check(self.handle, self._L.dg_ctx_profile(self.handle, 1 if enable else 0), "dg_ctx_profile")
 
+    def set_order(self, order: str):
+        """Order of octant records at the boundary: "morton" (default) or
+        "hilbert" (the reference's default HILBERT_ORDERING build)."""
+        code = {"morton": 0, "hilbert": 1}[order]
+        check(self.handle, self._L.dg_ctx_set_order(self.handle, code), "dg_ctx_set_order")
+
+    @property
+    def order(self) -> str:
+        v = ctypes.c_int()
+        check(self.handle, self._L.dg_ctx_get_order(self.handle, ctypes.byref(v)), "dg_ctx_get_order")
+        return ("morton", "hilbert")[v.value]
+
     def autotune_log(self) -> str:
         """The autotuner's decisions on this context, one line each."""
         return self._L.dg_ctx_autotune_log(self.handle).decode()

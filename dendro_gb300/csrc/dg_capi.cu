@@ -400,6 +400,18 @@ int dg_complete_octree(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxD
 
 const char *dg_ctx_autotune_log(dg_ctx ctx) { return ctx ? ctx->c.tune_log.c_str() : ""; }
 
+int dg_ctx_set_order(dg_ctx ctx, int order) {
+  if (!ctx || (order != DG_ORDER_MORTON && order != DG_ORDER_HILBERT)) return DG_ERR_INVALID_ARG;
+  ctx->c.order = order;
+  return DG_OK;
+}
+
+int dg_ctx_get_order(dg_ctx ctx, int *order) {
+  if (!ctx || !order) return DG_ERR_INVALID_ARG;
+  *order = ctx->c.order;
+  return DG_OK;
+}
+
 int dg_pts_file_count(const char *path, size_t *n) {
   if (!path || !n) return DG_ERR_INVALID_ARG;
   try {

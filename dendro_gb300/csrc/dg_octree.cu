@@ -26,6 +26,7 @@
 #include "dg_walk.cuh"
 
 #include <algorithm>
+#include <array>
 #include <vector>
 
 namespace dg {
@@ -940,6 +941,11 @@ __global__ void k_to_sortform(const Key128 *__restrict__ in, size_t n, Key128 *_
   if (i < n) out[i] = key_or(key_shl(tag_anchor(in[i]), 5), Key128{(uint64_t)tag_level(in[i]), 0});
 }
 
+__global__ void k_from_sortform(const Key128 *__restrict__ in, size_t n, Key128 *__restrict__ out) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = make_tagged(key_shr(in[i], 5), (unsigned)(in[i].lo & 31u));
+}
+
 // octant i is kept unless its successor is its descendant; an order that
 // breaks the caller's declaration raises DGF_ORDER
 __global__ void k_complete_leaves(const Key128 *__restrict__ s, size_t n, unsigned D, bool strict,
@@ -1016,8 +1022,145 @@ __global__ void k_from_xyzl(const uint4 *__restrict__ in, size_t n, unsigned D, 
   out[i] = make_tagged(morton3(v.x, v.y, v.z), lev);
 }
 
+// ------------------------------------------------------------------------
+// Hilbert order (the reference's default build, -DHILBERT_ORDERING:
+// TreeNode::operator< include/TreeNode.tcc:130-210 with the tables of
+// src/hcurvedata.cpp:329-520).  The curve is self-similar: a cell's 8
+// children are visited in the order HIL_BASE_ORDER, transformed by the
+// cell's own symmetry, and each child's cell carries its parent's symmetry
+// composed with HIL_CHILD_SYM of its base position.  A state table of the
+// reachable symmetries (24) is generated from these two rows; an octant's
+// key is its child ranks root to leaf (3 bits per level), padded to maxDepth,
+// above its level, which orders octants as the reference's comparison does
+// (an ancestor before its descendants).
+// ------------------------------------------------------------------------
+namespace {
+// corner index c = x | y << 1 | z << 2
+constexpr uint8_t HIL_BASE_ORDER[8] = {0, 2, 3, 1, 5, 7, 6, 4};
+// child symmetry per base corner: new bit i = old bit perm[i] ^ bit i of flip
+struct CubeSym {
+  uint8_t perm[3];
+  uint8_t flip;
+};
+constexpr CubeSym HIL_CHILD_SYM[8] = {{{0, 2, 1}, 0}, {{2, 0, 1}, 6}, {{2, 1, 0}, 0}, {{0, 1, 2}, 0},
+                                      {{0, 2, 1}, 6}, {{2, 0, 1}, 3}, {{2, 1, 0}, 5}, {{0, 1, 2}, 0}};
+constexpr int HIL_MAX_STATES = 32;
+
+struct HilbertTable {
+  uint8_t e[HIL_MAX_STATES * 8];  // [state][corner]: rank | next state << 3
+};
+
+HilbertTable build_hilbert_table() {
+  using Map = std::array<uint8_t, 8>;  // a symmetry as its action on corners
+  auto sym_map = [](const CubeSym &g) {
+    Map m{};
+    for (unsigned c = 0; c < 8; c++) {
+      unsigned r = 0;
+      for (unsigned i = 0; i < 3; i++) r |= (((c >> g.perm[i]) & 1u) ^ ((g.flip >> i) & 1u)) << i;
+      m[c] = (uint8_t)r;
+    }
+    return m;
+  };
+  uint8_t rank0[8];
+  for (unsigned k = 0; k < 8; k++) rank0[HIL_BASE_ORDER[k]] = (uint8_t)k;
+  std::vector<Map> states;
+  Map id{};
+  for (unsigned c = 0; c < 8; c++) id[c] = (uint8_t)c;
+  states.push_back(id);
+  HilbertTable t{};
+  for (size_t s = 0; s < states.size(); s++) {
+    const Map g = states[s];
+    Map ginv{};
+    for (unsigned c = 0; c < 8; c++) ginv[g[c]] = (uint8_t)c;
+    for (unsigned c = 0; c < 8; c++) {
+      const unsigned c0 = ginv[c];
+      const Map tc = sym_map(HIL_CHILD_SYM[c0]);
+      Map child{};
+      for (unsigned q = 0; q < 8; q++) child[q] = g[tc[q]];
+      size_t id2 = std::find(states.begin(), states.end(), child) - states.begin();
+      if (id2 == states.size()) {
+        if (states.size() == HIL_MAX_STATES) fail(DG_ERR_INTERNAL, "Hilbert table: too many states");
+        states.push_back(child);
+      }
+      t.e[s * 8 + c] = (uint8_t)(rank0[c0] | (id2 << 3));
+    }
+  }
+  return t;
+}
+
+const HilbertTable &hilbert_table() {
+  static const HilbertTable t = build_hilbert_table();
+  return t;
+}
+}  // namespace
+
+// key[i] = (Hilbert rank path << 5 | level) << 32 | i for the octants of
+// one cloud (i < 2^32)
+__global__ void k_hilbert_keys(const Key128 *__restrict__ k, size_t n, unsigned D, bool batched, HilbertTable tab,
+                               Key128 *__restrict__ out) {
+  __shared__ uint8_t t[HIL_MAX_STATES * 8];
+  for (int i = threadIdx.x; i < HIL_MAX_STATES * 8; i += blockDim.x) t[i] = tab.e[i];
+  __syncthreads();
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t x, y, z;
+  demorton3(batched ? morton_part(k[i], D) : tag_anchor(k[i]), x, y, z);
+  const unsigned lev = tag_level(k[i]);
+  u128 h = 0;
+  unsigned st = 0;
+  for (unsigned l = 0; l < lev; l++) {
+    const unsigned b = D - 1 - l;
+    const unsigned c = ((x >> b) & 1u) | (((y >> b) & 1u) << 1) | (((z >> b) & 1u) << 2);
+    const unsigned e = t[st * 8 + c];
+    h = (h << 3) | (e & 7u);
+    st = e >> 3;
+  }
+  h <<= 3 * (D - lev);
+  out[i] = from_u128((((h << 5) | lev) << 32) | (u128)(uint32_t)i);
+}
+
+__global__ void k_gather_xyzl(const Key128 *__restrict__ k, const Key128 *__restrict__ order, size_t n, unsigned D,
+                              bool batched, uint4 *__restrict__ out) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Key128 v = k[(uint32_t)order[i].lo];
+  uint32_t x, y, z;
+  demorton3(batched ? morton_part(v, D) : tag_anchor(v), x, y, z);
+  out[i] = make_uint4(x, y, z, tag_level(v));
+}
+
+// records of o in Hilbert order, cloud by cloud
+static void octree_to_xyzl_hilbert(Context &ctx, const Octree &o, uint32_t *d_xyzl) {
+  cudaStream_t s = ctx.stream;
+  const unsigned D = o.max_depth;
+  std::vector<uint64_t> off{0, (uint64_t)o.n};
+  if (o.nseg > 1) {
+    off.resize(o.nseg + 1);
+    DG_CUDA(cudaMemcpyAsync(off.data(), o.seg_off, (o.nseg + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    DG_CUDA(cudaStreamSynchronize(s));
+  }
+  const HilbertTable &tab = hilbert_table();
+  DBuf<Key128> a(o.n, s), b(o.n, s);
+  for (size_t g = 0; g + 1 < off.size(); g++) {
+    const size_t n = off[g + 1] - off[g];
+    if (!n) continue;
+    if (n > 0xffffffffull) fail(DG_ERR_UNSUPPORTED, "Hilbert order: more than 2^32 octants in one cloud");
+    ProfScope _prof(ctx, "hilbert_order", (double)n * 16 * 36);
+    k_hilbert_keys<<<grid_for(n, 256), 256, 0, s>>>(o.keys + off[g], n, D, o.nseg > 1, tab, a.get() + off[g]);
+    DG_LAUNCH_CHECK();
+    Key128 *srt = radix_sort<Key128>(ctx, a.get() + off[g], b.get() + off[g], n, 3 * (int)D + 5 + 32);
+    k_gather_xyzl<<<grid_for(n, 256), 256, 0, s>>>(o.keys + off[g], srt, n, D, o.nseg > 1,
+                                                   reinterpret_cast<uint4 *>(d_xyzl) + off[g]);
+    DG_LAUNCH_CHECK();
+  }
+}
+
 void octree_to_xyzl(Context &ctx, const Octree &o, uint32_t *d_xyzl) {
   if (!o.n) return;
+  if (ctx.order == 1) {
+    octree_to_xyzl_hilbert(ctx, o, d_xyzl);
+    return;
+  }
   {
     ProfScope _prof("to_xyzl", (double)o.n * 32);
     k_to_xyzl<<<grid_for(o.n, 256), 256, 0, ctx.stream>>>(o.keys, o.n, o.max_depth, o.nseg > 1,
@@ -1038,6 +1181,14 @@ void octree_from_xyzl(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned D
       DG_LAUNCH_CHECK();
     }
     check_device_flags(ctx, "octree upload");
+    if (ctx.order == 1) {  // records in Hilbert order: the device keeps Morton order
+      DBuf<Key128> a(n, ctx.stream), b(n, ctx.stream);
+      k_to_sortform<<<grid_for(n, 256), 256, 0, ctx.stream>>>(k.get(), n, a.get());
+      DG_LAUNCH_CHECK();
+      Key128 *srt = radix_sort<Key128>(ctx, a.get(), b.get(), n, 3 * (int)D + 5);
+      k_from_sortform<<<grid_for(n, 256), 256, 0, ctx.stream>>>(srt, n, k.get());
+      DG_LAUNCH_CHECK();
+    }
   }
   out.keys = k.release_ptr();
 }
@@ -1065,6 +1216,7 @@ void complete_octree(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned D,
   }
   check_device_flags(ctx, "completeOctree");  // domain and alignment of the records
   const int bits = 3 * (int)D + 5;
+  if (ctx.order == 1) is_sorted = false;  // records in Hilbert order: sorted into Morton order here
   Key128 *sorted = a.get();
   size_t m = n;
   if (!is_unique) m = sort_unique<Key128>(ctx, a.get(), b.get(), n, bits, &sorted);

@@ -55,6 +55,10 @@ struct Context {
   // log2 of the key count); 0 = not tuned yet, else the items per thread
   int tune_items[2][64] = {};
   std::string tune_log;  // one line per decision
+  // order of octant records at the boundary (downloads, uploads, files):
+  // 0 Morton, 1 Hilbert (the reference's HILBERT_ORDERING builds); the
+  // octrees themselves are always kept in Morton order on the device
+  int order = 0;
 };
 
 // thrown inside the library, converted to a status code at the C ABI

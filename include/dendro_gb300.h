@@ -66,6 +66,19 @@ const char *dg_ctx_last_error(dg_ctx ctx);
  * sort's tile: each size class's first sort times both tiles on its first
  * digit pass and keeps the faster).  No counterpart in the reference. */
 const char *dg_ctx_autotune_log(dg_ctx ctx);
+/* Order of octant records at the boundary: DG_ORDER_MORTON (default, the
+ * reference built without HILBERT_ORDERING) or DG_ORDER_HILBERT (the
+ * reference's default build, CMakeLists.txt:48; TreeNode::operator<
+ * include/TreeNode.tcc:130-210 with the tables of src/hcurvedata.cpp).
+ * Records leave the library (octree downloads, sortUniquePoints, MG level
+ * octrees, octree files) in this order and octant records given to it
+ * (octree uploads, completeOctree, octree files) are read in any order and
+ * sorted.  The same octrees result in both orders; only the records' order
+ * differs.  dg_sort_unique_points_noalloc has no context and stays Morton. */
+#define DG_ORDER_MORTON 0
+#define DG_ORDER_HILBERT 1
+int dg_ctx_set_order(dg_ctx ctx, int order);
+int dg_ctx_get_order(dg_ctx ctx, int *order);
 const char *dg_status_string(int status);
 int dg_version(void);
 

@@ -599,6 +599,129 @@ fail:
 }
 
 /* ------------------------------------------------------------------------ */
+/* Hilbert order: TreeNode::operator< of the reference's default build       */
+/* (-DHILBERT_ORDERING, include/TreeNode.tcc:130-210).  Its rotation tables  */
+/* (src/hcurvedata.cpp:329-520) describe a self-similar curve: the base      */
+/* cell visits its children in the order below, and each child cell carries */
+/* its parent's symmetry composed with a fixed symmetry of its base corner.  */
+/* The tables are generated here from those two rows.                        */
+/* ------------------------------------------------------------------------ */
+static const unsigned char hil_base[8] = {0, 2, 3, 1, 5, 7, 6, 4};
+/* per base corner: new bit i of a corner = old bit perm[i] ^ bit i of flip */
+static const unsigned char hil_child_perm[8][3] = {{0, 2, 1}, {2, 0, 1}, {2, 1, 0}, {0, 1, 2},
+                                                   {0, 2, 1}, {2, 0, 1}, {2, 1, 0}, {0, 1, 2}};
+static const unsigned char hil_child_flip[8] = {0, 6, 0, 0, 6, 3, 5, 0};
+
+typedef struct {
+  int n;                         /* states */
+  unsigned char map[48][8];      /* each state's symmetry, as its corner map */
+  unsigned char rank[48][8];     /* [state][corner] -> visit position */
+  unsigned char next[48][8];     /* [state][corner] -> child's state */
+} hil_tables;
+
+static void hil_build(hil_tables *t) {
+  unsigned char rank0[8];
+  for (int k = 0; k < 8; k++) rank0[hil_base[k]] = (unsigned char)k;
+  t->n = 1;
+  for (int c = 0; c < 8; c++) t->map[0][c] = (unsigned char)c;
+  for (int s = 0; s < t->n; s++) {
+    unsigned char inv[8];
+    for (int c = 0; c < 8; c++) inv[t->map[s][c]] = (unsigned char)c;
+    for (int c = 0; c < 8; c++) {
+      int c0 = inv[c];
+      unsigned char child[8];
+      for (int q = 0; q < 8; q++) {
+        int r = 0;
+        for (int i = 0; i < 3; i++) r |= (((q >> hil_child_perm[c0][i]) & 1) ^ ((hil_child_flip[c0] >> i) & 1)) << i;
+        child[q] = t->map[s][r];
+      }
+      int id = 0;
+      while (id < t->n && memcmp(t->map[id], child, 8) != 0) id++;
+      if (id == t->n) memcpy(t->map[t->n++], child, 8);
+      t->rank[s][c] = rank0[c0];
+      t->next[s][c] = (unsigned char)id;
+    }
+  }
+}
+
+static unsigned bin_length(unsigned v) { /* binOp::binLength (src/binUtils.cpp:24) */
+  unsigned len = 1;
+  while (v > 1) {
+    v >>= 1;
+    len++;
+  }
+  return len;
+}
+
+/* TreeNode::operator< of the Hilbert build, step by step */
+static int hil_lt(const dgo_oct *a, const dgo_oct *b, unsigned D, const hil_tables *t) {
+  if (a->x == b->x && a->y == b->y && a->z == b->z) return a->lev < b->lev;
+  if (a->lev > b->lev) {
+    uint64_t len = (uint64_t)1 << (D - b->lev);
+    if (!((a->x < b->x || a->x >= b->x + len) || (a->y < b->y || a->y >= b->y + len) ||
+          (a->z < b->z || a->z >= b->z + len)))
+      return 0;
+  } else if (a->lev < b->lev) {
+    uint64_t len = (uint64_t)1 << (D - a->lev);
+    if (!((b->x < a->x || b->x >= a->x + len) || (b->y < a->y || b->y >= a->y + len) ||
+          (b->z < a->z || b->z >= a->z + len)))
+      return 1;
+  }
+  unsigned dx = a->x ^ b->x, dy = a->y ^ b->y, dz = a->z ^ b->z;
+  unsigned md = dx > dy ? dx : dy;
+  if (dz > md) md = dz;
+  unsigned bl = bin_length(md);
+  unsigned nx = (a->x >> bl) << bl, ny = (a->y >> bl) << bl, nz = (a->z >> bl) << bl;
+  unsigned nca_lev = D - bl;
+  int rot = 0;
+  for (unsigned i = 0; i < nca_lev; i++) {
+    unsigned m = D - i - 1;
+    unsigned c = ((nz >> m) & 1u) << 2 | ((ny >> m) & 1u) << 1 | ((nx >> m) & 1u);
+    rot = t->next[rot][c];
+  }
+  unsigned m = D - nca_lev - 1;
+  unsigned c1 = ((a->z >> m) & 1u) << 2 | ((a->y >> m) & 1u) << 1 | ((a->x >> m) & 1u);
+  unsigned c2 = ((b->z >> m) & 1u) << 2 | ((b->y >> m) & 1u) << 1 | ((b->x >> m) & 1u);
+  return t->rank[rot][c1] < t->rank[rot][c2];
+}
+
+int dgo_hilbert_sort(dgo_oct *a, size_t n, unsigned D) {
+  if (D > 30) return DGO_EINVAL;
+  /* the reference's comparison is undefined outside the domain (its NCA
+   * level underflows, TreeNode.tcc:176) */
+  for (size_t i = 0; i < n; i++)
+    if (a[i].lev > D || (a[i].x >> D) || (a[i].y >> D) || (a[i].z >> D)) return DGO_EINVAL;
+  if (n < 2) return 0;
+  hil_tables t;
+  hil_build(&t);
+  dgo_oct *tmp = (dgo_oct *)malloc(n * sizeof(dgo_oct));
+  if (!tmp) return DGO_ENOMEM;
+  /* bottom-up merge sort (stable) with the comparison above */
+  dgo_oct *src = a, *dst = tmp;
+  for (size_t w = 1; w < n; w *= 2) {
+    for (size_t lo = 0; lo < n; lo += 2 * w) {
+      size_t mid = lo + w < n ? lo + w : n, hi = lo + 2 * w < n ? lo + 2 * w : n;
+      size_t i = lo, j = mid, k = lo;
+      while (i < mid && j < hi) dst[k++] = hil_lt(&src[j], &src[i], D, &t) ? src[j++] : src[i++];
+      while (i < mid) dst[k++] = src[i++];
+      while (j < hi) dst[k++] = src[j++];
+    }
+    dgo_oct *sw = src;
+    src = dst;
+    dst = sw;
+  }
+  if (src != a) memcpy(a, src, n * sizeof(dgo_oct));
+  free(tmp);
+  return 0;
+}
+
+int dgo_hilbert_states(void) {
+  hil_tables t;
+  hil_build(&t);
+  return t.n;
+}
+
+/* ------------------------------------------------------------------------ */
 /* checkers                                                                  */
 /* ------------------------------------------------------------------------ */
 int dgo_is_sorted_unique(const dgo_oct *a, size_t n, unsigned D) {

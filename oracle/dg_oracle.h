@@ -70,6 +70,12 @@ int dgo_coarsen(const dgo_oct *in, size_t n, unsigned maxDepth, dgo_oct **out, s
 int dgo_complete(const dgo_oct *in, size_t n, unsigned maxDepth, int isUnique, int isSorted, dgo_oct **out,
                  size_t *nout);
 
+/* the octants in the order of the reference's Hilbert build
+ * (TreeNode::operator<, include/TreeNode.tcc:130-210), in place; and the
+ * number of curve states the generated tables hold (24) */
+int dgo_hilbert_sort(dgo_oct *a, size_t n, unsigned maxDepth);
+int dgo_hilbert_states(void);
+
 int dgo_is_sorted_unique(const dgo_oct *a, size_t n, unsigned maxDepth);
 int dgo_is_linear(const dgo_oct *a, size_t n, unsigned maxDepth);
 int dgo_is_complete(const dgo_oct *a, size_t n, unsigned maxDepth);

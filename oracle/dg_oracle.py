@@ -59,6 +59,7 @@ def lib():
         L.dgo_p2o_local.argtypes = [P, SZ, U, U, ctypes.POINTER(P), ctypes.POINTER(SZ)]
         L.dgo_balance.argtypes = [P, SZ, U, ctypes.POINTER(P), ctypes.POINTER(SZ)]
         L.dgo_coarsen.argtypes = [P, SZ, U, ctypes.POINTER(P), ctypes.POINTER(SZ)]
+        L.dgo_hilbert_sort.argtypes = [P, SZ, U]
         L.dgo_complete.argtypes = [P, SZ, U, ctypes.c_int, ctypes.c_int, ctypes.POINTER(P), ctypes.POINTER(SZ)]
         for f in ("dgo_is_sorted_unique", "dgo_is_linear", "dgo_is_complete", "dgo_is_balanced"):
             getattr(L, f).argtypes = [P, SZ, U]
@@ -149,6 +150,16 @@ def complete(octs: np.ndarray, max_depth: int = 30, is_unique: bool = False, is_
     _check(lib().dgo_complete(_ptr(octs), octs.shape[0], max_depth, int(is_unique), int(is_sorted), ctypes.byref(p),
                               ctypes.byref(n)), "complete")
     return _take_octs(p, n.value)
+
+
+def hilbert_sort(octs: np.ndarray, max_depth: int = 30) -> np.ndarray:
+    a = np.array(octs, dtype=np.uint32).reshape(-1, 4)
+    _check(lib().dgo_hilbert_sort(_ptr(a), a.shape[0], max_depth), "hilbert_sort")
+    return a
+
+
+def hilbert_states() -> int:
+    return int(lib().dgo_hilbert_states())
 
 
 def checks(octs: np.ndarray, max_depth: int = 30) -> dict:

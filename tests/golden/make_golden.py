@@ -15,6 +15,9 @@ outputs next to the inputs:
                   descendant in its first child (getNCA's assertion,
                   src/octFunctions.cpp:310)
   io/             the reference's point and octree files
+  ref_hilbert.npz the reference's default Hilbert-ordered build
+                  (oracle/_ref_hilbert/ref_driver, make ORDER=hilbert):
+                  points2Octree, balanceOctree and completeOctree outputs
 
 Usage:  python tests/golden/make_golden.py [/path/to/reference]
 """
@@ -39,6 +42,7 @@ from tests.golden import cases  # noqa: E402
 
 REF = next((a for a in sys.argv[1:] if not a.startswith("--")), "/root/reference")
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+DRIVER_HILBERT = os.path.join(ROOT, "oracle", "_ref_hilbert", "ref_driver")
 
 
 SCRATCH = tempfile.mkdtemp(prefix="dendro_golden_")
@@ -130,7 +134,59 @@ def make_complete():
     np.savez_compressed(os.path.join(HERE, "ref_complete.npz"), **out)
 
 
+def run_hilbert(*args, timeout=20):
+    """The Hilbert build; None when it aborts or does not finish in time
+    (its construction walk runs for minutes or forever on some clustered
+    inputs that the Morton build finishes in milliseconds)."""
+    args = [os.path.abspath(a) if isinstance(a, str) and os.sep in a else a for a in args]
+    try:
+        r = subprocess.run([DRIVER_HILBERT, *map(str, args)], capture_output=True, text=True, cwd=SCRATCH,
+                           timeout=timeout)
+    except subprocess.TimeoutExpired:
+        return None
+    return None if r.returncode else json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def make_hilbert():
+    """The Hilbert build on the small point cases (points2Octree then
+    balanceOctree) and on the completeOctree inputs given in any order:
+    ref_hilbert.npz."""
+    if not os.path.exists(DRIVER_HILBERT):
+        subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), f"REF={REF}", "ORDER=hilbert"])
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        pf, of, bf = (os.path.join(tmp, f"h.{e}") for e in ("pts", "oct", "bal"))
+        for name, (fn, depth, maxpts) in cases.SMALL.items():
+            write_pts(pf, fn())
+            ok = run_hilbert("p2o", pf, depth, maxpts, of) is not None
+            ok = ok and run_hilbert("bal", of, depth, 1, 0, bf) is not None
+            out[f"p2o_{name}/finished"] = np.bool_(ok)
+            for what, f in (("lin", of), ("bal", bf)):
+                o = read_oct(f) if ok else np.zeros((0, 4), np.uint32)
+                # large outputs as count + FNV-1a of the records in order
+                out[f"p2o_{name}/{what}_n"] = np.int64(len(o))
+                out[f"p2o_{name}/{what}_fnv"] = np.uint64(fnv1a(o))
+                out[f"p2o_{name}/{what}"] = o if len(o) <= 4000 else np.zeros((0, 4), np.uint32)
+            out[f"p2o_{name}/params"] = np.array([depth, maxpts], np.int64)
+        fi, fo = os.path.join(tmp, "in.oct"), os.path.join(tmp, "out.oct")
+        for name, octs, D, uniq, srt in cases.complete_inputs():
+            if not name.endswith("_any") and name.startswith("sparse"):
+                continue
+            write_oct(fi, octs)
+            ok = run_hilbert("complete", fi, D, 0, 0, fo) is not None
+            out[f"complete_{name}/finished"] = np.bool_(ok)
+            o = read_oct(fo) if ok else np.zeros((0, 4), np.uint32)
+            out[f"complete_{name}/out_n"] = np.int64(len(o))
+            out[f"complete_{name}/out_fnv"] = np.uint64(fnv1a(o))
+            out[f"complete_{name}/out"] = o if len(o) <= 4000 else np.zeros((0, 4), np.uint32)
+            out[f"complete_{name}/params"] = np.array([D], np.int64)
+    np.savez_compressed(os.path.join(HERE, "ref_hilbert.npz"), **out)
+
+
 def main():
+    if "--hilbert-only" in sys.argv:
+        make_hilbert()
+        return
     if "--complete-only" in sys.argv:
         if not os.path.exists(DRIVER):
             subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), f"REF={REF}"])
@@ -236,6 +292,7 @@ def main():
     print("golden fixtures written to", HERE)
     make_io()
     make_complete()
+    make_hilbert()
 
 
 if __name__ == "__main__":
