@@ -4,12 +4,12 @@ Morton sort -> ot::points2Octree -> ot::balanceOctree(incCorner) -> ot::DA
 -> Laplacian + mass element matVec, as hand-written CUDA kernels behind the
 C ABI of include/dendro_gb300.h.
 """
-from .api import (DA, Context, DendroError, MultiGrid, Octree, balanceOctree, coarsenOctree, completeOctree,
+from .api import (DA, Context, Csr, DendroError, MultiGrid, Octree, balanceOctree, coarsenOctree, completeOctree,
                   default_context, points2Octree, points2OctreeBatch, readNodesFromFile, readNodesFromFile_binary,
                   readPtsFromFile, sortUniquePoints, writeNodesToFile, writeNodesToFile_binary, writePtsToFile)
 
 __all__ = [
-    "DA", "Context", "DendroError", "MultiGrid", "Octree", "balanceOctree", "coarsenOctree", "completeOctree",
+    "DA", "Context", "Csr", "DendroError", "MultiGrid", "Octree", "balanceOctree", "coarsenOctree", "completeOctree",
     "default_context", "points2Octree", "points2OctreeBatch",
     "sortUniquePoints", "readPtsFromFile", "writePtsToFile", "readNodesFromFile", "writeNodesToFile",
     "readNodesFromFile_binary", "writeNodesToFile_binary",

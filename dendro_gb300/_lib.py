@@ -91,6 +91,12 @@ def _declare(L):
         "dg_da_download": ([P, P, P, P, P, I], I),
         "dg_da_free": ([P, P], I),
         "dg_matvec": ([P, P, P, P, I, D, D, I], I),
+        "dg_da_assemble": ([P, P, D, D, PP], I),
+        "dg_mg_assemble": ([P, P, SZ, PP], I),
+        "dg_csr_sizes": ([P, ctypes.POINTER(SZ), ctypes.POINTER(SZ), ctypes.POINTER(U)], I),
+        "dg_csr_download": ([P, P, P, P, P, I], I),
+        "dg_csr_spmv": ([P, P, P, P, I], I),
+        "dg_csr_free": ([P, P], I),
         "dg_mg_setup": ([P, P, SZ, PP], I),
         "dg_mg_levels": ([P, ctypes.POINTER(SZ)], I),
         "dg_mg_level_sizes": ([P, SZ, ctypes.POINTER(SZ), ctypes.POINTER(SZ)], I),

@@ -373,6 +373,56 @@ def completeOctree(octants, maxDepth: int = 30, isUnique: bool = False, isSorted
     return Octree(ctx, h)
 
 
+class Csr:
+    """An assembled operator on the device (dg_csr): CSR over the DA's node
+    ids, columns sorted within each row, FP64 values."""
+
+    def __init__(self, ctx: Context, handle: ctypes.c_void_p):
+        self.ctx, self.handle = ctx, handle
+        n, z, mr = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_uint()
+        check(ctx.handle, ctx._L.dg_csr_sizes(handle, ctypes.byref(n), ctypes.byref(z), ctypes.byref(mr)),
+              "dg_csr_sizes")
+        self.n_rows, self.nnz, self.max_row_len = n.value, z.value, mr.value
+
+    def to_numpy(self):
+        """(row_ptr int64[n_rows + 1], col uint32[nnz], val float64[nnz])"""
+        rp = np.empty(self.n_rows + 1, np.int64)
+        col = np.empty(max(self.nnz, 1), np.uint32)
+        val = np.empty(max(self.nnz, 1), np.float64)
+        check(self.ctx.handle, self.ctx._L.dg_csr_download(self.ctx.handle, self.handle, _ptr(rp), _ptr(col), _ptr(val), 0),
+              "dg_csr_download")
+        return rp, col[: self.nnz], val[: self.nnz]
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+
+        rp, col, val = self.to_numpy()
+        return sp.csr_matrix((val, col.astype(np.int64), rp), shape=(self.n_rows, self.n_rows))
+
+    def spmv(self, x, out=None):
+        """y = A x (FP64); host arrays or CUDA tensors."""
+        on_dev = _is_device(x)
+        if on_dev:
+            out = x.new_empty(x.shape) if out is None else out
+        else:
+            x = np.ascontiguousarray(x, dtype=np.float64)
+            out = np.empty_like(x) if out is None else out
+        check(self.ctx.handle, self.ctx._L.dg_csr_spmv(self.ctx.handle, self.handle, _ptr(x), _ptr(out), 1 if on_dev else 0),
+              "dg_csr_spmv")
+        return out
+
+    def free(self):
+        if self.handle:
+            self.ctx._L.dg_csr_free(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
 class DA:
     """ot::DA (src/oda/oda.cpp:250) at one rank, device resident."""
 
@@ -389,6 +439,14 @@ class DA:
 
     def getElementSize(self) -> int:
         return self.n_elem
+
+    def assemble(self, lapFac: float = 1.0, massFac: float = 1.0) -> Csr:
+        """CreateAndComputeFullJacobian1 (examples/src/backend/odaJac.C:470):
+        lapFac K + massFac M as a CSR matrix."""
+        h = ctypes.c_void_p()
+        check(self.ctx.handle, self.ctx._L.dg_da_assemble(self.ctx.handle, self.handle, lapFac, massFac,
+                                                          ctypes.byref(h)), "dg_da_assemble")
+        return Csr(self.ctx, h)
 
     def getNodeSize(self) -> int:
         return self.n_node
@@ -463,6 +521,14 @@ class MultiGrid:
             e, v = ctypes.c_size_t(), ctypes.c_size_t()
             ctx._L.dg_mg_level_sizes(h, l, ctypes.byref(e), ctypes.byref(v))
             self.sizes.append((e.value, v.value))
+
+    def assemble(self, level: int) -> Csr:
+        """ComputeDirichletJacobian (examples/src/backend/omgJac.C:383): the
+        Dirichlet operator of a level as a CSR matrix."""
+        h = ctypes.c_void_p()
+        check(self.ctx.handle, self.ctx._L.dg_mg_assemble(self.ctx.handle, self.handle, level, ctypes.byref(h)),
+              "dg_mg_assemble")
+        return Csr(self.ctx, h)
 
     def level_nodes(self, level: int, device: bool = False):
         """Node coordinates (n_node, 3) of a level: numpy uint32, or with

@@ -4,10 +4,12 @@
 #include <cstdio>
 #include <exception>
 #include <iterator>
+#include <functional>
 #include <new>
 #include <string>
 
 #include "dendro_gb300.h"
+#include "dg_assemble.cuh"
 #include "dg_io.cuh"
 #include "dg_mg.cuh"
 
@@ -24,6 +26,9 @@ struct dg_da_s {
 };
 struct dg_mg_s {
   dg::MG mg;
+};
+struct dg_csr_s {
+  dg::Csr c;
 };
 
 namespace {
@@ -91,6 +96,19 @@ void copy_out(dg::Context &c, T *dst, const T *src, size_t n, int dst_on_device)
                           c.stream));
 }
 
+int csr_handle(dg_ctx ctx, dg_csr *out, const std::function<void(dg::Csr &)> &make) {
+  if (!out) return DG_ERR_INVALID_ARG;
+  *out = nullptr;
+  dg_csr h = new (std::nothrow) dg_csr_s();
+  if (!h) return DG_ERR_OUT_OF_MEMORY;
+  int rc = guarded(ctx, [&]() { make(h->c); });
+  if (rc != DG_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return DG_OK;
+}
 }  // namespace
 
 extern "C" {
@@ -684,6 +702,67 @@ int dg_mg_free(dg_ctx ctx, dg_mg mg) {
   cudaSetDevice(ctx->c.device);
   dg::mg_free(ctx->c, mg->mg);
   delete mg;
+  return DG_OK;
+}
+
+
+int dg_da_assemble(dg_ctx ctx, dg_da da, double lapFac, double massFac, dg_csr *out) {
+  if (!da) return DG_ERR_INVALID_ARG;
+  return csr_handle(ctx, out, [&](dg::Csr &c) { dg::assemble_csr(ctx->c, da->m, nullptr, lapFac, massFac, c); });
+}
+
+int dg_mg_assemble(dg_ctx ctx, dg_mg mg, size_t level, dg_csr *out) {
+  if (!mg || level >= mg->mg.lv.size()) return DG_ERR_INVALID_ARG;
+  const dg::MGLevel &L = mg->mg.lv[level];
+  return csr_handle(ctx, out, [&](dg::Csr &c) { dg::assemble_csr(ctx->c, L.mesh, L.bdy, 1.0, 1.0, c); });
+}
+
+int dg_csr_sizes(dg_csr a, size_t *n_rows, size_t *nnz, unsigned *max_row_len) {
+  if (!a) return DG_ERR_INVALID_ARG;
+  if (n_rows) *n_rows = a->c.n_rows;
+  if (nnz) *nnz = a->c.nnz;
+  if (max_row_len) *max_row_len = a->c.max_row;
+  return DG_OK;
+}
+
+int dg_csr_download(dg_ctx ctx, dg_csr a, int64_t *row_ptr, uint32_t *col, double *val, int dst_on_device) {
+  if (!a) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() {
+    const dg::Csr &c = a->c;
+    if (row_ptr) copy_out(ctx->c, row_ptr, c.row_ptr, c.n_rows + 1, dst_on_device);
+    if (col && c.nnz) copy_out(ctx->c, col, c.col, c.nnz, dst_on_device);
+    if (val && c.nnz) copy_out(ctx->c, val, c.val, c.nnz, dst_on_device);
+    DG_CUDA(cudaStreamSynchronize(ctx->c.stream));
+  });
+}
+
+int dg_csr_spmv(dg_ctx ctx, dg_csr a, const double *x, double *y, int on_device) {
+  if (!a || (!x && a->c.n_rows) || (!y && a->c.n_rows)) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() {
+    dg::Context &c = ctx->c;
+    const size_t V = a->c.n_rows;
+    dg::DBuf<double> hin, hout;
+    const double *dx = device_input(c, x, V, on_device, hin);
+    double *dy = y;
+    if (!on_device) {
+      hout.alloc(V ? V : 1, c.stream);
+      dy = hout.get();
+    }
+    dg::csr_spmv(c, a->c, dx, dy);
+    if (!on_device) copy_out(c, y, dy, V, 0);
+    DG_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int dg_csr_free(dg_ctx ctx, dg_csr a) {
+  if (!a) return DG_OK;
+  if (ctx) dg::csr_free(ctx->c, a->c);
+  else {
+    cudaFree(a->c.row_ptr);
+    cudaFree(a->c.col);
+    cudaFree(a->c.val);
+  }
+  delete a;
   return DG_OK;
 }
 

@@ -51,6 +51,7 @@ typedef struct dg_ctx_s *dg_ctx;
 typedef struct dg_octree_s *dg_octree;
 typedef struct dg_da_s *dg_da;
 typedef struct dg_mg_s *dg_mg;
+typedef struct dg_csr_s *dg_csr;
 
 /* ---- context ------------------------------------------------------------
  * Replaces the per-rank global state the reference sets up in
@@ -264,6 +265,28 @@ int dg_mg_rhs(dg_ctx ctx, dg_mg mg, const double *f, double *b, int on_device);
 int dg_mg_solve(dg_ctx ctx, dg_mg mg, const double *b, double *x, int precision, double rtol, int maxit, int on_device,
                 int *iterations, double *relres);
 int dg_mg_free(dg_ctx ctx, dg_mg mg);
+
+/* ---- assembled sparse matrices -------------------------------------------
+ * The element operators as CSR matrices on the device, rows and columns in
+ * this library's node numbering (DA node ids, dg_da_download /
+ * dg_mg_level_nodes give each node's coordinates), columns sorted within a
+ * row.  The reference assembles them into a PETSc Mat through
+ * DA::computeLocalToGlobalMappings (src/oda/oda.cpp:77) and
+ * DA::setValuesInMatrix (oda.cpp:139).
+ * dg_da_assemble: lapFac K + massFac M, the matrix of dg_matvec:
+ *   CreateAndComputeFullJacobian1 (examples/src/backend/odaJac.C:470), the
+ *   -buildFullMatAll / -buildFullCoarseMat matrices (omgJac.C:1333).
+ * dg_mg_assemble: the Dirichlet operator of a multigrid level (the matrix of
+ *   dg_mg_matvec): ComputeDirichletJacobian (omgJac.C:383); boundary rows
+ *   are the identity, boundary columns are dropped.
+ * dg_csr_download: row_ptr (n_rows + 1), col (nnz), val (nnz), host or
+ * device arrays.  dg_csr_spmv: y = A x (FP64). */
+int dg_da_assemble(dg_ctx ctx, dg_da da, double lapFac, double massFac, dg_csr *out);
+int dg_mg_assemble(dg_ctx ctx, dg_mg mg, size_t level, dg_csr *out);
+int dg_csr_sizes(dg_csr a, size_t *n_rows, size_t *nnz, unsigned *max_row_len);
+int dg_csr_download(dg_ctx ctx, dg_csr a, int64_t *row_ptr, uint32_t *col, double *val, int dst_on_device);
+int dg_csr_spmv(dg_ctx ctx, dg_csr a, const double *x, double *y, int on_device);
+int dg_csr_free(dg_ctx ctx, dg_csr a);
 
 /* ---- timing ---------------------------------------------------------------
  * Milliseconds of device time spent by the last completed call on ctx

@@ -257,3 +257,37 @@ class DA:
             lib().dgo_da_free(ctypes.byref(self._da))
         except Exception:
             pass
+
+
+def assemble(da: "DA", lap_fac: float = 1.0, mass_fac: float = 1.0, dirichlet: bool = False):
+    """The assembled operator of the oracle DA as a scipy CSR matrix
+    (duplicates summed): lap_fac K + mass_fac M, the records of
+    CreateAndComputeFullJacobian1 (examples/src/backend/odaJac.C:470-535), or
+    with ``dirichlet`` the Dirichlet K + M of ComputeDirichletJacobian
+    (examples/src/backend/omgJac.C:383-490: interior rows and columns, the
+    identity on boundary rows)."""
+    import scipy.sparse as sp
+
+    lap, mass = stencils()
+    if dirichlet:
+        lap_fac = mass_fac = 1.0
+    h = 1.0 / np.exp2(da.level.astype(np.float64))
+    f1 = lap_fac * h / 2.0
+    f2 = mass_fac * h * h * h / 8.0
+    a = f1[:, None, None] * lap[da.child, da.etype] + f2[:, None, None] * mass[da.child, da.etype]
+    rows = np.broadcast_to(da.nodes[:, :, None], a.shape).ravel().astype(np.int64)
+    cols = np.broadcast_to(da.nodes[:, None, :], a.shape).ravel().astype(np.int64)
+    vals = a.ravel()
+    n = da.n_node
+    if dirichlet:
+        b = da.bdy()
+        keep = ~b[rows] & ~b[cols]
+        ids = np.nonzero(b)[0]
+        rows = np.concatenate([rows[keep], ids])
+        cols = np.concatenate([cols[keep], ids])
+        vals = np.concatenate([vals[keep], np.ones(len(ids))])
+    m = sp.coo_matrix((vals, (rows, cols)), shape=(n, n)).tocsr()
+    m.sum_duplicates()
+    m.sort_indices()
+    return m
+

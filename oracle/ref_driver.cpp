@@ -25,15 +25,22 @@
  *         (examples/src/backend/odaJac.C:275-292, hFac as odaJac.C:311-313).
  *         Writes OUT_PREFIX.elem (per element: x y z level child hmask etype
  *         and the 8 node indices as node coordinates) and, when VEC_IN is
- *         given, OUT_PREFIX.mv (node coordinates + output value).
+ *         given, OUT_PREFIX.mv (node coordinates + output value).  A 7th
+ *         argument "mat" also writes OUT_PREFIX.mat: the assembled
+ *         K + M of CreateAndComputeFullJacobian1
+ *         (examples/src/backend/odaJac.C:470-535, lapFac = massFac = 1) with
+ *         every element's records added in element order, as
+ *         (row x y z, column x y z, value) by node coordinates.
  *
  * Formats
  *   .pts : u64 n, then n*3 f64 (x,y,z interleaved)
  *   .oct : u64 n, then n*(u32 x, u32 y, u32 z, u32 level)
+ *   mat  : u64 n, then n*(u32 rx, ry, rz, cx, cy, cz, f64 value)
  *   vec  : u64 n, then n*(u32 x, u32 y, u32 z, u32 pad, f64 value), node
  *          coordinates at the octree's maxDepth scale (vertices in [0,2^D]).
  */
 #include <chrono>
+#include <map>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -351,6 +358,39 @@ static int mode_da(int argc, char **argv) {
     }
     std::fclose(g);
     if (missing) std::fprintf(stderr, "warning: %ld node values missing from input vector\n", missing);
+  }
+  if (argc > 7 && std::strcmp(argv[7], "mat") == 0) {
+    /* the records of CreateAndComputeFullJacobian1, summed per (row, col) in
+     * the order the loop visits them (ADD_VALUES) */
+    std::map<std::pair<unsigned, unsigned>, double> mat;
+    double hFac = 1.0 / ((double)(1u << (maxD - 1)));
+    for (da.init<ot::DA_FLAGS::ALL>(); da.curr() < da.end<ot::DA_FLAGS::ALL>(); da.next<ot::DA_FLAGS::ALL>()) {
+      unsigned lev = da.getLevel(da.curr());
+      double h = hFac * (1u << (maxD - lev));
+      double fac1 = 1.0 * h / 2.0, fac2 = 1.0 * h * h * h / 8.0;
+      unsigned idx[8];
+      da.getNodeIndices(idx);
+      unsigned char cn = da.getChildNumber();
+      unsigned char hm = da.getHangingNodeIndex(da.curr());
+      unsigned char et = 0;
+      GET_ETYPE_BLOCK(et, hm, cn)
+      for (int k = 0; k < 8; k++)
+        for (int j = 0; j < 8; j++)
+          mat[std::make_pair(idx[k], idx[j])] +=
+              (fac1 * LaplacianType2Stencil[cn][et][k][j]) + (fac2 * MassType2Stencil[cn][et][k][j]);
+    }
+    std::string p = prefix + ".mat";
+    FILE *g = xopen(p.c_str(), "wb");
+    uint64_t n = mat.size();
+    std::fwrite(&n, 8, 1, g);
+    for (const auto &kv : mat) {
+      unsigned r = kv.first.first, c = kv.first.second;
+      uint32_t rc[6] = {idxPos[3 * r], idxPos[3 * r + 1], idxPos[3 * r + 2],
+                        idxPos[3 * c], idxPos[3 * c + 1], idxPos[3 * c + 2]};
+      std::fwrite(rc, 4, 6, g);
+      std::fwrite(&kv.second, 8, 1, g);
+    }
+    std::fclose(g);
   }
   std::printf(
       "{\"op\":\"da\",\"n_bal\":%zu,\"n_elem\":%zu,\"n_nodes_da\":%u,\"n_nodes_used\":%zu,\"conflicts\":%ld,"

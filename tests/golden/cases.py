@@ -51,6 +51,10 @@ def da_points():
     return datagen.gaussian(1000, 0.5, 0.1, seed=33)
 
 
+def mat_points():
+    return datagen.gaussian(150, 0.5, 0.12, seed=34)
+
+
 def nodal_function(xyz_u32: np.ndarray) -> np.ndarray:
     """Smooth nodal field used for the matVec fixture (coordinates at maxDepth 30)."""
     c = np.asarray(xyz_u32, np.float64) / float(1 << 30)

@@ -15,6 +15,8 @@ outputs next to the inputs:
                   descendant in its first child (getNCA's assertion,
                   src/octFunctions.cpp:310)
   io/             the reference's point and octree files
+  ref_mat.npz     the assembled K + M of CreateAndComputeFullJacobian1 on
+                  a small balanced octree (row, column node coordinates)
   ref_hilbert.npz the reference's default Hilbert-ordered build
                   (oracle/_ref_hilbert/ref_driver, make ORDER=hilbert):
                   points2Octree, balanceOctree and completeOctree outputs
@@ -183,7 +185,34 @@ def make_hilbert():
     np.savez_compressed(os.path.join(HERE, "ref_hilbert.npz"), **out)
 
 
+def make_mat():
+    """The reference's assembled K + M (CreateAndComputeFullJacobian1,
+    odaJac.C:470) on the balanced octree of cases.mat_points():
+    ref_mat.npz with the entries as indices into the sorted node
+    coordinates."""
+    with tempfile.TemporaryDirectory() as tmp:
+        _, bal = ref_p2o_bal(tmp, "mat", cases.mat_points(), 30, 1)
+        bf = os.path.join(tmp, "mat.bal")
+        write_oct(bf, bal)
+        prefix = os.path.join(tmp, "mat")
+        run("da", bf, 30, os.path.join(REF, "Stencils"), "-", prefix, "mat")
+        b = open(prefix + ".mat", "rb").read()
+        n = int(np.frombuffer(b[:8], np.uint64)[0])
+        rec = np.frombuffer(b[8:], dtype=[("rc", "<u4", (6,)), ("v", "<f8")], count=n)
+    rc = rec["rc"]
+    node_xyz = np.unique(rc.reshape(-1, 3), axis=0)
+    def index(xyz):
+        pos = np.searchsorted(node_xyz.view([("", node_xyz.dtype)] * 3).ravel(),
+                              np.ascontiguousarray(xyz).view([("", xyz.dtype)] * 3).ravel())
+        return pos.astype(np.uint32)
+    np.savez_compressed(os.path.join(HERE, "ref_mat.npz"), bal=bal, node_xyz=node_xyz,
+                        row=index(rc[:, :3]), col=index(rc[:, 3:]), val=rec["v"].copy())
+
+
 def main():
+    if "--mat-only" in sys.argv:
+        make_mat()
+        return
     if "--hilbert-only" in sys.argv:
         make_hilbert()
         return
@@ -293,6 +322,7 @@ def main():
     make_io()
     make_complete()
     make_hilbert()
+    make_mat()
 
 
 if __name__ == "__main__":

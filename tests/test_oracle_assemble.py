@@ -1,0 +1,44 @@
+"""Assembled operators: the oracle's assembly (numpy) against the matrix the
+reference itself assembles (CreateAndComputeFullJacobian1,
+examples/src/backend/odaJac.C:470, through its DA and stencil files:
+tests/golden/ref_mat.npz, written by tests/golden/make_golden.py).  The
+pattern must be identical; the values agree to the precision of the
+reference's stencil files (15 decimals).  CPU only."""
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _by_coords(m, node_xyz, ref_xyz):
+    """rows / cols of a scipy matrix over node_xyz, re-indexed into ref_xyz"""
+    key = lambda a: np.ascontiguousarray(a, np.uint32).view([("", np.uint32)] * 3).ravel()
+    order = np.argsort(key(ref_xyz))
+    pos = np.searchsorted(key(ref_xyz)[order], key(node_xyz))
+    idx = order[pos]
+    assert np.array_equal(ref_xyz[idx], node_xyz)
+    c = m.tocoo()
+    return idx[c.row], idx[c.col], c.data
+
+
+def test_oracle_matches_reference_matrix(oracle):
+    z = np.load(os.path.join(GOLDEN, "ref_mat.npz"))
+    da = oracle.DA(z["bal"], 30)
+    m = oracle.assemble(da)
+    assert m.nnz == len(z["val"])
+    r, c, v = _by_coords(m, da.node_xyz, z["node_xyz"])
+    got = {(int(a), int(b)): x for a, b, x in zip(r, c, v)}
+    ref = {(int(a), int(b)): x for a, b, x in zip(z["row"], z["col"], z["val"])}
+    assert got.keys() == ref.keys()
+    scale = np.abs(z["val"]).max()
+    err = max(abs(got[k] - ref[k]) for k in ref) / scale
+    assert err < 1e-12, err
+
+
+def test_oracle_matrix_is_the_matvec(oracle):
+    z = np.load(os.path.join(GOLDEN, "ref_mat.npz"))
+    da = oracle.DA(z["bal"], 30)
+    x = np.random.Generator(np.random.PCG64(3)).uniform(-1, 1, da.n_node)
+    np.testing.assert_allclose(oracle.assemble(da, 0.7, 1.3) @ x, da.matvec(x, 0.7, 1.3), rtol=0, atol=1e-12)
+    np.testing.assert_allclose(oracle.assemble(da, dirichlet=True) @ x, da.dirichlet_matvec(x), rtol=0, atol=1e-12)
