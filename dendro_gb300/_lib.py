@@ -92,6 +92,8 @@ def _declare(L):
         "dg_da_free": ([P, P], I),
         "dg_matvec": ([P, P, P, P, I, D, D, I], I),
         "dg_da_assemble": ([P, P, D, D, PP], I),
+        "dg_da_build_ex": ([P, P, I, PP], I),
+        "dg_da_memory": ([P, ctypes.POINTER(SZ)], I),
         "dg_mg_assemble": ([P, P, SZ, PP], I),
         "dg_csr_sizes": ([P, ctypes.POINTER(SZ), ctypes.POINTER(SZ), ctypes.POINTER(U)], I),
         "dg_csr_download": ([P, P, P, P, P, I], I),

@@ -426,12 +426,13 @@ class Csr:
 class DA:
     """ot::DA (src/oda/oda.cpp:250) at one rank, device resident."""
 
-    def __init__(self, octree: Octree):
+    def __init__(self, octree: Octree, compressLut: bool = False):
         ctx = octree.ctx
         self.ctx = ctx
         self.max_depth = octree.max_depth
+        self.compressLut = compressLut
         h = ctypes.c_void_p()
-        check(ctx.handle, ctx._L.dg_da_build(ctx.handle, octree.handle, ctypes.byref(h)), "DA")
+        check(ctx.handle, ctx._L.dg_da_build_ex(ctx.handle, octree.handle, int(compressLut), ctypes.byref(h)), "DA")
         self.handle = h
         ne, nn = ctypes.c_size_t(), ctypes.c_size_t()
         ctx._L.dg_da_sizes(h, ctypes.byref(ne), ctypes.byref(nn))
@@ -450,6 +451,12 @@ class DA:
 
     def getNodeSize(self) -> int:
         return self.n_node
+
+    def memory_bytes(self) -> int:
+        """Device bytes the DA holds."""
+        b = ctypes.c_size_t()
+        check(self.ctx.handle, self.ctx._L.dg_da_memory(self.handle, ctypes.byref(b)), "dg_da_memory")
+        return b.value
 
     def download(self) -> dict:
         meta = np.empty(max(self.n_elem, 1), np.uint32)

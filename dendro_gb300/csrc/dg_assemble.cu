@@ -170,10 +170,12 @@ void assemble_csr(Context &ctx, const Mesh &m, const uint8_t *bdy, double lap_fa
     return;
   }
   const size_t np = 8 * E;
+  DBuf<uint32_t> conn_tmp;
+  const uint32_t *conn = mesh_conn(ctx, m, conn_tmp);
   DBuf<uint64_t> ka(np, s), kb(np, s);
   {
     ProfScope _prof(ctx, "csr_incidence", (double)np * 12);
-    k_incidence<<<grid_for(np, 256), 256, 0, s>>>(m.conn, E, ka.get());
+    k_incidence<<<grid_for(np, 256), 256, 0, s>>>(conn, E, ka.get());
     DG_LAUNCH_CHECK();
   }
   uint64_t *key = radix_sort<uint64_t>(ctx, ka.get(), kb.get(), np, 32 + (int)bits_of(V));
@@ -185,7 +187,7 @@ void assemble_csr(Context &ctx, const Mesh &m, const uint8_t *bdy, double lap_fa
     ProfScope _prof(ctx, "csr_count", (double)np * 8 * 8);
     k_row_bounds<<<grid_for(V + 1, 256), 256, 0, s>>>(key, np, V, start.get());
     DG_LAUNCH_CHECK();
-    k_row_count<<<grid_for(V, 128), 128, 0, s>>>(key, start.get(), V, m.conn, E, bdy, len.get(), dmax.get(),
+    k_row_count<<<grid_for(V, 128), 128, 0, s>>>(key, start.get(), V, conn, E, bdy, len.get(), dmax.get(),
                                                   ctx.d_flags);
     DG_LAUNCH_CHECK();
   }
@@ -206,7 +208,7 @@ void assemble_csr(Context &ctx, const Mesh &m, const uint8_t *bdy, double lap_fa
   DBuf<double> val(nnz ? nnz : 1, s);
   {
     ProfScope _prof(ctx, "csr_fill", (double)np * 8 * 8 + (double)nnz * 12);
-    k_row_fill<<<grid_for(V, 128), 128, 0, s>>>(key, start.get(), V, m.meta, m.conn, E, bdy, ctx.d_sten64, lap_fac,
+    k_row_fill<<<grid_for(V, 128), 128, 0, s>>>(key, start.get(), V, m.meta, conn, E, bdy, ctx.d_sten64, lap_fac,
                                                  mass_fac, rp.get(), col.get(), val.get());
     DG_LAUNCH_CHECK();
   }

@@ -479,20 +479,28 @@ int dg_octree_free(dg_ctx ctx, dg_octree o) {
   return DG_OK;
 }
 
-int dg_da_build(dg_ctx ctx, dg_octree balanced, dg_da *out) {
+int dg_da_build(dg_ctx ctx, dg_octree balanced, dg_da *out) { return dg_da_build_ex(ctx, balanced, 0, out); }
+
+int dg_da_build_ex(dg_ctx ctx, dg_octree balanced, int compressLut, dg_da *out) {
   if (!balanced || !out) return DG_ERR_INVALID_ARG;
   *out = nullptr;
   dg_da h = new (std::nothrow) dg_da_s();
   if (!h) return DG_ERR_OUT_OF_MEMORY;
   int rc = guarded(ctx, [&]() {
     if (balanced->o.nseg != 1) dg::fail(DG_ERR_UNSUPPORTED, "DA: one cloud per mesh");
-    dg::mesh_build(ctx->c, balanced->o, h->m);
+    dg::mesh_build(ctx->c, balanced->o, h->m, compressLut != 0);
   });
   if (rc != DG_OK) {
     delete h;
     return rc;
   }
   *out = h;
+  return DG_OK;
+}
+
+int dg_da_memory(dg_da da, size_t *bytes) {
+  if (!da || !bytes) return DG_ERR_INVALID_ARG;
+  *bytes = dg::mesh_bytes(da->m);
   return DG_OK;
 }
 
@@ -526,10 +534,11 @@ int dg_da_download(dg_ctx ctx, dg_da da, uint32_t *meta, uint32_t *nodes, uint32
     const size_t E = da->m.n_elem, V = da->m.n_node;
     if (meta) copy_out(c, meta, da->m.meta, E, dst_on_device);
     if (nodes && E) {
-      dg::DBuf<uint32_t> t(8 * E, c.stream);
+      dg::DBuf<uint32_t> t(8 * E, c.stream), dec;
+      const uint32_t *conn = dg::mesh_conn(c, da->m, dec);
       {
         dg::ProfScope _prof("da_transpose", (double)E * 64);
-        k_transpose_conn<<<dg::grid_for(E, 256), 256, 0, c.stream>>>(da->m.conn, E, t.get());
+        k_transpose_conn<<<dg::grid_for(E, 256), 256, 0, c.stream>>>(conn, E, t.get());
         DG_LAUNCH_CHECK();
       }
       copy_out(c, nodes, t.get(), 8 * E, dst_on_device);

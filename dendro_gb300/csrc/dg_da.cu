@@ -472,7 +472,7 @@ __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict
                                                       uint16_t *__restrict__ pinc, uint16_t *__restrict__ pexc,
                                                       uint32_t *__restrict__ pmeta, uint16_t *__restrict__ pkeys,
                                                       uint16_t *__restrict__ pkcount, uint32_t *__restrict__ run_node,
-                                                      uint32_t *__restrict__ n_run) {
+                                                      uint32_t *__restrict__ n_run, uint16_t *__restrict__ pperm) {
   extern __shared__ __align__(16) unsigned char ps_raw[];
   PatchSortSmem &S = *reinterpret_cast<PatchSortSmem *>(ps_raw);
   const int tid = threadIdx.x;
@@ -506,6 +506,7 @@ __global__ void __launch_bounds__(PATCH) k_patch_sort(const uint32_t *__restrict
   if (tid < ne) {
     const uint32_t eo = S.ek[tid] & (PATCH - 1);
     S.rank[eo] = (uint16_t)tid;
+    if (pperm) pperm[p * PATCH + tid] = (uint16_t)eo;
     const uint32_t mo = meta[e0 + eo];
     pmeta[p * PATCH + tid] = (mo & 0xff00ffffu) | (uint32_t)(kidx < PKEY_MAX ? kidx : 0) << 16;
     if (gstart && kidx < PKEY_MAX) pkeys[p * PKEY_MAX + kidx] = (uint16_t)grp;
@@ -628,6 +629,55 @@ __global__ void k_patch_nodes(const uint32_t *__restrict__ run_node, const uint3
   for (uint32_t i = threadIdx.x; i < nr; i += blockDim.x) pnode[poff[p] + i] = run_node[p * PATCH_ENT + i];
 }
 
+// conn from the patch tables: pair i of patch p belongs to the run counted
+// by the run starts up to i (pexc gives the count before pair 8t), its slot
+// names the vertex and the element's (type, level) position
+__global__ void __launch_bounds__(PATCH) k_conn_from_patches(const uint16_t *__restrict__ pinc,
+                                                             const uint16_t *__restrict__ pexc,
+                                                             const uint32_t *__restrict__ pnode,
+                                                             const uint64_t *__restrict__ poff,
+                                                             const uint16_t *__restrict__ pperm, size_t E,
+                                                             uint32_t *__restrict__ conn) {
+  const size_t p = blockIdx.x;
+  const int t = threadIdx.x;
+  const size_t e0 = p * PATCH;
+  const int ne = (int)((E - e0) < (size_t)PATCH ? (E - e0) : (size_t)PATCH);
+  if (t >= ne) return;  // the pairs of a patch's ne elements are its first 8 ne entries
+  uint32_t r = pexc[p * PATCH + t];
+  const uint64_t ub = poff[p];
+  for (int i = 8 * t; i < 8 * t + 8; i++) {
+    const uint32_t ent = pinc[p * PATCH_ENT + i];
+    if (ent & ENT_START) r++;
+    const uint32_t slot = ent & ENT_SLOT;
+    const uint32_t v = slot / PATCH, pos = slot % PATCH;
+    conn[(size_t)v * E + e0 + pperm[p * PATCH + pos]] = pnode[ub + r - 1];
+  }
+}
+
+const uint32_t *mesh_conn(Context &ctx, const Mesh &m, DBuf<uint32_t> &tmp) {
+  if (!m.compressed) return m.conn;
+  tmp.alloc(8 * m.n_elem, ctx.stream);
+  ProfScope _prof(ctx, "da_conn_decode", (double)m.n_elem * (16 + 2 + 32) + (double)m.n_elem * 6);
+  k_conn_from_patches<<<(unsigned)m.n_patch, PATCH, 0, ctx.stream>>>(m.pinc, m.pexc, m.pnode, m.poff, m.pperm,
+                                                                     m.n_elem, tmp.get());
+  DG_LAUNCH_CHECK();
+  return tmp.get();
+}
+
+size_t mesh_bytes(const Mesh &m) {
+  const size_t E = m.n_elem, V = m.n_node, np = m.n_patch;
+  size_t runs = 0;
+  if (np && m.poff) {
+    uint64_t r = 0;
+    if (cudaMemcpy(&r, m.poff + np, sizeof(uint64_t), cudaMemcpyDeviceToHost) == cudaSuccess) runs = r;
+  }
+  size_t b = E * 4 + V * 12;                                    // meta, node coordinates
+  if (m.conn) b += 8 * E * 4;                                   // conn
+  b += np * (PATCH_ENT * 2 + PATCH * 2 + PATCH * 4 + PKEY_MAX * 2 + 2) + (np + 1) * 8 + runs * 4;  // patches
+  if (m.pperm) b += np * PATCH * 2;
+  return b;
+}
+
 static void mesh_patches(Context &ctx, Mesh &m) {
   cudaStream_t s = ctx.stream;
   const size_t n = m.n_elem, np = (n + PATCH - 1) / PATCH;
@@ -637,6 +687,8 @@ static void mesh_patches(Context &ctx, Mesh &m) {
   DBuf<uint32_t> pmeta(np * PATCH, s);
   DBuf<uint16_t> pkeys(np * PKEY_MAX, s), pkcount(np, s);
   DBuf<uint64_t> poff(np + 1, s);
+  DBuf<uint16_t> pperm;
+  if (m.compressed) pperm.alloc(np * PATCH, s);
   DG_CUDA(cudaMemsetAsync(pairs.get(), 0, m.n_node * sizeof(uint32_t), s));
   {
     ProfScope _prof(ctx, "da_node_pairs", (double)n * 8 * 8);
@@ -652,7 +704,8 @@ static void mesh_patches(Context &ctx, Mesh &m) {
     });
     k_patch_sort<<<(unsigned)np, PATCH, sizeof(PatchSortSmem), s>>>(m.conn, m.meta, n, pairs.get(), pinc.get(),
                                                                     pexc.get(), pmeta.get(), pkeys.get(),
-                                                                    pkcount.get(), run_node.get(), n_run.get());
+                                                                    pkcount.get(), run_node.get(), n_run.get(),
+                                                                    m.compressed ? pperm.get() : nullptr);
     DG_LAUNCH_CHECK();
   }
   exclusive_scan<uint32_t, uint64_t>(n_run.get(), poff.get(), np, poff.get() + np, s);
@@ -673,9 +726,10 @@ static void mesh_patches(Context &ctx, Mesh &m) {
   m.pkcount = pkcount.release_ptr();
   m.pnode = pnode.release_ptr();
   m.poff = poff.release_ptr();
+  if (m.compressed) m.pperm = pperm.release_ptr();
 }
 
-void mesh_build(Context &ctx, const Octree &bal, Mesh &m) {
+void mesh_build(Context &ctx, const Octree &bal, Mesh &m, bool compress) {
   cudaStream_t s = ctx.stream;
   const size_t n = bal.n;
   const unsigned D = bal.max_depth;
@@ -723,7 +777,12 @@ void mesh_build(Context &ctx, const Octree &bal, Mesh &m) {
   m.meta = meta.release_ptr();
   m.conn = conn.release_ptr();
   m.node_xyz = nxyz.release_ptr();
+  m.compressed = compress;
   mesh_patches(ctx, m);
+  if (compress) {  // the element loop needs only the patch tables
+    cudaFreeAsync(m.conn, s);
+    m.conn = nullptr;
+  }
 }
 
 void mesh_free(Context &ctx, Mesh &m) {
@@ -737,6 +796,7 @@ void mesh_free(Context &ctx, Mesh &m) {
   if (m.pkcount) cudaFreeAsync(m.pkcount, ctx.stream);
   if (m.pnode) cudaFreeAsync(m.pnode, ctx.stream);
   if (m.poff) cudaFreeAsync(m.poff, ctx.stream);
+  if (m.pperm) cudaFreeAsync(m.pperm, ctx.stream);
   m = Mesh();
 }
 

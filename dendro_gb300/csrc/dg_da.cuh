@@ -31,9 +31,19 @@ struct Mesh {
   uint16_t *pkcount = nullptr;  // keys per patch (> PKEY_MAX: per-element L, M path)
   uint32_t *pnode = nullptr;  // node of each run, patch after patch
   uint64_t *poff = nullptr;   // n_patch + 1 run offsets into pnode
+  // compressed mode (the reference's compressLut): conn is released once the
+  // patch tables exist and decoded from them on demand (mesh_conn); pperm
+  // maps a patch's (type, level) order back to its element order
+  uint16_t *pperm = nullptr;  // PATCH per patch
+  bool compressed = false;
 };
 
-void mesh_build(Context &ctx, const Octree &bal, Mesh &m);
+void mesh_build(Context &ctx, const Octree &bal, Mesh &m, bool compress = false);
+// the 8 x n_elem vertex-major node ids: m.conn, or decoded from the patch
+// tables into tmp when the mesh is compressed
+const uint32_t *mesh_conn(Context &ctx, const Mesh &m, DBuf<uint32_t> &tmp);
+// device bytes the mesh holds
+size_t mesh_bytes(const Mesh &m);
 void mesh_free(Context &ctx, Mesh &m);
 
 // y = (lapFac * Laplacian + massFac * mass) x over all elements

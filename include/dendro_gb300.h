@@ -211,6 +211,15 @@ int dg_octree_read_binary(dg_ctx ctx, const char *path, dg_octree *out);
  * reference's buffer layout; nodes are identified by coordinates
  * (dg_da_download node_xyz). */
 int dg_da_build(dg_ctx ctx, dg_octree balanced, dg_da *out);
+/* ot::DA with compressLut (include/oda/oda.h:622, decoded by
+ * getNodeIndices, include/oda/oda.tcc:1304-1420): compressLut = 1 keeps only
+ * the element loop's per-patch tables (16-bit slots per element vertex and
+ * one node id per node run) and releases the plain 8 x u32 node list; the
+ * node list is decoded from the tables when a call needs it
+ * (dg_da_download, dg_da_assemble).  Results are identical in both modes.
+ * dg_da_memory: device bytes the DA holds. */
+int dg_da_build_ex(dg_ctx ctx, dg_octree balanced, int compressLut, dg_da *out);
+int dg_da_memory(dg_da da, size_t *bytes);
 int dg_da_sizes(dg_da da, size_t *n_elem, size_t *n_node);
 /* Any output pointer may be NULL.  meta[e] = level | child<<8 | hmask<<16 |
  * etype<<24; nodes is 8*n_elem, element-major (nodes[8e+k]); node_xyz is

@@ -167,13 +167,15 @@ int sortUniquePoints(const std::vector<double> &pts, double *gLens, std::vector<
 // GPU, with the element loop of Jacobian1MatMult (odaJac.C:294).
 class DA {
  public:
+  // compressLut: the reference's DA(in, comm, activeComm, tol, compressLut)
+  // (include/oda/oda.h:622)
   template <class TN>
-  explicit DA(const std::vector<TN> &in, unsigned maxDepth) {
+  explicit DA(const std::vector<TN> &in, unsigned maxDepth, bool compressLut = false) {
     c_ = cxx::context();
     std::vector<uint32_t> r = cxx::nodes_to_records(in);
     dg_octree o = nullptr;
     cxx::check(c_, dg_octree_upload(c_, r.data(), in.size(), maxDepth, 0, &o), "DA (upload)");
-    int st = dg_da_build(c_, o, &da_);
+    int st = dg_da_build_ex(c_, o, compressLut ? 1 : 0, &da_);
     dg_octree_free(c_, o);
     cxx::check(c_, st, "DA");
     cxx::check(c_, dg_da_sizes(da_, &ne_, &nn_), "dg_da_sizes");

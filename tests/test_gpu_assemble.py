@@ -88,3 +88,20 @@ def test_device_spmv(ctx):
     x = torch.rand(da.n_node, dtype=torch.float64, device="cuda:0")
     y = csr.spmv(x)
     np.testing.assert_allclose(y.cpu().numpy(), csr.spmv(x.cpu().numpy()), rtol=0, atol=0)
+
+
+def test_compressed_da(ctx):
+    """compressLut: same element data, node list, matVec and matrix, in less
+    device memory."""
+    pts = datagen.lognormal(60_000, seed=21)
+    bal = balanceOctree(points2Octree(pts, ctx=ctx))
+    plain, comp = DA(bal), DA(bal, compressLut=True)
+    dp, dc = plain.download(), comp.download()
+    for k in dp:
+        assert np.array_equal(dp[k], dc[k]), k
+    x = np.random.Generator(np.random.PCG64(4)).uniform(-1, 1, plain.n_node)
+    assert np.array_equal(plain.matvec(x), comp.matvec(x))
+    assert np.array_equal(plain.matvec(x.astype(np.float32), precision=32), comp.matvec(x.astype(np.float32), precision=32))
+    a, b = plain.assemble().to_numpy(), comp.assemble().to_numpy()
+    assert all(np.array_equal(u, v) for u, v in zip(a, b))
+    assert comp.memory_bytes() < 0.7 * plain.memory_bytes()
