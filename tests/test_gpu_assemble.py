@@ -100,8 +100,10 @@ def test_compressed_da(ctx):
     for k in dp:
         assert np.array_equal(dp[k], dc[k]), k
     x = np.random.Generator(np.random.PCG64(4)).uniform(-1, 1, plain.n_node)
-    assert np.array_equal(plain.matvec(x), comp.matvec(x))
-    assert np.array_equal(plain.matvec(x.astype(np.float32), precision=32), comp.matvec(x.astype(np.float32), precision=32))
+    # the element loop adds shared nodes' sums atomically: equal to rounding
+    np.testing.assert_allclose(comp.matvec(x), plain.matvec(x), rtol=1e-12, atol=1e-15)
+    x32 = x.astype(np.float32)
+    np.testing.assert_allclose(comp.matvec(x32, precision=32), plain.matvec(x32, precision=32), rtol=1e-4, atol=1e-7)
     a, b = plain.assemble().to_numpy(), comp.assemble().to_numpy()
     assert all(np.array_equal(u, v) for u, v in zip(a, b))
     assert comp.memory_bytes() < 0.7 * plain.memory_bytes()
