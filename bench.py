@@ -589,6 +589,94 @@ def run_poisson(args, dg, ctx, local):
     return out
 
 
+def run_rows(args, dg, ctx, local):
+    """The rows beside the hot path on one log-normal cloud (--rows-npts
+    points, device resident): completeOctree of a shuffled third of its
+    balanced octree, Hilbert-ordered vs Morton-ordered record downloads, the
+    assembled K + M (CSR) with its SpMV against the matrix-free matVec, and
+    the compressed DA's memory and matVec.  Every library call returns with
+    its results complete, so host clocks around a call time its device work
+    and launch overhead; best of --rows-reps."""
+    import torch
+
+    from dendro_gb300 import datagen
+
+    dev = f"cuda:{local}"
+    reps = args.rows_reps
+
+    def best(fn):
+        fn()
+        ts = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = fn()
+            torch.cuda.synchronize()
+            ts.append(1e3 * (time.perf_counter() - t0))
+            if hasattr(r, "free"):
+                r.free()
+        return min(ts)
+
+    pts = torch.from_numpy(datagen.lognormal(args.rows_npts, seed=5)).to(dev)
+    lin = dg.points2Octree(pts, ctx=ctx)
+    bal = dg.balanceOctree(lin)
+    lin.free()
+    del pts
+    n = bal.size
+    rec = torch.empty((n, 4), dtype=torch.int32, device=dev)
+    res = {"workload": f"lognormal{args.rows_npts // 1_000_000}m", "points": args.rows_npts, "octants": n}
+
+    # completeOctree (construct.cpp:518) of every third octant, shuffled
+    g = torch.Generator(device=dev)
+    g.manual_seed(3)
+    bal.download_to(rec)
+    sub = rec[::3][torch.randperm((n + 2) // 3, device=dev, generator=g)].contiguous()
+    out = dg.completeOctree(sub, 30, ctx=ctx)
+    ms = best(lambda: dg.completeOctree(sub, 30, ctx=ctx))
+    res["complete_octree"] = {"input_octants": sub.shape[0], "output_octants": out.size, "ms": ms,
+                              "Mocts_per_s": sub.shape[0] / (ms * 1e-3) / 1e6}
+    out.free()
+    del sub
+
+    # record order at the boundary
+    ms_m = best(lambda: bal.download_to(rec))
+    ctx.set_order("hilbert")
+    ms_h = best(lambda: bal.download_to(rec))
+    ctx.set_order("morton")
+    res["records_download"] = {"morton_ms": ms_m, "hilbert_ms": ms_h,
+                               "hilbert_Mocts_per_s": n / (ms_h * 1e-3) / 1e6}
+    del rec
+
+    # assembled K + M (odaJac.C:470) and SpMV vs the matrix-free element loop
+    da = dg.DA(bal)
+    csr = da.assemble()
+    ms_a = best(lambda: da.assemble())
+    x = torch.rand(da.n_node, dtype=torch.float64, device=dev)
+    y = torch.empty_like(x)
+    ms_spmv = best(lambda: csr.spmv(x, y))
+    ms_mv = best(lambda: da.matvec(x, y))
+    res["assembly"] = {"n_elem": da.n_elem, "n_rows": csr.n_rows, "nnz": csr.nnz, "max_row_len": csr.max_row_len,
+                       "assemble_ms": ms_a, "spmv_fp64_ms": ms_spmv, "matvec_fp64_ms": ms_mv,
+                       "csr_bytes_per_row": (12 * csr.nnz + 8 * (csr.n_rows + 1)) / csr.n_rows}
+    csr.free()
+
+    # compressed DA (compressLut)
+    dac = dg.DA(bal, compressLut=True)
+    x32 = x.float()
+    y32 = torch.empty_like(x32)
+    res["compressed_da"] = {
+        "plain_bytes_per_elem": da.memory_bytes() / da.n_elem,
+        "compressed_bytes_per_elem": dac.memory_bytes() / dac.n_elem,
+        "matvec_fp32_ms_plain": best(lambda: da.matvec(x32, y32, precision=32)),
+        "matvec_fp32_ms_compressed": best(lambda: dac.matvec(x32, y32, precision=32)),
+    }
+    da.free()
+    dac.free()
+    bal.free()
+    torch.cuda.empty_cache()
+    return res
+
+
 def run_ours(args):
     import torch
 
@@ -625,6 +713,8 @@ def run_ours(args):
             extra["batching"] = run_batching(args, dg, ctx, local)
         if not args.skip_mg:
             extra["precision"] = run_poisson(args, dg, ctx, local)
+        if not args.skip_rows:
+            extra["next_rows"] = run_rows(args, dg, ctx, local)
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": None, "note": "serving skipped", **extra}), flush=True)
         return
@@ -645,6 +735,8 @@ def run_ours(args):
         extra["batching"] = run_batching(args, dg, ctx, local)
     if not args.skip_mg:
         extra["precision"] = run_poisson(args, dg, ctx, local)
+    if not args.skip_rows:
+        extra["next_rows"] = run_rows(args, dg, ctx, local)
 
     # roofline of the dominant kernel of the served step
     stats = serve["stats"]
@@ -728,6 +820,9 @@ def main():
     ap.add_argument("--skip-batch", action="store_true")
     ap.add_argument("--skip-mg", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-rows", action="store_true")
+    ap.add_argument("--rows-npts", type=int, default=8_000_000)
+    ap.add_argument("--rows-reps", type=int, default=3)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
