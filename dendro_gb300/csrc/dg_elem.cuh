@@ -148,11 +148,18 @@ __device__ __forceinline__ void apply_comb(const double *__restrict__ S, const d
 // Dirichlet form: boundary rows are the identity (y = x), boundary columns
 // are dropped.  One block of PATCH threads per patch, grid-strided; thread t
 // holds pairs 8t..8t+7 of the patch's table and is element t of the patch.
-// The slot buffer and the run-node array are double-buffered by patch
-// parity and the next patch's table words are loaded one patch ahead, so a
-// patch costs three barriers.
+// In FP32 the slot buffer and the run-node array are double-buffered by
+// patch parity, so a patch costs three barriers; in FP64 they are single
+// (one more barrier per patch) so that two blocks fit an SM and one block's
+// FP64 stencil phase overlaps the other's gathers and sums.  The next
+// patch's table words are loaded one patch ahead.
+template <typename T>
+constexpr int patch_nbuf() {
+  return sizeof(T) == 4 ? 2 : 1;
+}
+
 template <typename T, bool DIR>
-__global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
+__global__ void __launch_bounds__(PATCH, 2)
     k_patch_matvec(const uint32_t *__restrict__ pmeta, const uint16_t *__restrict__ pinc,
                    const uint16_t *__restrict__ pexc, const uint32_t *__restrict__ pnode,
                    const uint64_t *__restrict__ poff, const uint16_t *__restrict__ pkeys,
@@ -162,9 +169,10 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
   constexpr int NW = PATCH / 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *cs = reinterpret_cast<T *>(smem_raw);
+  constexpr int NBUF = patch_nbuf<T>();
   T *bufs = cs + fsten_entries<T>();
-  uint32_t *gns = reinterpret_cast<uint32_t *>(bufs + 2 * PATCH_ENT);
-  uint32_t *cp = gns + 2 * PATCH_ENT;
+  uint32_t *gns = reinterpret_cast<uint32_t *>(bufs + NBUF * PATCH_ENT);
+  uint32_t *cp = gns + NBUF * PATCH_ENT;
   T *sc = reinterpret_cast<T *>(cp + 8 * 18 + 4);  // PKEY_MAX combined stencils (16-byte aligned)
   __shared__ T ws_v[2][NW];
   __shared__ int ws_f[2][NW];
@@ -189,7 +197,7 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
     }
   }
   int par = 0;
-  for (; p < n_patch; p += gridDim.x, par ^= 1) {
+  for (; p < n_patch; p += gridDim.x, par ^= (NBUF - 1)) {
     const int ne = patch_ne(p);
     const bool have = tid < ne;
     const uint4 cw = w;
@@ -338,12 +346,13 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 2 : 1)
       }
       if (last_run_ends) emit(u, acc, ent(7));
     }
+    if (NBUF == 1) __syncthreads();  // the next patch rewrites buf and gn
   }
 }
 
 template <typename T>
 constexpr size_t patch_smem() {
-  return fsten_entries<T>() * sizeof(T) + 2 * PATCH_ENT * sizeof(T) + 2 * PATCH_ENT * sizeof(uint32_t) +
+  return fsten_entries<T>() * sizeof(T) + patch_nbuf<T>() * PATCH_ENT * (sizeof(T) + sizeof(uint32_t)) +
          (8 * 18 + 4) * sizeof(uint32_t) + PKEY_MAX * sstride<T>() * sizeof(T);
 }
 
