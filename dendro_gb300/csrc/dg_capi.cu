@@ -172,6 +172,8 @@ int dg_ctx_destroy(dg_ctx ctx) {
   if (ctx->c.h_scratch) cudaFreeHost(ctx->c.h_scratch);
   if (ctx->c.d_sten64) cudaFree(ctx->c.d_sten64);
   if (ctx->c.d_sten32) cudaFree(ctx->c.d_sten32);
+  if (ctx->c.d_comb64) cudaFree(ctx->c.d_comb64);
+  if (ctx->c.d_comb32) cudaFree(ctx->c.d_comb32);
   if (ctx->c.d_csten64) cudaFree(ctx->c.d_csten64);
   if (ctx->c.d_csten32) cudaFree(ctx->c.d_csten32);
   if (ctx->c.d_cperm) cudaFree(ctx->c.d_cperm);

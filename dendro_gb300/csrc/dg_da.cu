@@ -804,6 +804,27 @@ void mesh_free(Context &ctx, Mesh &m) {
 // element loop
 // ------------------------------------------------------------------------
 template <typename T>
+const T *comb_table(Context &ctx, double lap_fac, double mass_fac) {
+  ensure_stencils(ctx);
+  const bool dbl = std::is_same<T, double>::value;
+  T **tab = reinterpret_cast<T **>(dbl ? (void *)&ctx.d_comb64 : (void *)&ctx.d_comb32);
+  double *f = dbl ? ctx.comb64_f : ctx.comb32_f;
+  bool &ok = dbl ? ctx.comb64_ok : ctx.comb32_ok;
+  if (!*tab) DG_CUDA(cudaMalloc((void **)tab, COMB_ENTRIES * sizeof(T)));
+  if (!ok || f[0] != lap_fac || f[1] != mass_fac) {
+    const T *cs = dbl ? reinterpret_cast<const T *>(ctx.d_csten64) : reinterpret_cast<const T *>(ctx.d_csten32);
+    k_comb_table<T><<<(COMB_ENTRIES + 255) / 256, 256, 0, ctx.stream>>>(cs, (T)lap_fac, (T)mass_fac, *tab);
+    DG_LAUNCH_CHECK();
+    f[0] = lap_fac;
+    f[1] = mass_fac;
+    ok = true;
+  }
+  return *tab;
+}
+template const float *comb_table<float>(Context &, double, double);
+template const double *comb_table<double>(Context &, double, double);
+
+template <typename T>
 void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, double mass_fac) {
   ensure_stencils(ctx);
   cudaStream_t s = ctx.stream;
@@ -819,12 +840,13 @@ void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, 
   const unsigned grid = (unsigned)std::min<size_t>(m.n_patch, (size_t)per_sm * ctx.num_sms);
   const T *cs = std::is_same<T, double>::value ? reinterpret_cast<const T *>(ctx.d_csten64)
                                                : reinterpret_cast<const T *>(ctx.d_csten32);
+  const T *ctab = comb_table<T>(ctx, lap_fac, mass_fac);
   {
     ProfScope _prof(ctx, sizeof(T) == 4 ? "matvec_fp32" : "matvec_fp64",
                     (double)m.n_elem * 36 + (double)m.n_node * 3 * sizeof(T));
     k_patch_matvec<T, false><<<grid, PATCH, smem, s>>>(m.pmeta, m.pinc, m.pexc, m.pnode, m.poff, m.pkeys,
-                                                       m.pkcount, m.n_elem, m.n_patch, cs, ctx.d_cperm, nullptr, x,
-                                                       y, (T)lap_fac, (T)mass_fac);
+                                                       m.pkcount, m.n_elem, m.n_patch, cs, ctab, ctx.d_cperm, nullptr,
+                                                       x, y, (T)lap_fac, (T)mass_fac);
     DG_LAUNCH_CHECK();
   }
 }

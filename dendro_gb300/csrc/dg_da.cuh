@@ -108,6 +108,10 @@ constexpr int STEN_ENTRIES = 8 * 18 * 128;
 
 // stencil tables on the device, generated on first use
 void ensure_stencils(Context &ctx);
+// the combined-stencil table of the element loop for these factors
+// (rebuilt on ctx's stream when they differ from the last call's)
+template <typename T>
+const T *comb_table(Context &ctx, double lap_fac, double mass_fac);
 
 // host-side generators (same mathematics as the reference's .inp tables)
 void gen_etype_masks(uint8_t masks[8 * 18]);

@@ -57,6 +57,21 @@ __device__ __forceinline__ double exp2_neg(double, unsigned l) {
   return __longlong_as_double((long long)(1023u - l) << 52);
 }
 
+// combined stencils of every (type, level), 32 levels per type:
+// comb[(t * 32 + l) * 64 + q] = lapf 2^-l / 2 L_t[q] + massf 2^-3l / 8 M_t[q]
+// (the element loop copies the ones a patch uses into shared memory)
+constexpr int COMB_LEVELS = 32;
+constexpr int COMB_ENTRIES = 18 * COMB_LEVELS * 64;
+template <typename T>
+__global__ void k_comb_table(const T *__restrict__ cs, T lapf, T massf, T *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= COMB_ENTRIES) return;
+  const int t = i / (COMB_LEVELS * 64), l = (i / 64) % COMB_LEVELS, q = i % 64;
+  const T h = exp2_neg((T)0, (unsigned)l);
+  const T *st = cs + t * fsten_stride<T>();
+  out[i] = lapf * h * (T)0.5 * st[q] + massf * h * h * h * (T)0.125 * st[64 + q];
+}
+
 // two FP32 fused multiply-adds in one instruction (Blackwell f32x2)
 __device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
   float2 d;
@@ -133,14 +148,14 @@ template <typename Emit>
 __device__ __forceinline__ void apply_comb(const double *__restrict__ S, const double (&xv)[8], Emit &&emit) {
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    double a = 0, b = 0;
+    double a = 0;
 #pragma unroll
     for (int j = 0; j < 8; j += 2) {
       const double2 sv = reinterpret_cast<const double2 *>(S + 8 * k + j)[0];
       a = fma(sv.x, xv[j], a);
-      b = fma(sv.y, xv[j + 1], b);
+      a = fma(sv.y, xv[j + 1], a);
     }
-    emit(k, a + b);
+    emit(k, a);
   }
 }
 
@@ -164,8 +179,8 @@ __global__ void __launch_bounds__(PATCH, 2)
                    const uint16_t *__restrict__ pexc, const uint32_t *__restrict__ pnode,
                    const uint64_t *__restrict__ poff, const uint16_t *__restrict__ pkeys,
                    const uint16_t *__restrict__ pkcount, size_t E, size_t n_patch, const T *__restrict__ fsten,
-                   const uint32_t *__restrict__ cperm, const uint8_t *__restrict__ bdy, const T *__restrict__ x,
-                   T *__restrict__ y, T lapf, T massf) {
+                   const T *__restrict__ ctab, const uint32_t *__restrict__ cperm, const uint8_t *__restrict__ bdy,
+                   const T *__restrict__ x, T *__restrict__ y, T lapf, T massf) {
   constexpr int NW = PATCH / 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *cs = reinterpret_cast<T *>(smem_raw);
@@ -251,10 +266,15 @@ __global__ void __launch_bounds__(PATCH, 2)
       for (int i = tid; i < (int)ckc * 64; i += PATCH) {
         const uint32_t key = pkeys[p * PKEY_MAX + (i >> 6)];
         const unsigned t = key >> 5, l = key & 31u;
-        const T h = exp2_neg((T)0, l);
-        const T *st = cs + t * fsten_stride<T>();
-        sc[(i >> 6) * sstride<T>() + (i & 63)] =
-            lapf * h * (T)0.5 * st[i & 63] + massf * h * h * h * (T)0.125 * st[64 + (i & 63)];
+        if constexpr (sizeof(T) == 8) {
+          // FP64 issue is scarce: copy the precomputed entry
+          sc[(i >> 6) * sstride<T>() + (i & 63)] = ctab[(t * COMB_LEVELS + l) * 64 + (i & 63)];
+        } else {
+          const T h = exp2_neg((T)0, l);
+          const T *st = cs + t * fsten_stride<T>();
+          sc[(i >> 6) * sstride<T>() + (i & 63)] =
+              lapf * h * (T)0.5 * st[i & 63] + massf * h * h * h * (T)0.125 * st[64 + (i & 63)];
+        }
       }
     }
     if (lane == 0) ws_first[par][wid] = (ent(0) & ENT_START) ? 1 : 0;

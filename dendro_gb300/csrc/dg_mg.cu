@@ -459,8 +459,10 @@ void dirichlet_matvec(Context &ctx, const MGLevel &L, const T *x, T *y) {
                                                : reinterpret_cast<const T *>(ctx.d_csten32);
   ProfScope _prof(ctx, sizeof(T) == 4 ? "dirichlet_matvec_fp32" : "dirichlet_matvec_fp64",
                   (double)m.n_elem * 36 + (double)m.n_node * (3 * sizeof(T) + 1));
+  const T *ctab = comb_table<T>(ctx, 1.0, 1.0);
   k_patch_matvec<T, true><<<grid, PATCH, smem, s>>>(m.pmeta, m.pinc, m.pexc, m.pnode, m.poff, m.pkeys, m.pkcount,
-                                                    m.n_elem, m.n_patch, cs, ctx.d_cperm, L.bdy, x, y, (T)1, (T)1);
+                                                    m.n_elem, m.n_patch, cs, ctab, ctx.d_cperm, L.bdy, x, y, (T)1,
+                                                    (T)1);
   DG_LAUNCH_CHECK();
 }
 

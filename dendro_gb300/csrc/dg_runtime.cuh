@@ -47,6 +47,12 @@ struct Context {
   double *d_csten64 = nullptr;     // canonical full stencils, 18 types (dg_elem.cuh)
   float *d_csten32 = nullptr;
   uint32_t *d_cperm = nullptr;     // [8][18] vertex relabelling, 3 bits each
+  // combined stencils lapf 2^-l/2 L_t + massf 2^-3l/8 M_t per (type, level)
+  // for the factors of the last element loop (dg_elem.cuh, comb_table)
+  double *d_comb64 = nullptr;
+  float *d_comb32 = nullptr;
+  double comb64_f[2] = {0, 0}, comb32_f[2] = {0, 0};
+  bool comb64_ok = false, comb32_ok = false;
   bool prof = false;
   std::map<std::string, ProfStat> prof_stats;
   std::vector<ProfPending> prof_pending;
