@@ -9,8 +9,9 @@
 // the threads of a warp mostly read the same stencil (a broadcast).
 //
 // Patches: PATCH consecutive elements form a patch.  Its incidence table
-// lists the 8 x PATCH (element, vertex) pairs sorted by node id, 16 bits
-// each:
+// lists the 8 x PATCH (element, vertex) pairs grouped by node (one run per
+// node, runs in the order of a per-patch hash table, the pairs of a run by
+// slot), 16 bits each:
 //   bits 0..11  slot = vertex * PATCH + element within the patch
 //   bit 12      first pair of a node's run
 //   bit 13      the run holds every pair of its node in the whole mesh, so
