@@ -92,6 +92,10 @@ def _declare(L):
         "dg_da_free": ([P, P], I),
         "dg_matvec": ([P, P, P, P, I, D, D, I], I),
         "dg_da_assemble": ([P, P, D, D, PP], I),
+        "dg_da_assemble_coef": ([P, P, P, I, PP], I),
+        "dg_matvec_coef": ([P, P, P, P, P, I, I], I),
+        "dg_da_diagonal": ([P, P, P, D, D, P, I], I),
+        "dg_mg_diagonal": ([P, P, SZ, P, I], I),
         "dg_da_build_ex": ([P, P, I, PP], I),
         "dg_da_memory": ([P, ctypes.POINTER(SZ)], I),
         "dg_mg_assemble": ([P, P, SZ, PP], I),

@@ -452,6 +452,42 @@ class DA:
     def getNodeSize(self) -> int:
         return self.n_node
 
+    def matvec_coef(self, coef, x, out=None, precision: int = 64):
+        """Jacobian2MatMult (examples/src/backend/omgJac.C:1666-1735): per
+        element e, coef[e, 0] scales its Laplacian and coef[e, 1] its mass
+        (coef: n_elem x 2 FP64, elements in octree order)."""
+        on_dev = _is_device(x)
+        if on_dev:
+            out = x.new_empty(x.shape) if out is None else out
+            c = coef
+        else:
+            x = np.ascontiguousarray(x, dtype=np.float64 if precision == 64 else np.float32)
+            out = np.empty_like(x) if out is None else out
+            c = np.ascontiguousarray(coef, dtype=np.float64).reshape(-1, 2)
+            if c.shape[0] != self.n_elem:
+                raise ValueError("coef must hold 2 values per element")
+        check(self.ctx.handle, self.ctx._L.dg_matvec_coef(self.ctx.handle, self.handle, _ptr(c), _ptr(x), _ptr(out),
+                                                          precision, 1 if on_dev else 0), "dg_matvec_coef")
+        return out
+
+    def diagonal(self, lapFac: float = 1.0, massFac: float = 1.0, coef=None) -> np.ndarray:
+        """Jacobian1MatGetDiagonal (odaJac.C:160-222), or with coef
+        Jacobian2MatGetDiagonal (omgJac.C:1641); FP64, host array."""
+        d = np.empty(max(self.n_node, 1), np.float64)
+        c = None if coef is None else np.ascontiguousarray(coef, dtype=np.float64).reshape(-1, 2)
+        check(self.ctx.handle, self.ctx._L.dg_da_diagonal(self.ctx.handle, self.handle, None if c is None else _ptr(c),
+                                                          lapFac, massFac, _ptr(d), 0), "dg_da_diagonal")
+        return d[: self.n_node]
+
+    def assemble_coef(self, coef) -> "Csr":
+        """BUILD_FULL_JAC_TYPE2_BLOCK (omgJac.C:1804-1858): the per-element
+        operator of matvec_coef as a CSR matrix."""
+        c = np.ascontiguousarray(coef, dtype=np.float64).reshape(-1, 2)
+        h = ctypes.c_void_p()
+        check(self.ctx.handle, self.ctx._L.dg_da_assemble_coef(self.ctx.handle, self.handle, _ptr(c), 0, ctypes.byref(h)),
+              "dg_da_assemble_coef")
+        return Csr(self.ctx, h)
+
     def memory_bytes(self) -> int:
         """Device bytes the DA holds."""
         b = ctypes.c_size_t()
@@ -528,6 +564,14 @@ class MultiGrid:
             e, v = ctypes.c_size_t(), ctypes.c_size_t()
             ctx._L.dg_mg_level_sizes(h, l, ctypes.byref(e), ctypes.byref(v))
             self.sizes.append((e.value, v.value))
+
+    def diagonal(self, level: int) -> np.ndarray:
+        """DirichletJacobianMatGetDiagonal (omgJac.C:1111): FP64, 1 on boundary nodes."""
+        n = self.sizes[level][1]
+        d = np.empty(max(n, 1), np.float64)
+        check(self.ctx.handle, self.ctx._L.dg_mg_diagonal(self.ctx.handle, self.handle, level, _ptr(d), 0),
+              "dg_mg_diagonal")
+        return d[:n]
 
     def assemble(self, level: int) -> Csr:
         """ComputeDirichletJacobian (examples/src/backend/omgJac.C:383): the

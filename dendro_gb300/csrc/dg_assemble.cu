@@ -86,8 +86,8 @@ __global__ void k_row_count(const uint64_t *__restrict__ key, const uint64_t *__
 __global__ void k_row_fill(const uint64_t *__restrict__ key, const uint64_t *__restrict__ start, size_t V,
                            const uint32_t *__restrict__ meta, const uint32_t *__restrict__ conn, size_t E,
                            const uint8_t *__restrict__ bdy, const double *__restrict__ sten, double lap_fac,
-                           double mass_fac, const uint64_t *__restrict__ row_ptr, uint32_t *__restrict__ col,
-                           double *__restrict__ val) {
+                           double mass_fac, const double *__restrict__ coef, const uint64_t *__restrict__ row_ptr,
+                           uint32_t *__restrict__ col, double *__restrict__ val) {
   const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= V) return;
   const uint64_t out = row_ptr[v];
@@ -107,7 +107,8 @@ __global__ void k_row_fill(const uint64_t *__restrict__ key, const uint64_t *__r
     const uint32_t me = meta[e];
     const unsigned l = me & 255u, c = (me >> 8) & 7u, t = me >> 24;
     const double h = 1.0 / (double)(1ull << l);
-    const double f1 = lap_fac * h * 0.5, f2 = mass_fac * h * h * h * 0.125;
+    const double lf = coef ? coef[2 * e] : lap_fac, mf = coef ? coef[2 * e + 1] : mass_fac;
+    const double f1 = lf * h * 0.5, f2 = mf * h * h * h * 0.125;
     const double *S = sten + (c * 18 + t) * 128 + 8 * k;
     for (int j = 0; j < 8; j++) {
       const uint32_t cj = conn[(size_t)j * E + e];
@@ -155,12 +156,16 @@ unsigned bits_of(size_t v) {
 
 }  // namespace
 
-void assemble_csr(Context &ctx, const Mesh &m, const uint8_t *bdy, double lap_fac, double mass_fac, Csr &out) {
+void assemble_csr(Context &ctx, const Mesh &m, const uint8_t *bdy, double lap_fac, double mass_fac, Csr &out,
+                  const double *coef) {
   cudaStream_t s = ctx.stream;
   ensure_stencils(ctx);
   const size_t E = m.n_elem, V = m.n_node;
   if (E >= ((size_t)1 << 29)) fail(DG_ERR_UNSUPPORTED, "assemble: more than 2^29 elements");
-  if (bdy) lap_fac = mass_fac = 1.0;
+  if (bdy) {
+    lap_fac = mass_fac = 1.0;
+    coef = nullptr;
+  }
   out = Csr();
   out.n_rows = V;
   DBuf<uint64_t> rp(V + 1, s);
@@ -209,7 +214,7 @@ void assemble_csr(Context &ctx, const Mesh &m, const uint8_t *bdy, double lap_fa
   {
     ProfScope _prof(ctx, "csr_fill", (double)np * 8 * 8 + (double)nnz * 12);
     k_row_fill<<<grid_for(V, 128), 128, 0, s>>>(key, start.get(), V, m.meta, conn, E, bdy, ctx.d_sten64, lap_fac,
-                                                 mass_fac, rp.get(), col.get(), val.get());
+                                                 mass_fac, coef, rp.get(), col.get(), val.get());
     DG_LAUNCH_CHECK();
   }
   DG_CUDA(cudaStreamSynchronize(s));

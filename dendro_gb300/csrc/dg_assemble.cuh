@@ -27,9 +27,12 @@ struct Csr {
   unsigned max_row = 0;        // longest row
 };
 
-// bdy == nullptr: lap_fac K + mass_fac M; otherwise the Dirichlet form of
-// K + M with bdy[v] != 0 marking boundary nodes (lap_fac, mass_fac ignored)
-void assemble_csr(Context &ctx, const Mesh &m, const uint8_t *bdy, double lap_fac, double mass_fac, Csr &out);
+// bdy == nullptr: lap_fac K + mass_fac M, or with coef (2 per element,
+// device) each element's own factors (the matrix of Jacobian2MatMult:
+// BUILD_FULL_JAC_TYPE2_BLOCK, omgJac.C:1804-1858); bdy given: the Dirichlet
+// form of K + M with bdy[v] != 0 marking boundary nodes (factors ignored)
+void assemble_csr(Context &ctx, const Mesh &m, const uint8_t *bdy, double lap_fac, double mass_fac, Csr &out,
+                  const double *coef = nullptr);
 void csr_free(Context &ctx, Csr &c);
 // y = A x (FP64), rows split over groups of 8 lanes
 void csr_spmv(Context &ctx, const Csr &c, const double *x, double *y);

@@ -722,6 +722,78 @@ int dg_da_assemble(dg_ctx ctx, dg_da da, double lapFac, double massFac, dg_csr *
   return csr_handle(ctx, out, [&](dg::Csr &c) { dg::assemble_csr(ctx->c, da->m, nullptr, lapFac, massFac, c); });
 }
 
+int dg_da_assemble_coef(dg_ctx ctx, dg_da da, const double *coef, int coef_on_device, dg_csr *out) {
+  if (!da || (!coef && da->m.n_elem)) return DG_ERR_INVALID_ARG;
+  return csr_handle(ctx, out, [&](dg::Csr &c) {
+    dg::DBuf<double> hold;
+    const double *dc = device_input(ctx->c, coef, 2 * da->m.n_elem, coef_on_device, hold);
+    dg::assemble_csr(ctx->c, da->m, nullptr, 1.0, 1.0, c, dc);
+  });
+}
+
+int dg_matvec_coef(dg_ctx ctx, dg_da da, const double *coef, const void *in, void *out, int precision, int on_device) {
+  if (!da || !in || !out || (!coef && da->m.n_elem)) return DG_ERR_INVALID_ARG;
+  if (precision != 32 && precision != 64) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() {
+    dg::Context &c = ctx->c;
+    const size_t V = da->m.n_node;
+    dg::DBuf<double> hc;
+    const double *dc = device_input(c, coef, 2 * da->m.n_elem, on_device, hc);
+    auto run = [&](auto tag) {
+      using T = decltype(tag);
+      dg::DBuf<T> hin, hout;
+      const T *x = device_input(c, (const T *)in, V, on_device, hin);
+      T *y = (T *)out;
+      if (!on_device) {
+        hout.alloc(V, c.stream);
+        y = hout.get();
+      }
+      dg::mesh_matvec_coef<T>(c, da->m, dc, x, y);
+      if (!on_device) copy_out(c, (T *)out, y, V, 0);
+      DG_CUDA(cudaStreamSynchronize(c.stream));
+    };
+    if (precision == 64) run(double());
+    else run(float());
+  });
+}
+
+int dg_da_diagonal(dg_ctx ctx, dg_da da, const double *coef, double lapFac, double massFac, double *diag,
+                   int on_device) {
+  if (!da || !diag) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() {
+    dg::Context &c = ctx->c;
+    const size_t V = da->m.n_node;
+    dg::DBuf<double> hc, hd;
+    const double *dc = coef ? device_input(c, coef, 2 * da->m.n_elem, on_device, hc) : nullptr;
+    double *d = diag;
+    if (!on_device) {
+      hd.alloc(V ? V : 1, c.stream);
+      d = hd.get();
+    }
+    dg::mesh_diagonal(c, da->m, dc, lapFac, massFac, d);
+    if (!on_device) copy_out(c, diag, d, V, 0);
+    DG_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int dg_mg_diagonal(dg_ctx ctx, dg_mg mg, size_t level, double *diag, int on_device) {
+  if (!mg || level >= mg->mg.lv.size() || !diag) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() {
+    dg::Context &c = ctx->c;
+    const dg::MGLevel &L = mg->mg.lv[level];
+    const size_t V = L.mesh.n_node;
+    dg::DBuf<double> hd;
+    double *d = diag;
+    if (!on_device) {
+      hd.alloc(V ? V : 1, c.stream);
+      d = hd.get();
+    }
+    dg::dirichlet_diagonal(c, L, d);
+    if (!on_device) copy_out(c, diag, d, V, 0);
+    DG_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
 int dg_mg_assemble(dg_ctx ctx, dg_mg mg, size_t level, dg_csr *out) {
   if (!mg || level >= mg->mg.lv.size()) return DG_ERR_INVALID_ARG;
   const dg::MGLevel &L = mg->mg.lv[level];

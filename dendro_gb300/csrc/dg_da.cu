@@ -687,8 +687,7 @@ static void mesh_patches(Context &ctx, Mesh &m) {
   DBuf<uint32_t> pmeta(np * PATCH, s);
   DBuf<uint16_t> pkeys(np * PKEY_MAX, s), pkcount(np, s);
   DBuf<uint64_t> poff(np + 1, s);
-  DBuf<uint16_t> pperm;
-  if (m.compressed) pperm.alloc(np * PATCH, s);
+  DBuf<uint16_t> pperm(np * PATCH, s);
   DG_CUDA(cudaMemsetAsync(pairs.get(), 0, m.n_node * sizeof(uint32_t), s));
   {
     ProfScope _prof(ctx, "da_node_pairs", (double)n * 8 * 8);
@@ -705,7 +704,7 @@ static void mesh_patches(Context &ctx, Mesh &m) {
     k_patch_sort<<<(unsigned)np, PATCH, sizeof(PatchSortSmem), s>>>(m.conn, m.meta, n, pairs.get(), pinc.get(),
                                                                     pexc.get(), pmeta.get(), pkeys.get(),
                                                                     pkcount.get(), run_node.get(), n_run.get(),
-                                                                    m.compressed ? pperm.get() : nullptr);
+                                                                    pperm.get());
     DG_LAUNCH_CHECK();
   }
   exclusive_scan<uint32_t, uint64_t>(n_run.get(), poff.get(), np, poff.get() + np, s);
@@ -726,7 +725,7 @@ static void mesh_patches(Context &ctx, Mesh &m) {
   m.pkcount = pkcount.release_ptr();
   m.pnode = pnode.release_ptr();
   m.poff = poff.release_ptr();
-  if (m.compressed) m.pperm = pperm.release_ptr();
+  m.pperm = pperm.release_ptr();
 }
 
 void mesh_build(Context &ctx, const Octree &bal, Mesh &m, bool compress) {
@@ -853,5 +852,62 @@ void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, 
 
 template void mesh_matvec<float>(Context &, const Mesh &, const float *, float *, double, double);
 template void mesh_matvec<double>(Context &, const Mesh &, const double *, double *, double, double);
+
+template <typename T>
+void mesh_matvec_coef(Context &ctx, const Mesh &m, const double *coef, const T *x, T *y) {
+  ensure_stencils(ctx);
+  cudaStream_t s = ctx.stream;
+  DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
+  const size_t smem = patch_smem<T>();
+  static std::once_flag once;
+  std::call_once(once, [&]() {
+    DG_CUDA(cudaFuncSetAttribute(k_patch_matvec<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+  });
+  int per_sm = 1;
+  DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_patch_matvec<T, false, true>, PATCH, smem));
+  if (per_sm < 1) per_sm = 1;
+  const unsigned grid = (unsigned)std::min<size_t>(m.n_patch, (size_t)per_sm * ctx.num_sms);
+  const T *cs = std::is_same<T, double>::value ? reinterpret_cast<const T *>(ctx.d_csten64)
+                                               : reinterpret_cast<const T *>(ctx.d_csten32);
+  ProfScope _prof(ctx, sizeof(T) == 4 ? "matvec_coef_fp32" : "matvec_coef_fp64",
+                  (double)m.n_elem * (36 + 16 + 2) + (double)m.n_node * 3 * sizeof(T));
+  k_patch_matvec<T, false, true><<<grid, PATCH, smem, s>>>(m.pmeta, m.pinc, m.pexc, m.pnode, m.poff, m.pkeys,
+                                                           m.pkcount, m.n_elem, m.n_patch, cs, nullptr, ctx.d_cperm,
+                                                           nullptr, x, y, (T)1, (T)1, coef, m.pperm);
+  DG_LAUNCH_CHECK();
+}
+template void mesh_matvec_coef<float>(Context &, const Mesh &, const double *, const float *, float *);
+template void mesh_matvec_coef<double>(Context &, const Mesh &, const double *, const double *, double *);
+
+// diagonal entries per element, added atomically (a node's sum is over the
+// elements that hold it)
+__global__ void k_mesh_diag(const uint32_t *__restrict__ meta, const uint32_t *__restrict__ conn, size_t E,
+                            const double *__restrict__ sten, const double *__restrict__ coef, double lap_fac,
+                            double mass_fac, double *__restrict__ diag) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const uint32_t me = meta[e];
+  const unsigned l = me & 255u, c = (me >> 8) & 7u, t = me >> 24;
+  const double h = 1.0 / (double)(1ull << l);
+  const double lf = coef ? coef[2 * e] : lap_fac, mf = coef ? coef[2 * e + 1] : mass_fac;
+  const double f1 = lf * h / 2.0, f2 = mf * h * h * h / 8.0;
+  const double *S = sten + (c * 18 + t) * 128;
+#pragma unroll
+  for (int k = 0; k < 8; k++) atomicAdd(&diag[conn[(size_t)k * E + e]], f1 * S[9 * k] + f2 * S[64 + 9 * k]);
+}
+
+void mesh_diagonal(Context &ctx, const Mesh &m, const double *coef, double lap_fac, double mass_fac, double *diag) {
+  ensure_stencils(ctx);
+  cudaStream_t s = ctx.stream;
+  DG_CUDA(cudaMemsetAsync(diag, 0, m.n_node * sizeof(double), s));
+  if (!m.n_elem) return;
+  DBuf<uint32_t> tmp;
+  const uint32_t *conn = mesh_conn(ctx, m, tmp);
+  ProfScope _prof(ctx, "mesh_diagonal", (double)m.n_elem * (4 + 32 + (coef ? 16 : 0)) + (double)m.n_node * 8);
+  k_mesh_diag<<<grid_for(m.n_elem, 256), 256, 0, s>>>(m.meta, conn, m.n_elem, ctx.d_sten64, coef, lap_fac, mass_fac,
+                                                       diag);
+  DG_LAUNCH_CHECK();
+}
 
 }  // namespace dg

@@ -31,10 +31,10 @@ struct Mesh {
   uint16_t *pkcount = nullptr;  // keys per patch (> PKEY_MAX: per-element L, M path)
   uint32_t *pnode = nullptr;  // node of each run, patch after patch
   uint64_t *poff = nullptr;   // n_patch + 1 run offsets into pnode
-  // compressed mode (the reference's compressLut): conn is released once the
-  // patch tables exist and decoded from them on demand (mesh_conn); pperm
-  // maps a patch's (type, level) order back to its element order
+  // pperm maps a patch's (type, level) order back to its element order
   uint16_t *pperm = nullptr;  // PATCH per patch
+  // compressed mode (the reference's compressLut): conn is released once the
+  // patch tables exist and decoded from them on demand (mesh_conn)
   bool compressed = false;
 };
 
@@ -50,6 +50,13 @@ void mesh_free(Context &ctx, Mesh &m);
 // (examples/src/backend/odaJac.C:294-377, block :275-292)
 template <typename T>
 void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, double mass_fac);
+// the same with per-element factors: coef[2e] scales element e's Laplacian,
+// coef[2e + 1] its mass (Jacobian2MatMult, examples/src/backend/omgJac.C:1666-1735)
+template <typename T>
+void mesh_matvec_coef(Context &ctx, const Mesh &m, const double *coef, const T *x, T *y);
+// diagonal of lap_fac K + mass_fac M, or with coef the per-element form
+// (Jacobian1MatGetDiagonal odaJac.C:160-222, Jacobian2MatGetDiagonal omgJac.C:1641)
+void mesh_diagonal(Context &ctx, const Mesh &m, const double *coef, double lap_fac, double mass_fac, double *diag);
 
 // index of the leaf whose anchor is the largest anchor <= pos in a sorted
 // tagged-key array (0 when pos precedes every leaf; callers verify)

@@ -174,14 +174,17 @@ constexpr int patch_nbuf() {
   return sizeof(T) == 4 ? 2 : 1;
 }
 
-template <typename T, bool DIR>
+// With COEF, element e's factors are coef[2e] (Laplacian) and coef[2e + 1]
+// (mass) instead of lapf and massf (pperm gives e from the patch order).
+template <typename T, bool DIR, bool COEF = false>
 __global__ void __launch_bounds__(PATCH, 2)
     k_patch_matvec(const uint32_t *__restrict__ pmeta, const uint16_t *__restrict__ pinc,
                    const uint16_t *__restrict__ pexc, const uint32_t *__restrict__ pnode,
                    const uint64_t *__restrict__ poff, const uint16_t *__restrict__ pkeys,
                    const uint16_t *__restrict__ pkcount, size_t E, size_t n_patch, const T *__restrict__ fsten,
                    const T *__restrict__ ctab, const uint32_t *__restrict__ cperm, const uint8_t *__restrict__ bdy,
-                   const T *__restrict__ x, T *__restrict__ y, T lapf, T massf) {
+                   const T *__restrict__ x, T *__restrict__ y, T lapf, T massf,
+                   const double *__restrict__ coef = nullptr, const uint16_t *__restrict__ pperm = nullptr) {
   constexpr int NW = PATCH / 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *cs = reinterpret_cast<T *>(smem_raw);
@@ -262,7 +265,7 @@ __global__ void __launch_bounds__(PATCH, 2)
     }
     // the patch's combined stencils (read only in step 2 of this patch, and
     // rewritten only after every thread has passed that step's barrier)
-    const bool comb = ckc <= (uint32_t)PKEY_MAX;
+    const bool comb = !COEF && ckc <= (uint32_t)PKEY_MAX;
     if (comb) {
       for (int i = tid; i < (int)ckc * 64; i += PATCH) {
         const uint32_t key = pkeys[p * PKEY_MAX + (i >> 6)];
@@ -293,7 +296,13 @@ __global__ void __launch_bounds__(PATCH, 2)
         apply_comb(sc + ((cme >> 16) & 255u) * sstride<T>(), xv, put);
       } else {
         const T h = exp2_neg((T)0, l);
-        apply_full(cs + t * fsten_stride<T>(), lapf * h * (T)0.5, massf * h * h * h * (T)0.125, xv, put);
+        T lf = lapf, mf = massf;
+        if constexpr (COEF) {
+          const size_t e = p * PATCH + pperm[p * PATCH + tid];
+          lf = (T)coef[2 * e];
+          mf = (T)coef[2 * e + 1];
+        }
+        apply_full(cs + t * fsten_stride<T>(), lf * h * (T)0.5, mf * h * h * h * (T)0.125, xv, put);
       }
     }
     __syncthreads();

@@ -466,6 +466,16 @@ void dirichlet_matvec(Context &ctx, const MGLevel &L, const T *x, T *y) {
   DG_LAUNCH_CHECK();
 }
 
+void dirichlet_diagonal(Context &ctx, const MGLevel &L, double *diag) {
+  ensure_stencils(ctx);
+  const size_t V = L.mesh.n_node, E = L.mesh.n_elem;
+  DG_CUDA(cudaMemsetAsync(diag, 0, V * sizeof(double), ctx.stream));
+  if (!E) return;
+  ProfScope _prof(ctx, "dirichlet_diagonal", (double)E * 36 + (double)V * 9);
+  k_dirichlet_diag<<<grid_for(E, 256), 256, 0, ctx.stream>>>(L.mesh.meta, L.mesh.conn, E, ctx.d_sten64, L.bdy, diag);
+  DG_LAUNCH_CHECK();
+}
+
 template <typename T>
 void mg_restrict(Context &ctx, const MG &mg, int f, const T *rf, T *bc) {
   const MGLevel &F = mg.lv[f];

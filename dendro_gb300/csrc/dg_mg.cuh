@@ -50,6 +50,8 @@ void mg_solve(Context &ctx, MG &mg, const double *b, double *x, int precision, d
 // building blocks (level operators), exposed for tests and callers
 template <typename T>
 void dirichlet_matvec(Context &ctx, const MGLevel &L, const T *x, T *y);  // DirichletJacobianMatMult
+// DirichletJacobianMatGetDiagonal (omgJac.C:1111): 1 on boundary nodes
+void dirichlet_diagonal(Context &ctx, const MGLevel &L, double *diag);
 template <typename T>
 void mg_restrict(Context &ctx, const MG &mg, int fine_level, const T *rf, T *bc);  // restrictMatVecType1
 template <typename T>

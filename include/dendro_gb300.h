@@ -237,6 +237,20 @@ int dg_da_free(dg_ctx ctx, dg_da da);
  * the -lapMatPropFac / -massMatPropFac options (odaJac.C:302-306). */
 int dg_matvec(dg_ctx ctx, dg_da da, const void *in, void *out, int precision, double lapFac, double massFac,
               int on_device);
+/* Per-element factors: coef holds 2 FP64 values per element (element i =
+ * octant i of the balanced octree): coef[2i] scales its Laplacian and
+ * coef[2i + 1] its mass; the operator of Jacobian2MatMult
+ * (examples/src/backend/omgJac.C:1666-1735, its matProp vector). coef and
+ * the vectors are all host or all device memory (on_device). */
+int dg_matvec_coef(dg_ctx ctx, dg_da da, const double *coef, const void *in, void *out, int precision, int on_device);
+/* Diagonals (FP64): dg_da_diagonal of lapFac K + massFac M, or of the
+ * per-element form when coef is given (Jacobian1MatGetDiagonal
+ * odaJac.C:160-222, Jacobian2MatGetDiagonal omgJac.C:1641); dg_mg_diagonal of
+ * a level's Dirichlet operator, 1 on boundary nodes
+ * (DirichletJacobianMatGetDiagonal omgJac.C:1111). */
+int dg_da_diagonal(dg_ctx ctx, dg_da da, const double *coef, double lapFac, double massFac, double *diag,
+                   int on_device);
+int dg_mg_diagonal(dg_ctx ctx, dg_mg mg, size_t level, double *diag, int on_device);
 
 /* ---- geometric multigrid (omg) ---------------------------------------------
  * The reference's DAMG hierarchy and solve for -lap(u) + u = f, u = 0 on the
@@ -292,6 +306,9 @@ int dg_mg_free(dg_ctx ctx, dg_mg mg);
  * device arrays.  dg_csr_spmv: y = A x (FP64). */
 int dg_da_assemble(dg_ctx ctx, dg_da da, double lapFac, double massFac, dg_csr *out);
 int dg_mg_assemble(dg_ctx ctx, dg_mg mg, size_t level, dg_csr *out);
+/* with per-element factors (coef as for dg_matvec_coef):
+ * BUILD_FULL_JAC_TYPE2_BLOCK (omgJac.C:1804-1858) */
+int dg_da_assemble_coef(dg_ctx ctx, dg_da da, const double *coef, int coef_on_device, dg_csr *out);
 int dg_csr_sizes(dg_csr a, size_t *n_rows, size_t *nnz, unsigned *max_row_len);
 int dg_csr_download(dg_ctx ctx, dg_csr a, int64_t *row_ptr, uint32_t *col, double *val, int dst_on_device);
 int dg_csr_spmv(dg_ctx ctx, dg_csr a, const double *x, double *y, int on_device);

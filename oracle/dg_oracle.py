@@ -259,7 +259,42 @@ class DA:
             pass
 
 
-def assemble(da: "DA", lap_fac: float = 1.0, mass_fac: float = 1.0, dirichlet: bool = False):
+def element_matrices(da: "DA", lap_fac: float = 1.0, mass_fac: float = 1.0, coef=None) -> np.ndarray:
+    """Per element the 8x8 (f1 L + f2 M) of odaJac.C:311-316 with
+    f1 = lap h/2, f2 = mass h^3/8, h = 2^-level; lap/mass are the given
+    factors or, with ``coef`` (n_elem x 2), each element's own
+    (Jacobian2's matProp, omgJac.C:1666-1673)."""
+    lap, mass = stencils()
+    h = 1.0 / np.exp2(da.level.astype(np.float64))
+    if coef is not None:
+        c = np.asarray(coef, np.float64).reshape(-1, 2)
+        lf, mf = c[:, 0], c[:, 1]
+    else:
+        lf, mf = lap_fac, mass_fac
+    f1 = lf * h / 2.0
+    f2 = mf * h * h * h / 8.0
+    return f1[:, None, None] * lap[da.child, da.etype] + f2[:, None, None] * mass[da.child, da.etype]
+
+
+def matvec_coef(da: "DA", coef, x: np.ndarray) -> np.ndarray:
+    """Jacobian2MatMult (examples/src/backend/omgJac.C:1666-1735) on the
+    oracle DA: y[idx[k]] += sum_j A_e[k][j] x[idx[j]]."""
+    a = element_matrices(da, coef=coef)
+    y = np.zeros(da.n_node)
+    np.add.at(y, da.nodes, np.einsum("ekj,ej->ek", a, np.asarray(x, np.float64)[da.nodes]))
+    return y
+
+
+def diagonal(da: "DA", lap_fac: float = 1.0, mass_fac: float = 1.0, coef=None) -> np.ndarray:
+    """Jacobian1MatGetDiagonal (odaJac.C:160-222) / Jacobian2MatGetDiagonal
+    (omgJac.C:1641): the element matrices' diagonals summed per node."""
+    a = element_matrices(da, lap_fac, mass_fac, coef)
+    d = np.zeros(da.n_node)
+    np.add.at(d, da.nodes, np.einsum("ekk->ek", a))
+    return d
+
+
+def assemble(da: "DA", lap_fac: float = 1.0, mass_fac: float = 1.0, dirichlet: bool = False, coef=None):
     """The assembled operator of the oracle DA as a scipy CSR matrix
     (duplicates summed): lap_fac K + mass_fac M, the records of
     CreateAndComputeFullJacobian1 (examples/src/backend/odaJac.C:470-535), or
@@ -268,13 +303,9 @@ def assemble(da: "DA", lap_fac: float = 1.0, mass_fac: float = 1.0, dirichlet: b
     identity on boundary rows)."""
     import scipy.sparse as sp
 
-    lap, mass = stencils()
     if dirichlet:
-        lap_fac = mass_fac = 1.0
-    h = 1.0 / np.exp2(da.level.astype(np.float64))
-    f1 = lap_fac * h / 2.0
-    f2 = mass_fac * h * h * h / 8.0
-    a = f1[:, None, None] * lap[da.child, da.etype] + f2[:, None, None] * mass[da.child, da.etype]
+        lap_fac, mass_fac, coef = 1.0, 1.0, None
+    a = element_matrices(da, lap_fac, mass_fac, coef)
     rows = np.broadcast_to(da.nodes[:, :, None], a.shape).ravel().astype(np.int64)
     cols = np.broadcast_to(da.nodes[:, None, :], a.shape).ravel().astype(np.int64)
     vals = a.ravel()

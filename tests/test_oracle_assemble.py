@@ -42,3 +42,18 @@ def test_oracle_matrix_is_the_matvec(oracle):
     x = np.random.Generator(np.random.PCG64(3)).uniform(-1, 1, da.n_node)
     np.testing.assert_allclose(oracle.assemble(da, 0.7, 1.3) @ x, da.matvec(x, 0.7, 1.3), rtol=0, atol=1e-12)
     np.testing.assert_allclose(oracle.assemble(da, dirichlet=True) @ x, da.dirichlet_matvec(x), rtol=0, atol=1e-12)
+
+
+def test_oracle_per_element_forms(oracle):
+    """The per-element (Jacobian2) restatement with every element's factors
+    equal to (a, b) is the C restatement of lapFac = a, massFac = b; its
+    diagonal is the diagonal of its matrix."""
+    z = np.load(os.path.join(GOLDEN, "ref_mat.npz"))
+    da = oracle.DA(z["bal"], 30)
+    x = np.random.Generator(np.random.PCG64(5)).uniform(-1, 1, da.n_node)
+    coef = np.tile([0.4, 2.5], (da.n_elem, 1))
+    np.testing.assert_allclose(oracle.matvec_coef(da, coef, x), da.matvec(x, 0.4, 2.5), rtol=0, atol=1e-13)
+    rc = np.random.Generator(np.random.PCG64(6)).uniform(0.1, 3.0, (da.n_elem, 2))
+    m = oracle.assemble(da, coef=rc)
+    np.testing.assert_allclose(m @ x, oracle.matvec_coef(da, rc, x), rtol=0, atol=1e-13)
+    np.testing.assert_allclose(m.diagonal(), oracle.diagonal(da, coef=rc), rtol=0, atol=1e-15)
