@@ -73,6 +73,7 @@ def _declare(L):
         "dg_balance_octree": ([P, P, I, I, PP], I),
         "dg_coarsen_octree": ([P, P, PP], I),
         "dg_complete_octree": ([P, P, SZ, U, I, I, I, PP], I),
+        "dg_sort_octants": ([P, P, SZ, U, I, I, P, I, ctypes.POINTER(SZ)], I),
         "dg_ctx_set_order": ([P, I], I),
         "dg_ctx_get_order": ([P, ctypes.POINTER(I)], I),
         "dg_octree_size": ([P, ctypes.POINTER(SZ), ctypes.POINTER(U)], I),

@@ -357,6 +357,18 @@ def coarsenOctree(octree: Octree) -> Octree:
     return Octree(ctx, h)
 
 
+def sortOctants(octants, maxDepth: int = 30, removeDuplicates: bool = False, ctx: Context | None = None) -> np.ndarray:
+    """par::sampleSort / par::removeDuplicates (include/parUtils.h:424,437)
+    of n x 4 uint32 octant records, in the context's octant order."""
+    ctx = ctx or default_context()
+    a = np.ascontiguousarray(octants, dtype=np.uint32).reshape(-1, 4)
+    out = np.empty((max(a.shape[0], 1), 4), np.uint32)
+    n = ctypes.c_size_t()
+    check(ctx.handle, ctx._L.dg_sort_octants(ctx.handle, _ptr(a), a.shape[0], maxDepth, int(removeDuplicates), 0,
+                                             _ptr(out), 0, ctypes.byref(n)), "sortOctants")
+    return out[: n.value]
+
+
 def completeOctree(octants, maxDepth: int = 30, isUnique: bool = False, isSorted: bool = False,
                    ctx: Context | None = None) -> Octree:
     """ot::completeOctree (src/construct.cpp:518) at one rank.  ``octants``:

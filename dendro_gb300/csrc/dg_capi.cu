@@ -399,6 +399,29 @@ int dg_octree_upload(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDep
   return DG_OK;
 }
 
+int dg_sort_octants(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDepth, int removeDuplicates,
+                    int src_on_device, uint32_t *out_xyzl, int dst_on_device, size_t *n_out) {
+  if ((!xyzl && n) || (!out_xyzl && n) || !n_out || maxDepth > 30) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() {
+    dg::Context &c = ctx->c;
+    dg::DBuf<uint32_t> hold;
+    const uint32_t *d = device_input(c, xyzl, 4 * n, src_on_device, hold);
+    dg::Octree o;
+    dg::sort_octants(c, d, n, maxDepth, removeDuplicates != 0, o);
+    dg::DBuf<dg::Key128> own;
+    own.adopt(o.keys, o.n, c.stream);  // freed on return
+    if (dst_on_device) {
+      dg::octree_to_xyzl(c, o, out_xyzl);
+    } else if (o.n) {
+      dg::DBuf<uint32_t> dx(4 * o.n, c.stream);
+      dg::octree_to_xyzl(c, o, dx.get());
+      copy_out(c, out_xyzl, dx.get(), 4 * o.n, 0);
+    }
+    DG_CUDA(cudaStreamSynchronize(c.stream));
+    *n_out = o.n;
+  });
+}
+
 int dg_complete_octree(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDepth, int isUnique, int isSorted,
                        int src_on_device, dg_octree *out) {
   if (!out || (!xyzl && n) || maxDepth > 30) return DG_ERR_INVALID_ARG;

@@ -1252,4 +1252,35 @@ void complete_octree(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned D,
   out.keys = res.release_ptr();
 }
 
+// par::sampleSort (include/parUtils.h:424; at one rank a local sort,
+// src/parUtils.tcc:1868-1875) and par::removeDuplicates (parUtils.h:437) of
+// octant records: sorted in the octant order (ancestor first on equal
+// anchors), repeated records removed when asked.
+void sort_octants(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned D, bool unique, Octree &out) {
+  cudaStream_t s = ctx.stream;
+  out = Octree();
+  out.max_depth = D;
+  if (n == 0) return;
+  DBuf<Key128> a(n, s), b(n, s);
+  {
+    ProfScope _prof(ctx, "sort_octants_keys", (double)n * 48);
+    k_from_xyzl<<<grid_for(n, 256), 256, 0, s>>>(reinterpret_cast<const uint4 *>(d_xyzl), n, D, b.get(),
+                                                 ctx.d_flags);
+    DG_LAUNCH_CHECK();
+    k_to_sortform<<<grid_for(n, 256), 256, 0, s>>>(b.get(), n, a.get());
+    DG_LAUNCH_CHECK();
+  }
+  check_device_flags(ctx, "sortOctants");
+  const int bits = 3 * (int)D + 5;
+  Key128 *srt = a.get();
+  size_t m = n;
+  if (unique) m = sort_unique<Key128>(ctx, a.get(), b.get(), n, bits, &srt);
+  else srt = radix_sort<Key128>(ctx, a.get(), b.get(), n, bits);
+  DBuf<Key128> res(m, s);
+  k_from_sortform<<<grid_for(m, 256), 256, 0, s>>>(srt, m, res.get());
+  DG_LAUNCH_CHECK();
+  out.n = m;
+  out.keys = res.release_ptr();
+}
+
 }  // namespace dg

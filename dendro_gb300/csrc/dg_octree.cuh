@@ -69,6 +69,10 @@ void coarsen_octree(Context &ctx, const Octree &in, Octree &out);
 void complete_octree(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned max_depth, bool is_unique,
                      bool is_sorted, Octree &out);
 
+// par::sampleSort / par::removeDuplicates (include/parUtils.h:424,437) of
+// n octant records at max_depth
+void sort_octants(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned max_depth, bool unique, Octree &out);
+
 // conversions between tagged keys and {x, y, z, level} u32 records
 void octree_to_xyzl(Context &ctx, const Octree &o, uint32_t *d_xyzl);
 void octree_from_xyzl(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned max_depth, Octree &out);

@@ -130,6 +130,13 @@ struct DBuf {
     n = 0;
     return q;
   }
+  // take ownership of a stream-ordered allocation
+  void adopt(T *q, size_t count, cudaStream_t stream) {
+    release();
+    p = q;
+    n = count;
+    s = stream;
+  }
 };
 
 inline unsigned grid_for(size_t n, unsigned block, unsigned max_blocks = 1u << 30) {

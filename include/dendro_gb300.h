@@ -155,6 +155,17 @@ int dg_balance_octree(dg_ctx ctx, dg_octree in, int incCorner, int comm_size, dg
  * replaced by its parent.  One cloud per call. */
 int dg_coarsen_octree(dg_ctx ctx, dg_octree in, dg_octree *out);
 
+/* ---- par::sampleSort / par::removeDuplicates of octants ---------------------
+ * include/parUtils.h:424,437 (at one rank a local sort, src/parUtils.tcc:
+ * 1868-1875): the n octant records xyzl ({x, y, z, level} at maxDepth) in
+ * the octant order of the context (Morton unless dg_ctx_set_order chose
+ * Hilbert; an ancestor before its descendants), repeated records removed
+ * when removeDuplicates is set.  out_xyzl holds n records; *n_out is the
+ * count written.  Records outside the domain or not aligned to their level:
+ * DG_ERR_DOMAIN. */
+int dg_sort_octants(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDepth, int removeDuplicates,
+                    int src_on_device, uint32_t *out_xyzl, int dst_on_device, size_t *n_out);
+
 /* ---- ot::completeOctree ----------------------------------------------------
  * include/octUtils.h:813 / src/construct.cpp:518 at one rank: the n octants
  * xyzl ({x, y, z, level} records at maxDepth, host or device memory) are

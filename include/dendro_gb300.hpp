@@ -218,6 +218,43 @@ class DA {
 };
 
 }  // namespace ot
+
+namespace par {
+
+// par::sampleSort (include/parUtils.h:424) at one rank: out = in sorted in
+// the octant order (in is left unchanged).
+template <class TN>
+int sampleSort(std::vector<TN> &in, std::vector<TN> &out, int /*comm_size*/ = 1) {
+  if (in.empty()) {
+    out.clear();
+    return 1;
+  }
+  dg_ctx c = cxx::context();
+  const unsigned maxDepth = in[0].getMaxDepth();
+  std::vector<uint32_t> r = cxx::nodes_to_records(in), o(r.size());
+  size_t n = 0;
+  cxx::check(c, dg_sort_octants(c, r.data(), in.size(), maxDepth, 0, 0, o.data(), 0, &n), "sampleSort");
+  o.resize(4 * n);
+  cxx::records_to_nodes(o, maxDepth, out);
+  return 1;
+}
+
+// par::removeDuplicates (include/parUtils.h:437) at one rank: sorted, repeated
+// octants removed, in place.
+template <class TN>
+int removeDuplicates(std::vector<TN> &v, bool /*isSorted*/, int /*comm_size*/ = 1) {
+  if (v.empty()) return 1;
+  dg_ctx c = cxx::context();
+  const unsigned maxDepth = v[0].getMaxDepth();
+  std::vector<uint32_t> r = cxx::nodes_to_records(v), o(r.size());
+  size_t n = 0;
+  cxx::check(c, dg_sort_octants(c, r.data(), v.size(), maxDepth, 1, 0, o.data(), 0, &n), "removeDuplicates");
+  o.resize(4 * n);
+  cxx::records_to_nodes(o, maxDepth, v);
+  return 1;
+}
+
+}  // namespace par
 }  // namespace dg
 
 #endif

@@ -12,9 +12,10 @@
 #include "dendro_gb300.hpp"
 
 struct MyNode {
-  unsigned x, y, z, lev;
-  MyNode(unsigned x_, unsigned y_, unsigned z_, unsigned l_, unsigned /*dim*/, unsigned /*maxDepth*/)
-      : x(x_), y(y_), z(z_), lev(l_) {}
+  unsigned x, y, z, lev, md;
+  MyNode(unsigned x_, unsigned y_, unsigned z_, unsigned l_, unsigned /*dim*/, unsigned maxDepth)
+      : x(x_), y(y_), z(z_), lev(l_), md(maxDepth) {}
+  unsigned getMaxDepth() const { return md; }
   unsigned getX() const { return x; }
   unsigned getY() const { return y; }
   unsigned getZ() const { return z; }
@@ -53,13 +54,26 @@ int main(int argc, char **argv) {
   for (size_t i = 0; i < bal.size(); i += 5) sub.push_back(bal[bal.size() - 1 - i]);
   dg::ot::completeOctree(sub, comp, 3, 30, false, false);
   dg::ot::completeOctree(bal, same, 3, 30, true, true);
+  // par::sampleSort of the reversed subset gives it back in order;
+  // par::removeDuplicates of it twice over keeps one copy of each
+  std::vector<MyNode> srt, dup = sub;
+  dg::par::sampleSort(sub, srt);
+  bool sort_ok = srt.size() == sub.size();
+  for (size_t i = 0; sort_ok && i < srt.size(); i++) {
+    const MyNode &a = srt[i], &b = sub[sub.size() - 1 - i];
+    sort_ok = a.x == b.x && a.y == b.y && a.z == b.z && a.lev == b.lev;
+  }
+  dup.insert(dup.end(), sub.begin(), sub.end());
+  dg::par::removeDuplicates(dup, false);
+  sort_ok = sort_ok && dup.size() == sub.size();
   bool same_ok = same.size() == bal.size();
   for (size_t i = 0; same_ok && i < bal.size(); i++)
     same_ok = same[i].x == bal[i].x && same[i].y == bal[i].y && same[i].z == bal[i].z && same[i].lev == bal[i].lev;
   // sum of the mass matrix applied to ones = volume of the unit cube
   std::printf("{\"n_lin\": %zu, \"n_bal\": %zu, \"n_elem\": %u, \"n_node\": %u, \"sum_A1\": %.15f, "
-              "\"n_coarse\": %zu, \"n_complete_sub\": %zu, \"complete_bal_same\": %d}\n",
-              nlin, bal.size(), da.getElementSize(), da.getNodeSize(), s, coarse.size(), comp.size(), same_ok ? 1 : 0);
+              "\"n_coarse\": %zu, \"n_complete_sub\": %zu, \"complete_bal_same\": %d, \"sort_ok\": %d}\n",
+              nlin, bal.size(), da.getElementSize(), da.getNodeSize(), s, coarse.size(), comp.size(), same_ok ? 1 : 0,
+              sort_ok ? 1 : 0);
   // error path: a communicator of size 2 is refused
   try {
     std::vector<double> p2 = {0.5, 0.5, 0.5, 0.25, 0.25, 0.25};

@@ -74,3 +74,25 @@ def test_edge_and_error_cases(ctx):
     assert e.value.status == DG_ERR_INVALID_ARG
     # the context stays usable after the errors
     assert completeOctree(unsorted, 4, ctx=ctx).size == 8
+
+
+def test_sort_octants(ctx, oracle):
+    """par::sampleSort / par::removeDuplicates of octant records: the
+    oracle's Morton order (repeats kept or removed), and the Hilbert order
+    on a Hilbert context."""
+    from dendro_gb300 import Context, sortOctants
+
+    rng = np.random.Generator(np.random.PCG64(31))
+    octs = cases.sparse_octants(rng, 30, 7, keep=0.3, n_anc=40, n_dup=500)
+    uniq = cases.morton_sort(octs, 30)
+    assert np.array_equal(sortOctants(octs, 30, True, ctx=ctx), uniq)
+    got = sortOctants(octs, 30, False, ctx=ctx)
+    assert len(got) == len(octs)
+    assert np.array_equal(np.unique(got, axis=0), np.unique(octs, axis=0))
+    assert np.array_equal(got[np.r_[True, np.any(got[1:] != got[:-1], axis=1)]], uniq)
+    h = Context(0)
+    try:
+        h.set_order("hilbert")
+        assert np.array_equal(sortOctants(octs, 30, True, ctx=h), oracle.hilbert_sort(uniq, 30))
+    finally:
+        h.close()

@@ -40,3 +40,4 @@ def test_cpp_dropin(oracle, tmp_path):
     sub = ref[::-1][::5]
     assert info["n_complete_sub"] == len(oracle.complete(sub, 30, 0, 0))
     assert info["complete_bal_same"] == 1
+    assert info["sort_ok"] == 1
