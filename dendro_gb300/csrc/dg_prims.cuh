@@ -445,21 +445,34 @@ __global__ void __launch_bounds__(RS_BLOCK, 4) k_rs_onesweep(const K *__restrict
       st_relaxed(my, OS_FLAG_INCL | (uint64_t)run);
     } else {
       st_relaxed(my, OS_FLAG_AGG | (uint64_t)run);
+      // look back four predecessors per round trip: their words are read
+      // together, then summed newest first until an inclusive one; a word
+      // not yet published is waited for (bounded) and the walk resumes there
       long t = (long)tile - 1;
       unsigned spins = 0;
       while (t >= 0) {
-        uint64_t v = ld_relaxed(status + (size_t)t * 256 + dg);
-        if ((v & ~OS_VALUE) == 0) {
+        uint64_t v[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) v[q] = (t - q >= 0) ? ld_relaxed(status + (size_t)(t - q) * 256 + dg) : 0;
+        int q = 0;
+        bool done = false;
+        for (; q < 4 && t - q >= 0; q++) {
+          if ((v[q] & ~OS_VALUE) == 0) break;
+          excl += v[q] & OS_VALUE;
+          if (v[q] & OS_FLAG_INCL) {
+            done = true;
+            break;
+          }
+        }
+        if (done) break;
+        t -= q;
+        if (q < 4 && t >= 0) {  // tile t has not published yet
           if (++spins > OS_SPIN_LIMIT) {
             atomicOr(flags, DGF_TIMEOUT);
             break;
           }
           __nanosleep(32);
-          continue;
         }
-        excl += v & OS_VALUE;
-        if (v & OS_FLAG_INCL) break;
-        t--;
       }
       st_relaxed(my, OS_FLAG_INCL | (excl + run));
     }
