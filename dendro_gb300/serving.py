@@ -1,6 +1,6 @@
 """Serving of octree + Poisson requests on one GPU, with continuous batching.
 
-A request carries one point cloud.  Its work is the spec request:
+A request carries one point cloud.  Its work is the full request of the serving workload:
 points2Octree -> balanceOctree -> mesh -> multigrid set-up -> CG with an
 FP32 V-cycle (FP64 residuals), at most ``solve_maxit`` iterations.
 
