@@ -142,6 +142,25 @@ def _dist():
     return ws, rank, local
 
 
+def max_over_ranks(vals, device) -> list:
+    """The element-wise maximum of vals over all ranks (the slowest
+    replica's times); vals unchanged at one rank."""
+    import torch
+    import torch.distributed as dist
+
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return [float(v) for v in vals]
+    t = torch.tensor([float(v) for v in vals], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def replica_value(ws: int, points_per_replica: int, ms: float) -> float:
+    """Whole-job Mpts/s of ws replicas that each served points_per_replica
+    points, over the slowest replica's time."""
+    return ws * points_per_replica / (ms * 1e-3) / 1e6
+
+
 def _top_kernels(stats: dict, k: int = 10) -> dict:
     """{kernel: [total ms, launches]} of the k kernels with the most time."""
     top = sorted(stats.items(), key=lambda kv: -kv[1][0])[:k]
@@ -722,12 +741,8 @@ def run_ours(args):
     ms = serve["ms_per_step"]
     e2e_ms = serve["e2e_ms"]
     if ws > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([ms, e2e_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, e2e_ms = float(t[0]), float(t[1])
-    value = ws * serve["points"] / (ms * 1e-3) / 1e6
+        ms, e2e_ms = max_over_ranks([ms, e2e_ms], f"cuda:{local}")
+    value = replica_value(ws, serve["points"], ms)
     extra = {}
     if not args.skip_scale:
         extra["scale"] = run_scale(args, dg, ctx, local)
@@ -778,7 +793,7 @@ def run_ours(args):
             "solve_iterations_max": serve["iterations_max"],
             "solve_relres_max": serve["relres_max"],
             "request_errors": serve["errors"],
-            "e2e": {"value": ws * serve["points"] / (e2e_ms * 1e-3) / 1e6, "unit": "Mpts/s",
+            "e2e": {"value": replica_value(ws, serve["points"], e2e_ms), "unit": "Mpts/s",
                     "h2d_bytes_per_step": 24 * serve["points"], "d2h_bytes_per_step": 24 * serve["requests"]},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": tname, "achieved": achieved, "peak": peak, "unit": "GB/s",
