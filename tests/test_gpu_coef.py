@@ -83,3 +83,24 @@ def test_mg_diagonal(ctx, oracle):
         oda = oracle.DA(mg.level_octree(l), 30)
         p = _perm(mg.level_nodes(l), oda.node_xyz)
         _close(mg.diagonal(l)[p], oda.dirichlet_diag(), 1e-12)
+
+
+def test_single_element_mesh(ctx, oracle):
+    """The root octree: one element, eight nodes, a dense 8 x 8 matrix."""
+    from dendro_gb300 import Octree
+
+    root = np.array([[0, 0, 0, 0]], np.uint32)
+    da = DA(Octree.from_numpy(root, 30, ctx=ctx))
+    assert (da.n_elem, da.n_node) == (1, 8)
+    oda = oracle.DA(root, 30)
+    p = _perm(da.download()["node_xyz"], oda.node_xyz)
+    csr = da.assemble(1.0, 1.0)
+    assert csr.nnz == 64 and csr.max_row_len == 8
+    g = csr.to_scipy()[p][:, p].toarray()
+    _close(g, oracle.assemble(oda).toarray(), 1e-12)
+    x = np.linspace(-1, 1, 8)
+    _close(csr.spmv(x), da.matvec(x), 1e-12)
+    coef = np.array([[3.0, 0.5]])
+    xo = x[p]
+    _close(da.matvec_coef(coef, x)[p], oracle.matvec_coef(oda, coef, xo), 1e-12)
+    _close(da.diagonal(coef=coef)[p], oracle.diagonal(oda, coef=coef), 1e-12)
