@@ -696,11 +696,7 @@ static void mesh_patches(Context &ctx, Mesh &m) {
   }
   {
     ProfScope _prof(ctx, "da_patch_sort", (double)n * 8 * 14);
-    static std::once_flag once;
-    std::call_once(once, []() {
-      DG_CUDA(cudaFuncSetAttribute(k_patch_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)sizeof(PatchSortSmem)));
-    });
+    ensure_smem_attr(ctx, k_patch_sort, (int)sizeof(PatchSortSmem));
     k_patch_sort<<<(unsigned)np, PATCH, sizeof(PatchSortSmem), s>>>(m.conn, m.meta, n, pairs.get(), pinc.get(),
                                                                     pexc.get(), pmeta.get(), pkeys.get(),
                                                                     pkcount.get(), run_node.get(), n_run.get(),
@@ -829,10 +825,7 @@ void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, 
   cudaStream_t s = ctx.stream;
   DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
   const size_t smem = patch_smem<T>();
-  static std::once_flag once;
-  std::call_once(once, [&]() {
-    DG_CUDA(cudaFuncSetAttribute(k_patch_matvec<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  });
+  ensure_smem_attr(ctx, k_patch_matvec<T, false>, (int)smem);
   int per_sm = 1;
   DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_patch_matvec<T, false>, PATCH, smem));
   if (per_sm < 1) per_sm = 1;
@@ -859,11 +852,7 @@ void mesh_matvec_coef(Context &ctx, const Mesh &m, const double *coef, const T *
   cudaStream_t s = ctx.stream;
   DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
   const size_t smem = patch_smem<T>();
-  static std::once_flag once;
-  std::call_once(once, [&]() {
-    DG_CUDA(cudaFuncSetAttribute(k_patch_matvec<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-  });
+  ensure_smem_attr(ctx, k_patch_matvec<T, false, true>, (int)smem);
   int per_sm = 1;
   DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_patch_matvec<T, false, true>, PATCH, smem));
   if (per_sm < 1) per_sm = 1;

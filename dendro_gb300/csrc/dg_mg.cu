@@ -448,10 +448,7 @@ void dirichlet_matvec(Context &ctx, const MGLevel &L, const T *x, T *y) {
   const Mesh &m = L.mesh;
   DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
   const size_t smem = patch_smem<T>();
-  static std::once_flag once;
-  std::call_once(once, [&]() {
-    DG_CUDA(cudaFuncSetAttribute(k_patch_matvec<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  });
+  ensure_smem_attr(ctx, k_patch_matvec<T, true>, (int)smem);
   int per_sm = 1;
   DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_patch_matvec<T, true>, PATCH, smem));
   const unsigned grid = (unsigned)std::min<size_t>(m.n_patch, (size_t)std::max(per_sm, 1) * ctx.num_sms);

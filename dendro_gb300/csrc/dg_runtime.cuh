@@ -10,7 +10,10 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
+#include <set>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "dg_common.cuh"
@@ -138,6 +141,19 @@ struct DBuf {
     s = stream;
   }
 };
+
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per (device,
+// kernel): the attribute belongs to each device's context
+template <typename F>
+void ensure_smem_attr(const Context &ctx, F *kernel, int bytes) {
+  static std::mutex mu;
+  static std::set<std::pair<int, const void *>> done;
+  std::lock_guard<std::mutex> lk(mu);
+  const auto key = std::make_pair(ctx.device, reinterpret_cast<const void *>(kernel));
+  if (done.count(key)) return;
+  DG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  done.insert(key);
+}
 
 inline unsigned grid_for(size_t n, unsigned block, unsigned max_blocks = 1u << 30) {
   size_t g = (n + block - 1) / block;
