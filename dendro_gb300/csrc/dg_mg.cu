@@ -284,24 +284,31 @@ __global__ void __launch_bounds__(256) k_bgj_update(float *__restrict__ X, size_
   }
   __syncthreads();
   const int ty = tid / 16, tx = tid % 16;
-  float acc[4][4] = {};
+  // column pairs accumulate with the paired FMA (fma.rn.f32x2)
+  float2 acc[4][2];
+#pragma unroll
+  for (int r = 0; r < 4; r++) acc[r][0] = acc[r][1] = make_float2(0.f, 0.f);
   for (int m = 0; m < b; m++) {
     const float4 a = *reinterpret_cast<const float4 *>(&Ut[m][ty * 4]);
     const float4 c4 = *reinterpret_cast<const float4 *>(&Bs[m][tx * 4]);
-    const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {c4.x, c4.y, c4.z, c4.w};
+    const float av[4] = {a.x, a.y, a.z, a.w};
+    const float2 b01 = make_float2(c4.x, c4.y), b23 = make_float2(c4.z, c4.w);
 #pragma unroll
-    for (int r = 0; r < 4; r++)
-#pragma unroll
-      for (int c = 0; c < 4; c++) acc[r][c] = fmaf(av[r], bv[c], acc[r][c]);
+    for (int r = 0; r < 4; r++) {
+      const float2 ar = make_float2(av[r], av[r]);
+      acc[r][0] = ffma2(ar, b01, acc[r][0]);
+      acc[r][1] = ffma2(ar, b23, acc[r][1]);
+    }
   }
 #pragma unroll
   for (int r = 0; r < 4; r++) {
     const size_t i = i0 + ty * 4 + r;
     if (i >= n || (i >= k0 && i < k0 + (size_t)b)) continue;
+    const float accr[4] = {acc[r][0].x, acc[r][0].y, acc[r][1].x, acc[r][1].y};
 #pragma unroll
     for (int c = 0; c < 4; c++) {
       const size_t j = j0 + tx * 4 + c;
-      if (j < n && !(j >= k0 && j < k0 + (size_t)b)) X[i * n + j] -= acc[r][c];
+      if (j < n && !(j >= k0 && j < k0 + (size_t)b)) X[i * n + j] -= accr[c];
     }
   }
 }
