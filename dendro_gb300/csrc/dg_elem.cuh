@@ -164,20 +164,21 @@ __device__ __forceinline__ void apply_comb(const double *__restrict__ S, const d
 // Dirichlet form: boundary rows are the identity (y = x), boundary columns
 // are dropped.  One block of PATCH threads per patch, grid-strided; thread t
 // holds pairs 8t..8t+7 of the patch's table and is element t of the patch.
-// In FP32 the slot buffer and the run-node array are double-buffered by
-// patch parity, so a patch costs three barriers; in FP64 they are single
-// (one more barrier per patch) so that two blocks fit an SM and one block's
-// FP64 stencil phase overlaps the other's gathers and sums.  The next
-// patch's table words are loaded one patch ahead.
+// The slot buffer and the run-node array are single (a patch costs four
+// barriers) so that more blocks fit an SM: three in FP32 (40 registers per
+// thread), two in FP64; one block's gathers and sums overlap another's
+// stencil phase.  (Double-buffering them by patch parity saves a barrier
+// but halves the blocks; measured slower.)  The next patch's table words are
+// loaded one patch ahead.
 template <typename T>
 constexpr int patch_nbuf() {
-  return sizeof(T) == 4 ? 2 : 1;
+  return 1;
 }
 
 // With COEF, element e's factors are coef[2e] (Laplacian) and coef[2e + 1]
 // (mass) instead of lapf and massf (pperm gives e from the patch order).
 template <typename T, bool DIR, bool COEF = false>
-__global__ void __launch_bounds__(PATCH, 2)
+__global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
     k_patch_matvec(const uint32_t *__restrict__ pmeta, const uint16_t *__restrict__ pinc,
                    const uint16_t *__restrict__ pexc, const uint32_t *__restrict__ pnode,
                    const uint64_t *__restrict__ poff, const uint16_t *__restrict__ pkeys,
