@@ -48,6 +48,22 @@ def test_invalid_arguments_rejected_before_any_gpu_work():
     assert L.dg_points_to_octree(None, None, 0, None, 30, 1, 1, 0, ctypes.byref(out)) == 1
     assert L.dg_points_to_octree(None, None, 0, (ctypes.c_double * 3)(1, 1, 1), 30, 1, 2, 0, ctypes.byref(out)) == 8
     assert L.dg_matvec(None, None, None, None, 64, 1.0, 1.0, 0) == 1
+    # the entry points beside the hot path check their arguments the same way
+    rec = (ctypes.c_uint32 * 4)(0, 0, 0, 0)
+    n = ctypes.c_size_t()
+    assert L.dg_complete_octree(None, rec, 1, 30, 0, 0, 0, None) == 1          # no output handle
+    assert L.dg_complete_octree(None, rec, 1, 31, 0, 0, 0, ctypes.byref(out)) == 1  # maxDepth > 30
+    assert L.dg_sort_octants(None, rec, 1, 30, 0, 0, None, 0, ctypes.byref(n)) == 1
+    assert L.dg_da_assemble(None, None, 1.0, 1.0, ctypes.byref(out)) == 1
+    assert L.dg_mg_assemble(None, None, 0, ctypes.byref(out)) == 1
+    assert L.dg_csr_sizes(None, None, None, None) == 1
+    assert L.dg_csr_free(None, None) == 0
+    assert L.dg_matvec_coef(None, None, None, None, None, 64, 0) == 1
+    assert L.dg_da_diagonal(None, None, None, 1.0, 1.0, None, 0) == 1
+    assert L.dg_mg_diagonal(None, None, 0, None, 0) == 1
+    assert L.dg_da_memory(None, None) == 1
+    assert L.dg_ctx_set_order(None, 1) == 1
+    assert L.dg_da_build_ex(None, None, 1, ctypes.byref(out)) == 1
 
 
 def test_product_fails_loudly_without_gpu():
