@@ -210,6 +210,33 @@ class DA {
     out.resize(nn_);
     cxx::check(c_, dg_matvec(c_, da_, in.data(), out.data(), 32, lapFac, massFac, 0), "Jacobian1MatMult");
   }
+  // per-element factors, matProp[2e] (Laplacian) and matProp[2e + 1] (mass)
+  // of element e in octree order (Jacobian2MatMult)
+  void matVec(const std::vector<double> &matProp, const std::vector<double> &in, std::vector<double> &out) const {
+    if (matProp.size() != 2 * ne_) throw cxx::Error(DG_ERR_INVALID_ARG, "matProp must hold 2 values per element");
+    out.resize(nn_);
+    cxx::check(c_, dg_matvec_coef(c_, da_, matProp.data(), in.data(), out.data(), 64, 0), "Jacobian2MatMult");
+  }
+  // diagonal of lapFac L + massFac M (Jacobian1MatGetDiagonal)
+  void getDiagonal(std::vector<double> &diag, double lapFac = 1.0, double massFac = 1.0) const {
+    diag.resize(nn_);
+    cxx::check(c_, dg_da_diagonal(c_, da_, nullptr, lapFac, massFac, diag.data(), 0), "Jacobian1MatGetDiagonal");
+  }
+  // the assembled lapFac L + massFac M as CSR arrays over node ids
+  // (CreateAndComputeFullJacobian1)
+  void assemble(std::vector<int64_t> &rowPtr, std::vector<uint32_t> &col, std::vector<double> &val,
+                double lapFac = 1.0, double massFac = 1.0) const {
+    dg_csr a = nullptr;
+    cxx::check(c_, dg_da_assemble(c_, da_, lapFac, massFac, &a), "CreateAndComputeFullJacobian1");
+    size_t n = 0, nnz = 0;
+    dg_csr_sizes(a, &n, &nnz, nullptr);
+    rowPtr.resize(n + 1);
+    col.resize(nnz);
+    val.resize(nnz);
+    int st = dg_csr_download(c_, a, rowPtr.data(), col.data(), val.data(), 0);
+    dg_csr_free(c_, a);
+    cxx::check(c_, st, "dg_csr_download");
+  }
 
  private:
   dg_ctx c_ = nullptr;

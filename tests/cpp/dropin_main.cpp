@@ -4,6 +4,8 @@
 // balanceOctree -> DA -> matVec, writes the balanced octree as {x,y,z,level}
 // records and prints sizes; then coarsenOctree of the balanced octree and
 // completeOctree of every 5th balanced octant in reverse order.  Driven by tests/test_gpu_cpp_dropin.py.
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -49,6 +51,27 @@ int main(int argc, char **argv) {
     std::fwrite(r, 4, 4, g);
   }
   std::fclose(g);
+  // assembled matrix times ones = the matVec of ones; the diagonal is the
+  // matrix's; per-element factors (1, 1) give the plain operator
+  std::vector<int64_t> rp;
+  std::vector<uint32_t> col;
+  std::vector<double> val, diag, ones(da.getNodeSize(), 1.0), yc;
+  da.assemble(rp, col, val);
+  da.getDiagonal(diag);
+  da.matVec(std::vector<double>(2 * da.getElementSize(), 1.0), ones, yc);
+  double mat_err = 0, diag_err = 0, coef_err = 0, ymax = 0, dmax = 0;
+  for (double v : y) ymax = std::max(ymax, std::abs(v));
+  for (double v : diag) dmax = std::max(dmax, std::abs(v));
+  for (size_t r = 0; r + 1 < rp.size(); r++) {
+    double acc = 0, dv = 0;
+    for (int64_t q = rp[r]; q < rp[r + 1]; q++) {
+      acc += val[q];
+      if (col[q] == r) dv = val[q];
+    }
+    mat_err = std::max(mat_err, std::abs(acc - y[r]));
+    diag_err = std::max(diag_err, std::abs(dv - diag[r]));
+    coef_err = std::max(coef_err, std::abs(yc[r] - y[r]));
+  }
   std::vector<MyNode> coarse, sub, comp, same;
   dg::ot::coarsenOctree(bal, coarse, 3, 30);
   for (size_t i = 0; i < bal.size(); i += 5) sub.push_back(bal[bal.size() - 1 - i]);
@@ -71,9 +94,10 @@ int main(int argc, char **argv) {
     same_ok = same[i].x == bal[i].x && same[i].y == bal[i].y && same[i].z == bal[i].z && same[i].lev == bal[i].lev;
   // sum of the mass matrix applied to ones = volume of the unit cube
   std::printf("{\"n_lin\": %zu, \"n_bal\": %zu, \"n_elem\": %u, \"n_node\": %u, \"sum_A1\": %.15f, "
-              "\"n_coarse\": %zu, \"n_complete_sub\": %zu, \"complete_bal_same\": %d, \"sort_ok\": %d}\n",
+              "\"n_coarse\": %zu, \"n_complete_sub\": %zu, \"complete_bal_same\": %d, \"sort_ok\": %d, "
+              "\"mat_err\": %.3e, \"diag_err\": %.3e, \"coef_err\": %.3e}\n",
               nlin, bal.size(), da.getElementSize(), da.getNodeSize(), s, coarse.size(), comp.size(), same_ok ? 1 : 0,
-              sort_ok ? 1 : 0);
+              sort_ok ? 1 : 0, mat_err / ymax, diag_err / dmax, coef_err / ymax);
   // error path: a communicator of size 2 is refused
   try {
     std::vector<double> p2 = {0.5, 0.5, 0.5, 0.25, 0.25, 0.25};

@@ -41,3 +41,6 @@ def test_cpp_dropin(oracle, tmp_path):
     assert info["n_complete_sub"] == len(oracle.complete(sub, 30, 0, 0))
     assert info["complete_bal_same"] == 1
     assert info["sort_ok"] == 1
+    # A 1 from the CSR rows, the diagonal and the per-element form agree with
+    # the matVec, relative to the largest entry (FP64 rounding only)
+    assert info["mat_err"] < 1e-12 and info["diag_err"] < 1e-12 and info["coef_err"] < 1e-12
