@@ -652,8 +652,12 @@ def run_rows(args, dg, ctx, local):
     sub = rec[::3][torch.randperm((n + 2) // 3, device=dev, generator=g)].contiguous()
     out = dg.completeOctree(sub, 30, ctx=ctx)
     ms = best(lambda: dg.completeOctree(sub, 30, ctx=ctx))
+    peak, _ = _peaks()
+    io_bytes = 16.0 * (sub.shape[0] + out.size)  # records in + records out
     res["complete_octree"] = {"input_octants": sub.shape[0], "output_octants": out.size, "ms": ms,
-                              "Mocts_per_s": sub.shape[0] / (ms * 1e-3) / 1e6}
+                              "Mocts_per_s": sub.shape[0] / (ms * 1e-3) / 1e6,
+                              "record_GB_per_s": io_bytes / (ms * 1e-3) / 1e9,
+                              "frac_of_measured_peak": io_bytes / (ms * 1e-3) / 1e9 / peak}
     out.free()
     del sub
 
@@ -663,7 +667,8 @@ def run_rows(args, dg, ctx, local):
     ms_h = best(lambda: bal.download_to(rec))
     ctx.set_order("morton")
     res["records_download"] = {"morton_ms": ms_m, "hilbert_ms": ms_h,
-                               "hilbert_Mocts_per_s": n / (ms_h * 1e-3) / 1e6}
+                               "hilbert_Mocts_per_s": n / (ms_h * 1e-3) / 1e6,
+                               "morton_GB_per_s": 32.0 * n / (ms_m * 1e-3) / 1e9}
     del rec
 
     # assembled K + M (odaJac.C:470) and SpMV vs the matrix-free element loop
@@ -674,9 +679,12 @@ def run_rows(args, dg, ctx, local):
     y = torch.empty_like(x)
     ms_spmv = best(lambda: csr.spmv(x, y))
     ms_mv = best(lambda: da.matvec(x, y))
+    spmv_bytes = 12.0 * csr.nnz + 8.0 * (csr.n_rows + 1) + 16.0 * csr.n_rows + 8.0 * csr.n_rows  # A, x, y
     res["assembly"] = {"n_elem": da.n_elem, "n_rows": csr.n_rows, "nnz": csr.nnz, "max_row_len": csr.max_row_len,
                        "assemble_ms": ms_a, "spmv_fp64_ms": ms_spmv, "matvec_fp64_ms": ms_mv,
-                       "csr_bytes_per_row": (12 * csr.nnz + 8 * (csr.n_rows + 1)) / csr.n_rows}
+                       "csr_bytes_per_row": (12 * csr.nnz + 8 * (csr.n_rows + 1)) / csr.n_rows,
+                       "spmv_GB_per_s": spmv_bytes / (ms_spmv * 1e-3) / 1e9,
+                       "spmv_frac_of_measured_peak": spmv_bytes / (ms_spmv * 1e-3) / 1e9 / peak}
     csr.free()
 
     # compressed DA (compressLut)
