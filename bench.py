@@ -679,7 +679,7 @@ def run_rows(args, dg, ctx, local):
     y = torch.empty_like(x)
     ms_spmv = best(lambda: csr.spmv(x, y))
     ms_mv = best(lambda: da.matvec(x, y))
-    spmv_bytes = 12.0 * csr.nnz + 8.0 * (csr.n_rows + 1) + 16.0 * csr.n_rows + 8.0 * csr.n_rows  # A, x, y
+    spmv_bytes = 12.0 * csr.nnz + 8.0 * (csr.n_rows + 1) + 16.0 * csr.n_rows  # A; x read and y written once
     res["assembly"] = {"n_elem": da.n_elem, "n_rows": csr.n_rows, "nnz": csr.nnz, "max_row_len": csr.max_row_len,
                        "assemble_ms": ms_a, "spmv_fp64_ms": ms_spmv, "matvec_fp64_ms": ms_mv,
                        "csr_bytes_per_row": (12 * csr.nnz + 8 * (csr.n_rows + 1)) / csr.n_rows,
