@@ -135,16 +135,27 @@ __global__ void k_row_fill(const uint64_t *__restrict__ key, const uint64_t *__r
   }
 }
 
+template <int LANES>
 __global__ void k_csr_spmv(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
                            const double *__restrict__ val, size_t n, const double *__restrict__ x,
                            double *__restrict__ y) {
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const size_t r = t >> 3;
-  const unsigned lane = threadIdx.x & 7u;
+  const size_t r = t / LANES;
+  const unsigned lane = threadIdx.x % LANES;
   double acc = 0.0;
-  if (r < n)
-    for (uint64_t p = rp[r] + lane; p < rp[r + 1]; p += 8) acc += val[p] * x[col[p]];
-  for (int o = 4; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, 8);
+  if (r < n) {
+    const uint64_t end = rp[r + 1];
+    uint64_t p = rp[r] + lane;
+    // two entries per lane per step: both gathers of x in flight together
+    for (; p + LANES < end; p += 2 * LANES) {
+      const uint32_t c0 = col[p], c1 = col[p + LANES];
+      const double v0 = val[p], v1 = val[p + LANES];
+      acc = fma(v0, __ldg(x + c0), acc);
+      acc = fma(v1, __ldg(x + c1), acc);
+    }
+    if (p < end) acc = fma(val[p], __ldg(x + col[p]), acc);
+  }
+  for (int o = LANES / 2; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, LANES);
   if (r < n && lane == 0) y[r] = acc;
 }
 
@@ -235,8 +246,9 @@ void csr_free(Context &ctx, Csr &c) {
 void csr_spmv(Context &ctx, const Csr &c, const double *x, double *y) {
   if (!c.n_rows) return;
   ProfScope _prof(ctx, "csr_spmv", (double)c.nnz * 12 + (double)c.n_rows * 24);
-  k_csr_spmv<<<grid_for(8 * c.n_rows, 256), 256, 0, ctx.stream>>>(reinterpret_cast<const uint64_t *>(c.row_ptr),
-                                                                   c.col, c.val, c.n_rows, x, y);
+  constexpr int LANES = 4;
+  k_csr_spmv<LANES><<<grid_for(LANES * c.n_rows, 256), 256, 0, ctx.stream>>>(
+      reinterpret_cast<const uint64_t *>(c.row_ptr), c.col, c.val, c.n_rows, x, y);
   DG_LAUNCH_CHECK();
 }
 

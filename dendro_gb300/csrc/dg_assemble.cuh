@@ -34,7 +34,7 @@ struct Csr {
 void assemble_csr(Context &ctx, const Mesh &m, const uint8_t *bdy, double lap_fac, double mass_fac, Csr &out,
                   const double *coef = nullptr);
 void csr_free(Context &ctx, Csr &c);
-// y = A x (FP64), rows split over groups of 8 lanes
+// y = A x (FP64), rows split over groups of 4 lanes
 void csr_spmv(Context &ctx, const Csr &c, const double *x, double *y);
 
 }  // namespace dg
