@@ -83,6 +83,9 @@ __global__ void k_row_count(const uint64_t *__restrict__ key, const uint64_t *__
   atomicMax(max_row, (unsigned)n);
 }
 
+// the row's sorted columns are rebuilt as in the count pass and written
+// out; each contribution then adds into its entry of the row's slice of val
+// (private to the thread, so no atomics), found by a search of the columns
 __global__ void k_row_fill(const uint64_t *__restrict__ key, const uint64_t *__restrict__ start, size_t V,
                            const uint32_t *__restrict__ meta, const uint32_t *__restrict__ conn, size_t E,
                            const uint8_t *__restrict__ bdy, const double *__restrict__ sten, double lap_fac,
@@ -96,10 +99,26 @@ __global__ void k_row_fill(const uint64_t *__restrict__ key, const uint64_t *__r
     val[out] = 1.0;
     return;
   }
-  uint32_t cols[ROW_MAX];
-  double vals[ROW_MAX];
-  int n = 0;
   const int cap = (int)(row_ptr[v + 1] - out);
+  uint32_t cols[ROW_MAX];
+  int n = 0;
+  for (uint64_t p = start[v]; p < start[v + 1]; p++) {
+    const size_t e = (uint32_t)key[p] >> 3;
+    for (int j = 0; j < 8; j++) {
+      const uint32_t c = conn[(size_t)j * E + e];
+      if (bdy && bdy[c]) continue;
+      const int pos = col_lower_bound(cols, n, c);
+      if (pos < n && cols[pos] == c) continue;
+      if (n == cap) return;  // cannot happen after the count pass
+      for (int q = n; q > pos; q--) cols[q] = cols[q - 1];
+      cols[pos] = c;
+      n++;
+    }
+  }
+  for (int q = 0; q < n; q++) {
+    col[out + q] = cols[q];
+    val[out + q] = 0.0;
+  }
   for (uint64_t p = start[v]; p < start[v + 1]; p++) {
     const uint32_t ek = (uint32_t)key[p];
     const size_t e = ek >> 3;
@@ -113,25 +132,8 @@ __global__ void k_row_fill(const uint64_t *__restrict__ key, const uint64_t *__r
     for (int j = 0; j < 8; j++) {
       const uint32_t cj = conn[(size_t)j * E + e];
       if (bdy && bdy[cj]) continue;
-      const double a = f1 * S[j] + f2 * S[64 + j];
-      const int pos = col_lower_bound(cols, n, cj);
-      if (pos < n && cols[pos] == cj) {
-        vals[pos] += a;
-        continue;
-      }
-      if (n == cap) return;  // cannot happen after the count pass
-      for (int q = n; q > pos; q--) {
-        cols[q] = cols[q - 1];
-        vals[q] = vals[q - 1];
-      }
-      cols[pos] = cj;
-      vals[pos] = a;
-      n++;
+      val[out + col_lower_bound(cols, n, cj)] += f1 * S[j] + f2 * S[64 + j];
     }
-  }
-  for (int q = 0; q < n; q++) {
-    col[out + q] = cols[q];
-    val[out + q] = vals[q];
   }
 }
 
