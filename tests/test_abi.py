@@ -89,3 +89,22 @@ def test_no_oracle_in_product_sources():
             if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
                 text = open(os.path.join(dirpath, f)).read()
                 assert "oracle" not in text.replace("the oracle", ""), f
+
+
+def test_header_is_c99_and_a_c_caller_links(tmp_path):
+    """include/dendro_gb300.h compiles as plain C99; a C program links the
+    library and calls its context-free entry points (no GPU needed)."""
+    import shutil
+    import subprocess
+
+    if not shutil.which("gcc"):
+        pytest.skip("no C compiler")
+    lib = _lib.load()._name
+    exe = tmp_path / "abi_smoke"
+    subprocess.check_call(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                           os.path.join(ROOT, "tests", "c", "abi_smoke.c"), "-o", str(exe), lib,
+                           "-Wl,-rpath," + os.path.dirname(lib)])
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, (r.returncode, r.stderr)
+    assert '"version"' in r.stdout
+
