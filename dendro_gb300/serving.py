@@ -62,6 +62,25 @@ def estimate_bytes(npts: int) -> int:
     return int(npts * (24 + 3.4 * 32 + 5.6 * 16 + 5.6 * 40 + 5.6 * 80)) + (64 << 20)
 
 
+def admit(waiting: list, in_flight: int, budget: int, max_batch_points: int):
+    """The next batch from the head of ``waiting`` (removed from it, in
+    arrival order): requests join while the estimated bytes in flight stay
+    within ``budget`` and the batch within ``max_batch_points`` points; a
+    request that alone exceeds the budget is admitted when nothing else is in
+    flight.  Returns ([(request, bytes)], new bytes in flight)."""
+    batch, npts = [], 0
+    while waiting:
+        n = len(waiting[0].points)
+        need = estimate_bytes(n)
+        fits = in_flight + need <= budget or (not batch and in_flight == 0)
+        if not fits or (batch and npts + n > max_batch_points):
+            break
+        batch.append((waiting.pop(0), need))
+        in_flight += need
+        npts += n
+    return batch, in_flight
+
+
 def poisson_stream(count: int, rate: float = 200.0, lo: float = 1e4, hi: float = 8e6, seed: int = 4) -> list:
     """Poisson arrivals (mean ``rate``/s), sizes log-uniform in [lo, hi],
     half Gaussian-mixture clouds and half log-normal clouds."""
@@ -218,18 +237,11 @@ class BatchingServer:
                     break
                 continue
             # admission by the HBM budget, in arrival order
-            batch, npts = [], 0
             with self.cv:
-                while waiting:
-                    need = estimate_bytes(len(waiting[0].points))
-                    fits = self.in_flight + need <= self.budget or (not batch and self.in_flight == 0)
-                    if not fits or (batch and npts + len(waiting[0].points) > self.max_batch_points):
-                        break
-                    r = waiting.pop(0)
-                    self.in_flight += need
-                    r.t_admit = time.perf_counter() - t0
-                    batch.append((r, need))
-                    npts += len(r.points)
+                batch, self.in_flight = admit(waiting, self.in_flight, self.budget, self.max_batch_points)
+                now = time.perf_counter() - t0
+                for r, _ in batch:
+                    r.t_admit = now
                 if not batch:
                     self.cv.wait(timeout=0.05)
                     continue
