@@ -108,3 +108,15 @@ def test_header_is_c99_and_a_c_caller_links(tmp_path):
     assert r.returncode == 0, (r.returncode, r.stderr)
     assert '"version"' in r.stdout
 
+
+def test_cpp_mirror_compiles_cleanly():
+    """include/dendro_gb300.hpp with a C++ caller (tests/cpp/dropin_main.cpp):
+    no warnings at -Wall -Wextra (compile only; the GPU test runs it)."""
+    import shutil
+    import subprocess
+
+    if not shutil.which("g++"):
+        pytest.skip("no C++ compiler")
+    subprocess.check_call(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I",
+                           os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "dropin_main.cpp")])
+
