@@ -382,17 +382,13 @@ __global__ void k_mesh_conn(const Key128 *__restrict__ keys, size_t n, const uin
 }
 
 // ------------------------------------------------------------------------
-// element loop tables: per patch, the (element, vertex) pairs sorted by node
+// element loop tables: per patch, the (element, vertex) pairs grouped by node
 // ------------------------------------------------------------------------
 __global__ void k_node_incidence(const uint32_t *__restrict__ conn, size_t n8, uint32_t *__restrict__ cnt) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += stride) atomicAdd(&cnt[conn[i]], 1u);
 }
 
-// one block per patch: the patch's elements ordered by (type, level, index),
-// then a bitonic sort of its (node << 12 | slot) keys in shared memory, run
-// starts, run lengths against the node's mesh-wide pair count, and the
-// packed entries
 // Bitonic sort of BLOCK * I keys held I per thread (key I*t + j in v[j] of
 // thread t), ascending.  Compare-exchanges with partners in the same thread
 // run in registers, those within a warp by shuffles, and only the strides
