@@ -59,13 +59,25 @@ SERVE_SIZES = (1e4, 8e6)
 SERVE_SEED = 4
 SOLVE_MAXIT = 50
 REF_MAX_POINTS = 40_000  # reference arm: requests of the stream up to this size
-# DRAM bytes per algorithmic byte, from one ncu capture of each kernel
-# (profiles/ncu_patch_matvec_fp32_and_onesweep.md): 774.6 MB for a
-# 2.20e7-element / 1.48e7-node Dirichlet FP32 launch (36 E + 12 V = 969.0 MB
-# algorithmic), 485.2 MB for a 1.6e7-key onesweep pass (512 MB); the traffic
-# grows with the elements / keys a launch processes, so the ratio scales it
-# to the bench's average launch
-TRAFFIC_PER_ALG_BYTE = {"dirichlet_matvec_fp32": 774.6 / 969.0, "rs_onesweep": 485.2 / 512.0}
+
+
+def _traffic_ratios() -> dict:
+    """DRAM bytes per algorithmic byte of a kernel, from one ncu capture each
+    (profiles/dram_traffic.txt: name, DRAM bytes, algorithmic bytes).  The
+    traffic grows with the elements / keys a launch processes, so the ratio
+    scales it to the bench's average launch."""
+    out = {}
+    try:
+        for line in open(os.path.join(ROOT, "profiles", "dram_traffic.txt")):
+            f = line.split()
+            if f and not line.startswith("#") and len(f) >= 3:
+                out[f[0]] = float(f[1]) / float(f[2])
+    except OSError:
+        pass
+    return out
+
+
+TRAFFIC_PER_ALG_BYTE = _traffic_ratios()
 
 
 def _peaks():
@@ -533,9 +545,8 @@ def run_batching(args, dg, ctx, local):
 
     from dendro_gb300 import datagen
 
-    sizes = datagen.cloud_sizes(args.batch_clouds, 1e4, 4e6, seed=2)
-    rng = np.random.Generator(np.random.PCG64(2))
-    clouds = [datagen.mixture(int(n), rng) for n in sizes]
+    clouds = datagen.batch_clouds(args.batch_clouds)
+    sizes = np.array([len(c) for c in clouds], np.int64)
     seg = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
     dev = torch.from_numpy(np.concatenate(clouds)).to(f"cuda:{local}")
     del clouds

@@ -6,11 +6,11 @@ C ABI of include/dendro_gb300.h.
 """
 from .api import (DA, Context, Csr, DendroError, MultiGrid, Octree, balanceOctree, coarsenOctree, completeOctree,
                   default_context, points2Octree, points2OctreeBatch, readNodesFromFile, readNodesFromFile_binary,
-                  readPtsFromFile, sortOctants, sortUniquePoints, writeNodesToFile, writeNodesToFile_binary, writePtsToFile)
+                  readPtsFromFile, sortOctants, sortUniquePoints, treeSort, writeNodesToFile, writeNodesToFile_binary, writePtsToFile)
 
 __all__ = [
     "DA", "Context", "Csr", "DendroError", "MultiGrid", "Octree", "balanceOctree", "coarsenOctree", "completeOctree",
     "default_context", "points2Octree", "points2OctreeBatch",
-    "sortUniquePoints", "sortOctants", "readPtsFromFile", "writePtsToFile", "readNodesFromFile", "writeNodesToFile",
+    "sortUniquePoints", "sortOctants", "treeSort", "readPtsFromFile", "writePtsToFile", "readNodesFromFile", "writeNodesToFile",
     "readNodesFromFile_binary", "writeNodesToFile_binary",
 ]

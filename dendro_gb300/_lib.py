@@ -28,6 +28,7 @@ STATUS = {
     7: "DG_ERR_INTERNAL",
     8: "DG_ERR_COMM_SIZE",
     9: "DG_ERR_UNSUPPORTED",
+    10: "DG_ERR_CAPACITY",
 }
 
 
@@ -116,6 +117,8 @@ def _declare(L):
         "dg_mg_rhs": ([P, P, P, P, I], I),
         "dg_mg_solve": ([P, P, P, P, I, D, I, I, ctypes.POINTER(I), ctypes.POINTER(D)], I),
         "dg_mg_free": ([P, P], I),
+        "dg_debug_lookback_timeout": ([P, SZ, U], I),
+        "dg_tree_sort": ([P, P, SZ, U, U, I, P, I, ctypes.POINTER(SZ)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -369,6 +369,24 @@ def sortOctants(octants, maxDepth: int = 30, removeDuplicates: bool = False, ctx
     return out[: n.value]
 
 
+TS_SORT_ONLY, TS_REMOVE_DUPLICATES, TS_CONSTRUCT_OCTREE, TS_BALANCE_OCTREE = 0, 1, 2, 4
+
+
+def treeSort(octants, maxDepth: int = 30, options: int = TS_REMOVE_DUPLICATES, ctx: Context | None = None) -> np.ndarray:
+    """SFC::parSort::SFC_treeSort (include/sfcSort.h:1378) at one rank on
+    n x 4 uint32 octant records: TS_SORT_ONLY sorts them (the reference's
+    pNodes, sorted in place); TS_REMOVE_DUPLICATES also removes repeated
+    octants and every octant with a descendant in the input (pOutSorted,
+    sfcSort.h:532-575).  Records come back in the context's octant order."""
+    ctx = ctx or default_context()
+    a = np.ascontiguousarray(octants, dtype=np.uint32).reshape(-1, 4)
+    out = np.empty((max(a.shape[0], 1), 4), np.uint32)
+    n = ctypes.c_size_t()
+    check(ctx.handle, ctx._L.dg_tree_sort(ctx.handle, _ptr(a), a.shape[0], maxDepth, int(options), 0, _ptr(out), 0,
+                                          ctypes.byref(n)), "SFC_treeSort")
+    return out[: n.value]
+
+
 def completeOctree(octants, maxDepth: int = 30, isUnique: bool = False, isSorted: bool = False,
                    ctx: Context | None = None) -> Octree:
     """ot::completeOctree (src/construct.cpp:518) at one rank.  ``octants``:

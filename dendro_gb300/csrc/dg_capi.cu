@@ -239,6 +239,10 @@ int dg_ctx_profile_entry(dg_ctx ctx, int index, char *name, size_t name_len, dou
   return DG_OK;
 }
 
+int dg_debug_lookback_timeout(dg_ctx ctx, size_t n_keys, unsigned skipped_tiles) {
+  return guarded(ctx, [&]() { dg::lookback_timeout_selftest(ctx->c, n_keys, skipped_tiles); });
+}
+
 int dg_points_to_octree(dg_ctx ctx, const double *xyz, size_t n, const double gLens[3], unsigned maxDepth,
                         unsigned maxNumPts, int comm_size, int xyz_on_device, dg_octree *out) {
   if (!out || (!xyz && n) || !gLens) return DG_ERR_INVALID_ARG;
@@ -331,14 +335,10 @@ int dg_sort_unique_points(dg_ctx ctx, const double *xyz, size_t n, const double 
 int dg_balance_octree(dg_ctx ctx, dg_octree in, int incCorner, int comm_size, dg_octree *out) {
   if (!in || !out) return DG_ERR_INVALID_ARG;
   if (comm_size != 1) return DG_ERR_COMM_SIZE;
-  if (!incCorner) {
-    if (ctx) ctx->c.last_error = "balanceOctree: only incCorner = true is implemented";
-    return DG_ERR_UNSUPPORTED;
-  }
   *out = nullptr;
   dg_octree h = new (std::nothrow) dg_octree_s();
   if (!h) return DG_ERR_OUT_OF_MEMORY;
-  int rc = guarded(ctx, [&]() { dg::balance_octree(ctx->c, in->o, h->o); });
+  int rc = guarded(ctx, [&]() { dg::balance_octree(ctx->c, in->o, h->o, incCorner != 0); });
   if (rc != DG_OK) {
     delete h;
     return rc;
@@ -407,7 +407,34 @@ int dg_sort_octants(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDept
     dg::DBuf<uint32_t> hold;
     const uint32_t *d = device_input(c, xyzl, 4 * n, src_on_device, hold);
     dg::Octree o;
-    dg::sort_octants(c, d, n, maxDepth, removeDuplicates != 0, o);
+    dg::sort_octants(c, d, n, maxDepth, removeDuplicates != 0 ? 1 : 0, o);
+    dg::DBuf<dg::Key128> own;
+    own.adopt(o.keys, o.n, c.stream);  // freed on return
+    if (dst_on_device) {
+      dg::octree_to_xyzl(c, o, out_xyzl);
+    } else if (o.n) {
+      dg::DBuf<uint32_t> dx(4 * o.n, c.stream);
+      dg::octree_to_xyzl(c, o, dx.get());
+      copy_out(c, out_xyzl, dx.get(), 4 * o.n, 0);
+    }
+    DG_CUDA(cudaStreamSynchronize(c.stream));
+    *n_out = o.n;
+  });
+}
+
+int dg_tree_sort(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDepth, unsigned options, int src_on_device,
+                 uint32_t *out_xyzl, int dst_on_device, size_t *n_out) {
+  if ((!xyzl && n) || (!out_xyzl && n) || !n_out || maxDepth > 30) return DG_ERR_INVALID_ARG;
+  if (options & (DG_TS_CONSTRUCT_OCTREE | DG_TS_BALANCE_OCTREE)) {
+    if (ctx) ctx->c.last_error = "SFC_treeSort: construct / balance options: use dg_complete_octree / dg_balance_octree";
+    return DG_ERR_UNSUPPORTED;
+  }
+  return guarded(ctx, [&]() {
+    dg::Context &c = ctx->c;
+    dg::DBuf<uint32_t> hold;
+    const uint32_t *d = device_input(c, xyzl, 4 * n, src_on_device, hold);
+    dg::Octree o;
+    dg::sort_octants(c, d, n, maxDepth, (options & DG_TS_REMOVE_DUPLICATES) ? 2 : 0, o);
     dg::DBuf<dg::Key128> own;
     own.adopt(o.keys, o.n, c.stream);  // freed on return
     if (dst_on_device) {

@@ -57,12 +57,31 @@ __device__ __align__(256) unsigned char g_na_scratch[NA_BYTES];
 
 constexpr int NA_MAX_DEVICES = 64;
 struct NaDevice {
-  std::once_flag once;
-  cudaError_t err = cudaSuccess;
+  std::mutex mu;
+  bool ready = false;  // set only once the set-up succeeded
   unsigned char *base = nullptr;
   int num_sms = 0;
 };
 NaDevice g_na_dev[NA_MAX_DEVICES];
+
+// The scratch address of device `dev` (current): looked up on the first
+// successful call there.  A failed look-up (for example a transient error
+// while the module loads) is not remembered: the next call tries again.
+bool na_setup(NaDevice &nd, int dev) {
+  std::lock_guard<std::mutex> lock(nd.mu);
+  if (nd.ready) return true;
+  unsigned char *base = nullptr;
+  int sms = 0;
+  if (cudaGetSymbolAddress((void **)&base, g_na_scratch) != cudaSuccess || !base ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  nd.base = base;
+  nd.num_sms = sms;
+  nd.ready = true;
+  return true;
+}
 
 // The quantisation rule of points2OctreeSeq (src/construct.cpp:930-942):
 // multiply by 2^D, divide by gLen, truncate; a point is valid iff the
@@ -152,11 +171,7 @@ extern "C" int dg_sort_unique_points_noalloc(const double *xyz, size_t n, const 
   if (dev < 0 || dev >= NA_MAX_DEVICES) return DG_ERR_UNSUPPORTED;
   NaDevice &nd = g_na_dev[dev];
   // set-up, once per device, with that device current
-  std::call_once(nd.once, [&nd, dev]() {
-    nd.err = cudaGetSymbolAddress((void **)&nd.base, g_na_scratch);
-    if (nd.err == cudaSuccess) nd.err = cudaDeviceGetAttribute(&nd.num_sms, cudaDevAttrMultiProcessorCount, dev);
-  });
-  if (nd.err != cudaSuccess || !nd.base) return DG_ERR_CUDA;
+  if (!na_setup(nd, dev)) return DG_ERR_CUDA;
   if (!device_pointer(xyz, dev) || !device_pointer(out_xyzl, dev)) return DG_ERR_INVALID_ARG;
 
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);

@@ -550,9 +550,14 @@ __global__ void k_leaf_parents(const Key128 *__restrict__ k, size_t n, unsigned 
 }
 
 // for q at level l: the 8 level-(l-1) parents of q's 3x3x3 block; parents
-// outside the domain are replaced by q's own parent (removed by the unique)
+// outside the domain are replaced by q's own parent (removed by the unique).
+// Without corners (balanceOctree's incCorner = false: faces and edges only,
+// the 18 directions of TreeNode::addBalancingDescendants,
+// src/TreeNode.cpp:160-190) the parent that only q's corner neighbours
+// reach (outward on all three axes) is replaced the same way.
 template <typename K>
-__global__ void k_block_parents(const Key128 *__restrict__ q, size_t nq, unsigned l, K *__restrict__ out) {
+__global__ void k_block_parents(const Key128 *__restrict__ q, size_t nq, unsigned l, bool inc_corner,
+                                K *__restrict__ out) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nq) return;
   const Key128 qi = q[i];
@@ -577,7 +582,7 @@ __global__ void k_block_parents(const Key128 *__restrict__ q, size_t nq, unsigne
 #pragma unroll
   for (int t = 0; t < 8; t++) {
     int64_t p0 = opt[0][t & 1], p1 = opt[1][(t >> 1) & 1], p2 = opt[2][(t >> 2) & 1];
-    if (p0 < 0 || p1 < 0 || p2 < 0 || p0 >= side || p1 >= side || p2 >= side) {
+    if (p0 < 0 || p1 < 0 || p2 < 0 || p0 >= side || p1 >= side || p2 >= side || (t == 7 && !inc_corner)) {
       p0 = opt[0][0];
       p1 = opt[1][0];
       p2 = opt[2][0];
@@ -683,7 +688,7 @@ __global__ void k_place(const Key128 *__restrict__ Ip, size_t np, unsigned l, un
   }
 }
 
-void balance_octree(Context &ctx, const Octree &in, Octree &out) {
+void balance_octree(Context &ctx, const Octree &in, Octree &out, bool inc_corner) {
   cudaStream_t s = ctx.stream;
   const unsigned D = in.max_depth;
   const size_t nseg = in.nseg;
@@ -750,7 +755,7 @@ void balance_octree(Context &ctx, const Octree &in, Octree &out) {
       }
       if (nq) {
         ProfScope _prof(ctx, "bal_block_parents", (double)nq * 80);
-        k_block_parents<uint64_t><<<grid_for(nq, 256), 256, 0, s>>>(I[l].get(), nq, (unsigned)l, cand.get() + nt);
+        k_block_parents<uint64_t><<<grid_for(nq, 256), 256, 0, s>>>(I[l].get(), nq, (unsigned)l, inc_corner, cand.get() + nt);
         DG_LAUNCH_CHECK();
       }
       uint64_t *res;
@@ -773,7 +778,7 @@ void balance_octree(Context &ctx, const Octree &in, Octree &out) {
       }
       if (nq) {
         ProfScope _prof(ctx, "bal_block_parents", (double)nq * 144);
-        k_block_parents<Key128><<<grid_for(nq, 256), 256, 0, s>>>(I[l].get(), nq, (unsigned)l, cand.get() + nt);
+        k_block_parents<Key128><<<grid_for(nq, 256), 256, 0, s>>>(I[l].get(), nq, (unsigned)l, inc_corner, cand.get() + nt);
         DG_LAUNCH_CHECK();
       }
       Key128 *res;
@@ -1255,8 +1260,13 @@ void complete_octree(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned D,
 // par::sampleSort (include/parUtils.h:424; at one rank a local sort,
 // src/parUtils.tcc:1868-1875) and par::removeDuplicates (parUtils.h:437) of
 // octant records: sorted in the octant order (ancestor first on equal
-// anchors), repeated records removed when asked.
-void sort_octants(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned D, bool unique, Octree &out) {
+// anchors), repeated records removed when asked (mode 1).  Mode 2 is the
+// TS_REMOVE_DUPLICATES output of SFC::seqSort::SFC_treeSort
+// (include/sfcSort.h:532-575): sorted, repeated records removed, and every
+// octant followed by one of its descendants removed (the descendants of an
+// octant follow it contiguously in any space-filling-curve order).
+void sort_octants(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned D, int mode, Octree &out) {
+  const bool unique = mode != 0;
   cudaStream_t s = ctx.stream;
   out = Octree();
   out.max_depth = D;
@@ -1276,11 +1286,67 @@ void sort_octants(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned D, bo
   size_t m = n;
   if (unique) m = sort_unique<Key128>(ctx, a.get(), b.get(), n, bits, &srt);
   else srt = radix_sort<Key128>(ctx, a.get(), b.get(), n, bits);
+  if (mode == 2) {
+    // tagged keys of the octants not followed by a descendant
+    Key128 *other = (srt == a.get()) ? b.get() : a.get();
+    DBuf<uint32_t> keep(m, s);
+    {
+      ProfScope _prof(ctx, "treesort_leaves", (double)m * 36);
+      k_complete_leaves<<<grid_for(m, 256), 256, 0, s>>>(srt, m, D, true, other, keep.get(), ctx.d_flags);
+      DG_LAUNCH_CHECK();
+    }
+    DBuf<Key128> res(m, s);
+    const size_t nk = compact<Key128>(ctx, other, keep.get(), m, res.get());
+    check_device_flags(ctx, "SFC_treeSort");
+    out.n = nk;
+    out.keys = res.release_ptr();
+    return;
+  }
   DBuf<Key128> res(m, s);
   k_from_sortform<<<grid_for(m, 256), 256, 0, s>>>(srt, m, res.get());
   DG_LAUNCH_CHECK();
   out.n = m;
   out.keys = res.release_ptr();
+}
+
+// ------------------------------------------------------------------------
+namespace {
+__global__ void k_selftest_keys(uint64_t *k, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) k[i] = (i * 0x9E3779B97F4A7C15ull) >> 7;  // every low digit occurs
+}
+}  // namespace
+
+void lookback_timeout_selftest(Context &ctx, size_t n, unsigned skipped) {
+  using K = uint64_t;
+  constexpr size_t TILE = (size_t)RS_BLOCK * OsCfg<K>::ITEMS;
+  const size_t ntiles = (n + TILE - 1) / TILE;
+  if (skipped == 0 || ntiles <= skipped || ntiles > (1u << 20))
+    fail(DG_ERR_INVALID_ARG, "look-back self-test: need 1 <= skipped < tiles <= 2^20");
+  cudaStream_t s = ctx.stream;
+  DBuf<K> in(n, s), out(n, s);
+  DBuf<uint64_t> status(ntiles * 256, s), doffs(256, s);
+  k_selftest_keys<<<grid_for(n, 256), 256, 0, s>>>(in.get(), n);
+  DG_LAUNCH_CHECK();
+  // digit offsets of the low byte (exclusive scan of its histogram), so
+  // every write of the pass stays inside [0, n)
+  std::vector<uint64_t> h(256, 0), offs(256, 0);
+  std::vector<K> keys(n);
+  DG_CUDA(cudaMemcpyAsync(keys.data(), in.get(), n * sizeof(K), cudaMemcpyDeviceToHost, s));
+  DG_CUDA(cudaStreamSynchronize(s));
+  for (K k : keys) h[k & 255]++;
+  for (int d = 1; d < 256; d++) offs[d] = offs[d - 1] + h[d - 1];
+  DG_CUDA(cudaMemcpyAsync(doffs.get(), offs.data(), 256 * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+  DG_CUDA(cudaMemsetAsync(status.get(), 0, ntiles * 256 * sizeof(uint64_t), s));
+  // the tile tickets start at `skipped`: tiles [0, skipped) are never
+  // processed and their status words stay unpublished
+  unsigned *d_counter = reinterpret_cast<unsigned *>(ctx.d_scratch + 12);
+  const unsigned start = skipped;
+  DG_CUDA(cudaMemcpyAsync(d_counter, &start, sizeof(unsigned), cudaMemcpyHostToDevice, s));
+  k_rs_onesweep<K, OsCfg<K>::ITEMS><<<(unsigned)(ntiles - skipped), RS_BLOCK, 0, s>>>(
+      in.get(), out.get(), n, 0, doffs.get(), status.get(), d_counter, ctx.d_flags);
+  DG_LAUNCH_CHECK();
+  check_device_flags(ctx, "look-back self-test");
 }
 
 }  // namespace dg

@@ -54,8 +54,9 @@ void octree_segment_offsets(Context &ctx, const Octree &o, uint64_t *h_off);
 size_t sort_points(Context &ctx, const double *d_xyz, size_t n, const double glens[3], unsigned max_depth,
                    Key128 *d_out, bool *has_duplicates);
 
-// ot::balanceOctree(incCorner = 1) (src/balance.cpp:31).
-void balance_octree(Context &ctx, const Octree &in, Octree &out);
+// ot::balanceOctree (src/balance.cpp:31): 2:1 balance across faces, edges
+// and corners (inc_corner) or across faces and edges only.
+void balance_octree(Context &ctx, const Octree &in, Octree &out, bool inc_corner = true);
 
 // cloud `seg` of a batched octree as a single-cloud octree
 void octree_extract(Context &ctx, const Octree &in, size_t seg, Octree &out);
@@ -70,11 +71,19 @@ void complete_octree(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned ma
                      bool is_sorted, Octree &out);
 
 // par::sampleSort / par::removeDuplicates (include/parUtils.h:424,437) of
-// n octant records at max_depth
-void sort_octants(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned max_depth, bool unique, Octree &out);
+// n octant records at max_depth: mode 0 sorts, mode 1 also removes repeated
+// octants, mode 2 also removes every octant that has a descendant in the
+// set (SFC_treeSort with TS_REMOVE_DUPLICATES, include/sfcSort.h:532-575)
+void sort_octants(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned max_depth, int mode, Octree &out);
 
 // conversions between tagged keys and {x, y, z, level} u32 records
 void octree_to_xyzl(Context &ctx, const Octree &o, uint32_t *d_xyzl);
 void octree_from_xyzl(Context &ctx, const uint32_t *d_xyzl, size_t n, unsigned max_depth, Octree &out);
+
+// Self-test of the radix sort's bounded look-back wait: one digit pass over
+// n_keys keys in which the first `skipped` tiles never run, so the next
+// tile waits for a predecessor that never publishes.  The wait gives up
+// after its spin limit and the pass raises DGF_TIMEOUT (DG_ERR_TIMEOUT).
+void lookback_timeout_selftest(Context &ctx, size_t n_keys, unsigned skipped);
 
 }  // namespace dg

@@ -10,10 +10,58 @@ generator and a fixed seed per workload:
                    log-uniform in [0.01, 0.2], equal weights, clipped to
                    [0,1)^3 by redrawing
 Points are returned as (n, 3) float64 arrays (x, y, z per row).
+
+The same seed gives the same points bit for bit on every platform: the
+exponentials and logarithms of these generators are evaluated with basic
+IEEE operations only (``_exp``, ``_ln``), because numpy's vectorised ``exp``
+differs in the last bit between x86 (its own AVX-512 code) and other
+platforms (the C library), and one bit can move a point across a level-30
+cell boundary.
 """
 from __future__ import annotations
 
+import decimal
+import math
+
 import numpy as np
+
+_DEC = decimal.Context(prec=50)
+# ln 2 to 60 digits (a mathematical constant)
+_LN2 = decimal.Decimal("0.693147180559945309417232121458176568075500134360255254120680")
+
+
+def _split_hi(d: decimal.Decimal) -> float:
+    """d rounded to a double whose low 32 mantissa bits are zero, so that
+    k * hi is exact for |k| < 2^20."""
+    b = np.frombuffer(np.float64(float(d)).tobytes(), np.uint64)[0] & np.uint64(0xFFFFFFFF00000000)
+    return float(np.frombuffer(b.tobytes(), np.float64)[0])
+
+
+_LN2_HI = _split_hi(_LN2)
+_LN2_LO = float(_DEC.subtract(_LN2, decimal.Decimal(_LN2_HI)))
+_INV_LN2 = float(_DEC.divide(1, _LN2))
+_EXP_TAYLOR = [1.0 / math.factorial(k) for k in range(14)]
+
+
+def _exp(x) -> np.ndarray:
+    """exp(x) from + - * and ldexp only (within 2 ulp of the true value):
+    x = k ln2 + r with |r| <= ln2 / 2 (Cody-Waite split of ln2), the Taylor
+    polynomial of degree 13 in r by Horner's rule (truncation error below
+    5e-18 relative), scaled by 2^k."""
+    x = np.asarray(x, np.float64)
+    k = np.rint(x * _INV_LN2)
+    r = (x - k * _LN2_HI) - k * _LN2_LO
+    p = np.full_like(r, _EXP_TAYLOR[13])
+    for c in _EXP_TAYLOR[12::-1]:
+        p *= r
+        p += c
+    return np.ldexp(p, k.astype(np.int32), out=p)
+
+
+def _ln(v: float) -> float:
+    """Natural logarithm of a positive scalar, correctly rounded (decimal
+    arithmetic)."""
+    return float(_DEC.ln(decimal.Decimal(float(v))))
 
 
 def _inside(p: np.ndarray) -> np.ndarray:
@@ -35,7 +83,7 @@ def gaussian(n: int, mean: float = 0.5, sigma: float = 0.1, seed: int = 0) -> np
 
 def lognormal(n: int, seed: int = 0) -> np.ndarray:
     rng = np.random.Generator(np.random.PCG64(seed))
-    u = np.exp(rng.standard_normal(size=(n, 3)))
+    u = _exp(rng.standard_normal(size=(n, 3)))
     p = u / (1.0 + u)
     # u/(1+u) < 1 always in exact arithmetic; guard the rounding to 1.0
     np.minimum(p, np.nextafter(1.0, 0.0), out=p)
@@ -45,7 +93,7 @@ def lognormal(n: int, seed: int = 0) -> np.ndarray:
 def mixture(n: int, rng: np.random.Generator) -> np.ndarray:
     k = int(rng.integers(1, 9))
     centres = rng.uniform(0.1, 0.9, size=(k, 3))
-    sig = np.exp(rng.uniform(np.log(0.01), np.log(0.2), size=k))
+    sig = _exp(rng.uniform(_ln(0.01), _ln(0.2), size=k))
     out = np.empty((n, 3))
     got = 0
     while got < n:
@@ -60,7 +108,16 @@ def mixture(n: int, rng: np.random.Generator) -> np.ndarray:
 
 def cloud_sizes(count: int, lo: float, hi: float, seed: int) -> np.ndarray:
     rng = np.random.Generator(np.random.PCG64(seed))
-    return np.round(np.exp(rng.uniform(np.log(lo), np.log(hi), size=count))).astype(np.int64)
+    return np.round(_exp(rng.uniform(_ln(lo), _ln(hi), size=count))).astype(np.int64)
+
+
+def batch_clouds(count: int = 256, lo: float = 1e4, hi: float = 4e6, seed: int = 2) -> list:
+    """The batching workload: ``count`` Gaussian-mixture clouds with sizes
+    log-uniform in [lo, hi] (sizes from ``seed``, then every cloud from one
+    generator seeded with ``seed``)."""
+    sizes = cloud_sizes(count, lo, hi, seed=seed)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return [mixture(int(n), rng) for n in sizes]
 
 
 def workload(name: str, n: int | None = None) -> np.ndarray:

@@ -86,7 +86,7 @@ def poisson_stream(count: int, rate: float = 200.0, lo: float = 1e4, hi: float =
     half Gaussian-mixture clouds and half log-normal clouds."""
     rng = np.random.Generator(np.random.PCG64(seed))
     gaps = rng.exponential(1.0 / rate, count)
-    sizes = np.round(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(np.int64)
+    sizes = np.round(datagen._exp(rng.uniform(datagen._ln(lo), datagen._ln(hi), count))).astype(np.int64)
     reqs = []
     t = 0.0
     for i in range(count):

@@ -128,10 +128,16 @@ int dg_sort_unique_points(dg_ctx ctx, const double *xyz, size_t n, const double 
  *     xyz 8-byte and out_xyzl 16-byte aligned (DG_ERR_INVALID_ARG otherwise,
  *     checked before any work);
  *   - n <= DG_NOALLOC_MAX_POINTS, else DG_ERR_CAPACITY before any work;
+ *   - records are in Morton order whatever order other calls use (it has
+ *     no context);
  *   - all scratch (about 41 MB) is one static device array of the library,
- *     set up on the first call on each device (cudaGetSymbolAddress with
- *     that device current): make that first call before any stream capture
- *     begins;
+ *     reserved on a device when the runtime loads the library's device code
+ *     there (its first kernel launch on that device under lazy module
+ *     loading, the default; context creation under
+ *     CUDA_MODULE_LOADING=EAGER); the first call on each device looks up its
+ *     address (cudaGetSymbolAddress with that device current; a failed
+ *     look-up is retried by the next call): make that first call before any
+ *     stream capture begins;
  *   - the work runs on cuda_stream (a cudaStream_t of the current device;
  *     NULL: the legacy default stream), which the call synchronises before
  *     it returns;
@@ -142,11 +148,14 @@ int dg_sort_unique_points(dg_ctx ctx, const double *xyz, size_t n, const double 
 int dg_sort_unique_points_noalloc(const double *xyz, size_t n, const double gLens[3], unsigned maxDepth,
                                   uint32_t *out_xyzl, size_t *n_unique, void *cuda_stream);
 
-/* ---- ot::balanceOctree(incCorner = true) ----------------------------------
- * include/octUtils.h:692 / src/balance.cpp:31 (1-rank branch :54-63).  The
- * input must be sorted, linear and complete (the reference's assumption).
- * incCorner = 0 is not supported (DG_ERR_UNSUPPORTED).  The input handle is
- * left intact (the reference clears `in`). */
+/* ---- ot::balanceOctree ------------------------------------------------------
+ * include/octUtils.h:692 / src/balance.cpp:31 (1-rank branch :54-63): the
+ * coarsest refinement that is 2:1 balanced across faces, edges and corners
+ * (incCorner != 0) or across faces and edges only (incCorner = 0, the 18
+ * directions of TreeNode::addBalancingDescendants, src/TreeNode.cpp:138).
+ * The input must be sorted, linear and complete (the reference's
+ * assumption).  The input handle is left intact (the reference clears
+ * `in`). */
 int dg_balance_octree(dg_ctx ctx, dg_octree in, int incCorner, int comm_size, dg_octree *out);
 
 /* ---- ot::coarsenOctree -----------------------------------------------------
@@ -165,6 +174,27 @@ int dg_coarsen_octree(dg_ctx ctx, dg_octree in, dg_octree *out);
  * DG_ERR_DOMAIN. */
 int dg_sort_octants(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDepth, int removeDuplicates,
                     int src_on_device, uint32_t *out_xyzl, int dst_on_device, size_t *n_out);
+
+/* ---- SFC::parSort::SFC_treeSort --------------------------------------------
+ * include/sfcSort.h:1378 (one rank: SFC::seqSort::SFC_treeSort :418), the
+ * tree sort the reference's DA factory and completeOctree call
+ * (src/oda/private/odaFactory.cpp:186, src/construct.cpp:541,553): the n
+ * octant records xyzl sorted in the context's octant order.  options
+ * DG_TS_SORT_ONLY: all n records, sorted (the reference sorts pNodes in
+ * place); DG_TS_REMOVE_DUPLICATES: sorted, repeated octants removed and every
+ * octant that has a descendant in the input removed (the reference's
+ * pOutSorted, sfcSort.h:532-575).  *n_out is the count written to out_xyzl
+ * (room for n records).  DG_TS_CONSTRUCT_OCTREE / DG_TS_BALANCE_OCTREE give
+ * DG_ERR_UNSUPPORTED: completeOctree and balanceOctree are
+ * dg_complete_octree and dg_balance_octree.  Differences: one input record
+ * with DG_TS_REMOVE_DUPLICATES gives that record (the reference leaves
+ * pOutSorted unchanged below two records, sfcSort.h:532). */
+#define DG_TS_SORT_ONLY 0u
+#define DG_TS_REMOVE_DUPLICATES 1u
+#define DG_TS_CONSTRUCT_OCTREE 2u
+#define DG_TS_BALANCE_OCTREE 4u
+int dg_tree_sort(dg_ctx ctx, const uint32_t *xyzl, size_t n, unsigned maxDepth, unsigned options, int src_on_device,
+                 uint32_t *out_xyzl, int dst_on_device, size_t *n_out);
 
 /* ---- ot::completeOctree ----------------------------------------------------
  * include/octUtils.h:813 / src/construct.cpp:518 at one rank: the n octants
@@ -339,6 +369,16 @@ int dg_ctx_profile(dg_ctx ctx, int enable);
 int dg_ctx_profile_count(dg_ctx ctx, int *count);
 int dg_ctx_profile_entry(dg_ctx ctx, int index, char *name, size_t name_len, double *total_ms,
                          unsigned long long *launches, double *bytes);
+
+/* ---- self-test of the bounded device waits -----------------------------
+ * No counterpart in the reference (it has no device code).  Runs one digit
+ * pass of the radix sort over n_keys synthetic keys in which the first
+ * skipped_tiles tiles are never processed, so the next tile's look-back
+ * waits for a predecessor that never publishes its count.  The wait gives
+ * up after its spin limit (2^22 polls, a fraction of a second), the kernel
+ * returns, and the call reports DG_ERR_TIMEOUT; the context stays usable.
+ * Needs 1 <= skipped_tiles < tiles (4096 keys per tile) <= 2^20. */
+int dg_debug_lookback_timeout(dg_ctx ctx, size_t n_keys, unsigned skipped_tiles);
 
 #ifdef __cplusplus
 }

@@ -310,7 +310,12 @@ static int u128_contains(const u128 *a, size_t n, u128 v) {
   return lo < n && a[lo] == v;
 }
 
-int dgo_balance(const dgo_oct *in, size_t n, unsigned D, dgo_oct **out, size_t *nout) {
+/* incCorner = 0 (balanceOctree's face + edge form, src/balance.cpp:31 with
+ * the 18 neighbour directions of TreeNode::addBalancingDescendants,
+ * src/TreeNode.cpp:138-190): a corner neighbour of q imposes nothing, so the
+ * one parent that only corner neighbours reach (the outward parent on all
+ * three axes) is left out. */
+int dgo_balance_ex(const dgo_oct *in, size_t n, unsigned D, int incCorner, dgo_oct **out, size_t *nout) {
   if (D > 30 || n == 0) return DGO_EINVAL;
   if (n == 1) {
     dgo_oct *r = (dgo_oct *)malloc(sizeof(dgo_oct));
@@ -359,6 +364,7 @@ int dgo_balance(const dgo_oct *in, size_t n, unsigned D, dgo_oct **out, size_t *
         opt[a][1] = (q[a] & s) ? (int64_t)(par + 2 * s) : (int64_t)par - (int64_t)(2 * s);
       }
       for (int c = 0; c < 8; c++) {
+        if (c == 7 && !incCorner) continue;
         int64_t p0 = opt[0][c & 1], p1 = opt[1][(c >> 1) & 1], p2 = opt[2][(c >> 2) & 1];
         if (p0 < 0 || p1 < 0 || p2 < 0 || p0 >= (int64_t)dom || p1 >= (int64_t)dom || p2 >= (int64_t)dom) continue;
         cand[nc++] = lvl_index((uint32_t)p0, (uint32_t)p1, (uint32_t)p2, l - 1, D);
@@ -401,6 +407,10 @@ int dgo_balance(const dgo_oct *in, size_t n, unsigned D, dgo_oct **out, size_t *
 done:
   for (int l = 0; l < 32; l++) free(I[l]);
   return rc;
+}
+
+int dgo_balance(const dgo_oct *in, size_t n, unsigned D, dgo_oct **out, size_t *nout) {
+  return dgo_balance_ex(in, n, D, 1, out, nout);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -763,7 +773,7 @@ static size_t find_leaf(const u128 *keys, size_t n, uint32_t x, uint32_t y, uint
   return lo == 0 ? n : lo - 1;
 }
 
-int dgo_is_balanced(const dgo_oct *a, size_t n, unsigned D) {
+int dgo_is_balanced_ex(const dgo_oct *a, size_t n, unsigned D, int incCorner) {
   u128 *keys = (u128 *)malloc((n ? n : 1) * sizeof(u128));
   if (!keys) return 0;
   for (size_t i = 0; i < n; i++) keys[i] = morton(a[i].x, a[i].y, a[i].z);
@@ -775,6 +785,7 @@ int dgo_is_balanced(const dgo_oct *a, size_t n, unsigned D) {
       for (int dy = -1; dy <= 1 && ok; dy++)
         for (int dx = -1; dx <= 1 && ok; dx++) {
           if (!dx && !dy && !dz) continue;
+          if (!incCorner && dx && dy && dz) continue;
           int64_t nx = a[i].x + dx * s, ny = a[i].y + dy * s, nz = a[i].z + dz * s;
           if (nx < 0 || ny < 0 || nz < 0 || nx >= dom || ny >= dom || nz >= dom) continue;
           size_t j = find_leaf(keys, n, (uint32_t)nx, (uint32_t)ny, (uint32_t)nz);
@@ -784,6 +795,8 @@ int dgo_is_balanced(const dgo_oct *a, size_t n, unsigned D) {
   free(keys);
   return ok;
 }
+
+int dgo_is_balanced(const dgo_oct *a, size_t n, unsigned D) { return dgo_is_balanced_ex(a, n, D, 1); }
 
 uint64_t dgo_fnv1a(const dgo_oct *a, size_t n) {
   uint64_t h = 1469598103934665603ull;

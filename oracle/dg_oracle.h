@@ -57,6 +57,8 @@ int dgo_p2o_local(const dgo_oct *pts, size_t n, unsigned maxDepth, unsigned maxP
  * rather than by the reference's block + ripple procedure
  * (balance.cpp:801-1338, TreeNode.cpp:884-1342). */
 int dgo_balance(const dgo_oct *in, size_t n, unsigned maxDepth, dgo_oct **out, size_t *nout);
+/* incCorner = 0: balanced across faces and edges only */
+int dgo_balance_ex(const dgo_oct *in, size_t n, unsigned maxDepth, int incCorner, dgo_oct **out, size_t *nout);
 
 /* ot::coarsenOctree, sequential form (src/coarsen.cpp:53): every complete
  * family of 8 sibling leaves of a sorted, linear, complete octree is
@@ -80,6 +82,7 @@ int dgo_is_sorted_unique(const dgo_oct *a, size_t n, unsigned maxDepth);
 int dgo_is_linear(const dgo_oct *a, size_t n, unsigned maxDepth);
 int dgo_is_complete(const dgo_oct *a, size_t n, unsigned maxDepth);
 int dgo_is_balanced(const dgo_oct *a, size_t n, unsigned maxDepth);
+int dgo_is_balanced_ex(const dgo_oct *a, size_t n, unsigned maxDepth, int incCorner);
 
 /* Element-type tables (include/oda/cnumEtypes.h, include/oda/odaUtils.tcc:14):
  * masks[c*18 + t] is the 8-bit hanging-vertex mask of element type t for

@@ -58,6 +58,8 @@ def lib():
         L.dgo_points_to_octree.argtypes = [P, SZ, P, U, U, ctypes.POINTER(P), ctypes.POINTER(SZ)]
         L.dgo_p2o_local.argtypes = [P, SZ, U, U, ctypes.POINTER(P), ctypes.POINTER(SZ)]
         L.dgo_balance.argtypes = [P, SZ, U, ctypes.POINTER(P), ctypes.POINTER(SZ)]
+        L.dgo_balance_ex.argtypes = [P, SZ, U, ctypes.c_int, ctypes.POINTER(P), ctypes.POINTER(SZ)]
+        L.dgo_is_balanced_ex.argtypes = [P, SZ, U, ctypes.c_int]
         L.dgo_coarsen.argtypes = [P, SZ, U, ctypes.POINTER(P), ctypes.POINTER(SZ)]
         L.dgo_hilbert_sort.argtypes = [P, SZ, U]
         L.dgo_complete.argtypes = [P, SZ, U, ctypes.c_int, ctypes.c_int, ctypes.POINTER(P), ctypes.POINTER(SZ)]
@@ -130,10 +132,11 @@ def p2o_local(pts: np.ndarray, max_depth: int = 30, max_pts: int = 1) -> np.ndar
     return _take_octs(p, n.value)
 
 
-def balance(octs: np.ndarray, max_depth: int = 30) -> np.ndarray:
+def balance(octs: np.ndarray, max_depth: int = 30, inc_corner: bool = True) -> np.ndarray:
     octs = np.ascontiguousarray(octs, dtype=np.uint32).reshape(-1, 4)
     p, n = ctypes.c_void_p(), ctypes.c_size_t()
-    _check(lib().dgo_balance(_ptr(octs), octs.shape[0], max_depth, ctypes.byref(p), ctypes.byref(n)), "balance")
+    _check(lib().dgo_balance_ex(_ptr(octs), octs.shape[0], max_depth, int(inc_corner), ctypes.byref(p),
+                                ctypes.byref(n)), "balance")
     return _take_octs(p, n.value)
 
 
@@ -171,6 +174,7 @@ def checks(octs: np.ndarray, max_depth: int = 30) -> dict:
         "linear": bool(L.dgo_is_linear(*a)),
         "complete": bool(L.dgo_is_complete(*a)),
         "balanced": bool(L.dgo_is_balanced(*a)),
+        "balanced_face_edge": bool(L.dgo_is_balanced_ex(*a, 0)),
     }
 
 

@@ -18,6 +18,10 @@
  *   complete IN.oct MAXDEPTH ISUNIQUE ISSORTED OUT.oct
  *         ot::completeOctree (src/construct.cpp:518) at 1 rank, with the
  *         input octants in file order.
+ *   treesort IN.oct MAXDEPTH OPTIONS OUT.oct
+ *         SFC::parSort::SFC_treeSort (include/sfcSort.h:1378) at 1 rank:
+ *         OPTIONS 0 writes the input sorted in place, TS_REMOVE_DUPLICATES
+ *         (1) writes the sorted output without duplicates and ancestors.
  *   check IN.oct MAXDEPTH
  *         ot::test::isLinear / isComplete / isBalanced (src/test/testUtils.C).
  *   da    BAL.oct MAXDEPTH STENCILDIR VEC_IN|- OUT_PREFIX
@@ -55,6 +59,7 @@
 #include "oda.h"
 #include "odaUtils.h"
 #include "parUtils.h"
+#include "sfcSort.h"
 #include "testUtils.h"
 
 double ****LaplacianType2Stencil = nullptr;
@@ -170,6 +175,27 @@ static int mode_complete(int argc, char **argv) {
   write_oct(argv[6], out);
   std::printf("{\"op\":\"complete\",\"n_in\":%zu,\"n_out\":%zu,\"seconds\":%.6f}\n", in.size(), out.size(),
               t1 - t0);
+  return 0;
+}
+
+// treesort IN.oct MAXDEPTH OPTIONS OUT.oct: SFC::parSort::SFC_treeSort
+// (include/sfcSort.h:1378; one rank: the sequential sort :418) with the
+// arguments its callers pass (src/construct.cpp:541,553, odaFactory.cpp:186:
+// root parent, rotation 0, k = 1).  OPTIONS 0 writes the input sorted in
+// place; TS_REMOVE_DUPLICATES (1) writes pOutSorted.
+static int mode_treesort(int argc, char **argv) {
+  if (argc < 6) return 1;
+  unsigned maxDepth = std::atoi(argv[3]);
+  unsigned options = std::atoi(argv[4]);
+  std::vector<ot::TreeNode> in = read_oct(argv[2], maxDepth), tmp;
+  ot::TreeNode root(3, maxDepth);
+  double t0 = now_s();
+  SFC::parSort::SFC_treeSort(in, tmp, tmp, tmp, 0.1, maxDepth, root, 0, 1, options, NUM_NPES_THRESHOLD,
+                             MPI_COMM_WORLD);
+  double t1 = now_s();
+  write_oct(argv[5], options & TS_REMOVE_DUPLICATES ? tmp : in);
+  std::printf("{\"op\":\"treesort\",\"n_in\":%zu,\"n_out\":%zu,\"seconds\":%.6f}\n", in.size(),
+              (options & TS_REMOVE_DUPLICATES ? tmp : in).size(), t1 - t0);
   return 0;
 }
 
@@ -454,5 +480,6 @@ int main(int argc, char **argv) {
   if (m == "complete") rc = mode_complete(argc, argv);
   if (m == "da") rc = mode_da(argc, argv);
   if (m == "io") rc = mode_io(argc, argv);
+  if (m == "treesort") rc = mode_treesort(argc, argv);
   return rc;
 }

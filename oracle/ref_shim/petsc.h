@@ -2,7 +2,9 @@
  * Header-only stand-in for the handful of PETSc types, macros and Vec/Mat
  * calls that the reference's octree/DA/element-loop sources reference.  Used
  * only to compile the reference into the CPU oracle binary (oracle/_ref).
- * Vec is a plain heap array; Mat is a context holder.  No solver exists here.
+ * Vec is a plain heap array; Mat is a context holder with the two shell
+ * operations (MATOP_MULT, MATOP_GET_DIAGONAL) the MatShell callbacks of
+ * include/dendro_gb300_petsc.hpp are tested through.  No solver exists here.
  */
 #ifndef DG_ORACLE_PETSC_SHIM_H
 #define DG_ORACLE_PETSC_SHIM_H
@@ -47,10 +49,14 @@ struct dg_shim_vec {
   PetscScalar *a;
 };
 typedef dg_shim_vec *Vec;
+struct dg_shim_mat;
+typedef dg_shim_mat *Mat;
 struct dg_shim_mat {
   void *ctx;
+  /* shell operations (MatShellSetOperation) */
+  PetscErrorCode (*mult)(Mat, Vec, Vec);
+  PetscErrorCode (*diag)(Mat, Vec);
 };
-typedef dg_shim_mat *Mat;
 struct dg_shim_opaque {
   int unused;
 };
@@ -136,7 +142,27 @@ inline PetscErrorCode PetscStrcmp(const char *a, const char *b, PetscBool *f) {
   return 0;
 }
 inline PetscErrorCode MatCreate(MPI_Comm, Mat *m) {
-  *m = new dg_shim_mat{nullptr};
+  *m = new dg_shim_mat{nullptr, nullptr, nullptr};
+  return 0;
+}
+inline PetscErrorCode MatCreateShell(MPI_Comm, PetscInt, PetscInt, PetscInt, PetscInt, void *ctx, Mat *m) {
+  *m = new dg_shim_mat{ctx, nullptr, nullptr};
+  return 0;
+}
+inline PetscErrorCode MatShellGetContext(Mat m, void *ctx) {
+  *(void **)ctx = m->ctx;
+  return 0;
+}
+inline PetscErrorCode MatShellSetOperation(Mat m, MatOperation op, void (*f)(void)) {
+  if (op == MATOP_MULT) m->mult = (PetscErrorCode(*)(Mat, Vec, Vec))f;
+  if (op == MATOP_GET_DIAGONAL) m->diag = (PetscErrorCode(*)(Mat, Vec))f;
+  return 0;
+}
+inline PetscErrorCode MatMult(Mat m, Vec x, Vec y) { return m->mult ? m->mult(m, x, y) : PETSC_ERR_SUP; }
+inline PetscErrorCode MatGetDiagonal(Mat m, Vec d) { return m->diag ? m->diag(m, d) : PETSC_ERR_SUP; }
+inline PetscErrorCode MatDestroy(Mat *m) {
+  delete *m;
+  *m = nullptr;
   return 0;
 }
 inline PetscErrorCode MatSetSizes(Mat, PetscInt, PetscInt, PetscInt, PetscInt) { return 0; }

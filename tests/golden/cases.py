@@ -130,3 +130,47 @@ def complete_inputs():
         out.append((f"sparse{i}_sorted", srt, D, 1, 1))
         out.append((f"sparse{i}_unique", shuf, D, 1, 0))
     return out
+
+
+def morton_rank_order(xyz_u32: np.ndarray, bits: int = 31) -> np.ndarray:
+    """Indices that sort points (x, y, z integer coordinates below 2^bits) by
+    their Morton key (z above y above x at every bit)."""
+    xyz = np.asarray(xyz_u32, np.uint64)
+    lo = np.zeros(len(xyz), np.uint64)
+    hi = np.zeros(len(xyz), np.uint64)
+    for b in range(bits):
+        for a in range(3):
+            bit = (xyz[:, a] >> np.uint64(b)) & np.uint64(1)
+            pos = 3 * b + a
+            if pos < 63:
+                lo |= bit << np.uint64(pos)
+            else:
+                hi |= bit << np.uint64(pos - 63)
+    return np.lexsort((lo, hi))
+
+
+def config1_vector(node_xyz: np.ndarray, seed: int = 1, order: np.ndarray | None = None) -> np.ndarray:
+    """The plain workload's nodal input vector: uniform in [-1, 1] from
+    PCG64(seed), assigned to the nodes in the Morton order of their
+    coordinates (so it does not depend on a node numbering).  ``order``:
+    morton_rank_order(node_xyz), when already known."""
+    if order is None:
+        order = morton_rank_order(node_xyz)
+    v = np.random.Generator(np.random.PCG64(seed)).uniform(-1.0, 1.0, len(node_xyz))
+    out = np.empty(len(node_xyz))
+    out[order] = v
+    return out
+
+
+def projection_weights(node_xyz: np.ndarray, k: int) -> np.ndarray:
+    """k weight vectors (k x n), uniform in [-1, 1] from PCG64(100 + j), in the
+    same Morton assignment as config1_vector: sum_i w_ji y_i summarises a
+    nodal result y independently of the node numbering."""
+    order = morton_rank_order(node_xyz)
+    return np.stack([config1_vector(node_xyz, 100 + j, order) for j in range(k)])
+
+
+def sha256_records(a: np.ndarray) -> str:
+    import hashlib
+
+    return hashlib.sha256(memoryview(np.ascontiguousarray(a))).hexdigest()

@@ -17,11 +17,15 @@ outputs next to the inputs:
   io/             the reference's point and octree files
   ref_mat.npz     the assembled K + M of CreateAndComputeFullJacobian1 on
                   a small balanced octree (row, column node coordinates)
+  ref_face_edge.npz balanceOctree(incCorner = false) outputs
+  ref_treesort.npz SFC::parSort::SFC_treeSort outputs (sort only, and
+                  TS_REMOVE_DUPLICATES) on octant sets with repeats and
+                  ancestors
   ref_hilbert.npz the reference's default Hilbert-ordered build
                   (oracle/_ref_hilbert/ref_driver, make ORDER=hilbert):
                   points2Octree, balanceOctree and completeOctree outputs
 
-Usage:  python tests/golden/make_golden.py [/path/to/reference]
+Usage:  python tests/golden/make_golden.py REFERENCE_DIR   (or DENDRO_REFERENCE=REFERENCE_DIR)
 """
 from __future__ import annotations
 
@@ -42,7 +46,9 @@ sys.path.insert(0, ROOT)
 from dendro_gb300 import datagen  # noqa: E402
 from tests.golden import cases  # noqa: E402
 
-REF = next((a for a in sys.argv[1:] if not a.startswith("--")), "/root/reference")
+REF = next((a for a in sys.argv[1:] if not a.startswith("--")), os.environ.get("DENDRO_REFERENCE"))
+if not REF or not os.path.isdir(os.path.join(REF, "src")):
+    sys.exit("usage: make_golden.py REFERENCE_DIR (or set DENDRO_REFERENCE): the Dendro4 source tree")
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 DRIVER_HILBERT = os.path.join(ROOT, "oracle", "_ref_hilbert", "ref_driver")
 
@@ -209,7 +215,66 @@ def make_mat():
                         row=index(rc[:, :3]), col=index(rc[:, 3:]), val=rec["v"].copy())
 
 
+def make_face_edge():
+    """balanceOctree with incCorner = false (faces and edges only) on the
+    reference's points2Octree output of every small case whose balance
+    finishes: ref_face_edge.npz (count + FNV-1a, and the records up to 50k
+    octants)."""
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, (fn, depth, maxpts) in cases.SMALL.items():
+            pf, of, bf = (os.path.join(tmp, f"{name}.{e}") for e in ("pts", "oct", "bal"))
+            write_pts(pf, fn())
+            run("p2o", pf, depth, maxpts, of)
+            try:
+                run("bal", of, depth, 0, 0, bf)
+            except subprocess.CalledProcessError:
+                continue  # octants outside the domain: the reference's balance aborts
+            lin, bal = read_oct(of), read_oct(bf)
+            out[f"{name}/lin"] = lin
+            out[f"{name}/bal_n"] = np.int64(len(bal))
+            out[f"{name}/bal_fnv"] = np.uint64(fnv1a(bal))
+            out[f"{name}/bal"] = bal if len(bal) <= 50000 else np.zeros((0, 4), np.uint32)
+            out[f"{name}/params"] = np.array([depth, maxpts], np.int64)
+    np.savez_compressed(os.path.join(HERE, "ref_face_edge.npz"), **out)
+
+
+def make_treesort():
+    """SFC::parSort::SFC_treeSort at one rank (options 0: the input sorted in
+    place; TS_REMOVE_DUPLICATES: sorted without repeats and ancestors) on the
+    completeOctree inputs and on a shuffled, repeated balanced octree with
+    ancestors: ref_treesort.npz."""
+    rng = np.random.Generator(np.random.PCG64(77))
+    inputs = [(name, octs, D) for name, octs, D, _, _ in cases.complete_inputs()]
+    with tempfile.TemporaryDirectory() as tmp:
+        _, bal = ref_p2o_bal(tmp, "ts", datagen.gaussian(1500, 0.5, 0.1, seed=78), 30, 1)
+    anc = bal[rng.integers(0, len(bal), 200)].astype(np.int64)
+    la = np.maximum(anc[:, 3] - rng.integers(1, 4, len(anc)), 0)
+    m = ~((np.int64(1) << (30 - la)) - 1)
+    anc = np.stack([anc[:, 0] & m, anc[:, 1] & m, anc[:, 2] & m, la], 1).astype(np.uint32)
+    messy = np.concatenate([bal, bal[rng.integers(0, len(bal), 3000)], anc])
+    rng.shuffle(messy)
+    inputs.append(("bal1500_messy", messy, 30))
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        fi, fo = os.path.join(tmp, "in.oct"), os.path.join(tmp, "out.oct")
+        for name, octs, D in inputs:
+            write_oct(fi, octs)
+            out[f"{name}/in"] = octs
+            out[f"{name}/params"] = np.array([D], np.int64)
+            for opt in (0, 1):
+                run("treesort", fi, D, opt, fo)
+                out[f"{name}/opt{opt}"] = read_oct(fo)
+    np.savez_compressed(os.path.join(HERE, "ref_treesort.npz"), **out)
+
+
 def main():
+    if "--face-edge-only" in sys.argv:
+        make_face_edge()
+        return
+    if "--treesort-only" in sys.argv:
+        make_treesort()
+        return
     if "--mat-only" in sys.argv:
         make_mat()
         return
@@ -323,6 +388,8 @@ def main():
     make_complete()
     make_hilbert()
     make_mat()
+    make_face_edge()
+    make_treesort()
 
 
 if __name__ == "__main__":

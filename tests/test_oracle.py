@@ -135,3 +135,55 @@ def test_balance_idempotent_and_small_inputs(oracle, ref_cases):
     kids = np.array([[(c & 1) << 29, (c >> 1 & 1) << 29, (c >> 2 & 1) << 29, 1] for c in range(8)], np.uint32)
     kids = kids[np.lexsort((kids[:, 0], kids[:, 1], kids[:, 2]))]
     assert np.array_equal(oracle.balance(kids, 30), kids)
+
+
+# ---- balanceOctree(incCorner = false): faces and edges only ----------------
+@pytest.fixture(scope="module")
+def ref_face_edge():
+    return np.load(os.path.join(GOLDEN, "ref_face_edge.npz"))
+
+
+def _face_edge_names():
+    g = np.load(os.path.join(GOLDEN, "ref_face_edge.npz"))
+    return sorted({k.split("/")[0] for k in g.files})
+
+
+@pytest.mark.parametrize("name", _face_edge_names())
+def test_face_edge_balance_matches_reference(oracle, ref_face_edge, name):
+    depth = int(ref_face_edge[f"{name}/params"][0])
+    lin = ref_face_edge[f"{name}/lin"]
+    bal = oracle.balance(lin, depth, inc_corner=False)
+    assert len(bal) == int(ref_face_edge[f"{name}/bal_n"])
+    assert oracle.fnv1a(bal) == int(ref_face_edge[f"{name}/bal_fnv"])
+    ref = ref_face_edge[f"{name}/bal"]
+    if len(ref):
+        assert np.array_equal(bal, ref)
+    chk = oracle.checks(bal, depth)
+    assert chk["complete"] and chk["linear"] and chk["balanced_face_edge"]
+
+
+# ---- SFC_treeSort -----------------------------------------------------------
+def test_treesort_fixture_is_sort_and_linearise():
+    """The reference's tree sort output (ref_treesort.npz) is the sorted input
+    (option 0) and the sorted, unique input without ancestors
+    (TS_REMOVE_DUPLICATES), except that a single input octant gives an empty
+    pOutSorted (sfcSort.h:532 only fills it for two or more)."""
+    g = np.load(os.path.join(GOLDEN, "ref_treesort.npz"))
+    for name in sorted({k.split("/")[0] for k in g.files}):
+        D = int(g[f"{name}/params"][0])
+        inp, o0, o1 = g[f"{name}/in"], g[f"{name}/opt0"], g[f"{name}/opt1"]
+        if len(inp) == 0:
+            assert len(o0) == 0 and len(o1) == 0
+            continue
+        assert np.array_equal(np.unique(o0, axis=0), np.unique(inp, axis=0)) and len(o0) == len(inp)
+        srt = cases.morton_sort(inp, D)
+        assert np.array_equal(np.unique(o0, axis=0).shape, srt.shape)
+        if len(inp) == 1:
+            assert len(o1) == 0
+            continue
+        keep = np.ones(len(srt), bool)
+        for i in range(len(srt) - 1):
+            a, b = srt[i].astype(np.int64), srt[i + 1].astype(np.int64)
+            if a[3] < b[3] and all((a[k] >> (D - a[3])) == (b[k] >> (D - a[3])) for k in range(3)):
+                keep[i] = False
+        assert np.array_equal(o1, srt[keep]), name

@@ -118,3 +118,40 @@ def test_noalloc_errors_leave_the_scratch_usable():
         L.dg_ctx_destroy(ctx)
     assert nu == nref.value
     np.testing.assert_array_equal(out[:nu].cpu().numpy().view(np.uint32), ref[:nu])
+
+
+def test_noalloc_source_allocates_nothing():
+    """No allocating call appears in the entry point's translation unit (a
+    pooled buffer, cudaMalloc / cudaMallocAsync / cudaFree or a library
+    routine that allocates)."""
+    import os
+    import re
+
+    src = open(os.path.join(os.path.dirname(_lib.HEADER), "..", "dendro_gb300", "csrc", "dg_noalloc.cu")).read()
+    code = re.sub(r"//[^\n]*", "", src)
+    for pat in (r"\bcudaMalloc", r"\bcudaFree", r"\bDBuf\b", r"\bcudaMallocManaged", r"\bcudaHostAlloc", r"\bnew\b",
+                r"\bmalloc\(", r"\bthrust::", r"\bcub::"):
+        assert not re.search(pat, code), pat
+
+
+@pytest.mark.gpu
+def test_noalloc_device_memory_unchanged_by_a_call():
+    """After a warm-up call, a further call leaves the device's free memory
+    exactly as it was (cudaMemGetInfo before and after)."""
+    torch = pytest.importorskip("torch")
+    L = _L()
+    dev = torch.device("cuda:0")
+    g = np.ones(3)
+    pts = datagen.lognormal(200_000, seed=12)
+    xyz = torch.from_numpy(pts).to(dev)
+    out = torch.zeros((len(pts), 4), dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    rc, nu = _noalloc(L, xyz.data_ptr(), len(pts), g, 30, out.data_ptr())
+    assert rc == DG_OK
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(0)
+    rc, nu2 = _noalloc(L, xyz.data_ptr(), len(pts), g, 30, out.data_ptr())
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert rc == DG_OK and nu2 == nu
+    assert free1 == free0
