@@ -133,9 +133,12 @@ def test_reference_surface_caller(oracle, tmp_path):
     assert np.array_equal(E[:, :3], bal[:, :3])
     assert np.array_equal(E[:, 3] & 255, bal[:, 3] + 1)
     assert np.array_equal(E[:, 4:].reshape(-1, 8, 3), oda.node_xyz[oda.nodes])
-    # MatShell callbacks give exactly what the direct calls give
-    assert info["shell_err"] == 0.0 and info["diag_err"] == 0.0
+    # MatShell callbacks give what the direct calls give (the element loop
+    # adds shared node runs atomically, so repeated FP64 calls agree to
+    # rounding, not bit for bit)
+    tol = 1e-13 * info["ymax"]
+    assert info["shell_err"] <= tol and info["diag_err"] <= tol
     assert abs(info["mass_sum"] - 1.0) < 1e-12
-    assert info["dir_err"] == 0.0 and info["dirdiag_err"] == 0.0 and info["mg_levels"] >= 2
+    assert info["dir_err"] <= tol and info["dirdiag_err"] <= tol and info["mg_levels"] >= 2
     # SFC_treeSort(TS_REMOVE_DUPLICATES) of the messy copy gives back the balanced octree
     assert np.array_equal(_read(pre + ".sorted"), bal) and info["inplace_sorted"] == 1
