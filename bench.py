@@ -379,18 +379,41 @@ def run_serving(args, local, barrier):
     for c in ctxs:
         c.profile(False)
     batches = list(srv.batches)
-    # the same stream from pinned host memory (copies in, results out)
-    e2e_walls = []
+    # the same stream from pinned host memory: every request's points copied
+    # in, and its FP64 solution vector copied back to pinned host memory
+    e2e_walls, d2h = [], 0
     if not args.skip_e2e:
+        srv.keep = "solution"
         replay(srv, pinned)
         for _ in range(args.steps):
-            _, wall = replay(srv, pinned)
+            out_e, wall = replay(srv, pinned)
             e2e_walls.append(wall)
+        d2h = sum(r.solution.nbytes for r in out_e)
+        assert all(r.solution is not None and len(r.solution) > 0 for r in out_e)
+        srv.keep = ""
+    # the reference arm's own sample (the stream's requests of at most
+    # REF_MAX_POINTS points, as many as the host has cores), all arriving at
+    # once, so the CPU and GPU figures compare the same inputs
+    same = _ref_tasks(os.cpu_count() or 1)
+    same_pts = sum(len(r.points) for r in same)
+    same_dev = [torch.from_numpy(r.points).to(dev) for r in same]
+
+    def replay_same(server):
+        reqs = [serving.Request(i, 0.0, c) for i, c in enumerate(same_dev)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        server.run(reqs)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    replay_same(srv)
+    same_served = min(replay_same(srv) for _ in range(3))
     tune = sorted({ln for c in [srv.ctx] + srv.worker_ctx for ln in c.autotune_log().splitlines()})
     srv.close()
     # the per-call drop-in on the same stream
     p_walls, p_outs = [], []
     plain_build_s = None
+    same_plain = None
     if not args.skip_plain:
         plain = serving.PlainServer(device=local, solve_maxit=SOLVE_MAXIT)
         replay(plain, on_dev)
@@ -398,6 +421,7 @@ def run_serving(args, local, barrier):
             out, wall = replay(plain, on_dev)
             p_walls.append(wall)
             p_outs.extend(out)
+        same_plain = min(replay_same(plain) for _ in range(2))
         plain.close()
         plain_build_s = sum(r.t_built - r.t_admit for r in p_outs) / 2
     errors = sum(1 for r in outs + p_outs if r.error)
@@ -415,6 +439,11 @@ def run_serving(args, local, barrier):
         "iterations_max": max(r.iterations for r in outs),
         "relres_max": max(r.relres for r in outs),
         "errors": errors,
+        "d2h_bytes_per_step": d2h,
+        "served_same_sample": {"requests": len(same), "points": same_pts,
+                               "served_Mpts_per_s": same_pts / same_served / 1e6,
+                               "plain_Mpts_per_s": (same_pts / same_plain / 1e6) if same_plain else None,
+                               "note": "the reference arm's sample (all requests at once), served on the GPU"},
         "stats": stats,
         "clocks": clocks,
         "autotune": tune,
@@ -847,7 +876,9 @@ def run_ours(args):
             "solve_relres_max": serve["relres_max"],
             "request_errors": serve["errors"],
             "e2e": {"value": replica_value(ws, serve["points"], e2e_ms), "unit": "Mpts/s",
-                    "h2d_bytes_per_step": 24 * serve["points"], "d2h_bytes_per_step": 24 * serve["requests"]},
+                    "h2d_bytes_per_step": 24 * serve["points"], "d2h_bytes_per_step": serve["d2h_bytes_per_step"],
+                    "d2h": "each request's FP64 solution vector, into pinned host memory"},
+            "served_same_sample": serve["served_same_sample"],
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": tname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,

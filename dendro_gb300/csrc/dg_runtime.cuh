@@ -9,6 +9,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <map>
 #include <mutex>
 #include <set>
@@ -232,6 +233,48 @@ inline void prof_resolve(Context &c) {
   }
   c.prof_pending.clear();
 }
+
+// A CUDA graph captured from the launches a function makes on one stream,
+// then replayed with cudaGraphLaunch.  capture() records in thread-local
+// mode (other host threads keep launching on their own streams); a failure
+// to capture or instantiate leaves exec null, and the caller launches the
+// work directly instead.
+struct CudaGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  CudaGraph() = default;
+  CudaGraph(const CudaGraph &) = delete;
+  CudaGraph &operator=(const CudaGraph &) = delete;
+  ~CudaGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+  template <typename F>
+  void capture(cudaStream_t s, F &&work) {
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    std::exception_ptr failed;
+    try {
+      work();
+    } catch (...) {
+      failed = std::current_exception();
+    }
+    cudaGraph_t g = nullptr;
+    if (cudaStreamEndCapture(s, &g) != cudaSuccess || failed) {
+      cudaGetLastError();
+      if (g) cudaGraphDestroy(g);
+      if (failed) std::rethrow_exception(failed);  // the work itself failed: report it as the eager path would
+      return;
+    }
+    graph = g;
+    if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+      cudaGetLastError();
+      exec = nullptr;
+    }
+  }
+};
 
 // read and clear the device error word; throw on any flag
 void check_device_flags(Context &ctx, const char *where);

@@ -48,6 +48,12 @@ class Request:
     solution_norm: float = 0.0
     t_setup: float = 0.0        # multigrid set-up seconds (mesh hierarchy)
     error: str = ""
+    # results handed back to the caller (filled when the server keeps them):
+    # the balanced octree's {x, y, z, level} records, and the FP64 solution
+    # with the coordinates of its nodes (level-0 numbering of the request)
+    octree: np.ndarray | None = None
+    solution: np.ndarray | None = None
+    node_xyz: np.ndarray | None = None
 
     @property
     def latency(self) -> float:
@@ -99,26 +105,40 @@ def poisson_stream(count: int, rate: float = 200.0, lo: float = 1e4, hi: float =
     return reqs
 
 
-def _solve(ctx: Context, bal, req: Request, maxit: int, max_coarse: int, stream=None):
+def _solve(ctx: Context, bal, req: Request, maxit: int, max_coarse: int, stream=None, keep: str = ""):
     """Mesh + multigrid + FP32-V-cycle CG for one balanced octree, all on the
     device: the right-hand side field is evaluated at the device-resident
-    node coordinates, and only the iteration count, the residual and the
-    solution norm come back to the host.  ``stream``: the torch stream for
-    the field evaluation (synchronised before the library reads it)."""
+    node coordinates.  The iteration count, the residual and the solution
+    norm always come back to the host; ``keep`` names what else does:
+    "solution" (the FP64 solution vector, into pinned host memory) and
+    "octree" (the balanced octree records and the node coordinates).
+    ``stream``: the torch stream for the field evaluation (synchronised
+    before the library reads it)."""
     import torch
 
     t0 = time.perf_counter()
+    if "octree" in keep:
+        req.octree = bal.to_numpy()
     mg = MultiGrid(bal, max_coarse_elems=max_coarse, ctx=ctx)
     try:
         req.t_setup = time.perf_counter() - t0
         with torch.cuda.stream(stream or torch.cuda.current_stream(ctx.device)):
-            f = datagen.bumps(mg.level_nodes(0, device=True))
+            nodes = mg.level_nodes(0, device=True)
+            f = datagen.bumps(nodes)
             torch.cuda.current_stream(ctx.device).synchronize()
         b = mg.rhs(f)
         x, it, rr = mg.solve(b, precision=32, rtol=1e-8, maxit=maxit)
         req.iterations, req.relres = it, rr
         with torch.cuda.stream(stream or torch.cuda.current_stream(ctx.device)):
             req.solution_norm = float(torch.linalg.vector_norm(x))
+            if "solution" in keep:
+                host = torch.empty(x.shape, dtype=x.dtype, pin_memory=True)
+                host.copy_(x, non_blocking=True)
+            if "octree" in keep:
+                req.node_xyz = nodes.cpu().numpy().view(np.uint32)
+            torch.cuda.current_stream(ctx.device).synchronize()
+            if "solution" in keep:
+                req.solution = host.numpy()
     finally:
         mg.free()
 
@@ -134,9 +154,10 @@ def _host_or_device(points):
 class PlainServer:
     """One request at a time through the single-cloud API."""
 
-    def __init__(self, device: int = 0, solve_maxit: int = 50, max_coarse: int = 4096):
+    def __init__(self, device: int = 0, solve_maxit: int = 50, max_coarse: int = 4096, keep: str = ""):
         self.ctx = Context(device)
         self.maxit, self.max_coarse = solve_maxit, max_coarse
+        self.keep = keep  # results copied back per request (see _solve)
 
     def run(self, reqs: list) -> list:
         t0 = time.perf_counter()
@@ -151,7 +172,7 @@ class PlainServer:
             lin.free()
             r.t_built = time.perf_counter() - t0
             try:
-                _solve(self.ctx, bal, r, self.maxit, self.max_coarse)
+                _solve(self.ctx, bal, r, self.maxit, self.max_coarse, keep=self.keep)
             except Exception as e:  # reported per request
                 r.error = str(e)
             bal.free()
@@ -167,7 +188,8 @@ class BatchingServer:
     construction + balance per batch, solves overlapped on worker streams."""
 
     def __init__(self, device: int = 0, hbm_budget: int = 64 << 30, workers: int = 3, solve_maxit: int = 50,
-                 max_coarse: int = 4096, max_batch_points: int = 64_000_000):
+                 max_coarse: int = 4096, max_batch_points: int = 64_000_000, keep: str = ""):
+        self.keep = keep  # results copied back per request (see _solve)
         self.ctx = Context(device)
         self.worker_ctx = [Context(device) for _ in range(workers)]
         self.budget, self.maxit, self.max_coarse = hbm_budget, solve_maxit, max_coarse
@@ -192,7 +214,7 @@ class BatchingServer:
                 return
             req, bal, nbytes = item
             try:
-                _solve(ctx, bal, req, self.maxit, self.max_coarse, stream)
+                _solve(ctx, bal, req, self.maxit, self.max_coarse, stream, keep=self.keep)
             except Exception as e:  # reported per request
                 req.error = str(e)
             finally:
