@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <array>
+#include <cmath>
 #include <vector>
 
 namespace dg {
@@ -54,16 +55,28 @@ __host__ __device__ __forceinline__ Key128 seg_key(uint64_t seg, unsigned D) {
 // ------------------------------------------------------------------------
 // quantize + Morton key (construct.cpp:930-942)
 // ------------------------------------------------------------------------
+// (unsigned int)(x * (double)(1u << D) / gLen): multiply, divide, truncate.
+// When every gLen is a power of two (the unit cube of the workloads), its
+// reciprocal is exact and x * 2^D * (1 / gLen) is the same correctly rounded
+// value as the division (both round the same exact quotient), without the
+// FP64 divide.
+template <bool POW2>
 __global__ void k_quantize(const double *__restrict__ xyz, size_t n, double scale, double gx, double gy, double gz,
                            unsigned D, const uint64_t *__restrict__ seg_start, size_t nseg, Key128 *__restrict__ keys,
                            uint32_t *flags) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
-  // (unsigned int)(x * (double)(1u << D) / gLen): multiply, divide, truncate
-  double qx = __ddiv_rn(__dmul_rn(x, scale), gx);
-  double qy = __ddiv_rn(__dmul_rn(y, scale), gy);
-  double qz = __ddiv_rn(__dmul_rn(z, scale), gz);
+  double qx, qy, qz;
+  if constexpr (POW2) {  // gx, gy, gz hold the exact reciprocals here
+    qx = __dmul_rn(__dmul_rn(x, scale), gx);
+    qy = __dmul_rn(__dmul_rn(y, scale), gy);
+    qz = __dmul_rn(__dmul_rn(z, scale), gz);
+  } else {
+    qx = __ddiv_rn(__dmul_rn(x, scale), gx);
+    qy = __ddiv_rn(__dmul_rn(y, scale), gy);
+    qz = __ddiv_rn(__dmul_rn(z, scale), gz);
+  }
   // valid iff the truncated value lies in [0, 2^D): q in (-1, 2^D); NaN fails
   bool ok = (qx > -1.0) && (qx < scale) && (qy > -1.0) && (qy < scale) && (qz > -1.0) && (qz < scale);
   uint32_t ux = 0, uy = 0, uz = 0;
@@ -278,8 +291,18 @@ static void quantize_sorted(Context &ctx, const double *d_xyz, size_t n, const d
   tmp.alloc(n, ctx.stream);
   {
     ProfScope _prof(ctx, "quantize", (double)n * 40);
-    k_quantize<<<grid_for(n, 256), 256, 0, ctx.stream>>>(d_xyz, n, (double)(1u << D), g[0], g[1], g[2], D,
-                                                         d_seg_start, nseg, keys.get(), ctx.d_flags);
+    // a power of two whose reciprocal is a normal double
+    auto pow2 = [](double v) {
+      int e = 0;
+      return std::frexp(v, &e) == 0.5 && e > -1020 && e < 1020;
+    };
+    if (pow2(g[0]) && pow2(g[1]) && pow2(g[2]))
+      k_quantize<true><<<grid_for(n, 256), 256, 0, ctx.stream>>>(d_xyz, n, (double)(1u << D), 1.0 / g[0], 1.0 / g[1],
+                                                                 1.0 / g[2], D, d_seg_start, nseg, keys.get(),
+                                                                 ctx.d_flags);
+    else
+      k_quantize<false><<<grid_for(n, 256), 256, 0, ctx.stream>>>(d_xyz, n, (double)(1u << D), g[0], g[1], g[2], D,
+                                                                  d_seg_start, nseg, keys.get(), ctx.d_flags);
     DG_LAUNCH_CHECK();
   }
   check_device_flags(ctx, "points2Octree");
@@ -333,8 +356,8 @@ void points_to_octree(Context &ctx, const double *d_xyz, size_t n, const double 
       DBuf<Key128> keys(n, s);
       {
         ProfScope _prof(ctx, "quantize", (double)n * 40);
-        k_quantize<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, (double)(1u << D), g[0], g[1], g[2], D, nullptr, 1,
-                                                    keys.get(), ctx.d_flags);
+        k_quantize<false><<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, (double)(1u << D), g[0], g[1], g[2], D, nullptr,
+                                                           1, keys.get(), ctx.d_flags);
         DG_LAUNCH_CHECK();
       }
       check_device_flags(ctx, "points2Octree");

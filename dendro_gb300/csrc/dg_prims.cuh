@@ -383,8 +383,10 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_digit_hists(const K *__restrict
 // running counters order the rounds), placed in shared memory in digit
 // order, then written out so that consecutive threads write consecutive
 // addresses of each digit's run.
-template <typename K, int ITEMS = OsCfg<K>::ITEMS>
-__global__ void __launch_bounds__(RS_BLOCK, 4) k_rs_onesweep(const K *__restrict__ in, K *__restrict__ out, size_t n,
+// MINB: blocks per SM the kernel is compiled for (register budget); the
+// autotuner picks the tile and MINB per size class.
+template <typename K, int ITEMS = OsCfg<K>::ITEMS, int MINB = 4>
+__global__ void __launch_bounds__(RS_BLOCK, MINB) k_rs_onesweep(const K *__restrict__ in, K *__restrict__ out, size_t n,
                                                           int shift, const uint64_t *__restrict__ digit_off,
                                                           uint64_t *__restrict__ status, unsigned *tile_counter,
                                                           uint32_t *flags) {
@@ -509,13 +511,56 @@ K *radix_sort(Context &ctx, K *keys, K *tmp, size_t n, int end_bit) {
   DBuf<unsigned long long> ghist(npass * 256, s);
   DBuf<int> dshifts(npass, s);
   DG_CUDA(cudaMemcpyAsync(dshifts.get(), shifts, npass * sizeof(int), cudaMemcpyHostToDevice, s));
-  DG_CUDA(cudaMemsetAsync(ghist.get(), 0, npass * 256 * sizeof(unsigned long long), s));
-  {
+  // launch shape of this size class: the context's decision, else the
+  // disk cache's, else tuned below
+  const int width = sizeof(K) == 16 ? 1 : 0;
+  int bucket = 0;
+  while (bucket < 63 && ((size_t)2 << bucket) <= n) bucket++;
+  Context::Tune &tn = ctx.tune[width][bucket];
+  const bool tunable = n >= OS_TUNE_MIN;
+  if (tunable && tn.items == 0 && tune_cache_get(ctx.device, width, bucket, &tn)) {
+    char line[160];
+    std::snprintf(line, sizeof(line), "onesweep %d-byte keys, 2^%d: %d keys/thread, %d blocks/SM, histogram %d "
+                  "blocks/SM (disk cache)\n", (int)sizeof(K), bucket, tn.items, tn.minb, tn.hist_mul);
+    ctx.tune_log += line;
+  }
+  const bool tuning = tunable && tn.items == 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (tuning) {
+    DG_CUDA(cudaEventCreate(&e0));
+    DG_CUDA(cudaEventCreate(&e1));
+  }
+  // best of two timings: other streams sharing the GPU can slow any one
+  auto time2 = [&](auto &&launch) {
+    float best = 0.f;
+    for (int rep = 0; rep < 2; rep++) {
+      float t = 0.f;
+      DG_CUDA(cudaEventRecord(e0, s));
+      launch();
+      DG_CUDA(cudaEventRecord(e1, s));
+      DG_CUDA(cudaEventSynchronize(e1));
+      DG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+      best = rep == 0 ? t : std::min(best, t);
+    }
+    return best;
+  };
+  auto hists = [&](int mul) {
+    DG_CUDA(cudaMemsetAsync(ghist.get(), 0, npass * 256 * sizeof(unsigned long long), s));
     ProfScope _prof(ctx, "rs_digit_hists", (double)n * sizeof(K));
-    unsigned g = grid_for(n, RS_BLOCK, (unsigned)(ctx.num_sms * 4));
+    unsigned g = grid_for(n, RS_BLOCK, (unsigned)(ctx.num_sms * mul));
     k_rs_digit_hists<K><<<g, RS_BLOCK, 0, s>>>(keys, n, npass, dshifts.get(), ghist.get());
     DG_LAUNCH_CHECK();
+  };
+  float hist_ms[3] = {0.f, 0.f, 0.f};
+  const int hist_cand[3] = {2, 4, 8};
+  if (tuning) {
+    for (int c = 0; c < 3; c++) hist_ms[c] = time2([&]() { hists(hist_cand[c]); });
+    int b = 0;
+    for (int c = 1; c < 3; c++)
+      if (hist_ms[c] < hist_ms[b]) b = c;
+    tn.hist_mul = hist_cand[b];
   }
+  hists(tn.hist_mul ? tn.hist_mul : 4);
   std::vector<unsigned long long> h(npass * 256);
   DG_CUDA(cudaMemcpyAsync(h.data(), ghist.get(), h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
   DG_CUDA(cudaStreamSynchronize(s));
@@ -532,68 +577,80 @@ K *radix_sort(Context &ctx, K *keys, K *tmp, size_t n, int end_bit) {
       run += h[p * 256 + d];
     }
   }
-  if (active.empty()) return keys;
+  if (active.empty()) {
+    if (tuning) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      tn = Context::Tune();  // nothing to sort here: decide on a later sort of this size
+    }
+    return keys;
+  }
   DBuf<uint64_t> doffs(offs.size(), s);
   DG_CUDA(cudaMemcpyAsync(doffs.get(), offs.data(), offs.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
   const size_t max_tiles = (n + RS_BLOCK * OsAlt<K>::ITEMS - 1) / (RS_BLOCK * OsAlt<K>::ITEMS);
   if (max_tiles >= 0xffffffffull) fail(DG_ERR_INVALID_ARG, "radix sort: too many keys");
   DBuf<uint64_t> status(max_tiles * 256, s);
   unsigned *d_counter = reinterpret_cast<unsigned *>(ctx.d_scratch + 12);
-  // one digit pass with `items` keys per thread
-  auto pass = [&](int items, const K *src, K *dst, size_t a) {
+  // one digit pass with `items` keys per thread, compiled for `minb` blocks
+  // per SM
+  auto pass = [&](int items, int minb, const K *src, K *dst, size_t a) {
     const size_t tile = (size_t)RS_BLOCK * items, ntiles = (n + tile - 1) / tile;
     DG_CUDA(cudaMemsetAsync(status.get(), 0, ntiles * 256 * sizeof(uint64_t), s));
     DG_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s));
     ProfScope _prof(ctx, "rs_onesweep", (double)n * sizeof(K) * 2);
-    if (items == OsCfg<K>::ITEMS)
-      k_rs_onesweep<K, OsCfg<K>::ITEMS><<<(unsigned)ntiles, RS_BLOCK, 0, s>>>(
-          src, dst, n, shifts[active[a]], doffs.get() + 256 * a, status.get(), d_counter, ctx.d_flags);
+    const int sh = shifts[active[a]];
+    const uint64_t *off = doffs.get() + 256 * a;
+    const unsigned g = (unsigned)ntiles;
+    if (items == OsCfg<K>::ITEMS && minb == 3)
+      k_rs_onesweep<K, OsCfg<K>::ITEMS, 3><<<g, RS_BLOCK, 0, s>>>(src, dst, n, sh, off, status.get(), d_counter,
+                                                                  ctx.d_flags);
+    else if (items == OsCfg<K>::ITEMS && minb == 5)
+      k_rs_onesweep<K, OsCfg<K>::ITEMS, 5><<<g, RS_BLOCK, 0, s>>>(src, dst, n, sh, off, status.get(), d_counter,
+                                                                  ctx.d_flags);
+    else if (items == OsCfg<K>::ITEMS)
+      k_rs_onesweep<K, OsCfg<K>::ITEMS, 4><<<g, RS_BLOCK, 0, s>>>(src, dst, n, sh, off, status.get(), d_counter,
+                                                                  ctx.d_flags);
     else
-      k_rs_onesweep<K, OsAlt<K>::ITEMS><<<(unsigned)ntiles, RS_BLOCK, 0, s>>>(
-          src, dst, n, shifts[active[a]], doffs.get() + 256 * a, status.get(), d_counter, ctx.d_flags);
+      k_rs_onesweep<K, OsAlt<K>::ITEMS, 4><<<g, RS_BLOCK, 0, s>>>(src, dst, n, sh, off, status.get(), d_counter,
+                                                                  ctx.d_flags);
     DG_LAUNCH_CHECK();
   };
-  // autotuner: the first sort of each size (log2 of the key count) times both
-  // tiles on its first digit pass (the pass is stable, so every run writes
-  // the same output) and keeps the faster for every later pass and sort of
-  // that size on this context
-  const int width = sizeof(K) == 16 ? 1 : 0;
-  int bucket = 0;
-  while (bucket < 63 && ((size_t)2 << bucket) <= n) bucket++;
-  int &items = ctx.tune_items[width][bucket];
+  // autotuner: the first sort of each size class (log2 of the key count)
+  // times every onesweep shape on its first digit pass (the pass is stable,
+  // so every run writes the same output) and keeps the fastest for every
+  // later pass and sort of that class
   K *src = keys, *dst = tmp;
   size_t a0 = 0;
-  if (items == 0 && n >= OS_TUNE_MIN) {
-    const int cand[2] = {OsCfg<K>::ITEMS, OsAlt<K>::ITEMS};
-    float ms[2] = {0.f, 0.f};
-    cudaEvent_t e0, e1;
-    DG_CUDA(cudaEventCreate(&e0));
-    DG_CUDA(cudaEventCreate(&e1));
-    // two timings per tile, the faster kept: other streams sharing the GPU
-    // can slow any single one
-    for (int rep = 0; rep < 2; rep++)
-      for (int c = 0; c < 2; c++) {
-        float t = 0.f;
-        DG_CUDA(cudaEventRecord(e0, s));
-        pass(cand[c], src, dst, 0);
-        DG_CUDA(cudaEventRecord(e1, s));
-        DG_CUDA(cudaEventSynchronize(e1));
-        DG_CUDA(cudaEventElapsedTime(&t, e0, e1));
-        ms[c] = rep == 0 ? t : std::min(ms[c], t);
-      }
+  if (tuning) {
+    struct Cand {
+      int items, minb;
+    };
+    const Cand cand[4] = {{OsCfg<K>::ITEMS, 4}, {OsAlt<K>::ITEMS, 4}, {OsCfg<K>::ITEMS, 3}, {OsCfg<K>::ITEMS, 5}};
+    float ms[4];
+    int b = 0;
+    for (int c = 0; c < 4; c++) {
+      ms[c] = time2([&]() { pass(cand[c].items, cand[c].minb, src, dst, 0); });
+      if (ms[c] < ms[b]) b = c;
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    items = ms[1] < ms[0] ? cand[1] : cand[0];
-    char line[160];
-    std::snprintf(line, sizeof(line), "onesweep %d-byte keys, 2^%d: %d keys/thread (%.3f ms) vs %d (%.3f ms) -> %d\n",
-                  (int)sizeof(K), bucket, cand[0], ms[0], cand[1], ms[1], items);
+    tn.items = cand[b].items;
+    tn.minb = cand[b].minb;
+    char line[320];
+    std::snprintf(line, sizeof(line),
+                  "onesweep %d-byte keys, 2^%d: keys/thread x blocks/SM %dx%d %.3f ms, %dx%d %.3f, %dx%d %.3f, "
+                  "%dx%d %.3f -> %dx%d; histogram blocks/SM 2/4/8 %.3f/%.3f/%.3f ms -> %d\n",
+                  (int)sizeof(K), bucket, cand[0].items, cand[0].minb, ms[0], cand[1].items, cand[1].minb, ms[1],
+                  cand[2].items, cand[2].minb, ms[2], cand[3].items, cand[3].minb, ms[3], tn.items, tn.minb,
+                  hist_ms[0], hist_ms[1], hist_ms[2], tn.hist_mul);
     ctx.tune_log += line;
+    tune_cache_put(ctx.device, width, bucket, tn);
     std::swap(src, dst);
     a0 = 1;
   }
-  const int use = items ? items : OsCfg<K>::ITEMS;
+  const int use = tn.items ? tn.items : OsCfg<K>::ITEMS, use_minb = tn.minb ? tn.minb : 4;
   for (size_t a = a0; a < active.size(); a++) {
-    pass(use, src, dst, a);
+    pass(use, use_minb, src, dst, a);
     K *t = src;
     src = dst;
     dst = t;

@@ -61,9 +61,13 @@ struct Context {
   std::map<std::string, ProfStat> prof_stats;
   std::vector<ProfPending> prof_pending;
   std::vector<cudaEvent_t> prof_pool;
-  // autotuner: onesweep tile per (key width: 0 = 8 bytes, 1 = 16 bytes,
-  // log2 of the key count); 0 = not tuned yet, else the items per thread
-  int tune_items[2][64] = {};
+  // autotuner: the radix sort's launch shape per (key width: 0 = 8 bytes,
+  // 1 = 16 bytes, log2 of the key count); items == 0: not tuned yet
+  struct Tune {
+    int items = 0;     // keys per thread of a onesweep tile
+    int minb = 0;      // onesweep blocks per SM the kernel is compiled for
+    int hist_mul = 0;  // digit-histogram blocks per SM
+  } tune[2][64];
   std::string tune_log;  // one line per decision
   // order of octant records at the boundary (downloads, uploads, files):
   // 0 Morton, 1 Hilbert (the reference's HILBERT_ORDERING builds); the
@@ -278,5 +282,15 @@ struct CudaGraph {
 
 // read and clear the device error word; throw on any flag
 void check_device_flags(Context &ctx, const char *where);
+
+// Persistent autotuner decisions, shared by the contexts of a process and
+// kept on disk between processes, keyed by the device (name, SM count,
+// compute capability) and the size class.  The file is
+// $DENDRO_GB300_TUNE_CACHE when set (an empty value turns the disk cache
+// off), else $XDG_CACHE_HOME/dendro_gb300/autotune.tsv or
+// $HOME/.cache/dendro_gb300/autotune.tsv.  I/O failures only lose the cache.
+bool tune_cache_get(int device, int width, int bucket, Context::Tune *out);
+void tune_cache_put(int device, int width, int bucket, const Context::Tune &t);
+std::string tune_cache_path();
 
 }  // namespace dg
