@@ -594,6 +594,7 @@ K *radix_sort(Context &ctx, K *keys, K *tmp, size_t n, int end_bit) {
   // one digit pass with `items` keys per thread, compiled for `minb` blocks
   // per SM
   auto pass = [&](int items, int minb, const K *src, K *dst, size_t a) {
+    if (items != OsCfg<K>::ITEMS) items = OsAlt<K>::ITEMS;  // the two compiled tiles
     const size_t tile = (size_t)RS_BLOCK * items, ntiles = (n + tile - 1) / tile;
     DG_CUDA(cudaMemsetAsync(status.get(), 0, ntiles * 256 * sizeof(uint64_t), s));
     DG_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s));

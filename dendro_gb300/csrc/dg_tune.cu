@@ -70,8 +70,11 @@ void load_locked() {
     t.minb = std::atoi(mb.c_str());
     t.hist_mul = std::atoi(hm.c_str());
     const int wi = std::atoi(w.c_str()), bi = std::atoi(b.c_str());
-    const bool valid = (wi == 0 || wi == 1) && bi >= 0 && bi < 64 && t.items > 0 && t.minb >= 3 && t.minb <= 5 &&
-                       (t.hist_mul == 2 || t.hist_mul == 4 || t.hist_mul == 8);
+    // only shapes the library compiles: 16 or 8 keys per thread for 8-byte
+    // keys, 8 or 4 for 16-byte keys; 3 to 5 blocks per SM
+    const int big = wi == 0 ? 16 : 8;
+    const bool valid = (wi == 0 || wi == 1) && bi >= 0 && bi < 64 && (t.items == big || t.items == big / 2) &&
+                       t.minb >= 3 && t.minb <= 5 && (t.hist_mul == 2 || t.hist_mul == 4 || t.hist_mul == 8);
     if (valid) g_tune[std::make_tuple(key, wi, bi)] = t;
   }
 }
