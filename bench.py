@@ -428,6 +428,32 @@ def run_serving(args, local, barrier):
         same_plain = min(replay_same(plain) for _ in range(2))
         plain.close()
         plain_build_s = sum(r.t_built - r.t_admit for r in p_outs) / 2
+    # build + balance requests only (the benchmark spec's served-vs-plain figure
+    # for construction and balance), on the same clouds: with the stream's
+    # Poisson arrivals, and as a burst (every request waiting at the start,
+    # the servers' capacity)
+    def replay_build(server, burst):
+        reqs = [serving.Request(r.rid, 0.0 if burst else r.arrival, c) for r, c in zip(host, on_dev)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = server.run(reqs)
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    build_only = {}
+    sb = serving.BatchingServer(device=local, workers=1, solve=False)
+    pb = serving.PlainServer(device=local, solve=False)
+    for mode in ("poisson", "burst"):
+        row = {}
+        for name, server in (("served", sb), ("plain", pb)):
+            replay_build(server, mode == "burst")
+            runs = [replay_build(server, mode == "burst") for _ in range(3)]
+            out_b, wall_b = min(runs, key=lambda t: t[1])
+            row[name] = {"Mpts_per_s": npts / wall_b / 1e6, **_latency(out_b)}
+        row["served_over_plain"] = row["served"]["Mpts_per_s"] / row["plain"]["Mpts_per_s"]
+        build_only[mode] = row
+    sb.close()
+    pb.close()
     errors = sum(1 for r in outs + p_outs if r.error)
     ms = 1e3 * sum(walls) / len(walls)
     res = {
@@ -444,6 +470,7 @@ def run_serving(args, local, barrier):
         "relres_max": max(r.relres for r in outs),
         "errors": errors,
         "d2h_bytes_per_step": d2h,
+        "build_balance_only": build_only,
         "served_same_sample": {"requests": len(same), "points": same_pts,
                                "served_Mpts_per_s": same_pts / same_served / 1e6,
                                "plain_Mpts_per_s": (same_pts / same_plain / 1e6) if same_plain else None,
@@ -884,6 +911,9 @@ def run_ours(args):
                     "h2d_bytes_per_step": 24 * serve["points"], "d2h_bytes_per_step": serve["d2h_bytes_per_step"],
                     "d2h": "each request's FP64 solution vector, into pinned host memory"},
             "served_same_sample": serve["served_same_sample"],
+            "serving_build_balance": {**serve["build_balance_only"],
+                                      "note": ("requests of build + balance only, same clouds; burst = every "
+                                               "request waiting at the start")},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": tname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,

@@ -205,16 +205,23 @@ __global__ void k_set_bdy_identity(const uint8_t *__restrict__ bdy, size_t n, do
 // In-place block Gauss-Jordan (no pivoting: the operator is SPD).  For each
 // block K of GJB pivots, with R the other indices and P = inv(X_KK):
 //   X_RR -= (X_RK P) X_KR,  X_KR = P X_KR,  X_RK = -(X_RK P),  X_KK = P;
-// after the last block X holds the inverse.  The X_RR update is a tiled
-// rank-GJB product, so the inverse costs n^3 FP32 multiply-adds in n / GJB
-// steps of five launches.
+// after the last block X holds the inverse (n^3 FP32 multiply-adds).
+// Each block costs two launches: k_bgj_diag inverts X_KK (one CTA), then
+// k_bgj_step updates every 64 x 64 tile at once.  So that no tile is
+// overwritten while another CTA of the same launch still reads it, the new
+// row K and column K go to scratch strips (R: GJB x n, C: n x GJB,
+// double-buffered by block parity) and reach X one block later: a tile in
+// the previous block's row or column is read from its strip, and
+// k_bgj_flush writes the last strips into X.
 constexpr int GJB = 64;
+constexpr int GJT = 64 + 4;  // shared tile row stride (floats)
 
 // P = inv(X_KK) for one diagonal block (one CTA of 256 threads): thread t
 // holds 16 entries of row t / 4 in registers; per pivot the pivot row goes
 // through shared memory (double-buffered, one barrier) and each row's pivot
 // column entry comes by a shuffle within the row's four threads.  A partial
-// last block is padded with the identity.
+// last block is padded with the identity; P is written as a full GJB x GJB
+// block.
 __global__ void __launch_bounds__(256) k_bgj_diag(const float *__restrict__ X, size_t n, size_t k0, int b,
                                                   float *__restrict__ P) {
   static_assert(GJB == 64, "one CTA of 256 threads covers a 64 x 64 block");
@@ -244,53 +251,43 @@ __global__ void __launch_bounds__(256) k_bgj_diag(const float *__restrict__ X, s
       else v[i] = (c == p) ? -f * inv : v[i] - f * pr[c] * inv;
     }
   }
-  if (r < b) {
 #pragma unroll
-    for (int i = 0; i < 16; i++)
-      if (c0 + i < b) P[r * b + c0 + i] = v[i];
+  for (int i = 0; i < 16; i++) P[r * GJB + c0 + i] = v[i];
+}
+
+// where tile entries live while the block steps run: X, or the strips of
+// the previous block pk (R rows k0p.., C columns k0p..); 0 outside n x n
+struct GjSrc {
+  const float *X, *R, *C;
+  size_t n;
+  long pk;  // previous block's tile index, -1 before the first block
+  __device__ __forceinline__ float at(size_t i, size_t j) const {
+    if (i >= n || j >= n) return 0.f;
+    if ((long)(i / GJB) == pk) return R[(i % GJB) * n + j];
+    if ((long)(j / GJB) == pk) return C[i * GJB + (j % GJB)];
+    return X[i * n + j];
+  }
+};
+
+// shared tile T[m][r] = src(i0 + r, j0 + m) (transposed) or T[m][c] =
+// src(i0 + m, j0 + c) (as is)
+__device__ __forceinline__ void gj_load(float *T, const GjSrc &src, size_t i0, size_t j0, bool transposed) {
+  for (int q = threadIdx.x; q < 64 * 64; q += 256) {
+    const int a = q / 64, bb = q % 64;  // a: row of the source tile, bb: its column
+    const float v = src.at(i0 + a, j0 + bb);
+    if (transposed) T[bb * GJT + a] = v;
+    else T[a * GJT + bb] = v;
   }
 }
 
-// U[i][:] = X[i][K] P for rows i outside K (one block of GJB threads per row)
-__global__ void k_bgj_u(const float *__restrict__ X, size_t n, size_t k0, int b, const float *__restrict__ P,
-                        float *__restrict__ U) {
-  const size_t i = blockIdx.x;
-  if (i >= k0 && i < k0 + (size_t)b) return;
-  __shared__ float xs[GJB];
-  const int j = threadIdx.x;
-  if (j < b) xs[j] = X[i * n + k0 + j];
-  __syncthreads();
-  if (j < b) {
-    float acc = 0.f;
-    for (int m = 0; m < b; m++) acc += xs[m] * P[m * b + j];
-    U[i * GJB + j] = acc;
-  }
-}
-
-// X[i][j] -= sum_m U[i][m] X[K_m][j] for i, j outside K: 64 x 64 tiles, 4 x 4 per thread
-__global__ void __launch_bounds__(256) k_bgj_update(float *__restrict__ X, size_t n, size_t k0, int b,
-                                                    const float *__restrict__ U) {
-  __shared__ __align__(16) float Ut[GJB][64 + 4];
-  __shared__ __align__(16) float Bs[GJB][64 + 4];
-  const size_t i0 = (size_t)blockIdx.y * 64, j0 = (size_t)blockIdx.x * 64;
-  const int tid = threadIdx.x;
-  for (int q = tid; q < 64 * GJB; q += 256) {
-    const int r = q / GJB, m = q % GJB;
-    Ut[m][r] = (m < b && i0 + r < n) ? U[(i0 + r) * GJB + m] : 0.f;
-  }
-  for (int q = tid; q < GJB * 64; q += 256) {
-    const int m = q / 64, c = q % 64;
-    Bs[m][c] = (m < b && j0 + c < n) ? X[(k0 + m) * n + j0 + c] : 0.f;
-  }
-  __syncthreads();
-  const int ty = tid / 16, tx = tid % 16;
-  // column pairs accumulate with the paired FMA (fma.rn.f32x2)
-  float2 acc[4][2];
-#pragma unroll
-  for (int r = 0; r < 4; r++) acc[r][0] = acc[r][1] = make_float2(0.f, 0.f);
-  for (int m = 0; m < b; m++) {
-    const float4 a = *reinterpret_cast<const float4 *>(&Ut[m][ty * 4]);
-    const float4 c4 = *reinterpret_cast<const float4 *>(&Bs[m][tx * 4]);
+// acc[4][4] += L R over the 64-deep product, L given transposed (Lt[m][r]),
+// R as is (R[m][c]); thread (ty, tx) owns rows 4ty.., columns 4tx..
+__device__ __forceinline__ void gj_mma(const float *Lt, const float *Rm, float2 (&acc)[4][2]) {
+  const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+#pragma unroll 8
+  for (int m = 0; m < 64; m++) {
+    const float4 a = *reinterpret_cast<const float4 *>(&Lt[m * GJT + ty * 4]);
+    const float4 c4 = *reinterpret_cast<const float4 *>(&Rm[m * GJT + tx * 4]);
     const float av[4] = {a.x, a.y, a.z, a.w};
     const float2 b01 = make_float2(c4.x, c4.y), b23 = make_float2(c4.z, c4.w);
 #pragma unroll
@@ -300,49 +297,96 @@ __global__ void __launch_bounds__(256) k_bgj_update(float *__restrict__ X, size_
       acc[r][1] = ffma2(ar, b23, acc[r][1]);
     }
   }
+}
+
+// One block step over every tile (ti, tj) (grid nt x nt, 256 threads,
+// three 64 x GJT shared tiles):
+//   (K, K): R = P;  (K, j): R = P X_Kj;  (i, K): C = -(X_iK P);
+//   (i, j): X_ij -= (X_iK P) X_Kj
+__global__ void __launch_bounds__(256) k_bgj_step(float *__restrict__ X, size_t n, size_t k0, GjSrc src,
+                                                  const float *__restrict__ P, float *__restrict__ Rn,
+                                                  float *__restrict__ Cn) {
+  extern __shared__ __align__(16) float gsm[];
+  float *A = gsm, *B = gsm + 64 * GJT, *Q = gsm + 2 * 64 * GJT;
+  const size_t tk = k0 / GJB, ti = blockIdx.y, tj = blockIdx.x;
+  const size_t i0 = ti * 64, j0 = tj * 64;
+  const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+  float2 acc[4][2];
+#pragma unroll
+  for (int r = 0; r < 4; r++) acc[r][0] = acc[r][1] = make_float2(0.f, 0.f);
+  if (ti == tk && tj == tk) {
+    for (int q = threadIdx.x; q < 64 * 64; q += 256) {
+      const int r = q / 64, c = q % 64;
+      if (k0 + c < n) Rn[r * n + k0 + c] = P[q];
+    }
+    return;
+  }
+  if (ti == tk) {  // R[:, j] = P X_Kj
+    for (int q = threadIdx.x; q < 64 * 64; q += 256) A[(q % 64) * GJT + q / 64] = P[q];  // P transposed
+    gj_load(B, src, k0, j0, false);
+    __syncthreads();
+    gj_mma(A, B, acc);
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const size_t j = j0 + tx * 4 + c;
+        const float v = c < 2 ? (c == 0 ? acc[r][0].x : acc[r][0].y) : (c == 2 ? acc[r][1].x : acc[r][1].y);
+        if (j < n) Rn[(size_t)(ty * 4 + r) * n + j] = v;
+      }
+    return;
+  }
+  // U = X_iK P (the (i, K) tile's new value is -U)
+  gj_load(A, src, i0, k0, true);
+  for (int q = threadIdx.x; q < 64 * 64; q += 256) Q[(q / 64) * GJT + q % 64] = P[q];
+  __syncthreads();
+  gj_mma(A, Q, acc);
+  if (tj == tk) {
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const size_t i = i0 + ty * 4 + r;
+      if (i >= n) continue;
+      float4 v = make_float4(-acc[r][0].x, -acc[r][0].y, -acc[r][1].x, -acc[r][1].y);
+      *reinterpret_cast<float4 *>(&Cn[i * GJB + tx * 4]) = v;
+    }
+    return;
+  }
+  // X_ij -= U X_Kj: U goes to A transposed, X_Kj to B
+  __syncthreads();  // every thread is done reading A and Q
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    A[(tx * 4 + 0) * GJT + ty * 4 + r] = acc[r][0].x;
+    A[(tx * 4 + 1) * GJT + ty * 4 + r] = acc[r][0].y;
+    A[(tx * 4 + 2) * GJT + ty * 4 + r] = acc[r][1].x;
+    A[(tx * 4 + 3) * GJT + ty * 4 + r] = acc[r][1].y;
+    acc[r][0] = acc[r][1] = make_float2(0.f, 0.f);
+  }
+  gj_load(B, src, k0, j0, false);
+  __syncthreads();
+  gj_mma(A, B, acc);
 #pragma unroll
   for (int r = 0; r < 4; r++) {
     const size_t i = i0 + ty * 4 + r;
-    if (i >= n || (i >= k0 && i < k0 + (size_t)b)) continue;
-    const float accr[4] = {acc[r][0].x, acc[r][0].y, acc[r][1].x, acc[r][1].y};
+    if (i >= n) continue;
+    const float av[4] = {acc[r][0].x, acc[r][0].y, acc[r][1].x, acc[r][1].y};
 #pragma unroll
     for (int c = 0; c < 4; c++) {
       const size_t j = j0 + tx * 4 + c;
-      if (j < n && !(j >= k0 && j < k0 + (size_t)b)) X[i * n + j] -= accr[c];
+      if (j < n) X[i * n + j] = src.at(i, j) - av[c];
     }
   }
 }
 
-// X[K_r][j] = sum_m P[r][m] X[K_m][j] for columns j outside K (64 columns per block)
-__global__ void __launch_bounds__(256) k_bgj_row(float *__restrict__ X, size_t n, size_t k0, int b,
-                                                 const float *__restrict__ P) {
-  __shared__ float Ps[GJB][GJB + 1];
-  __shared__ float Bs[GJB][64 + 1];
-  const size_t j0 = (size_t)blockIdx.x * 64;
-  for (int q = threadIdx.x; q < b * b; q += 256) Ps[q / b][q % b] = P[q];
-  for (int q = threadIdx.x; q < b * 64; q += 256) {
-    const int m = q / 64, c = q % 64;
-    Bs[m][c] = (j0 + c < n) ? X[(k0 + m) * n + j0 + c] : 0.f;
-  }
-  __syncthreads();
-  for (int q = threadIdx.x; q < b * 64; q += 256) {
-    const int r = q / 64, c = q % 64;
-    const size_t j = j0 + c;
-    if (j >= n || (j >= k0 && j < k0 + (size_t)b)) continue;
-    float acc = 0.f;
-    for (int m = 0; m < b; m++) acc = fmaf(Ps[r][m], Bs[m][c], acc);
-    X[(k0 + r) * n + j] = acc;
-  }
-}
-
-// X[i][K] = -U[i][:] for rows outside K, X[K][K] = P
-__global__ void k_bgj_col(float *__restrict__ X, size_t n, size_t k0, int b, const float *__restrict__ P,
-                          const float *__restrict__ U) {
+// the last block's strips into X
+__global__ void k_bgj_flush(float *__restrict__ X, size_t n, size_t k0, int b, const float *__restrict__ R,
+                            const float *__restrict__ C) {
   const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n * (size_t)b) return;
+  const size_t r = q / n, j = q % n;  // row k0 + r of R
+  X[(k0 + r) * n + j] = R[r * n + j];
   const size_t i = q / b;
-  const int j = (int)(q % b);
-  X[i * n + k0 + j] = (i >= k0 && i < k0 + (size_t)b) ? P[(i - k0) * b + j] : -U[i * GJB + j];
+  const int c = (int)(q % b);  // column k0 + c of C
+  if (i < k0 || i >= k0 + (size_t)b) X[i * n + k0 + c] = C[i * GJB + c];
 }
 
 // coarse solve x = A^-1 b to FP64 accuracy: x = X b, then CS_REFINE rounds of
@@ -675,30 +719,23 @@ void mg_setup(Context &ctx, const Octree &fine, size_t max_coarse_elem, MG &mg) 
     DG_LAUNCH_CHECK();
     {
       ProfScope _prof_inv(ctx, "mg_coarse_inverse", (double)n * n * 4 * 2 * ((n + GJB - 1) / GJB));
-      DBuf<float> P(GJB * GJB, s), U(n * GJB, s);
-      const unsigned nt = (unsigned)((n + 63) / 64);
-      for (size_t k0 = 0; k0 < n; k0 += GJB) {
+      const size_t nt = (n + GJB - 1) / GJB;
+      DBuf<float> P(GJB * GJB, s), R(2 * GJB * n, s), C(2 * n * GJB, s);
+      const int smem = 3 * 64 * GJT * (int)sizeof(float);
+      ensure_smem_attr(ctx, k_bgj_step, smem);
+      long pk = -1;
+      for (size_t k0 = 0, step = 0; k0 < n; k0 += GJB, step++) {
         const int b = (int)std::min<size_t>(GJB, n - k0);
-        {
-          ProfScope _p(ctx, "bgj_diag", (double)b * b * 8);
-          k_bgj_diag<<<1, 256, 0, s>>>(mg.cinv32, n, k0, b, P.get());
-        }
-        {
-          ProfScope _p(ctx, "bgj_u", (double)n * b * 8);
-          k_bgj_u<<<(unsigned)n, GJB, 0, s>>>(mg.cinv32, n, k0, b, P.get(), U.get());
-        }
-        {
-          ProfScope _p(ctx, "bgj_update", (double)n * n * 8);
-          k_bgj_update<<<dim3(nt, nt), 256, 0, s>>>(mg.cinv32, n, k0, b, U.get());
-        }
-        {
-          ProfScope _p(ctx, "bgj_row", (double)n * b * 8);
-          k_bgj_row<<<nt, 256, 0, s>>>(mg.cinv32, n, k0, b, P.get());
-        }
-        {
-          ProfScope _p(ctx, "bgj_col", (double)n * b * 8);
-          k_bgj_col<<<grid_for(n * b, 256), 256, 0, s>>>(mg.cinv32, n, k0, b, P.get(), U.get());
-        }
+        const size_t cur = step & 1, prev = cur ^ 1;
+        k_bgj_diag<<<1, 256, 0, s>>>(mg.cinv32, n, k0, b, P.get());
+        GjSrc src{mg.cinv32, R.get() + prev * GJB * n, C.get() + prev * n * GJB, n, pk};
+        k_bgj_step<<<dim3((unsigned)nt, (unsigned)nt), 256, smem, s>>>(mg.cinv32, n, k0, src, P.get(),
+                                                                         R.get() + cur * GJB * n,
+                                                                         C.get() + cur * n * GJB);
+        pk = (long)(k0 / GJB);
+        if (k0 + GJB >= n)
+          k_bgj_flush<<<grid_for(n * (size_t)b, 256), 256, 0, s>>>(mg.cinv32, n, k0, b, R.get() + cur * GJB * n,
+                                                                   C.get() + cur * n * GJB);
       }
       DG_LAUNCH_CHECK();
     }

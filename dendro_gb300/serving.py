@@ -2,7 +2,8 @@
 
 A request carries one point cloud.  Its work is the full request of the serving workload:
 points2Octree -> balanceOctree -> mesh -> multigrid set-up -> CG with an
-FP32 V-cycle (FP64 residuals), at most ``solve_maxit`` iterations.
+FP32 V-cycle (FP64 residuals), at most ``solve_maxit`` iterations; with
+``solve=False`` a request is points2Octree -> balanceOctree only.
 
 ``PlainServer`` is the per-call drop-in: one request at a time, in arrival
 order, every call made for that cloud alone.
@@ -154,10 +155,12 @@ def _host_or_device(points):
 class PlainServer:
     """One request at a time through the single-cloud API."""
 
-    def __init__(self, device: int = 0, solve_maxit: int = 50, max_coarse: int = 4096, keep: str = ""):
+    def __init__(self, device: int = 0, solve_maxit: int = 50, max_coarse: int = 4096, keep: str = "",
+                 solve: bool = True):
         self.ctx = Context(device)
         self.maxit, self.max_coarse = solve_maxit, max_coarse
         self.keep = keep  # results copied back per request (see _solve)
+        self.solve = solve  # False: a request is points2Octree + balanceOctree only
 
     def run(self, reqs: list) -> list:
         t0 = time.perf_counter()
@@ -171,10 +174,14 @@ class PlainServer:
             r.n_octants, r.n_balanced = lin.size, bal.size
             lin.free()
             r.t_built = time.perf_counter() - t0
-            try:
-                _solve(self.ctx, bal, r, self.maxit, self.max_coarse, keep=self.keep)
-            except Exception as e:  # reported per request
-                r.error = str(e)
+            if not self.solve:
+                if "octree" in self.keep:
+                    r.octree = bal.to_numpy()
+            else:
+                try:
+                    _solve(self.ctx, bal, r, self.maxit, self.max_coarse, keep=self.keep)
+                except Exception as e:  # reported per request
+                    r.error = str(e)
             bal.free()
             r.t_done = time.perf_counter() - t0
         return reqs
@@ -188,8 +195,9 @@ class BatchingServer:
     construction + balance per batch, solves overlapped on worker streams."""
 
     def __init__(self, device: int = 0, hbm_budget: int = 64 << 30, workers: int = 3, solve_maxit: int = 50,
-                 max_coarse: int = 4096, max_batch_points: int = 64_000_000, keep: str = ""):
+                 max_coarse: int = 4096, max_batch_points: int = 64_000_000, keep: str = "", solve: bool = True):
         self.keep = keep  # results copied back per request (see _solve)
+        self.solve = solve  # False: a request is points2Octree + balanceOctree only
         self.ctx = Context(device)
         self.worker_ctx = [Context(device) for _ in range(workers)]
         self.budget, self.maxit, self.max_coarse = hbm_budget, solve_maxit, max_coarse
@@ -289,7 +297,17 @@ class BatchingServer:
                 r.n_octants = int(off_lin[s + 1] - off_lin[s])
                 r.n_balanced = int(off_bal[s + 1] - off_bal[s])
                 r.t_built = tb
-                work.put((r, bal.extract(s), need))
+                if self.solve:
+                    work.put((r, bal.extract(s), need))
+            if not self.solve:  # build + balance requests end with the batch
+                if "octree" in self.keep:
+                    recs, off = bal.to_numpy(), off_bal
+                    for s, (r, _) in enumerate(batch):
+                        r.octree = recs[off[s]:off[s + 1]]
+                done = time.perf_counter() - t0
+                for r, need in batch:
+                    r.t_done = done
+                    self._release(need)
             bal.free()
         for _ in workers:
             work.put(None)

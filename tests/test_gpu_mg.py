@@ -117,3 +117,24 @@ def test_mg_rejects_batches(ctx):
     with pytest.raises(DendroError) as e:
         MultiGrid(balanceOctree(lin))
     assert e.value.status == 9
+
+
+@pytest.mark.parametrize("npts", [3, 40, 500, 700])
+def test_single_level_is_an_exact_coarse_solve(ctx, oracle, npts):
+    """With one level the V-cycle is the coarsest solve itself (block
+    Gauss-Jordan FP32 inverse, FP64 refinement rounds): CG stops after one
+    iteration, and the solution equals the oracle's dense FP64 solve.  The
+    sizes put the coarse operator below one 64-wide block, across a few
+    blocks and with a partial last block."""
+    from oracle.mg_ref import OracleMG
+
+    bal = oracle.balance(oracle.points_to_octree(datagen.gaussian(npts, 0.5, 0.2, seed=npts), 30, 1), 30)
+    mg = MultiGrid(Octree.from_numpy(bal, 30, ctx=ctx), max_coarse_elems=len(bal))
+    assert mg.n_levels == 1
+    b = mg.rhs(datagen.bumps(mg.level_nodes(0)))
+    x, it, rr = mg.solve(b, precision=32, rtol=1e-10, maxit=5)
+    assert it == 1 and rr <= 1e-10
+    ref = OracleMG(bal, 30, max_coarse=len(bal))
+    p = _perm(mg.level_nodes(0), ref.das[0].node_xyz)
+    x_ref = ref.cinv @ ref.rhs(datagen.bumps(ref.das[0].node_xyz))
+    assert np.linalg.norm(x[p] - x_ref) <= 1e-10 * np.linalg.norm(x_ref)
