@@ -207,7 +207,8 @@ __global__ void k_set_bdy_identity(const uint8_t *__restrict__ bdy, size_t n, do
 //   X_RR -= (X_RK P) X_KR,  X_KR = P X_KR,  X_RK = -(X_RK P),  X_KK = P;
 // after the last block X holds the inverse (n^3 FP32 multiply-adds).
 // Each block costs two launches: k_bgj_diag inverts X_KK (one CTA), then
-// k_bgj_step updates every 64 x 64 tile at once.  So that no tile is
+// k_bgj_step updates every 64 x 64 tile at once (a CTA per tile row and
+// GJ_TJ tile columns).  So that no tile is
 // overwritten while another CTA of the same launch still reads it, the new
 // row K and column K go to scratch strips (R: GJB x n, C: n x GJB,
 // double-buffered by block parity) and reach X one block later: a tile in
@@ -299,59 +300,62 @@ __device__ __forceinline__ void gj_mma(const float *Lt, const float *Rm, float2 
   }
 }
 
-// One block step over every tile (ti, tj) (grid nt x nt, 256 threads,
-// three 64 x GJT shared tiles):
-//   (K, K): R = P;  (K, j): R = P X_Kj;  (i, K): C = -(X_iK P);
-//   (i, j): X_ij -= (X_iK P) X_Kj
+// One block step.  A CTA takes one tile row ti and GJ_TJ consecutive tile
+// columns (grid ceil(nt / GJ_TJ) x nt, 256 threads, three 64 x GJT shared
+// tiles), so that U = X_iK P is formed once per row and CTA:
+//   row K:      R[:, j] = P X_Kj (R[:, K] = P);
+//   other rows: C[i, :] = -U on the tile in column K,
+//               X_ij -= U X_Kj on the others.
+constexpr int GJ_TJ = 8;
 __global__ void __launch_bounds__(256) k_bgj_step(float *__restrict__ X, size_t n, size_t k0, GjSrc src,
                                                   const float *__restrict__ P, float *__restrict__ Rn,
                                                   float *__restrict__ Cn) {
   extern __shared__ __align__(16) float gsm[];
   float *A = gsm, *B = gsm + 64 * GJT, *Q = gsm + 2 * 64 * GJT;
-  const size_t tk = k0 / GJB, ti = blockIdx.y, tj = blockIdx.x;
-  const size_t i0 = ti * 64, j0 = tj * 64;
+  const size_t nt = (n + GJB - 1) / GJB;
+  const size_t tk = k0 / GJB, ti = blockIdx.y, tj0 = (size_t)blockIdx.x * GJ_TJ;
+  const size_t tj1 = tj0 + GJ_TJ < nt ? tj0 + GJ_TJ : nt;
+  const size_t i0 = ti * 64;
   const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
   float2 acc[4][2];
+  auto zero = [&]() {
 #pragma unroll
-  for (int r = 0; r < 4; r++) acc[r][0] = acc[r][1] = make_float2(0.f, 0.f);
-  if (ti == tk && tj == tk) {
-    for (int q = threadIdx.x; q < 64 * 64; q += 256) {
-      const int r = q / 64, c = q % 64;
-      if (k0 + c < n) Rn[r * n + k0 + c] = P[q];
+    for (int r = 0; r < 4; r++) acc[r][0] = acc[r][1] = make_float2(0.f, 0.f);
+  };
+  auto accv = [&](int r, int c) {
+    return c < 2 ? (c == 0 ? acc[r][0].x : acc[r][0].y) : (c == 2 ? acc[r][1].x : acc[r][1].y);
+  };
+  if (ti == tk) {
+    // the pivot row: A = P transposed, then R[:, j] = P X_Kj per tile
+    for (int q = threadIdx.x; q < 64 * 64; q += 256) A[(q % 64) * GJT + q / 64] = P[q];
+    for (size_t tj = tj0; tj < tj1; tj++) {
+      const size_t j0 = tj * 64;
+      if (tj == tk) {
+        for (int q = threadIdx.x; q < 64 * 64; q += 256)
+          if (k0 + q % 64 < n) Rn[(q / 64) * n + k0 + q % 64] = P[q];
+        continue;
+      }
+      __syncthreads();  // B free again
+      gj_load(B, src, k0, j0, false);
+      __syncthreads();
+      zero();
+      gj_mma(A, B, acc);
+#pragma unroll
+      for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const size_t j = j0 + tx * 4 + c;
+          if (j < n) Rn[(size_t)(ty * 4 + r) * n + j] = accv(r, c);
+        }
     }
     return;
   }
-  if (ti == tk) {  // R[:, j] = P X_Kj
-    for (int q = threadIdx.x; q < 64 * 64; q += 256) A[(q % 64) * GJT + q / 64] = P[q];  // P transposed
-    gj_load(B, src, k0, j0, false);
-    __syncthreads();
-    gj_mma(A, B, acc);
-#pragma unroll
-    for (int r = 0; r < 4; r++)
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const size_t j = j0 + tx * 4 + c;
-        const float v = c < 2 ? (c == 0 ? acc[r][0].x : acc[r][0].y) : (c == 2 ? acc[r][1].x : acc[r][1].y);
-        if (j < n) Rn[(size_t)(ty * 4 + r) * n + j] = v;
-      }
-    return;
-  }
-  // U = X_iK P (the (i, K) tile's new value is -U)
+  // U = X_iK P, kept transposed in A for the updates
   gj_load(A, src, i0, k0, true);
   for (int q = threadIdx.x; q < 64 * 64; q += 256) Q[(q / 64) * GJT + q % 64] = P[q];
   __syncthreads();
+  zero();
   gj_mma(A, Q, acc);
-  if (tj == tk) {
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-      const size_t i = i0 + ty * 4 + r;
-      if (i >= n) continue;
-      float4 v = make_float4(-acc[r][0].x, -acc[r][0].y, -acc[r][1].x, -acc[r][1].y);
-      *reinterpret_cast<float4 *>(&Cn[i * GJB + tx * 4]) = v;
-    }
-    return;
-  }
-  // X_ij -= U X_Kj: U goes to A transposed, X_Kj to B
   __syncthreads();  // every thread is done reading A and Q
 #pragma unroll
   for (int r = 0; r < 4; r++) {
@@ -359,20 +363,33 @@ __global__ void __launch_bounds__(256) k_bgj_step(float *__restrict__ X, size_t 
     A[(tx * 4 + 1) * GJT + ty * 4 + r] = acc[r][0].y;
     A[(tx * 4 + 2) * GJT + ty * 4 + r] = acc[r][1].x;
     A[(tx * 4 + 3) * GJT + ty * 4 + r] = acc[r][1].y;
-    acc[r][0] = acc[r][1] = make_float2(0.f, 0.f);
   }
-  gj_load(B, src, k0, j0, false);
-  __syncthreads();
-  gj_mma(A, B, acc);
+  if (tk >= tj0 && tk < tj1) {  // this CTA holds the tile in column K: C = -U
 #pragma unroll
-  for (int r = 0; r < 4; r++) {
-    const size_t i = i0 + ty * 4 + r;
-    if (i >= n) continue;
-    const float av[4] = {acc[r][0].x, acc[r][0].y, acc[r][1].x, acc[r][1].y};
+    for (int r = 0; r < 4; r++) {
+      const size_t i = i0 + ty * 4 + r;
+      if (i < n)
+        *reinterpret_cast<float4 *>(&Cn[i * GJB + tx * 4]) =
+            make_float4(-acc[r][0].x, -acc[r][0].y, -acc[r][1].x, -acc[r][1].y);
+    }
+  }
+  for (size_t tj = tj0; tj < tj1; tj++) {
+    if (tj == tk) continue;
+    const size_t j0 = tj * 64;
+    __syncthreads();  // A written; B free again
+    gj_load(B, src, k0, j0, false);
+    __syncthreads();
+    zero();
+    gj_mma(A, B, acc);
 #pragma unroll
-    for (int c = 0; c < 4; c++) {
-      const size_t j = j0 + tx * 4 + c;
-      if (j < n) X[i * n + j] = src.at(i, j) - av[c];
+    for (int r = 0; r < 4; r++) {
+      const size_t i = i0 + ty * 4 + r;
+      if (i >= n) continue;
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const size_t j = j0 + tx * 4 + c;
+        if (j < n) X[i * n + j] = src.at(i, j) - accv(r, c);
+      }
     }
   }
 }
@@ -729,9 +746,8 @@ void mg_setup(Context &ctx, const Octree &fine, size_t max_coarse_elem, MG &mg) 
         const size_t cur = step & 1, prev = cur ^ 1;
         k_bgj_diag<<<1, 256, 0, s>>>(mg.cinv32, n, k0, b, P.get());
         GjSrc src{mg.cinv32, R.get() + prev * GJB * n, C.get() + prev * n * GJB, n, pk};
-        k_bgj_step<<<dim3((unsigned)nt, (unsigned)nt), 256, smem, s>>>(mg.cinv32, n, k0, src, P.get(),
-                                                                         R.get() + cur * GJB * n,
-                                                                         C.get() + cur * n * GJB);
+        k_bgj_step<<<dim3((unsigned)((nt + GJ_TJ - 1) / GJ_TJ), (unsigned)nt), 256, smem, s>>>(
+            mg.cinv32, n, k0, src, P.get(), R.get() + cur * GJB * n, C.get() + cur * n * GJB);
         pk = (long)(k0 / GJB);
         if (k0 + GJB >= n)
           k_bgj_flush<<<grid_for(n * (size_t)b, 256), 256, 0, s>>>(mg.cinv32, n, k0, b, R.get() + cur * GJB * n,
