@@ -208,7 +208,7 @@ __global__ void k_set_bdy_identity(const uint8_t *__restrict__ bdy, size_t n, do
 // after the last block X holds the inverse (n^3 FP32 multiply-adds).
 // Each block costs two launches: k_bgj_diag inverts X_KK (one CTA), then
 // k_bgj_step updates every 64 x 64 tile at once (a CTA per tile row and
-// GJ_TJ tile columns).  So that no tile is
+// tjn tile columns).  So that no tile is
 // overwritten while another CTA of the same launch still reads it, the new
 // row K and column K go to scratch strips (R: GJB x n, C: n x GJB,
 // double-buffered by block parity) and reach X one block later: a tile in
@@ -300,21 +300,20 @@ __device__ __forceinline__ void gj_mma(const float *Lt, const float *Rm, float2 
   }
 }
 
-// One block step.  A CTA takes one tile row ti and GJ_TJ consecutive tile
-// columns (grid ceil(nt / GJ_TJ) x nt, 256 threads, three 64 x GJT shared
+// One block step.  A CTA takes one tile row ti and tjn consecutive tile
+// columns (grid ceil(nt / tjn) x nt, 256 threads, three 64 x GJT shared
 // tiles), so that U = X_iK P is formed once per row and CTA:
 //   row K:      R[:, j] = P X_Kj (R[:, K] = P);
 //   other rows: C[i, :] = -U on the tile in column K,
 //               X_ij -= U X_Kj on the others.
-constexpr int GJ_TJ = 8;
-__global__ void __launch_bounds__(256) k_bgj_step(float *__restrict__ X, size_t n, size_t k0, GjSrc src,
-                                                  const float *__restrict__ P, float *__restrict__ Rn,
+__global__ void __launch_bounds__(256) k_bgj_step(float *__restrict__ X, size_t n, size_t k0, size_t tjn,
+                                                  GjSrc src, const float *__restrict__ P, float *__restrict__ Rn,
                                                   float *__restrict__ Cn) {
   extern __shared__ __align__(16) float gsm[];
   float *A = gsm, *B = gsm + 64 * GJT, *Q = gsm + 2 * 64 * GJT;
   const size_t nt = (n + GJB - 1) / GJB;
-  const size_t tk = k0 / GJB, ti = blockIdx.y, tj0 = (size_t)blockIdx.x * GJ_TJ;
-  const size_t tj1 = tj0 + GJ_TJ < nt ? tj0 + GJ_TJ : nt;
+  const size_t tk = k0 / GJB, ti = blockIdx.y, tj0 = (size_t)blockIdx.x * tjn;
+  const size_t tj1 = tj0 + tjn < nt ? tj0 + tjn : nt;
   const size_t i0 = ti * 64;
   const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
   float2 acc[4][2];
@@ -739,6 +738,9 @@ void mg_setup(Context &ctx, const Octree &fine, size_t max_coarse_elem, MG &mg) 
       const size_t nt = (n + GJB - 1) / GJB;
       DBuf<float> P(GJB * GJB, s), R(2 * GJB * n, s), C(2 * n * GJB, s);
       const int smem = 3 * 64 * GJT * (int)sizeof(float);
+      // tile columns per CTA: about three CTAs per SM over the nt x nt tiles
+      // (each CTA forms U once and reuses it across its columns)
+      const size_t tjn = std::max<size_t>(1, (nt * nt + 3 * ctx.num_sms - 1) / (3 * (size_t)ctx.num_sms));
       ensure_smem_attr(ctx, k_bgj_step, smem);
       long pk = -1;
       for (size_t k0 = 0, step = 0; k0 < n; k0 += GJB, step++) {
@@ -746,8 +748,8 @@ void mg_setup(Context &ctx, const Octree &fine, size_t max_coarse_elem, MG &mg) 
         const size_t cur = step & 1, prev = cur ^ 1;
         k_bgj_diag<<<1, 256, 0, s>>>(mg.cinv32, n, k0, b, P.get());
         GjSrc src{mg.cinv32, R.get() + prev * GJB * n, C.get() + prev * n * GJB, n, pk};
-        k_bgj_step<<<dim3((unsigned)((nt + GJ_TJ - 1) / GJ_TJ), (unsigned)nt), 256, smem, s>>>(
-            mg.cinv32, n, k0, src, P.get(), R.get() + cur * GJB * n, C.get() + cur * n * GJB);
+        k_bgj_step<<<dim3((unsigned)((nt + tjn - 1) / tjn), (unsigned)nt), 256, smem, s>>>(
+            mg.cinv32, n, k0, tjn, src, P.get(), R.get() + cur * GJB * n, C.get() + cur * n * GJB);
         pk = (long)(k0 / GJB);
         if (k0 + GJB >= n)
           k_bgj_flush<<<grid_for(n * (size_t)b, 256), 256, 0, s>>>(mg.cinv32, n, k0, b, R.get() + cur * GJB * n,
