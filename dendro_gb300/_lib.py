@@ -114,6 +114,7 @@ def _declare(L):
         "dg_mg_restrict": ([P, P, SZ, P, P, I, I], I),
         "dg_mg_prolong": ([P, P, SZ, P, P, I, I], I),
         "dg_mg_set_smoother": ([P, D, I, I], I),
+        "dg_mg_set_cg_operator": ([P, I, D], I),
         "dg_mg_rhs": ([P, P, P, P, I], I),
         "dg_mg_solve": ([P, P, P, P, I, D, I, I, ctypes.POINTER(I), ctypes.POINTER(D)], I),
         "dg_mg_free": ([P, P], I),

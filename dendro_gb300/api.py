@@ -655,6 +655,12 @@ class MultiGrid:
     def set_smoother(self, omega: float = 0.667, nu_pre: int = 2, nu_post: int = 2):
         check(self.ctx.handle, self.ctx._L.dg_mg_set_smoother(self.handle, omega, nu_pre, nu_post), "set_smoother")
 
+    def set_cg_operator(self, precision: int = 64, reliable_delta: float = 1e-3):
+        """The CG's operator q = A p with an FP32 V-cycle: FP64 every
+        iteration (64), or FP32 with FP64 residual replacement (32)."""
+        check(self.ctx.handle, self.ctx._L.dg_mg_set_cg_operator(self.handle, precision, reliable_delta),
+              "set_cg_operator")
+
     def rhs(self, f):
         """Load vector b = M f of a nodal field on the finest level, 0 on the boundary."""
         on_dev = 1 if _is_device(f) else 0

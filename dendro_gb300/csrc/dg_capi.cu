@@ -733,6 +733,14 @@ int dg_mg_set_smoother(dg_mg mg, double omega, int nu_pre, int nu_post) {
   return DG_OK;
 }
 
+int dg_mg_set_cg_operator(dg_mg mg, int precision, double reliable_delta) {
+  if (!mg || (precision != 32 && precision != 64) || !(reliable_delta > 0 && reliable_delta < 1))
+    return DG_ERR_INVALID_ARG;
+  mg->mg.cg_operator = precision;
+  mg->mg.reliable_delta = reliable_delta;
+  return DG_OK;
+}
+
 int dg_mg_rhs(dg_ctx ctx, dg_mg mg, const double *f, double *b, int on_device) {
   if (!mg) return DG_ERR_INVALID_ARG;
   const dg::MGLevel &L = mg->mg.lv[0];

@@ -208,7 +208,7 @@ __global__ void k_set_bdy_identity(const uint8_t *__restrict__ bdy, size_t n, do
 // after the last block X holds the inverse (n^3 FP32 multiply-adds).
 // Each block costs two launches: k_bgj_diag inverts X_KK (one CTA), then
 // k_bgj_step updates every 64 x 64 tile at once (a CTA per tile row and
-// tjn tile columns).  So that no tile is
+// tjn tile columns, about four CTAs per SM).  So that no tile is
 // overwritten while another CTA of the same launch still reads it, the new
 // row K and column K go to scratch strips (R: GJB x n, C: n x GJB,
 // double-buffered by block parity) and reach X one block later: a tile in
@@ -257,25 +257,36 @@ __global__ void __launch_bounds__(256) k_bgj_diag(const float *__restrict__ X, s
 }
 
 // where tile entries live while the block steps run: X, or the strips of
-// the previous block pk (R rows k0p.., C columns k0p..); 0 outside n x n
+// the previous block pk (R: its rows, C: its columns)
 struct GjSrc {
   const float *X, *R, *C;
   size_t n;
   long pk;  // previous block's tile index, -1 before the first block
-  __device__ __forceinline__ float at(size_t i, size_t j) const {
-    if (i >= n || j >= n) return 0.f;
-    if ((long)(i / GJB) == pk) return R[(i % GJB) * n + j];
-    if ((long)(j / GJB) == pk) return C[i * GJB + (j % GJB)];
-    return X[i * n + j];
+  // the tile at (i0, j0) (multiples of GJB) lies wholly in X, in the R strip
+  // or in the C strip: its first entry and row stride
+  __device__ __forceinline__ const float *tile(size_t i0, size_t j0, size_t *ld) const {
+    if ((long)(i0 / GJB) == pk) {
+      *ld = n;
+      return R + j0;
+    }
+    if ((long)(j0 / GJB) == pk) {
+      *ld = GJB;
+      return C + i0 * GJB;
+    }
+    *ld = n;
+    return X + i0 * n + j0;
   }
 };
 
 // shared tile T[m][r] = src(i0 + r, j0 + m) (transposed) or T[m][c] =
-// src(i0 + m, j0 + c) (as is)
+// src(i0 + m, j0 + c) (as is); entries outside n x n are 0
 __device__ __forceinline__ void gj_load(float *T, const GjSrc &src, size_t i0, size_t j0, bool transposed) {
+  size_t ld;
+  const float *t = src.tile(i0, j0, &ld);
+  const int rows = (int)(src.n - i0 < 64 ? src.n - i0 : 64), cols = (int)(src.n - j0 < 64 ? src.n - j0 : 64);
   for (int q = threadIdx.x; q < 64 * 64; q += 256) {
-    const int a = q / 64, bb = q % 64;  // a: row of the source tile, bb: its column
-    const float v = src.at(i0 + a, j0 + bb);
+    const int a = q >> 6, bb = q & 63;  // a: row of the source tile, bb: its column
+    const float v = (a < rows && bb < cols) ? t[(size_t)a * ld + bb] : 0.f;
     if (transposed) T[bb * GJT + a] = v;
     else T[a * GJT + bb] = v;
   }
@@ -306,7 +317,7 @@ __device__ __forceinline__ void gj_mma(const float *Lt, const float *Rm, float2 
 //   row K:      R[:, j] = P X_Kj (R[:, K] = P);
 //   other rows: C[i, :] = -U on the tile in column K,
 //               X_ij -= U X_Kj on the others.
-__global__ void __launch_bounds__(256) k_bgj_step(float *__restrict__ X, size_t n, size_t k0, size_t tjn,
+__global__ void __launch_bounds__(256, 4) k_bgj_step(float *__restrict__ X, size_t n, size_t k0, size_t tjn,
                                                   GjSrc src, const float *__restrict__ P, float *__restrict__ Rn,
                                                   float *__restrict__ Cn) {
   extern __shared__ __align__(16) float gsm[];
@@ -380,6 +391,8 @@ __global__ void __launch_bounds__(256) k_bgj_step(float *__restrict__ X, size_t 
     __syncthreads();
     zero();
     gj_mma(A, B, acc);
+    size_t ld;
+    const float *own = src.tile(i0, j0, &ld);  // this tile's current values
 #pragma unroll
     for (int r = 0; r < 4; r++) {
       const size_t i = i0 + ty * 4 + r;
@@ -387,7 +400,7 @@ __global__ void __launch_bounds__(256) k_bgj_step(float *__restrict__ X, size_t 
 #pragma unroll
       for (int c = 0; c < 4; c++) {
         const size_t j = j0 + tx * 4 + c;
-        if (j < n) X[i * n + j] = src.at(i, j) - accv(r, c);
+        if (j < n) X[i * n + j] = own[(size_t)(ty * 4 + r) * ld + tx * 4 + c] - accv(r, c);
       }
     }
   }
@@ -738,9 +751,9 @@ void mg_setup(Context &ctx, const Octree &fine, size_t max_coarse_elem, MG &mg) 
       const size_t nt = (n + GJB - 1) / GJB;
       DBuf<float> P(GJB * GJB, s), R(2 * GJB * n, s), C(2 * n * GJB, s);
       const int smem = 3 * 64 * GJT * (int)sizeof(float);
-      // tile columns per CTA: about three CTAs per SM over the nt x nt tiles
+      // tile columns per CTA: about four CTAs per SM over the nt x nt tiles
       // (each CTA forms U once and reuses it across its columns)
-      const size_t tjn = std::max<size_t>(1, (nt * nt + 3 * ctx.num_sms - 1) / (3 * (size_t)ctx.num_sms));
+      const size_t tjn = std::max<size_t>(1, (nt * nt + 4 * ctx.num_sms - 1) / (4 * (size_t)ctx.num_sms));
       ensure_smem_attr(ctx, k_bgj_step, smem);
       long pk = -1;
       for (size_t k0 = 0, step = 0; k0 < n; k0 += GJB, step++) {
@@ -810,9 +823,24 @@ void mg_solve(Context &ctx, MG &mg, const double *b, double *x, int precision, d
   if (bb == 0.0) return;
   const double bnorm = std::sqrt(bb);
   // CG iteration: step A (q = A p, x and r updated, r.r) and step B (the
-  // next direction from z = V-cycle(r)); the host reads r.r after each A
+  // next direction from z = V-cycle(r)); the host reads r.r after each A.
+  // With the FP32 operator, q = A p runs through the FP32 element loop and
+  // the recurrence residual is replaced by the FP64 one from time to time.
+  const bool op32 = precision == 32 && mg.cg_operator == 32;
+  DBuf<float> p32, q32;
+  if (op32) {
+    p32.alloc(n, s);
+    q32.alloc(n, s);
+  }
   auto step_a = [&]() {
-    dirichlet_matvec<double>(ctx, L0, p.get(), q.get());
+    if (op32) {
+      k_to_float<<<g, 256, 0, s>>>(p.get(), n, p32.get());
+      dirichlet_matvec<float>(ctx, L0, p32.get(), q32.get());
+      k_to_double<<<g, 256, 0, s>>>(q32.get(), n, q.get());
+      DG_LAUNCH_CHECK();
+    } else {
+      dirichlet_matvec<double>(ctx, L0, p.get(), q.get());
+    }
     dot(p.get(), q.get(), d_pq);
     k_cg_xr<<<g, 256, 0, s>>>(x, r.get(), p.get(), q.get(), d_rz, d_pq, n);
     DG_LAUNCH_CHECK();
@@ -828,9 +856,28 @@ void mg_solve(Context &ctx, MG &mg, const double *b, double *x, int precision, d
   precond(r.get(), z.get());
   DG_CUDA(cudaMemcpyAsync(p.get(), z.get(), n * sizeof(double), cudaMemcpyDeviceToDevice, s));
   dot(r.get(), z.get(), d_rz);
+  // r = b - A x in FP64 (the reliable update of the FP32-operator form)
+  auto true_residual = [&]() {
+    dirichlet_matvec<double>(ctx, L0, x, q.get());
+    k_residual<double><<<g, 256, 0, s>>>(b, q.get(), r.get(), n);
+    DG_LAUNCH_CHECK();
+    dot(r.get(), nullptr, d_rr);
+    return std::sqrt(read_scalar(ctx, d_rr)) / bnorm;
+  };
+  double anchor = 1.0;  // relative residual at the last replacement
+  // the recurrence's relative residual, replaced by the FP64 one when it has
+  // fallen far enough (or would stop the iteration)
+  auto residual_now = [&]() {
+    double rel = std::sqrt(read_scalar(ctx, d_rr)) / bnorm;
+    if (op32 && (rel <= rtol || rel <= mg.reliable_delta * anchor)) {
+      rel = true_residual();
+      anchor = rel;
+    }
+    return rel;
+  };
   step_a();
   int it = 1;
-  double relres = std::sqrt(read_scalar(ctx, d_rr)) / bnorm;
+  double relres = residual_now();
   // Iterations after the first: B then A, a few hundred launches (the
   // V-cycle visits every level), captured once into a CUDA graph and
   // replayed, so each iteration costs one launch.  Everything the capture
@@ -851,7 +898,7 @@ void mg_solve(Context &ctx, MG &mg, const double *b, double *x, int precision, d
       step_a();
     }
     it++;
-    relres = std::sqrt(read_scalar(ctx, d_rr)) / bnorm;
+    relres = residual_now();
   }
   // the true residual, recomputed in FP64
   dirichlet_matvec<double>(ctx, L0, x, q.get());

@@ -30,6 +30,12 @@ struct MG {
   float *cinv32 = nullptr;   // its inverse in FP32 (refined in FP64 when applied)
   double omega = 0.667;  // Jacobi damping (bin/options:190)
   int nu_pre = 2, nu_post = 2;
+  // CG operator with an FP32 V-cycle: 64 applies A p in FP64 every
+  // iteration; 32 applies it in FP32 and replaces the recurrence residual by
+  // the FP64 residual b - A x whenever it has fallen by reliable_delta since
+  // the last replacement (and before stopping)
+  int cg_operator = 64;
+  double reliable_delta = 1e-3;
 };
 
 struct MGResult {

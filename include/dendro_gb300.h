@@ -320,6 +320,15 @@ int dg_mg_prolong(dg_ctx ctx, dg_mg mg, size_t fine_level, const void *in, void 
 /* damped-Jacobi smoother (default omega 0.667, bin/options:190) and sweeps
  * per V-cycle side (default 2 and 2) */
 int dg_mg_set_smoother(dg_mg mg, double omega, int nu_pre, int nu_post);
+/* The CG's own operator application q = A p when the V-cycle runs in FP32
+ * (precision 32 of dg_mg_solve).  64 (the default): A p in FP64 every
+ * iteration.  32: A p in FP32 (the FP32 element loop), and the recurrence
+ * residual replaced by the FP64 residual b - A x whenever it has fallen by
+ * reliable_delta since the last replacement, and before the stopping test
+ * accepts it ("reliable updates"); residual, dot products, updates and the
+ * stopping test stay FP64.  No counterpart in the reference (PETSc's CG
+ * runs one precision). */
+int dg_mg_set_cg_operator(dg_mg mg, int precision, double reliable_delta);
 /* load vector of a nodal field on level 0: b = M f, boundary entries 0 */
 int dg_mg_rhs(dg_ctx ctx, dg_mg mg, const double *f, double *b, int on_device);
 /* CG preconditioned by one V-cycle per iteration, to ||b - A x|| <= rtol

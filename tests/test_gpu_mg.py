@@ -141,3 +141,21 @@ def test_single_level_is_an_exact_coarse_solve(ctx, oracle, npts):
         x, it, rr = mg.solve(b, precision=precision, rtol=1e-10, maxit=5)
         assert it <= iters and rr <= 1e-10, (precision, it, rr)
         assert np.linalg.norm(x[p] - x_ref) <= 1e-9 * np.linalg.norm(x_ref)
+
+
+def test_fp32_cg_operator_with_reliable_updates(ctx):
+    """The FP32 CG operator (dg_mg_set_cg_operator(32)): the recurrence
+    residual is replaced by the FP64 one, so the solve still stops at an FP64
+    relative residual of 1e-8 and agrees with the FP64-operator solve."""
+    pts = datagen.gaussian(200_000, 0.5, 0.15, seed=3)
+    bal = balanceOctree(points2Octree(pts, ctx=ctx))
+    mg = MultiGrid(bal, max_coarse_elems=4096)
+    b = mg.rhs(datagen.bumps(mg.level_nodes(0)))
+    x64, it64, rr64 = mg.solve(b, precision=32)
+    mg.set_cg_operator(32, 1e-3)
+    x32, it32, rr32 = mg.solve(b, precision=32)
+    assert rr64 <= 1e-8 and rr32 <= 1e-8
+    assert it32 <= it64 + 4
+    assert np.linalg.norm(x32 - x64) <= 1e-6 * np.linalg.norm(x64)
+    with pytest.raises(DendroError):
+        mg.set_cg_operator(16)
