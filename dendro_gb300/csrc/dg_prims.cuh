@@ -667,6 +667,92 @@ __global__ void k_flag_unique(const K *__restrict__ keys, size_t n, uint32_t *__
   if (i < n) flags[i] = (i == 0 || !KeyOps<K>::eq(keys[i], keys[i - 1])) ? 1u : 0u;
 }
 
+// Small sorts in one CTA: up to SMALL_SORT_MAX keys are sorted in shared
+// memory (bitonic network, padded with the largest key), repeated keys are
+// dropped and the rest written in order with their count.  Keys agree on
+// every bit above the sorted ones, so whole-key order is the radix order.
+// Used by sort_unique below the size where the radix sort's passes, each a
+// launch, and its histogram read-back cost more than the keys themselves
+// (the deep and coarse levels of a balance, most multigrid levels).
+constexpr int SMALL_SORT_MAX = 4096;
+constexpr int SMALL_SORT_BLOCK = 1024;
+
+__device__ __forceinline__ bool key_less(uint64_t a, uint64_t b) { return a < b; }
+__device__ __forceinline__ bool key_less(const Key128 &a, const Key128 &b) {
+  return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo);
+}
+template <typename K>
+__device__ __forceinline__ K key_max();
+template <>
+__device__ __forceinline__ uint64_t key_max<uint64_t>() {
+  return ~0ull;
+}
+template <>
+__device__ __forceinline__ Key128 key_max<Key128>() {
+  return Key128{~0ull, ~0ull};
+}
+
+template <typename K>
+__global__ void __launch_bounds__(SMALL_SORT_BLOCK) k_small_sort_unique(const K *__restrict__ in, int n, int n2,
+                                                                         K *__restrict__ out,
+                                                                         unsigned long long *count) {
+  extern __shared__ __align__(16) unsigned char ss_raw[];
+  K *sk = reinterpret_cast<K *>(ss_raw);
+  __shared__ int wsum[SMALL_SORT_BLOCK / 32];
+  const int tid = threadIdx.x;
+  for (int i = tid; i < n2; i += SMALL_SORT_BLOCK) sk[i] = i < n ? in[i] : key_max<K>();
+  __syncthreads();
+  for (int k = 2; k <= n2; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = tid; i < n2; i += SMALL_SORT_BLOCK) {
+        const int l = i ^ j;
+        if (l > i) {
+          const K a = sk[i], b = sk[l];
+          const bool up = (i & k) == 0;
+          if (up ? key_less(b, a) : key_less(a, b)) {
+            sk[i] = b;
+            sk[l] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  // thread t owns the consecutive items [4t, 4t + 4); first of each run kept
+  constexpr int PER = SMALL_SORT_MAX / SMALL_SORT_BLOCK;
+  int keep[PER], c = 0;
+#pragma unroll
+  for (int q = 0; q < PER; q++) {
+    const int i = tid * PER + q;
+    keep[q] = i < n && (i == 0 || key_less(sk[i - 1], sk[i]));
+    c += keep[q];
+  }
+  // block exclusive scan of the counts
+  const int lane = tid & 31, w = tid >> 5;
+  int incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) wsum[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    int v = lane < SMALL_SORT_BLOCK / 32 ? wsum[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += t;
+    }
+    if (lane < SMALL_SORT_BLOCK / 32) wsum[lane] = v;  // inclusive per warp
+  }
+  __syncthreads();
+  int pos = (w > 0 ? wsum[w - 1] : 0) + incl - c;
+#pragma unroll
+  for (int q = 0; q < PER; q++)
+    if (keep[q]) out[pos++] = sk[tid * PER + q];
+  if (tid == SMALL_SORT_BLOCK - 1) *count = (unsigned long long)(pos);
+}
+
 // sort + unique.  The unique keys end up in whichever of keys/tmp does not
 // hold the sorted sequence; *result points at them.  Returns their count.
 template <typename K>
@@ -674,6 +760,20 @@ size_t sort_unique(Context &ctx, K *keys, K *tmp, size_t n, int end_bit, K **res
   if (n == 0) {
     *result = keys;
     return 0;
+  }
+  if (n <= (size_t)SMALL_SORT_MAX) {
+    int n2 = 2;
+    while (n2 < (int)n) n2 <<= 1;
+    const int smem = n2 * (int)sizeof(K);
+    ensure_smem_attr(ctx, k_small_sort_unique<K>, SMALL_SORT_MAX * (int)sizeof(K));
+    unsigned long long *d_count = ctx.d_scratch + 8;
+    {
+      ProfScope _prof(ctx, "sort_unique_small", (double)n * sizeof(K) * 2);
+      k_small_sort_unique<K><<<1, SMALL_SORT_BLOCK, smem, ctx.stream>>>(keys, (int)n, n2, tmp, d_count);
+      DG_LAUNCH_CHECK();
+    }
+    *result = tmp;
+    return (size_t)read_scalar(ctx, d_count);
   }
   K *sorted = radix_sort<K>(ctx, keys, tmp, n, end_bit);
   K *out = (sorted == keys) ? tmp : keys;
