@@ -164,9 +164,13 @@ class Octree:
         off = self.segments()
         return [a[off[i]:off[i + 1]] for i in range(len(off) - 1)]
 
-    def to_numpy(self) -> np.ndarray:
+    def to_numpy(self, ctx: "Context | None" = None) -> np.ndarray:
+        """The records on the host, downloaded through ``ctx`` (default: the
+        context that made the octree; a context serves one host thread at a
+        time, so a worker thread passes its own)."""
+        c = ctx or self.ctx
         out = np.empty((self.size, 4), np.uint32)
-        check(self.ctx.handle, self.ctx._L.dg_octree_download(self.ctx.handle, self.handle, _ptr(out), 0), "dg_octree_download")
+        check(c.handle, c._L.dg_octree_download(c.handle, self.handle, _ptr(out), 0), "dg_octree_download")
         return out
 
     def download_to(self, dst):

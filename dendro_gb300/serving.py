@@ -119,7 +119,7 @@ def _solve(ctx: Context, bal, req: Request, maxit: int, max_coarse: int, stream=
 
     t0 = time.perf_counter()
     if "octree" in keep:
-        req.octree = bal.to_numpy()
+        req.octree = bal.to_numpy(ctx)
     mg = MultiGrid(bal, max_coarse_elems=max_coarse, ctx=ctx)
     try:
         req.t_setup = time.perf_counter() - t0
