@@ -418,6 +418,7 @@ def run_serving(args, local, barrier):
     p_walls, p_outs = [], []
     plain_build_s = None
     same_plain = None
+    plain_stats = {}
     if not args.skip_plain:
         plain = serving.PlainServer(device=local, solve_maxit=SOLVE_MAXIT)
         replay(plain, on_dev)
@@ -426,6 +427,13 @@ def run_serving(args, local, barrier):
             p_walls.append(wall)
             p_outs.extend(out)
         same_plain = min(replay_same(plain) for _ in range(2))
+        # per-kernel device times of the per-call path: one request at a time,
+        # so every launch has the GPU to itself (the served replay's times
+        # include waiting for SMs that other requests' kernels hold)
+        plain.ctx.profile(True)
+        replay(plain, on_dev)
+        plain_stats = plain.ctx.profile_stats()
+        plain.ctx.profile(False)
         plain.close()
         plain_build_s = sum(r.t_built - r.t_admit for r in p_outs) / 2
     # build + balance requests only (the benchmark spec's served-vs-plain figure
@@ -470,6 +478,7 @@ def run_serving(args, local, barrier):
         "relres_max": max(r.relres for r in outs),
         "errors": errors,
         "d2h_bytes_per_step": d2h,
+        "plain_stats": plain_stats,
         "build_balance_only": build_only,
         "served_same_sample": {"requests": len(same), "points": same_pts,
                                "served_Mpts_per_s": same_pts / same_served / 1e6,
@@ -887,6 +896,18 @@ def run_ours(args):
                    "GB/s": (v[2] / (v[0] * 1e-3) / 1e9) if v[0] > 0 else None,
                    "share": v[0] / step_total if step_total else None}
                for k, v in sorted(stats.items(), key=lambda kv: -kv[1][0])[:15]}
+    # the same figures from the per-call path's profiled replay (sequential)
+    pst = serve["plain_stats"]
+    roof_seq, kernels_seq = None, None
+    if pst and tname in pst:
+        sms, scnt, sbytes = pst[tname]
+        sach = (sbytes / scnt) / (sms / scnt * 1e-3) / 1e9
+        roof_seq = {"kernel": tname, "achieved": sach, "peak": peak, "unit": "GB/s", "frac": sach / peak,
+                    "ms_per_launch": sms / scnt, "algorithmic_bytes_per_launch": sbytes / scnt,
+                    "note": "per-call path, one request at a time: each launch has the GPU to itself"}
+        ptot = sum(v[0] for v in pst.values())
+        kernels_seq = {k: {"ms": v[0], "launches": v[1], "share": v[0] / ptot}
+                       for k, v in sorted(pst.items(), key=lambda kv: -kv[1][0])[:15]}
     if rank == 0:
         line = {
             "metric": METRIC,
@@ -933,6 +954,8 @@ def run_ours(args):
             "clocks": serve["clocks"],
             "cpu_baseline": cpu,
             "kernels": kernels,
+            "roofline_sequential": roof_seq,
+            "kernels_per_call": kernels_seq,
             "kernels_note": ("device ms of one replay of the step with each launch timed by CUDA events on its "
                              "stream (the timed steps replay the CG iterations from CUDA graphs instead)"),
             **extra,
