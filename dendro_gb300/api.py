@@ -77,6 +77,11 @@ class Context:
         """Start (or stop) per-kernel timing; clears the statistics."""
         check(self.handle, self._L.dg_ctx_profile(self.handle, 1 if enable else 0), "dg_ctx_profile")
 
+    def set_matvec_form(self, form: str):
+        """FP32 element loop form: "runs" (default) or "pairs"."""
+        check(self.handle, self._L.dg_ctx_set_matvec_form(self.handle, {"runs": 0, "pairs": 1}[form]),
+              "set_matvec_form")
+
     def set_order(self, order: str):
         """Order of octant records at the boundary: "morton" (default) or
         "hilbert" (the reference's default HILBERT_ORDERING build)."""

@@ -239,6 +239,12 @@ int dg_ctx_profile_entry(dg_ctx ctx, int index, char *name, size_t name_len, dou
   return DG_OK;
 }
 
+int dg_ctx_set_matvec_form(dg_ctx ctx, int form) {
+  if (!ctx || (form != 0 && form != 1)) return DG_ERR_INVALID_ARG;
+  ctx->c.matvec_form = form;
+  return DG_OK;
+}
+
 int dg_debug_lookback_timeout(dg_ctx ctx, size_t n_keys, unsigned skipped_tiles) {
   return guarded(ctx, [&]() { dg::lookback_timeout_selftest(ctx->c, n_keys, skipped_tiles); });
 }

@@ -625,6 +625,50 @@ __global__ void k_patch_nodes(const uint32_t *__restrict__ run_node, const uint3
   for (uint32_t i = threadIdx.x; i < nr; i += blockDim.x) pnode[poff[p] + i] = run_node[p * PATCH_ENT + i];
 }
 
+// run-form tables from the pair tables: every pair's run index (run starts
+// counted from pexc) per slot in shared memory, then per (type, level)
+// position the runs of its vertices in the canonical order of its stencil
+// (vertex cperm[c][t] digit m at canonical position m), and per run its node
+// with the complete flag of its pairs
+__global__ void __launch_bounds__(PATCH) k_patch_runs(const uint16_t *__restrict__ pinc,
+                                                      const uint16_t *__restrict__ pexc,
+                                                      const uint32_t *__restrict__ pnode,
+                                                      const uint64_t *__restrict__ poff,
+                                                      const uint32_t *__restrict__ pmeta,
+                                                      const uint32_t *__restrict__ cperm, size_t E,
+                                                      uint4 *__restrict__ plid, uint32_t *__restrict__ prun) {
+  __shared__ uint16_t run_of[PATCH_ENT];
+  const size_t p = blockIdx.x;
+  const int t = threadIdx.x;
+  const size_t e0 = p * PATCH;
+  const int ne = (int)((E - e0) < (size_t)PATCH ? (E - e0) : (size_t)PATCH);
+  const uint64_t ub = poff[p];
+  if (t < ne) {
+    int r = (int)pexc[p * PATCH + t] - 1;
+    for (int i = 8 * t; i < 8 * t + 8; i++) {
+      const uint32_t ent = pinc[p * PATCH_ENT + i];
+      if (ent & ENT_START) {
+        r++;
+        prun[ub + r] = pnode[ub + r] | ((ent & ENT_COMPLETE) ? PRUN_COMPLETE : 0u);
+      }
+      run_of[ent & ENT_SLOT] = (uint16_t)r;
+    }
+  }
+  __syncthreads();
+  if (t < ne) {
+    const uint32_t me = pmeta[p * PATCH + t];
+    const uint32_t sig = cperm[((me >> 8) & 7u) * 18 + (me >> 24)];
+    uint32_t w[4];
+#pragma unroll
+    for (int m = 0; m < 8; m += 2) {
+      const uint32_t a = run_of[((sig >> (3 * m)) & 7u) * PATCH + t];
+      const uint32_t b = run_of[((sig >> (3 * (m + 1))) & 7u) * PATCH + t];
+      w[m >> 1] = a | (b << 16);
+    }
+    plid[p * PATCH + t] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
 // conn from the patch tables: pair i of patch p belongs to the run counted
 // by the run starts up to i (pexc gives the count before pair 8t), its slot
 // names the vertex and the element's (type, level) position
@@ -671,6 +715,7 @@ size_t mesh_bytes(const Mesh &m) {
   if (m.conn) b += 8 * E * 4;                                   // conn
   b += np * (PATCH_ENT * 2 + PATCH * 2 + PATCH * 4 + PKEY_MAX * 2 + 2) + (np + 1) * 8 + runs * 4;  // patches
   if (m.pperm) b += np * PATCH * 2;
+  if (m.plid) b += np * PATCH * 16 + runs * 4;  // run-form tables
   return b;
 }
 
@@ -708,6 +753,18 @@ static void mesh_patches(Context &ctx, Mesh &m) {
     ProfScope _prof(ctx, "da_patch_nodes", (double)nruns * 8);
     k_patch_nodes<<<(unsigned)np, 256, 0, s>>>(run_node.get(), n_run.get(), poff.get(), pnode.get());
     DG_LAUNCH_CHECK();
+  }
+  if (!m.compressed) {  // a compressed DA keeps the pair tables only
+    DBuf<uint4> plid(np * PATCH, s);
+    DBuf<uint32_t> prun(nruns ? nruns : 1, s);
+    {
+      ProfScope _prof(ctx, "da_patch_runs", (double)n * (16 + 2 + 4 + 16) + (double)nruns * 8);
+      k_patch_runs<<<(unsigned)np, PATCH, 0, s>>>(pinc.get(), pexc.get(), pnode.get(), poff.get(), pmeta.get(),
+                                                  ctx.d_cperm, n, plid.get(), prun.get());
+      DG_LAUNCH_CHECK();
+    }
+    m.plid = plid.release_ptr();
+    m.prun = prun.release_ptr();
   }
   m.n_patch = np;
   m.pinc = pinc.release_ptr();
@@ -788,6 +845,8 @@ void mesh_free(Context &ctx, Mesh &m) {
   if (m.pnode) cudaFreeAsync(m.pnode, ctx.stream);
   if (m.poff) cudaFreeAsync(m.poff, ctx.stream);
   if (m.pperm) cudaFreeAsync(m.pperm, ctx.stream);
+  if (m.plid) cudaFreeAsync(m.plid, ctx.stream);
+  if (m.prun) cudaFreeAsync(m.prun, ctx.stream);
   m = Mesh();
 }
 
@@ -815,11 +874,40 @@ const T *comb_table(Context &ctx, double lap_fac, double mass_fac) {
 template const float *comb_table<float>(Context &, double, double);
 template const double *comb_table<double>(Context &, double, double);
 
+// the run-form FP32 element loop (k_patch_matvec_runs); DIR: the
+// Dirichlet form, bdy the boundary flags
+template <bool DIR>
+void launch_matvec_runs(Context &ctx, const Mesh &m, const uint8_t *bdy, const float *x, float *y, double lap_fac,
+                        double mass_fac, const char *name, double bytes) {
+  const size_t smem = patch_runs_smem();
+  ensure_smem_attr(ctx, k_patch_matvec_runs<DIR>, (int)smem);
+  int per_sm = 1;
+  DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_patch_matvec_runs<DIR>, PATCH, smem));
+  if (per_sm < 1) per_sm = 1;
+  const unsigned grid = (unsigned)std::min<size_t>(m.n_patch, (size_t)per_sm * ctx.num_sms);
+  ProfScope _prof(ctx, name, bytes);
+  k_patch_matvec_runs<DIR><<<grid, PATCH, smem, ctx.stream>>>(m.pmeta, m.plid, m.prun, m.poff, m.pkeys, m.pkcount,
+                                                             m.n_elem, m.n_patch, ctx.d_csten32, bdy, x, y,
+                                                             (float)lap_fac, (float)mass_fac);
+  DG_LAUNCH_CHECK();
+}
+template void launch_matvec_runs<true>(Context &, const Mesh &, const uint8_t *, const float *, float *, double,
+                                       double, const char *, double);
+template void launch_matvec_runs<false>(Context &, const Mesh &, const uint8_t *, const float *, float *, double,
+                                        double, const char *, double);
+
 template <typename T>
 void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, double mass_fac) {
   ensure_stencils(ctx);
   cudaStream_t s = ctx.stream;
   DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
+  if constexpr (std::is_same<T, float>::value) {
+    if (m.plid && ctx.matvec_form != 1) {
+      launch_matvec_runs<false>(ctx, m, nullptr, x, y, lap_fac, mass_fac, "matvec_fp32",
+                                (double)m.n_elem * 36 + (double)m.n_node * 3 * sizeof(T));
+      return;
+    }
+  }
   const size_t smem = patch_smem<T>();
   ensure_smem_attr(ctx, k_patch_matvec<T, false>, (int)smem);
   int per_sm = 1;

@@ -33,6 +33,12 @@ struct Mesh {
   uint64_t *poff = nullptr;   // n_patch + 1 run offsets into pnode
   // pperm maps a patch's (type, level) order back to its element order
   uint16_t *pperm = nullptr;  // PATCH per patch
+  // run form of the FP32 element loop (dg_elem.cuh, k_patch_matvec_runs):
+  // per (type, level) position the 8 patch-local run indices of its
+  // vertices in the canonical stencil order (8 x 16 bits), and per run its
+  // node with bit 31 set when the run holds all the node's pairs
+  uint4 *plid = nullptr;      // PATCH per patch
+  uint32_t *prun = nullptr;   // one per run, at poff
   // compressed mode (the reference's compressLut): conn is released once the
   // patch tables exist and decoded from them on demand (mesh_conn)
   bool compressed = false;
@@ -119,6 +125,11 @@ void ensure_stencils(Context &ctx);
 // (rebuilt on ctx's stream when they differ from the last call's)
 template <typename T>
 const T *comb_table(Context &ctx, double lap_fac, double mass_fac);
+
+// the run-form FP32 element loop on a mesh with run tables (m.plid)
+template <bool DIR>
+void launch_matvec_runs(Context &ctx, const Mesh &m, const uint8_t *bdy, const float *x, float *y, double lap_fac,
+                        double mass_fac, const char *name, double bytes);
 
 // host-side generators (same mathematics as the reference's .inp tables)
 void gen_etype_masks(uint8_t masks[8 * 18]);

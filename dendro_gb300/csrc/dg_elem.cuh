@@ -381,6 +381,112 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
   }
 }
 
+// The same operator in FP32 from run-indexed tables (run form).  Per
+// patch: plid[p][t] holds, for the element at (type, level) position t, the
+// patch-local run (node) index of each of its 8 vertices in the canonical
+// (relabelled) order of its stencil, and prun[poff[p] + u] the node of run u
+// with bit 31 set when the run holds every pair of its node in the mesh.
+// One block of PATCH threads per patch, grid-strided, three barriers per
+// patch:
+//   1. x of every run's node into xs[u] (runs spread over the threads, so
+//      the node ids are read coalesced), ys[u] = 0;
+//   2. thread t = element t: x from xs through its 8 run indices, the
+//      element stencil, the 8 results added into ys with shared-memory
+//      atomics;
+//   3. each run's sum stored (complete runs) or added atomically to y.
+// No per-pair slots and no segmented scan: the shared traffic per element
+// is 8 loads and 8 atomic adds, against 8 stores, 16 loads and 8 stores in
+// the pair form above.
+constexpr uint32_t PRUN_COMPLETE = 1u << 31;
+constexpr int RUN_PER_THREAD = PATCH_ENT / PATCH;  // at most 8 runs per thread
+
+template <bool DIR>
+__global__ void __launch_bounds__(PATCH, 3)
+    k_patch_matvec_runs(const uint32_t *__restrict__ pmeta, const uint4 *__restrict__ plid,
+                        const uint32_t *__restrict__ prun, const uint64_t *__restrict__ poff,
+                        const uint16_t *__restrict__ pkeys, const uint16_t *__restrict__ pkcount, size_t E,
+                        size_t n_patch, const float *__restrict__ fsten, const uint8_t *__restrict__ bdy,
+                        const float *__restrict__ x, float *__restrict__ y, float lapf, float massf) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *cs = reinterpret_cast<float *>(smem_raw);
+  float *xs = cs + fsten_entries<float>();
+  float *ys = xs + PATCH_ENT;
+  float *sc = ys + PATCH_ENT;  // PKEY_MAX combined stencils (16-byte aligned)
+  for (int i = threadIdx.x; i < fsten_entries<float>(); i += PATCH) cs[i] = fsten[i];
+  const int tid = threadIdx.x;
+  for (size_t p = blockIdx.x; p < n_patch; p += gridDim.x) {
+    const int ne = (int)((E - p * PATCH) < (size_t)PATCH ? (E - p * PATCH) : (size_t)PATCH);
+    const uint64_t ub = poff[p];
+    const int nr = (int)(poff[p + 1] - ub);
+    const uint32_t kc = pkcount[p];
+    const bool comb = kc <= (uint32_t)PKEY_MAX;
+    __syncthreads();  // the previous patch is done with xs, ys and sc (and cs is loaded)
+    // 1. gather
+    uint32_t rn[RUN_PER_THREAD];
+#pragma unroll
+    for (int k = 0; k < RUN_PER_THREAD; k++) {
+      const int u = tid + k * PATCH;
+      rn[k] = 0;
+      if (u < nr) {
+        rn[k] = prun[ub + u];
+        const uint32_t g = rn[k] & ~PRUN_COMPLETE;
+        float xv = x[g];
+        if (DIR && bdy[g]) xv = 0.f;
+        xs[u] = xv;
+        ys[u] = 0.f;
+      }
+    }
+    if (comb) {
+      for (int i = tid; i < (int)kc * 64; i += PATCH) {
+        const uint32_t key = pkeys[p * PKEY_MAX + (i >> 6)];
+        const unsigned t = key >> 5, l = key & 31u;
+        const float h = exp2_neg(0.f, l);
+        const float *st = cs + t * fsten_stride<float>();
+        sc[(i >> 6) * sstride<float>() + (i & 63)] =
+            lapf * h * 0.5f * st[i & 63] + massf * h * h * h * 0.125f * st[64 + (i & 63)];
+      }
+    }
+    __syncthreads();
+    // 2. element stencils
+    if (tid < ne) {
+      const uint32_t me = pmeta[p * PATCH + tid];
+      const uint4 lw = plid[p * PATCH + tid];
+      const uint32_t lv[4] = {lw.x, lw.y, lw.z, lw.w};
+      int lid[8];
+#pragma unroll
+      for (int m = 0; m < 8; m++) lid[m] = (int)((lv[m >> 1] >> ((m & 1) * 16)) & 0xffffu);
+      float xv[8];
+#pragma unroll
+      for (int m = 0; m < 8; m++) xv[m] = xs[lid[m]];
+      auto put = [&](int m, float ym) { atomicAdd(&ys[lid[m]], ym); };
+      if (comb) {
+        apply_comb(sc + ((me >> 16) & 255u) * sstride<float>(), xv, put);
+      } else {
+        const unsigned l = me & 255u, t = me >> 24;
+        const float h = exp2_neg(0.f, l);
+        apply_full(cs + t * fsten_stride<float>(), lapf * h * 0.5f, massf * h * h * h * 0.125f, xv, put);
+      }
+    }
+    __syncthreads();
+    // 3. run sums out
+#pragma unroll
+    for (int k = 0; k < RUN_PER_THREAD; k++) {
+      const int u = tid + k * PATCH;
+      if (u < nr) {
+        const uint32_t g = rn[k] & ~PRUN_COMPLETE;
+        if (DIR && bdy[g]) y[g] = x[g];
+        else if (rn[k] & PRUN_COMPLETE) y[g] = ys[u];
+        else atomicAdd(&y[g], ys[u]);
+      }
+    }
+  }
+}
+
+constexpr size_t patch_runs_smem() {
+  return fsten_entries<float>() * sizeof(float) + 2 * PATCH_ENT * sizeof(float) +
+         PKEY_MAX * sstride<float>() * sizeof(float);
+}
+
 template <typename T>
 constexpr size_t patch_smem() {
   return fsten_entries<T>() * sizeof(T) + patch_nbuf<T>() * PATCH_ENT * (sizeof(T) + sizeof(uint32_t)) +

@@ -73,6 +73,9 @@ struct Context {
   // 0 Morton, 1 Hilbert (the reference's HILBERT_ORDERING builds); the
   // octrees themselves are always kept in Morton order on the device
   int order = 0;
+  // FP32 element loop form: 0 the run form where the mesh has its tables,
+  // 1 the pair form (dg_ctx_set_matvec_form)
+  int matvec_form = 0;
 };
 
 // thrown inside the library, converted to a status code at the C ABI

@@ -258,3 +258,40 @@ def test_golden_reference_da_and_matvec(ctx):
     assert np.linalg.norm(y64 - r) <= FP64_RTOL * np.linalg.norm(r)
     y32 = da.matvec(x.astype(np.float32), precision=32).astype(np.float64)
     assert np.linalg.norm(y32 - r) <= FP32_RTOL * np.linalg.norm(r)
+
+
+@pytest.mark.parametrize("name", ["gauss", "lognormal", "clustered"])
+def test_fp32_matvec_both_loop_forms(ctx, oracle, name):
+    """The FP32 element loop's run form (the default) and its pair form give
+    the same operator: each within FP32_RTOL of the oracle's FP64 loop, and
+    the Dirichlet level operator of a hierarchy likewise."""
+    from dendro_gb300 import Context, MultiGrid
+
+    pts = CASES[name]()
+    c = Context(0)
+    bal = balanceOctree(points2Octree(pts, ctx=c))
+    da = DA(bal)
+    d = da.download()
+    oda = oracle.DA(bal.to_numpy(), 30)
+    x = np.sin(d["node_xyz"][:, 0] * 3e-9) + np.cos(d["node_xyz"][:, 1] * 2e-9) * (d["node_xyz"][:, 2] * 1e-9)
+    order_g = np.lexsort(d["node_xyz"].T[::-1])
+    order_o = np.lexsort(oda.node_xyz.T[::-1])
+    xo = np.empty(oda.n_node)
+    xo[order_o] = x[order_g]
+    ref = oda.matvec(xo)[order_o]
+    ys = {}
+    for form in ("runs", "pairs"):
+        c.set_matvec_form(form)
+        y = da.matvec(x.astype(np.float32), precision=32).astype(np.float64)[order_g]
+        assert np.linalg.norm(y - ref) <= FP32_RTOL * np.linalg.norm(ref), form
+        ys[form] = y
+    assert np.linalg.norm(ys["runs"] - ys["pairs"]) <= FP32_RTOL * np.linalg.norm(ref)
+    mg = MultiGrid(bal, max_coarse_elems=1000, ctx=c)
+    z = {}
+    for form in ("runs", "pairs"):
+        c.set_matvec_form(form)
+        z[form] = mg.matvec(0, x.astype(np.float32), precision=32).astype(np.float64)
+    y64 = mg.matvec(0, x, precision=64)
+    for form in ("runs", "pairs"):
+        assert np.linalg.norm(z[form] - y64) <= FP32_RTOL * np.linalg.norm(y64), form
+    c.set_matvec_form("runs")
