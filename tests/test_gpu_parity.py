@@ -260,7 +260,7 @@ def test_golden_reference_da_and_matvec(ctx):
     assert np.linalg.norm(y32 - r) <= FP32_RTOL * np.linalg.norm(r)
 
 
-@pytest.mark.parametrize("name", ["gauss", "lognormal", "clustered"])
+@pytest.mark.parametrize("name", ["gauss", "lognormal", "mixture"])
 def test_fp32_matvec_both_loop_forms(ctx, oracle, name):
     """The FP32 element loop's run form (the default) and its pair form give
     the same operator: each within FP32_RTOL of the oracle's FP64 loop, and
