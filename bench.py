@@ -578,9 +578,9 @@ def run_scale(args, dg, ctx, local):
         V, E = da.n_node, da.n_elem
         res["n_elem"], res["n_node"] = E, V
         mv = {}
-        # fp32: the run form of the FP32 loop (default); fp32_pairs: its pair form
+        # fp32 / fp64: the run form of the element loop (default); *_pairs: its pair form
         for name, prec, dt, form in (("fp32", 32, torch.float32, "runs"), ("fp32_pairs", 32, torch.float32, "pairs"),
-                                     ("fp64", 64, torch.float64, "runs")):
+                                     ("fp64", 64, torch.float64, "runs"), ("fp64_pairs", 64, torch.float64, "pairs")):
             ctx.set_matvec_form(form)
             x = torch.rand(V, dtype=dt, device=f"cuda:{local}") * 2 - 1
             y = torch.empty_like(x)
@@ -977,7 +977,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--serve-requests", type=int, default=SERVE_REQUESTS)
-    ap.add_argument("--serve-workers", type=int, default=6, help="solver streams of the batching server")
+    ap.add_argument("--serve-workers", type=int, default=8, help="solver streams of the batching server")
     ap.add_argument("--skip-serve", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")

@@ -874,39 +874,45 @@ const T *comb_table(Context &ctx, double lap_fac, double mass_fac) {
 template const float *comb_table<float>(Context &, double, double);
 template const double *comb_table<double>(Context &, double, double);
 
-// the run-form FP32 element loop (k_patch_matvec_runs); DIR: the
-// Dirichlet form, bdy the boundary flags
-template <bool DIR>
-void launch_matvec_runs(Context &ctx, const Mesh &m, const uint8_t *bdy, const float *x, float *y, double lap_fac,
+// the run-form element loop (k_patch_matvec_runs); DIR: the Dirichlet
+// form, bdy the boundary flags
+template <typename T, bool DIR>
+void launch_matvec_runs(Context &ctx, const Mesh &m, const uint8_t *bdy, const T *x, T *y, double lap_fac,
                         double mass_fac, const char *name, double bytes) {
-  const size_t smem = patch_runs_smem();
-  ensure_smem_attr(ctx, k_patch_matvec_runs<DIR>, (int)smem);
+  const size_t smem = patch_runs_smem<T>();
+  ensure_smem_attr(ctx, k_patch_matvec_runs<T, DIR>, (int)smem);
   int per_sm = 1;
-  DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_patch_matvec_runs<DIR>, PATCH, smem));
+  DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_patch_matvec_runs<T, DIR>, PATCH, smem));
   if (per_sm < 1) per_sm = 1;
   const unsigned grid = (unsigned)std::min<size_t>(m.n_patch, (size_t)per_sm * ctx.num_sms);
+  const T *cs = std::is_same<T, double>::value ? reinterpret_cast<const T *>(ctx.d_csten64)
+                                               : reinterpret_cast<const T *>(ctx.d_csten32);
+  const T *ctab = std::is_same<T, double>::value ? comb_table<T>(ctx, lap_fac, mass_fac) : nullptr;
   ProfScope _prof(ctx, name, bytes);
-  k_patch_matvec_runs<DIR><<<grid, PATCH, smem, ctx.stream>>>(m.pmeta, m.plid, m.prun, m.poff, m.pkeys, m.pkcount,
-                                                             m.n_elem, m.n_patch, ctx.d_csten32, bdy, x, y,
-                                                             (float)lap_fac, (float)mass_fac);
+  k_patch_matvec_runs<T, DIR><<<grid, PATCH, smem, ctx.stream>>>(m.pmeta, m.plid, m.prun, m.poff, m.pkeys,
+                                                                m.pkcount, m.n_elem, m.n_patch, cs, ctab, bdy, x, y,
+                                                                (T)lap_fac, (T)mass_fac);
   DG_LAUNCH_CHECK();
 }
-template void launch_matvec_runs<true>(Context &, const Mesh &, const uint8_t *, const float *, float *, double,
-                                       double, const char *, double);
-template void launch_matvec_runs<false>(Context &, const Mesh &, const uint8_t *, const float *, float *, double,
-                                        double, const char *, double);
+template void launch_matvec_runs<float, true>(Context &, const Mesh &, const uint8_t *, const float *, float *,
+                                              double, double, const char *, double);
+template void launch_matvec_runs<float, false>(Context &, const Mesh &, const uint8_t *, const float *, float *,
+                                               double, double, const char *, double);
+template void launch_matvec_runs<double, true>(Context &, const Mesh &, const uint8_t *, const double *, double *,
+                                               double, double, const char *, double);
+template void launch_matvec_runs<double, false>(Context &, const Mesh &, const uint8_t *, const double *,
+                                                double *, double, double, const char *, double);
 
 template <typename T>
 void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, double mass_fac) {
   ensure_stencils(ctx);
   cudaStream_t s = ctx.stream;
   DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
-  if constexpr (std::is_same<T, float>::value) {
-    if (m.plid && ctx.matvec_form != 1) {
-      launch_matvec_runs<false>(ctx, m, nullptr, x, y, lap_fac, mass_fac, "matvec_fp32",
-                                (double)m.n_elem * 36 + (double)m.n_node * 3 * sizeof(T));
-      return;
-    }
+  if (m.plid && ctx.matvec_form != 1) {
+    launch_matvec_runs<T, false>(ctx, m, nullptr, x, y, lap_fac, mass_fac,
+                                 sizeof(T) == 4 ? "matvec_fp32" : "matvec_fp64",
+                                 (double)m.n_elem * 36 + (double)m.n_node * 3 * sizeof(T));
+    return;
   }
   const size_t smem = patch_smem<T>();
   ensure_smem_attr(ctx, k_patch_matvec<T, false>, (int)smem);

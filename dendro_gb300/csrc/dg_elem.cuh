@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
   }
 }
 
-// The same operator in FP32 from run-indexed tables (run form).  Per
+// The same operator from run-indexed tables (run form).  Per
 // patch: plid[p][t] holds, for the element at (type, level) position t, the
 // patch-local run (node) index of each of its 8 vertices in the canonical
 // (relabelled) order of its stencil, and prun[poff[p] + u] the node of run u
@@ -400,19 +400,27 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
 constexpr uint32_t PRUN_COMPLETE = 1u << 31;
 constexpr int RUN_PER_THREAD = PATCH_ENT / PATCH;  // at most 8 runs per thread
 
-template <bool DIR>
-__global__ void __launch_bounds__(PATCH, 3)
+template <typename T, bool DIR>
+__global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
     k_patch_matvec_runs(const uint32_t *__restrict__ pmeta, const uint4 *__restrict__ plid,
                         const uint32_t *__restrict__ prun, const uint64_t *__restrict__ poff,
                         const uint16_t *__restrict__ pkeys, const uint16_t *__restrict__ pkcount, size_t E,
-                        size_t n_patch, const float *__restrict__ fsten, const uint8_t *__restrict__ bdy,
-                        const float *__restrict__ x, float *__restrict__ y, float lapf, float massf) {
+                        size_t n_patch, const T *__restrict__ fsten, const T *__restrict__ ctab,
+                        const uint8_t *__restrict__ bdy, const T *__restrict__ x, T *__restrict__ y, T lapf, T massf) {
+  // FP32 keeps the canonical stencils in shared memory and forms the
+  // patch's combined stencils from them; FP64 (whose arithmetic is the
+  // scarce resource) copies the combined stencils from the (type, level)
+  // table and reads the canonical ones from global memory on the rare
+  // patches with more than PKEY_MAX keys
+  constexpr bool F32 = sizeof(T) == 4;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float *cs = reinterpret_cast<float *>(smem_raw);
-  float *xs = cs + fsten_entries<float>();
-  float *ys = xs + PATCH_ENT;
-  float *sc = ys + PATCH_ENT;  // PKEY_MAX combined stencils (16-byte aligned)
-  for (int i = threadIdx.x; i < fsten_entries<float>(); i += PATCH) cs[i] = fsten[i];
+  T *cs = reinterpret_cast<T *>(smem_raw);
+  T *xs = cs + (F32 ? fsten_entries<T>() : 0);
+  T *ys = xs + PATCH_ENT;
+  T *sc = ys + PATCH_ENT;  // PKEY_MAX combined stencils (16-byte aligned)
+  if (F32)
+    for (int i = threadIdx.x; i < fsten_entries<T>(); i += PATCH) cs[i] = fsten[i];
+  const T *gst = F32 ? cs : fsten;
   const int tid = threadIdx.x;
   for (size_t p = blockIdx.x; p < n_patch; p += gridDim.x) {
     const int ne = (int)((E - p * PATCH) < (size_t)PATCH ? (E - p * PATCH) : (size_t)PATCH);
@@ -430,20 +438,24 @@ __global__ void __launch_bounds__(PATCH, 3)
       if (u < nr) {
         rn[k] = prun[ub + u];
         const uint32_t g = rn[k] & ~PRUN_COMPLETE;
-        float xv = x[g];
-        if (DIR && bdy[g]) xv = 0.f;
+        T xv = x[g];
+        if (DIR && bdy[g]) xv = (T)0;
         xs[u] = xv;
-        ys[u] = 0.f;
+        ys[u] = (T)0;
       }
     }
     if (comb) {
       for (int i = tid; i < (int)kc * 64; i += PATCH) {
         const uint32_t key = pkeys[p * PKEY_MAX + (i >> 6)];
         const unsigned t = key >> 5, l = key & 31u;
-        const float h = exp2_neg(0.f, l);
-        const float *st = cs + t * fsten_stride<float>();
-        sc[(i >> 6) * sstride<float>() + (i & 63)] =
-            lapf * h * 0.5f * st[i & 63] + massf * h * h * h * 0.125f * st[64 + (i & 63)];
+        if constexpr (F32) {
+          const T h = exp2_neg((T)0, l);
+          const T *st = cs + t * fsten_stride<T>();
+          sc[(i >> 6) * sstride<T>() + (i & 63)] =
+              lapf * h * (T)0.5 * st[i & 63] + massf * h * h * h * (T)0.125 * st[64 + (i & 63)];
+        } else {
+          sc[(i >> 6) * sstride<T>() + (i & 63)] = ctab[(t * COMB_LEVELS + l) * 64 + (i & 63)];
+        }
       }
     }
     __syncthreads();
@@ -455,16 +467,16 @@ __global__ void __launch_bounds__(PATCH, 3)
       int lid[8];
 #pragma unroll
       for (int m = 0; m < 8; m++) lid[m] = (int)((lv[m >> 1] >> ((m & 1) * 16)) & 0xffffu);
-      float xv[8];
+      T xv[8];
 #pragma unroll
       for (int m = 0; m < 8; m++) xv[m] = xs[lid[m]];
-      auto put = [&](int m, float ym) { atomicAdd(&ys[lid[m]], ym); };
+      auto put = [&](int m, T ym) { atomicAdd(&ys[lid[m]], ym); };
       if (comb) {
-        apply_comb(sc + ((me >> 16) & 255u) * sstride<float>(), xv, put);
+        apply_comb(sc + ((me >> 16) & 255u) * sstride<T>(), xv, put);
       } else {
         const unsigned l = me & 255u, t = me >> 24;
-        const float h = exp2_neg(0.f, l);
-        apply_full(cs + t * fsten_stride<float>(), lapf * h * 0.5f, massf * h * h * h * 0.125f, xv, put);
+        const T h = exp2_neg((T)0, l);
+        apply_full(gst + t * fsten_stride<T>(), lapf * h * (T)0.5, massf * h * h * h * (T)0.125, xv, put);
       }
     }
     __syncthreads();
@@ -482,9 +494,10 @@ __global__ void __launch_bounds__(PATCH, 3)
   }
 }
 
+template <typename T>
 constexpr size_t patch_runs_smem() {
-  return fsten_entries<float>() * sizeof(float) + 2 * PATCH_ENT * sizeof(float) +
-         PKEY_MAX * sstride<float>() * sizeof(float);
+  return (sizeof(T) == 4 ? fsten_entries<T>() * sizeof(T) : 0) + 2 * PATCH_ENT * sizeof(T) +
+         PKEY_MAX * sstride<T>() * sizeof(T);
 }
 
 template <typename T>

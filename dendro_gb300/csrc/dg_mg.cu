@@ -527,12 +527,11 @@ void dirichlet_matvec(Context &ctx, const MGLevel &L, const T *x, T *y) {
   cudaStream_t s = ctx.stream;
   const Mesh &m = L.mesh;
   DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
-  if constexpr (std::is_same<T, float>::value) {
-    if (m.plid && ctx.matvec_form != 1) {
-      launch_matvec_runs<true>(ctx, m, L.bdy, x, y, 1.0, 1.0, "dirichlet_matvec_fp32",
-                               (double)m.n_elem * 36 + (double)m.n_node * (3 * sizeof(T) + 1));
-      return;
-    }
+  if (m.plid && ctx.matvec_form != 1) {
+    launch_matvec_runs<T, true>(ctx, m, L.bdy, x, y, 1.0, 1.0,
+                                sizeof(T) == 4 ? "dirichlet_matvec_fp32" : "dirichlet_matvec_fp64",
+                                (double)m.n_elem * 36 + (double)m.n_node * (3 * sizeof(T) + 1));
+    return;
   }
   const size_t smem = patch_smem<T>();
   ensure_smem_attr(ctx, k_patch_matvec<T, true>, (int)smem);

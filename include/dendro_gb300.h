@@ -83,12 +83,13 @@ int dg_ctx_get_order(dg_ctx ctx, int *order);
 const char *dg_status_string(int status);
 int dg_version(void);
 
-/* Form of the FP32 element loop (dg_matvec, dg_mg_matvec and the FP32
- * V-cycle): DG_MATVEC_RUNS (the default) sums each element's results into
- * patch-local node slots, DG_MATVEC_PAIRS sums them through per-pair slots
- * and a segmented scan.  Both give the same operator (to FP32 rounding); a
- * compressed DA and the per-element-factor and FP64 loops always use the
- * pair form.  No counterpart in the reference. */
+/* Form of the element loop (dg_matvec, dg_mg_matvec, the V-cycle and the
+ * CG operator, FP32 and FP64): DG_MATVEC_RUNS (the default) sums each
+ * element's results into patch-local node slots, DG_MATVEC_PAIRS sums them
+ * through per-pair slots and a segmented scan.  Both give the same operator
+ * (to the rounding of the precision); a compressed DA and the
+ * per-element-factor loop always use the pair form.  No counterpart in the
+ * reference. */
 #define DG_MATVEC_RUNS 0
 #define DG_MATVEC_PAIRS 1
 int dg_ctx_set_matvec_form(dg_ctx ctx, int form);

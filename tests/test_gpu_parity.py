@@ -297,3 +297,36 @@ def test_fp32_matvec_both_loop_forms(ctx, oracle, name):
     for form in ("runs", "pairs"):
         assert np.linalg.norm(z[form] - y64) <= FP32_RTOL * np.linalg.norm(y64), form
     c.set_matvec_form("runs")
+
+
+@pytest.mark.parametrize("name", ["gauss", "mixture"])
+def test_fp64_matvec_both_loop_forms(ctx, oracle, name):
+    """The FP64 element loop in run form (the default) and in pair form:
+    each within FP64_RTOL of the oracle's loop, and the Dirichlet level
+    operator likewise between the two forms."""
+    from dendro_gb300 import Context, MultiGrid
+
+    pts = CASES[name]()
+    c = Context(0)
+    bal = balanceOctree(points2Octree(pts, ctx=c))
+    da = DA(bal)
+    d = da.download()
+    oda = oracle.DA(bal.to_numpy(), 30)
+    x = np.random.Generator(np.random.PCG64(11)).uniform(-1.0, 1.0, da.n_node)
+    order_g = np.lexsort(d["node_xyz"].T[::-1])
+    order_o = np.lexsort(oda.node_xyz.T[::-1])
+    xo = np.empty(oda.n_node)
+    xo[order_o] = x[order_g]
+    ref = oda.matvec(xo)[order_o]
+    ys = {}
+    for form in ("runs", "pairs"):
+        c.set_matvec_form(form)
+        ys[form] = da.matvec(x, precision=64)[order_g]
+        assert np.linalg.norm(ys[form] - ref) <= FP64_RTOL * np.linalg.norm(ref), form
+    mg = MultiGrid(bal, max_coarse_elems=1000, ctx=c)
+    z = {}
+    for form in ("runs", "pairs"):
+        c.set_matvec_form(form)
+        z[form] = mg.matvec(0, x, precision=64)
+    assert np.linalg.norm(z["runs"] - z["pairs"]) <= FP64_RTOL * np.linalg.norm(z["pairs"])
+    c.set_matvec_form("runs")
