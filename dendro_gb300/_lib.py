@@ -121,6 +121,7 @@ def _declare(L):
         "dg_debug_lookback_timeout": ([P, SZ, U], I),
         "dg_tree_sort": ([P, P, SZ, U, U, I, P, I, ctypes.POINTER(SZ)], I),
         "dg_ctx_set_matvec_form": ([P, I], I),
+        "dg_dense_spd_inverse": ([P, P, SZ], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -181,6 +181,9 @@ int dg_ctx_destroy(dg_ctx ctx) {
   if (ctx->c.d_etype_mask) cudaFree(ctx->c.d_etype_mask);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->c.side_ev[0]) cudaEventDestroy(ctx->c.side_ev[0]);
+  if (ctx->c.side_ev[1]) cudaEventDestroy(ctx->c.side_ev[1]);
+  if (ctx->c.side) cudaStreamDestroy(ctx->c.side);
   if (ctx->c.own_stream && ctx->c.stream) cudaStreamDestroy(ctx->c.stream);
   delete ctx;
   return DG_OK;
@@ -243,6 +246,15 @@ int dg_ctx_set_matvec_form(dg_ctx ctx, int form) {
   if (!ctx || (form != 0 && form != 1)) return DG_ERR_INVALID_ARG;
   ctx->c.matvec_form = form;
   return DG_OK;
+}
+
+int dg_dense_spd_inverse(dg_ctx ctx, float *X, size_t n) {
+  if (!X && n) return DG_ERR_INVALID_ARG;
+  return guarded(ctx, [&]() {
+    if (n > 20000) dg::fail(DG_ERR_INVALID_ARG, "dense inverse: at most 20000 rows");
+    dg::coarse_inverse(ctx->c, X, n);
+    dg::check_device_flags(ctx->c, "dense inverse");
+  });
 }
 
 int dg_debug_lookback_timeout(dg_ctx ctx, size_t n_keys, unsigned skipped_tiles) {

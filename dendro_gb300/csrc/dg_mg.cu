@@ -201,223 +201,6 @@ __global__ void k_set_bdy_identity(const uint8_t *__restrict__ bdy, size_t n, do
   if (i < n && bdy[i]) A[i * n + i] = 1.0;
 }
 
-// ---- coarsest level: FP32 inverse by block Gauss-Jordan, FP64 refinement
-// In-place block Gauss-Jordan (no pivoting: the operator is SPD).  For each
-// block K of GJB pivots, with R the other indices and P = inv(X_KK):
-//   X_RR -= (X_RK P) X_KR,  X_KR = P X_KR,  X_RK = -(X_RK P),  X_KK = P;
-// after the last block X holds the inverse (n^3 FP32 multiply-adds).
-// Each block costs two launches: k_bgj_diag inverts X_KK (one CTA), then
-// k_bgj_step updates every 64 x 64 tile at once (a CTA per tile row and
-// tjn tile columns, about four CTAs per SM).  So that no tile is
-// overwritten while another CTA of the same launch still reads it, the new
-// row K and column K go to scratch strips (R: GJB x n, C: n x GJB,
-// double-buffered by block parity) and reach X one block later: a tile in
-// the previous block's row or column is read from its strip, and
-// k_bgj_flush writes the last strips into X.
-constexpr int GJB = 64;
-constexpr int GJT = 64 + 4;  // shared tile row stride (floats)
-
-// P = inv(X_KK) for one diagonal block (one CTA of 256 threads): thread t
-// holds 16 entries of row t / 4 in registers; per pivot the pivot row goes
-// through shared memory (double-buffered, one barrier) and each row's pivot
-// column entry comes by a shuffle within the row's four threads.  A partial
-// last block is padded with the identity; P is written as a full GJB x GJB
-// block.
-__global__ void __launch_bounds__(256) k_bgj_diag(const float *__restrict__ X, size_t n, size_t k0, int b,
-                                                  float *__restrict__ P) {
-  static_assert(GJB == 64, "one CTA of 256 threads covers a 64 x 64 block");
-  __shared__ float prow[2][GJB];
-  const int t = threadIdx.x, r = t >> 2, c0 = (t & 3) * 16;
-  const int lane = t & 31, base = lane & ~3;
-  float v[16];
-#pragma unroll
-  for (int i = 0; i < 16; i++) {
-    const int c = c0 + i;
-    v[i] = (r < b && c < b) ? X[(k0 + r) * n + k0 + c] : (r == c ? 1.f : 0.f);
-  }
-#pragma unroll
-  for (int p = 0; p < GJB; p++) {
-    float *pr = prow[p & 1];
-    if (r == p) {
-#pragma unroll
-      for (int i = 0; i < 16; i++) pr[c0 + i] = v[i];
-    }
-    __syncthreads();
-    const float inv = 1.0f / pr[p];
-    const float f = __shfl_sync(0xffffffffu, v[p & 15], base | (p >> 4));  // this row's entry in column p
-#pragma unroll
-    for (int i = 0; i < 16; i++) {
-      const int c = c0 + i;
-      if (r == p) v[i] = (c == p) ? inv : v[i] * inv;
-      else v[i] = (c == p) ? -f * inv : v[i] - f * pr[c] * inv;
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < 16; i++) P[r * GJB + c0 + i] = v[i];
-}
-
-// where tile entries live while the block steps run: X, or the strips of
-// the previous block pk (R: its rows, C: its columns)
-struct GjSrc {
-  const float *X, *R, *C;
-  size_t n;
-  long pk;  // previous block's tile index, -1 before the first block
-  // the tile at (i0, j0) (multiples of GJB) lies wholly in X, in the R strip
-  // or in the C strip: its first entry and row stride
-  __device__ __forceinline__ const float *tile(size_t i0, size_t j0, size_t *ld) const {
-    if ((long)(i0 / GJB) == pk) {
-      *ld = n;
-      return R + j0;
-    }
-    if ((long)(j0 / GJB) == pk) {
-      *ld = GJB;
-      return C + i0 * GJB;
-    }
-    *ld = n;
-    return X + i0 * n + j0;
-  }
-};
-
-// shared tile T[m][r] = src(i0 + r, j0 + m) (transposed) or T[m][c] =
-// src(i0 + m, j0 + c) (as is); entries outside n x n are 0
-__device__ __forceinline__ void gj_load(float *T, const GjSrc &src, size_t i0, size_t j0, bool transposed) {
-  size_t ld;
-  const float *t = src.tile(i0, j0, &ld);
-  const int rows = (int)(src.n - i0 < 64 ? src.n - i0 : 64), cols = (int)(src.n - j0 < 64 ? src.n - j0 : 64);
-  for (int q = threadIdx.x; q < 64 * 64; q += 256) {
-    const int a = q >> 6, bb = q & 63;  // a: row of the source tile, bb: its column
-    const float v = (a < rows && bb < cols) ? t[(size_t)a * ld + bb] : 0.f;
-    if (transposed) T[bb * GJT + a] = v;
-    else T[a * GJT + bb] = v;
-  }
-}
-
-// acc[4][4] += L R over the 64-deep product, L given transposed (Lt[m][r]),
-// R as is (R[m][c]); thread (ty, tx) owns rows 4ty.., columns 4tx..
-__device__ __forceinline__ void gj_mma(const float *Lt, const float *Rm, float2 (&acc)[4][2]) {
-  const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
-#pragma unroll 8
-  for (int m = 0; m < 64; m++) {
-    const float4 a = *reinterpret_cast<const float4 *>(&Lt[m * GJT + ty * 4]);
-    const float4 c4 = *reinterpret_cast<const float4 *>(&Rm[m * GJT + tx * 4]);
-    const float av[4] = {a.x, a.y, a.z, a.w};
-    const float2 b01 = make_float2(c4.x, c4.y), b23 = make_float2(c4.z, c4.w);
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-      const float2 ar = make_float2(av[r], av[r]);
-      acc[r][0] = ffma2(ar, b01, acc[r][0]);
-      acc[r][1] = ffma2(ar, b23, acc[r][1]);
-    }
-  }
-}
-
-// One block step.  A CTA takes one tile row ti and tjn consecutive tile
-// columns (grid ceil(nt / tjn) x nt, 256 threads, three 64 x GJT shared
-// tiles), so that U = X_iK P is formed once per row and CTA:
-//   row K:      R[:, j] = P X_Kj (R[:, K] = P);
-//   other rows: C[i, :] = -U on the tile in column K,
-//               X_ij -= U X_Kj on the others.
-__global__ void __launch_bounds__(256, 4) k_bgj_step(float *__restrict__ X, size_t n, size_t k0, size_t tjn,
-                                                  GjSrc src, const float *__restrict__ P, float *__restrict__ Rn,
-                                                  float *__restrict__ Cn) {
-  extern __shared__ __align__(16) float gsm[];
-  float *A = gsm, *B = gsm + 64 * GJT, *Q = gsm + 2 * 64 * GJT;
-  const size_t nt = (n + GJB - 1) / GJB;
-  const size_t tk = k0 / GJB, ti = blockIdx.y, tj0 = (size_t)blockIdx.x * tjn;
-  const size_t tj1 = tj0 + tjn < nt ? tj0 + tjn : nt;
-  const size_t i0 = ti * 64;
-  const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
-  float2 acc[4][2];
-  auto zero = [&]() {
-#pragma unroll
-    for (int r = 0; r < 4; r++) acc[r][0] = acc[r][1] = make_float2(0.f, 0.f);
-  };
-  auto accv = [&](int r, int c) {
-    return c < 2 ? (c == 0 ? acc[r][0].x : acc[r][0].y) : (c == 2 ? acc[r][1].x : acc[r][1].y);
-  };
-  if (ti == tk) {
-    // the pivot row: A = P transposed, then R[:, j] = P X_Kj per tile
-    for (int q = threadIdx.x; q < 64 * 64; q += 256) A[(q % 64) * GJT + q / 64] = P[q];
-    for (size_t tj = tj0; tj < tj1; tj++) {
-      const size_t j0 = tj * 64;
-      if (tj == tk) {
-        for (int q = threadIdx.x; q < 64 * 64; q += 256)
-          if (k0 + q % 64 < n) Rn[(q / 64) * n + k0 + q % 64] = P[q];
-        continue;
-      }
-      __syncthreads();  // B free again
-      gj_load(B, src, k0, j0, false);
-      __syncthreads();
-      zero();
-      gj_mma(A, B, acc);
-#pragma unroll
-      for (int r = 0; r < 4; r++)
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-          const size_t j = j0 + tx * 4 + c;
-          if (j < n) Rn[(size_t)(ty * 4 + r) * n + j] = accv(r, c);
-        }
-    }
-    return;
-  }
-  // U = X_iK P, kept transposed in A for the updates
-  gj_load(A, src, i0, k0, true);
-  for (int q = threadIdx.x; q < 64 * 64; q += 256) Q[(q / 64) * GJT + q % 64] = P[q];
-  __syncthreads();
-  zero();
-  gj_mma(A, Q, acc);
-  __syncthreads();  // every thread is done reading A and Q
-#pragma unroll
-  for (int r = 0; r < 4; r++) {
-    A[(tx * 4 + 0) * GJT + ty * 4 + r] = acc[r][0].x;
-    A[(tx * 4 + 1) * GJT + ty * 4 + r] = acc[r][0].y;
-    A[(tx * 4 + 2) * GJT + ty * 4 + r] = acc[r][1].x;
-    A[(tx * 4 + 3) * GJT + ty * 4 + r] = acc[r][1].y;
-  }
-  if (tk >= tj0 && tk < tj1) {  // this CTA holds the tile in column K: C = -U
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-      const size_t i = i0 + ty * 4 + r;
-      if (i < n)
-        *reinterpret_cast<float4 *>(&Cn[i * GJB + tx * 4]) =
-            make_float4(-acc[r][0].x, -acc[r][0].y, -acc[r][1].x, -acc[r][1].y);
-    }
-  }
-  for (size_t tj = tj0; tj < tj1; tj++) {
-    if (tj == tk) continue;
-    const size_t j0 = tj * 64;
-    __syncthreads();  // A written; B free again
-    gj_load(B, src, k0, j0, false);
-    __syncthreads();
-    zero();
-    gj_mma(A, B, acc);
-    size_t ld;
-    const float *own = src.tile(i0, j0, &ld);  // this tile's current values
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-      const size_t i = i0 + ty * 4 + r;
-      if (i >= n) continue;
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const size_t j = j0 + tx * 4 + c;
-        if (j < n) X[i * n + j] = own[(size_t)(ty * 4 + r) * ld + tx * 4 + c] - accv(r, c);
-      }
-    }
-  }
-}
-
-// the last block's strips into X
-__global__ void k_bgj_flush(float *__restrict__ X, size_t n, size_t k0, int b, const float *__restrict__ R,
-                            const float *__restrict__ C) {
-  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n * (size_t)b) return;
-  const size_t r = q / n, j = q % n;  // row k0 + r of R
-  X[(k0 + r) * n + j] = R[r * n + j];
-  const size_t i = q / b;
-  const int c = (int)(q % b);  // column k0 + c of C
-  if (i < k0 || i >= k0 + (size_t)b) X[i * n + k0 + c] = C[i * GJB + c];
-}
-
 // coarse solve x = A^-1 b to FP64 accuracy: x = X b, then CS_REFINE rounds of
 // r = b - A x (FP64), x += X r, with X the FP32 inverse and A the assembled
 // FP64 operator; one warp per row
@@ -752,30 +535,8 @@ void mg_setup(Context &ctx, const Octree &fine, size_t max_coarse_elem, MG &mg) 
     DG_LAUNCH_CHECK();
     k_to_float<<<grid_for(n * n, 256), 256, 0, s>>>(mg.ca64, n * n, mg.cinv32);
     DG_LAUNCH_CHECK();
-    {
-      ProfScope _prof_inv(ctx, "mg_coarse_inverse", (double)n * n * 4 * 2 * ((n + GJB - 1) / GJB));
-      const size_t nt = (n + GJB - 1) / GJB;
-      DBuf<float> P(GJB * GJB, s), R(2 * GJB * n, s), C(2 * n * GJB, s);
-      const int smem = 3 * 64 * GJT * (int)sizeof(float);
-      // tile columns per CTA: about four CTAs per SM over the nt x nt tiles
-      // (each CTA forms U once and reuses it across its columns)
-      const size_t tjn = std::max<size_t>(1, (nt * nt + 4 * ctx.num_sms - 1) / (4 * (size_t)ctx.num_sms));
-      ensure_smem_attr(ctx, k_bgj_step, smem);
-      long pk = -1;
-      for (size_t k0 = 0, step = 0; k0 < n; k0 += GJB, step++) {
-        const int b = (int)std::min<size_t>(GJB, n - k0);
-        const size_t cur = step & 1, prev = cur ^ 1;
-        k_bgj_diag<<<1, 256, 0, s>>>(mg.cinv32, n, k0, b, P.get());
-        GjSrc src{mg.cinv32, R.get() + prev * GJB * n, C.get() + prev * n * GJB, n, pk};
-        k_bgj_step<<<dim3((unsigned)((nt + tjn - 1) / tjn), (unsigned)nt), 256, smem, s>>>(
-            mg.cinv32, n, k0, tjn, src, P.get(), R.get() + cur * GJB * n, C.get() + cur * n * GJB);
-        pk = (long)(k0 / GJB);
-        if (k0 + GJB >= n)
-          k_bgj_flush<<<grid_for(n * (size_t)b, 256), 256, 0, s>>>(mg.cinv32, n, k0, b, R.get() + cur * GJB * n,
-                                                                   C.get() + cur * n * GJB);
-      }
-      DG_LAUNCH_CHECK();
-    }
+    coarse_inverse(ctx, mg.cinv32, n);
+    check_device_flags(ctx, "multigrid coarse inverse");
     DG_CUDA(cudaStreamSynchronize(s));
   } catch (...) {
     mg_free(ctx, mg);

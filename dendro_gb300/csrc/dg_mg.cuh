@@ -48,6 +48,9 @@ struct MGResult {
 // (examples/src/omg/blockDiag.cpp:1384-1425 coarsens to < 500 octants)
 void mg_setup(Context &ctx, const Octree &fine, size_t max_coarse_elem, MG &mg);
 void mg_free(Context &ctx, MG &mg);
+// in-place FP32 inverse of an SPD n x n row-major matrix on the device
+// (block Gauss-Jordan, rank-64 updates on the tensor cores; dg_coarse.cu)
+void coarse_inverse(Context &ctx, float *X, size_t n);
 
 // PCG to ||r|| / ||b|| <= rtol; residual, dot products and updates in FP64,
 // the V-cycle preconditioner in FP32 (precision 32) or FP64 (precision 64)

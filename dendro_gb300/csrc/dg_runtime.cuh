@@ -38,6 +38,10 @@ struct Context {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  // a second stream and two events for work that overlaps the main
+  // stream's (the coarse inverse's look-ahead), created on first use
+  cudaStream_t side = nullptr;
+  cudaEvent_t side_ev[2] = {nullptr, nullptr};
   uint32_t *d_flags = nullptr;     // device error bitmask (DGF_*)
   unsigned long long *d_scratch = nullptr;  // small device counters
   unsigned long long *h_scratch = nullptr;  // pinned mirror of d_scratch

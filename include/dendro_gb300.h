@@ -400,6 +400,14 @@ int dg_ctx_profile_entry(dg_ctx ctx, int index, char *name, size_t name_len, dou
  * Needs 1 <= skipped_tiles < tiles (4096 keys per tile) <= 2^20. */
 int dg_debug_lookback_timeout(dg_ctx ctx, size_t n_keys, unsigned skipped_tiles);
 
+/* In-place FP32 inverse of a symmetric positive definite n x n row-major
+ * matrix in device memory (n <= 20000), the routine that inverts the
+ * coarsest multigrid operator: block Gauss-Jordan without pivoting, the
+ * rank-64 trailing updates on the tensor cores (3xTF32).  Replaces the
+ * coarse LU the reference's PCMG configuration asks PETSc for
+ * (bin/options:206); no direct counterpart in Dendro itself. */
+int dg_dense_spd_inverse(dg_ctx ctx, float *X, size_t n);
+
 #ifdef __cplusplus
 }
 #endif
