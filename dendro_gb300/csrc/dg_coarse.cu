@@ -602,10 +602,14 @@ void coarse_inverse(Context &ctx, float *X, size_t n) {
     k_gj_strips<<<(unsigned)nb, 256, 0, st>>>(X, n, k0, b, P.get() + o * GJB * GJB, Cs.get() + o * n * GJB,
                                              Rs.get() + o * GJB * n);
   };
+  // an update CTA fills its SM (shared memory), so the update of the
+  // remaining tiles leaves some SMs to the side stream's diag and strips
+  const size_t side_sms = std::min<size_t>(16, (size_t)ctx.num_sms / 8);
   auto update = [&](size_t k, int mode, size_t tp) {
     const size_t o = k & 1, cnt = gj_tile_count(mode, nt);
     if (cnt == 0) return;
-    const unsigned grid = (unsigned)std::min<size_t>(cnt, (size_t)ctx.num_sms);
+    const size_t sms = mode == GJ_REST ? (size_t)ctx.num_sms - side_sms : (size_t)ctx.num_sms;
+    const unsigned grid = (unsigned)std::min<size_t>(cnt, sms);
     k_gj_update<<<grid, TC_THREADS, TC_SMEM, s>>>(X, n, k * GJB, Cs.get() + o * n * GJB, Rs.get() + o * GJB * n,
                                                   nt, mode, tp, ctx.d_flags);
   };
