@@ -398,7 +398,6 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
 // is 8 loads and 8 atomic adds, against 8 stores, 16 loads and 8 stores in
 // the pair form above.
 constexpr uint32_t PRUN_COMPLETE = 1u << 31;
-constexpr int RUN_PER_THREAD = PATCH_ENT / PATCH;  // at most 8 runs per thread
 
 template <typename T, bool DIR>
 __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
@@ -428,21 +427,22 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
     const int nr = (int)(poff[p + 1] - ub);
     const uint32_t kc = pkcount[p];
     const bool comb = kc <= (uint32_t)PKEY_MAX;
+    // this element's tables, loaded before the gather so that their latency
+    // overlaps it
+    uint32_t me = 0;
+    uint4 lw = make_uint4(0, 0, 0, 0);
+    if (tid < ne) {
+      me = pmeta[p * PATCH + tid];
+      lw = plid[p * PATCH + tid];
+    }
     __syncthreads();  // the previous patch is done with xs, ys and sc (and cs is loaded)
     // 1. gather
-    uint32_t rn[RUN_PER_THREAD];
-#pragma unroll
-    for (int k = 0; k < RUN_PER_THREAD; k++) {
-      const int u = tid + k * PATCH;
-      rn[k] = 0;
-      if (u < nr) {
-        rn[k] = prun[ub + u];
-        const uint32_t g = rn[k] & ~PRUN_COMPLETE;
-        T xv = x[g];
-        if (DIR && bdy[g]) xv = (T)0;
-        xs[u] = xv;
-        ys[u] = (T)0;
-      }
+    for (int u = tid; u < nr; u += PATCH) {
+      const uint32_t g = prun[ub + u] & ~PRUN_COMPLETE;
+      T xv = x[g];
+      if (DIR && bdy[g]) xv = (T)0;
+      xs[u] = xv;
+      ys[u] = (T)0;
     }
     if (comb) {
       for (int i = tid; i < (int)kc * 64; i += PATCH) {
@@ -461,8 +461,6 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
     __syncthreads();
     // 2. element stencils
     if (tid < ne) {
-      const uint32_t me = pmeta[p * PATCH + tid];
-      const uint4 lw = plid[p * PATCH + tid];
       const uint32_t lv[4] = {lw.x, lw.y, lw.z, lw.w};
       int lid[8];
 #pragma unroll
@@ -480,16 +478,12 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
       }
     }
     __syncthreads();
-    // 3. run sums out
-#pragma unroll
-    for (int k = 0; k < RUN_PER_THREAD; k++) {
-      const int u = tid + k * PATCH;
-      if (u < nr) {
-        const uint32_t g = rn[k] & ~PRUN_COMPLETE;
-        if (DIR && bdy[g]) y[g] = x[g];
-        else if (rn[k] & PRUN_COMPLETE) y[g] = ys[u];
-        else atomicAdd(&y[g], ys[u]);
-      }
+    // 3. run sums out (the run words are read again: cached since step 1)
+    for (int u = tid; u < nr; u += PATCH) {
+      const uint32_t r = prun[ub + u], g = r & ~PRUN_COMPLETE;
+      if (DIR && bdy[g]) y[g] = x[g];
+      else if (r & PRUN_COMPLETE) y[g] = ys[u];
+      else atomicAdd(&y[g], ys[u]);
     }
   }
 }
