@@ -629,14 +629,17 @@ __global__ void k_patch_nodes(const uint32_t *__restrict__ run_node, const uint3
 // counted from pexc) per slot in shared memory, then per (type, level)
 // position the runs of its vertices in the canonical order of its stencil
 // (vertex cperm[c][t] digit m at canonical position m), and per run its node
-// with the complete flag of its pairs
+// with the complete flag of its pairs and the domain-boundary flag of the
+// node (the Dirichlet rows and columns)
 __global__ void __launch_bounds__(PATCH) k_patch_runs(const uint16_t *__restrict__ pinc,
                                                       const uint16_t *__restrict__ pexc,
                                                       const uint32_t *__restrict__ pnode,
                                                       const uint64_t *__restrict__ poff,
                                                       const uint32_t *__restrict__ pmeta,
                                                       const uint32_t *__restrict__ cperm, size_t E,
-                                                      uint4 *__restrict__ plid, uint32_t *__restrict__ prun) {
+                                                      const uint32_t *__restrict__ node_xyz, size_t V,
+                                                      uint32_t dom, uint4 *__restrict__ plid,
+                                                      uint32_t *__restrict__ prun) {
   __shared__ uint16_t run_of[PATCH_ENT];
   const size_t p = blockIdx.x;
   const int t = threadIdx.x;
@@ -649,7 +652,10 @@ __global__ void __launch_bounds__(PATCH) k_patch_runs(const uint16_t *__restrict
       const uint32_t ent = pinc[p * PATCH_ENT + i];
       if (ent & ENT_START) {
         r++;
-        prun[ub + r] = pnode[ub + r] | ((ent & ENT_COMPLETE) ? PRUN_COMPLETE : 0u);
+        const uint32_t g = pnode[ub + r];
+        const uint32_t cx = node_xyz[g], cy = node_xyz[V + g], cz = node_xyz[2 * V + g];
+        const bool on_bdy = cx == 0 || cy == 0 || cz == 0 || cx == dom || cy == dom || cz == dom;
+        prun[ub + r] = g | ((ent & ENT_COMPLETE) ? PRUN_COMPLETE : 0u) | (on_bdy ? PRUN_BDY : 0u);
       }
       run_of[ent & ENT_SLOT] = (uint16_t)r;
     }
@@ -722,7 +728,7 @@ size_t mesh_bytes(const Mesh &m) {
 static void mesh_patches(Context &ctx, Mesh &m) {
   cudaStream_t s = ctx.stream;
   const size_t n = m.n_elem, np = (n + PATCH - 1) / PATCH;
-  if (m.n_node >= (size_t)RUN_BDY) fail(DG_ERR_INVALID_ARG, "DA: too many nodes for the element loop tables");
+  if (m.n_node >= (size_t)PRUN_BDY) fail(DG_ERR_INVALID_ARG, "DA: too many nodes for the element loop tables");
   DBuf<uint32_t> pairs(m.n_node, s), run_node(np * PATCH_ENT, s), n_run(np, s);
   DBuf<uint16_t> pinc(np * PATCH_ENT, s), pexc(np * PATCH, s);
   DBuf<uint32_t> pmeta(np * PATCH, s);
@@ -760,7 +766,8 @@ static void mesh_patches(Context &ctx, Mesh &m) {
     {
       ProfScope _prof(ctx, "da_patch_runs", (double)n * (16 + 2 + 4 + 16) + (double)nruns * 8);
       k_patch_runs<<<(unsigned)np, PATCH, 0, s>>>(pinc.get(), pexc.get(), pnode.get(), poff.get(), pmeta.get(),
-                                                  ctx.d_cperm, n, plid.get(), prun.get());
+                                                  ctx.d_cperm, n, m.node_xyz, m.n_node, 1u << m.max_depth,
+                                                  plid.get(), prun.get());
       DG_LAUNCH_CHECK();
     }
     m.plid = plid.release_ptr();
@@ -875,9 +882,9 @@ template const float *comb_table<float>(Context &, double, double);
 template const double *comb_table<double>(Context &, double, double);
 
 // the run-form element loop (k_patch_matvec_runs); DIR: the Dirichlet
-// form, bdy the boundary flags
+// form (boundary rows and columns from the run words' boundary flag)
 template <typename T, bool DIR>
-void launch_matvec_runs(Context &ctx, const Mesh &m, const uint8_t *bdy, const T *x, T *y, double lap_fac,
+void launch_matvec_runs(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac,
                         double mass_fac, const char *name, double bytes) {
   const size_t smem = patch_runs_smem<T>();
   ensure_smem_attr(ctx, k_patch_matvec_runs<T, DIR>, (int)smem);
@@ -890,17 +897,17 @@ void launch_matvec_runs(Context &ctx, const Mesh &m, const uint8_t *bdy, const T
   const T *ctab = std::is_same<T, double>::value ? comb_table<T>(ctx, lap_fac, mass_fac) : nullptr;
   ProfScope _prof(ctx, name, bytes);
   k_patch_matvec_runs<T, DIR><<<grid, PATCH, smem, ctx.stream>>>(m.pmeta, m.plid, m.prun, m.poff, m.pkeys,
-                                                                m.pkcount, m.n_elem, m.n_patch, cs, ctab, bdy, x, y,
+                                                                m.pkcount, m.n_elem, m.n_patch, cs, ctab, x, y,
                                                                 (T)lap_fac, (T)mass_fac);
   DG_LAUNCH_CHECK();
 }
-template void launch_matvec_runs<float, true>(Context &, const Mesh &, const uint8_t *, const float *, float *,
+template void launch_matvec_runs<float, true>(Context &, const Mesh &, const float *, float *,
                                               double, double, const char *, double);
-template void launch_matvec_runs<float, false>(Context &, const Mesh &, const uint8_t *, const float *, float *,
+template void launch_matvec_runs<float, false>(Context &, const Mesh &, const float *, float *,
                                                double, double, const char *, double);
-template void launch_matvec_runs<double, true>(Context &, const Mesh &, const uint8_t *, const double *, double *,
+template void launch_matvec_runs<double, true>(Context &, const Mesh &, const double *, double *,
                                                double, double, const char *, double);
-template void launch_matvec_runs<double, false>(Context &, const Mesh &, const uint8_t *, const double *,
+template void launch_matvec_runs<double, false>(Context &, const Mesh &, const double *,
                                                 double *, double, double, const char *, double);
 
 template <typename T>
@@ -909,7 +916,7 @@ void mesh_matvec(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac, 
   cudaStream_t s = ctx.stream;
   DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
   if (m.plid && ctx.matvec_form != 1) {
-    launch_matvec_runs<T, false>(ctx, m, nullptr, x, y, lap_fac, mass_fac,
+    launch_matvec_runs<T, false>(ctx, m, x, y, lap_fac, mass_fac,
                                  sizeof(T) == 4 ? "matvec_fp32" : "matvec_fp64",
                                  (double)m.n_elem * 36 + (double)m.n_node * 3 * sizeof(T));
     return;

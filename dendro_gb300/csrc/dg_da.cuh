@@ -128,7 +128,7 @@ const T *comb_table(Context &ctx, double lap_fac, double mass_fac);
 
 // the run-form element loop on a mesh with run tables (m.plid)
 template <typename T, bool DIR>
-void launch_matvec_runs(Context &ctx, const Mesh &m, const uint8_t *bdy, const T *x, T *y, double lap_fac,
+void launch_matvec_runs(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac,
                         double mass_fac, const char *name, double bytes);
 
 // host-side generators (same mathematics as the reference's .inp tables)

@@ -398,6 +398,8 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
 // is 8 loads and 8 atomic adds, against 8 stores, 16 loads and 8 stores in
 // the pair form above.
 constexpr uint32_t PRUN_COMPLETE = 1u << 31;
+constexpr uint32_t PRUN_BDY = 1u << 30;  // the run's node lies on the domain boundary
+constexpr uint32_t PRUN_NODE = PRUN_BDY - 1;
 
 template <typename T, bool DIR>
 __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
@@ -405,7 +407,7 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
                         const uint32_t *__restrict__ prun, const uint64_t *__restrict__ poff,
                         const uint16_t *__restrict__ pkeys, const uint16_t *__restrict__ pkcount, size_t E,
                         size_t n_patch, const T *__restrict__ fsten, const T *__restrict__ ctab,
-                        const uint8_t *__restrict__ bdy, const T *__restrict__ x, T *__restrict__ y, T lapf, T massf) {
+                        const T *__restrict__ x, T *__restrict__ y, T lapf, T massf) {
   // FP32 keeps the canonical stencils in shared memory and forms the
   // patch's combined stencils from them; FP64 (whose arithmetic is the
   // scarce resource) copies the combined stencils from the (type, level)
@@ -438,10 +440,8 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
     __syncthreads();  // the previous patch is done with xs, ys and sc (and cs is loaded)
     // 1. gather
     for (int u = tid; u < nr; u += PATCH) {
-      const uint32_t g = prun[ub + u] & ~PRUN_COMPLETE;
-      T xv = x[g];
-      if (DIR && bdy[g]) xv = (T)0;
-      xs[u] = xv;
+      const uint32_t r = prun[ub + u];
+      xs[u] = (DIR && (r & PRUN_BDY)) ? (T)0 : x[r & PRUN_NODE];
       ys[u] = (T)0;
     }
     if (comb) {
@@ -480,8 +480,8 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
     __syncthreads();
     // 3. run sums out (the run words are read again: cached since step 1)
     for (int u = tid; u < nr; u += PATCH) {
-      const uint32_t r = prun[ub + u], g = r & ~PRUN_COMPLETE;
-      if (DIR && bdy[g]) y[g] = x[g];
+      const uint32_t r = prun[ub + u], g = r & PRUN_NODE;
+      if (DIR && (r & PRUN_BDY)) y[g] = x[g];
       else if (r & PRUN_COMPLETE) y[g] = ys[u];
       else atomicAdd(&y[g], ys[u]);
     }

@@ -311,7 +311,7 @@ void dirichlet_matvec(Context &ctx, const MGLevel &L, const T *x, T *y) {
   const Mesh &m = L.mesh;
   DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(T), s));
   if (m.plid && ctx.matvec_form != 1) {
-    launch_matvec_runs<T, true>(ctx, m, L.bdy, x, y, 1.0, 1.0,
+    launch_matvec_runs<T, true>(ctx, m, x, y, 1.0, 1.0,
                                 sizeof(T) == 4 ? "dirichlet_matvec_fp32" : "dirichlet_matvec_fp64",
                                 (double)m.n_elem * 36 + (double)m.n_node * (3 * sizeof(T) + 1));
     return;
