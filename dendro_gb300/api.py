@@ -644,13 +644,14 @@ class MultiGrid:
         if on_dev:
             out = x.new_empty((n_out,))
         else:
-            x = np.ascontiguousarray(x, dtype=np.float64 if precision == 64 else np.float32)
+            x = np.ascontiguousarray(x, dtype=np.float32 if precision == 32 else np.float64)
             out = np.empty(n_out, x.dtype)
         check(self.ctx.handle, fn(self.ctx.handle, self.handle, level, _ptr(x), _ptr(out), precision, on_dev), fn.__name__)
         return out
 
     def matvec(self, level: int, x, precision: int = 64):
-        """DirichletJacobianMatMult on a level."""
+        """DirichletJacobianMatMult on a level: FP64 (64), FP32 (32), or FP64
+        vectors in double-single arithmetic (48)."""
         return self._op(self.ctx._L.dg_mg_matvec, level, x, self.sizes[level][1], precision)
 
     def restrict(self, fine_level: int, x, precision: int = 64):
@@ -664,9 +665,10 @@ class MultiGrid:
     def set_smoother(self, omega: float = 0.667, nu_pre: int = 2, nu_post: int = 2):
         check(self.ctx.handle, self.ctx._L.dg_mg_set_smoother(self.handle, omega, nu_pre, nu_post), "set_smoother")
 
-    def set_cg_operator(self, precision: int = 64, reliable_delta: float = 1e-3):
-        """The CG's operator q = A p with an FP32 V-cycle: FP64 every
-        iteration (64), or FP32 with FP64 residual replacement (32)."""
+    def set_cg_operator(self, precision: int = 48, reliable_delta: float = 1e-3):
+        """The CG's operator q = A p with an FP32 V-cycle: double-single
+        arithmetic on FP64 vectors (48, the default), FP64 (64), or FP32
+        with FP64 residual replacement (32)."""
         check(self.ctx.handle, self.ctx._L.dg_mg_set_cg_operator(self.handle, precision, reliable_delta),
               "set_cg_operator")
 

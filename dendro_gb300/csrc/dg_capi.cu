@@ -174,6 +174,7 @@ int dg_ctx_destroy(dg_ctx ctx) {
   if (ctx->c.d_sten32) cudaFree(ctx->c.d_sten32);
   if (ctx->c.d_comb64) cudaFree(ctx->c.d_comb64);
   if (ctx->c.d_comb32) cudaFree(ctx->c.d_comb32);
+  if (ctx->c.d_comb_ds) cudaFree(ctx->c.d_comb_ds);
   if (ctx->c.d_csten64) cudaFree(ctx->c.d_csten64);
   if (ctx->c.d_csten32) cudaFree(ctx->c.d_csten32);
   if (ctx->c.d_cperm) cudaFree(ctx->c.d_cperm);
@@ -718,9 +719,11 @@ int dg_mg_level_octree(dg_ctx ctx, dg_mg mg, size_t level, uint32_t *xyzl, int d
 int dg_mg_matvec(dg_ctx ctx, dg_mg mg, size_t level, const void *in, void *out, int precision, int on_device) {
   if (!mg || level >= mg->mg.lv.size()) return DG_ERR_INVALID_ARG;
   const dg::MGLevel &L = mg->mg.lv[level];
-  return level_op(ctx, mg, L.mesh.n_node, L.mesh.n_node, in, out, precision, on_device,
+  const bool ds = precision == 48;  // FP64 vectors, double-single arithmetic
+  return level_op(ctx, mg, L.mesh.n_node, L.mesh.n_node, in, out, ds ? 64 : precision, on_device,
                   [&](dg::Context &c, const void *x, void *y) {
-                    if (precision == 64) dg::dirichlet_matvec<double>(c, L, (const double *)x, (double *)y);
+                    if (ds) dg::dirichlet_matvec_ds(c, L, (const double *)x, (double *)y);
+                    else if (precision == 64) dg::dirichlet_matvec<double>(c, L, (const double *)x, (double *)y);
                     else dg::dirichlet_matvec<float>(c, L, (const float *)x, (float *)y);
                   });
 }
@@ -752,7 +755,7 @@ int dg_mg_set_smoother(dg_mg mg, double omega, int nu_pre, int nu_post) {
 }
 
 int dg_mg_set_cg_operator(dg_mg mg, int precision, double reliable_delta) {
-  if (!mg || (precision != 32 && precision != 64) || !(reliable_delta > 0 && reliable_delta < 1))
+  if (!mg || (precision != 32 && precision != 48 && precision != 64) || !(reliable_delta > 0 && reliable_delta < 1))
     return DG_ERR_INVALID_ARG;
   mg->mg.cg_operator = precision;
   mg->mg.reliable_delta = reliable_delta;

@@ -914,6 +914,48 @@ const T *comb_table(Context &ctx, double lap_fac, double mass_fac) {
 template const float *comb_table<float>(Context &, double, double);
 template const double *comb_table<double>(Context &, double, double);
 
+__global__ void k_split_pairs(const double *__restrict__ in, size_t n, float2 *__restrict__ out) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = in[i];
+  const float hi = __double2float_rn(v);
+  out[i] = make_float2(hi, __double2float_rn(v - (double)hi));
+}
+
+const float2 *comb_table_ds(Context &ctx, double lap_fac, double mass_fac) {
+  if (!ctx.d_comb_ds) DG_CUDA(cudaMalloc((void **)&ctx.d_comb_ds, COMB_ENTRIES * sizeof(float2)));
+  if (!ctx.comb_ds_ok || ctx.comb_ds_f[0] != lap_fac || ctx.comb_ds_f[1] != mass_fac) {
+    const double *d = comb_table<double>(ctx, lap_fac, mass_fac);
+    k_split_pairs<<<(COMB_ENTRIES + 255) / 256, 256, 0, ctx.stream>>>(d, COMB_ENTRIES, ctx.d_comb_ds);
+    DG_LAUNCH_CHECK();
+    ctx.comb_ds_f[0] = lap_fac;
+    ctx.comb_ds_f[1] = mass_fac;
+    ctx.comb_ds_ok = true;
+  }
+  return ctx.d_comb_ds;
+}
+
+// the double-single run-form loop (k_patch_matvec_runs_ds): FP64 vectors
+template <bool DIR>
+void launch_matvec_runs_ds(Context &ctx, const Mesh &m, const double *x, double *y, double lap_fac,
+                           double mass_fac, const char *name, double bytes) {
+  const size_t smem = patch_runs_ds_smem();
+  ensure_smem_attr(ctx, k_patch_matvec_runs_ds<DIR>, (int)smem);
+  int per_sm = 1;
+  DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_patch_matvec_runs_ds<DIR>, PATCH, smem));
+  if (per_sm < 1) per_sm = 1;
+  const unsigned grid = (unsigned)std::min<size_t>(m.n_patch, (size_t)per_sm * ctx.num_sms);
+  const float2 *ctab = comb_table_ds(ctx, lap_fac, mass_fac);
+  ProfScope _prof(ctx, name, bytes);
+  k_patch_matvec_runs_ds<DIR><<<grid, PATCH, smem, ctx.stream>>>(m.pmeta, m.plid, m.prun, m.poff, m.pkeys,
+                                                                 m.pkcount, m.n_elem, m.n_patch, ctab, x, y);
+  DG_LAUNCH_CHECK();
+}
+template void launch_matvec_runs_ds<true>(Context &, const Mesh &, const double *, double *, double, double,
+                                          const char *, double);
+template void launch_matvec_runs_ds<false>(Context &, const Mesh &, const double *, double *, double, double,
+                                           const char *, double);
+
 // the run-form element loop (k_patch_matvec_runs); DIR: the Dirichlet
 // form (boundary rows and columns from the run words' boundary flag)
 template <typename T, bool DIR>

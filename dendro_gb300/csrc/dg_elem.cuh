@@ -488,6 +488,112 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
   }
 }
 
+// ---- double-single (FP32 pair) form of the run-form loop: the CG operator
+// of the FP32-V-cycle solve.  GB300 issues FP64 at 2 multiply-adds per
+// clock per SM, and the FP64 loop is bound by that.  Here each stencil
+// entry a and each gathered x are pairs (hi, lo) of FP32 values with
+// hi + lo equal to the FP64 value to about 2^-48; each product is formed
+// exactly (hi * hi and its rounding error by an FMA, plus the two cross
+// terms) and the 8 products of a row are summed with an error-free sum
+// (TwoSum) into a (hi, lo) pair, so a row is exact to about 2^-46 of the
+// sum of its terms' magnitudes; the row result goes to FP64 (hi + lo is
+// exact there) and is added across elements in FP64 as in the FP64 loop.
+// Per element that is 8 FP64 adds instead of 64 FP64 multiply-adds.
+// The explicit _rn intrinsics keep the compiler from fusing the sums with
+// the products.
+__device__ __forceinline__ void ds_term(float &sh, float &sl, float ah, float al, float2 x) {
+  const float ph = __fmul_rn(ah, x.x);
+  float pl = fmaf(ah, x.x, -ph);
+  pl = fmaf(ah, x.y, pl);
+  pl = fmaf(al, x.x, pl);
+  const float s = __fadd_rn(sh, ph);
+  const float v = __fsub_rn(s, sh);
+  const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, v)), __fsub_rn(ph, v));
+  sl = __fadd_rn(sl, __fadd_rn(e, pl));
+  sh = s;
+}
+
+constexpr int DS_STRIDE = 64;  // float2 entries per combined stencil in shared memory
+
+// ctab: the combined stencils of every (type, level) as (hi, lo) pairs
+template <bool DIR>
+__global__ void __launch_bounds__(PATCH, 2)
+    k_patch_matvec_runs_ds(const uint32_t *__restrict__ pmeta, const uint4 *__restrict__ plid,
+                           const uint32_t *__restrict__ prun, const uint64_t *__restrict__ poff,
+                           const uint16_t *__restrict__ pkeys, const uint16_t *__restrict__ pkcount, size_t E,
+                           size_t n_patch, const float2 *__restrict__ ctab, const double *__restrict__ x,
+                           double *__restrict__ y) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *xs = reinterpret_cast<float2 *>(smem_raw);
+  double *ys = reinterpret_cast<double *>(xs + PATCH_ENT);
+  float2 *sc = reinterpret_cast<float2 *>(ys + PATCH_ENT);  // PKEY_MAX combined stencils
+  const int tid = threadIdx.x;
+  for (size_t p = blockIdx.x; p < n_patch; p += gridDim.x) {
+    const int ne = (int)((E - p * PATCH) < (size_t)PATCH ? (E - p * PATCH) : (size_t)PATCH);
+    const uint64_t ub = poff[p];
+    const int nr = (int)(poff[p + 1] - ub);
+    const uint32_t kc = pkcount[p];
+    const bool comb = kc <= (uint32_t)PKEY_MAX;
+    uint32_t me = 0;
+    uint4 lw = make_uint4(0, 0, 0, 0);
+    if (tid < ne) {
+      me = pmeta[p * PATCH + tid];
+      lw = plid[p * PATCH + tid];
+    }
+    __syncthreads();  // the previous patch is done with xs, ys and sc
+    // 1. gather, each x split into (hi, lo)
+    for (int u = tid; u < nr; u += PATCH) {
+      const uint32_t r = prun[ub + u];
+      const double xv = (DIR && (r & PRUN_BDY)) ? 0.0 : x[r & PRUN_NODE];
+      const float hi = __double2float_rn(xv);
+      xs[u] = make_float2(hi, __double2float_rn(xv - (double)hi));
+      ys[u] = 0.0;
+    }
+    if (comb) {
+      for (int i = tid; i < (int)kc * 64; i += PATCH) {
+        const uint32_t key = pkeys[p * PKEY_MAX + (i >> 6)];
+        sc[(i >> 6) * DS_STRIDE + (i & 63)] = ctab[((key >> 5) * COMB_LEVELS + (key & 31u)) * 64 + (i & 63)];
+      }
+    }
+    __syncthreads();
+    // 2. element stencils
+    if (tid < ne) {
+      const uint32_t lv[4] = {lw.x, lw.y, lw.z, lw.w};
+      int lid[8];
+#pragma unroll
+      for (int m = 0; m < 8; m++) lid[m] = (int)((lv[m >> 1] >> ((m & 1) * 16)) & 0xffffu);
+      float2 xv[8];
+#pragma unroll
+      for (int m = 0; m < 8; m++) xv[m] = xs[lid[m]];
+      const float2 *S = comb ? sc + ((me >> 16) & 255u) * DS_STRIDE
+                             : ctab + ((me >> 24) * COMB_LEVELS + (me & 31u)) * 64;
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        float sh = 0.f, sl = 0.f;
+#pragma unroll
+        for (int j2 = 0; j2 < 4; j2++) {
+          const float4 a2 = reinterpret_cast<const float4 *>(S + 8 * k)[j2];
+          ds_term(sh, sl, a2.x, a2.y, xv[2 * j2]);
+          ds_term(sh, sl, a2.z, a2.w, xv[2 * j2 + 1]);
+        }
+        atomicAdd(&ys[lid[k]], (double)sh + (double)sl);
+      }
+    }
+    __syncthreads();
+    // 3. run sums out
+    for (int u = tid; u < nr; u += PATCH) {
+      const uint32_t r = prun[ub + u], g = r & PRUN_NODE;
+      if (DIR && (r & PRUN_BDY)) y[g] = x[g];
+      else if (r & PRUN_COMPLETE) y[g] = ys[u];
+      else atomicAdd(&y[g], ys[u]);
+    }
+  }
+}
+
+constexpr size_t patch_runs_ds_smem() {
+  return PATCH_ENT * sizeof(float2) + PATCH_ENT * sizeof(double) + PKEY_MAX * DS_STRIDE * sizeof(float2);
+}
+
 template <typename T>
 constexpr size_t patch_runs_smem() {
   return (sizeof(T) == 4 ? fsten_entries<T>() * sizeof(T) : 0) + 2 * PATCH_ENT * sizeof(T) +

@@ -605,6 +605,8 @@ void mg_solve(Context &ctx, MG &mg, const double *b, double *x, int precision, d
       dirichlet_matvec<float>(ctx, L0, p32.get(), q32.get());
       k_to_double<<<g, 256, 0, s>>>(q32.get(), n, q.get());
       DG_LAUNCH_CHECK();
+    } else if (precision == 32 && mg.cg_operator == 48) {
+      dirichlet_matvec_ds(ctx, L0, p.get(), q.get());
     } else {
       dirichlet_matvec<double>(ctx, L0, p.get(), q.get());
     }
@@ -674,6 +676,18 @@ void mg_solve(Context &ctx, MG &mg, const double *b, double *x, int precision, d
   dot(r.get(), nullptr, d_rr);
   res.iterations = it;
   res.relres = std::sqrt(read_scalar(ctx, d_rr)) / bnorm;
+}
+
+void dirichlet_matvec_ds(Context &ctx, const MGLevel &L, const double *x, double *y) {
+  const Mesh &m = L.mesh;
+  if (!m.plid) {
+    dirichlet_matvec<double>(ctx, L, x, y);
+    return;
+  }
+  ensure_stencils(ctx);
+  DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(double), ctx.stream));
+  launch_matvec_runs_ds<true>(ctx, m, x, y, 1.0, 1.0, "dirichlet_matvec_ds",
+                              (double)m.n_elem * 36 + (double)m.n_node * (3 * sizeof(double) + 1));
 }
 
 template void dirichlet_matvec<float>(Context &, const MGLevel &, const float *, float *);

@@ -30,11 +30,12 @@ struct MG {
   float *cinv32 = nullptr;   // its inverse in FP32 (refined in FP64 when applied)
   double omega = 0.667;  // Jacobi damping (bin/options:190)
   int nu_pre = 2, nu_post = 2;
-  // CG operator with an FP32 V-cycle: 64 applies A p in FP64 every
-  // iteration; 32 applies it in FP32 and replaces the recurrence residual by
-  // the FP64 residual b - A x whenever it has fallen by reliable_delta since
-  // the last replacement (and before stopping)
-  int cg_operator = 64;
+  // CG operator with an FP32 V-cycle: 48 (the default) applies A p in
+  // double-single arithmetic on FP64 vectors (about 2^-46 relative per
+  // element row); 64 in FP64; 32 in FP32, with the recurrence residual
+  // replaced by the FP64 residual b - A x whenever it has fallen by
+  // reliable_delta since the last replacement (and before stopping)
+  int cg_operator = 48;
   double reliable_delta = 1e-3;
 };
 
@@ -59,6 +60,10 @@ void mg_solve(Context &ctx, MG &mg, const double *b, double *x, int precision, d
 // building blocks (level operators), exposed for tests and callers
 template <typename T>
 void dirichlet_matvec(Context &ctx, const MGLevel &L, const T *x, T *y);  // DirichletJacobianMatMult
+// the same operator on FP64 vectors in double-single arithmetic (FP32
+// pairs, about 2^-46 relative per element row; the FP64 loop where a mesh
+// has no run tables)
+void dirichlet_matvec_ds(Context &ctx, const MGLevel &L, const double *x, double *y);
 // DirichletJacobianMatGetDiagonal (omgJac.C:1111): 1 on boundary nodes
 void dirichlet_diagonal(Context &ctx, const MGLevel &L, double *diag);
 template <typename T>

@@ -61,6 +61,10 @@ struct Context {
   float *d_comb32 = nullptr;
   double comb64_f[2] = {0, 0}, comb32_f[2] = {0, 0};
   bool comb64_ok = false, comb32_ok = false;
+  // the FP64 combined stencils as (hi, lo) FP32 pairs (double-single loop)
+  float2 *d_comb_ds = nullptr;
+  double comb_ds_f[2] = {0, 0};
+  bool comb_ds_ok = false;
   bool prof = false;
   std::map<std::string, ProfStat> prof_stats;
   std::vector<ProfPending> prof_pending;

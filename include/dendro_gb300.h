@@ -322,7 +322,8 @@ int dg_mg_level_nodes(dg_ctx ctx, dg_mg mg, size_t level, uint32_t *node_xyz, in
 /* the level's balanced octree as {x, y, z, level} records */
 int dg_mg_level_octree(dg_ctx ctx, dg_mg mg, size_t level, uint32_t *xyzl, int dst_on_device);
 /* DirichletJacobianMatMult on a level: boundary rows identity, boundary
- * columns skipped.  precision 32 / 64 as dg_matvec. */
+ * columns skipped.  precision 32 / 64 as dg_matvec; 48: FP64 vectors in
+ * double-single arithmetic (the CG operator of dg_mg_set_cg_operator 48). */
 int dg_mg_matvec(dg_ctx ctx, dg_mg mg, size_t level, const void *in, void *out, int precision, int on_device);
 /* restrictMatVecType1: out (level+1) = R in (level); prolongMatVecType1:
  * out (level) = P in (level+1), P = R^T. */
@@ -332,8 +333,12 @@ int dg_mg_prolong(dg_ctx ctx, dg_mg mg, size_t fine_level, const void *in, void 
  * per V-cycle side (default 2 and 2) */
 int dg_mg_set_smoother(dg_mg mg, double omega, int nu_pre, int nu_post);
 /* The CG's own operator application q = A p when the V-cycle runs in FP32
- * (precision 32 of dg_mg_solve).  64 (the default): A p in FP64 every
- * iteration.  32: A p in FP32 (the FP32 element loop), and the recurrence
+ * (precision 32 of dg_mg_solve).  48 (the default): A p on the FP64
+ * vectors in double-single arithmetic (stencil entries and x as FP32 pairs,
+ * each element row exact to about 2^-46 of its terms, summed across
+ * elements in FP64; GB300's FP64 pipe issues 2 multiply-adds per clock per
+ * SM).  64: A p in FP64 every iteration.  32: A p in FP32
+ * (the FP32 element loop), and the recurrence
  * residual replaced by the FP64 residual b - A x whenever it has fallen by
  * reliable_delta since the last replacement, and before the stopping test
  * accepts it ("reliable updates"); residual, dot products, updates and the

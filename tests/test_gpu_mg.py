@@ -159,3 +159,33 @@ def test_fp32_cg_operator_with_reliable_updates(ctx):
     assert np.linalg.norm(x32 - x64) <= 1e-6 * np.linalg.norm(x64)
     with pytest.raises(DendroError):
         mg.set_cg_operator(16)
+
+
+def test_double_single_operator(ctx):
+    """The double-single level operator (precision 48: FP64 vectors, FP32-pair
+    arithmetic) agrees with the FP64 operator to 1e-12 of its norm, and a
+    solve with it as the CG operator reaches the same FP64 relative residual
+    in the same number of iterations (within one) as the FP64 operator."""
+    pts = datagen.gaussian(200_000, 0.5, 0.15, seed=3)
+    bal = balanceOctree(points2Octree(pts, ctx=ctx))
+    mg = MultiGrid(bal, max_coarse_elems=4096)
+    rng = np.random.Generator(np.random.PCG64(21))
+    for level in range(min(mg.n_levels, 3)):
+        x = rng.uniform(-1.0, 1.0, mg.sizes[level][1])
+        y64 = mg.matvec(level, x, precision=64)
+        y48 = mg.matvec(level, x, precision=48)
+        assert np.linalg.norm(y48 - y64) <= FP64_RTOL * np.linalg.norm(y64), level
+    # a smooth field: the Laplacian cancels, the rows' terms are large
+    # against the result
+    xs = datagen.bumps(mg.level_nodes(0))
+    y64 = mg.matvec(0, xs, precision=64)
+    y48 = mg.matvec(0, xs, precision=48)
+    assert np.linalg.norm(y48 - y64) <= 1e-10 * np.linalg.norm(y64)
+    b = mg.rhs(datagen.bumps(mg.level_nodes(0)))
+    mg.set_cg_operator(64)
+    x64, it64, rr64 = mg.solve(b, precision=32)
+    mg.set_cg_operator(48)  # the default
+    x48, it48, rr48 = mg.solve(b, precision=32)
+    assert rr64 <= 1e-8 and rr48 <= 1e-8
+    assert abs(it48 - it64) <= 1
+    assert np.linalg.norm(x48 - x64) <= 1e-7 * np.linalg.norm(x64)
