@@ -513,6 +513,20 @@ __device__ __forceinline__ void ds_term(float &sh, float &sl, float ah, float al
   sh = s;
 }
 
+// FP32 -> FP64 by integer operations (the ALU pipe, not the FP64 one):
+// exact for normal values, zero and infinities; FP32 subnormals (below
+// 1.2e-38) become zero
+__device__ __forceinline__ double f2d_bits(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  const uint64_t sign = (uint64_t)(u >> 31) << 63;
+  uint64_t bits;
+  if (e == 0) bits = 0;
+  else if (e == 0xffu) bits = (0x7ffull << 52) | ((uint64_t)(u & 0x7fffffu) << 29);
+  else bits = ((uint64_t)(e + (1023 - 127)) << 52) | ((uint64_t)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)(sign | bits));
+}
+
 constexpr int DS_STRIDE = 64;  // float2 entries per combined stencil in shared memory
 
 // ctab: the combined stencils of every (type, level) as (hi, lo) pairs
@@ -576,7 +590,7 @@ __global__ void __launch_bounds__(PATCH, 2)
           ds_term(sh, sl, a2.x, a2.y, xv[2 * j2]);
           ds_term(sh, sl, a2.z, a2.w, xv[2 * j2 + 1]);
         }
-        atomicAdd(&ys[lid[k]], (double)sh + (double)sl);
+        atomicAdd(&ys[lid[k]], f2d_bits(sh) + f2d_bits(sl));
       }
     }
     __syncthreads();
