@@ -938,7 +938,7 @@ const float2 *comb_table_ds(Context &ctx, double lap_fac, double mass_fac) {
 // the double-single run-form loop (k_patch_matvec_runs_ds): FP64 vectors
 template <bool DIR>
 void launch_matvec_runs_ds(Context &ctx, const Mesh &m, const double *x, double *y, double lap_fac,
-                           double mass_fac, const char *name, double bytes) {
+                           double mass_fac, int scale_exp, const char *name, double bytes) {
   const size_t smem = patch_runs_ds_smem();
   ensure_smem_attr(ctx, k_patch_matvec_runs_ds<DIR>, (int)smem);
   int per_sm = 1;
@@ -948,12 +948,13 @@ void launch_matvec_runs_ds(Context &ctx, const Mesh &m, const double *x, double 
   const float2 *ctab = comb_table_ds(ctx, lap_fac, mass_fac);
   ProfScope _prof(ctx, name, bytes);
   k_patch_matvec_runs_ds<DIR><<<grid, PATCH, smem, ctx.stream>>>(m.pmeta, m.plid, m.prun, m.poff, m.pkeys,
-                                                                 m.pkcount, m.n_elem, m.n_patch, ctab, x, y);
+                                                                 m.pkcount, m.n_elem, m.n_patch, ctab, x, y,
+                                                                 std::ldexp(1.0, scale_exp), -scale_exp);
   DG_LAUNCH_CHECK();
 }
-template void launch_matvec_runs_ds<true>(Context &, const Mesh &, const double *, double *, double, double,
+template void launch_matvec_runs_ds<true>(Context &, const Mesh &, const double *, double *, double, double, int,
                                           const char *, double);
-template void launch_matvec_runs_ds<false>(Context &, const Mesh &, const double *, double *, double, double,
+template void launch_matvec_runs_ds<false>(Context &, const Mesh &, const double *, double *, double, double, int,
                                            const char *, double);
 
 // the run-form element loop (k_patch_matvec_runs); DIR: the Dirichlet

@@ -126,10 +126,11 @@ void ensure_stencils(Context &ctx);
 template <typename T>
 const T *comb_table(Context &ctx, double lap_fac, double mass_fac);
 
-// the double-single run-form loop (FP64 vectors, FP32-pair arithmetic)
+// the double-single run-form loop (FP64 vectors, FP32-pair arithmetic; x
+// scaled by 2^scale_exp inside, the result by 2^-scale_exp)
 template <bool DIR>
 void launch_matvec_runs_ds(Context &ctx, const Mesh &m, const double *x, double *y, double lap_fac,
-                           double mass_fac, const char *name, double bytes);
+                           double mass_fac, int scale_exp, const char *name, double bytes);
 // the run-form element loop on a mesh with run tables (m.plid)
 template <typename T, bool DIR>
 void launch_matvec_runs(Context &ctx, const Mesh &m, const T *x, T *y, double lap_fac,

@@ -240,13 +240,15 @@ __global__ void k_cs_out(const double *__restrict__ x, size_t n, T *__restrict__
   if (i < n) out[i] = (T)x[i];
 }
 
-__global__ void k_to_float(const double *__restrict__ a, size_t n, float *__restrict__ b) {
+// FP64 <-> FP32 with an exact power-of-two scale (the FP32 parts of the
+// solve work on the CG vectors scaled to order one)
+__global__ void k_to_float(const double *__restrict__ a, size_t n, float *__restrict__ b, double scale = 1.0) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] = (float)a[i];
+  if (i < n) b[i] = (float)(a[i] * scale);
 }
-__global__ void k_to_double(const float *__restrict__ a, size_t n, double *__restrict__ b) {
+__global__ void k_to_double(const float *__restrict__ a, size_t n, double *__restrict__ b, double scale = 1.0) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] = (double)a[i];
+  if (i < n) b[i] = (double)a[i] * scale;
 }
 
 // block partial sums of a.b (and of a.a when b is null)
@@ -571,11 +573,16 @@ void mg_solve(Context &ctx, MG &mg, const double *b, double *x, int precision, d
     k_sum<<<1, 256, 0, s>>>(part.get(), nparts, out);
     DG_LAUNCH_CHECK();
   };
+  // the CG vectors scale with b: the FP32 V-cycle, the FP32 and the
+  // double-single operators work on them scaled by 2^ds_exp (exact), of
+  // order one, away from FP32's underflow (a fine mesh's load vector is of
+  // order h^3, and the residual falls by the tolerance on top)
+  int ds_exp = 0;
   auto precond = [&](const double *rin, double *zout) {
     if (precision == 32) {
-      k_to_float<<<g, 256, 0, s>>>(rin, n, r32.get());
+      k_to_float<<<g, 256, 0, s>>>(rin, n, r32.get(), std::ldexp(1.0, ds_exp));
       vcycle_level<float>(ctx, mg, w32, 0, r32.get(), z32.get());
-      k_to_double<<<g, 256, 0, s>>>(z32.get(), n, zout);
+      k_to_double<<<g, 256, 0, s>>>(z32.get(), n, zout, std::ldexp(1.0, -ds_exp));
       DG_LAUNCH_CHECK();
     } else {
       vcycle_level<double>(ctx, mg, w64, 0, rin, zout);
@@ -589,6 +596,7 @@ void mg_solve(Context &ctx, MG &mg, const double *b, double *x, int precision, d
   res = MGResult();
   if (bb == 0.0) return;
   const double bnorm = std::sqrt(bb);
+  ds_exp = std::max(-900, std::min(900, -std::ilogb(bnorm / std::sqrt((double)n))));
   // CG iteration: step A (q = A p, x and r updated, r.r) and step B (the
   // next direction from z = V-cycle(r)); the host reads r.r after each A.
   // With the FP32 operator, q = A p runs through the FP32 element loop and
@@ -601,12 +609,12 @@ void mg_solve(Context &ctx, MG &mg, const double *b, double *x, int precision, d
   }
   auto step_a = [&]() {
     if (op32) {
-      k_to_float<<<g, 256, 0, s>>>(p.get(), n, p32.get());
+      k_to_float<<<g, 256, 0, s>>>(p.get(), n, p32.get(), std::ldexp(1.0, ds_exp));
       dirichlet_matvec<float>(ctx, L0, p32.get(), q32.get());
-      k_to_double<<<g, 256, 0, s>>>(q32.get(), n, q.get());
+      k_to_double<<<g, 256, 0, s>>>(q32.get(), n, q.get(), std::ldexp(1.0, -ds_exp));
       DG_LAUNCH_CHECK();
     } else if (precision == 32 && mg.cg_operator == 48) {
-      dirichlet_matvec_ds(ctx, L0, p.get(), q.get());
+      dirichlet_matvec_ds(ctx, L0, p.get(), q.get(), ds_exp);
     } else {
       dirichlet_matvec<double>(ctx, L0, p.get(), q.get());
     }
@@ -678,15 +686,31 @@ void mg_solve(Context &ctx, MG &mg, const double *b, double *x, int precision, d
   res.relres = std::sqrt(read_scalar(ctx, d_rr)) / bnorm;
 }
 
-void dirichlet_matvec_ds(Context &ctx, const MGLevel &L, const double *x, double *y) {
+__global__ void k_absmax_bits(const double *__restrict__ x, size_t n, unsigned long long *__restrict__ out) {
+  unsigned long long m = 0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    m = max(m, (unsigned long long)__double_as_longlong(fabs(x[i])));  // non-negative: bits order as values
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+void dirichlet_matvec_ds(Context &ctx, const MGLevel &L, const double *x, double *y, int scale_exp) {
   const Mesh &m = L.mesh;
   if (!m.plid) {
     dirichlet_matvec<double>(ctx, L, x, y);
     return;
   }
   ensure_stencils(ctx);
+  if (scale_exp == DS_SCALE_AUTO) {  // from the largest entry of x
+    DG_CUDA(cudaMemsetAsync(ctx.d_scratch, 0, sizeof(unsigned long long), ctx.stream));
+    k_absmax_bits<<<grid_for(m.n_node, 256, (unsigned)ctx.num_sms * 4), 256, 0, ctx.stream>>>(x, m.n_node,
+                                                                                         ctx.d_scratch);
+    DG_LAUNCH_CHECK();
+    const double xmax = __builtin_bit_cast(double, (unsigned long long)read_scalar(ctx, ctx.d_scratch));
+    scale_exp = xmax > 0 && std::isfinite(xmax) ? std::max(-900, std::min(900, -std::ilogb(xmax))) : 0;
+  }
   DG_CUDA(cudaMemsetAsync(y, 0, m.n_node * sizeof(double), ctx.stream));
-  launch_matvec_runs_ds<true>(ctx, m, x, y, 1.0, 1.0, "dirichlet_matvec_ds",
+  launch_matvec_runs_ds<true>(ctx, m, x, y, 1.0, 1.0, scale_exp, "dirichlet_matvec_ds",
                               (double)m.n_elem * 36 + (double)m.n_node * (3 * sizeof(double) + 1));
 }
 

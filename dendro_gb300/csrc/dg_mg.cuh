@@ -63,7 +63,10 @@ void dirichlet_matvec(Context &ctx, const MGLevel &L, const T *x, T *y);  // Dir
 // the same operator on FP64 vectors in double-single arithmetic (FP32
 // pairs, about 2^-46 relative per element row; the FP64 loop where a mesh
 // has no run tables)
-void dirichlet_matvec_ds(Context &ctx, const MGLevel &L, const double *x, double *y);
+// (scale_exp: x is multiplied by 2^scale_exp inside the loop, chosen so
+// that x is of order one; DS_SCALE_AUTO takes it from x's largest entry)
+constexpr int DS_SCALE_AUTO = -100000;
+void dirichlet_matvec_ds(Context &ctx, const MGLevel &L, const double *x, double *y, int scale_exp = DS_SCALE_AUTO);
 // DirichletJacobianMatGetDiagonal (omgJac.C:1111): 1 on boundary nodes
 void dirichlet_diagonal(Context &ctx, const MGLevel &L, double *diag);
 template <typename T>

@@ -175,6 +175,13 @@ def test_double_single_operator(ctx):
         y64 = mg.matvec(level, x, precision=64)
         y48 = mg.matvec(level, x, precision=48)
         assert np.linalg.norm(y48 - y64) <= FP64_RTOL * np.linalg.norm(y64), level
+    # magnitudes far from one: the loop scales x by a power of two to keep
+    # its FP32 parts away from FP32's underflow and overflow
+    x = rng.uniform(-1.0, 1.0, mg.sizes[0][1])
+    for scale in (1e-30, 1e-12, 1e25):
+        y64 = mg.matvec(0, x * scale, precision=64)
+        y48 = mg.matvec(0, x * scale, precision=48)
+        assert np.linalg.norm(y48 - y64) <= FP64_RTOL * np.linalg.norm(y64), scale
     # a smooth field: the Laplacian cancels, the rows' terms are large
     # against the result
     xs = datagen.bumps(mg.level_nodes(0))
@@ -182,10 +189,11 @@ def test_double_single_operator(ctx):
     y48 = mg.matvec(0, xs, precision=48)
     assert np.linalg.norm(y48 - y64) <= 1e-10 * np.linalg.norm(y64)
     b = mg.rhs(datagen.bumps(mg.level_nodes(0)))
-    mg.set_cg_operator(64)
-    x64, it64, rr64 = mg.solve(b, precision=32)
-    mg.set_cg_operator(48)  # the default
-    x48, it48, rr48 = mg.solve(b, precision=32)
-    assert rr64 <= 1e-8 and rr48 <= 1e-8
-    assert abs(it48 - it64) <= 1
-    assert np.linalg.norm(x48 - x64) <= 1e-7 * np.linalg.norm(x64)
+    for bscale in (1.0, 1e-25):  # a tiny right-hand side (fine meshes' loads are of order h^3)
+        mg.set_cg_operator(64)
+        x64, it64, rr64 = mg.solve(b * bscale, precision=32)
+        mg.set_cg_operator(48)  # the default
+        x48, it48, rr48 = mg.solve(b * bscale, precision=32)
+        assert rr64 <= 1e-8 and rr48 <= 1e-8, bscale
+        assert abs(it48 - it64) <= 1, bscale
+        assert np.linalg.norm(x48 - x64) <= 1e-7 * np.linalg.norm(x64), bscale
