@@ -175,6 +175,7 @@ int dg_ctx_destroy(dg_ctx ctx) {
   if (ctx->c.d_comb64) cudaFree(ctx->c.d_comb64);
   if (ctx->c.d_comb32) cudaFree(ctx->c.d_comb32);
   if (ctx->c.d_comb_ds) cudaFree(ctx->c.d_comb_ds);
+  if (ctx->c.d_comb_rowabs) cudaFree(ctx->c.d_comb_rowabs);
   if (ctx->c.d_csten64) cudaFree(ctx->c.d_csten64);
   if (ctx->c.d_csten32) cudaFree(ctx->c.d_csten32);
   if (ctx->c.d_cperm) cudaFree(ctx->c.d_cperm);

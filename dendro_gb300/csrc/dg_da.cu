@@ -922,11 +922,26 @@ __global__ void k_split_pairs(const double *__restrict__ in, size_t n, float2 *_
   out[i] = make_float2(hi, __double2float_rn(v - (double)hi));
 }
 
+__global__ void k_row_abs_max(const double *__restrict__ comb, float *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;  // (type, level)
+  if (i >= COMB_ENTRIES / 64) return;
+  double m = 0.0;
+  for (int k = 0; k < 8; k++) {
+    double r = 0.0;
+    for (int j = 0; j < 8; j++) r += fabs(comb[i * 64 + 8 * k + j]);
+    m = fmax(m, r);
+  }
+  out[i] = __double2float_ru(m * (1.0 + 1e-12));
+}
+
 const float2 *comb_table_ds(Context &ctx, double lap_fac, double mass_fac) {
   if (!ctx.d_comb_ds) DG_CUDA(cudaMalloc((void **)&ctx.d_comb_ds, COMB_ENTRIES * sizeof(float2)));
+  if (!ctx.d_comb_rowabs) DG_CUDA(cudaMalloc((void **)&ctx.d_comb_rowabs, COMB_ENTRIES / 64 * sizeof(float)));
   if (!ctx.comb_ds_ok || ctx.comb_ds_f[0] != lap_fac || ctx.comb_ds_f[1] != mass_fac) {
     const double *d = comb_table<double>(ctx, lap_fac, mass_fac);
     k_split_pairs<<<(COMB_ENTRIES + 255) / 256, 256, 0, ctx.stream>>>(d, COMB_ENTRIES, ctx.d_comb_ds);
+    DG_LAUNCH_CHECK();
+    k_row_abs_max<<<(COMB_ENTRIES / 64 + 127) / 128, 128, 0, ctx.stream>>>(d, ctx.d_comb_rowabs);
     DG_LAUNCH_CHECK();
     ctx.comb_ds_f[0] = lap_fac;
     ctx.comb_ds_f[1] = mass_fac;
@@ -948,7 +963,8 @@ void launch_matvec_runs_ds(Context &ctx, const Mesh &m, const double *x, double 
   const float2 *ctab = comb_table_ds(ctx, lap_fac, mass_fac);
   ProfScope _prof(ctx, name, bytes);
   k_patch_matvec_runs_ds<DIR><<<grid, PATCH, smem, ctx.stream>>>(m.pmeta, m.plid, m.prun, m.poff, m.pkeys,
-                                                                 m.pkcount, m.n_elem, m.n_patch, ctab, x, y,
+                                                                 m.pkcount, m.n_elem, m.n_patch, ctab,
+                                                                 ctx.d_comb_rowabs, x, y,
                                                                  std::ldexp(1.0, scale_exp), -scale_exp);
   DG_LAUNCH_CHECK();
 }

@@ -513,64 +513,51 @@ __device__ __forceinline__ void ds_term(float &sh, float &sl, float ah, float al
   sh = s;
 }
 
-// (hi + lo) * 2^e2shift in FP64 by integer operations (the ALU pipe, not
-// the FP64 one): both FP32 values (normal or subnormal) as integers at the
-// larger one's exponent (62 bits), summed exactly, normalised and rounded to
-// 53 bits (nearest, ties to even); a part more than 62 binades below the
-// other is dropped.  Matches the FP64 sum (double)hi + (double)lo to within
-// one unit in the last place (checked on the CPU over 2e7 pairs, with
-// subnormals, cancellations and zeros).
-__device__ __forceinline__ double ds_to_double(float hi, float lo, int e2shift) {
-  const uint32_t uh = __float_as_uint(hi), ul = __float_as_uint(lo);
-  if (((uh | ul) & 0x7fffffffu) == 0) return 0.0;
-  const int eh = (int)((uh >> 23) & 0xffu), el = (int)((ul >> 23) & 0xffu);
-  const bool swap = el > eh;
-  const uint32_t ua = swap ? ul : uh, ub = swap ? uh : ul;
-  const int ea = swap ? el : eh, eb = swap ? eh : el;
-  const long long ma = ea ? (long long)((ua & 0x7fffffu) | 0x800000u) : (long long)(ua & 0x7fffffu);
-  const long long mb = eb ? (long long)((ub & 0x7fffffu) | 0x800000u) : (long long)(ub & 0x7fffffu);
-  const int ea1 = ea ? ea : 1, d = ea1 - (eb ? eb : 1);
-  long long A = ma << 38;
-  long long B = d <= 38 ? (mb << (38 - d)) : (d < 62 ? (mb >> (d - 38)) : 0);
-  if (ua >> 31) A = -A;
-  if (ub >> 31) B = -B;
-  const long long S = A + B;
-  if (S == 0) return 0.0;
-  const unsigned long long sign = S < 0 ? (1ull << 63) : 0ull;
-  unsigned long long m = (unsigned long long)(S < 0 ? -S : S);
-  const int lz = __clzll((long long)m);
-  m <<= lz;
-  const unsigned long long drop = m & 0x7ffull;
-  unsigned long long q = m >> 11;
-  if (drop > 0x400ull || (drop == 0x400ull && (q & 1ull))) q++;
-  int e2 = ea1 - 150 - 38 + (63 - lz) + e2shift;
-  if (q >> 53) {
-    q >>= 1;
-    e2++;
-  }
-  return __longlong_as_double(
-      (long long)(sign | ((unsigned long long)(e2 + 1023) << 52) | (q & ((1ull << 52) - 1))));
+// round(f * 2^s) as a 64-bit integer, by integer operations (the ALU
+// pipe): FP32 normal and subnormal values; the caller keeps |f| * 2^s below
+// 2^62
+__device__ __forceinline__ long long f2fix(float f, int s) {
+  const uint32_t u = __float_as_uint(f);
+  if (!(u & 0x7fffffffu)) return 0;
+  const int e = (int)((u >> 23) & 0xffu);
+  const long long m = e ? (long long)((u & 0x7fffffu) | 0x800000u) : (long long)(u & 0x7fffffu);
+  const int sh = (e ? e : 1) - 150 + s;  // f * 2^s = m * 2^sh
+  long long r;
+  if (sh >= 0) r = m << (sh < 39 ? sh : 39);
+  else if (sh > -63) r = (m + (1ll << (-sh - 1))) >> (-sh);
+  else r = 0;
+  return (u >> 31) ? -r : r;
 }
 
 constexpr int DS_STRIDE = 64;  // float2 entries per combined stencil in shared memory
 
-// ctab: the combined stencils of every (type, level) as (hi, lo) pairs.
-// x is scaled by xscale = 2^k on the way in and the row results by
-// 2^yshift = 2^-k on the way out (both exact), so that the FP32 parts stay
-// far from FP32's underflow whatever the vectors' magnitude.
+// ctab: the combined stencils of every (type, level) as (hi, lo) pairs;
+// rowabs: per (type, level) the largest row sum of |entries| (rounded up).
+// x is scaled by xscale = 2^k on the way in and the results by 2^yshift =
+// 2^-k on the way out (both exact), so that the FP32 parts stay far from
+// FP32's underflow whatever the vectors' magnitude.  The row results are
+// summed per run in 64-bit fixed point (shared-memory integer atomic adds;
+// FP64 shared-memory atomic adds cost about three FP64 operations each on
+// GB300's narrow FP64 pipe): the patch's scale 2^s makes (largest |x| of
+// the patch) x (largest row sum of its stencils) x 4096 (the most pairs a
+// run can have) smaller than 2^62, so no sum overflows, and a row result is
+// kept to 2^-50 of that bound.
 template <bool DIR>
 __global__ void __launch_bounds__(PATCH, 2)
     k_patch_matvec_runs_ds(const uint32_t *__restrict__ pmeta, const uint4 *__restrict__ plid,
                            const uint32_t *__restrict__ prun, const uint64_t *__restrict__ poff,
                            const uint16_t *__restrict__ pkeys, const uint16_t *__restrict__ pkcount, size_t E,
-                           size_t n_patch, const float2 *__restrict__ ctab, const double *__restrict__ x,
-                           double *__restrict__ y, double xscale, int yshift) {
+                           size_t n_patch, const float2 *__restrict__ ctab, const float *__restrict__ rowabs,
+                           const double *__restrict__ x, double *__restrict__ y, double xscale, int yshift) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *xs = reinterpret_cast<float2 *>(smem_raw);
-  double *ys = reinterpret_cast<double *>(xs + PATCH_ENT);
+  unsigned long long *ys = reinterpret_cast<unsigned long long *>(xs + PATCH_ENT);
   float2 *sc = reinterpret_cast<float2 *>(ys + PATCH_ENT);  // PKEY_MAX combined stencils
+  __shared__ uint32_t xmax_bits[2], smax_bits[2];  // per patch parity: largest |x|, largest row sum
   const int tid = threadIdx.x;
-  for (size_t p = blockIdx.x; p < n_patch; p += gridDim.x) {
+  if (tid < 2) xmax_bits[tid] = smax_bits[tid] = 0;
+  int par = 0;
+  for (size_t p = blockIdx.x; p < n_patch; p += gridDim.x, par ^= 1) {
     const int ne = (int)((E - p * PATCH) < (size_t)PATCH ? (E - p * PATCH) : (size_t)PATCH);
     const uint64_t ub = poff[p];
     const int nr = (int)(poff[p + 1] - ub);
@@ -578,18 +565,28 @@ __global__ void __launch_bounds__(PATCH, 2)
     const bool comb = kc <= (uint32_t)PKEY_MAX;
     uint32_t me = 0;
     uint4 lw = make_uint4(0, 0, 0, 0);
+    float rmax = 0.f;
     if (tid < ne) {
       me = pmeta[p * PATCH + tid];
       lw = plid[p * PATCH + tid];
+      rmax = rowabs[(me >> 24) * COMB_LEVELS + (me & 31u)];
     }
-    __syncthreads();  // the previous patch is done with xs, ys and sc
-    // 1. gather, each x split into (hi, lo)
+    __syncthreads();  // the previous patch is done with xs, ys, sc and its bounds
+    // 1. gather, each x split into (hi, lo); the patch's bounds
+    float xmax = 0.f;
     for (int u = tid; u < nr; u += PATCH) {
       const uint32_t r = prun[ub + u];
       const double xv = (DIR && (r & PRUN_BDY)) ? 0.0 : x[r & PRUN_NODE] * xscale;
       const float hi = __double2float_rn(xv);
       xs[u] = make_float2(hi, __double2float_rn(xv - (double)hi));
-      ys[u] = 0.0;
+      ys[u] = 0ull;
+      xmax = fmaxf(xmax, fabsf(hi));
+    }
+    const uint32_t wx = __reduce_max_sync(0xffffffffu, __float_as_uint(xmax));  // non-negative: bits order as values
+    const uint32_t ws = __reduce_max_sync(0xffffffffu, __float_as_uint(rmax));
+    if ((tid & 31) == 0) {
+      atomicMax(&xmax_bits[par], wx);
+      atomicMax(&smax_bits[par], ws);
     }
     if (comb) {
       for (int i = tid; i < (int)kc * 64; i += PATCH) {
@@ -598,6 +595,10 @@ __global__ void __launch_bounds__(PATCH, 2)
       }
     }
     __syncthreads();
+    const double bound = (double)__uint_as_float(xmax_bits[par]) * (double)__uint_as_float(smax_bits[par]);
+    const int fs = bound > 0.0 ? 49 - ilogb(bound) : 0;  // the fixed-point scale 2^fs
+    const double out_scale = ldexp(1.0, yshift - fs);
+    if (tid == 0) xmax_bits[par ^ 1] = smax_bits[par ^ 1] = 0;  // for the next patch
     // 2. element stencils
     if (tid < ne) {
       const uint32_t lv[4] = {lw.x, lw.y, lw.z, lw.w};
@@ -618,22 +619,23 @@ __global__ void __launch_bounds__(PATCH, 2)
           ds_term(sh, sl, a2.x, a2.y, xv[2 * j2]);
           ds_term(sh, sl, a2.z, a2.w, xv[2 * j2 + 1]);
         }
-        atomicAdd(&ys[lid[k]], ds_to_double(sh, sl, yshift));
+        atomicAdd(&ys[lid[k]], (unsigned long long)(f2fix(sh, fs) + f2fix(sl, fs)));
       }
     }
     __syncthreads();
     // 3. run sums out
     for (int u = tid; u < nr; u += PATCH) {
       const uint32_t r = prun[ub + u], g = r & PRUN_NODE;
+      const double v = (double)(long long)ys[u] * out_scale;
       if (DIR && (r & PRUN_BDY)) y[g] = x[g];
-      else if (r & PRUN_COMPLETE) y[g] = ys[u];
-      else atomicAdd(&y[g], ys[u]);
+      else if (r & PRUN_COMPLETE) y[g] = v;
+      else atomicAdd(&y[g], v);
     }
   }
 }
 
 constexpr size_t patch_runs_ds_smem() {
-  return PATCH_ENT * sizeof(float2) + PATCH_ENT * sizeof(double) + PKEY_MAX * DS_STRIDE * sizeof(float2);
+  return PATCH_ENT * sizeof(float2) + PATCH_ENT * sizeof(unsigned long long) + PKEY_MAX * DS_STRIDE * sizeof(float2);
 }
 
 template <typename T>

@@ -63,6 +63,7 @@ struct Context {
   bool comb64_ok = false, comb32_ok = false;
   // the FP64 combined stencils as (hi, lo) FP32 pairs (double-single loop)
   float2 *d_comb_ds = nullptr;
+  float *d_comb_rowabs = nullptr;  // per (type, level): largest row sum of |combined stencil entries|
   double comb_ds_f[2] = {0, 0};
   bool comb_ds_ok = false;
   bool prof = false;
