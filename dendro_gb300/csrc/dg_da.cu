@@ -914,12 +914,16 @@ const T *comb_table(Context &ctx, double lap_fac, double mass_fac) {
 template const float *comb_table<float>(Context &, double, double);
 template const double *comb_table<double>(Context &, double, double);
 
-__global__ void k_split_pairs(const double *__restrict__ in, size_t n, float2 *__restrict__ out) {
+// the FP64 combined stencils as (hi, lo) FP32 pairs, per (type, level) laid
+// out by (row pair p, column j): (hi[2p][j], hi[2p+1][j], lo[2p][j], lo[2p+1][j])
+__global__ void k_split_pairs(const double *__restrict__ in, size_t n_stencils, float4 *__restrict__ out) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double v = in[i];
-  const float hi = __double2float_rn(v);
-  out[i] = make_float2(hi, __double2float_rn(v - (double)hi));
+  if (i >= n_stencils * 32) return;
+  const size_t st = i / 32;
+  const int p = (int)(i % 32) / 8, j = (int)(i % 8);
+  const double a = in[st * 64 + (2 * p) * 8 + j], b = in[st * 64 + (2 * p + 1) * 8 + j];
+  const float ah = __double2float_rn(a), bh = __double2float_rn(b);
+  out[i] = make_float4(ah, bh, __double2float_rn(a - (double)ah), __double2float_rn(b - (double)bh));
 }
 
 __global__ void k_row_abs_max(const double *__restrict__ comb, float *__restrict__ out) {
@@ -934,12 +938,12 @@ __global__ void k_row_abs_max(const double *__restrict__ comb, float *__restrict
   out[i] = __double2float_ru(m * (1.0 + 1e-12));
 }
 
-const float2 *comb_table_ds(Context &ctx, double lap_fac, double mass_fac) {
-  if (!ctx.d_comb_ds) DG_CUDA(cudaMalloc((void **)&ctx.d_comb_ds, COMB_ENTRIES * sizeof(float2)));
+const float4 *comb_table_ds(Context &ctx, double lap_fac, double mass_fac) {
+  if (!ctx.d_comb_ds) DG_CUDA(cudaMalloc((void **)&ctx.d_comb_ds, COMB_ENTRIES / 2 * sizeof(float4)));
   if (!ctx.d_comb_rowabs) DG_CUDA(cudaMalloc((void **)&ctx.d_comb_rowabs, COMB_ENTRIES / 64 * sizeof(float)));
   if (!ctx.comb_ds_ok || ctx.comb_ds_f[0] != lap_fac || ctx.comb_ds_f[1] != mass_fac) {
     const double *d = comb_table<double>(ctx, lap_fac, mass_fac);
-    k_split_pairs<<<(COMB_ENTRIES + 255) / 256, 256, 0, ctx.stream>>>(d, COMB_ENTRIES, ctx.d_comb_ds);
+    k_split_pairs<<<(COMB_ENTRIES / 2 + 255) / 256, 256, 0, ctx.stream>>>(d, COMB_ENTRIES / 64, ctx.d_comb_ds);
     DG_LAUNCH_CHECK();
     k_row_abs_max<<<(COMB_ENTRIES / 64 + 127) / 128, 128, 0, ctx.stream>>>(d, ctx.d_comb_rowabs);
     DG_LAUNCH_CHECK();
@@ -960,7 +964,7 @@ void launch_matvec_runs_ds(Context &ctx, const Mesh &m, const double *x, double 
   DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_patch_matvec_runs_ds<DIR>, PATCH, smem));
   if (per_sm < 1) per_sm = 1;
   const unsigned grid = (unsigned)std::min<size_t>(m.n_patch, (size_t)per_sm * ctx.num_sms);
-  const float2 *ctab = comb_table_ds(ctx, lap_fac, mass_fac);
+  const float4 *ctab = comb_table_ds(ctx, lap_fac, mass_fac);
   ProfScope _prof(ctx, name, bytes);
   k_patch_matvec_runs_ds<DIR><<<grid, PATCH, smem, ctx.stream>>>(m.pmeta, m.plid, m.prun, m.poff, m.pkeys,
                                                                  m.pkcount, m.n_elem, m.n_patch, ctab,

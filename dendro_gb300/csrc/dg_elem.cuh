@@ -84,6 +84,35 @@ __device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
   return d;
 }
 
+// paired FP32 add, subtract and multiply (Blackwell f32x2), round to nearest
+__device__ __forceinline__ float2 fadd2(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+
 // y_k = f1 sum_j L[k][j] x_j + f2 sum_j M[k][j] x_j (full-row stencil S),
 // handing each y_k to emit(k, y_k)
 template <typename Emit>
@@ -501,15 +530,19 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
 // Per element that is 8 FP64 adds instead of 64 FP64 multiply-adds.
 // The explicit _rn intrinsics keep the compiler from fusing the sums with
 // the products.
-__device__ __forceinline__ void ds_term(float &sh, float &sl, float ah, float al, float2 x) {
-  const float ph = __fmul_rn(ah, x.x);
-  float pl = fmaf(ah, x.x, -ph);
-  pl = fmaf(ah, x.y, pl);
-  pl = fmaf(al, x.x, pl);
-  const float s = __fadd_rn(sh, ph);
-  const float v = __fsub_rn(s, sh);
-  const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, v)), __fsub_rn(ph, v));
-  sl = __fadd_rn(sl, __fadd_rn(e, pl));
+// two rows k, k + 1 at once: a = (hi_k, hi_k+1, lo_k, lo_k+1) of column j,
+// x = (hi, lo) of x_j; (sh, sl) hold the two rows' running (hi, lo) sums
+__device__ __forceinline__ void ds_term2(float2 &sh, float2 &sl, float4 a, float2 x) {
+  const float2 ah = make_float2(a.x, a.y), al = make_float2(a.z, a.w);
+  const float2 xh = make_float2(x.x, x.x), xl = make_float2(x.y, x.y);
+  const float2 ph = fmul2(ah, xh);
+  float2 pl = make_float2(fmaf(a.x, x.x, -ph.x), fmaf(a.y, x.x, -ph.y));  // exact: hi * hi - ph
+  pl = ffma2(ah, xl, pl);
+  pl = ffma2(al, xh, pl);
+  const float2 s = fadd2(sh, ph);
+  const float2 v = fsub2(s, sh);
+  const float2 e = fadd2(fsub2(sh, fsub2(s, v)), fsub2(ph, v));
+  sl = fadd2(sl, fadd2(e, pl));
   sh = s;
 }
 
@@ -529,9 +562,11 @@ __device__ __forceinline__ long long f2fix(float f, int s) {
   return (u >> 31) ? -r : r;
 }
 
-constexpr int DS_STRIDE = 64;  // float2 entries per combined stencil in shared memory
+constexpr int DS_STRIDE = 32;  // float4 entries per combined stencil: (row pair, column)
 
-// ctab: the combined stencils of every (type, level) as (hi, lo) pairs;
+// ctab: the combined stencils of every (type, level) as (hi, lo) pairs,
+// laid out per (row pair p, column j) as (hi[2p][j], hi[2p+1][j],
+// lo[2p][j], lo[2p+1][j]);
 // rowabs: per (type, level) the largest row sum of |entries| (rounded up).
 // x is scaled by xscale = 2^k on the way in and the results by 2^yshift =
 // 2^-k on the way out (both exact), so that the FP32 parts stay far from
@@ -547,12 +582,12 @@ __global__ void __launch_bounds__(PATCH, 2)
     k_patch_matvec_runs_ds(const uint32_t *__restrict__ pmeta, const uint4 *__restrict__ plid,
                            const uint32_t *__restrict__ prun, const uint64_t *__restrict__ poff,
                            const uint16_t *__restrict__ pkeys, const uint16_t *__restrict__ pkcount, size_t E,
-                           size_t n_patch, const float2 *__restrict__ ctab, const float *__restrict__ rowabs,
+                           size_t n_patch, const float4 *__restrict__ ctab, const float *__restrict__ rowabs,
                            const double *__restrict__ x, double *__restrict__ y, double xscale, int yshift) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *xs = reinterpret_cast<float2 *>(smem_raw);
   unsigned long long *ys = reinterpret_cast<unsigned long long *>(xs + PATCH_ENT);
-  float2 *sc = reinterpret_cast<float2 *>(ys + PATCH_ENT);  // PKEY_MAX combined stencils
+  float4 *sc = reinterpret_cast<float4 *>(ys + PATCH_ENT);  // PKEY_MAX combined stencils
   __shared__ uint32_t xmax_bits[2], smax_bits[2];  // per patch parity: largest |x|, largest row sum
   const int tid = threadIdx.x;
   if (tid < 2) xmax_bits[tid] = smax_bits[tid] = 0;
@@ -589,9 +624,9 @@ __global__ void __launch_bounds__(PATCH, 2)
       atomicMax(&smax_bits[par], ws);
     }
     if (comb) {
-      for (int i = tid; i < (int)kc * 64; i += PATCH) {
-        const uint32_t key = pkeys[p * PKEY_MAX + (i >> 6)];
-        sc[(i >> 6) * DS_STRIDE + (i & 63)] = ctab[((key >> 5) * COMB_LEVELS + (key & 31u)) * 64 + (i & 63)];
+      for (int i = tid; i < (int)kc * DS_STRIDE; i += PATCH) {
+        const uint32_t key = pkeys[p * PKEY_MAX + i / DS_STRIDE];
+        sc[i] = ctab[((key >> 5) * COMB_LEVELS + (key & 31u)) * DS_STRIDE + i % DS_STRIDE];
       }
     }
     __syncthreads();
@@ -608,18 +643,15 @@ __global__ void __launch_bounds__(PATCH, 2)
       float2 xv[8];
 #pragma unroll
       for (int m = 0; m < 8; m++) xv[m] = xs[lid[m]];
-      const float2 *S = comb ? sc + ((me >> 16) & 255u) * DS_STRIDE
-                             : ctab + ((me >> 24) * COMB_LEVELS + (me & 31u)) * 64;
+      const float4 *S = comb ? sc + ((me >> 16) & 255u) * DS_STRIDE
+                             : ctab + ((me >> 24) * COMB_LEVELS + (me & 31u)) * DS_STRIDE;
 #pragma unroll
-      for (int k = 0; k < 8; k++) {
-        float sh = 0.f, sl = 0.f;
+      for (int pr = 0; pr < 4; pr++) {
+        float2 sh = make_float2(0.f, 0.f), sl = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int j2 = 0; j2 < 4; j2++) {
-          const float4 a2 = reinterpret_cast<const float4 *>(S + 8 * k)[j2];
-          ds_term(sh, sl, a2.x, a2.y, xv[2 * j2]);
-          ds_term(sh, sl, a2.z, a2.w, xv[2 * j2 + 1]);
-        }
-        atomicAdd(&ys[lid[k]], (unsigned long long)(f2fix(sh, fs) + f2fix(sl, fs)));
+        for (int j = 0; j < 8; j++) ds_term2(sh, sl, S[pr * 8 + j], xv[j]);
+        atomicAdd(&ys[lid[2 * pr]], (unsigned long long)(f2fix(sh.x, fs) + f2fix(sl.x, fs)));
+        atomicAdd(&ys[lid[2 * pr + 1]], (unsigned long long)(f2fix(sh.y, fs) + f2fix(sl.y, fs)));
       }
     }
     __syncthreads();
@@ -635,7 +667,7 @@ __global__ void __launch_bounds__(PATCH, 2)
 }
 
 constexpr size_t patch_runs_ds_smem() {
-  return PATCH_ENT * sizeof(float2) + PATCH_ENT * sizeof(unsigned long long) + PKEY_MAX * DS_STRIDE * sizeof(float2);
+  return PATCH_ENT * sizeof(float2) + PATCH_ENT * sizeof(unsigned long long) + PKEY_MAX * DS_STRIDE * sizeof(float4);
 }
 
 template <typename T>

@@ -61,8 +61,9 @@ struct Context {
   float *d_comb32 = nullptr;
   double comb64_f[2] = {0, 0}, comb32_f[2] = {0, 0};
   bool comb64_ok = false, comb32_ok = false;
-  // the FP64 combined stencils as (hi, lo) FP32 pairs (double-single loop)
-  float2 *d_comb_ds = nullptr;
+  // the FP64 combined stencils as (hi, lo) FP32 pairs, two rows per float4
+  // (double-single loop)
+  float4 *d_comb_ds = nullptr;
   float *d_comb_rowabs = nullptr;  // per (type, level): largest row sum of |combined stencil entries|
   double comb_ds_f[2] = {0, 0};
   bool comb_ds_ok = false;
