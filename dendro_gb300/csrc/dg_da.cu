@@ -349,23 +349,32 @@ __global__ void k_mesh_conn(const Key128 *__restrict__ keys, size_t n, const uin
     // the owner is the element anchored at the vertex; on the positive domain
     // boundary, the leaf containing the vertex clamped inward (a search)
     size_t o;
+    bool found = true;
     if (k == 0 && !(hm & 1u)) {
       o = e;  // a vertex 0 that does not hang is the element's own anchor
     } else if (kb == 0) {
       const uint32_t f = anchor_find(keys, tab, mask, morton3((uint32_t)cl[0], (uint32_t)cl[1], (uint32_t)cl[2]));
-      o = f == AH_EMPTY ? 0 : f;
+      found = f != AH_EMPTY;
+      o = found ? f : 0;
     } else {
       o = find_leaf_from(keys, n, morton3((uint32_t)cl[0], (uint32_t)cl[1], (uint32_t)cl[2]), e);
     }
     const Key128 ko = keys[o];
     const unsigned lo_ = tag_level(ko);
-    uint32_t ox, oy, oz;
-    demorton3(tag_anchor(ko), ox, oy, oz);
     const int64_t ho = (int64_t)1 << (D - lo_);
-    const int64_t oc[3] = {ox, oy, oz};
-    bool ok = true;
+    // the owner's anchor: the vertex itself when it was found by its anchor
+    // (no decode needed), else decoded from the owner's key
+    int64_t oc[3] = {v[0], v[1], v[2]};
+    bool ok = found;
+    if (kb != 0) {
+      uint32_t ox, oy, oz;
+      demorton3(tag_anchor(ko), ox, oy, oz);
+      oc[0] = ox;
+      oc[1] = oy;
+      oc[2] = oz;
 #pragma unroll
-    for (int a = 0; a < 3; a++) ok = ok && ((kb >> a & 1) ? (oc[a] + ho == dom) : (oc[a] == v[a]));
+      for (int a = 0; a < 3; a++) ok = ok && ((kb >> a & 1) ? (oc[a] + ho == dom) : (oc[a] == v[a]));
+    }
     const unsigned bo = ((oc[0] + ho == dom) ? 1u : 0u) | ((oc[1] + ho == dom) ? 2u : 0u) | ((oc[2] + ho == dom) ? 4u : 0u);
     const unsigned hmo = (meta[o] >> 16) & 255u;
     ok = ok && ((kb & bo) == kb) && !(hmo >> kb & 1);
