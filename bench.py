@@ -436,8 +436,8 @@ def run_serving(args, local, barrier):
         plain.ctx.profile(False)
         plain.close()
         plain_build_s = sum(r.t_built - r.t_admit for r in p_outs) / 2
-    # build + balance requests only (the benchmark spec's served-vs-plain figure
-    # for construction and balance), on the same clouds: with the stream's
+    # build + balance requests only (the served-vs-plain figure for
+    # construction and balance), on the same clouds: with the stream's
     # Poisson arrivals, and as a burst (every request waiting at the start,
     # the servers' capacity)
     def replay_build(server, burst):
