@@ -201,9 +201,9 @@ __global__ void k_set_bdy_identity(const uint8_t *__restrict__ bdy, size_t n, do
   if (i < n && bdy[i]) A[i * n + i] = 1.0;
 }
 
-// coarse solve x = A^-1 b to FP64 accuracy: x = X b, then CS_REFINE rounds of
-// r = b - A x (FP64), x += X r, with X the FP32 inverse and A the assembled
-// FP64 operator; one warp per row
+// coarse solve of the FP64 V-cycle, x = A^-1 b to FP64 accuracy: x = X b,
+// then CS_REFINE rounds of r = b - A x (FP64), x += X r, with X the FP32
+// inverse and A the assembled FP64 operator; one warp per row
 constexpr int CS_REFINE = 3;
 
 template <typename T>
@@ -218,6 +218,20 @@ __global__ void k_cs_apply(const float *__restrict__ Xi, size_t n, const T *__re
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if (lane == 0) x[row] = accumulate ? x[row] + acc : acc;
+}
+
+// x = X b in FP32 (one warp per row), the coarse solve of the FP32 V-cycle
+__global__ void k_cs_apply_f32(const float *__restrict__ Xi, size_t n, const float *__restrict__ v,
+                               float *__restrict__ x) {
+  const size_t row = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const float *a = Xi + row * n;
+  float acc = 0.f;
+  for (size_t j = lane; j < n; j += 32) acc = fmaf(a[j], v[j], acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) x[row] = acc;
 }
 
 template <typename T>
@@ -382,8 +396,16 @@ void vcycle_level(Context &ctx, const MG &mg, VWork<T> &w, int l, const T *b, T 
   const MGLevel &L = mg.lv[l];
   const size_t n = L.mesh.n_node;
   if (l + 1 == (int)mg.lv.size()) {
-    ProfScope _prof(ctx, "mg_coarse_solve", (double)n * n * (4 + CS_REFINE * 12));
     const unsigned gw = grid_for(n * 32, 256);
+    if constexpr (std::is_same<T, float>::value) {
+      // FP32 V-cycle: the result is FP32, so x = X b in FP32 without
+      // refinement (the FP64 rounds would be rounded away)
+      ProfScope _prof(ctx, "mg_coarse_solve", (double)n * n * 4);
+      k_cs_apply_f32<<<gw, 256, 0, s>>>(mg.cinv32, n, b, x);
+      DG_LAUNCH_CHECK();
+      return;
+    }
+    ProfScope _prof(ctx, "mg_coarse_solve", (double)n * n * (4 + CS_REFINE * 12));
     k_cs_apply<T><<<gw, 256, 0, s>>>(mg.cinv32, n, b, w.cx.get(), false);
     for (int it = 0; it < CS_REFINE; it++) {
       k_cs_resid<T><<<gw, 256, 0, s>>>(mg.ca64, n, b, w.cx.get(), w.cr.get());
