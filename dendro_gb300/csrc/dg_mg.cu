@@ -145,12 +145,14 @@ __global__ void k_prolong(const uint32_t *__restrict__ pid, const float *__restr
   xf[v] = add ? xf[v] + acc : acc;
 }
 
+// bc += R rf, or with ax given, bc += R (rf - ax) (the V-cycle's residual
+// restricted without storing it)
 template <typename T>
 __global__ void k_restrict(const uint32_t *__restrict__ pid, const float *__restrict__ pw, size_t Vf,
-                           const T *__restrict__ rf, T *__restrict__ bc) {
+                           const T *__restrict__ rf, T *__restrict__ bc, const T *__restrict__ ax = nullptr) {
   size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= Vf) return;
-  const T r = rf[v];
+  const T r = ax ? rf[v] - ax[v] : rf[v];
   if (r == (T)0) return;
 #pragma unroll
   for (int j = 0; j < 8; j++) {
@@ -426,13 +428,14 @@ void vcycle_level(Context &ctx, const MG &mg, VWork<T> &w, int l, const T *b, T 
   }
   if (mg.nu_pre == 0) DG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(T), s));
   dirichlet_matvec<T>(ctx, L, x, ax);
+  T *bc = w.b[l + 1].get(), *xc = w.x[l + 1].get();
   {
-    ProfScope _prof(ctx, "mg_residual", (double)n * 3 * sizeof(T));
-    k_residual<T><<<g, 256, 0, s>>>(b, ax, ax, n);  // ax now holds the residual
+    // the residual b - A x restricted to the next level in one pass
+    DG_CUDA(cudaMemsetAsync(bc, 0, mg.lv[l + 1].mesh.n_node * sizeof(T), s));
+    ProfScope _prof(ctx, "mg_restrict", (double)n * (8 * 8 + 2 * sizeof(T)));
+    k_restrict<T><<<g, 256, 0, s>>>(L.pid, L.pw, n, b, bc, ax);
     DG_LAUNCH_CHECK();
   }
-  T *bc = w.b[l + 1].get(), *xc = w.x[l + 1].get();
-  mg_restrict<T>(ctx, mg, l, ax, bc);
   vcycle_level<T>(ctx, mg, w, l + 1, bc, xc);
   {
     ProfScope _prof(ctx, "mg_prolong", (double)n * (8 * 8 + 2 * sizeof(T)));
