@@ -554,8 +554,14 @@ def run_scale(args, dg, ctx, local):
                    "GB/s": (v[2] / (v[0] * 1e-3) / 1e9) if v[0] > 0 else None}
                for k, v in sorted(stats.items(), key=lambda kv: -kv[1][0])[:12]}
     top, (tms, tcnt, tbytes) = max(stats.items(), key=lambda kv: kv[1][0])
+    # the step's algorithmic bytes: 40 per point to form its key (24 read,
+    # 16 written), 32 per key to sort it and 32 to drop duplicates (16 read,
+    # 16 written), 32 per constructed octant and 32 per balanced octant
+    step_bytes = 104.0 * npts + 32.0 * n_lin + 32.0 * n_bal
     res = {"workload": "lognormal64m", "points": npts, "octants_p2o": n_lin, "octants_balanced": n_bal,
            "build_balance_Mpts_per_s": npts / (ms * 1e-3) / 1e6, "ms_per_step": ms,
+           "step_algorithmic_bytes": step_bytes, "step_algorithmic_GB_per_s": step_bytes / (ms * 1e-3) / 1e9,
+           "step_frac_of_measured_peak": step_bytes / (ms * 1e-3) / 1e9 / peak,
            "e2e_Mpts_per_s": npts / (sum(e2e) / len(e2e)) / 1e6,
            "top_kernel": {"name": top, "ms_per_launch": tms / tcnt, "GB/s": tbytes / (tms * 1e-3) / 1e9,
                           "frac_of_measured_peak": tbytes / (tms * 1e-3) / 1e9 / peak,
