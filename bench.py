@@ -94,7 +94,7 @@ class ClockSampler:
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-              "clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.sw_power_cap,utilization.gpu")
 
     def __init__(self, device: int):
         self.device = device
@@ -128,7 +128,7 @@ class ClockSampler:
             self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
-        sm, smax, reasons = [], [], set()
+        sm, smax, util, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in self.rows:
             try:
@@ -137,6 +137,7 @@ class ClockSampler:
                 for nm, v in zip(names, r[4:8]):
                     if v.lower() == "active":
                         reasons.add(nm)
+                util.append(float(r[8]))
             except (ValueError, IndexError):
                 continue
         return {
@@ -144,6 +145,9 @@ class ClockSampler:
             "sm_max_mhz": max(smax) if smax else None,
             "reasons": sorted(reasons),
             "samples": len(sm),
+            # nvidia-smi's utilization.gpu: the share of each sample period in
+            # which some kernel ran (not how many SMs it kept busy)
+            "gpu_util_pct_mean": statistics.mean(util) if util else None,
         }
 
 
