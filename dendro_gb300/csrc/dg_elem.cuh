@@ -525,13 +525,15 @@ __global__ void __launch_bounds__(PATCH, sizeof(T) == 4 ? 3 : 2)
 // exactly (hi * hi and its rounding error by an FMA, plus the two cross
 // terms) and the 8 products of a row are summed with an error-free sum
 // (TwoSum) into a (hi, lo) pair, so a row is exact to about 2^-46 of the
-// sum of its terms' magnitudes; the row result goes to FP64 (hi + lo is
-// exact there) and is added across elements in FP64 as in the FP64 loop.
-// Per element that is 8 FP64 adds instead of 64 FP64 multiply-adds.
-// The explicit _rn intrinsics keep the compiler from fusing the sums with
-// the products.
-// two rows k, k + 1 at once: a = (hi_k, hi_k+1, lo_k, lo_k+1) of column j,
-// x = (hi, lo) of x_j; (sh, sl) hold the two rows' running (hi, lo) sums
+// sum of its terms' magnitudes.  The row results are summed per run in
+// 64-bit fixed point (below), so an element costs no FP64 operation at all;
+// only the split of each gathered x and each run's final sum use the FP64
+// pipe.  The paired instructions (f32x2) keep the compiler from fusing the
+// sums with the products, as the explicit FMAs do for the exact products.
+//
+// ds_term2: two rows k, k + 1 at once; a = (hi_k, hi_k+1, lo_k, lo_k+1) of
+// column j, x = (hi, lo) of x_j; (sh, sl) hold the two rows' running
+// (hi, lo) sums
 __device__ __forceinline__ void ds_term2(float2 &sh, float2 &sl, float4 a, float2 x) {
   const float2 ah = make_float2(a.x, a.y), al = make_float2(a.z, a.w);
   const float2 xh = make_float2(x.x, x.x), xl = make_float2(x.y, x.y);
