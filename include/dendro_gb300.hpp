@@ -563,8 +563,14 @@ class MultiGrid {
   }
   // load vector of a nodal field on level 0
   void rhs(const double *f, double *b) const { cxx::check(c_, dg_mg_rhs(c_, mg_, f, b, 0), "dg_mg_rhs"); }
+  // the CG's operator with an FP32 V-cycle: 48 double-single (the default),
+  // 64 FP64, 32 FP32 with FP64 residual replacement (dg_mg_set_cg_operator)
+  void setCgOperator(int precision, double reliableDelta = 1e-3) {
+    cxx::check(c_, dg_mg_set_cg_operator(mg_, precision, reliableDelta), "dg_mg_set_cg_operator");
+  }
   // CG with one V-cycle per iteration to rtol; precision 32 runs the V-cycle
-  // in FP32 (FP64 residuals), 64 all in FP64; returns the iterations
+  // in FP32 (FP64 vectors and residuals), 64 all in FP64; returns the
+  // iterations
   int solve(const double *b, double *x, int precision, double rtol, int maxit, double *relres = nullptr) const {
     int it = 0;
     double rr = 0;
