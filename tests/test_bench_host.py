@@ -29,12 +29,17 @@ class _DoneProc:
 def test_clock_summary():
     cs = bench.ClockSampler(0)
     cs.proc = _DoneProc()
-    cs.rows = [["2070", "2070", "900", "0x0", "Not Active", "Not Active", "Not Active", "Not Active"],
-               ["2040", "2070", "1380", "0x4", "Not Active", "Not Active", "Not Active", "Active"],
-               ["2055", "2070", "1200", "0x0", "Not Active", "Not Active", "Not Active", "Not Active"],
+    cs.rows = [["2070", "2070", "900", "0x0", "Not Active", "Not Active", "Not Active", "Not Active", "100"],
+               ["2040", "2070", "1380", "0x4", "Not Active", "Not Active", "Not Active", "Active", "96"],
+               ["2055", "2070", "1200", "0x0", "Not Active", "Not Active", "Not Active", "Not Active", "98"],
                ["garbage"]]
     s = cs.stop()
-    assert s == {"sm_mhz": 2055.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    assert s == {"sm_mhz": 2055.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3,
+                 "gpu_util_pct_mean": 98.0}
+    # a sample without the utilisation column still counts for the clocks
+    cs.rows = [["2070", "2070", "900", "0x0", "Not Active", "Not Active", "Not Active", "Not Active"]]
+    s = cs.stop()
+    assert (s["samples"], s["gpu_util_pct_mean"]) == (1, None)
 
 
 def test_kernel_tables():
