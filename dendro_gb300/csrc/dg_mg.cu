@@ -10,7 +10,9 @@
 // {0, 1/2, 1}^3 of the coarse element that contains it.  Its prolongation
 // weights are the coarse element's trilinear shape functions there, folded
 // through the coarse element's hanging-vertex interpolation; the weights are
-// dyadic and exact in FP32.  They reproduce the reference's restriction
+// multiples of 1/64 (shape-function values in {1, 1/2, 1/4, 1/8}, shared
+// among at most 8 parent corners), exact in FP32 and stored as w * 64 in
+// one byte, nonzero ones only (about 3 per fine node).  They reproduce the reference's restriction
 // stencils RmatType1 / RmatType2 exactly.  Restriction is the transpose.
 // Pairs with a fine or a coarse boundary node carry no weight, as with the
 // reference's suppressed Dirichlet DOFs.
@@ -64,13 +66,22 @@ __global__ void k_invert(const double *__restrict__ d, size_t n, double *__restr
   inv32[i] = (float)v;
 }
 
-// prolongation weights of every fine node (see the file comment)
-__global__ void k_prolong_map(const uint32_t *__restrict__ fxyz, size_t Vf, const uint8_t *__restrict__ fbdy,
-                              const Key128 *__restrict__ ckeys, size_t Ec, const uint32_t *__restrict__ cmeta,
-                              const uint32_t *__restrict__ cconn, const uint8_t *__restrict__ cbdy, unsigned D,
-                              uint32_t *__restrict__ pid, float *__restrict__ pw, uint32_t *flags) {
-  size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= Vf) return;
+// the transfer tables: every fine node's nonzero prolongation weights, in
+// the coarse element's vertex order, packed per warp-chunk of 32 nodes: the
+// entries of chunk k start at k * TCHUNK, node v's at its chunk's start plus
+// tpos[v] & 255, and number tpos[v] >> 8 (at most 8).  Entry e refers to
+// coarse node tid[e] with weight tw[e] / 64.
+constexpr int TCHUNK = 32 * 8;
+
+// prolongation weights of fine node v (see the file comment): the 8
+// vertices of the coarse element that contains it, with weight 0 where the
+// fine or the coarse node is on the domain boundary; false if the node does
+// not sit at {0, 1/2, 1}^3 of that element
+__device__ __forceinline__ bool prolong_weights(size_t v, const uint32_t *__restrict__ fxyz, size_t Vf,
+                                                const uint8_t *__restrict__ fbdy, const Key128 *__restrict__ ckeys,
+                                                size_t Ec, const uint32_t *__restrict__ cmeta,
+                                                const uint32_t *__restrict__ cconn, const uint8_t *__restrict__ cbdy,
+                                                unsigned D, uint32_t (&ids)[8], float (&wv)[8]) {
   const uint32_t dom = 1u << D;
   uint32_t p[3] = {fxyz[v], fxyz[Vf + v], fxyz[2 * Vf + v]};
   uint32_t q[3];
@@ -123,42 +134,111 @@ __global__ void k_prolong_map(const uint32_t *__restrict__ fxyz, size_t Vf, cons
   const bool fb = fbdy[v] != 0;
 #pragma unroll
   for (int j = 0; j < 8; j++) {
-    uint32_t id = cconn[(size_t)j * Ec + e];
-    float w = (fb || cbdy[id]) ? 0.f : wj[j];
-    pid[(size_t)j * Vf + v] = id;
-    pw[(size_t)j * Vf + v] = w;
+    ids[j] = cconn[(size_t)j * Ec + e];
+    wv[j] = (fb || cbdy[ids[j]]) ? 0.f : wj[j];
   }
+  return ok;
+}
+
+// the transfer tables of one fine level (one thread per fine node, blocks of
+// 256 threads: a warp is a chunk); every weight must be a multiple of 1/64
+// in (0, 1] (kept as w * 64 in one byte).  A warp collects its chunk in
+// shared memory and writes it out contiguously.  nnz counts the level's
+// entries.
+__global__ void __launch_bounds__(256, 6)
+    k_prolong_map(const uint32_t *__restrict__ fxyz, size_t Vf, const uint8_t *__restrict__ fbdy,
+                  const Key128 *__restrict__ ckeys, size_t Ec, const uint32_t *__restrict__ cmeta,
+                  const uint32_t *__restrict__ cconn, const uint8_t *__restrict__ cbdy, unsigned D,
+                  uint16_t *__restrict__ tpos, uint32_t *__restrict__ tid, uint8_t *__restrict__ tw,
+                  unsigned long long *nnz, uint32_t *flags) {
+  __shared__ uint32_t s_id[8][TCHUNK];
+  __shared__ __align__(16) uint8_t s_w[8][TCHUNK];
+  const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t ids[8];
+  float wv[8];
+  bool ok = true;
+  int cnt = 0;
+  if (v < Vf) {
+    ok = prolong_weights(v, fxyz, Vf, fbdy, ckeys, Ec, cmeta, cconn, cbdy, D, ids, wv);
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      if (wv[j] != 0.f) {
+        cnt++;
+        const float k = wv[j] * 64.f;
+        ok = ok && k >= 1.f && k <= 64.f && k == truncf(k);
+      }
+    }
+  }
+  // the chunk's entries in lane order (every lane of the warp takes part)
+  int incl = cnt;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= (unsigned)d) incl += t;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  if (v < Vf) {
+    const int start = incl - cnt;
+    tpos[v] = (uint16_t)(start | cnt << 8);
+    int k = start;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      if (wv[j] != 0.f) {
+        s_id[warp][k] = ids[j];
+        s_w[warp][k] = (uint8_t)(wv[j] * 64.f);
+        k++;
+      }
+    }
+  }
+  __syncwarp();
+  // chunk v / 32 (the same for every lane; total is 0 for a warp past Vf)
+  const size_t cb = (v >> 5) * TCHUNK;
+  for (int i = (int)lane; i < total; i += 32) tid[cb + i] = s_id[warp][i];
+  const uint32_t *sw4 = reinterpret_cast<const uint32_t *>(s_w[warp]);
+  uint32_t *tw4 = reinterpret_cast<uint32_t *>(tw + cb);  // chunks start 256-byte aligned
+  for (int i = (int)lane; i < (total + 3) / 4; i += 32) tw4[i] = sw4[i];
+  if (lane == 31u) atomicAdd(nnz, (unsigned long long)total);
   if (!ok) atomicOr(flags, DGF_INTERNAL);
 }
 
+// weight e of the transfer tables (exact: a multiple of 1/64)
+__device__ __forceinline__ float transfer_w(const uint8_t *__restrict__ tw, size_t e) {
+  return (float)tw[e] * (1.f / 64.f);
+}
+
+// xf = P xc, or xf += P xc with add (at most 8 terms per fine node, in the
+// coarse element's vertex order)
 template <typename T>
-__global__ void k_prolong(const uint32_t *__restrict__ pid, const float *__restrict__ pw, size_t Vf,
-                          const T *__restrict__ xc, T *__restrict__ xf, bool add) {
+__global__ void k_prolong(const uint16_t *__restrict__ tpos, const uint32_t *__restrict__ tid,
+                          const uint8_t *__restrict__ tw, size_t Vf, const T *__restrict__ xc, T *__restrict__ xf,
+                          bool add) {
   size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= Vf) return;
+  const uint32_t p = tpos[v], ne = p >> 8;
+  const size_t e0 = (v >> 5) * TCHUNK + (p & 255u);
   T acc = 0;
 #pragma unroll
-  for (int j = 0; j < 8; j++) {
-    float w = pw[(size_t)j * Vf + v];
-    if (w != 0.f) acc += (T)w * xc[pid[(size_t)j * Vf + v]];
-  }
+  for (uint32_t j = 0; j < 8; j++)
+    if (j < ne) acc += (T)transfer_w(tw, e0 + j) * xc[tid[e0 + j]];
   xf[v] = add ? xf[v] + acc : acc;
 }
 
 // bc += R rf, or with ax given, bc += R (rf - ax) (the V-cycle's residual
 // restricted without storing it)
 template <typename T>
-__global__ void k_restrict(const uint32_t *__restrict__ pid, const float *__restrict__ pw, size_t Vf,
-                           const T *__restrict__ rf, T *__restrict__ bc, const T *__restrict__ ax = nullptr) {
+__global__ void k_restrict(const uint16_t *__restrict__ tpos, const uint32_t *__restrict__ tid,
+                           const uint8_t *__restrict__ tw, size_t Vf, const T *__restrict__ rf, T *__restrict__ bc,
+                           const T *__restrict__ ax = nullptr) {
   size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= Vf) return;
   const T r = ax ? rf[v] - ax[v] : rf[v];
   if (r == (T)0) return;
+  const uint32_t p = tpos[v], ne = p >> 8;
+  const size_t e0 = (v >> 5) * TCHUNK + (p & 255u);
 #pragma unroll
-  for (int j = 0; j < 8; j++) {
-    float w = pw[(size_t)j * Vf + v];
-    if (w != 0.f) atomicAdd(&bc[pid[(size_t)j * Vf + v]], (T)w * r);
-  }
+  for (uint32_t j = 0; j < 8; j++)
+    if (j < ne) atomicAdd(&bc[tid[e0 + j]], (T)transfer_w(tw, e0 + j) * r);
 }
 
 // damped Jacobi: x = w D^-1 b (first sweep from zero) or x += w D^-1 (b - Ax)
@@ -360,22 +440,29 @@ void dirichlet_diagonal(Context &ctx, const MGLevel &L, double *diag) {
   DG_LAUNCH_CHECK();
 }
 
+// algorithmic bytes of one transfer over fine level F: its tables (2 bytes
+// per node, 5 per weight) and vec bytes of vectors per node
+static double transfer_bytes(const MGLevel &F, size_t vec) {
+  return (double)F.mesh.n_node * (2 + vec) + (double)F.tnnz * 5;
+}
+
 template <typename T>
 void mg_restrict(Context &ctx, const MG &mg, int f, const T *rf, T *bc) {
   const MGLevel &F = mg.lv[f];
   const MGLevel &C = mg.lv[f + 1];
   cudaStream_t s = ctx.stream;
   DG_CUDA(cudaMemsetAsync(bc, 0, C.mesh.n_node * sizeof(T), s));
-  ProfScope _prof(ctx, "mg_restrict", (double)F.mesh.n_node * (8 * 8 + sizeof(T)));
-  k_restrict<T><<<grid_for(F.mesh.n_node, 256), 256, 0, s>>>(F.pid, F.pw, F.mesh.n_node, rf, bc);
+  ProfScope _prof(ctx, "mg_restrict", transfer_bytes(F, sizeof(T)));
+  k_restrict<T><<<grid_for(F.mesh.n_node, 256), 256, 0, s>>>(F.tpos, F.tid, F.tw, F.mesh.n_node, rf, bc);
   DG_LAUNCH_CHECK();
 }
 
 template <typename T>
 void mg_prolong(Context &ctx, const MG &mg, int f, const T *xc, T *xf) {
   const MGLevel &F = mg.lv[f];
-  ProfScope _prof(ctx, "mg_prolong", (double)F.mesh.n_node * (8 * 8 + sizeof(T)));
-  k_prolong<T><<<grid_for(F.mesh.n_node, 256), 256, 0, ctx.stream>>>(F.pid, F.pw, F.mesh.n_node, xc, xf, false);
+  ProfScope _prof(ctx, "mg_prolong", transfer_bytes(F, sizeof(T)));
+  k_prolong<T><<<grid_for(F.mesh.n_node, 256), 256, 0, ctx.stream>>>(F.tpos, F.tid, F.tw, F.mesh.n_node, xc, xf,
+                                                                       false);
   DG_LAUNCH_CHECK();
 }
 
@@ -432,14 +519,14 @@ void vcycle_level(Context &ctx, const MG &mg, VWork<T> &w, int l, const T *b, T 
   {
     // the residual b - A x restricted to the next level in one pass
     DG_CUDA(cudaMemsetAsync(bc, 0, mg.lv[l + 1].mesh.n_node * sizeof(T), s));
-    ProfScope _prof(ctx, "mg_restrict", (double)n * (8 * 8 + 2 * sizeof(T)));
-    k_restrict<T><<<g, 256, 0, s>>>(L.pid, L.pw, n, b, bc, ax);
+    ProfScope _prof(ctx, "mg_restrict", transfer_bytes(L, 2 * sizeof(T)));
+    k_restrict<T><<<g, 256, 0, s>>>(L.tpos, L.tid, L.tw, n, b, bc, ax);
     DG_LAUNCH_CHECK();
   }
   vcycle_level<T>(ctx, mg, w, l + 1, bc, xc);
   {
-    ProfScope _prof(ctx, "mg_prolong", (double)n * (8 * 8 + 2 * sizeof(T)));
-    k_prolong<T><<<g, 256, 0, s>>>(L.pid, L.pw, n, xc, x, true);
+    ProfScope _prof(ctx, "mg_prolong", transfer_bytes(L, 2 * sizeof(T)));
+    k_prolong<T><<<g, 256, 0, s>>>(L.tpos, L.tid, L.tw, n, xc, x, true);
     DG_LAUNCH_CHECK();
   }
   for (int it = 0; it < mg.nu_post; it++) {
@@ -480,8 +567,9 @@ void mg_free(Context &ctx, MG &mg) {
     if (L.bdy) cudaFreeAsync(L.bdy, ctx.stream);
     if (L.dinv64) cudaFreeAsync(L.dinv64, ctx.stream);
     if (L.dinv32) cudaFreeAsync(L.dinv32, ctx.stream);
-    if (L.pid) cudaFreeAsync(L.pid, ctx.stream);
-    if (L.pw) cudaFreeAsync(L.pw, ctx.stream);
+    if (L.tpos) cudaFreeAsync(L.tpos, ctx.stream);
+    if (L.tid) cudaFreeAsync(L.tid, ctx.stream);
+    if (L.tw) cudaFreeAsync(L.tw, ctx.stream);
   }
   if (mg.ca64) cudaFreeAsync(mg.ca64, ctx.stream);
   if (mg.cinv32) cudaFreeAsync(mg.cinv32, ctx.stream);
@@ -536,15 +624,30 @@ void mg_setup(Context &ctx, const Octree &fine, size_t max_coarse_elem, MG &mg) 
       DG_LAUNCH_CHECK();
     }
     DG_CUDA(cudaMemsetAsync(ctx.d_flags, 0, sizeof(uint32_t), s));
+    DBuf<unsigned long long> nnz(mg.lv.size(), s);  // nonzero weights per fine level
+    DG_CUDA(cudaMemsetAsync(nnz.get(), 0, mg.lv.size() * sizeof(unsigned long long), s));
     for (size_t l = 0; l + 1 < mg.lv.size(); l++) {
       MGLevel &F = mg.lv[l];
       const MGLevel &C = mg.lv[l + 1];
       const size_t Vf = F.mesh.n_node;
-      DG_CUDA(cudaMallocAsync((void **)&F.pid, 8 * Vf * sizeof(uint32_t), s));
-      DG_CUDA(cudaMallocAsync((void **)&F.pw, 8 * Vf * sizeof(float), s));
+      const size_t chunks = (Vf + 31) / 32;
+      DG_CUDA(cudaMallocAsync((void **)&F.tpos, std::max<size_t>(Vf, 1) * sizeof(uint16_t), s));
+      DG_CUDA(cudaMallocAsync((void **)&F.tid, std::max<size_t>(chunks, 1) * TCHUNK * sizeof(uint32_t), s));
+      DG_CUDA(cudaMallocAsync((void **)&F.tw, std::max<size_t>(chunks, 1) * TCHUNK, s));
+      // per fine node: coordinates, boundary flag, the containing coarse
+      // element's key, meta, 8 vertex ids and their boundary flags in; the
+      // position word and about 3 entries of 5 bytes out
+      ProfScope _prof(ctx, "mg_prolong_map", (double)Vf * (12 + 1 + 16 + 4 + 32 + 8 + 2 + 15));
       k_prolong_map<<<grid_for(Vf, 256), 256, 0, s>>>(F.mesh.node_xyz, Vf, F.bdy, C.oct.keys, C.oct.n, C.mesh.meta,
-                                                      C.mesh.conn, C.bdy, D, F.pid, F.pw, ctx.d_flags);
+                                                      C.mesh.conn, C.bdy, D, F.tpos, F.tid, F.tw, nnz.get() + l,
+                                                      ctx.d_flags);
       DG_LAUNCH_CHECK();
+    }
+    if (mg.lv.size() > 1) {
+      std::vector<unsigned long long> h(mg.lv.size() - 1);
+      DG_CUDA(cudaMemcpyAsync(h.data(), nnz.get(), h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+      DG_CUDA(cudaStreamSynchronize(s));
+      for (size_t l = 0; l < h.size(); l++) mg.lv[l].tnnz = (size_t)h[l];
     }
     check_device_flags(ctx, "multigrid transfers");
     // dense inverse of the coarsest operator

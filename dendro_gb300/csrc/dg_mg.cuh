@@ -17,10 +17,15 @@ struct MGLevel {
   uint8_t *bdy = nullptr;  // 1 for nodes on the domain boundary
   double *dinv64 = nullptr;  // inverse diagonal of the Dirichlet operator
   float *dinv32 = nullptr;
-  // prolongation from the next coarser level onto this level's nodes:
-  // slot j of node v refers to coarse node pid[j*V + v] with weight pw[j*V + v]
-  uint32_t *pid = nullptr;
-  float *pw = nullptr;
+  // prolongation from the next coarser level onto this level's nodes, the
+  // nonzero weights only, packed per chunk of 32 nodes (256 entries per
+  // chunk): node v takes coarse nodes tid[e] with weights tw[e] / 64 for
+  // e = (v / 32) * 256 + (tpos[v] & 255) + j, j < tpos[v] >> 8, in the
+  // coarse element's vertex order (every weight is a multiple of 1/64)
+  uint16_t *tpos = nullptr;
+  uint32_t *tid = nullptr;
+  uint8_t *tw = nullptr;
+  size_t tnnz = 0;  // nonzero weights (the tables' algorithmic size)
 };
 
 struct MG {
