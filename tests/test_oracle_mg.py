@@ -68,3 +68,23 @@ def test_oracle_solver_converges(small_mg):
     assert rr <= 1e-8
     assert it < 30
     assert np.all(x[small_mg.das[0].bdy()] == 0.0)
+
+
+@pytest.mark.parametrize("cloud", ["gaussian", "lognormal"])
+def test_prolongation_weights_fit_the_packed_tables(oracle, small_mg, cloud):
+    """The device keeps each nonzero prolongation weight as w * 64 in one
+    byte, at most 8 per fine node: every weight of every level is a multiple
+    of 1/64 in (0, 1] (shape-function values 1, 1/2, 1/4, 1/8 shared among
+    at most 8 parent corners)."""
+    if cloud == "gaussian":
+        mg = small_mg
+    else:
+        pts = datagen.lognormal(3000, seed=7)
+        mg = OracleMG(oracle.balance(oracle.points_to_octree(pts, 30, 1), 30), 30, max_coarse=300)
+    assert mg.n_levels >= 3
+    for l in range(mg.n_levels - 1):
+        ids, w = mg.pmaps[l]
+        nz = w[w != 0] * 64
+        assert np.all(nz == np.round(nz)) and nz.min() >= 1 and nz.max() <= 64
+        assert (w != 0).sum(1).max() <= 8
+        assert np.all(ids[w != 0] < mg.das[l + 1].n_node)
