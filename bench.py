@@ -178,9 +178,17 @@ def replica_value(ws: int, points_per_replica: int, ms: float) -> float:
 
 
 def _top_kernels(stats: dict, k: int = 10) -> dict:
-    """{kernel: [total ms, launches]} of the k kernels with the most time."""
+    """{kernel: [total ms, launches]} of the k kernels with the most time;
+    where the statistics carry each kernel's algorithmic bytes, a third
+    entry gives its achieved GB/s (bytes over event time)."""
     top = sorted(stats.items(), key=lambda kv: -kv[1][0])[:k]
-    return {name: [round(v[0], 3), int(v[1])] for name, v in top}
+    out = {}
+    for name, v in top:
+        row = [round(v[0], 3), int(v[1])]
+        if len(v) > 2:
+            row.append(round(v[2] / (v[0] * 1e6), 1) if v[0] > 0 and v[2] > 0 else None)
+        out[name] = row
+    return out
 
 
 def _merge_stats(parts) -> dict:

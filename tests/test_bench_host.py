@@ -49,6 +49,9 @@ def test_kernel_tables():
     assert m == {"k1": (15.0, 3, 150.0), "k2": (1.0, 1, 5.0), "k3": (7.0, 3, 0.0)}
     top = bench._top_kernels({k: (v[0], v[1]) for k, v in m.items()}, k=2)
     assert list(top) == ["k1", "k3"] and top["k1"] == [15.0, 3]
+    # with algorithmic bytes: GB/s = bytes / (ms * 1e6); none without bytes
+    top = bench._top_kernels({"k1": (2.0, 4, 3e9), "k3": (1.0, 1, 0.0)})
+    assert top == {"k1": [2.0, 4, 1500.0], "k3": [1.0, 1, None]}
 
 
 def test_reference_sample_fills_the_cores():
