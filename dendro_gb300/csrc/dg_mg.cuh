@@ -32,7 +32,7 @@ struct MG {
   std::vector<MGLevel> lv;  // 0 = finest
   size_t nc = 0;            // nodes of the coarsest level
   double *ca64 = nullptr;    // the coarsest level's assembled operator (dense, FP64)
-  float *cinv32 = nullptr;   // its inverse in FP32 (refined in FP64 when applied)
+  float *cinv32 = nullptr;   // its inverse in FP32 (refined in FP64 when the FP64 V-cycle applies it)
   double omega = 0.667;  // Jacobi damping (bin/options:190)
   int nu_pre = 2, nu_post = 2;
   // CG operator with an FP32 V-cycle: 48 (the default) applies A p in
