@@ -36,6 +36,20 @@
  *         every element's records added in element order, as
  *         (row x y z, column x y z, value) by node coordinates.
  *
+ *   transfer FINE.oct MAXDEPTH STENCILDIR VEC_F VEC_C OUT_PREFIX
+ *         the reference's inter-grid transfers between FINE (a balanced
+ *         octree) and its next coarser level, made as DAMGCreateAndSetDA
+ *         makes it at one rank (src/omg/blockDiag.cpp:1384-1425: coarsen,
+ *         then balance with incCorner): the two ot::DAs, the Dirichlet
+ *         flags of SetDirichletJacContexts (examples/src/backend/
+ *         omgJac.C:509-575) as the suppressed DOFs, the TransferOpData of
+ *         createInterpolationType1 (blockDiag.cpp:2254-2303) with its dummy
+ *         pass, then one restrictMatVecType1 of VEC_F
+ *         (src/omg/restrictMatVec.cpp) and one prolongMatVecType1 of VEC_C
+ *         (src/omg/prolongMatVec.cpp).  Writes OUT_PREFIX.coarse (the
+ *         coarse octree), OUT_PREFIX.r (R VEC_F by coarse node coordinates)
+ *         and OUT_PREFIX.p (P VEC_C by fine node coordinates).
+ *
  * Formats
  *   .pts : u64 n, then n*3 f64 (x,y,z interleaved)
  *   .oct : u64 n, then n*(u32 x, u32 y, u32 z, u32 level)
@@ -55,6 +69,7 @@
 
 #include "TreeNode.h"
 #include "handleStencils.h"
+#include "omg.h"
 #include "octUtils.h"
 #include "oda.h"
 #include "odaUtils.h"
@@ -66,6 +81,24 @@ double ****LaplacianType2Stencil = nullptr;
 double ****MassType2Stencil = nullptr;
 namespace ot {
 double ****ShapeFnCoeffs = nullptr;
+/* the restriction tables and vertex maps (defined in src/omg/blockDiag.cpp,
+ * which is not compiled here; loaded by the transfer mode) */
+double *****RmatType1Stencil = nullptr;
+double ****RmatType2Stencil = nullptr;
+unsigned short ****VtxMap1 = nullptr;
+unsigned short *****VtxMap2 = nullptr;
+unsigned short *****VtxMap3 = nullptr;
+unsigned short ******VtxMap4 = nullptr;
+int readRmatType1Stencil(double *****&lut);
+int readRmatType2Stencil(double ****&lut);
+int readVtxMaps(unsigned short ****&map1, unsigned short *****&map2, unsigned short *****&map3,
+                unsigned short ******&map4);
+/* the scatter of the type-2 transfers (blockDiag.cpp), which only run where
+ * a level has an auxiliary mesh: never at one rank */
+int scatterValues(Vec, Vec, PetscInt, PetscInt, int *&, int *&, int *&, int *&, MPI_Comm) {
+  std::fprintf(stderr, "scatterValues: type-2 transfers are not used at one rank\n");
+  std::abort();
+}
 }
 
 static double now_s() {
@@ -425,6 +458,192 @@ static int mode_da(int argc, char **argv) {
   return conflicts ? 5 : 0;
 }
 
+/* node coordinates of every buffer index of a DA (vertex k of an element, or
+ * vertex k of its parent where the vertex is hanging); returns the number of
+ * indices seen at two positions (0 when the hanging-vertex rule holds) */
+static long node_positions(ot::DA &da, std::vector<uint32_t> &pos, std::vector<unsigned char> &seen) {
+  const unsigned maxD = da.getMaxDepth();
+  const size_t nb = da.getLocalBufferSize();
+  pos.assign(3 * nb, 0);
+  seen.assign(nb, 0);
+  long conflicts = 0;
+  for (da.init<ot::DA_FLAGS::ALL>(); da.curr() < da.end<ot::DA_FLAGS::ALL>(); da.next<ot::DA_FLAGS::ALL>()) {
+    Point pt = da.getCurrentOffset();
+    unsigned lev = da.getLevel(da.curr());
+    unsigned idx[8];
+    da.getNodeIndices(idx);
+    unsigned char cn = da.getChildNumber();
+    unsigned char hm = da.getHangingNodeIndex(da.curr());
+    uint32_t x = pt.xint(), y = pt.yint(), z = pt.zint();
+    uint32_t h = 1u << (maxD - lev);
+    uint32_t px = x - ((cn & 1) ? h : 0), py = y - ((cn & 2) ? h : 0), pz = z - ((cn & 4) ? h : 0);
+    for (int k = 0; k < 8; k++) {
+      uint32_t v[3];
+      if (hm & (1u << k)) {
+        v[0] = px + ((k & 1) ? 2 * h : 0);
+        v[1] = py + ((k & 2) ? 2 * h : 0);
+        v[2] = pz + ((k & 4) ? 2 * h : 0);
+      } else {
+        v[0] = x + ((k & 1) ? h : 0);
+        v[1] = y + ((k & 2) ? h : 0);
+        v[2] = z + ((k & 4) ? h : 0);
+      }
+      if (seen[idx[k]]) {
+        if (pos[3 * idx[k]] != v[0] || pos[3 * idx[k] + 1] != v[1] || pos[3 * idx[k] + 2] != v[2]) conflicts++;
+      } else {
+        seen[idx[k]] = 1;
+        for (int a = 0; a < 3; a++) pos[3 * idx[k] + a] = v[a];
+      }
+    }
+  }
+  return conflicts;
+}
+
+static bool read_vec(const char *path, std::unordered_map<unsigned __int128, double, CKeyHash> &val) {
+  FILE *f = xopen(path, "rb");
+  uint64_t nv = 0;
+  if (std::fread(&nv, 8, 1, f) != 1) return false;
+  val.reserve(2 * nv);
+  for (uint64_t i = 0; i < nv; i++) {
+    uint32_t c[4];
+    double v;
+    if (std::fread(c, 4, 4, f) != 4 || std::fread(&v, 8, 1, f) != 1) return false;
+    val[ckey(c[0], c[1], c[2])] = v;
+  }
+  std::fclose(f);
+  return true;
+}
+
+/* a nodal PETSc vector of da filled by node coordinate (through the DA's own
+ * buffer, as the reference moves data between vectors and buffers) */
+static long fill_vec(ot::DA &da, Vec v, const std::vector<uint32_t> &pos, const std::vector<unsigned char> &seen,
+                     const std::unordered_map<unsigned __int128, double, CKeyHash> &val) {
+  PetscScalar *arr = NULL;
+  da.vecGetBuffer(v, arr, false, false, false, 1);
+  long missing = 0;
+  for (size_t i = 0; i < seen.size(); i++) {
+    arr[i] = 0.0;
+    if (!seen[i]) continue;
+    auto it = val.find(ckey(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]));
+    if (it == val.end())
+      missing++;
+    else
+      arr[i] = it->second;
+  }
+  da.vecRestoreBuffer(v, arr, false, false, false, 1);
+  return missing;
+}
+
+static void write_vec(ot::DA &da, Vec v, const std::vector<uint32_t> &pos, const std::vector<unsigned char> &seen,
+                      const std::string &path) {
+  PetscScalar *arr = NULL;
+  da.vecGetBuffer(v, arr, false, false, true, 1);
+  FILE *g = xopen(path.c_str(), "wb");
+  uint64_t n = 0;
+  for (size_t i = 0; i < seen.size(); i++) n += seen[i];
+  std::fwrite(&n, 8, 1, g);
+  for (size_t i = 0; i < seen.size(); i++) {
+    if (!seen[i]) continue;
+    uint32_t c[4] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0};
+    std::fwrite(c, 4, 4, g);
+    std::fwrite(&arr[i], 8, 1, g);
+  }
+  std::fclose(g);
+  da.vecRestoreBuffer(v, arr, false, false, true, 1);
+}
+
+/* the Dirichlet flags of SetDirichletJacContexts (omgJac.C:509-575) as a
+ * suppressed-DOF array indexed like the DA's buffers */
+static std::vector<unsigned char> suppressed_dofs(ot::DA &da) {
+  std::vector<unsigned char> flags;
+  ot::assignBoundaryFlags(&da, flags);
+  unsigned char *bdy = NULL;
+  da.vecGetBuffer<unsigned char>(flags, bdy, false, false, true, 1);
+  std::vector<unsigned char> sup(da.getLocalBufferSize(), 0);
+  for (da.init<ot::DA_FLAGS::ALL>(); da.curr() < da.end<ot::DA_FLAGS::ALL>(); da.next<ot::DA_FLAGS::ALL>()) {
+    unsigned idx[8];
+    da.getNodeIndices(idx);
+    for (int k = 0; k < 8; k++) sup[idx[k]] = bdy[idx[k]];
+  }
+  da.vecRestoreBuffer<unsigned char>(flags, bdy, false, false, true, 1);
+  return sup;
+}
+
+static int mode_transfer(int argc, char **argv) {
+  if (argc < 8) return 1;
+  unsigned maxDepth = std::atoi(argv[3]);
+  std::string stencilDir = argv[4];
+  std::string prefix = argv[7];
+  std::vector<ot::TreeNode> fine = read_oct(argv[2], maxDepth), coarse;
+  {
+    /* the next coarser level: coarsen, then balance (blockDiag.cpp:1384-1425) */
+    std::vector<ot::TreeNode> tmp, in = fine;
+    ot::coarsenOctree(in, tmp);
+    ot::balanceOctree(tmp, coarse, 3, maxDepth, true, MPI_COMM_WORLD, NULL, NULL);
+  }
+  write_oct((prefix + ".coarse").c_str(), coarse);
+  {
+    /* the tables are read from the working directory */
+    char oldcwd[4096];
+    if (!getcwd(oldcwd, sizeof(oldcwd))) return 4;
+    if (chdir(stencilDir.c_str()) != 0) return 4;
+    ot::DA_Initialize(MPI_COMM_WORLD);
+    ot::readRmatType1Stencil(ot::RmatType1Stencil);
+    ot::readRmatType2Stencil(ot::RmatType2Stencil);
+    ot::readVtxMaps(ot::VtxMap1, ot::VtxMap2, ot::VtxMap3, ot::VtxMap4);
+    if (chdir(oldcwd) != 0) return 4;
+  }
+  const size_t nFine = fine.size(), nCoarse = coarse.size();
+  /* the coarse DA first; the fine DA takes its blocks (blockDiag.cpp:2005-2007) */
+  std::vector<ot::TreeNode> cIn = coarse, fIn = fine;
+  ot::DA dac(cIn, MPI_COMM_WORLD, MPI_COMM_WORLD, 0.3, false);
+  std::vector<ot::TreeNode> blocks = dac.getBlocks();
+  ot::DA daf(fIn, MPI_COMM_WORLD, MPI_COMM_WORLD, 0.3, false, &blocks, NULL);
+  std::vector<uint32_t> posC, posF;
+  std::vector<unsigned char> seenC, seenF;
+  long conflicts = node_positions(dac, posC, seenC) + node_positions(daf, posF, seenF);
+  std::vector<unsigned char> supC = suppressed_dofs(dac), supF = suppressed_dofs(daf);
+
+  /* createInterpolationType1 (blockDiag.cpp:2254-2303) at one rank */
+  ot::TransferOpData data;
+  std::memset(&data, 0, sizeof(data));
+  data.dac = &dac;
+  data.daf = &daf;
+  data.minIndependentSize = dac.getIndependentSize();
+  data.suppressedDOFc = supC.data();
+  data.suppressedDOFf = supF.data();
+  data.comm = MPI_COMM_WORLD;
+  data.dof = 1;
+  data.fineTouchedFlags = new std::vector<ot::FineTouchedStatus>;
+  Mat R;
+  MatCreateShell(MPI_COMM_WORLD, dac.getNodeSize(), daf.getNodeSize(), PETSC_DETERMINE, PETSC_DETERMINE,
+                 (void *)&data, &R);
+  MatShellSetOperation(R, MATOP_MULT, (void (*)(void))ot::restrictMatVecType1);
+  MatShellSetOperation(R, MATOP_MULT_TRANSPOSE, (void (*)(void))ot::prolongMatVecType1);
+  daf.createVector<ot::FineTouchedStatus>(*data.fineTouchedFlags, false, false, 1);
+  ot::dummyRestrictMatVecType1(&data);
+
+  std::unordered_map<unsigned __int128, double, CKeyHash> vf, vc;
+  if (!read_vec(argv[5], vf) || !read_vec(argv[6], vc)) return 3;
+  Vec f, c, pf;
+  daf.createVector(f, false, false, 1);
+  daf.createVector(pf, false, false, 1);
+  dac.createVector(c, false, false, 1);
+  long missing = fill_vec(daf, f, posF, seenF, vf);
+  Vec rc;
+  dac.createVector(rc, false, false, 1);
+  if (MatMult(R, f, rc) != 0) return 6;
+  write_vec(dac, rc, posC, seenC, prefix + ".r");
+  missing += fill_vec(dac, c, posC, seenC, vc);
+  if (MatMultTranspose(R, c, pf) != 0) return 6;
+  write_vec(daf, pf, posF, seenF, prefix + ".p");
+  if (missing) std::fprintf(stderr, "warning: %ld node values missing from the input vectors\n", missing);
+  std::printf("{\"op\":\"transfer\",\"n_fine\":%zu,\"n_coarse\":%zu,\"fine_nodes\":%u,\"coarse_nodes\":%u,"
+              "\"conflicts\":%ld,\"missing\":%ld}\n",
+              nFine, nCoarse, daf.getNodeSize(), dac.getNodeSize(), conflicts, missing);
+  return conflicts ? 5 : 0;
+}
+
 // io PTS D OUTPREFIX: the reference's own file writers on one cloud --
 // writePtsToFile (OUTPREFIX.pts), and for its balanced octree writeNodesToFile
 // (OUTPREFIX.ot, text) and writeNodesToFile_binary (OUTPREFIX.otb); then its
@@ -481,5 +700,6 @@ int main(int argc, char **argv) {
   if (m == "da") rc = mode_da(argc, argv);
   if (m == "io") rc = mode_io(argc, argv);
   if (m == "treesort") rc = mode_treesort(argc, argv);
+  if (m == "transfer") rc = mode_transfer(argc, argv);
   return rc;
 }

@@ -2,9 +2,11 @@
  * Header-only stand-in for the handful of PETSc types, macros and Vec/Mat
  * calls that the reference's octree/DA/element-loop sources reference.  Used
  * only to compile the reference into the CPU oracle binary (oracle/_ref).
- * Vec is a plain heap array; Mat is a context holder with the two shell
- * operations (MATOP_MULT, MATOP_GET_DIAGONAL) the MatShell callbacks of
- * include/dendro_gb300_petsc.hpp are tested through.  No solver exists here.
+ * Vec is a plain heap array; Mat is a context holder with the shell
+ * operations MATOP_MULT and MATOP_GET_DIAGONAL (the MatShell callbacks of
+ * include/dendro_gb300_petsc.hpp are tested through them) and
+ * MATOP_MULT_TRANSPOSE (the reference's prolongation shell).  No solver
+ * exists here.
  */
 #ifndef DG_ORACLE_PETSC_SHIM_H
 #define DG_ORACLE_PETSC_SHIM_H
@@ -56,6 +58,7 @@ struct dg_shim_mat {
   /* shell operations (MatShellSetOperation) */
   PetscErrorCode (*mult)(Mat, Vec, Vec);
   PetscErrorCode (*diag)(Mat, Vec);
+  PetscErrorCode (*multT)(Mat, Vec, Vec);
 };
 struct dg_shim_opaque {
   int unused;
@@ -133,6 +136,20 @@ inline PetscErrorCode VecZeroEntries(Vec v) {
   std::memset(v->a, 0, v->n * sizeof(PetscScalar));
   return 0;
 }
+inline PetscErrorCode VecDuplicate(Vec v, Vec *w) {
+  VecCreate(MPI_COMM_SELF, w);
+  return VecSetSizes(*w, (PetscInt)v->n, PETSC_DETERMINE);
+}
+/* y = y + alpha x */
+inline PetscErrorCode VecAXPY(Vec y, PetscScalar alpha, Vec x) {
+  for (size_t i = 0; i < y->n; i++) y->a[i] += alpha * x->a[i];
+  return 0;
+}
+/* w = alpha x + y */
+inline PetscErrorCode VecWAXPY(Vec w, PetscScalar alpha, Vec x, Vec y) {
+  for (size_t i = 0; i < w->n; i++) w->a[i] = alpha * x->a[i] + y->a[i];
+  return 0;
+}
 inline PetscErrorCode VecSet(Vec v, PetscScalar s) {
   for (size_t i = 0; i < v->n; i++) v->a[i] = s;
   return 0;
@@ -142,11 +159,11 @@ inline PetscErrorCode PetscStrcmp(const char *a, const char *b, PetscBool *f) {
   return 0;
 }
 inline PetscErrorCode MatCreate(MPI_Comm, Mat *m) {
-  *m = new dg_shim_mat{nullptr, nullptr, nullptr};
+  *m = new dg_shim_mat{nullptr, nullptr, nullptr, nullptr};
   return 0;
 }
 inline PetscErrorCode MatCreateShell(MPI_Comm, PetscInt, PetscInt, PetscInt, PetscInt, void *ctx, Mat *m) {
-  *m = new dg_shim_mat{ctx, nullptr, nullptr};
+  *m = new dg_shim_mat{ctx, nullptr, nullptr, nullptr};
   return 0;
 }
 inline PetscErrorCode MatShellGetContext(Mat m, void *ctx) {
@@ -156,10 +173,12 @@ inline PetscErrorCode MatShellGetContext(Mat m, void *ctx) {
 inline PetscErrorCode MatShellSetOperation(Mat m, MatOperation op, void (*f)(void)) {
   if (op == MATOP_MULT) m->mult = (PetscErrorCode(*)(Mat, Vec, Vec))f;
   if (op == MATOP_GET_DIAGONAL) m->diag = (PetscErrorCode(*)(Mat, Vec))f;
+  if (op == MATOP_MULT_TRANSPOSE) m->multT = (PetscErrorCode(*)(Mat, Vec, Vec))f;
   return 0;
 }
 inline PetscErrorCode MatMult(Mat m, Vec x, Vec y) { return m->mult ? m->mult(m, x, y) : PETSC_ERR_SUP; }
 inline PetscErrorCode MatGetDiagonal(Mat m, Vec d) { return m->diag ? m->diag(m, d) : PETSC_ERR_SUP; }
+inline PetscErrorCode MatMultTranspose(Mat m, Vec x, Vec y) { return m->multT ? m->multT(m, x, y) : PETSC_ERR_SUP; }
 inline PetscErrorCode MatDestroy(Mat *m) {
   delete *m;
   *m = nullptr;

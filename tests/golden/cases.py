@@ -61,6 +61,23 @@ def nodal_function(xyz_u32: np.ndarray) -> np.ndarray:
     return np.sin(3.0 * c[:, 0]) * np.cos(2.0 * c[:, 1]) + c[:, 2] ** 2 - 0.5
 
 
+def hashed_nodal_values(xyz_u32: np.ndarray) -> np.ndarray:
+    """Rough nodal values in [-0.5, 0.5) from a hash of the node coordinates,
+    so that every transfer weight shows in the result (transfer fixtures)."""
+    x, y, z = (np.asarray(xyz_u32)[:, i].astype(np.uint64) for i in range(3))
+    h = (x * np.uint64(73856093)) ^ (y * np.uint64(19349663)) ^ (z * np.uint64(83492791))
+    return (h % np.uint64(1 << 20)).astype(np.float64) / float(1 << 20) - 0.5
+
+
+# transfer fixtures: name -> (points, coarsenings before the fine level)
+TRANSFER = {
+    "gauss1500": (lambda: datagen.gaussian(1500, 0.5, 0.15, seed=35), 0),
+    "gauss1500_l1": (lambda: datagen.gaussian(1500, 0.5, 0.15, seed=35), 1),
+    "mixture1500": (lambda: datagen.mixture(1500, np.random.Generator(np.random.PCG64(36))), 0),
+    "boundary800": (lambda: boundary(800, 37), 0),
+}
+
+
 def sparse_octants(rng, D: int, lmax: int, keep: float = 0.3, p_split: float = 0.6, n_anc: int = 0,
                    n_dup: int = 0) -> np.ndarray:
     """Octants {x, y, z, level} at maxDepth D for completeOctree: the leaves

@@ -21,6 +21,10 @@ outputs next to the inputs:
   ref_treesort.npz SFC::parSort::SFC_treeSort outputs (sort only, and
                   TS_REMOVE_DUPLICATES) on octant sets with repeats and
                   ancestors
+  ref_transfer.npz the reference's own restriction and prolongation
+                  (restrictMatVecType1 / prolongMatVecType1 with the Dirichlet
+                  DOFs suppressed) between a balanced octree and its next
+                  coarser level, on cases.TRANSFER
   ref_hilbert.npz the reference's default Hilbert-ordered build
                   (oracle/_ref_hilbert/ref_driver, make ORDER=hilbert):
                   points2Octree, balanceOctree and completeOctree outputs
@@ -215,6 +219,61 @@ def make_mat():
                         row=index(rc[:, :3]), col=index(rc[:, 3:]), val=rec["v"].copy())
 
 
+def read_vec(path):
+    b = open(path, "rb").read()
+    n = int(np.frombuffer(b[:8], np.uint64)[0])
+    rec = np.frombuffer(b[8:], dtype=[("c", "<u4", (4,)), ("v", "<f8")], count=n)
+    return rec["c"][:, :3].copy(), rec["v"].copy()
+
+
+def write_vec(path, xyz, v):
+    rec = np.zeros(len(v), dtype=[("c", "<u4", (4,)), ("v", "<f8")])
+    rec["c"][:, :3] = xyz
+    rec["v"] = v
+    with open(path, "wb") as f:
+        f.write(np.uint64(len(v)).tobytes())
+        f.write(rec.tobytes())
+
+
+def make_transfer():
+    """The reference's transfers (driver mode transfer) on cases.TRANSFER:
+    per case the fine octree, the reference's coarse level, and R v_f and
+    P v_c by node coordinates, v = cases.hashed_nodal_values of the nodes.
+    The node coordinates of the inputs are the oracle's (test
+    infrastructure), and the reference reports any node it did not find."""
+    from oracle import dg_oracle
+
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, (fn, levels) in cases.TRANSFER.items():
+            pf, of, bf = (os.path.join(tmp, f"{name}.{e}") for e in ("pts", "oct", "bal"))
+            write_pts(pf, fn())
+            run("p2o", pf, 30, 1, of)
+            run("bal", of, 30, 1, 0, bf)
+            fine = read_oct(bf)
+            for _ in range(levels):
+                cf = os.path.join(tmp, f"{name}.c")
+                run("coarsen", bf, 30, cf)
+                run("bal", cf, 30, 1, 0, bf)
+                fine = read_oct(bf)
+            coarse = dg_oracle.balance(dg_oracle.coarsen(fine, 30), 30)
+            fxyz = dg_oracle.DA(fine, 30).node_xyz
+            cxyz = dg_oracle.DA(coarse, 30).node_xyz
+            vf, vc = os.path.join(tmp, f"{name}.vf"), os.path.join(tmp, f"{name}.vc")
+            write_vec(vf, fxyz, cases.hashed_nodal_values(fxyz))
+            write_vec(vc, cxyz, cases.hashed_nodal_values(cxyz))
+            prefix = os.path.join(tmp, name)
+            info = run("transfer", bf, 30, os.path.join(REF, "Stencils"), vf, vc, prefix)
+            assert info["missing"] == 0 and info["conflicts"] == 0, info
+            rx, rv = read_vec(prefix + ".r")
+            px, pv = read_vec(prefix + ".p")
+            out[f"{name}/fine"] = fine
+            out[f"{name}/coarse"] = read_oct(prefix + ".coarse")
+            out[f"{name}/r_xyz"], out[f"{name}/r"] = rx, rv
+            out[f"{name}/p_xyz"], out[f"{name}/p"] = px, pv
+    np.savez_compressed(os.path.join(HERE, "ref_transfer.npz"), **out)
+
+
 def make_face_edge():
     """balanceOctree with incCorner = false (faces and edges only) on the
     reference's points2Octree output of every small case whose balance
@@ -277,6 +336,9 @@ def main():
         return
     if "--mat-only" in sys.argv:
         make_mat()
+        return
+    if "--transfer-only" in sys.argv:
+        make_transfer()
         return
     if "--hilbert-only" in sys.argv:
         make_hilbert()
@@ -388,6 +450,7 @@ def main():
     make_complete()
     make_hilbert()
     make_mat()
+    make_transfer()
     make_face_edge()
     make_treesort()
 

@@ -1,13 +1,16 @@
 """Multigrid oracle checks (CPU): transfer stencils pinned to the reference's
-RmatType1/2 tables, coarsening pinned to the reference, P = R^T, and the
-restated PCG + V-cycle converging."""
+RmatType1/2 tables, the transfers themselves pinned to the reference's own
+restriction and prolongation loops, coarsening pinned to the reference,
+P = R^T, and the restated PCG + V-cycle converging."""
 import os
+from types import SimpleNamespace
 
 import numpy as np
 import pytest
 
 from dendro_gb300 import datagen
 from oracle.mg_ref import OracleMG
+from tests.golden import cases
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -88,3 +91,26 @@ def test_prolongation_weights_fit_the_packed_tables(oracle, small_mg, cloud):
         assert np.all(nz == np.round(nz)) and nz.min() >= 1 and nz.max() <= 64
         assert (w != 0).sum(1).max() <= 8
         assert np.all(ids[w != 0] < mg.das[l + 1].n_node)
+
+
+@pytest.mark.parametrize("name", list(cases.TRANSFER))
+def test_transfers_match_the_reference_loops(oracle, name):
+    """The oracle's restriction and prolongation (the ones the GPU transfers
+    are tested against) equal the reference's own restrictMatVecType1 and
+    prolongMatVecType1 (src/omg/restrictMatVec.cpp, prolongMatVec.cpp, with
+    the Dirichlet DOFs suppressed as SetDirichletJacContexts sets them), run
+    by oracle/_ref/ref_driver between a balanced octree and its next coarser
+    level: the same coarse level, and R v, P v at every node."""
+    g = np.load(os.path.join(GOLDEN, "ref_transfer.npz"))
+    fine, coarse = g[f"{name}/fine"], g[f"{name}/coarse"]
+    assert np.array_equal(oracle.balance(oracle.coarsen(fine, 30), 30), coarse)
+    fda, cda = oracle.DA(fine, 30), oracle.DA(coarse, 30)
+    two = SimpleNamespace(pmaps=[fda.prolong_map(coarse, cda)], das=[fda, cda])
+    r = OracleMG.restrict(two, 0, cases.hashed_nodal_values(fda.node_xyz))
+    p = OracleMG.prolong(two, 0, cases.hashed_nodal_values(cda.node_xyz))
+    for xyz, got, ref_xyz, ref in ((cda.node_xyz, r, g[f"{name}/r_xyz"], g[f"{name}/r"]),
+                                   (fda.node_xyz, p, g[f"{name}/p_xyz"], g[f"{name}/p"])):
+        mine, theirs = np.lexsort(xyz.T[::-1]), np.lexsort(ref_xyz.T[::-1])
+        assert np.array_equal(xyz[mine], ref_xyz[theirs])
+        assert np.abs(ref).max() > 0.1
+        assert np.abs(got[mine] - ref[theirs]).max() <= 1e-14 * np.abs(ref).max()
