@@ -49,6 +49,14 @@
  *         (src/omg/prolongMatVec.cpp).  Writes OUT_PREFIX.coarse (the
  *         coarse octree), OUT_PREFIX.r (R VEC_F by coarse node coordinates)
  *         and OUT_PREFIX.p (P VEC_C by fine node coordinates).
+ *   dirichlet BAL.oct MAXDEPTH STENCILDIR VEC_IN OUT_PREFIX
+ *         the multigrid level operator at one rank: the ot::DA of BAL, the
+ *         DirichletJacData of SetDirichletJacContexts
+ *         (examples/src/backend/omgJac.C:509-575), then one
+ *         DirichletJacobianMatMult of VEC_IN (omgJac.C:958) and
+ *         DirichletJacobianMatGetDiagonal (omgJac.C:1111), through a
+ *         MatShell as the reference registers them.  Writes OUT_PREFIX.mv
+ *         (A VEC_IN) and OUT_PREFIX.diag by node coordinates.
  *
  * Formats
  *   .pts : u64 n, then n*3 f64 (x,y,z interleaved)
@@ -70,6 +78,7 @@
 #include "TreeNode.h"
 #include "handleStencils.h"
 #include "omg.h"
+#include "omgJac.h"
 #include "octUtils.h"
 #include "oda.h"
 #include "odaUtils.h"
@@ -79,6 +88,9 @@
 
 double ****LaplacianType2Stencil = nullptr;
 double ****MassType2Stencil = nullptr;
+/* the type-1 tables of omgJac.C's Jacobian3 (never called here) */
+double *****LaplacianType1Stencil = nullptr;
+double *****MassType1Stencil = nullptr;
 namespace ot {
 double ****ShapeFnCoeffs = nullptr;
 /* the restriction tables and vertex maps (defined in src/omg/blockDiag.cpp,
@@ -644,6 +656,63 @@ static int mode_transfer(int argc, char **argv) {
   return conflicts ? 5 : 0;
 }
 
+static int mode_dirichlet(int argc, char **argv) {
+  if (argc < 7) return 1;
+  unsigned maxDepth = std::atoi(argv[3]);
+  std::string stencilDir = argv[4];
+  std::string prefix = argv[6];
+  std::vector<ot::TreeNode> bal = read_oct(argv[2], maxDepth);
+  const size_t nb = bal.size();
+  {
+    /* the tables are read from the working directory */
+    char oldcwd[4096];
+    if (!getcwd(oldcwd, sizeof(oldcwd))) return 4;
+    if (chdir(stencilDir.c_str()) != 0) return 4;
+    ot::DA_Initialize(MPI_COMM_WORLD);
+    createLmatType2(LaplacianType2Stencil);
+    createMmatType2(MassType2Stencil);
+    if (chdir(oldcwd) != 0) return 4;
+  }
+  ot::DA da(bal, MPI_COMM_WORLD, MPI_COMM_WORLD, 0.3, false);
+  std::vector<uint32_t> pos;
+  std::vector<unsigned char> seen;
+  long conflicts = node_positions(da, pos, seen);
+  /* one level of the DAMG, as DAMGCreateAndSetDA and DAMGCreateSuppressedDOFs
+   * (src/omg/blockDiag.cpp:1836-1860, 46-60) leave it at one rank */
+  ot::DAMG damg[1];
+  damg[0] = new ot::_p_DAMG();
+  damg[0]->da = &da;
+  damg[0]->dof = 1;
+  damg[0]->nlevels = 1;
+  damg[0]->totalLevels = 1;
+  damg[0]->comm = MPI_COMM_WORLD;
+  std::vector<unsigned char> sup(da.getLocalBufferSize(), 0);
+  damg[0]->suppressedDOF = sup.data();
+  SetDirichletJacContexts(damg);
+  Mat J;
+  MatCreateShell(MPI_COMM_WORLD, da.getNodeSize(), da.getNodeSize(), PETSC_DETERMINE, PETSC_DETERMINE,
+                 (void *)damg[0], &J);
+  MatShellSetOperation(J, MATOP_MULT, (void (*)(void))DirichletJacobianMatMult);
+  MatShellSetOperation(J, MATOP_GET_DIAGONAL, (void (*)(void))DirichletJacobianMatGetDiagonal);
+  std::unordered_map<unsigned __int128, double, CKeyHash> val;
+  if (!read_vec(argv[5], val)) return 3;
+  Vec in, out, diag;
+  da.createVector(in, false, false, 1);
+  da.createVector(out, false, false, 1);
+  da.createVector(diag, false, false, 1);
+  long missing = fill_vec(da, in, pos, seen, val);
+  if (MatMult(J, in, out) != 0 || MatGetDiagonal(J, diag) != 0) return 6;
+  write_vec(da, out, pos, seen, prefix + ".mv");
+  write_vec(da, diag, pos, seen, prefix + ".diag");
+  size_t nbdy = 0;
+  for (unsigned char b : sup) nbdy += b != 0;
+  if (missing) std::fprintf(stderr, "warning: %ld node values missing from the input vector\n", missing);
+  std::printf("{\"op\":\"dirichlet\",\"n_bal\":%zu,\"nodes\":%u,\"boundary_nodes\":%zu,\"conflicts\":%ld,"
+              "\"missing\":%ld}\n",
+              nb, da.getNodeSize(), nbdy, conflicts, missing);
+  return conflicts ? 5 : 0;
+}
+
 // io PTS D OUTPREFIX: the reference's own file writers on one cloud --
 // writePtsToFile (OUTPREFIX.pts), and for its balanced octree writeNodesToFile
 // (OUTPREFIX.ot, text) and writeNodesToFile_binary (OUTPREFIX.otb); then its
@@ -701,5 +770,6 @@ int main(int argc, char **argv) {
   if (m == "io") rc = mode_io(argc, argv);
   if (m == "treesort") rc = mode_treesort(argc, argv);
   if (m == "transfer") rc = mode_transfer(argc, argv);
+  if (m == "dirichlet") rc = mode_dirichlet(argc, argv);
   return rc;
 }

@@ -154,6 +154,24 @@ inline PetscErrorCode VecSet(Vec v, PetscScalar s) {
   for (size_t i = 0; i < v->n; i++) v->a[i] = s;
   return 0;
 }
+/* options: none is ever set here (the reference's defaults apply) */
+inline PetscErrorCode PetscOptionsGetInt(void *, const char *, const char *, PetscInt *, PetscBool *set) {
+  if (set) *set = PETSC_FALSE;
+  return 0;
+}
+inline PetscErrorCode PetscOptionsGetReal(void *, const char *, const char *, PetscReal *, PetscBool *set) {
+  if (set) *set = PETSC_FALSE;
+  return 0;
+}
+inline PetscErrorCode PetscOptionsGetString(void *, const char *, const char *, char *, size_t, PetscBool *set) {
+  if (set) *set = PETSC_FALSE;
+  return 0;
+}
+inline PetscErrorCode VecPlaceArray(Vec v, const PetscScalar *a) {
+  v->a = (PetscScalar *)a;
+  return 0;
+}
+inline PetscErrorCode VecResetArray(Vec) { return 0; }
 inline PetscErrorCode PetscStrcmp(const char *a, const char *b, PetscBool *f) {
   *f = (PetscBool)(std::strcmp(a, b) == 0);
   return 0;
@@ -185,6 +203,13 @@ inline PetscErrorCode MatDestroy(Mat *m) {
   return 0;
 }
 inline PetscErrorCode MatSetSizes(Mat, PetscInt, PetscInt, PetscInt, PetscInt) { return 0; }
+/* every Mat made here is a shell (MatCreateShell) or an empty stand-in */
+inline PetscErrorCode PetscObjectTypeCompare(PetscObject, const char *type, PetscBool *same) {
+  *same = (PetscBool)(std::strcmp(type, MATSHELL) == 0);
+  return 0;
+}
+inline PetscErrorCode MatZeroEntries(Mat) { return 0; }
+inline PetscErrorCode MatCreateVecs(Mat, Vec *, Vec *) { return PETSC_ERR_SUP; }
 inline PetscErrorCode MatSetType(Mat, MatType) { return 0; }
 inline PetscErrorCode MatSeqAIJSetPreallocation(Mat, PetscInt, const PetscInt *) { return 0; }
 inline PetscErrorCode MatMPIAIJSetPreallocation(Mat, PetscInt, const PetscInt *, PetscInt, const PetscInt *) {

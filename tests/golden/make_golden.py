@@ -21,10 +21,13 @@ outputs next to the inputs:
   ref_treesort.npz SFC::parSort::SFC_treeSort outputs (sort only, and
                   TS_REMOVE_DUPLICATES) on octant sets with repeats and
                   ancestors
-  ref_transfer.npz the reference's own restriction and prolongation
+  ref_mg_ops.npz  the reference's own multigrid level operators on
+                  cases.TRANSFER: restriction and prolongation
                   (restrictMatVecType1 / prolongMatVecType1 with the Dirichlet
                   DOFs suppressed) between a balanced octree and its next
-                  coarser level, on cases.TRANSFER
+                  coarser level, and the Dirichlet operator and diagonal
+                  (DirichletJacobianMatMult / DirichletJacobianMatGetDiagonal)
+                  on the finer one
   ref_hilbert.npz the reference's default Hilbert-ordered build
                   (oracle/_ref_hilbert/ref_driver, make ORDER=hilbert):
                   points2Octree, balanceOctree and completeOctree outputs
@@ -235,12 +238,14 @@ def write_vec(path, xyz, v):
         f.write(rec.tobytes())
 
 
-def make_transfer():
-    """The reference's transfers (driver mode transfer) on cases.TRANSFER:
-    per case the fine octree, the reference's coarse level, and R v_f and
-    P v_c by node coordinates, v = cases.hashed_nodal_values of the nodes.
-    The node coordinates of the inputs are the oracle's (test
-    infrastructure), and the reference reports any node it did not find."""
+def make_mg_ops():
+    """The reference's multigrid level operators (driver modes transfer and
+    dirichlet) on cases.TRANSFER: per case the fine octree, the reference's
+    coarse level, R v_f and P v_c, and A v_f and diag(A) of the Dirichlet
+    operator on the fine level, by node coordinates, v =
+    cases.hashed_nodal_values of the nodes.  The node coordinates of the
+    inputs are the oracle's (test infrastructure), and the reference reports
+    any node it did not find."""
     from oracle import dg_oracle
 
     out = {}
@@ -267,11 +272,17 @@ def make_transfer():
             assert info["missing"] == 0 and info["conflicts"] == 0, info
             rx, rv = read_vec(prefix + ".r")
             px, pv = read_vec(prefix + ".p")
+            info = run("dirichlet", bf, 30, os.path.join(REF, "Stencils"), vf, prefix)
+            assert info["missing"] == 0 and info["conflicts"] == 0, info
+            ax, av = read_vec(prefix + ".mv")
+            dx, dv = read_vec(prefix + ".diag")
+            assert np.array_equal(ax, dx)
+            out[f"{name}/a_xyz"], out[f"{name}/a"], out[f"{name}/diag"] = ax, av, dv
             out[f"{name}/fine"] = fine
             out[f"{name}/coarse"] = read_oct(prefix + ".coarse")
             out[f"{name}/r_xyz"], out[f"{name}/r"] = rx, rv
             out[f"{name}/p_xyz"], out[f"{name}/p"] = px, pv
-    np.savez_compressed(os.path.join(HERE, "ref_transfer.npz"), **out)
+    np.savez_compressed(os.path.join(HERE, "ref_mg_ops.npz"), **out)
 
 
 def make_face_edge():
@@ -337,8 +348,8 @@ def main():
     if "--mat-only" in sys.argv:
         make_mat()
         return
-    if "--transfer-only" in sys.argv:
-        make_transfer()
+    if "--mg-ops-only" in sys.argv:
+        make_mg_ops()
         return
     if "--hilbert-only" in sys.argv:
         make_hilbert()
@@ -450,7 +461,7 @@ def main():
     make_complete()
     make_hilbert()
     make_mat()
-    make_transfer()
+    make_mg_ops()
     make_face_edge()
     make_treesort()
 

@@ -101,7 +101,7 @@ def test_transfers_match_the_reference_loops(oracle, name):
     the Dirichlet DOFs suppressed as SetDirichletJacContexts sets them), run
     by oracle/_ref/ref_driver between a balanced octree and its next coarser
     level: the same coarse level, and R v, P v at every node."""
-    g = np.load(os.path.join(GOLDEN, "ref_transfer.npz"))
+    g = np.load(os.path.join(GOLDEN, "ref_mg_ops.npz"))
     fine, coarse = g[f"{name}/fine"], g[f"{name}/coarse"]
     assert np.array_equal(oracle.balance(oracle.coarsen(fine, 30), 30), coarse)
     fda, cda = oracle.DA(fine, 30), oracle.DA(coarse, 30)
@@ -114,3 +114,25 @@ def test_transfers_match_the_reference_loops(oracle, name):
         assert np.array_equal(xyz[mine], ref_xyz[theirs])
         assert np.abs(ref).max() > 0.1
         assert np.abs(got[mine] - ref[theirs]).max() <= 1e-14 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("name", list(cases.TRANSFER))
+def test_dirichlet_operator_matches_the_reference(oracle, name):
+    """The oracle's Dirichlet level operator and its diagonal (the GPU's are
+    tested against them) equal the reference's own DirichletJacobianMatMult
+    and DirichletJacobianMatGetDiagonal (examples/src/backend/omgJac.C:958,
+    1111, with SetDirichletJacContexts' boundary flags), run by
+    oracle/_ref/ref_driver on the same octree: A v and diag(A) at every node
+    to 1e-14 of the largest value (the sums run in another order)."""
+    g = np.load(os.path.join(GOLDEN, "ref_mg_ops.npz"))
+    da = oracle.DA(g[f"{name}/fine"], 30)
+    av = da.dirichlet_matvec(cases.hashed_nodal_values(da.node_xyz))
+    dg = da.dirichlet_diag()
+    mine, theirs = np.lexsort(da.node_xyz.T[::-1]), np.lexsort(g[f"{name}/a_xyz"].T[::-1])
+    assert np.array_equal(da.node_xyz[mine], g[f"{name}/a_xyz"][theirs])
+    for got, ref in ((av, g[f"{name}/a"]), (dg, g[f"{name}/diag"])):
+        assert np.abs(ref).max() > 0
+        assert np.abs(got[mine] - ref[theirs]).max() <= 1e-14 * np.abs(ref).max()
+    # boundary rows are the identity: diag 1 exactly, A v = v there
+    bdy = g[f"{name}/diag"][theirs] == 1.0
+    assert bdy.sum() > 0 and np.array_equal(av[mine][bdy], cases.hashed_nodal_values(da.node_xyz)[mine][bdy])
