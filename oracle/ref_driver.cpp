@@ -57,8 +57,20 @@
  *         DirichletJacobianMatGetDiagonal (omgJac.C:1111), through a
  *         MatShell as the reference registers them.  Writes OUT_PREFIX.mv
  *         (A VEC_IN) and OUT_PREFIX.diag by node coordinates.
+ *   jac   BAL.oct MAXDEPTH STENCILDIR VEC_IN COEF_IN OUT_PREFIX
+ *         the element-loop MatShell callbacks at one rank on the ot::DA of
+ *         BAL, registered as the reference registers them:
+ *         Jacobian1MatMult, Jacobian1MatGetDiagonal, MassMatMult and
+ *         MassMatGetDiagonal (examples/src/backend/odaJac.C:294,160,399,229;
+ *         context Jac1MFreeData) and Jacobian2MatMult / Jacobian2MatGetDiagonal
+ *         (examples/src/backend/omgJac.C:1776,1641; a one-level DAMG whose
+ *         Jac2MFreeData holds the per-element (lap, mass) factors of COEF_IN,
+ *         an elemental 2-dof vector).  Writes OUT_PREFIX.{j1,j1d,m,md,j2,j2d}
+ *         by node coordinates.
  *
  * Formats
+ *   coef : u64 n, then n*(u32 x, u32 y, u32 z, u32 level, f64 lap, f64 mass),
+ *          one record per octant of BAL (octree level)
  *   .pts : u64 n, then n*3 f64 (x,y,z interleaved)
  *   .oct : u64 n, then n*(u32 x, u32 y, u32 z, u32 level)
  *   mat  : u64 n, then n*(u32 rx, ry, rz, cx, cy, cz, f64 value)
@@ -78,6 +90,7 @@
 #include "TreeNode.h"
 #include "handleStencils.h"
 #include "omg.h"
+#include "odaJac.h"
 #include "omgJac.h"
 #include "octUtils.h"
 #include "oda.h"
@@ -713,6 +726,117 @@ static int mode_dirichlet(int argc, char **argv) {
   return conflicts ? 5 : 0;
 }
 
+static int mode_jac(int argc, char **argv) {
+  if (argc < 8) return 1;
+  unsigned maxDepth = std::atoi(argv[3]);
+  std::string stencilDir = argv[4];
+  std::string prefix = argv[7];
+  std::vector<ot::TreeNode> bal = read_oct(argv[2], maxDepth);
+  const size_t nb = bal.size();
+  {
+    /* the tables are read from the working directory */
+    char oldcwd[4096];
+    if (!getcwd(oldcwd, sizeof(oldcwd))) return 4;
+    if (chdir(stencilDir.c_str()) != 0) return 4;
+    ot::DA_Initialize(MPI_COMM_WORLD);
+    createLmatType2(LaplacianType2Stencil);
+    createMmatType2(MassType2Stencil);
+    if (chdir(oldcwd) != 0) return 4;
+  }
+  /* per-element factors by (anchor, octree level) */
+  std::map<std::pair<unsigned __int128, unsigned>, std::pair<double, double>> coef;
+  {
+    FILE *f = xopen(argv[6], "rb");
+    uint64_t n = 0;
+    if (std::fread(&n, 8, 1, f) != 1) return 3;
+    for (uint64_t i = 0; i < n; i++) {
+      uint32_t c[4];
+      double v[2];
+      if (std::fread(c, 4, 4, f) != 4 || std::fread(v, 8, 2, f) != 2) return 3;
+      coef[std::make_pair(ckey(c[0], c[1], c[2]), c[3])] = std::make_pair(v[0], v[1]);
+    }
+    std::fclose(f);
+  }
+  ot::DA da(bal, MPI_COMM_WORLD, MPI_COMM_WORLD, 0.3, false);
+  std::vector<uint32_t> pos;
+  std::vector<unsigned char> seen;
+  long conflicts = node_positions(da, pos, seen);
+  /* the elemental, ghosted 2-dof factor vector (lap, mass per element) */
+  std::vector<double> matProp;
+  da.createVector<double>(matProp, true, true, 2);
+  long missing = 0;
+  {
+    double *arr = NULL;
+    da.vecGetBuffer<double>(matProp, arr, true, true, false, 2);
+    for (da.init<ot::DA_FLAGS::ALL>(); da.curr() < da.end<ot::DA_FLAGS::ALL>(); da.next<ot::DA_FLAGS::ALL>()) {
+      Point pt = da.getCurrentOffset();
+      unsigned lev = da.getLevel(da.curr()) - 1; /* the DA adds one level */
+      auto it = coef.find(std::make_pair(ckey(pt.xint(), pt.yint(), pt.zint()), lev));
+      if (it == coef.end()) {
+        missing++;
+        continue;
+      }
+      arr[2 * da.curr()] = it->second.first;
+      arr[2 * da.curr() + 1] = it->second.second;
+    }
+    da.vecRestoreBuffer<double>(matProp, arr, true, true, false, 2);
+  }
+  Jac1MFreeData jd;
+  jd.da = &da;
+  jd.isFinestLevel = false;
+  jd.Jmat_private = NULL;
+  jd.inTmp = NULL;
+  jd.outTmp = NULL;
+  Mat J1, M;
+  MatCreateShell(MPI_COMM_WORLD, da.getNodeSize(), da.getNodeSize(), PETSC_DETERMINE, PETSC_DETERMINE, (void *)&jd,
+                 &J1);
+  MatShellSetOperation(J1, MATOP_MULT, (void (*)(void))Jacobian1MatMult);
+  MatShellSetOperation(J1, MATOP_GET_DIAGONAL, (void (*)(void))Jacobian1MatGetDiagonal);
+  MatCreateShell(MPI_COMM_WORLD, da.getNodeSize(), da.getNodeSize(), PETSC_DETERMINE, PETSC_DETERMINE, (void *)&jd,
+                 &M);
+  MatShellSetOperation(M, MATOP_MULT, (void (*)(void))MassMatMult);
+  MatShellSetOperation(M, MATOP_GET_DIAGONAL, (void (*)(void))MassMatGetDiagonal);
+  Jac2MFreeData j2d;
+  j2d.matProp = &matProp;
+  j2d.isFinestLevel = false;
+  j2d.Jmat_private = NULL;
+  j2d.inTmp = NULL;
+  j2d.outTmp = NULL;
+  ot::DAMG damg = new ot::_p_DAMG();
+  damg->da = &da;
+  damg->dof = 1;
+  damg->nlevels = 1;
+  damg->totalLevels = 1;
+  damg->comm = MPI_COMM_WORLD;
+  damg->user = &j2d;
+  Mat J2;
+  MatCreateShell(MPI_COMM_WORLD, da.getNodeSize(), da.getNodeSize(), PETSC_DETERMINE, PETSC_DETERMINE, (void *)damg,
+                 &J2);
+  MatShellSetOperation(J2, MATOP_MULT, (void (*)(void))Jacobian2MatMult);
+  MatShellSetOperation(J2, MATOP_GET_DIAGONAL, (void (*)(void))Jacobian2MatGetDiagonal);
+
+  std::unordered_map<unsigned __int128, double, CKeyHash> val;
+  if (!read_vec(argv[5], val)) return 3;
+  Vec in, out;
+  da.createVector(in, false, false, 1);
+  da.createVector(out, false, false, 1);
+  missing += fill_vec(da, in, pos, seen, val);
+  const struct {
+    Mat m;
+    const char *ext;
+  } ops[3] = {{J1, ".j1"}, {M, ".m"}, {J2, ".j2"}};
+  for (const auto &op : ops) {
+    if (MatMult(op.m, in, out) != 0) return 6;
+    write_vec(da, out, pos, seen, prefix + op.ext);
+    if (MatGetDiagonal(op.m, out) != 0) return 6;
+    write_vec(da, out, pos, seen, prefix + op.ext + "d");
+  }
+  if (missing) std::fprintf(stderr, "warning: %ld values missing from the inputs\n", missing);
+  std::printf("{\"op\":\"jac\",\"n_bal\":%zu,\"nodes\":%u,\"conflicts\":%ld,\"missing\":%ld}\n", nb,
+              da.getNodeSize(), conflicts, missing);
+  return conflicts ? 5 : 0;
+}
+
 // io PTS D OUTPREFIX: the reference's own file writers on one cloud --
 // writePtsToFile (OUTPREFIX.pts), and for its balanced octree writeNodesToFile
 // (OUTPREFIX.ot, text) and writeNodesToFile_binary (OUTPREFIX.otb); then its
@@ -771,5 +895,6 @@ int main(int argc, char **argv) {
   if (m == "treesort") rc = mode_treesort(argc, argv);
   if (m == "transfer") rc = mode_transfer(argc, argv);
   if (m == "dirichlet") rc = mode_dirichlet(argc, argv);
+  if (m == "jac") rc = mode_jac(argc, argv);
   return rc;
 }

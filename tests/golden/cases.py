@@ -69,6 +69,17 @@ def hashed_nodal_values(xyz_u32: np.ndarray) -> np.ndarray:
     return (h % np.uint64(1 << 20)).astype(np.float64) / float(1 << 20) - 0.5
 
 
+def element_factors(octs: np.ndarray) -> np.ndarray:
+    """Per-octant (Laplacian, mass) factors in [0.5, 1.5) x [0.25, 2.25) from
+    a hash of the octant's anchor and level (Jacobian2 fixtures)."""
+    o = np.asarray(octs)
+    x, y, z, l = (o[:, i].astype(np.uint64) for i in range(4))
+    h = (x * np.uint64(73856093)) ^ (y * np.uint64(19349663)) ^ (z * np.uint64(83492791)) ^ (l * np.uint64(2654435761))
+    lap = 0.5 + (h % np.uint64(1024)).astype(np.float64) / 1024.0
+    mass = 0.25 + ((h >> np.uint64(10)) % np.uint64(1024)).astype(np.float64) / 512.0
+    return np.stack([lap, mass], 1)
+
+
 # transfer fixtures: name -> (points, coarsenings before the fine level)
 TRANSFER = {
     "gauss1500": (lambda: datagen.gaussian(1500, 0.5, 0.15, seed=35), 0),

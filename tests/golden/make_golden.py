@@ -21,13 +21,16 @@ outputs next to the inputs:
   ref_treesort.npz SFC::parSort::SFC_treeSort outputs (sort only, and
                   TS_REMOVE_DUPLICATES) on octant sets with repeats and
                   ancestors
-  ref_mg_ops.npz  the reference's own multigrid level operators on
-                  cases.TRANSFER: restriction and prolongation
-                  (restrictMatVecType1 / prolongMatVecType1 with the Dirichlet
-                  DOFs suppressed) between a balanced octree and its next
-                  coarser level, and the Dirichlet operator and diagonal
-                  (DirichletJacobianMatMult / DirichletJacobianMatGetDiagonal)
-                  on the finer one
+  ref_mg_ops.npz  the reference's own operators on cases.TRANSFER:
+                  restriction and prolongation (restrictMatVecType1 /
+                  prolongMatVecType1 with the Dirichlet DOFs suppressed)
+                  between a balanced octree and its next coarser level, the
+                  Dirichlet operator and diagonal (DirichletJacobianMatMult /
+                  DirichletJacobianMatGetDiagonal) on the finer one, and on
+                  the level-0 octrees the element-loop MatShell callbacks
+                  (Jacobian1MatMult / Jacobian1MatGetDiagonal, MassMatMult /
+                  MassMatGetDiagonal, Jacobian2MatMult /
+                  Jacobian2MatGetDiagonal with cases.element_factors)
   ref_hilbert.npz the reference's default Hilbert-ordered build
                   (oracle/_ref_hilbert/ref_driver, make ORDER=hilbert):
                   points2Octree, balanceOctree and completeOctree outputs
@@ -238,6 +241,14 @@ def write_vec(path, xyz, v):
         f.write(rec.tobytes())
 
 
+def write_coef(path, octs, coef):
+    rec = np.zeros(len(octs), dtype=[("c", "<u4", (4,)), ("v", "<f8", (2,))])
+    rec["c"], rec["v"] = octs, coef
+    with open(path, "wb") as f:
+        f.write(np.uint64(len(octs)).tobytes())
+        f.write(rec.tobytes())
+
+
 def make_mg_ops():
     """The reference's multigrid level operators (driver modes transfer and
     dirichlet) on cases.TRANSFER: per case the fine octree, the reference's
@@ -278,6 +289,14 @@ def make_mg_ops():
             dx, dv = read_vec(prefix + ".diag")
             assert np.array_equal(ax, dx)
             out[f"{name}/a_xyz"], out[f"{name}/a"], out[f"{name}/diag"] = ax, av, dv
+            if levels == 0:
+                cf = os.path.join(tmp, f"{name}.coef")
+                write_coef(cf, fine, cases.element_factors(fine))
+                info = run("jac", bf, 30, os.path.join(REF, "Stencils"), vf, cf, prefix)
+                assert info["missing"] == 0 and info["conflicts"] == 0, info
+                for op in ("j1", "j1d", "m", "md", "j2", "j2d"):
+                    jx, out[f"{name}/{op}"] = read_vec(f"{prefix}.{op}")
+                    assert np.array_equal(jx, ax)
             out[f"{name}/fine"] = fine
             out[f"{name}/coarse"] = read_oct(prefix + ".coarse")
             out[f"{name}/r_xyz"], out[f"{name}/r"] = rx, rv

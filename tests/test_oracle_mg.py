@@ -136,3 +136,32 @@ def test_dirichlet_operator_matches_the_reference(oracle, name):
     # boundary rows are the identity: diag 1 exactly, A v = v there
     bdy = g[f"{name}/diag"][theirs] == 1.0
     assert bdy.sum() > 0 and np.array_equal(av[mine][bdy], cases.hashed_nodal_values(da.node_xyz)[mine][bdy])
+
+
+@pytest.mark.parametrize("name", [n for n, (_, lv) in cases.TRANSFER.items() if lv == 0])
+def test_element_callbacks_match_the_reference(oracle, name):
+    """The oracle's element-loop operators (the GPU's are tested against
+    them) equal the reference's own MatShell callbacks, run by
+    oracle/_ref/ref_driver on the same octree: Jacobian1MatMult /
+    Jacobian1MatGetDiagonal and MassMatMult / MassMatGetDiagonal
+    (examples/src/backend/odaJac.C:294,160,399,229), Jacobian2MatMult /
+    Jacobian2MatGetDiagonal with per-element factors (omgJac.C:1776,1641).
+    Tolerance 1e-12 of the largest value: the oracle's stencils come from
+    their definition, the reference's from .inp files with 15 decimals."""
+    from oracle import dg_oracle
+
+    g = np.load(os.path.join(GOLDEN, "ref_mg_ops.npz"))
+    fine = g[f"{name}/fine"]
+    da = oracle.DA(fine, 30)
+    assert np.array_equal(da.level, fine[:, 3])  # elements in octant order
+    x = cases.hashed_nodal_values(da.node_xyz)
+    coef = cases.element_factors(fine)
+    want = {"j1": da.matvec(x), "j1d": dg_oracle.diagonal(da), "m": da.matvec(x, 0.0, 1.0),
+            "md": dg_oracle.diagonal(da, 0.0, 1.0), "j2": dg_oracle.matvec_coef(da, coef, x),
+            "j2d": dg_oracle.diagonal(da, coef=coef)}
+    mine, theirs = np.lexsort(da.node_xyz.T[::-1]), np.lexsort(g[f"{name}/a_xyz"].T[::-1])
+    assert np.array_equal(da.node_xyz[mine], g[f"{name}/a_xyz"][theirs])
+    for op, got in want.items():
+        ref = g[f"{name}/{op}"][theirs]
+        assert np.abs(ref).max() > 0
+        assert np.abs(got[mine] - ref).max() <= 1e-12 * np.abs(ref).max(), op
