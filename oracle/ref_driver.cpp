@@ -67,6 +67,16 @@
  *         Jac2MFreeData holds the per-element (lap, mass) factors of COEF_IN,
  *         an elemental 2-dof vector).  Writes OUT_PREFIX.{j1,j1d,m,md,j2,j2d}
  *         by node coordinates.
+ *   assemble BAL.oct MAXDEPTH STENCILDIR COEF_IN OUT_PREFIX
+ *         the reference's assembled matrices at one rank on the ot::DA of
+ *         BAL (after DA::computeLocalToGlobalMappings, src/oda/oda.cpp:77;
+ *         entries through DA::setValuesInMatrix, oda.cpp:139, into the
+ *         shim's recording MatSetValues): CreateAndComputeFullJacobian1
+ *         (examples/src/backend/odaJac.C:470, -fullJacMatType aij),
+ *         ComputeDirichletJacobian (omgJac.C:383, the boundary flags of
+ *         SetDirichletJacContexts) and ComputeJacobian2 (omgJac.C:1861,
+ *         BUILD_FULL_JAC_TYPE2_BLOCK with the per-element factors of
+ *         COEF_IN).  Writes OUT_PREFIX.{k,kd,k2} in the mat format.
  *
  * Formats
  *   coef : u64 n, then n*(u32 x, u32 y, u32 z, u32 level, f64 lap, f64 mass),
@@ -837,6 +847,140 @@ static int mode_jac(int argc, char **argv) {
   return conflicts ? 5 : 0;
 }
 
+/* per-element (lap, mass) factors of a coef file into the DA's elemental,
+ * ghosted 2-dof vector; returns the elements without a record */
+static long read_coef(const char *path, ot::DA &da, std::vector<double> &matProp) {
+  std::map<std::pair<unsigned __int128, unsigned>, std::pair<double, double>> coef;
+  FILE *f = xopen(path, "rb");
+  uint64_t n = 0;
+  if (std::fread(&n, 8, 1, f) != 1) return -1;
+  for (uint64_t i = 0; i < n; i++) {
+    uint32_t c[4];
+    double v[2];
+    if (std::fread(c, 4, 4, f) != 4 || std::fread(v, 8, 2, f) != 2) return -1;
+    coef[std::make_pair(ckey(c[0], c[1], c[2]), c[3])] = std::make_pair(v[0], v[1]);
+  }
+  std::fclose(f);
+  da.createVector<double>(matProp, true, true, 2);
+  long missing = 0;
+  double *arr = NULL;
+  da.vecGetBuffer<double>(matProp, arr, true, true, false, 2);
+  for (da.init<ot::DA_FLAGS::ALL>(); da.curr() < da.end<ot::DA_FLAGS::ALL>(); da.next<ot::DA_FLAGS::ALL>()) {
+    Point pt = da.getCurrentOffset();
+    unsigned lev = da.getLevel(da.curr()) - 1; /* the DA adds one level */
+    auto it = coef.find(std::make_pair(ckey(pt.xint(), pt.yint(), pt.zint()), lev));
+    if (it == coef.end()) {
+      missing++;
+      continue;
+    }
+    arr[2 * da.curr()] = it->second.first;
+    arr[2 * da.curr() + 1] = it->second.second;
+  }
+  da.vecRestoreBuffer<double>(matProp, arr, true, true, false, 2);
+  return missing;
+}
+
+/* the recorded entries of an assembled matrix, by node coordinates (global
+ * index -> buffer index through the DA's local-to-global map) */
+static long write_entries(ot::DA &da, Mat m, const std::vector<uint32_t> &pos, const std::vector<unsigned char> &seen,
+                          const std::string &path) {
+  const DendroIntL *l2g = da.getLocalToGlobalMap();
+  std::unordered_map<DendroIntL, size_t> g2b;
+  for (size_t i = 0; i < seen.size(); i++)
+    if (seen[i]) g2b[l2g[i]] = i;
+  FILE *g = xopen(path.c_str(), "wb");
+  uint64_t n = m->entries ? m->entries->size() : 0;
+  std::fwrite(&n, 8, 1, g);
+  long unmapped = 0;
+  if (m->entries)
+    for (const auto &kv : *m->entries) {
+      auto r = g2b.find(kv.first.first), c = g2b.find(kv.first.second);
+      if (r == g2b.end() || c == g2b.end()) {
+        unmapped++;
+        continue;
+      }
+      uint32_t rc[6] = {pos[3 * r->second], pos[3 * r->second + 1], pos[3 * r->second + 2],
+                        pos[3 * c->second], pos[3 * c->second + 1], pos[3 * c->second + 2]};
+      std::fwrite(rc, 4, 6, g);
+      std::fwrite(&kv.second, 8, 1, g);
+    }
+  std::fclose(g);
+  return unmapped;
+}
+
+static int mode_assemble(int argc, char **argv) {
+  if (argc < 7) return 1;
+  unsigned maxDepth = std::atoi(argv[3]);
+  std::string stencilDir = argv[4];
+  std::string prefix = argv[6];
+  std::vector<ot::TreeNode> bal = read_oct(argv[2], maxDepth);
+  const size_t nb = bal.size();
+  {
+    /* the tables are read from the working directory */
+    char oldcwd[4096];
+    if (!getcwd(oldcwd, sizeof(oldcwd))) return 4;
+    if (chdir(stencilDir.c_str()) != 0) return 4;
+    ot::DA_Initialize(MPI_COMM_WORLD);
+    createLmatType2(LaplacianType2Stencil);
+    createMmatType2(MassType2Stencil);
+    if (chdir(oldcwd) != 0) return 4;
+  }
+  ot::DA da(bal, MPI_COMM_WORLD, MPI_COMM_WORLD, 0.3, false);
+  std::vector<uint32_t> pos;
+  std::vector<unsigned char> seen;
+  long conflicts = node_positions(da, pos, seen);
+  da.computeLocalToGlobalMappings();
+  std::vector<double> matProp;
+  long missing = read_coef(argv[5], da, matProp);
+  if (missing < 0) return 3;
+
+  dg_shim_options()["-fullJacMatType"] = MATAIJ;
+  Mat K = NULL;
+  if (CreateAndComputeFullJacobian1(&da, &K) != 0) return 6;
+
+  /* one level of the DAMG (as in the dirichlet mode) for the Dirichlet
+   * matrix, and one with the Jacobian2 context */
+  ot::DAMG damg[1];
+  damg[0] = new ot::_p_DAMG();
+  damg[0]->da = &da;
+  damg[0]->dof = 1;
+  damg[0]->nlevels = 1;
+  damg[0]->totalLevels = 1;
+  damg[0]->comm = MPI_COMM_WORLD;
+  std::vector<unsigned char> sup(da.getLocalBufferSize(), 0);
+  damg[0]->suppressedDOF = sup.data();
+  SetDirichletJacContexts(damg);
+  Mat KD = NULL;
+  da.createMatrix(KD, MATAIJ, 1);
+  if (ComputeDirichletJacobian(damg[0], KD, KD) != 0) return 6;
+
+  Jac2MFreeData j2d;
+  j2d.matProp = &matProp;
+  j2d.isFinestLevel = false;
+  j2d.Jmat_private = NULL;
+  j2d.inTmp = NULL;
+  j2d.outTmp = NULL;
+  ot::DAMG damg2 = new ot::_p_DAMG();
+  damg2->da = &da;
+  damg2->dof = 1;
+  damg2->nlevels = 1;
+  damg2->totalLevels = 1;
+  damg2->comm = MPI_COMM_WORLD;
+  damg2->user = &j2d;
+  Mat K2 = NULL;
+  da.createMatrix(K2, MATAIJ, 1);
+  if (ComputeJacobian2(damg2, K2, K2) != 0) return 6;
+
+  long unmapped = write_entries(da, K, pos, seen, prefix + ".k") + write_entries(da, KD, pos, seen, prefix + ".kd") +
+                  write_entries(da, K2, pos, seen, prefix + ".k2");
+  std::printf("{\"op\":\"assemble\",\"n_bal\":%zu,\"nodes\":%u,\"nnz\":[%zu,%zu,%zu],\"conflicts\":%ld,"
+              "\"missing\":%ld,\"unmapped\":%ld}\n",
+              nb, da.getNodeSize(), K->entries ? K->entries->size() : (size_t)0,
+              KD->entries ? KD->entries->size() : (size_t)0, K2->entries ? K2->entries->size() : (size_t)0, conflicts,
+              missing, unmapped);
+  return (conflicts || unmapped) ? 5 : 0;
+}
+
 // io PTS D OUTPREFIX: the reference's own file writers on one cloud --
 // writePtsToFile (OUTPREFIX.pts), and for its balanced octree writeNodesToFile
 // (OUTPREFIX.ot, text) and writeNodesToFile_binary (OUTPREFIX.otb); then its
@@ -896,5 +1040,6 @@ int main(int argc, char **argv) {
   if (m == "transfer") rc = mode_transfer(argc, argv);
   if (m == "dirichlet") rc = mode_dirichlet(argc, argv);
   if (m == "jac") rc = mode_jac(argc, argv);
+  if (m == "assemble") rc = mode_assemble(argc, argv);
   return rc;
 }

@@ -14,6 +14,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <string>
+#include <utility>
 
 #include "mpi.h"
 
@@ -59,6 +62,9 @@ struct dg_shim_mat {
   PetscErrorCode (*mult)(Mat, Vec, Vec);
   PetscErrorCode (*diag)(Mat, Vec);
   PetscErrorCode (*multT)(Mat, Vec, Vec);
+  const char *type;
+  /* the entries of an assembled (non-shell) matrix, by global (row, column) */
+  std::map<std::pair<PetscInt, PetscInt>, PetscScalar> *entries;
 };
 struct dg_shim_opaque {
   int unused;
@@ -154,7 +160,13 @@ inline PetscErrorCode VecSet(Vec v, PetscScalar s) {
   for (size_t i = 0; i < v->n; i++) v->a[i] = s;
   return 0;
 }
-/* options: none is ever set here (the reference's defaults apply) */
+/* options: string options without a prefix can be set by the caller
+ * (dg_shim_options()); integer and real options are never set, so the
+ * reference's defaults apply */
+inline std::map<std::string, std::string> &dg_shim_options() {
+  static std::map<std::string, std::string> opts;
+  return opts;
+}
 inline PetscErrorCode PetscOptionsGetInt(void *, const char *, const char *, PetscInt *, PetscBool *set) {
   if (set) *set = PETSC_FALSE;
   return 0;
@@ -163,8 +175,15 @@ inline PetscErrorCode PetscOptionsGetReal(void *, const char *, const char *, Pe
   if (set) *set = PETSC_FALSE;
   return 0;
 }
-inline PetscErrorCode PetscOptionsGetString(void *, const char *, const char *, char *, size_t, PetscBool *set) {
-  if (set) *set = PETSC_FALSE;
+inline PetscErrorCode PetscOptionsGetString(void *, const char *pre, const char *name, char *out, size_t len,
+                                            PetscBool *set) {
+  auto it = dg_shim_options().find(name);
+  const bool found = pre == nullptr && it != dg_shim_options().end() && len > 0;
+  if (found) {
+    std::strncpy(out, it->second.c_str(), len - 1);
+    out[len - 1] = 0;
+  }
+  if (set) *set = (PetscBool)found;
   return 0;
 }
 inline PetscErrorCode VecPlaceArray(Vec v, const PetscScalar *a) {
@@ -177,11 +196,11 @@ inline PetscErrorCode PetscStrcmp(const char *a, const char *b, PetscBool *f) {
   return 0;
 }
 inline PetscErrorCode MatCreate(MPI_Comm, Mat *m) {
-  *m = new dg_shim_mat{nullptr, nullptr, nullptr, nullptr};
+  *m = new dg_shim_mat{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   return 0;
 }
 inline PetscErrorCode MatCreateShell(MPI_Comm, PetscInt, PetscInt, PetscInt, PetscInt, void *ctx, Mat *m) {
-  *m = new dg_shim_mat{ctx, nullptr, nullptr, nullptr};
+  *m = new dg_shim_mat{ctx, nullptr, nullptr, nullptr, MATSHELL, nullptr};
   return 0;
 }
 inline PetscErrorCode MatShellGetContext(Mat m, void *ctx) {
@@ -198,25 +217,42 @@ inline PetscErrorCode MatMult(Mat m, Vec x, Vec y) { return m->mult ? m->mult(m,
 inline PetscErrorCode MatGetDiagonal(Mat m, Vec d) { return m->diag ? m->diag(m, d) : PETSC_ERR_SUP; }
 inline PetscErrorCode MatMultTranspose(Mat m, Vec x, Vec y) { return m->multT ? m->multT(m, x, y) : PETSC_ERR_SUP; }
 inline PetscErrorCode MatDestroy(Mat *m) {
+  if (*m) delete (*m)->entries;
   delete *m;
   *m = nullptr;
   return 0;
 }
 inline PetscErrorCode MatSetSizes(Mat, PetscInt, PetscInt, PetscInt, PetscInt) { return 0; }
-/* every Mat made here is a shell (MatCreateShell) or an empty stand-in */
-inline PetscErrorCode PetscObjectTypeCompare(PetscObject, const char *type, PetscBool *same) {
-  *same = (PetscBool)(std::strcmp(type, MATSHELL) == 0);
+/* the reference asks this of matrices only */
+inline PetscErrorCode PetscObjectTypeCompare(PetscObject o, const char *type, PetscBool *same) {
+  const dg_shim_mat *m = reinterpret_cast<const dg_shim_mat *>(o);
+  *same = (PetscBool)(m && m->type && std::strcmp(m->type, type) == 0);
   return 0;
 }
-inline PetscErrorCode MatZeroEntries(Mat) { return 0; }
+inline PetscErrorCode MatZeroEntries(Mat m) {
+  if (m->entries) m->entries->clear();
+  return 0;
+}
 inline PetscErrorCode MatCreateVecs(Mat, Vec *, Vec *) { return PETSC_ERR_SUP; }
-inline PetscErrorCode MatSetType(Mat, MatType) { return 0; }
+inline PetscErrorCode MatSetType(Mat m, MatType t) {
+  /* the name may live in the caller's stack: keep a copy */
+  static std::map<std::string, int> names;
+  m->type = names.emplace(t, 0).first->first.c_str();
+  return 0;
+}
 inline PetscErrorCode MatSeqAIJSetPreallocation(Mat, PetscInt, const PetscInt *) { return 0; }
 inline PetscErrorCode MatMPIAIJSetPreallocation(Mat, PetscInt, const PetscInt *, PetscInt, const PetscInt *) {
   return 0;
 }
-inline PetscErrorCode MatSetValues(Mat, PetscInt, const PetscInt *, PetscInt, const PetscInt *,
-                                   const PetscScalar *, InsertMode) {
+/* records the entries (ADD_VALUES adds, INSERT_VALUES overwrites) */
+inline PetscErrorCode MatSetValues(Mat m, PetscInt nr, const PetscInt *rows, PetscInt nc, const PetscInt *cols,
+                                   const PetscScalar *v, InsertMode mode) {
+  if (!m->entries) m->entries = new std::map<std::pair<PetscInt, PetscInt>, PetscScalar>;
+  for (PetscInt i = 0; i < nr; i++)
+    for (PetscInt j = 0; j < nc; j++) {
+      PetscScalar &e = (*m->entries)[std::make_pair(rows[i], cols[j])];
+      e = mode == ADD_VALUES ? e + v[i * nc + j] : v[i * nc + j];
+    }
   return 0;
 }
 inline PetscErrorCode MatZeroRows(Mat, PetscInt, const PetscInt *, PetscScalar, Vec, Vec) { return 0; }

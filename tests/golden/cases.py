@@ -80,6 +80,36 @@ def element_factors(octs: np.ndarray) -> np.ndarray:
     return np.stack([lap, mass], 1)
 
 
+def csr_summary(node_xyz: np.ndarray, rows: np.ndarray, cols: np.ndarray, vals: np.ndarray) -> dict:
+    """Size-independent summary of an assembled matrix given by entries
+    between node indices (duplicates summed): with the nodes in lexicographic
+    order of their coordinates, the entry count, a SHA-256 of the sorted
+    (row, column) pattern, A v for v = hashed_nodal_values, A 1 and the
+    diagonal (assembled-matrix fixtures)."""
+    order = np.lexsort(np.asarray(node_xyz).T[::-1])
+    rank = np.empty(len(order), np.int64)
+    rank[order] = np.arange(len(order))
+    r, c = rank[np.asarray(rows, np.int64)], rank[np.asarray(cols, np.int64)]
+    key = r * len(order) + c
+    u, inv = np.unique(key, return_inverse=True)
+    v = np.zeros(len(u))
+    np.add.at(v, inv, np.asarray(vals, np.float64))
+    ur, uc = u // len(order), u % len(order)
+    x = hashed_nodal_values(np.asarray(node_xyz)[order])
+    av, a1, dg = (np.zeros(len(order)) for _ in range(3))
+    np.add.at(av, ur, v * x[uc])
+    np.add.at(a1, ur, v)
+    np.add.at(dg, ur[ur == uc], v[ur == uc])
+    return {"nnz": np.int64(len(u)), "pattern": sha256_records(np.stack([ur, uc], 1)), "av": av, "a1": a1, "diag": dg}
+
+
+# assembled-matrix fixtures: name -> points
+ASSEMBLE = {
+    "gauss400": lambda: datagen.gaussian(400, 0.5, 0.15, seed=38),
+    "boundary300": lambda: boundary(300, 39),
+}
+
+
 # transfer fixtures: name -> (points, coarsenings before the fine level)
 TRANSFER = {
     "gauss1500": (lambda: datagen.gaussian(1500, 0.5, 0.15, seed=35), 0),

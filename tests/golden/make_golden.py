@@ -31,6 +31,10 @@ outputs next to the inputs:
                   (Jacobian1MatMult / Jacobian1MatGetDiagonal, MassMatMult /
                   MassMatGetDiagonal, Jacobian2MatMult /
                   Jacobian2MatGetDiagonal with cases.element_factors)
+  ref_assemble.npz the reference's assembled matrices on cases.ASSEMBLE
+                  (CreateAndComputeFullJacobian1, ComputeDirichletJacobian and
+                  ComputeJacobian2 with cases.element_factors, through
+                  DA::setValuesInMatrix), as cases.csr_summary
   ref_hilbert.npz the reference's default Hilbert-ordered build
                   (oracle/_ref_hilbert/ref_driver, make ORDER=hilbert):
                   points2Octree, balanceOctree and completeOctree outputs
@@ -304,6 +308,42 @@ def make_mg_ops():
     np.savez_compressed(os.path.join(HERE, "ref_mg_ops.npz"), **out)
 
 
+def read_mat(path):
+    b = open(path, "rb").read()
+    n = int(np.frombuffer(b[:8], np.uint64)[0])
+    rec = np.frombuffer(b[8:], dtype=[("rc", "<u4", (6,)), ("v", "<f8")], count=n)
+    return rec["rc"].copy(), rec["v"].copy()
+
+
+def make_assemble():
+    """The reference's assembled matrices (driver mode assemble) on
+    cases.ASSEMBLE: the node coordinates in lexicographic order and, per
+    matrix, cases.csr_summary of its entries."""
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, fn in cases.ASSEMBLE.items():
+            pf, of, bf, cf = (os.path.join(tmp, f"{name}.{e}") for e in ("pts", "oct", "bal", "coef"))
+            write_pts(pf, fn())
+            run("p2o", pf, 30, 1, of)
+            run("bal", of, 30, 1, 0, bf)
+            bal = read_oct(bf)
+            write_coef(cf, bal, cases.element_factors(bal))
+            prefix = os.path.join(tmp, name)
+            info = run("assemble", bf, 30, os.path.join(REF, "Stencils"), cf, prefix)
+            assert info["missing"] == 0 and info["conflicts"] == 0 and info["unmapped"] == 0, info
+            mats = {m: read_mat(f"{prefix}.{m}") for m in ("k", "kd", "k2")}
+            xyz = np.unique(np.concatenate([rc.reshape(-1, 3) for rc, _ in mats.values()]), axis=0)
+            index = {tuple(p): i for i, p in enumerate(xyz.tolist())}
+            out[f"{name}/bal"] = bal
+            out[f"{name}/node_xyz"] = xyz
+            for m, (rc, v) in mats.items():
+                rows = np.array([index[tuple(p)] for p in rc[:, :3].tolist()])
+                cols = np.array([index[tuple(p)] for p in rc[:, 3:].tolist()])
+                for k, val in cases.csr_summary(xyz, rows, cols, v).items():
+                    out[f"{name}/{m}/{k}"] = val
+    np.savez_compressed(os.path.join(HERE, "ref_assemble.npz"), **out)
+
+
 def make_face_edge():
     """balanceOctree with incCorner = false (faces and edges only) on the
     reference's points2Octree output of every small case whose balance
@@ -369,6 +409,9 @@ def main():
         return
     if "--mg-ops-only" in sys.argv:
         make_mg_ops()
+        return
+    if "--assemble-only" in sys.argv:
+        make_assemble()
         return
     if "--hilbert-only" in sys.argv:
         make_hilbert()
@@ -481,6 +524,7 @@ def main():
     make_hilbert()
     make_mat()
     make_mg_ops()
+    make_assemble()
     make_face_edge()
     make_treesort()
 

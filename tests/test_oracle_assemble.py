@@ -1,12 +1,18 @@
-"""Assembled operators: the oracle's assembly (numpy) against the matrix the
-reference itself assembles (CreateAndComputeFullJacobian1,
+"""Assembled operators: the oracle's assembly (numpy) against the matrices
+the reference itself assembles (CreateAndComputeFullJacobian1,
 examples/src/backend/odaJac.C:470, through its DA and stencil files:
-tests/golden/ref_mat.npz, written by tests/golden/make_golden.py).  The
-pattern must be identical; the values agree to the precision of the
-reference's stencil files (15 decimals).  CPU only."""
+tests/golden/ref_mat.npz; and, called as the reference calls them with
+entries through DA::setValuesInMatrix, CreateAndComputeFullJacobian1,
+ComputeDirichletJacobian and ComputeJacobian2: tests/golden/ref_assemble.npz;
+both written by tests/golden/make_golden.py).  The pattern must be
+identical; the values agree to the precision of the reference's stencil
+files (15 decimals).  CPU only."""
 import os
 
 import numpy as np
+import pytest
+
+from tests.golden import cases
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -57,3 +63,28 @@ def test_oracle_per_element_forms(oracle):
     m = oracle.assemble(da, coef=rc)
     np.testing.assert_allclose(m @ x, oracle.matvec_coef(da, rc, x), rtol=0, atol=1e-13)
     np.testing.assert_allclose(m.diagonal(), oracle.diagonal(da, coef=rc), rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("name", list(cases.ASSEMBLE))
+def test_oracle_matches_reference_assembly_functions(oracle, name):
+    """K + M, the Dirichlet matrix and the per-element-factor matrix of the
+    oracle (which the GPU's CSR assembly is tested against) summarised as the
+    reference's own CreateAndComputeFullJacobian1, ComputeDirichletJacobian
+    (examples/src/backend/omgJac.C:383) and ComputeJacobian2 (omgJac.C:1861)
+    are: the same pattern and entry count, and A v, A 1 and diag(A) to 1e-12
+    of their largest values."""
+    z = np.load(os.path.join(GOLDEN, "ref_assemble.npz"))
+    bal = z[f"{name}/bal"]
+    da = oracle.DA(bal, 30)
+    key = lambda a: np.ascontiguousarray(a, np.uint32).view([("", np.uint32)] * 3).ravel()
+    assert np.array_equal(np.sort(key(da.node_xyz)), key(z[f"{name}/node_xyz"]))
+    mats = {"k": oracle.assemble(da), "kd": oracle.assemble(da, dirichlet=True),
+            "k2": oracle.assemble(da, coef=cases.element_factors(bal))}
+    for m, a in mats.items():
+        c = a.tocoo()
+        got = cases.csr_summary(da.node_xyz, c.row, c.col, c.data)
+        assert int(got["nnz"]) == int(z[f"{name}/{m}/nnz"]), m
+        assert got["pattern"] == str(z[f"{name}/{m}/pattern"]), m
+        for k in ("av", "a1", "diag"):
+            ref = z[f"{name}/{m}/{k}"]
+            assert np.abs(got[k] - ref).max() <= 1e-12 * np.abs(ref).max(), (m, k)
