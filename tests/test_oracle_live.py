@@ -2,7 +2,8 @@
 (CPU only; skipped where oracle/_ref has not been built from the
 reference's sources, as on machines without them): points2Octree and
 balanceOctree bit-exact, completeOctree on inputs the reference completes,
-and the Hilbert order of the reference's Hilbert build."""
+the Hilbert order of the reference's Hilbert build, and the multigrid level
+operators (transfers, Dirichlet operator and diagonal)."""
 import os
 import subprocess
 import tempfile
@@ -88,3 +89,59 @@ def test_hilbert_order_fresh_cloud(oracle):
         assert _run(DRIVER_H, "bal", of, 30, 1, 0, bf, cwd=tmp)
         m = oracle.balance(oracle.points_to_octree(pts, 30, 1), 30)
         assert np.array_equal(_read_oct(bf), oracle.hilbert_sort(m, 30))
+
+
+def _write_vec(path, xyz, v):
+    rec = np.zeros(len(v), dtype=[("c", "<u4", (4,)), ("v", "<f8")])
+    rec["c"][:, :3] = xyz
+    rec["v"] = v
+    with open(path, "wb") as f:
+        f.write(np.uint64(len(v)).tobytes())
+        f.write(rec.tobytes())
+
+
+def _read_vec(path):
+    b = open(path, "rb").read()
+    n = int(np.frombuffer(b[:8], np.uint64)[0])
+    rec = np.frombuffer(b[8:], dtype=[("c", "<u4", (4,)), ("v", "<f8")], count=n)
+    return rec["c"][:, :3].copy(), rec["v"].copy()
+
+
+def _same_by_coords(xyz, got, ref_xyz, ref, tol):
+    mine, theirs = np.lexsort(xyz.T[::-1]), np.lexsort(ref_xyz.T[::-1])
+    assert np.array_equal(xyz[mine], ref_xyz[theirs])
+    assert np.abs(got[mine] - ref[theirs]).max() <= tol * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("seed", [404, 505])
+def test_multigrid_operators_fresh_clouds(oracle, seed):
+    """The reference's restrictMatVecType1 / prolongMatVecType1 and
+    DirichletJacobianMatMult / DirichletJacobianMatGetDiagonal (driver modes
+    transfer and dirichlet) against the oracle's on a fresh mixture cloud."""
+    from types import SimpleNamespace
+
+    from oracle.mg_ref import OracleMG
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pts = datagen.mixture(int(rng.integers(1500, 5000)), rng)
+    fine = oracle.balance(oracle.points_to_octree(pts, 30, 1), 30)
+    coarse = oracle.balance(oracle.coarsen(fine, 30), 30)
+    fda, cda = oracle.DA(fine, 30), oracle.DA(coarse, 30)
+    vf, vc = rng.standard_normal(fda.n_node), rng.standard_normal(cda.n_node)
+    ref_file = os.path.join(os.path.dirname(DRIVER), "REF")  # the source tree the driver was built from
+    stencils = os.path.join(open(ref_file).read().strip(), "Stencils") if os.path.exists(ref_file) else ""
+    if not os.path.isdir(stencils):
+        pytest.skip("reference stencil tables not present")
+    with tempfile.TemporaryDirectory() as tmp:
+        bf, ff, cf, pre = (os.path.join(tmp, n) for n in ("f.oct", "vf", "vc", "out"))
+        _write_oct(bf, fine)
+        _write_vec(ff, fda.node_xyz, vf)
+        _write_vec(cf, cda.node_xyz, vc)
+        assert _run(DRIVER, "transfer", bf, 30, stencils, ff, cf, pre, cwd=tmp)
+        assert np.array_equal(_read_oct(pre + ".coarse"), coarse)
+        two = SimpleNamespace(pmaps=[fda.prolong_map(coarse, cda)], das=[fda, cda])
+        _same_by_coords(cda.node_xyz, OracleMG.restrict(two, 0, vf), *_read_vec(pre + ".r"), 1e-14)
+        _same_by_coords(fda.node_xyz, OracleMG.prolong(two, 0, vc), *_read_vec(pre + ".p"), 1e-14)
+        assert _run(DRIVER, "dirichlet", bf, 30, stencils, ff, pre, cwd=tmp)
+        _same_by_coords(fda.node_xyz, fda.dirichlet_matvec(vf), *_read_vec(pre + ".mv"), 1e-14)
+        _same_by_coords(fda.node_xyz, fda.dirichlet_diag(), *_read_vec(pre + ".diag"), 1e-14)
