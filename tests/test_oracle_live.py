@@ -113,17 +113,19 @@ def _same_by_coords(xyz, got, ref_xyz, ref, tol):
     assert np.abs(got[mine] - ref[theirs]).max() <= tol * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("seed", [404, 505])
+@pytest.mark.parametrize("seed", [404, 505, 0])
 def test_multigrid_operators_fresh_clouds(oracle, seed):
     """The reference's restrictMatVecType1 / prolongMatVecType1 and
     DirichletJacobianMatMult / DirichletJacobianMatGetDiagonal (driver modes
-    transfer and dirichlet) against the oracle's on a fresh mixture cloud."""
+    transfer and dirichlet) against the oracle's on a fresh mixture cloud,
+    and (seed 0) on a 50,000-point log-normal cloud (277k octants, 185k
+    nodes)."""
     from types import SimpleNamespace
 
     from oracle.mg_ref import OracleMG
 
     rng = np.random.Generator(np.random.PCG64(seed))
-    pts = datagen.mixture(int(rng.integers(1500, 5000)), rng)
+    pts = datagen.mixture(int(rng.integers(1500, 5000)), rng) if seed else datagen.lognormal(50_000, seed=41)
     fine = oracle.balance(oracle.points_to_octree(pts, 30, 1), 30)
     coarse = oracle.balance(oracle.coarsen(fine, 30), 30)
     fda, cda = oracle.DA(fine, 30), oracle.DA(coarse, 30)
