@@ -1,6 +1,6 @@
-// Device-wide primitives: exclusive scan, stream compaction, key OR/AND
-// reduction and a stable LSD radix sort of 64- or 128-bit keys that skips
-// the digits on which all keys agree.
+// Device-wide primitives: exclusive scan, stream compaction and a stable
+// LSD radix sort of 64- or 128-bit keys that skips the digits on which all
+// keys agree.
 //
 // Radix sort, per 8-bit digit: (1) per-tile 256-bin histograms (shared
 // atomics), (2) one exclusive scan of the digit-major histogram matrix,
@@ -187,42 +187,6 @@ size_t compact(Context &ctx, const T *in, const uint32_t *flags, size_t n, T *ou
   DG_LAUNCH_CHECK();
     }
   return (size_t)read_scalar(ctx, d_total);
-}
-
-// ------------------------------------------------------------------------
-// OR / AND of all keys (bits that vary across the array = OR ^ AND)
-// ------------------------------------------------------------------------
-template <typename K>
-__global__ void k_key_or_and(const K *__restrict__ keys, size_t n, unsigned long long *orand) {
-  // orand[0..1] = OR (lo, hi), orand[2..3] = AND (lo, hi)
-  uint64_t olo = 0, ohi = 0, alo = ~0ull, ahi = ~0ull;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    K k = keys[i];
-    if constexpr (sizeof(K) == 16) {
-      const Key128 &q = reinterpret_cast<const Key128 &>(k);
-      olo |= q.lo;
-      ohi |= q.hi;
-      alo &= q.lo;
-      ahi &= q.hi;
-    } else {
-      const uint64_t &q = reinterpret_cast<const uint64_t &>(k);
-      olo |= q;
-      alo &= q;
-    }
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    olo |= __shfl_xor_sync(0xffffffffu, olo, o);
-    ohi |= __shfl_xor_sync(0xffffffffu, ohi, o);
-    alo &= __shfl_xor_sync(0xffffffffu, alo, o);
-    ahi &= __shfl_xor_sync(0xffffffffu, ahi, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicOr(&orand[0], (unsigned long long)olo);
-    atomicOr(&orand[1], (unsigned long long)ohi);
-    atomicAnd(&orand[2], (unsigned long long)alo);
-    atomicAnd(&orand[3], (unsigned long long)ahi);
-  }
 }
 
 // ------------------------------------------------------------------------
