@@ -40,6 +40,14 @@ def _is_device(a) -> bool:
     return hasattr(a, "data_ptr") and getattr(a, "is_cuda", False)
 
 
+def _check_len(x, n: int, what: str) -> None:
+    """Host and device vectors must hold exactly n entries: the C ABI takes
+    plain pointers and cannot check their lengths."""
+    m = x.numel() if _is_device(x) else np.asarray(x).size
+    if m != n:
+        raise ValueError(f"{what}: vector of {m} entries where the mesh has {n} nodes")
+
+
 def _ptr(a):
     """Address of an argument.  A CUDA tensor may still be being written by
     torch on torch's current stream, while the library works on its own
@@ -505,6 +513,7 @@ class DA:
             c = np.ascontiguousarray(coef, dtype=np.float64).reshape(-1, 2)
             if c.shape[0] != self.n_elem:
                 raise ValueError("coef must hold 2 values per element")
+        _check_len(x, self.n_node, "Jacobian2MatMult")
         check(self.ctx.handle, self.ctx._L.dg_matvec_coef(self.ctx.handle, self.handle, _ptr(c), _ptr(x), _ptr(out),
                                                           precision, 1 if on_dev else 0), "dg_matvec_coef")
         return out
@@ -639,7 +648,8 @@ class MultiGrid:
         check(self.ctx.handle, self.ctx._L.dg_mg_level_octree(self.ctx.handle, self.handle, level, _ptr(out), 0), "level_octree")
         return out
 
-    def _op(self, fn, level, x, n_out, precision):
+    def _op(self, fn, level, x, n_in, n_out, precision):
+        _check_len(x, n_in, fn.__name__)
         on_dev = 1 if _is_device(x) else 0
         if on_dev:
             out = x.new_empty((n_out,))
@@ -652,15 +662,18 @@ class MultiGrid:
     def matvec(self, level: int, x, precision: int = 64):
         """DirichletJacobianMatMult on a level: FP64 (64), FP32 (32), or FP64
         vectors in double-single arithmetic (48)."""
-        return self._op(self.ctx._L.dg_mg_matvec, level, x, self.sizes[level][1], precision)
+        n = self.sizes[level][1]
+        return self._op(self.ctx._L.dg_mg_matvec, level, x, n, n, precision)
 
     def restrict(self, fine_level: int, x, precision: int = 64):
         """restrictMatVecType1: fine level -> next coarser level."""
-        return self._op(self.ctx._L.dg_mg_restrict, fine_level, x, self.sizes[fine_level + 1][1], precision)
+        return self._op(self.ctx._L.dg_mg_restrict, fine_level, x, self.sizes[fine_level][1],
+                        self.sizes[fine_level + 1][1], precision)
 
     def prolong(self, fine_level: int, x, precision: int = 64):
         """prolongMatVecType1: next coarser level -> fine level."""
-        return self._op(self.ctx._L.dg_mg_prolong, fine_level, x, self.sizes[fine_level][1], precision)
+        return self._op(self.ctx._L.dg_mg_prolong, fine_level, x, self.sizes[fine_level + 1][1],
+                        self.sizes[fine_level][1], precision)
 
     def set_smoother(self, omega: float = 0.667, nu_pre: int = 2, nu_post: int = 2):
         check(self.ctx.handle, self.ctx._L.dg_mg_set_smoother(self.handle, omega, nu_pre, nu_post), "set_smoother")
@@ -674,6 +687,7 @@ class MultiGrid:
 
     def rhs(self, f):
         """Load vector b = M f of a nodal field on the finest level, 0 on the boundary."""
+        _check_len(f, self.sizes[0][1], "rhs")
         on_dev = 1 if _is_device(f) else 0
         if on_dev:
             out = f.new_empty(f.shape)
@@ -688,6 +702,9 @@ class MultiGrid:
 
         Returns (x, iterations, final FP64 relative residual).
         """
+        _check_len(b, self.sizes[0][1], "solve")
+        if x is not None:
+            _check_len(x, self.sizes[0][1], "solve (x)")
         on_dev = 1 if _is_device(b) else 0
         if on_dev:
             x = b.new_empty(b.shape) if x is None else x

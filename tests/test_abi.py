@@ -120,3 +120,43 @@ def test_cpp_mirror_compiles_cleanly():
     subprocess.check_call(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I",
                            os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "dropin_main.cpp")])
 
+
+
+def test_python_mirror_checks_vector_lengths():
+    """The C ABI takes plain pointers, so the Python mirror checks every
+    vector's length before a call: a wrong length raises ValueError and
+    reaches no native code (the objects here hold sizes only)."""
+    from types import SimpleNamespace
+
+    import numpy as np
+
+    from dendro_gb300.api import DA, MultiGrid
+
+    def refuse(*a):
+        raise AssertionError("native code reached")
+
+    L = SimpleNamespace(dg_mg_matvec=refuse, dg_mg_restrict=refuse, dg_mg_prolong=refuse, dg_mg_rhs=refuse,
+                        dg_mg_solve=refuse, dg_matvec_coef=refuse)
+    mg = MultiGrid.__new__(MultiGrid)
+    mg.ctx, mg.handle, mg.sizes = SimpleNamespace(_L=L, handle=None), None, [(10, 8), (3, 5)]
+    for call in (lambda: mg.matvec(0, np.zeros(7)), lambda: mg.matvec(1, np.zeros(8)),
+                 lambda: mg.restrict(0, np.zeros(5)), lambda: mg.prolong(0, np.zeros(8)),
+                 lambda: mg.rhs(np.zeros(5)), lambda: mg.solve(np.zeros(9)),
+                 lambda: mg.solve(np.zeros(8), x=np.zeros(7))):
+        with pytest.raises(ValueError):
+            call()
+    # the right lengths pass the checks and reach the native call
+    for call in (lambda: mg.matvec(0, np.zeros(8)), lambda: mg.matvec(1, np.zeros(5)),
+                 lambda: mg.restrict(0, np.zeros(8)), lambda: mg.prolong(0, np.zeros(5)),
+                 lambda: mg.rhs(np.zeros(8)), lambda: mg.solve(np.zeros(8), x=np.zeros(8))):
+        with pytest.raises(AssertionError, match="native code reached"):
+            call()
+    da = DA.__new__(DA)
+    da.ctx, da.handle, da.n_elem, da.n_node = SimpleNamespace(_L=L, handle=None), None, 2, 6
+    with pytest.raises(AssertionError, match="native code reached"):
+        da.matvec_coef(np.ones((2, 2)), np.zeros(6))
+    with pytest.raises(ValueError):
+        da.matvec_coef(np.ones((2, 2)), np.zeros(5))
+    with pytest.raises(ValueError):
+        da.matvec(np.zeros(5))
+    mg.handle = da.handle = None  # nothing to free
