@@ -448,6 +448,7 @@ class Csr:
 
     def spmv(self, x, out=None):
         """y = A x (FP64); host arrays or CUDA tensors."""
+        _check_len(x, self.n_rows, "dg_csr_spmv")
         on_dev = _is_device(x)
         if on_dev:
             out = x.new_empty(x.shape) if out is None else out
@@ -507,22 +508,29 @@ class DA:
         if on_dev:
             out = x.new_empty(x.shape) if out is None else out
             c = coef
+            if c.numel() != 2 * self.n_elem:
+                raise ValueError("coef must hold 2 values per element")
         else:
             x = np.ascontiguousarray(x, dtype=np.float64 if precision == 64 else np.float32)
             out = np.empty_like(x) if out is None else out
-            c = np.ascontiguousarray(coef, dtype=np.float64).reshape(-1, 2)
-            if c.shape[0] != self.n_elem:
-                raise ValueError("coef must hold 2 values per element")
+            c = self._coef(coef)
         _check_len(x, self.n_node, "Jacobian2MatMult")
         check(self.ctx.handle, self.ctx._L.dg_matvec_coef(self.ctx.handle, self.handle, _ptr(c), _ptr(x), _ptr(out),
                                                           precision, 1 if on_dev else 0), "dg_matvec_coef")
         return out
 
+    def _coef(self, coef) -> np.ndarray:
+        """Per-element (lap, mass) factors as an n_elem x 2 FP64 host array."""
+        c = np.ascontiguousarray(coef, dtype=np.float64).reshape(-1, 2)
+        if c.shape[0] != self.n_elem:
+            raise ValueError("coef must hold 2 values per element")
+        return c
+
     def diagonal(self, lapFac: float = 1.0, massFac: float = 1.0, coef=None) -> np.ndarray:
         """Jacobian1MatGetDiagonal (odaJac.C:160-222), or with coef
         Jacobian2MatGetDiagonal (omgJac.C:1641); FP64, host array."""
         d = np.empty(max(self.n_node, 1), np.float64)
-        c = None if coef is None else np.ascontiguousarray(coef, dtype=np.float64).reshape(-1, 2)
+        c = None if coef is None else self._coef(coef)
         check(self.ctx.handle, self.ctx._L.dg_da_diagonal(self.ctx.handle, self.handle, None if c is None else _ptr(c),
                                                           lapFac, massFac, _ptr(d), 0), "dg_da_diagonal")
         return d[: self.n_node]
@@ -530,7 +538,7 @@ class DA:
     def assemble_coef(self, coef) -> "Csr":
         """BUILD_FULL_JAC_TYPE2_BLOCK (omgJac.C:1804-1858): the per-element
         operator of matvec_coef as a CSR matrix."""
-        c = np.ascontiguousarray(coef, dtype=np.float64).reshape(-1, 2)
+        c = self._coef(coef)
         h = ctypes.c_void_p()
         check(self.ctx.handle, self.ctx._L.dg_da_assemble_coef(self.ctx.handle, self.handle, _ptr(c), 0, ctypes.byref(h)),
               "dg_da_assemble_coef")

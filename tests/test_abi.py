@@ -159,4 +159,16 @@ def test_python_mirror_checks_vector_lengths():
         da.matvec_coef(np.ones((2, 2)), np.zeros(5))
     with pytest.raises(ValueError):
         da.matvec(np.zeros(5))
+    for call in (lambda: da.matvec_coef(np.ones((3, 2)), np.zeros(6)), lambda: da.diagonal(coef=np.ones(2)),
+                 lambda: da.assemble_coef(np.ones((1, 2)))):
+        with pytest.raises(ValueError):
+            call()
+    from dendro_gb300.api import Csr
+
+    m = Csr.__new__(Csr)
+    m.ctx, m.handle, m.n_rows = SimpleNamespace(_L=SimpleNamespace(dg_csr_spmv=refuse), handle=None), None, 4
+    with pytest.raises(ValueError):
+        m.spmv(np.zeros(3))
+    with pytest.raises(AssertionError, match="native code reached"):
+        m.spmv(np.zeros(4))
     mg.handle = da.handle = None  # nothing to free
