@@ -356,10 +356,12 @@ class DA {
   }
   void matVec(const std::vector<double> &in, std::vector<double> &out, double lapFac = 1.0,
               double massFac = 1.0) const {
+    if (in.size() != nn_) throw cxx::Error(DG_ERR_INVALID_ARG, "Jacobian1MatMult: vector length != node count");
     out.resize(nn_);
     matVec(in.data(), out.data(), lapFac, massFac);
   }
   void matVec(const std::vector<float> &in, std::vector<float> &out, double lapFac = 1.0, double massFac = 1.0) const {
+    if (in.size() != nn_) throw cxx::Error(DG_ERR_INVALID_ARG, "Jacobian1MatMult: vector length != node count");
     out.resize(nn_);
     cxx::check(c_, dg_matvec(c_, da_, in.data(), out.data(), 32, lapFac, massFac, 0), "Jacobian1MatMult");
   }
@@ -367,6 +369,7 @@ class DA {
   // of element e in octree order (Jacobian2MatMult)
   void matVec(const std::vector<double> &matProp, const std::vector<double> &in, std::vector<double> &out) const {
     if (matProp.size() != 2 * ne_) throw cxx::Error(DG_ERR_INVALID_ARG, "matProp must hold 2 values per element");
+    if (in.size() != nn_) throw cxx::Error(DG_ERR_INVALID_ARG, "Jacobian2MatMult: vector length != node count");
     out.resize(nn_);
     cxx::check(c_, dg_matvec_coef(c_, da_, matProp.data(), in.data(), out.data(), 64, 0), "Jacobian2MatMult");
   }
